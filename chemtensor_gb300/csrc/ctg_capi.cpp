@@ -1,0 +1,169 @@
+// ctg_capi.cpp - extern "C" boundary (include/ctgpu.h).
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include "ctgpu.h"
+#include "ctg_dmrg.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+thread_local ctg::DmrgOptions g_opts = [] {
+	ctg::DmrgOptions o;
+	if (const char* p = std::getenv("CTGPU_PRECISION")) o.precision = std::atoi(p);
+	if (const char* d = std::getenv("CTGPU_DEVICE")) o.device = std::atoi(d);
+	return o;
+}();
+thread_local ctg::DmrgStats g_stats;
+
+constexpr int ERR_RUNTIME = -5;
+
+template <class F>
+int guarded(F&& f)
+{
+	try
+	{
+		g_last_error.clear();
+		return f();
+	}
+	catch (const std::exception& e)
+	{
+		g_last_error = e.what();
+		fprintf(stderr, "ctgpu: %s\n", e.what());
+		return ERR_RUNTIME;
+	}
+}
+
+}  // namespace
+
+extern "C" {
+
+int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int maxiter_lanczos, const double tol_split,
+                 const ct_long max_vdim, struct mps* psi, double* en_sweeps, double* entropy)
+{
+	return guarded([&] {
+		CTG_CHECK(hamiltonian && psi && en_sweeps && entropy, "null argument");
+		CTG_CHECK(tol_split >= 0, "tol_split must be non-negative");
+		CTG_CHECK(max_vdim > 0, "max_vdim must be positive");
+		return ctg::dmrg_twosite_gpu(hamiltonian, num_sweeps, maxiter_lanczos, tol_split, max_vdim, psi, en_sweeps, entropy,
+		                             g_opts, &g_stats);
+	});
+}
+
+int ctgpu_set_precision(int precision)
+{
+	const int old = g_opts.precision;
+	if (precision >= ctg::GEMM_FP64 && precision <= ctg::GEMM_TF32) g_opts.precision = precision;
+	return old;
+}
+
+int ctgpu_set_device(int device)
+{
+	const int old = g_opts.device;
+	g_opts.device = device;
+	return old;
+}
+
+int ctgpu_get_last_stats(struct ctgpu_stats* out)
+{
+	if (!out) return -1;
+	const ctg::DmrgStats& s = g_stats;
+	out->wall_s = s.wall_s;
+	out->upload_s = s.upload_s;
+	out->download_s = s.download_s;
+	out->setup_s = s.setup_s;
+	out->sweep_s = s.sweep_s;
+	out->lanczos_ms = s.lanczos_ms;
+	out->split_ms = s.split_ms;
+	out->env_ms = s.env_ms;
+	out->matvec_flops = s.matvec_flops;
+	out->total_gemm_flops = s.total_gemm_flops;
+	out->matvecs = s.matvecs;
+	out->kernel_launches = s.kernel_launches;
+	out->sweeps = s.sweeps;
+	out->max_bond_dim = s.max_bond_dim;
+	return 0;
+}
+
+const char* ctgpu_last_error(void) { return g_last_error.c_str(); }
+
+int ctgpu_block_sparse_tensor_dot(const struct block_sparse_tensor* s, int axrange_s, const struct block_sparse_tensor* t,
+                                  int axrange_t, int ndim_mult, struct block_sparse_tensor* r)
+{
+	return guarded([&] {
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor ds = ctg::tensor_from_struct(c, s), dt = ctg::tensor_from_struct(c, t);
+		ctg::DTensor dr = ctg::op_dot(c, ds, axrange_s, dt, axrange_t, ndim_mult);
+		ctg::tensor_to_struct(c, dr, r);
+		return 0;
+	});
+}
+
+int ctgpu_block_sparse_tensor_transpose(const int* perm, const struct block_sparse_tensor* t, struct block_sparse_tensor* r)
+{
+	return guarded([&] {
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor dt = ctg::tensor_from_struct(c, t);
+		ctg::DTensor dr = ctg::op_transpose(c, dt, perm);
+		ctg::tensor_to_struct(c, dr, r);
+		return 0;
+	});
+}
+
+int ctgpu_apply_local_hamiltonian(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
+                                  const struct block_sparse_tensor* l, const struct block_sparse_tensor* r,
+                                  struct block_sparse_tensor* b)
+{
+	return guarded([&] {
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor da = ctg::tensor_from_struct(c, a), dw = ctg::tensor_from_struct(c, w);
+		ctg::DTensor dl = ctg::tensor_from_struct(c, l), dr = ctg::tensor_from_struct(c, r);
+		ctg::DTensor out = ctg::apply_local_hamiltonian_once(c, da, dw, dl, dr, g_opts.precision);
+		ctg::tensor_to_struct(c, out, b);
+		return 0;
+	});
+}
+
+int ctgpu_contraction_operator_step_left(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
+                                         const struct block_sparse_tensor* l, struct block_sparse_tensor* l_next)
+{
+	return guarded([&] {
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor da = ctg::tensor_from_struct(c, a), dw = ctg::tensor_from_struct(c, w), dl = ctg::tensor_from_struct(c, l);
+		ctg::tensor_to_struct(c, ctg::contraction_step_left(c, da, dw, dl), l_next);
+		return 0;
+	});
+}
+
+int ctgpu_contraction_operator_step_right(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
+                                          const struct block_sparse_tensor* r, struct block_sparse_tensor* r_next)
+{
+	return guarded([&] {
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor da = ctg::tensor_from_struct(c, a), dw = ctg::tensor_from_struct(c, w), dr = ctg::tensor_from_struct(c, r);
+		ctg::tensor_to_struct(c, ctg::contraction_step_right(c, da, dw, dr), r_next);
+		return 0;
+	});
+}
+
+int ctgpu_block_sparse_tensor_svd_values(const struct block_sparse_tensor* a, double* sigma, ct_long* ns)
+{
+	return guarded([&] {
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor da = ctg::tensor_from_struct(c, a);
+		ctg::SvdResult sv;
+		const int ret = ctg::op_svd(c, da, sv);
+		if (ret < 0) return ret;
+		CTG_CUDA(cudaMemcpy(sigma, sv.s->ptr, (size_t)sv.ns * sizeof(double), cudaMemcpyDeviceToHost));
+		*ns = sv.ns;
+		return 0;
+	});
+}
+
+void ctgpu_delete_block_sparse_tensor(struct block_sparse_tensor* t)
+{
+	if (t) ctg::free_struct(t);
+}
+
+}  // extern "C"

@@ -1,0 +1,45 @@
+// ctg_common.h - shared definitions for the GB300 two-site DMRG engine.
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace ctg {
+
+using i64 = int64_t;
+using q32 = int32_t;
+
+struct CudaError : std::runtime_error {
+	using std::runtime_error::runtime_error;
+};
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char* what, const char* file, int line);
+
+#define CTG_CUDA(call)                                                              \
+	do {                                                                            \
+		cudaError_t ctg_e_ = (call);                                                \
+		if (ctg_e_ != cudaSuccess) ::ctg::throw_cuda(ctg_e_, #call, __FILE__, __LINE__); \
+	} while (0)
+
+#define CTG_CHECK(cond, msg)                                                        \
+	do {                                                                            \
+		if (!(cond)) throw std::runtime_error(std::string("ctgpu: ") + (msg));       \
+	} while (0)
+
+// Axis range selector of block_sparse_tensor_dot (include/tensor/dense_tensor.h,
+// TENSOR_AXIS_RANGE_LEADING = 0, TENSOR_AXIS_RANGE_TRAILING = 1).
+enum AxRange { AX_LEADING = 0, AX_TRAILING = 1 };
+
+// Arithmetic used for the bulk block GEMMs.
+enum GemmPrecision {
+	GEMM_FP64 = 0,        // plain IEEE double on the FP64 pipe
+	GEMM_BF16X3 = 1,      // split-BF16, 3 products, FP32 accumulation on tcgen05
+	GEMM_TF32 = 2,        // TF32 on tcgen05, FP32 accumulation
+};
+
+}  // namespace ctg

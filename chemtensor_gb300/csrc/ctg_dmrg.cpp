@@ -1,0 +1,579 @@
+// ctg_dmrg.cpp - two-site DMRG driver on the device engine.
+//
+// Control flow follows dmrg_twosite (src/algorithm/dmrg.c:262-399): right
+// normalisation, right environments, merged MPO pairs, then sweeps of
+// merge -> Lanczos -> SVD split -> environment update. All tensors stay in
+// HBM for the whole call; the host only handles block structure (integers)
+// and, once per bond, the singular values that decide the truncation.
+#include "ctg_dmrg.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+
+namespace ctg {
+
+namespace {
+
+double now_s()
+{
+	return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void* ct_alloc(size_t n)
+{
+	// the reference's ct_malloc contract (include/aligned_memory.h:17-29)
+	void* p = aligned_alloc(16, std::max<size_t>(16, (n + 15) & ~(size_t)15));
+	if (!p) throw std::bad_alloc();
+	return p;
+}
+
+template <class T>
+T* ct_copy(const T* src, size_t n)
+{
+	T* p = (T*)ct_alloc(n * sizeof(T));
+	if (n) memcpy(p, src, n * sizeof(T));
+	return p;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// boundary conversions
+// ------------------------------------------------------------------------------------
+
+Meta meta_from_struct(const struct block_sparse_tensor* t)
+{
+	CTG_CHECK(t->ndim >= 1, "tensor of degree 0 at the boundary");
+	CTG_CHECK(t->dtype == CT_DOUBLE_REAL, "only double precision real tensors are supported");
+	std::vector<i64> dim(t->dim_logical, t->dim_logical + t->ndim);
+	std::vector<int> dir(t->ndim);
+	std::vector<std::vector<q32>> ql(t->ndim);
+	for (int i = 0; i < t->ndim; i++)
+	{
+		dir[i] = (int)t->axis_dir[i];
+		ql[i].assign(t->qnums_logical[i], t->qnums_logical[i] + dim[i]);
+	}
+	Meta m = make_meta(t->ndim, dim.data(), dir.data(), ql);
+	for (int i = 0; i < t->ndim; i++)
+	{
+		CTG_CHECK(t->dim_blocks[i] == m.nb[i], "block dimensions differ from the structure rule");
+		for (i64 j = 0; j < m.nb[i]; j++)
+			CTG_CHECK(t->qnums_blocks[i][j] == m.qb[i][(size_t)j], "block quantum numbers differ from the structure rule");
+	}
+	return m;
+}
+
+DTensor tensor_from_struct(Ctx& c, const struct block_sparse_tensor* t)
+{
+	Meta m = meta_from_struct(t);
+	std::vector<double> host((size_t)std::max<i64>(m.nnz, 1));
+	for (int b = 0; b < m.nblocks; b++)
+	{
+		const struct dense_tensor* bl = t->blocks[m.linear(m.index(b))];
+		CTG_CHECK(bl != nullptr, "missing dense block in the input tensor");
+		for (int i = 0; i < m.ndim; i++) CTG_CHECK(bl->dim[i] == m.dims(b)[i], "dense block shape mismatch");
+		memcpy(host.data() + m.boff[b], bl->data, (size_t)m.block_size(b) * sizeof(double));
+	}
+	DTensor d;
+	d.meta = std::make_shared<const Meta>(std::move(m));
+	d.buf = c.upload(host.data(), host.size() * sizeof(double));
+	return d;
+}
+
+void tensor_to_struct(Ctx& c, const DTensor& t, struct block_sparse_tensor* out)
+{
+	std::vector<double> host((size_t)std::max<i64>(t.m().nnz, 1));
+	copy_to_host(c, t, host.data());
+	write_struct_host(t.m(), host.data(), out);
+}
+
+void write_struct_host(const Meta& m, const double* host, struct block_sparse_tensor* out)
+{
+	out->dtype = CT_DOUBLE_REAL;
+	out->ndim = m.ndim;
+	out->dim_logical = ct_copy(m.dim.data(), (size_t)m.ndim);
+	out->dim_blocks = ct_copy(m.nb.data(), (size_t)m.ndim);
+	out->axis_dir = (enum tensor_axis_direction*)ct_alloc(m.ndim * sizeof(enum tensor_axis_direction));
+	for (int i = 0; i < m.ndim; i++) out->axis_dir[i] = (enum tensor_axis_direction)m.dir[i];
+	out->qnums_logical = (qnumber**)ct_alloc(m.ndim * sizeof(qnumber*));
+	out->qnums_blocks = (qnumber**)ct_alloc(m.ndim * sizeof(qnumber*));
+	for (int i = 0; i < m.ndim; i++)
+	{
+		out->qnums_logical[i] = ct_copy(m.ql[i].data(), m.ql[i].size());
+		out->qnums_blocks[i] = ct_copy(m.qb[i].data(), m.qb[i].size());
+	}
+	i64 total = 1;
+	for (int i = 0; i < m.ndim; i++) total *= m.nb[i];
+	out->blocks = (struct dense_tensor**)ct_alloc((size_t)total * sizeof(struct dense_tensor*));
+	memset(out->blocks, 0, (size_t)total * sizeof(struct dense_tensor*));
+	for (int b = 0; b < m.nblocks; b++)
+	{
+		struct dense_tensor* d = (struct dense_tensor*)ct_alloc(sizeof(struct dense_tensor));
+		d->dtype = CT_DOUBLE_REAL;
+		d->ndim = m.ndim;
+		d->dim = ct_copy(m.dims(b), (size_t)m.ndim);
+		d->data = ct_copy(host + m.boff[b], (size_t)m.block_size(b));
+		out->blocks[m.linear(m.index(b))] = d;
+	}
+}
+
+void free_struct(struct block_sparse_tensor* t)
+{
+	// delete_block_sparse_tensor (src/tensor/block_sparse_tensor.c:168-205)
+	if (!t->blocks) return;
+	i64 total = 1;
+	for (int i = 0; i < t->ndim; i++) total *= t->dim_blocks[i];
+	for (i64 k = 0; k < total; k++)
+	{
+		if (!t->blocks[k]) continue;
+		free(t->blocks[k]->data);
+		free(t->blocks[k]->dim);
+		free(t->blocks[k]);
+	}
+	free(t->blocks);
+	for (int i = 0; i < t->ndim; i++)
+	{
+		free(t->qnums_blocks[i]);
+		free(t->qnums_logical[i]);
+	}
+	free(t->qnums_blocks);
+	free(t->qnums_logical);
+	free(t->axis_dir);
+	free(t->dim_blocks);
+	free(t->dim_logical);
+	t->blocks = nullptr;
+}
+
+// ------------------------------------------------------------------------------------
+// truncation (src/algorithm/truncation.c:110-223, von_neumann_entropy :13-31)
+// ------------------------------------------------------------------------------------
+
+TruncResult retained_bond_indices(const double* sigma, i64 n, double tol, bool relative_thresh, i64 max_vdim)
+{
+	TruncResult res;
+	res.tol_eff = tol;
+	// ascending by value; equal values in index order
+	std::vector<std::pair<double, i64>> ss((size_t)n);
+	for (i64 i = 0; i < n; i++) ss[(size_t)i] = {sigma[i], i};
+	std::stable_sort(ss.begin(), ss.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+	double sqsum = 0;
+	for (auto& p : ss) { p.first = p.first * p.first; sqsum += p.first; }
+	if (sqsum == 0) return res;
+	if (relative_thresh)
+		for (auto& p : ss) p.first /= sqsum;
+	for (size_t i = 1; i < ss.size(); i++) ss[i].first += ss[i - 1].first;
+	if (max_vdim < n)
+	{
+		res.tol_eff = std::fmax(tol, ss[(size_t)(n - max_vdim - 1)].first);
+		for (i64 i = 0; i < n - max_vdim; i++) ss[(size_t)i].first = 0;
+	}
+	std::vector<double> accum((size_t)n);
+	for (const auto& p : ss) accum[(size_t)p.second] = p.first;
+	for (i64 i = 0; i < n; i++)
+		if (accum[(size_t)i] > tol) res.ind.push_back(i);
+	if (res.ind.empty()) return res;
+	double nrm2 = 0;
+	for (i64 i : res.ind) nrm2 += sigma[i] * sigma[i];
+	res.norm_sigma = std::sqrt(nrm2);
+	double s = 0;
+	for (i64 i : res.ind)
+	{
+		const double x = sigma[i] / res.norm_sigma;
+		if (x > 0) s -= x * x * std::log(x * x);
+	}
+	res.entropy = s;
+	return res;
+}
+
+// ------------------------------------------------------------------------------------
+// chain operations on device tensors
+// ------------------------------------------------------------------------------------
+
+namespace {
+
+// mps_merge_tensor_pair (src/state/mps.c:1166-1178)
+DTensor merge_mps_pair(Ctx& c, const DTensor& a0, const DTensor& a1)
+{
+	DTensor t = op_dot(c, a0, AX_TRAILING, a1, AX_LEADING, 1);
+	return op_flatten(c, t, 1, TENSOR_AXIS_OUT);
+}
+
+// mpo_merge_tensor_pair (src/operator/mpo.c:255-279)
+DTensor merge_mpo_pair(Ctx& c, const DTensor& w0, const DTensor& w1)
+{
+	DTensor t = op_dot(c, w0, AX_TRAILING, w1, AX_LEADING, 1);
+	const int perm[6] = {0, 1, 3, 2, 4, 5};
+	DTensor p = op_transpose(c, t, perm);
+	DTensor f = op_flatten(c, p, 1, TENSOR_AXIS_OUT);
+	return op_flatten(c, f, 2, TENSOR_AXIS_IN);
+}
+
+}  // namespace
+
+// contraction_operator_step_left (src/algorithm/chain_ops.c:196-245), with b = a
+DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l)
+{
+	DTensor br = view_reversed(a);
+	DTensor s = op_dot(c, l, AX_TRAILING, br, AX_LEADING, 1);
+	const int p0[5] = {0, 1, 4, 2, 3};
+	DTensor t = op_transpose(c, s, p0);
+	s = op_dot(c, t, AX_TRAILING, w, AX_LEADING, 2);
+	const int p1[5] = {1, 3, 4, 2, 0};
+	t = op_transpose(c, s, p1);
+	s = op_dot(c, a, AX_LEADING, t, AX_LEADING, 2);
+	const int p2[4] = {3, 0, 1, 2};
+	return op_transpose(c, s, p2);
+}
+
+// contraction_operator_step_right (src/algorithm/chain_ops.c:116-165), with b = a
+DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& r)
+{
+	DTensor s = op_dot(c, a, AX_TRAILING, r, AX_LEADING, 1);
+	const int p0[5] = {1, 2, 0, 3, 4};
+	DTensor t = op_transpose(c, s, p0);
+	s = op_dot(c, w, AX_TRAILING, t, AX_LEADING, 2);
+	const int p1[5] = {4, 2, 0, 1, 3};
+	t = op_transpose(c, s, p1);
+	DTensor br = view_reversed(a);
+	s = op_dot(c, t, AX_TRAILING, br, AX_TRAILING, 2);
+	const int p2[4] = {1, 2, 3, 0};
+	return op_transpose(c, s, p2);
+}
+
+namespace {
+
+// create_dummy_operator_block_right / _left (src/algorithm/chain_ops.c:14-85)
+DTensor dummy_block(Ctx& c, const std::vector<q32>& qa, const std::vector<q32>& qw, const std::vector<q32>& qb, bool right)
+{
+	const i64 dim[6] = {1, 1, 1, 1, 1, 1};
+	const int dir[6] = {TENSOR_AXIS_OUT, TENSOR_AXIS_OUT, TENSOR_AXIS_IN, TENSOR_AXIS_IN, TENSOR_AXIS_IN, TENSOR_AXIS_OUT};
+	Meta m = make_meta(6, dim, dir, {qa, qw, qb, qa, qw, qb});
+	CTG_CHECK(m.nblocks == 1, "dummy operator block: unexpected structure");
+	const double one = 1.0;
+	DTensor s;
+	s.meta = std::make_shared<const Meta>(std::move(m));
+	s.buf = c.upload(&one, sizeof(double));
+	if (right)
+	{
+		DTensor t = op_flatten(c, s, 4, TENSOR_AXIS_IN);
+		return op_flatten(c, t, 3, TENSOR_AXIS_IN);
+	}
+	DTensor t = op_flatten(c, s, 0, TENSOR_AXIS_OUT);
+	return op_flatten(c, t, 0, TENSOR_AXIS_OUT);
+}
+
+// mps_local_orthonormalize_rq (src/state/mps.c:560-600)
+int local_orthonormalize_rq(Ctx& c, DTensor& a, DTensor& a_prev)
+{
+	const Meta& am = a.m();
+	const i64 dr[2] = {am.dim[1], am.dim[2]};
+	const std::vector<q32> qr[2] = {am.ql[1], am.ql[2]};
+	const int adr[2] = {TENSOR_AXIS_OUT, TENSOR_AXIS_IN};
+	DTensor mat = op_flatten(c, a, 1, TENSOR_AXIS_IN);
+	DTensor r, q;
+	const int ret = op_rq(c, mat, r, q);
+	a = op_split(c, q, 1, dr, adr, qr);
+	a_prev = op_dot(c, a_prev, AX_TRAILING, r, AX_LEADING, 1);
+	return ret;
+}
+
+DTensor head_tensor(Ctx& c, const DTensor& a0, double value)
+{
+	const i64 dim[3] = {a0.m().dim[0], 1, a0.m().dim[0]};
+	const int dir[3] = {TENSOR_AXIS_OUT, TENSOR_AXIS_OUT, TENSOR_AXIS_IN};
+	Meta m = make_meta(3, dim, dir, {a0.m().ql[0], std::vector<q32>{0}, a0.m().ql[0]});
+	DTensor h = c.zeros(m);
+	if (value != 0 && m.nblocks > 0)
+	{
+		std::vector<double> v((size_t)m.nnz, 0.0);
+		v[0] = value;
+		h.buf = c.upload(v.data(), v.size() * sizeof(double));
+	}
+	return h;
+}
+
+// mps_split_tensor_svd (src/state/mps.c:1119-1159) -> split_block_sparse_matrix_svd (bond_ops.c:15-138)
+int split_mps_svd(Ctx& c, const DTensor& a, i64 d, const std::vector<q32>& qsite, double tol, i64 max_vdim, bool distr_left,
+                  DTensor& a0, DTensor& a1, double* entropy)
+{
+	const i64 dd[2] = {d, d};
+	const int od[2] = {TENSOR_AXIS_OUT, TENSOR_AXIS_OUT};
+	const std::vector<q32> qq[2] = {qsite, qsite};
+	DTensor a4 = op_split(c, a, 1, dd, od, qq);
+	DTensor tmp = op_flatten(c, a4, 0, TENSOR_AXIS_OUT);
+	DTensor am = op_flatten(c, tmp, 1, TENSOR_AXIS_IN);
+	SvdResult sv;
+	int ret = op_svd(c, am, sv);    // synchronises
+	if (ret < 0) return ret;
+	std::vector<double> sigma((size_t)sv.ns);
+	CTG_CUDA(cudaMemcpy(sigma.data(), sv.s->ptr, sigma.size() * sizeof(double), cudaMemcpyDeviceToHost));
+	TruncResult tr = retained_bond_indices(sigma.data(), sv.ns, tol, true, max_vdim);
+	std::vector<double> sret;
+	if (tr.ind.empty())
+	{
+		tr.ind = {0};
+		sret = {0.0};
+		tr.entropy = 0;
+	}
+	else
+	{
+		for (i64 i : tr.ind) sret.push_back(sigma[(size_t)i]);
+	}
+	*entropy = tr.entropy;
+	DTensor m0 = op_slice(c, sv.u, 1, tr.ind);
+	DTensor m1 = op_slice(c, sv.vh, 0, tr.ind);
+	DBufPtr dsv = c.upload(sret.data(), sret.size() * sizeof(double));
+	if (distr_left) m0 = op_scale_axis(c, m0, (const double*)dsv->ptr, AX_TRAILING);
+	else m1 = op_scale_axis(c, m1, (const double*)dsv->ptr, AX_LEADING);
+	const Meta& m4 = a4.m();
+	const i64 d01[2] = {m4.dim[0], m4.dim[1]};
+	const int r01[2] = {m4.dir[0], m4.dir[1]};
+	const std::vector<q32> q01[2] = {m4.ql[0], m4.ql[1]};
+	const i64 d23[2] = {m4.dim[2], m4.dim[3]};
+	const int r23[2] = {m4.dir[2], m4.dir[3]};
+	const std::vector<q32> q23[2] = {m4.ql[2], m4.ql[3]};
+	a0 = op_split(c, m0, 0, d01, r01, q01);
+	a1 = op_split(c, m1, 1, d23, r23, q23);
+	return 0;
+}
+
+// ------------------------------------------------------------------------------------
+// local Hamiltonian (apply_local_hamiltonian, src/algorithm/chain_ops.c:353-390) as a
+// reusable plan: the block structure is fixed for all Lanczos iterations of one bond
+// ------------------------------------------------------------------------------------
+
+struct LocalH {
+	DotPlan d1, d2, d3;
+	CopyPlan t0, t1;
+	DTensor k;                       // transpose(l, {0,3,1,2}), computed once per bond
+	DTensor w, r;
+	DBufPtr s1, tt1, s2, tt2;
+	double flops = 0;
+
+	LocalH(Ctx& c, const Meta& a, const DTensor& w_, const DTensor& l, const DTensor& r_) : w(w_), r(r_)
+	{
+		d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1);
+		const int p0[5] = {1, 2, 0, 3, 4};
+		t0 = make_transpose_plan(c, *d1.out, p0);
+		d2 = make_dot_plan(c, w.m(), AX_TRAILING, *t0.out, AX_LEADING, 2);
+		const int p1[5] = {2, 0, 1, 3, 4};
+		t1 = make_transpose_plan(c, *d2.out, p1);
+		const int p2[4] = {0, 3, 1, 2};
+		k = op_transpose(c, l, p2);
+		d3 = make_dot_plan(c, k.m(), AX_TRAILING, *t1.out, AX_LEADING, 2);
+		// the cyclic partial trace of the unit outer bonds keeps blocks and entries (view_trace_unit)
+		const Meta& o = *d3.out;
+		std::vector<std::vector<q32>> ql(o.ql.begin() + 1, o.ql.end() - 1);
+		Meta tr = make_meta(o.ndim - 2, o.dim.data() + 1, o.dir.data() + 1, ql);
+		CTG_CHECK(tr.same_structure(a) && tr.nnz == a.nnz && tr.nblocks == a.nblocks && o.nnz == a.nnz,
+		          "local Hamiltonian output structure differs from the input");
+		s1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
+		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t0.out->nnz, 1) * sizeof(double));
+		s2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
+		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t1.out->nnz, 1) * sizeof(double));
+		flops = d1.flops + d2.flops + d3.flops;
+	}
+
+	void apply(Ctx& c, const double* x, double* y) const
+	{
+		d1.run(c, x, r.data(), (double*)s1->ptr);
+		t0.run(c, (const double*)s1->ptr, (double*)tt1->ptr);
+		d2.run(c, w.data(), (const double*)tt1->ptr, (double*)s2->ptr);
+		t1.run(c, (const double*)s2->ptr, (double*)tt2->ptr);
+		d3.run(c, k.data(), (const double*)tt2->ptr, y);
+	}
+};
+
+// minimize_local_energy (src/algorithm/dmrg.c:86-147) with lanczos_iteration_d and
+// eigensystem_krylov_symmetric (src/util/krylov.c:24-89, :172-251) on the device
+int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTensor& r, const DTensor& a_start, int maxiter,
+                          LanczosScalars* d_sc, DTensor& a_opt, DmrgStats* st)
+{
+	LocalH h(c, a_start.m(), w, l, r);
+	const i64 n = a_start.m().nnz;
+	DBuf V(&c, (size_t)maxiter * n * sizeof(double));
+	DBuf wv(&c, (size_t)n * sizeof(double));
+	DBuf partial(&c, RED_BLOCKS * sizeof(double));
+	double* Vp = (double*)V.ptr;
+	double* wp = (double*)wv.ptr;
+	double* pp = (double*)partial.ptr;
+	cudaStream_t s = c.stream();
+	launch_lz_normalize_start(a_start.data(), Vp, n, pp, d_sc, s);
+	for (int j = 0; j < maxiter; j++)
+	{
+		h.apply(c, Vp + (i64)j * n, wp);
+		launch_lz_alpha(wp, Vp + (i64)j * n, n, j, pp, d_sc, s);
+		if (j < maxiter - 1)
+		{
+			launch_lz_orth_beta(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, n, j, pp, d_sc, s);
+			launch_lz_next(wp, Vp + (i64)(j + 1) * n, n, j, d_sc, s);
+		}
+	}
+	launch_lz_tridiag(maxiter, d_sc, s);
+	a_opt = c.empty(a_start.m());
+	launch_lz_ritz(Vp, n, maxiter, d_sc, a_opt.data(), s);
+	c.kernel_launches += 4L * maxiter + 5;
+	if (st)
+	{
+		st->matvecs += maxiter;
+		st->matvec_flops += h.flops * maxiter;
+	}
+	return 0;
+}
+
+}  // namespace
+
+DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,
+                                     int precision)
+{
+	(void)precision;
+	LocalH h(c, a.m(), w, l, r);
+	DTensor out = c.empty(a.m());
+	h.apply(c, a.data(), out.data());
+	return out;
+}
+
+// ------------------------------------------------------------------------------------
+// dmrg_twosite
+// ------------------------------------------------------------------------------------
+
+int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double tol_split, i64 max_vdim, struct mps* psi,
+                     double* en_sweeps, double* entropy, const DmrgOptions& opt, DmrgStats* stats)
+{
+	const double t_start = now_s();
+	DmrgStats local;
+	DmrgStats* st = stats ? stats : &local;
+	*st = DmrgStats();
+	const int L = H->nsites;
+	CTG_CHECK(L >= 2 && psi->nsites == L, "dmrg_twosite: need nsites >= 2 and matching MPO / MPS lengths");
+	CTG_CHECK(psi->d == H->d, "dmrg_twosite: physical dimensions of MPO and MPS differ");
+	CTG_CHECK(maxiter >= 1 && maxiter <= LANCZOS_MAX, "dmrg_twosite: maxiter_lanczos out of the supported range");
+	CTG_CHECK(num_sweeps >= 0, "dmrg_twosite: negative number of sweeps");
+	const std::vector<q32> qsite(psi->qsite, psi->qsite + psi->d);
+
+	Ctx& c = context_for_device(opt.device);
+	c.gemm_flops = 0;
+	c.kernel_launches = 0;
+	DBuf sc_buf(&c, sizeof(LanczosScalars));
+	LanczosScalars* d_sc = (LanczosScalars*)sc_buf.ptr;
+	LanczosScalars h_sc;
+
+	// upload
+	std::vector<DTensor> W(L), A(L);
+	for (int i = 0; i < L; i++) W[i] = tensor_from_struct(c, &H->a[i]);
+	for (int i = 0; i < L; i++) A[i] = tensor_from_struct(c, &psi->a[i]);
+	c.sync();
+	const double t_up = now_s();
+	st->upload_s = t_up - t_start;
+
+	int ret = 0;
+	// right-normalise (mps_orthonormalize_qr, src/state/mps.c:609-757)
+	for (int i = L - 1; i > 0 && ret == 0; i--) ret = local_orthonormalize_rq(c, A[i], A[i - 1]);
+	{
+		DTensor head = head_tensor(c, A[0], 1.0);
+		if (ret == 0) ret = local_orthonormalize_rq(c, A[0], head);
+		std::vector<double> hv((size_t)std::max<i64>(head.m().nnz, 1), 0.0);
+		if (head.m().nnz > 0) copy_to_host(c, head, hv.data());
+		double nrm = head.m().nblocks > 0 ? hv[0] : 0.0;
+		if (nrm < 0)
+		{
+			// flip the sign of site 0 so that the normalisation factor is non-negative
+			std::vector<double> vec((size_t)A[0].m().dim[0], -1.0);
+			DBufPtr mv = c.upload(vec.data(), vec.size() * sizeof(double));
+			A[0] = op_scale_axis(c, A[0], (const double*)mv->ptr, AX_LEADING);
+			nrm = -nrm;
+		}
+		if (nrm == 0) printf("Warning: in 'dmrg_twosite': initial MPS has norm zero (possibly due to mismatching quantum numbers)\n");
+	}
+	if (ret < 0) return ret;
+
+	// environments and merged MPO pairs
+	std::vector<DTensor> lb(L), rb(L), h2(L - 1);
+	rb[L - 1] = dummy_block(c, A[L - 1].m().ql[2], W[L - 1].m().ql[3], A[L - 1].m().ql[2], true);
+	for (int i = L - 1; i > 0; i--) rb[i - 1] = contraction_step_right(c, A[i], W[i], rb[i]);
+	lb[0] = dummy_block(c, A[0].m().ql[0], W[0].m().ql[0], A[0].m().ql[0], false);
+	for (int i = 1; i < L; i++) lb[i] = lb[0];
+	for (int i = 0; i < L - 1; i++) h2[i] = merge_mpo_pair(c, W[i], W[i + 1]);
+	c.sync();
+	const double t_setup = now_s();
+	st->setup_s = t_setup - t_up;
+
+	cudaEvent_t ev[4];
+	for (auto& e : ev) CTG_CUDA(cudaEventCreate(&e));
+	auto bond_step = [&](int i, bool left_to_right) -> int {
+		CTG_CUDA(cudaEventRecord(ev[0], c.stream()));
+		DTensor cur = merge_mps_pair(c, A[i], A[i + 1]);
+		DTensor aopt;
+		int r = minimize_local_energy(c, h2[i], lb[i], rb[i + 1], cur, maxiter, d_sc, aopt, st);
+		if (r < 0) return r;
+		CTG_CUDA(cudaEventRecord(ev[1], c.stream()));
+		double ent = 0;
+		r = split_mps_svd(c, aopt, psi->d, qsite, tol_split, max_vdim, !left_to_right, A[i], A[i + 1], &ent);
+		if (r < 0) return r;
+		CTG_CUDA(cudaMemcpy(&h_sc, d_sc, sizeof(LanczosScalars), cudaMemcpyDeviceToHost));
+		if (h_sc.status != 0) return h_sc.status;
+		CTG_CUDA(cudaEventRecord(ev[2], c.stream()));
+		if (left_to_right) lb[i + 1] = contraction_step_left(c, A[i], W[i], lb[i]);
+		else
+		{
+			entropy[i] = ent;
+			rb[i] = contraction_step_right(c, A[i + 1], W[i + 1], rb[i + 1]);
+		}
+		CTG_CUDA(cudaEventRecord(ev[3], c.stream()));
+		CTG_CUDA(cudaEventSynchronize(ev[1]));
+		float ms = 0;
+		CTG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+		st->lanczos_ms += ms;
+		CTG_CUDA(cudaEventElapsedTime(&ms, ev[1], ev[2]));
+		st->split_ms += ms;
+		return 0;
+	};
+
+	double en = 0;
+	for (int sw = 0; sw < num_sweeps && ret == 0; sw++)
+	{
+		for (int i = 0; i < L - 2 && ret == 0; i++) ret = bond_step(i, true);
+		for (int i = L - 2; i >= 0 && ret == 0; i--)
+		{
+			ret = bond_step(i, false);
+			if (ret == 0)
+			{
+				CTG_CUDA(cudaEventSynchronize(ev[3]));
+				float ms = 0;
+				CTG_CUDA(cudaEventElapsedTime(&ms, ev[2], ev[3]));
+				st->env_ms += ms;
+			}
+		}
+		if (ret < 0) break;
+		en = h_sc.lambda;
+		// right-normalise the leftmost tensor (dmrg.c:366-378)
+		DTensor t = head_tensor(c, A[0], 0.0);
+		ret = local_orthonormalize_rq(c, A[0], t);
+		en_sweeps[sw] = en;
+		st->sweeps++;
+	}
+	c.sync();
+	for (auto& e : ev) cudaEventDestroy(e);
+	const double t_sweeps = now_s();
+	st->sweep_s = t_sweeps - t_setup;
+	if (ret < 0) return ret;
+
+	// hand the optimised MPS back in the reference's layout (the caller's tensors are replaced)
+	for (int i = 0; i < L; i++)
+	{
+		free_struct(&psi->a[i]);
+		tensor_to_struct(c, A[i], &psi->a[i]);
+		st->max_bond_dim = std::max(st->max_bond_dim, A[i].m().dim[2]);
+	}
+	c.sync();
+	st->download_s = now_s() - t_sweeps;
+	st->kernel_launches = c.kernel_launches;
+	st->total_gemm_flops = c.gemm_flops;
+	st->wall_s = now_s() - t_start;
+	return 0;
+}
+
+}  // namespace ctg

@@ -1,0 +1,60 @@
+// ctg_dmrg.h - two-site DMRG on one GB300, MPS / MPO / environments resident in HBM.
+#pragma once
+
+#include "ct_structs.h"
+#include "ctg_engine.h"
+
+namespace ctg {
+
+struct DmrgOptions {
+	int device = 0;
+	int precision = GEMM_FP64;   // GemmPrecision of the bulk local-H GEMMs
+	int final_fp64_sweeps = 1;   // trailing sweeps forced to FP64 when precision != FP64
+	int verbose = 0;
+};
+
+struct DmrgStats {
+	double wall_s = 0;           // host wall time of the whole call
+	double upload_s = 0;         // host structs -> HBM
+	double download_s = 0;       // HBM -> host structs
+	double setup_s = 0;          // right-normalisation, environments, merged MPO pairs
+	double sweep_s = 0;          // all sweeps
+	double lanczos_ms = 0;       // device time in the Lanczos eigensolver (CUDA events)
+	double split_ms = 0;         // device+host time in the SVD split
+	double env_ms = 0;           // device time in the environment updates
+	double matvec_flops = 0;     // algorithmic GEMM FLOPs of all local-H applications
+	double total_gemm_flops = 0; // algorithmic GEMM FLOPs of everything
+	long matvecs = 0;
+	long kernel_launches = 0;
+	int sweeps = 0;
+	i64 max_bond_dim = 0;
+};
+
+// Same contract as dmrg_twosite (src/algorithm/dmrg.c:262-399).
+int dmrg_twosite_gpu(const struct mpo* hamiltonian, int num_sweeps, int maxiter_lanczos, double tol_split, i64 max_vdim,
+                     struct mps* psi, double* en_sweeps, double* entropy, const DmrgOptions& opt, DmrgStats* stats);
+
+// truncation rule of retained_bond_indices (src/algorithm/truncation.c:110-223)
+struct TruncResult {
+	std::vector<i64> ind;
+	double norm_sigma = 0, entropy = 0, tol_eff = 0;
+};
+TruncResult retained_bond_indices(const double* sigma, i64 n, double tol, bool relative_thresh, i64 max_vdim);
+
+// environment updates with b = a (src/algorithm/chain_ops.c:196-245, :116-165)
+DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l);
+DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& r);
+
+// one application of the local two-site Hamiltonian (src/algorithm/chain_ops.c:353-390)
+DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,
+                                     int precision);
+
+// host <-> device conversions of reference structs
+Meta meta_from_struct(const struct block_sparse_tensor* t);
+DTensor tensor_from_struct(Ctx& c, const struct block_sparse_tensor* t);
+void tensor_to_struct(Ctx& c, const DTensor& t, struct block_sparse_tensor* out);
+// allocate a reference-layout tensor (aligned_alloc) holding host entries in block order
+void write_struct_host(const Meta& m, const double* host, struct block_sparse_tensor* out);
+void free_struct(struct block_sparse_tensor* t);
+
+}  // namespace ctg

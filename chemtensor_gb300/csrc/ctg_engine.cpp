@@ -1,0 +1,745 @@
+// ctg_engine.cpp - lowering of block-sparse tensor operations to device work lists.
+#include "ctg_engine.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace ctg {
+
+// ------------------------------------------------------------------------------------
+// memory and context
+// ------------------------------------------------------------------------------------
+
+DBuf::DBuf(Ctx* c, size_t n) : ctx(c), bytes(n) { ptr = c->alloc(n); }
+DBuf::~DBuf()
+{
+	if (ptr && ctx) ctx->free(ptr);
+}
+
+Ctx::Ctx(int device) : dev_(device)
+{
+	CTG_CUDA(cudaSetDevice(dev_));
+	CTG_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+	cudaMemPoolProps props = {};
+	props.allocType = cudaMemAllocationTypePinned;
+	props.handleTypes = cudaMemHandleTypeNone;
+	props.location.type = cudaMemLocationTypeDevice;
+	props.location.id = dev_;
+	CTG_CUDA(cudaMemPoolCreate(&pool_, &props));
+	uint64_t thr = UINT64_MAX;
+	CTG_CUDA(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &thr));
+	staging_cap_ = (size_t)64 << 20;
+	CTG_CUDA(cudaMallocHost((void**)&staging_, staging_cap_));
+}
+
+Ctx::~Ctx()
+{
+	if (st_) cudaStreamSynchronize(st_);
+	if (staging_) cudaFreeHost(staging_);
+	if (pool_) cudaMemPoolDestroy(pool_);
+	if (st_) cudaStreamDestroy(st_);
+}
+
+Ctx& context_for_device(int device)
+{
+	// one context per (thread, device); deliberately never destroyed so that no CUDA call
+	// runs during process teardown
+	thread_local std::vector<Ctx*> ctxs;
+	for (Ctx* c : ctxs)
+		if (c->device() == device)
+		{
+			CTG_CUDA(cudaSetDevice(device));
+			return *c;
+		}
+	ctxs.push_back(new Ctx(device));
+	return *ctxs.back();
+}
+
+void* Ctx::alloc(size_t bytes)
+{
+	void* p = nullptr;
+	if (bytes == 0) bytes = 16;
+	CTG_CUDA(cudaMallocFromPoolAsync(&p, (bytes + 255) & ~(size_t)255, pool_, st_));
+	return p;
+}
+
+void Ctx::free(void* p)
+{
+	cudaFreeAsync(p, st_);
+}
+
+void Ctx::sync()
+{
+	CTG_CUDA(cudaStreamSynchronize(st_));
+	staging_used_ = 0;
+}
+
+DBufPtr Ctx::upload(const void* host, size_t bytes)
+{
+	auto b = std::make_shared<DBuf>(this, bytes);
+	size_t done = 0;
+	while (done < bytes)
+	{
+		if (staging_used_ >= staging_cap_) sync();
+		const size_t chunk = std::min(bytes - done, staging_cap_ - staging_used_);
+		char* stage = staging_ + staging_used_;
+		memcpy(stage, (const char*)host + done, chunk);
+		CTG_CUDA(cudaMemcpyAsync((char*)b->ptr + done, stage, chunk, cudaMemcpyHostToDevice, st_));
+		staging_used_ += (chunk + 255) & ~(size_t)255;
+		done += chunk;
+	}
+	return b;
+}
+
+DTensor Ctx::empty(const Meta& m)
+{
+	DTensor t;
+	t.meta = std::make_shared<const Meta>(m);
+	t.buf = std::make_shared<DBuf>(this, (size_t)std::max<i64>(m.nnz, 1) * sizeof(double));
+	return t;
+}
+
+DTensor Ctx::zeros(const Meta& m)
+{
+	DTensor t = empty(m);
+	CTG_CUDA(cudaMemsetAsync(t.data(), 0, (size_t)std::max<i64>(m.nnz, 1) * sizeof(double), st_));
+	return t;
+}
+
+void copy_to_device(Ctx& c, DTensor& t, const double* host)
+{
+	if (t.m().nnz == 0) return;
+	DBufPtr b = c.upload(host, (size_t)t.m().nnz * sizeof(double));
+	t.buf = b;
+}
+
+void copy_to_host(Ctx& c, const DTensor& t, double* host)
+{
+	if (t.m().nnz == 0) return;
+	CTG_CUDA(cudaMemcpyAsync(host, t.data(), (size_t)t.m().nnz * sizeof(double), cudaMemcpyDeviceToHost, c.stream()));
+	c.sync();
+}
+
+// ------------------------------------------------------------------------------------
+// descriptor packing: several typed arrays in one device buffer
+// ------------------------------------------------------------------------------------
+
+namespace {
+
+struct Packer {
+	std::vector<char> bytes;
+	template <class T>
+	size_t add(const std::vector<T>& v)
+	{
+		const size_t off = (bytes.size() + 15) & ~(size_t)15;
+		bytes.resize(off + v.size() * sizeof(T));
+		if (!v.empty()) memcpy(bytes.data() + off, v.data(), v.size() * sizeof(T));
+		return off;
+	}
+};
+
+template <class T>
+const T* at(const DBufPtr& b, size_t off)
+{
+	return (const T*)((const char*)b->ptr + off);
+}
+
+i64 prod(const i64* d, int n)
+{
+	i64 p = 1;
+	for (int i = 0; i < n; i++) p *= d[i];
+	return p;
+}
+
+void add_chunks(std::vector<Chunk>& chunks, int desc, i64 n)
+{
+	for (i64 s = 0; s < n; s += COPY_CHUNK) chunks.push_back(Chunk{desc, 0, s});
+}
+
+// logical indices carrying quantum number q on an axis, in order
+std::vector<i64> fanout(const Meta& t, int ax, q32 q)
+{
+	std::vector<i64> f;
+	for (i64 j = 0; j < t.dim[ax]; j++)
+		if (t.ql[ax][(size_t)j] == q) f.push_back(j);
+	return f;
+}
+
+int tile_class(int m, int n)
+{
+	if (m <= 16 && n <= 16) return TILE_S;
+	if (m <= 32 || n <= 32) return TILE_M;
+	return TILE_L;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// dot (block_sparse_tensor.c:1826-2001; dense_tensor.c:1761-1837)
+// ------------------------------------------------------------------------------------
+
+DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult)
+{
+	DotPlan p;
+	auto out = std::make_shared<Meta>(dot_result_meta(s, axs, t, axt, nmult));
+	p.out = out;
+	const Meta& r = *out;
+	const int shift_s = (axs == AX_LEADING ? 0 : s.ndim - nmult);
+	const int shift_t = (axt == AX_LEADING ? 0 : t.ndim - nmult);
+	const int off_s = (axs == AX_LEADING ? nmult : 0);
+	const int off_t = (axt == AX_LEADING ? nmult : 0);
+	const int nfs = s.ndim - nmult, nft = t.ndim - nmult;
+	const int nlds = (axs == AX_LEADING ? nmult : s.ndim - nmult);
+	const int nldt = (axt == AX_LEADING ? nmult : t.ndim - nmult);
+
+	std::vector<GemmOut> outs(r.nblocks);
+	std::vector<GemmContrib> cons;
+	std::vector<GemmTile> tiles[NUM_TILE_CLASSES];
+	i64 ncontract = 1;
+	for (int i = 0; i < nmult; i++) ncontract *= t.nb[shift_t + i];
+	std::vector<i64> is(s.ndim), it(t.ndim), ic(nmult);
+	double flops = 0;
+	for (int b = 0; b < r.nblocks; b++)
+	{
+		const i64* ir = r.index(b);
+		const i64* rd = r.dims(b);
+		GemmOut& o = outs[b];
+		o.c_off = r.boff[b];
+		o.m = (int)prod(rd, nfs);
+		o.n = (int)prod(rd + nfs, nft);
+		o.c0 = (int)cons.size();
+		for (i64 mm = 0; mm < ncontract; mm++)
+		{
+			i64 rem = mm;
+			for (int i = nmult - 1; i >= 0; i--) { ic[i] = rem % t.nb[shift_t + i]; rem /= t.nb[shift_t + i]; }
+			for (int i = 0; i < nfs; i++) is[off_s + i] = ir[i];
+			for (int i = 0; i < nmult; i++) is[shift_s + i] = ic[i];
+			const int bs = s.find(is.data());
+			if (bs < 0) continue;
+			for (int i = 0; i < nft; i++) it[off_t + i] = ir[nfs + i];
+			for (int i = 0; i < nmult; i++) it[shift_t + i] = ic[i];
+			const int bt = t.find(it.data());
+			CTG_CHECK(bt >= 0, "dot: missing partner block");
+			const i64* sd = s.dims(bs);
+			const i64* td = t.dims(bt);
+			const i64 lds = prod(sd, nlds), tds = prod(sd + nlds, s.ndim - nlds);
+			const i64 ldt = prod(td, nldt), tdt = prod(td + nldt, t.ndim - nldt);
+			GemmContrib g;
+			g.a_off = s.boff[bs];
+			g.b_off = t.boff[bt];
+			const i64 k = (axs == AX_LEADING ? lds : tds);
+			g.k = (int)k;
+			if (axs == AX_LEADING) { g.sAm = 1; g.sAk = (int)tds; }
+			else { g.sAm = (int)tds; g.sAk = 1; }
+			if (axt == AX_LEADING) { g.sBk = (int)tdt; g.sBn = 1; }
+			else { g.sBk = 1; g.sBn = (int)tdt; }
+			CTG_CHECK(k == (axt == AX_LEADING ? ldt : tdt), "dot: inner dimensions differ");
+			// every operand access stays inside its block (checked once per plan, on the host)
+			CTG_CHECK(k >= 1 && g.a_off + (i64)(o.m - 1) * g.sAm + (k - 1) * g.sAk < s.boff[bs] + s.block_size(bs),
+			          "dot: A operand out of range");
+			CTG_CHECK(g.b_off + (k - 1) * g.sBk + (i64)(o.n - 1) * g.sBn < t.boff[bt] + t.block_size(bt),
+			          "dot: B operand out of range");
+			cons.push_back(g);
+			flops += 2.0 * (double)o.m * (double)o.n * (double)k;
+		}
+		o.nc = (int)cons.size() - o.c0;
+		CTG_CHECK(o.m >= 1 && o.n >= 1 && o.c_off + (i64)o.m * o.n <= r.nnz, "dot: output block out of range");
+		const int cls = tile_class(o.m, o.n);
+		const int tr = tile_rows(cls), tc = tile_cols(cls);
+		for (int m0 = 0; m0 < o.m; m0 += tr)
+			for (int n0 = 0; n0 < o.n; n0 += tc) tiles[cls].push_back(GemmTile{b, m0, n0});
+	}
+	Packer pk;
+	const size_t o_outs = pk.add(outs);
+	const size_t o_cons = pk.add(cons);
+	size_t o_tiles[NUM_TILE_CLASSES];
+	for (int k = 0; k < NUM_TILE_CLASSES; k++) o_tiles[k] = pk.add(tiles[k]);
+	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	p.outs = at<GemmOut>(p.desc, o_outs);
+	p.cons = at<GemmContrib>(p.desc, o_cons);
+	for (int k = 0; k < NUM_TILE_CLASSES; k++)
+	{
+		p.ntiles[k] = (int)tiles[k].size();
+		p.tiles[k] = at<GemmTile>(p.desc, o_tiles[k]);
+	}
+	p.flops = flops;
+	return p;
+}
+
+void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
+{
+	for (int k = 0; k < NUM_TILE_CLASSES; k++)
+	{
+		if (ntiles[k] == 0) continue;
+		launch_gemm_f64(k, ntiles[k], tiles[k], outs, cons, A, B, C, c.stream());
+		c.kernel_launches++;
+	}
+	c.gemm_flops += flops;
+}
+
+// ------------------------------------------------------------------------------------
+// data movement plans
+// ------------------------------------------------------------------------------------
+
+void CopyPlan::run(Ctx& c, const double* src, double* dst) const
+{
+	if (nchunks == 0) return;
+	if (kind == 0) launch_permute(nchunks, chunks, (const PermDesc*)descs, src, dst, c.stream());
+	else launch_rowmap(nchunks, chunks, (const RowDesc*)descs, maps, src, dst, c.stream());
+	c.kernel_launches++;
+}
+
+static CopyPlan finish_perm(Ctx& c, std::shared_ptr<Meta> out, const std::vector<PermDesc>& d, const std::vector<Chunk>& ch)
+{
+	CopyPlan p;
+	p.out = out;
+	p.kind = 0;
+	Packer pk;
+	const size_t od = pk.add(d), oc = pk.add(ch);
+	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	p.descs = at<PermDesc>(p.desc, od);
+	p.chunks = at<Chunk>(p.desc, oc);
+	p.nchunks = (int)ch.size();
+	return p;
+}
+
+static void check_rows(const std::vector<RowDesc>& descs, const std::vector<i64>& maps, i64 src_nnz, i64 dst_nnz)
+{
+	for (const RowDesc& d : descs)
+	{
+		CTG_CHECK(d.map_off + d.nrow <= (i64)maps.size(), "row map: table out of range");
+		const int mrows = d.scatter ? d.dst_rows : d.src_rows;
+		for (int j = 0; j < d.nrow; j++)
+			CTG_CHECK(maps[(size_t)(d.map_off + j)] >= 0 && maps[(size_t)(d.map_off + j)] < mrows, "row map: entry out of range");
+		CTG_CHECK(d.src_off + d.nlead * d.src_rows * d.ntrail <= src_nnz, "row map: source out of range");
+		CTG_CHECK(d.dst_off + d.nlead * d.dst_rows * d.ntrail <= dst_nnz, "row map: destination out of range");
+		CTG_CHECK(d.scatter ? d.nrow <= d.src_rows : d.nrow <= d.dst_rows, "row map: row count out of range");
+	}
+}
+
+static CopyPlan finish_rows(Ctx& c, std::shared_ptr<Meta> out, const std::vector<RowDesc>& d, const std::vector<Chunk>& ch,
+                            const std::vector<i64>& maps)
+{
+	CopyPlan p;
+	p.out = out;
+	p.kind = 1;
+	Packer pk;
+	const size_t od = pk.add(d), oc = pk.add(ch), om = pk.add(maps);
+	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	p.descs = at<RowDesc>(p.desc, od);
+	p.chunks = at<Chunk>(p.desc, oc);
+	p.maps = at<i64>(p.desc, om);
+	p.nchunks = (int)ch.size();
+	return p;
+}
+
+// block_sparse_tensor_transpose (block_sparse_tensor.c:785-870)
+CopyPlan make_transpose_plan(Ctx& c, const Meta& t, const int* perm)
+{
+	auto out = std::make_shared<Meta>(transpose_meta(t, perm));
+	const Meta& r = *out;
+	CTG_CHECK(t.ndim <= 6, "transpose: at most 6 axes");
+	std::vector<PermDesc> descs;
+	std::vector<Chunk> chunks;
+	std::vector<i64> ir(t.ndim);
+	for (int b = 0; b < t.nblocks; b++)
+	{
+		const i64* it = t.index(b);
+		const i64* td = t.dims(b);
+		for (int i = 0; i < t.ndim; i++) ir[i] = it[perm[i]];
+		const int rb = r.find(ir.data());
+		CTG_CHECK(rb >= 0, "transpose: missing block");
+		i64 st[8];
+		st[t.ndim - 1] = 1;
+		for (int i = t.ndim - 2; i >= 0; i--) st[i] = st[i + 1] * td[i + 1];
+		PermDesc d = {};
+		d.src_off = t.boff[b];
+		d.dst_off = r.boff[rb];
+		d.n = t.block_size(b);
+		d.ndim = t.ndim;
+		for (int i = 0; i < t.ndim; i++) { d.dims[i] = (int)td[perm[i]]; d.sstr[i] = st[perm[i]]; }
+		i64 smax = 0;
+		for (int i = 0; i < t.ndim; i++) smax += (i64)(d.dims[i] - 1) * d.sstr[i];
+		CTG_CHECK(d.src_off + smax < t.nnz && d.dst_off + d.n <= r.nnz, "transpose: descriptor out of range");
+		add_chunks(chunks, (int)descs.size(), d.n);
+		descs.push_back(d);
+	}
+	return finish_perm(c, out, descs, chunks);
+}
+
+// block_sparse_tensor_flatten_axes (block_sparse_tensor.c:950-1112): each source block
+// scatters its rows (j0, j1) into the fused rows of one target block
+CopyPlan make_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
+{
+	auto out = std::make_shared<Meta>(flatten_meta(t, ax, newdir));
+	const Meta& r = *out;
+	const i64 d1 = t.dim[ax + 1];
+	std::vector<RowDesc> descs;
+	std::vector<Chunk> chunks;
+	std::vector<i64> maps;
+	std::vector<i64> ir(r.ndim);
+	for (int b = 0; b < t.nblocks; b++)
+	{
+		const i64* it = t.index(b);
+		const i64* td = t.dims(b);
+		const q32 q0 = t.qb[ax][it[ax]], q1 = t.qb[ax + 1][it[ax + 1]];
+		const q32 qf = newdir * (t.dir[ax] * q0 + t.dir[ax + 1] * q1);
+		for (int i = 0; i < ax; i++) ir[i] = it[i];
+		ir[ax] = r.find_q(ax, qf);
+		for (int i = ax + 2; i < t.ndim; i++) ir[i - 1] = it[i];
+		const int rb = r.find(ir.data());
+		CTG_CHECK(rb >= 0, "flatten: missing target block");
+		const auto f0 = fanout(t, ax, q0), f1 = fanout(t, ax + 1, q1);
+		RowDesc d = {};
+		d.src_off = t.boff[b];
+		d.dst_off = r.boff[rb];
+		d.nlead = prod(td, ax);
+		d.ntrail = prod(td + ax + 2, t.ndim - ax - 2);
+		d.nrow = (int)(td[ax] * td[ax + 1]);
+		d.src_rows = d.nrow;
+		d.dst_rows = (int)r.dims(rb)[ax];
+		d.scatter = 1;
+		d.map_off = (i64)maps.size();
+		for (size_t j0 = 0; j0 < f0.size(); j0++)
+			for (size_t j1 = 0; j1 < f1.size(); j1++) maps.push_back(r.pos[ax][(size_t)(f0[j0] * d1 + f1[j1])]);
+		add_chunks(chunks, (int)descs.size(), d.nlead * d.nrow * d.ntrail);
+		descs.push_back(d);
+	}
+	check_rows(descs, maps, t.nnz, r.nnz);
+	return finish_rows(c, out, descs, chunks, maps);
+}
+
+// block_sparse_tensor_split_axis (block_sparse_tensor.c:1123-1285): each target block
+// gathers its rows (j0, j1) from the fused rows of one source block
+CopyPlan make_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
+{
+	auto out = std::make_shared<Meta>(split_meta(t, ax, nd, ndir, nq));
+	const Meta& r = *out;
+	std::vector<RowDesc> descs;
+	std::vector<Chunk> chunks;
+	std::vector<i64> maps;
+	std::vector<i64> it(t.ndim);
+	for (int b = 0; b < r.nblocks; b++)
+	{
+		const i64* ir = r.index(b);
+		const i64* rd = r.dims(b);
+		const q32 q0 = r.qb[ax][ir[ax]], q1 = r.qb[ax + 1][ir[ax + 1]];
+		const q32 qf = t.dir[ax] * (r.dir[ax] * q0 + r.dir[ax + 1] * q1);
+		for (int i = 0; i < ax; i++) it[i] = ir[i];
+		it[ax] = t.find_q(ax, qf);
+		for (int i = ax + 1; i < t.ndim; i++) it[i] = ir[i + 1];
+		const int tb = t.find(it.data());
+		CTG_CHECK(tb >= 0, "split: missing source block");
+		const auto f0 = fanout(r, ax, q0), f1 = fanout(r, ax + 1, q1);
+		RowDesc d = {};
+		d.src_off = t.boff[tb];
+		d.dst_off = r.boff[b];
+		d.nlead = prod(rd, ax);
+		d.ntrail = prod(rd + ax + 2, r.ndim - ax - 2);
+		d.nrow = (int)(rd[ax] * rd[ax + 1]);
+		d.dst_rows = d.nrow;
+		d.src_rows = (int)t.dims(tb)[ax];
+		d.scatter = 0;
+		d.map_off = (i64)maps.size();
+		for (size_t j0 = 0; j0 < f0.size(); j0++)
+			for (size_t j1 = 0; j1 < f1.size(); j1++) maps.push_back(t.pos[ax][(size_t)(f0[j0] * nd[1] + f1[j1])]);
+		add_chunks(chunks, (int)descs.size(), d.nlead * d.nrow * d.ntrail);
+		descs.push_back(d);
+	}
+	check_rows(descs, maps, t.nnz, r.nnz);
+	return finish_rows(c, out, descs, chunks, maps);
+}
+
+// block_sparse_tensor_slice (block_sparse_tensor.c:1446-1553)
+CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& ind)
+{
+	auto out = std::make_shared<Meta>(slice_meta(t, ax, ind));
+	const Meta& r = *out;
+	std::vector<RowDesc> descs;
+	std::vector<Chunk> chunks;
+	std::vector<i64> maps;
+	std::vector<i64> it(t.ndim);
+	for (int b = 0; b < r.nblocks; b++)
+	{
+		const i64* ir = r.index(b);
+		const i64* rd = r.dims(b);
+		const q32 qn = r.qb[ax][ir[ax]];
+		for (int i = 0; i < t.ndim; i++) it[i] = ir[i];
+		it[ax] = t.find_q(ax, qn);
+		const int tb = t.find(it.data());
+		CTG_CHECK(tb >= 0, "slice: missing source block");
+		const auto fr = fanout(r, ax, qn);
+		RowDesc d = {};
+		d.src_off = t.boff[tb];
+		d.dst_off = r.boff[b];
+		d.nlead = prod(rd, ax);
+		d.ntrail = prod(rd + ax + 1, r.ndim - ax - 1);
+		d.nrow = (int)rd[ax];
+		d.dst_rows = d.nrow;
+		d.src_rows = (int)t.dims(tb)[ax];
+		d.scatter = 0;
+		d.map_off = (i64)maps.size();
+		for (size_t j = 0; j < fr.size(); j++) maps.push_back(t.pos[ax][(size_t)ind[(size_t)fr[j]]]);
+		add_chunks(chunks, (int)descs.size(), d.nlead * d.nrow * d.ntrail);
+		descs.push_back(d);
+	}
+	check_rows(descs, maps, t.nnz, r.nnz);
+	return finish_rows(c, out, descs, chunks, maps);
+}
+
+// ------------------------------------------------------------------------------------
+// one-shot operations
+// ------------------------------------------------------------------------------------
+
+DTensor op_dot(Ctx& c, const DTensor& s, int axs, const DTensor& t, int axt, int nmult)
+{
+	DotPlan p = make_dot_plan(c, s.m(), axs, t.m(), axt, nmult);
+	DTensor r;
+	r.meta = p.out;
+	r.buf = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(p.out->nnz, 1) * sizeof(double));
+	p.run(c, s.data(), t.data(), r.data());
+	return r;
+}
+
+static DTensor run_copy(Ctx& c, const CopyPlan& p, const DTensor& src)
+{
+	DTensor r;
+	r.meta = p.out;
+	r.buf = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(p.out->nnz, 1) * sizeof(double));
+	p.run(c, src.data(), r.data());
+	return r;
+}
+
+DTensor op_transpose(Ctx& c, const DTensor& t, const int* perm)
+{
+	return run_copy(c, make_transpose_plan(c, t.m(), perm), t);
+}
+
+DTensor op_flatten(Ctx& c, const DTensor& t, int ax, int newdir)
+{
+	return run_copy(c, make_flatten_plan(c, t.m(), ax, newdir), t);
+}
+
+DTensor op_split(Ctx& c, const DTensor& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
+{
+	return run_copy(c, make_split_plan(c, t.m(), ax, nd, ndir, nq), t);
+}
+
+DTensor op_slice(Ctx& c, const DTensor& t, int ax, const std::vector<i64>& ind)
+{
+	return run_copy(c, make_slice_plan(c, t.m(), ax, ind), t);
+}
+
+// block_sparse_tensor_multiply_pointwise_vector (block_sparse_tensor.c:1654-1703)
+DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange)
+{
+	const Meta& m = s.m();
+	const int ax = (axrange == AX_LEADING ? 0 : m.ndim - 1);
+	std::vector<ScaleDesc> descs;
+	std::vector<Chunk> chunks;
+	std::vector<i64> maps;
+	for (int b = 0; b < m.nblocks; b++)
+	{
+		const i64* ib = m.index(b);
+		const i64* bd = m.dims(b);
+		const auto f = fanout(m, ax, m.qb[ax][ib[ax]]);
+		ScaleDesc d = {};
+		d.off = m.boff[b];
+		d.nlead = prod(bd, ax);
+		d.nax = (int)bd[ax];
+		d.ntrail = prod(bd + ax + 1, m.ndim - ax - 1);
+		d.map_off = (i64)maps.size();
+		maps.insert(maps.end(), f.begin(), f.end());
+		CTG_CHECK((i64)f.size() == d.nax && d.off + d.nlead * d.nax * d.ntrail <= m.nnz, "scale: descriptor out of range");
+		add_chunks(chunks, (int)descs.size(), d.nlead * d.nax * d.ntrail);
+		descs.push_back(d);
+	}
+	Packer pk;
+	const size_t od = pk.add(descs), oc = pk.add(chunks), om = pk.add(maps);
+	DBufPtr desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	DTensor r = c.empty(m);
+	launch_scale_axis((int)chunks.size(), at<Chunk>(desc, oc), at<ScaleDesc>(desc, od), at<i64>(desc, om), dvec, s.data(),
+	                  r.data(), c.stream());
+	c.kernel_launches++;
+	return r;
+}
+
+DTensor view_reversed(const DTensor& t)
+{
+	DTensor r;
+	r.meta = std::make_shared<const Meta>(reversed_meta(t.m()));
+	r.buf = t.buf;
+	return r;
+}
+
+// block_sparse_tensor_cyclic_partial_trace with ndim_trace = 1 (block_sparse_tensor.c:1560-1611):
+// with unit traced dimensions carrying equal quantum numbers and opposite directions, the
+// traced tensor has the same blocks in the same order and the same entries
+DTensor view_trace_unit(const DTensor& t)
+{
+	const Meta& m = t.m();
+	CTG_CHECK(m.ndim >= 3 && m.dim[0] == 1 && m.dim[m.ndim - 1] == 1, "trace: unit outer dimensions expected");
+	CTG_CHECK(m.dir[0] == -m.dir[m.ndim - 1] && m.ql[0] == m.ql[m.ndim - 1], "trace: outer axes must match");
+	std::vector<std::vector<q32>> ql(m.ql.begin() + 1, m.ql.end() - 1);
+	Meta r = make_meta(m.ndim - 2, m.dim.data() + 1, m.dir.data() + 1, ql);
+	CTG_CHECK(r.nnz == m.nnz && r.nblocks == m.nblocks, "trace: unexpected block structure");
+	DTensor o;
+	o.meta = std::make_shared<const Meta>(std::move(r));
+	o.buf = t.buf;
+	return o;
+}
+
+// ------------------------------------------------------------------------------------
+// SVD and RQ of block-sparse matrices
+// ------------------------------------------------------------------------------------
+
+int op_svd(Ctx& c, const DTensor& a, SvdResult& res)
+{
+	const Meta& am = a.m();
+	CTG_CHECK(am.ndim == 2, "svd: matrix expected");
+	// intermediate axis: column quantum numbers (sorted), min(m, n) copies per block
+	std::vector<q32> qi;
+	struct Blk { int ab; i64 m, n, k; };
+	std::vector<Blk> blks;
+	for (i64 j = 0; j < am.nb[1]; j++)
+		for (i64 i = 0; i < am.nb[0]; i++)
+		{
+			const i64 idx[2] = {i, j};
+			const int b = am.find(idx);
+			if (b < 0) continue;
+			const i64 m = am.dims(b)[0], n = am.dims(b)[1], k = std::min(m, n);
+			for (i64 l = 0; l < k; l++) qi.push_back(am.qb[1][j]);
+			blks.push_back(Blk{b, m, n, k});
+		}
+	bool dummy = false;
+	if (qi.empty())
+	{
+		dummy = true;
+		qi.push_back(-am.dir[0] * am.dir[1] * am.qb[0][0]);
+	}
+	const i64 ni = (i64)qi.size();
+	const i64 du[2] = {am.dim[0], ni};
+	Meta mu = make_meta(2, du, am.dir.data(), {am.ql[0], qi});
+	const i64 dv[2] = {ni, am.dim[1]};
+	const int dirv[2] = {-am.dir[1], am.dir[1]};
+	Meta mv = make_meta(2, dv, dirv, {qi, am.ql[1]});
+	res.u = c.zeros(mu);
+	res.vh = c.zeros(mv);
+	res.ns = ni;
+	res.s = std::make_shared<DBuf>(&c, (size_t)ni * sizeof(double));
+	CTG_CUDA(cudaMemsetAsync(res.s->ptr, 0, (size_t)ni * sizeof(double), c.stream()));
+	if (dummy)
+	{
+		const i64 idx[2] = {0, (i64)mu.find_q(1, qi[0])};
+		const int b = mu.find(idx);
+		CTG_CHECK(b >= 0, "svd: dummy block missing");
+		static const double one = 1.0;
+		CTG_CUDA(cudaMemcpyAsync(res.u.data() + mu.boff[b], &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
+		c.sync();
+		return 0;
+	}
+	std::vector<SvdDesc> descs;
+	i64 woff = 0;
+	for (const Blk& bl : blks)
+	{
+		const i64* ia = am.index(bl.ab);
+		const i64 kb = mu.find_q(1, am.qb[1][ia[1]]);
+		const i64 iu[2] = {ia[0], kb}, iv[2] = {kb, ia[1]};
+		const int bu = mu.find(iu), bv = mv.find(iv);
+		CTG_CHECK(bu >= 0 && bv >= 0, "svd: factor blocks missing");
+		CTG_CHECK(std::min(bl.m, bl.n) <= 4096, "svd: block with more than 4096 singular values");
+		i64 first = 0;
+		while (mu.ql[1][(size_t)first] != am.qb[1][ia[1]]) first++;
+		SvdDesc d = {};
+		d.a_off = am.boff[bl.ab];
+		d.u_off = mu.boff[bu];
+		d.v_off = mv.boff[bv];
+		d.s_off = first;
+		d.w_off = woff;
+		d.m = (int)bl.m;
+		d.n = (int)bl.n;
+		woff += std::max(bl.m, bl.n) * bl.k + bl.k * bl.k;
+		descs.push_back(d);
+	}
+	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(SvdDesc));
+	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
+	DBuf status(&c, sizeof(int));
+	CTG_CUDA(cudaMemsetAsync(status.ptr, 0, sizeof(int), c.stream()));
+	launch_svd_jacobi((int)descs.size(), (const SvdDesc*)desc->ptr, a.data(), res.u.data(), (double*)res.s->ptr,
+	                  res.vh.data(), (double*)scratch.ptr, (int*)status.ptr, c.stream());
+	c.kernel_launches++;
+	int hst = 0;
+	CTG_CUDA(cudaMemcpyAsync(&hst, status.ptr, sizeof(int), cudaMemcpyDeviceToHost, c.stream()));
+	c.sync();
+	return hst == 0 ? 0 : -1;
+}
+
+int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q)
+{
+	const Meta& am = a.m();
+	CTG_CHECK(am.ndim == 2, "rq: matrix expected");
+	std::vector<q32> qi;
+	struct Blk { int ab; i64 m, n, k; };
+	std::vector<Blk> blks;
+	for (i64 i = 0; i < am.nb[0]; i++)
+		for (i64 j = 0; j < am.nb[1]; j++)
+		{
+			const i64 idx[2] = {i, j};
+			const int b = am.find(idx);
+			if (b < 0) continue;
+			const i64 m = am.dims(b)[0], n = am.dims(b)[1], k = std::min(m, n);
+			for (i64 l = 0; l < k; l++) qi.push_back(am.qb[0][i]);
+			blks.push_back(Blk{b, m, n, k});
+		}
+	bool dummy = false;
+	if (qi.empty())
+	{
+		dummy = true;
+		qi.push_back(-am.dir[0] * am.dir[1] * am.qb[1][0]);
+	}
+	const i64 ni = (i64)qi.size();
+	const i64 dr[2] = {am.dim[0], ni};
+	const int dirr[2] = {am.dir[0], -am.dir[0]};
+	Meta mr = make_meta(2, dr, dirr, {am.ql[0], qi});
+	const i64 dq[2] = {ni, am.dim[1]};
+	Meta mq = make_meta(2, dq, am.dir.data(), {qi, am.ql[1]});
+	r = c.zeros(mr);
+	q = c.zeros(mq);
+	if (dummy)
+	{
+		const i64 idx[2] = {(i64)mq.find_q(0, qi[0]), 0};
+		const int b = mq.find(idx);
+		CTG_CHECK(b >= 0, "rq: dummy block missing");
+		static const double one = 1.0;
+		CTG_CUDA(cudaMemcpyAsync(q.data() + mq.boff[b], &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
+		c.sync();
+		return 0;
+	}
+	std::vector<RqDesc> descs;
+	i64 woff = 0;
+	for (const Blk& bl : blks)
+	{
+		const i64* ia = am.index(bl.ab);
+		const i64 kb = mq.find_q(0, am.qb[0][ia[0]]);
+		const i64 ir[2] = {ia[0], kb}, iq[2] = {kb, ia[1]};
+		const int br = mr.find(ir), bq = mq.find(iq);
+		CTG_CHECK(br >= 0 && bq >= 0, "rq: factor blocks missing");
+		RqDesc d = {};
+		d.a_off = am.boff[bl.ab];
+		d.r_off = mr.boff[br];
+		d.q_off = mq.boff[bq];
+		d.w_off = woff;
+		d.m = (int)bl.m;
+		d.n = (int)bl.n;
+		woff += bl.n * bl.m + bl.n * bl.k + bl.k;
+		descs.push_back(d);
+	}
+	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(RqDesc));
+	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
+	launch_rq_householder((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr,
+	                      c.stream());
+	c.kernel_launches++;
+	return 0;
+}
+
+}  // namespace ctg

@@ -1,0 +1,130 @@
+// ctg_engine.h - device-resident block-sparse tensors and their operations.
+//
+// A DTensor is a host-side Meta (block structure, integers only) plus one
+// contiguous device buffer holding every dense block in row-major block
+// order. Operations are lowered on the host into descriptor arrays ("plans")
+// that are uploaded once and launched on the engine's stream; the host never
+// touches tensor entries except at the C-ABI boundary and when it reads the
+// singular values needed for the truncation decision.
+#pragma once
+
+#include <memory>
+
+#include "ctg_kernels.h"
+#include "ctg_meta.h"
+
+namespace ctg {
+
+class Ctx;
+
+// Stream-ordered device allocation, freed on the owning context's stream.
+struct DBuf {
+	Ctx* ctx = nullptr;
+	void* ptr = nullptr;
+	size_t bytes = 0;
+	DBuf(Ctx* c, size_t n);
+	~DBuf();
+	DBuf(const DBuf&) = delete;
+	DBuf& operator=(const DBuf&) = delete;
+};
+using DBufPtr = std::shared_ptr<DBuf>;
+
+struct DTensor {
+	std::shared_ptr<const Meta> meta;
+	DBufPtr buf;
+	double* data() const { return buf ? (double*)buf->ptr : nullptr; }
+	const Meta& m() const { return *meta; }
+};
+
+// Execution context: one CUDA stream, a private memory pool and a pinned staging
+// arena for descriptor uploads. All work of one DMRG call runs on this stream.
+class Ctx {
+public:
+	explicit Ctx(int device);
+	~Ctx();
+	cudaStream_t stream() const { return st_; }
+	int device() const { return dev_; }
+	void* alloc(size_t bytes);
+	void free(void* p);
+	// copy host bytes to a new device buffer (through pinned staging, asynchronous)
+	DBufPtr upload(const void* host, size_t bytes);
+	// block until the stream is idle; recycles the staging arena
+	void sync();
+	DTensor empty(const Meta& m);
+	DTensor zeros(const Meta& m);
+	// statistics
+	double gemm_flops = 0;       // algorithmic FP64-path GEMM FLOPs issued
+	long kernel_launches = 0;
+
+private:
+	int dev_;
+	cudaStream_t st_ = nullptr;
+	cudaMemPool_t pool_ = nullptr;
+	char* staging_ = nullptr;
+	size_t staging_cap_ = 0, staging_used_ = 0;
+};
+
+// Per-thread execution context for a device, created on first use and kept for the
+// life of the thread, so that repeated calls reuse the stream, pool and staging arena.
+Ctx& context_for_device(int device);
+
+// ---- plans ------------------------------------------------------------------------
+
+struct DotPlan {
+	std::shared_ptr<const Meta> out;
+	DBufPtr desc;
+	int ntiles[NUM_TILE_CLASSES] = {0, 0, 0};
+	const GemmTile* tiles[NUM_TILE_CLASSES] = {nullptr, nullptr, nullptr};
+	const GemmOut* outs = nullptr;
+	const GemmContrib* cons = nullptr;
+	double flops = 0;
+	void run(Ctx& c, const double* A, const double* B, double* C) const;
+};
+DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult);
+
+struct CopyPlan {
+	std::shared_ptr<const Meta> out;
+	DBufPtr desc;
+	int kind = 0;                // 0 permute, 1 rowmap
+	int nchunks = 0;
+	const Chunk* chunks = nullptr;
+	const void* descs = nullptr;
+	const i64* maps = nullptr;
+	void run(Ctx& c, const double* src, double* dst) const;
+};
+CopyPlan make_transpose_plan(Ctx& c, const Meta& t, const int* perm);
+CopyPlan make_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir);
+CopyPlan make_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq);
+CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& ind);
+
+// ---- one-shot operations (plan + run) ------------------------------------------------
+
+DTensor op_dot(Ctx& c, const DTensor& s, int axs, const DTensor& t, int axt, int nmult);
+DTensor op_transpose(Ctx& c, const DTensor& t, const int* perm);
+DTensor op_flatten(Ctx& c, const DTensor& t, int ax, int newdir);
+DTensor op_split(Ctx& c, const DTensor& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq);
+DTensor op_slice(Ctx& c, const DTensor& t, int ax, const std::vector<i64>& ind);
+// multiply along the leading (axrange 0) or trailing (1) axis by a device vector indexed by logical position
+DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange);
+// same entries, all axis directions reversed
+DTensor view_reversed(const DTensor& t);
+// cyclic partial trace of one leading with one trailing axis of logical dimension 1 (a relabelling)
+DTensor view_trace_unit(const DTensor& t);
+
+// block SVD (block_sparse_tensor_svd, block_sparse_tensor.c:2686-2848); singular values in a
+// device buffer indexed like the logical intermediate axis. Returns 0 or -1.
+struct SvdResult {
+	DTensor u, vh;
+	DBufPtr s;
+	i64 ns = 0;
+};
+int op_svd(Ctx& c, const DTensor& a, SvdResult& res);
+
+// block RQ (block_sparse_tensor_rq, block_sparse_tensor.c:2544-2676). Returns 0 or -1.
+int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q);
+
+// host <-> device entry copies (asynchronous on the context stream; host memory must stay valid)
+void copy_to_device(Ctx& c, DTensor& t, const double* host);
+void copy_to_host(Ctx& c, const DTensor& t, double* host);
+
+}  // namespace ctg

@@ -1,0 +1,214 @@
+// ctg_kernels.cu - FP64 grouped block GEMM and the block data-movement kernels.
+#include "ctg_kernels.h"
+
+namespace ctg {
+
+// ------------------------------------------------------------------------------------
+// grouped FP64 block GEMM (plain path; dense_tensor_dot_update, dense_tensor.c:1761-1837)
+// ------------------------------------------------------------------------------------
+
+template <int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const GemmContrib* __restrict__ cons,
+           const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C)
+{
+	constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
+	__shared__ double As[BK][BM + 1];
+	__shared__ double Bs[BK][BN + 1];
+	const GemmTile tile = tiles[blockIdx.x];
+	const GemmOut o = outs[tile.out];
+	const int tid = threadIdx.x;
+	const int tx = tid % NTX, ty = tid / NTX;
+	double acc[TM][TN];
+#pragma unroll
+	for (int i = 0; i < TM; i++)
+#pragma unroll
+		for (int j = 0; j < TN; j++) acc[i][j] = 0.0;
+
+	for (int c = o.c0; c < o.c0 + o.nc; c++)
+	{
+		const GemmContrib g = cons[c];
+		const double* a = A + g.a_off;
+		const double* b = B + g.b_off;
+		for (int k0 = 0; k0 < g.k; k0 += BK)
+		{
+			// A tile: BM x BK; the thread-to-element map follows the unit-stride index
+			if (g.sAk == 1)
+			{
+				for (int e = tid; e < BM * BK; e += NT)
+				{
+					const int kk = e % BK, i = e / BK;
+					const int gi = tile.m0 + i, gk = k0 + kk;
+					As[kk][i] = (gi < o.m && gk < g.k) ? a[(i64)gi * g.sAm + gk] : 0.0;
+				}
+			}
+			else
+			{
+				for (int e = tid; e < BM * BK; e += NT)
+				{
+					const int i = e % BM, kk = e / BM;
+					const int gi = tile.m0 + i, gk = k0 + kk;
+					As[kk][i] = (gi < o.m && gk < g.k) ? a[(i64)gi * g.sAm + (i64)gk * g.sAk] : 0.0;
+				}
+			}
+			// B tile: BK x BN
+			if (g.sBn == 1)
+			{
+				for (int e = tid; e < BK * BN; e += NT)
+				{
+					const int j = e % BN, kk = e / BN;
+					const int gj = tile.n0 + j, gk = k0 + kk;
+					Bs[kk][j] = (gj < o.n && gk < g.k) ? b[(i64)gk * g.sBk + gj] : 0.0;
+				}
+			}
+			else
+			{
+				for (int e = tid; e < BK * BN; e += NT)
+				{
+					const int kk = e % BK, j = e / BK;
+					const int gj = tile.n0 + j, gk = k0 + kk;
+					Bs[kk][j] = (gj < o.n && gk < g.k) ? b[(i64)gk * g.sBk + (i64)gj * g.sBn] : 0.0;
+				}
+			}
+			__syncthreads();
+			const int kmax = min(BK, g.k - k0);
+			for (int kk = 0; kk < kmax; kk++)
+			{
+				double av[TM], bv[TN];
+#pragma unroll
+				for (int i = 0; i < TM; i++) av[i] = As[kk][ty + i * NTY];
+#pragma unroll
+				for (int j = 0; j < TN; j++) bv[j] = Bs[kk][tx + j * NTX];
+#pragma unroll
+				for (int i = 0; i < TM; i++)
+#pragma unroll
+					for (int j = 0; j < TN; j++) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+			}
+			__syncthreads();
+		}
+	}
+	double* cblk = C + o.c_off;
+#pragma unroll
+	for (int i = 0; i < TM; i++)
+	{
+		const int gi = tile.m0 + ty + i * NTY;
+		if (gi >= o.m) continue;
+#pragma unroll
+		for (int j = 0; j < TN; j++)
+		{
+			const int gj = tile.n0 + tx + j * NTX;
+			if (gj < o.n) cblk[(i64)gi * o.n + gj] = acc[i][j];
+		}
+	}
+}
+
+int tile_rows(int cls) { return cls == TILE_L ? 64 : (cls == TILE_M ? 32 : 16); }
+int tile_cols(int cls) { return cls == TILE_L ? 64 : (cls == TILE_M ? 32 : 16); }
+
+void launch_gemm_f64(int cls, int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
+                     const double* A, const double* B, double* C, cudaStream_t st)
+{
+	if (ntiles <= 0) return;
+	switch (cls)
+	{
+	case TILE_L: k_gemm_f64<64, 64, 16, 4, 4><<<ntiles, 256, 0, st>>>(tiles, outs, cons, A, B, C); break;
+	case TILE_M: k_gemm_f64<32, 32, 16, 4, 4><<<ntiles, 64, 0, st>>>(tiles, outs, cons, A, B, C); break;
+	default:     k_gemm_f64<16, 16, 16, 2, 2><<<ntiles, 64, 0, st>>>(tiles, outs, cons, A, B, C); break;
+	}
+	CTG_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------------------------
+// block permutation (dense_tensor_transpose, dense_tensor.c:799-932)
+// ------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256)
+k_permute(const Chunk* __restrict__ chunks, const PermDesc* __restrict__ descs, const double* __restrict__ src,
+          double* __restrict__ dst)
+{
+	const Chunk ch = chunks[blockIdx.x];
+	const PermDesc d = descs[ch.desc];
+	const i64 end = min(d.n, ch.start + (i64)COPY_CHUNK);
+	for (i64 e = ch.start + threadIdx.x; e < end; e += blockDim.x)
+	{
+		i64 r = e, so = 0;
+		for (int i = d.ndim - 1; i >= 0; i--)
+		{
+			const i64 q = r / d.dims[i];
+			so += (r - q * d.dims[i]) * d.sstr[i];
+			r = q;
+		}
+		dst[d.dst_off + e] = src[d.src_off + so];
+	}
+}
+
+void launch_permute(int nchunks, const Chunk* chunks, const PermDesc* descs, const double* src, double* dst, cudaStream_t st)
+{
+	if (nchunks <= 0) return;
+	k_permute<<<nchunks, 256, 0, st>>>(chunks, descs, src, dst);
+	CTG_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------------------------
+// row maps: flatten / split / slice (block_sparse_tensor.c:950-1553)
+// ------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256)
+k_rowmap(const Chunk* __restrict__ chunks, const RowDesc* __restrict__ descs, const i64* __restrict__ maps,
+         const double* __restrict__ src, double* __restrict__ dst)
+{
+	const Chunk ch = chunks[blockIdx.x];
+	const RowDesc d = descs[ch.desc];
+	const i64 n = d.nlead * d.nrow * d.ntrail;
+	const i64 end = min(n, ch.start + (i64)COPY_CHUNK);
+	const i64* map = maps + d.map_off;
+	for (i64 e = ch.start + threadIdx.x; e < end; e += blockDim.x)
+	{
+		const i64 t = e % d.ntrail;
+		const i64 lj = e / d.ntrail;
+		const i64 j = lj % d.nrow;
+		const i64 lead = lj / d.nrow;
+		const i64 mj = map[j];
+		const i64 srow = d.scatter ? j : mj;
+		const i64 drow = d.scatter ? mj : j;
+		dst[d.dst_off + (lead * d.dst_rows + drow) * d.ntrail + t] = src[d.src_off + (lead * d.src_rows + srow) * d.ntrail + t];
+	}
+}
+
+void launch_rowmap(int nchunks, const Chunk* chunks, const RowDesc* descs, const i64* maps, const double* src, double* dst,
+                   cudaStream_t st)
+{
+	if (nchunks <= 0) return;
+	k_rowmap<<<nchunks, 256, 0, st>>>(chunks, descs, maps, src, dst);
+	CTG_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------------------------
+// pointwise multiplication along an axis (block_sparse_tensor_multiply_pointwise_vector,
+// block_sparse_tensor.c:1654-1703)
+// ------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256)
+k_scale_axis(const Chunk* __restrict__ chunks, const ScaleDesc* __restrict__ descs, const i64* __restrict__ maps,
+             const double* __restrict__ vec, const double* __restrict__ src, double* __restrict__ dst)
+{
+	const Chunk ch = chunks[blockIdx.x];
+	const ScaleDesc d = descs[ch.desc];
+	const i64 n = d.nlead * d.nax * d.ntrail;
+	const i64 end = min(n, ch.start + (i64)COPY_CHUNK);
+	for (i64 e = ch.start + threadIdx.x; e < end; e += blockDim.x)
+	{
+		const i64 p = (e / d.ntrail) % d.nax;
+		dst[d.off + e] = src[d.off + e] * vec[maps[d.map_off + p]];
+	}
+}
+
+void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs, const i64* maps, const double* vec,
+                       const double* src, double* dst, cudaStream_t st)
+{
+	if (nchunks <= 0) return;
+	k_scale_axis<<<nchunks, 256, 0, st>>>(chunks, descs, maps, vec, src, dst);
+	CTG_CUDA(cudaGetLastError());
+}
+
+}  // namespace ctg

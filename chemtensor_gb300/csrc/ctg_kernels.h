@@ -1,0 +1,130 @@
+// ctg_kernels.h - device work descriptors and launchers for the block-sparse engine.
+//
+// A block-sparse operation is lowered on the host (integer arithmetic only) into
+// flat descriptor arrays; the kernels below consume them. One launch covers all
+// dense blocks of one tensor operation.
+#pragma once
+
+#include "ctg_common.h"
+
+namespace ctg {
+
+// ---- grouped block GEMM ----------------------------------------------------
+// Output block: C[m x n] (row-major, leading dimension n) at c_off in the output
+// buffer equals the sum over its contributions of op(A) op(B), where A element
+// (i, kk) lives at a_off + i*sAm + kk*sAk and B element (kk, j) at
+// b_off + kk*sBk + j*sBn. Outputs with no contribution are written as zeros.
+struct GemmOut {
+	i64 c_off;
+	int m, n;
+	int c0, nc;        // contribution range in the contribution array
+};
+
+struct GemmContrib {
+	i64 a_off, b_off;
+	int k;
+	int sAm, sAk, sBk, sBn;
+};
+
+struct GemmTile {
+	int out;           // output block
+	int m0, n0;        // tile origin inside the output block
+};
+
+// tile classes (rows x cols of C per CTA)
+enum { TILE_S = 0, TILE_M = 1, TILE_L = 2, NUM_TILE_CLASSES = 3 };
+int tile_rows(int cls);
+int tile_cols(int cls);
+
+void launch_gemm_f64(int cls, int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
+                     const double* A, const double* B, double* C, cudaStream_t st);
+
+// ---- data movement -----------------------------------------------------------
+// Generic per-block permutation: dst block (row-major over dims) gathers
+// src[src_off + sum_i idx_i * sstr_i].
+struct PermDesc {
+	i64 src_off, dst_off, n;
+	int ndim;
+	int dims[6];
+	i64 sstr[6];
+};
+
+// Row map: for lead < nlead, j < nrow, t < ntrail:
+//   gather  (scatter == 0): dst[(lead*dst_rows + j)*ntrail + t]        = src[(lead*src_rows + map[j])*ntrail + t]
+//   scatter (scatter == 1): dst[(lead*dst_rows + map[j])*ntrail + t]   = src[(lead*src_rows + j)*ntrail + t]
+struct RowDesc {
+	i64 src_off, dst_off;
+	i64 nlead, ntrail;
+	int nrow, src_rows, dst_rows, scatter;
+	i64 map_off;
+};
+
+// Chunk of work for the copy kernels: descriptor index and first element.
+struct Chunk {
+	int desc;
+	int pad;
+	i64 start;
+};
+
+constexpr int COPY_CHUNK = 4096;
+
+void launch_permute(int nchunks, const Chunk* chunks, const PermDesc* descs, const double* src, double* dst, cudaStream_t st);
+void launch_rowmap(int nchunks, const Chunk* chunks, const RowDesc* descs, const i64* maps, const double* src, double* dst,
+                   cudaStream_t st);
+
+// Multiply entries along one axis of each block by vec[map[position]]:
+// entry (lead, p, trail) of a block of shape (nlead, nax, ntrail) is scaled by vec[map[map_off + p]].
+struct ScaleDesc {
+	i64 off, nlead, ntrail;
+	int nax, pad;
+	i64 map_off;
+};
+void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs, const i64* maps, const double* vec,
+                       const double* src, double* dst, cudaStream_t st);
+
+// ---- dense linear algebra per block ---------------------------------------------
+// One-sided Jacobi SVD of a row-major m x n block: u (m x k), s (k), vh (k x n), k = min(m, n),
+// singular values in descending order. Scratch holds max(m,n)*k + k*k doubles per block.
+struct SvdDesc {
+	i64 a_off, u_off, s_off, v_off, w_off;
+	int m, n;
+};
+void launch_svd_jacobi(int nblocks, const SvdDesc* descs, const double* a, double* u, double* s, double* vh,
+                       double* scratch, int* status, cudaStream_t st);
+
+// Householder RQ of a row-major m x n block: A = R Q with Q (k x n) orthonormal rows, R (m x k), k = min(m, n).
+// Scratch holds n*m + n*k + k doubles per block.
+struct RqDesc {
+	i64 a_off, r_off, q_off, w_off;
+	int m, n;
+};
+void launch_rq_householder(int nblocks, const RqDesc* descs, const double* a, double* r, double* q, double* scratch,
+                           cudaStream_t st);
+
+// ---- Lanczos (krylov.c:24-89) ------------------------------------------------------
+// Device-resident scalars of one Lanczos run.
+constexpr int LANCZOS_MAX = 32;     // largest maxiter_lanczos accepted
+
+struct LanczosScalars {
+	double alpha[LANCZOS_MAX];
+	double beta[LANCZOS_MAX];
+	double y[LANCZOS_MAX];  // Ritz coefficients of the lowest eigenpair
+	double lambda;         // lowest Ritz value
+	double nrm0;           // norm of the start vector
+	int numiter;
+	int stopped;
+	int status;            // 0 ok, -1 fewer iterations than eigenvalues, -2 tridiagonal solver failure
+	int pad;
+};
+
+constexpr int RED_BLOCKS = 608;     // 4 x 152 SMs: fixed grid for deterministic reductions
+
+void launch_lz_normalize_start(const double* v0, double* v, i64 n, double* partial, LanczosScalars* sc, cudaStream_t st);
+void launch_lz_alpha(const double* w, const double* vj, i64 n, int j, double* partial, LanczosScalars* sc, cudaStream_t st);
+void launch_lz_orth_beta(double* w, const double* vj, const double* vjm1, i64 n, int j, double* partial,
+                         LanczosScalars* sc, cudaStream_t st);
+void launch_lz_next(const double* w, double* vj1, i64 n, int j, const LanczosScalars* sc, cudaStream_t st);
+void launch_lz_tridiag(int maxiter, LanczosScalars* sc, cudaStream_t st);
+void launch_lz_ritz(const double* V, i64 n, int maxiter, const LanczosScalars* sc, double* out, cudaStream_t st);
+
+}  // namespace ctg

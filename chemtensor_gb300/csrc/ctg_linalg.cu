@@ -1,0 +1,519 @@
+// ctg_linalg.cu - FP64 dense linear algebra on the device: per-block SVD
+// (one-sided Jacobi), per-block RQ (Householder) and the Lanczos vector
+// operations with deterministic warp-shuffle reductions.
+#include <cfloat>
+
+#include "ctg_kernels.h"
+
+namespace ctg {
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+	// xor butterfly: every lane ends with the bitwise-identical total
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// ------------------------------------------------------------------------------------
+// block SVD: one-sided (Hestenes) Jacobi, one CTA per block.
+// Replaces LAPACK dgesvd in dense_tensor_svd_fill (dense_tensor.c:3538-3680); the
+// singular values agree to rounding, the singular vectors up to the usual sign /
+// degenerate-subspace freedom.
+// ------------------------------------------------------------------------------------
+
+constexpr int SVD_THREADS = 256;
+constexpr int SVD_MAX_SWEEPS = 60;
+
+__global__ void __launch_bounds__(SVD_THREADS)
+k_svd_jacobi(const SvdDesc* __restrict__ descs, const double* __restrict__ a, double* __restrict__ u, double* __restrict__ s,
+             double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status)
+{
+	const SvdDesc d = descs[blockIdx.x];
+	const int m = d.m, n = d.n;
+	const bool tall = m >= n;
+	const int M = tall ? m : n, N = tall ? n : m;
+	double* W = scratch + d.w_off;             // M x N, column-major
+	double* V = W + (i64)M * N;                // N x N, column-major
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = SVD_THREADS / 32;
+	const double* ab = a + d.a_off;
+	for (i64 e = tid; e < (i64)M * N; e += SVD_THREADS)
+	{
+		const i64 col = e / M, row = e % M;
+		W[e] = tall ? ab[row * n + col] : ab[col * n + row];
+	}
+	for (i64 e = tid; e < (i64)N * N; e += SVD_THREADS) V[e] = (e / N == e % N) ? 1.0 : 0.0;
+	__syncthreads();
+
+	__shared__ int rotated;
+	const double tol = sqrt((double)M) * DBL_EPSILON;
+	const int Np = N + (N & 1);
+	int sweep = 0;
+	for (; sweep < SVD_MAX_SWEEPS && N > 1; sweep++)
+	{
+		if (tid == 0) rotated = 0;
+		__syncthreads();
+		for (int rnd = 0; rnd < Np - 1; rnd++)
+		{
+			for (int pi = warp; pi < Np / 2; pi += nwarps)
+			{
+				// circle-method round-robin pairing
+				int p, q;
+				if (pi == 0) { p = rnd; q = Np - 1; }
+				else { p = (rnd + pi) % (Np - 1); q = (rnd - pi + (Np - 1)) % (Np - 1); }
+				if (p > q) { const int t = p; p = q; q = t; }
+				if (q >= N) continue;
+				double* wp = W + (i64)p * M;
+				double* wq = W + (i64)q * M;
+				double al = 0, be = 0, ga = 0;
+				for (int r = lane; r < M; r += 32)
+				{
+					const double x = wp[r], y = wq[r];
+					al = fma(x, x, al);
+					be = fma(y, y, be);
+					ga = fma(x, y, ga);
+				}
+				al = warp_sum(al);
+				be = warp_sum(be);
+				ga = warp_sum(ga);
+				if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be))
+				{
+					const double zeta = (be - al) / (2.0 * ga);
+					const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+					const double c = 1.0 / sqrt(1.0 + t * t);
+					const double sn = c * t;
+					for (int r = lane; r < M; r += 32)
+					{
+						const double x = wp[r], y = wq[r];
+						wp[r] = c * x - sn * y;
+						wq[r] = sn * x + c * y;
+					}
+					double* vp = V + (i64)p * N;
+					double* vq = V + (i64)q * N;
+					for (int r = lane; r < N; r += 32)
+					{
+						const double x = vp[r], y = vq[r];
+						vp[r] = c * x - sn * y;
+						vq[r] = sn * x + c * y;
+					}
+					if (lane == 0) rotated = 1;
+				}
+			}
+			__syncthreads();
+		}
+		if (!rotated) break;
+		__syncthreads();
+	}
+	if (tid == 0 && sweep >= SVD_MAX_SWEEPS) atomicExch(status, -1);
+
+	// column norms = singular values; rank by descending value (ties by column index)
+	extern __shared__ double sig[];            // N values
+	for (int c = warp; c < N; c += nwarps)
+	{
+		const double* wc = W + (i64)c * M;
+		double acc = 0;
+		for (int r = lane; r < M; r += 32) acc = fma(wc[r], wc[r], acc);
+		acc = warp_sum(acc);
+		if (lane == 0) sig[c] = sqrt(acc);
+	}
+	__syncthreads();
+	const int k = N;
+	for (int c = tid; c < N; c += SVD_THREADS)
+	{
+		int rank = 0;
+		const double sc = sig[c];
+		for (int c2 = 0; c2 < N; c2++)
+			if (sig[c2] > sc || (sig[c2] == sc && c2 < c)) rank++;
+		s[d.s_off + rank] = sc;
+	}
+	__syncthreads();
+	// write u (m x k) and vh (k x n), row-major
+	for (int c = warp; c < N; c += nwarps)
+	{
+		const double sc = sig[c];
+		int rank = 0;
+		for (int c2 = 0; c2 < N; c2++)
+			if (sig[c2] > sc || (sig[c2] == sc && c2 < c)) rank++;
+		const double inv = sc > 0 ? 1.0 / sc : 0.0;
+		const double* wc = W + (i64)c * M;
+		const double* vc = V + (i64)c * N;
+		if (tall)
+		{
+			for (int r = lane; r < m; r += 32) u[d.u_off + (i64)r * k + rank] = wc[r] * inv;
+			for (int r = lane; r < n; r += 32) vh[d.v_off + (i64)rank * n + r] = vc[r];
+		}
+		else
+		{
+			for (int r = lane; r < m; r += 32) u[d.u_off + (i64)r * k + rank] = vc[r];
+			for (int r = lane; r < n; r += 32) vh[d.v_off + (i64)rank * n + r] = wc[r] * inv;
+		}
+	}
+}
+
+void launch_svd_jacobi(int nblocks, const SvdDesc* descs, const double* a, double* u, double* s, double* vh,
+                       double* scratch, int* status, cudaStream_t st)
+{
+	if (nblocks <= 0) return;
+	// dynamic shared memory: singular values of the largest block (at most 4096 columns)
+	k_svd_jacobi<<<nblocks, SVD_THREADS, 4096 * sizeof(double), st>>>(descs, a, u, s, vh, scratch, status);
+	CTG_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------------------------
+// block RQ through a Householder QR of the transpose, one CTA per block.
+// Replaces LAPACK dgerqf + dorgrq in dense_tensor_rq_fill (dense_tensor.c:2680-2880):
+// A = R Q with orthonormal rows of Q; R is the transpose of the triangular QR factor.
+// ------------------------------------------------------------------------------------
+
+constexpr int RQ_THREADS = 256;
+
+__device__ double block_sum(double v, double* red)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	v = warp_sum(v);
+	__syncthreads();
+	if (lane == 0) red[warp] = v;
+	__syncthreads();
+	double t = 0;
+	for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+	return t;
+}
+
+__global__ void __launch_bounds__(RQ_THREADS)
+k_rq_householder(const RqDesc* __restrict__ descs, const double* __restrict__ a, double* __restrict__ r,
+                 double* __restrict__ q, double* __restrict__ scratch)
+{
+	__shared__ double red[RQ_THREADS / 32];
+	__shared__ double sh_beta, sh_tau, sh_scale;
+	const RqDesc d = descs[blockIdx.x];
+	const int m = d.m, n = d.n;
+	const int k = min(m, n);
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = RQ_THREADS / 32;
+	// B = A^T (n x m) column-major equals A row-major: column c of B is row c of A
+	double* B = scratch + d.w_off;             // n x m
+	double* Q = B + (i64)n * m;                // n x k
+	double* tau = Q + (i64)n * k;              // k
+	const double* ab = a + d.a_off;
+	for (i64 e = tid; e < (i64)n * m; e += RQ_THREADS) B[e] = ab[e];
+	__syncthreads();
+	for (int c = 0; c < k; c++)
+	{
+		double* bc = B + (i64)c * n;
+		double part = 0;
+		for (int i = c + 1 + tid; i < n; i += RQ_THREADS) part = fma(bc[i], bc[i], part);
+		const double xnorm2 = block_sum(part, red);
+		if (tid == 0)
+		{
+			const double alpha = bc[c];
+			if (xnorm2 == 0.0)
+			{
+				sh_tau = 0.0;
+				sh_beta = alpha;
+				sh_scale = 0.0;
+			}
+			else
+			{
+				const double beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
+				sh_tau = (beta - alpha) / beta;
+				sh_beta = beta;
+				sh_scale = 1.0 / (alpha - beta);
+			}
+		}
+		__syncthreads();
+		const double tc = sh_tau;
+		for (int i = c + 1 + tid; i < n; i += RQ_THREADS) bc[i] *= sh_scale;
+		__syncthreads();
+		if (tid == 0) { bc[c] = sh_beta; tau[c] = tc; }
+		__syncthreads();
+		// apply H = I - tau v v^T (v = (1, bc[c+1:])) to the remaining columns
+		if (tc != 0.0)
+		{
+			for (int c2 = c + 1 + warp; c2 < m; c2 += nwarps)
+			{
+				double* b2 = B + (i64)c2 * n;
+				double acc = 0;
+				for (int i = c + lane; i < n; i += 32) acc = fma(i == c ? 1.0 : bc[i], b2[i], acc);
+				acc = warp_sum(acc) * tc;
+				for (int i = c + lane; i < n; i += 32) b2[i] -= acc * (i == c ? 1.0 : bc[i]);
+			}
+		}
+		__syncthreads();
+	}
+	// Q1 = H_0 ... H_{k-1} E (n x k), accumulated backwards, column-major
+	for (i64 e = tid; e < (i64)n * k; e += RQ_THREADS) Q[e] = (e / n == e % n) ? 1.0 : 0.0;
+	__syncthreads();
+	for (int c = k - 1; c >= 0; c--)
+	{
+		const double tc = tau[c];
+		const double* bc = B + (i64)c * n;
+		if (tc != 0.0)
+		{
+			for (int j = warp; j < k; j += nwarps)
+			{
+				double* qj = Q + (i64)j * n;
+				double acc = 0;
+				for (int i = c + lane; i < n; i += 32) acc = fma(i == c ? 1.0 : bc[i], qj[i], acc);
+				acc = warp_sum(acc) * tc;
+				for (int i = c + lane; i < n; i += 32) qj[i] -= acc * (i == c ? 1.0 : bc[i]);
+			}
+		}
+		__syncthreads();
+	}
+	// R = R1^T (m x k): R[i][j] = R1[j][i] = B(col i, row j) for i >= j
+	for (i64 e = tid; e < (i64)m * k; e += RQ_THREADS)
+	{
+		const i64 i = e / k, j = e % k;
+		r[d.r_off + e] = (i >= j) ? B[i * n + j] : 0.0;
+	}
+	// Q = Q1^T (k x n)
+	for (i64 e = tid; e < (i64)k * n; e += RQ_THREADS)
+	{
+		const i64 j = e / n, i = e % n;
+		q[d.q_off + e] = Q[j * n + i];
+	}
+}
+
+void launch_rq_householder(int nblocks, const RqDesc* descs, const double* a, double* r, double* q, double* scratch,
+                           cudaStream_t st)
+{
+	if (nblocks <= 0) return;
+	k_rq_householder<<<nblocks, RQ_THREADS, 0, st>>>(descs, a, r, q, scratch);
+	CTG_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------------------------
+// Lanczos (lanczos_iteration_d, krylov.c:24-89; eigensystem_krylov_symmetric, :172-251)
+// Reductions: fixed grid, fixed per-thread stride, fixed tree, so results are
+// reproducible run to run.
+// ------------------------------------------------------------------------------------
+
+constexpr int RED_THREADS = 256;
+
+__device__ void block_partial(double v, double* partial)
+{
+	__shared__ double red[RED_THREADS / 32];
+	v = warp_sum(v);
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		double t = 0;
+		for (int w = 0; w < RED_THREADS / 32; w++) t += red[w];
+		partial[blockIdx.x] = t;
+	}
+}
+
+__device__ double final_sum(const double* partial)
+{
+	__shared__ double red[RED_THREADS / 32];
+	double v = 0;
+	for (int i = threadIdx.x; i < RED_BLOCKS; i += RED_THREADS) v += partial[i];
+	v = warp_sum(v);
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+	__syncthreads();
+	double t = 0;
+	for (int w = 0; w < RED_THREADS / 32; w++) t += red[w];
+	return t;
+}
+
+__global__ void k_partial_dot(const double* __restrict__ x, const double* __restrict__ y, i64 n, double* partial,
+                              const LanczosScalars* sc)
+{
+	if (sc != nullptr && sc->stopped) return;
+	double v = 0;
+	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += (i64)RED_BLOCKS * RED_THREADS) v = fma(x[i], y[i], v);
+	block_partial(v, partial);
+}
+
+__global__ void k_start_final(const double* partial, LanczosScalars* sc)
+{
+	const double t = final_sum(partial);
+	if (threadIdx.x == 0)
+	{
+		sc->nrm0 = sqrt(t);
+		sc->stopped = 0;
+		sc->numiter = 0;
+		sc->status = 0;
+	}
+}
+
+__global__ void k_scale_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, const LanczosScalars* sc)
+{
+	const double inv = 1.0 / sc->nrm0;
+	for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) v[i] = inv * v0[i];
+}
+
+void launch_lz_normalize_start(const double* v0, double* v, i64 n, double* partial, LanczosScalars* sc, cudaStream_t st)
+{
+	k_partial_dot<<<RED_BLOCKS, RED_THREADS, 0, st>>>(v0, v0, n, partial, nullptr);
+	k_start_final<<<1, RED_THREADS, 0, st>>>(partial, sc);
+	k_scale_start<<<RED_BLOCKS, 256, 0, st>>>(v0, v, n, sc);
+	CTG_CUDA(cudaGetLastError());
+}
+
+__global__ void k_alpha_final(const double* partial, LanczosScalars* sc, int j)
+{
+	if (sc->stopped) return;
+	const double t = final_sum(partial);
+	if (threadIdx.x == 0) sc->alpha[j] = t;
+}
+
+void launch_lz_alpha(const double* w, const double* vj, i64 n, int j, double* partial, LanczosScalars* sc, cudaStream_t st)
+{
+	k_partial_dot<<<RED_BLOCKS, RED_THREADS, 0, st>>>(w, vj, n, partial, sc);
+	k_alpha_final<<<1, RED_THREADS, 0, st>>>(partial, sc, j);
+	CTG_CUDA(cudaGetLastError());
+}
+
+__global__ void k_orth_partial(double* __restrict__ w, const double* __restrict__ vj, const double* __restrict__ vjm1, i64 n,
+                               int j, double* partial, const LanczosScalars* sc)
+{
+	if (sc->stopped) return;
+	const double al = sc->alpha[j];
+	const double be = j > 0 ? sc->beta[j - 1] : 0.0;
+	double v = 0;
+	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += (i64)RED_BLOCKS * RED_THREADS)
+	{
+		// w = w' - alpha_j v_j - beta_{j-1} v_{j-1}, evaluated as in krylov.c:44-53
+		const double x = (j > 0) ? w[i] - (al * vj[i] + be * vjm1[i]) : w[i] - al * vj[i];
+		w[i] = x;
+		v = fma(x, x, v);
+	}
+	block_partial(v, partial);
+}
+
+__global__ void k_beta_final(const double* partial, LanczosScalars* sc, int j, i64 n)
+{
+	if (sc->stopped) return;
+	const double t = final_sum(partial);
+	if (threadIdx.x == 0)
+	{
+		const double b = sqrt(t);
+		sc->beta[j] = b;
+		if (b < 100.0 * (double)n * DBL_EPSILON)
+		{
+			sc->stopped = 1;
+			sc->numiter = j + 1;
+		}
+	}
+}
+
+void launch_lz_orth_beta(double* w, const double* vj, const double* vjm1, i64 n, int j, double* partial,
+                         LanczosScalars* sc, cudaStream_t st)
+{
+	k_orth_partial<<<RED_BLOCKS, RED_THREADS, 0, st>>>(w, vj, vjm1, n, j, partial, sc);
+	k_beta_final<<<1, RED_THREADS, 0, st>>>(partial, sc, j, n);
+	CTG_CUDA(cudaGetLastError());
+}
+
+__global__ void k_next(const double* __restrict__ w, double* __restrict__ vj1, i64 n, int j, const LanczosScalars* sc)
+{
+	if (sc->stopped) return;
+	const double inv = 1.0 / sc->beta[j];
+	for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) vj1[i] = inv * w[i];
+}
+
+void launch_lz_next(const double* w, double* vj1, i64 n, int j, const LanczosScalars* sc, cudaStream_t st)
+{
+	k_next<<<RED_BLOCKS, 256, 0, st>>>(w, vj1, n, j, sc);
+	CTG_CUDA(cudaGetLastError());
+}
+
+// Lowest eigenpair of the k x k symmetric tridiagonal Lanczos matrix by cyclic
+// Jacobi rotations (replaces LAPACK dsteqr, krylov.c:230). One thread; k <= LANCZOS_MAX.
+__global__ void k_tridiag(int maxiter, LanczosScalars* sc)
+{
+	if (threadIdx.x != 0) return;
+	if (!sc->stopped) sc->numiter = maxiter;
+	const int k = sc->numiter;
+	if (k < 1) { sc->status = -1; return; }
+	// dense symmetric matrix in local memory, eigenvectors accumulated in Z
+	double A[LANCZOS_MAX * LANCZOS_MAX], Z[LANCZOS_MAX * LANCZOS_MAX];
+	if (k > LANCZOS_MAX) { sc->status = -2; return; }
+	for (int i = 0; i < k; i++)
+		for (int j = 0; j < k; j++)
+		{
+			double v = 0;
+			if (i == j) v = sc->alpha[i];
+			else if (j == i + 1) v = sc->beta[i];
+			else if (i == j + 1) v = sc->beta[j];
+			A[i * k + j] = v;
+			Z[i * k + j] = (i == j) ? 1.0 : 0.0;
+		}
+	for (int sweep = 0; sweep < 100; sweep++)
+	{
+		double off = 0, diag = 0;
+		for (int i = 0; i < k; i++)
+		{
+			diag += A[i * k + i] * A[i * k + i];
+			for (int j = i + 1; j < k; j++) off += A[i * k + j] * A[i * k + j];
+		}
+		if (off <= DBL_EPSILON * DBL_EPSILON * 1e-2 * diag || off == 0.0) break;
+		for (int p = 0; p < k - 1; p++)
+			for (int q = p + 1; q < k; q++)
+			{
+				const double apq = A[p * k + q];
+				if (apq == 0.0) continue;
+				const double app = A[p * k + p], aqq = A[q * k + q];
+				const double theta = (aqq - app) / (2.0 * apq);
+				const double t = copysign(1.0, theta) / (fabs(theta) + sqrt(1.0 + theta * theta));
+				const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
+				for (int r = 0; r < k; r++)
+				{
+					const double arp = A[r * k + p], arq = A[r * k + q];
+					A[r * k + p] = c * arp - s * arq;
+					A[r * k + q] = s * arp + c * arq;
+				}
+				for (int r = 0; r < k; r++)
+				{
+					const double apr = A[p * k + r], aqr = A[q * k + r];
+					A[p * k + r] = c * apr - s * aqr;
+					A[q * k + r] = s * apr + c * aqr;
+				}
+				A[p * k + q] = 0.0;
+				A[q * k + p] = 0.0;
+				for (int r = 0; r < k; r++)
+				{
+					const double zrp = Z[r * k + p], zrq = Z[r * k + q];
+					Z[r * k + p] = c * zrp - s * zrq;
+					Z[r * k + q] = s * zrp + c * zrq;
+				}
+			}
+	}
+	int imin = 0;
+	for (int i = 1; i < k; i++)
+		if (A[i * k + i] < A[imin * k + imin]) imin = i;
+	sc->lambda = A[imin * k + imin];
+	// deterministic sign: largest-magnitude component positive
+	int imax = 0;
+	for (int i = 1; i < k; i++)
+		if (fabs(Z[i * k + imin]) > fabs(Z[imax * k + imin])) imax = i;
+	const double sgn = Z[imax * k + imin] < 0 ? -1.0 : 1.0;
+	for (int i = 0; i < k; i++) sc->y[i] = sgn * Z[i * k + imin];
+}
+
+void launch_lz_tridiag(int maxiter, LanczosScalars* sc, cudaStream_t st)
+{
+	k_tridiag<<<1, 32, 0, st>>>(maxiter, sc);
+	CTG_CUDA(cudaGetLastError());
+}
+
+__global__ void k_ritz(const double* __restrict__ V, i64 n, const LanczosScalars* sc, double* __restrict__ out)
+{
+	const int k = sc->numiter;
+	for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+	{
+		double acc = 0;
+		for (int j = 0; j < k; j++) acc = fma(V[(i64)j * n + i], sc->y[j], acc);
+		out[i] = acc;
+	}
+}
+
+void launch_lz_ritz(const double* V, i64 n, int maxiter, const LanczosScalars* sc, double* out, cudaStream_t st)
+{
+	(void)maxiter;
+	k_ritz<<<RED_BLOCKS, 256, 0, st>>>(V, n, sc, out);
+	CTG_CUDA(cudaGetLastError());
+}
+
+}  // namespace ctg

@@ -1,0 +1,219 @@
+// ctg_meta.cpp - block structure rules (integer arithmetic only).
+#include "ctg_meta.h"
+
+#include <algorithm>
+#include <numeric>
+
+namespace ctg {
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char* what, const char* file, int line)
+{
+	char buf[512];
+	snprintf(buf, sizeof(buf), "CUDA error %d (%s) in %s at %s:%d", (int)e, cudaGetErrorString(e), what, file, line);
+	throw CudaError(buf);
+}
+
+i64 Meta::block_size(int b) const
+{
+	i64 p = 1;
+	for (int i = 0; i < ndim; i++) p *= bdim[(size_t)b * ndim + i];
+	return p;
+}
+
+i64 Meta::linear(const i64* idx) const
+{
+	i64 k = 0;
+	for (int i = 0; i < ndim; i++) k = k * nb[i] + idx[i];
+	return k;
+}
+
+int Meta::find(const i64* idx) const
+{
+	for (int i = 0; i < ndim; i++)
+		if (idx[i] < 0 || idx[i] >= nb[i]) return -1;
+	const i64 k = linear(idx);
+	if (!lut.empty()) return lut[(size_t)k];
+	auto it = lut_map.find(k);
+	return it == lut_map.end() ? -1 : it->second;
+}
+
+int Meta::find_q(int ax, q32 q) const
+{
+	const auto& v = qb[ax];
+	auto it = std::lower_bound(v.begin(), v.end(), q);
+	if (it == v.end() || *it != q) return -1;
+	return (int)(it - v.begin());
+}
+
+bool Meta::same_structure(const Meta& o) const
+{
+	return ndim == o.ndim && dim == o.dim && dir == o.dir && ql == o.ql;
+}
+
+Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::vector<q32>>& ql)
+{
+	CTG_CHECK(ndim >= 1 && ndim <= 8, "tensor degree out of range");
+	Meta m;
+	m.ndim = ndim;
+	m.dim.assign(dim, dim + ndim);
+	m.dir.assign(dir, dir + ndim);
+	m.ql = ql;
+	m.qb.resize(ndim);
+	m.bd.resize(ndim);
+	m.pos.resize(ndim);
+	m.blk.resize(ndim);
+	m.nb.resize(ndim);
+	for (int a = 0; a < ndim; a++)
+	{
+		CTG_CHECK(dim[a] > 0 && (i64)ql[a].size() == dim[a], "logical quantum numbers do not match the dimension");
+		std::vector<q32> u(ql[a]);
+		std::sort(u.begin(), u.end());
+		u.erase(std::unique(u.begin(), u.end()), u.end());
+		m.qb[a] = u;
+		m.nb[a] = (i64)u.size();
+		m.bd[a].assign(u.size(), 0);
+		m.pos[a].resize(dim[a]);
+		m.blk[a].resize(dim[a]);
+		for (i64 j = 0; j < dim[a]; j++)
+		{
+			const int b = (int)(std::lower_bound(u.begin(), u.end(), ql[a][j]) - u.begin());
+			m.blk[a][j] = b;
+			m.pos[a][j] = m.bd[a][b]++;
+		}
+	}
+	// enumerate allowed blocks in row-major order: for every prefix over the first
+	// ndim-1 axes, at most one quantum number of the last axis makes the sum vanish
+	const int last = ndim - 1;
+	i64 nprefix = 1;
+	for (int a = 0; a < last; a++) nprefix *= m.nb[a];
+	std::vector<i64> idx(ndim, 0);
+	for (i64 p = 0; p < nprefix; p++)
+	{
+		i64 r = p;
+		long long qs = 0;
+		for (int a = last - 1; a >= 0; a--) { idx[a] = r % m.nb[a]; r /= m.nb[a]; }
+		for (int a = 0; a < last; a++) qs += (long long)dir[a] * m.qb[a][idx[a]];
+		const long long qneed = -(long long)dir[last] * qs;
+		if (qneed < INT32_MIN || qneed > INT32_MAX) continue;
+		const int j = m.find_q(last, (q32)qneed);
+		if (j < 0) continue;
+		idx[last] = j;
+		for (int a = 0; a < ndim; a++)
+		{
+			m.bidx.push_back(idx[a]);
+			m.bdim.push_back(m.bd[a][idx[a]]);
+		}
+		m.nblocks++;
+	}
+	m.boff.resize(m.nblocks);
+	i64 off = 0;
+	for (int b = 0; b < m.nblocks; b++) { m.boff[b] = off; off += m.block_size(b); }
+	m.nnz = off;
+	i64 total = 1;
+	bool small = true;
+	for (int a = 0; a < ndim; a++)
+	{
+		total *= m.nb[a];
+		if (total > (i64)1 << 24) { small = false; break; }
+	}
+	if (small)
+	{
+		m.lut.assign((size_t)total, -1);
+		for (int b = 0; b < m.nblocks; b++) m.lut[(size_t)m.linear(m.index(b))] = b;
+	}
+	else
+	{
+		for (int b = 0; b < m.nblocks; b++) m.lut_map[m.linear(m.index(b))] = b;
+	}
+	return m;
+}
+
+Meta dot_result_meta(const Meta& s, int axs, const Meta& t, int axt, int nmult)
+{
+	const int shift_s = (axs == AX_LEADING ? 0 : s.ndim - nmult);
+	const int shift_t = (axt == AX_LEADING ? 0 : t.ndim - nmult);
+	for (int i = 0; i < nmult; i++)
+	{
+		CTG_CHECK(s.dim[shift_s + i] == t.dim[shift_t + i], "dot: contracted dimensions differ");
+		CTG_CHECK(s.dir[shift_s + i] == -t.dir[shift_t + i], "dot: contracted axis directions must be reversed");
+		CTG_CHECK(s.ql[shift_s + i] == t.ql[shift_t + i], "dot: contracted quantum numbers differ");
+	}
+	const int off_s = (axs == AX_LEADING ? nmult : 0);
+	const int off_t = (axt == AX_LEADING ? nmult : 0);
+	const int nfs = s.ndim - nmult, nft = t.ndim - nmult;
+	std::vector<i64> dim;
+	std::vector<int> dir;
+	std::vector<std::vector<q32>> ql;
+	for (int i = 0; i < nfs; i++) { dim.push_back(s.dim[off_s + i]); dir.push_back(s.dir[off_s + i]); ql.push_back(s.ql[off_s + i]); }
+	for (int i = 0; i < nft; i++) { dim.push_back(t.dim[off_t + i]); dir.push_back(t.dir[off_t + i]); ql.push_back(t.ql[off_t + i]); }
+	CTG_CHECK(!dim.empty(), "dot: scalar results are not on the DMRG path");
+	return make_meta((int)dim.size(), dim.data(), dir.data(), ql);
+}
+
+Meta transpose_meta(const Meta& t, const int* perm)
+{
+	std::vector<i64> dim(t.ndim);
+	std::vector<int> dir(t.ndim);
+	std::vector<std::vector<q32>> ql(t.ndim);
+	for (int i = 0; i < t.ndim; i++) { dim[i] = t.dim[perm[i]]; dir[i] = t.dir[perm[i]]; ql[i] = t.ql[perm[i]]; }
+	return make_meta(t.ndim, dim.data(), dir.data(), ql);
+}
+
+Meta flatten_meta(const Meta& t, int ax, int newdir)
+{
+	CTG_CHECK(ax >= 0 && ax + 1 < t.ndim, "flatten: axis out of range");
+	std::vector<i64> dim;
+	std::vector<int> dir;
+	std::vector<std::vector<q32>> ql;
+	for (int i = 0; i < ax; i++) { dim.push_back(t.dim[i]); dir.push_back(t.dir[i]); ql.push_back(t.ql[i]); }
+	const i64 d0 = t.dim[ax], d1 = t.dim[ax + 1];
+	std::vector<q32> qf((size_t)(d0 * d1));
+	for (i64 j = 0; j < d0; j++)
+		for (i64 k = 0; k < d1; k++)
+			qf[(size_t)(j * d1 + k)] = newdir * (t.dir[ax] * t.ql[ax][j] + t.dir[ax + 1] * t.ql[ax + 1][k]);
+	dim.push_back(d0 * d1);
+	dir.push_back(newdir);
+	ql.push_back(qf);
+	for (int i = ax + 2; i < t.ndim; i++) { dim.push_back(t.dim[i]); dir.push_back(t.dir[i]); ql.push_back(t.ql[i]); }
+	return make_meta((int)dim.size(), dim.data(), dir.data(), ql);
+}
+
+Meta split_meta(const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
+{
+	CTG_CHECK(nd[0] * nd[1] == t.dim[ax], "split: dimensions do not multiply to the original");
+	for (i64 j = 0; j < nd[0]; j++)
+		for (i64 k = 0; k < nd[1]; k++)
+			CTG_CHECK(t.dir[ax] * t.ql[ax][(size_t)(j * nd[1] + k)] == ndir[0] * nq[0][j] + ndir[1] * nq[1][k],
+			          "split: quantum numbers inconsistent with the original axis");
+	std::vector<i64> dim;
+	std::vector<int> dir;
+	std::vector<std::vector<q32>> ql;
+	for (int i = 0; i < ax; i++) { dim.push_back(t.dim[i]); dir.push_back(t.dir[i]); ql.push_back(t.ql[i]); }
+	for (int h = 0; h < 2; h++) { dim.push_back(nd[h]); dir.push_back(ndir[h]); ql.push_back(nq[h]); }
+	for (int i = ax + 1; i < t.ndim; i++) { dim.push_back(t.dim[i]); dir.push_back(t.dir[i]); ql.push_back(t.ql[i]); }
+	return make_meta((int)dim.size(), dim.data(), dir.data(), ql);
+}
+
+Meta slice_meta(const Meta& t, int ax, const std::vector<i64>& ind)
+{
+	CTG_CHECK(!ind.empty(), "slice: empty index list");
+	std::vector<std::vector<q32>> ql = t.ql;
+	std::vector<i64> dim = t.dim;
+	ql[ax].resize(ind.size());
+	for (size_t j = 0; j < ind.size(); j++)
+	{
+		CTG_CHECK(ind[j] >= 0 && ind[j] < t.dim[ax], "slice: index out of range");
+		ql[ax][j] = t.ql[ax][(size_t)ind[j]];
+	}
+	dim[ax] = (i64)ind.size();
+	return make_meta(t.ndim, dim.data(), t.dir.data(), ql);
+}
+
+Meta reversed_meta(const Meta& t)
+{
+	Meta r = t;
+	for (auto& d : r.dir) d = -d;
+	return r;
+}
+
+}  // namespace ctg

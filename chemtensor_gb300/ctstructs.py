@@ -344,3 +344,47 @@ def free_mps(c: MPS) -> None:
 
 def free_mpo(c: MPO) -> None:
     _free_chain(c)
+
+
+# ---------------------------------------------------------------------------
+# flat array form (golden fixtures, .npz)
+# ---------------------------------------------------------------------------
+
+def bst_to_arrays(prefix: str, t: BlockSparse) -> dict:
+    out = {f"{prefix}_dim": np.array(t.dim_logical, dtype=np.int64),
+           f"{prefix}_dir": np.array(t.axis_dir, dtype=np.int32),
+           f"{prefix}_data": t.serialize().astype(np.float64)}
+    for i, q in enumerate(t.qnums_logical):
+        out[f"{prefix}_q{i}"] = np.asarray(q, dtype=np.int32)
+    return out
+
+
+def bst_from_arrays(prefix: str, arr) -> BlockSparse:
+    dim = [int(x) for x in arr[f"{prefix}_dim"]]
+    dirs = [int(x) for x in arr[f"{prefix}_dir"]]
+    qn = [np.asarray(arr[f"{prefix}_q{i}"], dtype=np.int32) for i in range(len(dim))]
+    t = BlockSparse(dim, dirs, qn)
+    data = np.asarray(arr[f"{prefix}_data"], dtype=np.float64)
+    off = 0
+    for idx in t.allowed:
+        shp = t.block_shape(idx)
+        n = int(np.prod(shp))
+        t.blocks[idx] = data[off:off + n].reshape(shp).copy()
+        off += n
+    if off != len(data):
+        raise ValueError(f"{prefix}: {len(data)} entries for {off} block entries")
+    return t
+
+
+def chain_to_arrays(prefix: str, ch: Chain) -> dict:
+    out = {f"{prefix}_nsites": np.array(ch.nsites), f"{prefix}_d": np.array(ch.d),
+           f"{prefix}_qsite": np.asarray(ch.qsite, dtype=np.int32)}
+    for i, t in enumerate(ch.tensors):
+        out.update(bst_to_arrays(f"{prefix}{i}", t))
+    return out
+
+
+def chain_from_arrays(prefix: str, arr) -> Chain:
+    n = int(arr[f"{prefix}_nsites"])
+    ts = [bst_from_arrays(f"{prefix}{i}", arr) for i in range(n)]
+    return Chain(ts, np.asarray(arr[f"{prefix}_qsite"], dtype=np.int32), int(arr[f"{prefix}_d"]))

@@ -1,0 +1,113 @@
+"""Loader and ctypes signatures of libctgpu.so (declared in include/ctgpu.h).
+
+The library is built in-tree by ``chemtensor_gb300.build``. There is no
+fallback: if the library is missing, importing this module raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import ctstructs as cs
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libctgpu.so")
+
+# exported C symbols (include/ctgpu.h)
+EXPORTS = [
+    "dmrg_twosite",
+    "ctgpu_set_precision",
+    "ctgpu_set_device",
+    "ctgpu_get_last_stats",
+    "ctgpu_last_error",
+    "ctgpu_construct_random_mps",
+    "ctgpu_randn_sequence",
+    "ctgpu_block_sparse_tensor_dot",
+    "ctgpu_block_sparse_tensor_transpose",
+    "ctgpu_apply_local_hamiltonian",
+    "ctgpu_contraction_operator_step_left",
+    "ctgpu_contraction_operator_step_right",
+    "ctgpu_block_sparse_tensor_svd_values",
+    "ctgpu_delete_block_sparse_tensor",
+]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("wall_s", C.c_double), ("upload_s", C.c_double), ("download_s", C.c_double),
+        ("setup_s", C.c_double), ("sweep_s", C.c_double), ("lanczos_ms", C.c_double),
+        ("split_ms", C.c_double), ("env_ms", C.c_double), ("matvec_flops", C.c_double),
+        ("total_gemm_flops", C.c_double), ("matvecs", C.c_long), ("kernel_launches", C.c_long),
+        ("sweeps", C.c_int), ("max_bond_dim", C.c_int64),
+    ]
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing; build it with `python -m chemtensor_gb300.build`")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    lib.dmrg_twosite.argtypes = [P, C.c_int, C.c_int, C.c_double, C.c_int64, P, P, P]
+    lib.dmrg_twosite.restype = C.c_int
+    lib.ctgpu_set_precision.argtypes = [C.c_int]
+    lib.ctgpu_set_device.argtypes = [C.c_int]
+    lib.ctgpu_get_last_stats.argtypes = [P]
+    lib.ctgpu_last_error.restype = C.c_char_p
+    lib.ctgpu_construct_random_mps.argtypes = [C.c_int, C.c_int64, P, C.c_int32, C.c_int64, C.c_uint64, P]
+    lib.ctgpu_randn_sequence.argtypes = [C.c_uint64, C.c_int, P]
+    lib.ctgpu_randn_sequence.restype = None
+    lib.ctgpu_block_sparse_tensor_dot.argtypes = [P, C.c_int, P, C.c_int, C.c_int, P]
+    lib.ctgpu_block_sparse_tensor_transpose.argtypes = [P, P, P]
+    lib.ctgpu_apply_local_hamiltonian.argtypes = [P] * 5
+    lib.ctgpu_contraction_operator_step_left.argtypes = [P] * 4
+    lib.ctgpu_contraction_operator_step_right.argtypes = [P] * 4
+    lib.ctgpu_block_sparse_tensor_svd_values.argtypes = [P, P, P]
+    lib.ctgpu_delete_block_sparse_tensor.argtypes = [P]
+    lib.ctgpu_delete_block_sparse_tensor.restype = None
+    return lib
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = load()
+    return _lib
+
+
+def last_error() -> str:
+    return lib().ctgpu_last_error().decode()
+
+
+def last_stats() -> dict:
+    s = Stats()
+    lib().ctgpu_get_last_stats(C.byref(s))
+    return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+
+def set_precision(p: int) -> int:
+    return lib().ctgpu_set_precision(int(p))
+
+
+def random_mps(nsites: int, d: int, qsite, qnum_sector: int, max_vdim: int, seed: int) -> cs.MPS:
+    """Reference-identical seeded random MPS as a C struct (caller frees with free_mps)."""
+    q = np.ascontiguousarray(qsite, dtype=np.int32)
+    m = cs.MPS()
+    ret = lib().ctgpu_construct_random_mps(nsites, d, q.ctypes.data, int(qnum_sector), max_vdim, seed, C.byref(m))
+    if ret != 0:
+        raise ValueError("invalid random MPS parameters")
+    return m
+
+
+def dmrg_twosite(mpo: cs.MPO, psi: cs.MPS, num_sweeps: int, maxiter_lanczos: int, tol_split: float, max_vdim: int):
+    """Call the C-ABI dmrg_twosite; psi is updated in place. Returns (ret, en_sweeps, entropy)."""
+    en = np.zeros(max(num_sweeps, 1))
+    ent = np.zeros(max(mpo.nsites - 1, 1))
+    ret = lib().dmrg_twosite(C.byref(mpo), num_sweeps, maxiter_lanczos, tol_split, max_vdim, C.byref(psi),
+                             en.ctypes.data, ent.ctypes.data)
+    return ret, en[:num_sweeps], ent[:mpo.nsites - 1]

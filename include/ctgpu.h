@@ -1,0 +1,113 @@
+/* ctgpu.h - C ABI of the GB300 implementation of chemtensor's two-site DMRG path.
+ *
+ * Drop-in boundary: dmrg_twosite below has the reference's exact name,
+ * signature, argument meaning, ownership rules and return codes, so a C caller
+ * of the reference (python/pymodule.c:3317, perf/perf_dmrg.c:94,
+ * examples/dmrg/basic_dmrg_fermi_hubbard.c:79) links libctgpu.so in place of
+ * the reference's dmrg.c and is otherwise unchanged. All other entry points
+ * carry a ctgpu_ prefix so that the library can sit beside the reference's
+ * own symbols in one process.
+ *
+ * Return codes (reference: src/util/krylov.c:220-236, src/algorithm/dmrg.c:310-355):
+ *    0  success
+ *   -1  Lanczos breakdown before the first eigenvalue, or SVD / RQ failure
+ *   -2  tridiagonal eigensolver failure
+ *   -5  invalid arguments or a CUDA runtime error (message via ctgpu_last_error);
+ *       this code has no counterpart in the reference, where such cases are assert()s
+ *
+ * Threading: every host thread gets its own CUDA stream and memory pool, so
+ * independent calls from several threads run concurrently on the GPU.
+ */
+#ifndef CTGPU_H
+#define CTGPU_H
+
+#include "ct_structs.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Two-site DMRG ground-state search.
+ * Replaces dmrg_twosite, src/algorithm/dmrg.c:262-399 (declared in include/algorithm/dmrg.h:11-12).
+ * hamiltonian: read only. psi: in/out; its site tensors are freed with free() and replaced by
+ * tensors allocated with aligned_alloc(16, .), as the reference does. en_sweeps[num_sweeps] and
+ * entropy[nsites-1] are caller-allocated; entropy[i] is written on the right-to-left pass. */
+int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int maxiter_lanczos,
+	const double tol_split, const ct_long max_vdim, struct mps* psi, double* en_sweeps, double* entropy);
+
+/* Arithmetic of the bulk block GEMMs for subsequent calls from this thread.
+ * 0 = FP64 (plain path), 1 = split-BF16 with FP32 accumulation, 2 = TF32 with FP32 accumulation.
+ * The reference has no such setting (it always computes in FP64). Returns the previous value. */
+int ctgpu_set_precision(int precision);
+
+/* CUDA device used by subsequent calls from this thread. Returns the previous device. */
+int ctgpu_set_device(int device);
+
+/* Measurements of the most recent dmrg_twosite call in this thread. */
+struct ctgpu_stats
+{
+	double wall_s;            /* host wall time of the whole call */
+	double upload_s;          /* host structs -> HBM */
+	double download_s;        /* HBM -> host structs */
+	double setup_s;           /* right-normalisation, environments, merged MPO pairs */
+	double sweep_s;           /* all sweeps */
+	double lanczos_ms;        /* device time in the Lanczos eigensolver */
+	double split_ms;          /* time in the SVD split, including the truncation decision */
+	double env_ms;            /* device time in the environment updates (right-to-left pass) */
+	double matvec_flops;      /* algorithmic GEMM FLOPs of all local-Hamiltonian applications */
+	double total_gemm_flops;  /* algorithmic GEMM FLOPs of the whole call */
+	long   matvecs;           /* local-Hamiltonian applications */
+	long   kernel_launches;   /* kernels launched by the call */
+	int    sweeps;
+	ct_long max_bond_dim;
+};
+int ctgpu_get_last_stats(struct ctgpu_stats* out);
+
+/* Message of the most recent failure in this thread ("" if none). */
+const char* ctgpu_last_error(void);
+
+/* ---- inputs ------------------------------------------------------------------------------ */
+
+/* Seeded random MPS with the reference's generator, bit for bit: seed_rng_state followed by
+ * construct_random_mps (src/util/rng.c:15-27, src/state/mps.c:93-175), real double precision.
+ * Tensors are allocated with aligned_alloc(16, .). Returns 0, or -5 on invalid arguments. */
+int ctgpu_construct_random_mps(int nsites, ct_long d, const qnumber* qsite, qnumber qnum_sector,
+	ct_long max_vdim, uint64_t rng_seed, struct mps* mps);
+
+/* First n standard normal draws of a freshly seeded generator (randn, src/util/rng.c:116-125). */
+void ctgpu_randn_sequence(uint64_t seed, int n, double* out);
+
+/* ---- single operations, for parity checks of the device kernels ------------------------ */
+
+/* block_sparse_tensor_dot (src/tensor/block_sparse_tensor.c:1826-2001); axrange 0 = leading,
+ * 1 = trailing; r is allocated here (aligned_alloc / free contract). */
+int ctgpu_block_sparse_tensor_dot(const struct block_sparse_tensor* s, int axrange_s,
+	const struct block_sparse_tensor* t, int axrange_t, int ndim_mult, struct block_sparse_tensor* r);
+
+/* block_sparse_tensor_transpose (src/tensor/block_sparse_tensor.c:785-870) */
+int ctgpu_block_sparse_tensor_transpose(const int* perm, const struct block_sparse_tensor* t,
+	struct block_sparse_tensor* r);
+
+/* apply_local_hamiltonian (src/algorithm/chain_ops.c:353-390): b = H_loc(w, l, r) a */
+int ctgpu_apply_local_hamiltonian(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
+	const struct block_sparse_tensor* l, const struct block_sparse_tensor* r, struct block_sparse_tensor* b);
+
+/* contraction_operator_step_left / _right (src/algorithm/chain_ops.c:196-245 / :116-165), with b = a */
+int ctgpu_contraction_operator_step_left(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
+	const struct block_sparse_tensor* l, struct block_sparse_tensor* l_next);
+int ctgpu_contraction_operator_step_right(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
+	const struct block_sparse_tensor* r, struct block_sparse_tensor* r_next);
+
+/* singular values of a block-sparse matrix as block_sparse_tensor_svd orders them
+ * (src/tensor/block_sparse_tensor.c:2686-2848); sigma must hold min(dim0, dim1) entries,
+ * *ns receives the count */
+int ctgpu_block_sparse_tensor_svd_values(const struct block_sparse_tensor* a, double* sigma, ct_long* ns);
+
+/* release a tensor returned by one of the calls above (free() on every array) */
+void ctgpu_delete_block_sparse_tensor(struct block_sparse_tensor* t);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTGPU_H */

@@ -1,0 +1,147 @@
+"""Generate the golden fixtures in this directory from the chemtensor reference.
+
+The reference is compiled from its own sources by ``make -C oracle ref`` into
+oracle/_ref/libct_ref.so (only where the reference checkout exists); this script
+drives it through ctypes and stores, as .npz:
+
+* the reference's own inputs: MPOs built by its Hamiltonian assembly code and
+  seeded random MPS from construct_random_mps (src/state/mps.c:93);
+* the reference's outputs of dmrg_twosite (src/algorithm/dmrg.c:262): energies
+  per sweep, entanglement entropies and the optimised MPS;
+* pseudo-random sequences of its PCG32x2 + Box-Muller generator (src/util/rng.c);
+* single-operation pins: apply_local_hamiltonian and the environment updates on
+  one bond (src/algorithm/chain_ops.c).
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from chemtensor_gb300 import ctstructs as cs  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+ref = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libct_ref.so"))
+ref.dmrg_twosite.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+ref.ref_heisenberg_mpo.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_void_p]
+ref.ref_hubbard_mpo.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_void_p]
+ref.ref_random_mps.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_void_p]
+ref.ref_randn_sequence.argtypes = [C.c_uint64, C.c_int, C.c_void_p]
+ref.ref_local_hamiltonian_setup.argtypes = [C.c_void_p] * 2 + [C.c_int] + [C.c_void_p] * 4
+ref.apply_local_hamiltonian.argtypes = [C.c_void_p] * 5
+ref.contraction_operator_step_left.argtypes = [C.c_void_p] * 5
+ref.contraction_operator_step_right.argtypes = [C.c_void_p] * 5
+
+HUB_QSITE = [(n << 16) + s for n, s in [(0, 0), (1, -1), (1, 1), (2, 0)]]
+
+
+def mpo(model, L, **kw):
+    m = cs.MPO()
+    if model == "heisenberg":
+        ref.ref_heisenberg_mpo(L, kw.get("J", 1.0), kw.get("Delta", 1.0), kw.get("h", 0.0), C.byref(m))
+    else:
+        ref.ref_hubbard_mpo(L, kw.get("t", 1.0), kw.get("u", 4.0), kw.get("mu", 0.0), C.byref(m))
+    return m
+
+
+def random_mps(L, qsite, sector, D, seed):
+    p = cs.MPS()
+    qa = (C.c_int32 * len(qsite))(*qsite)
+    ref.ref_random_mps(1, L, len(qsite), qa, sector, D, seed, C.byref(p))
+    return p
+
+
+def dmrg_case(name, model, L, D, sweeps, maxiter, tol, seed, **kw):
+    H = mpo(model, L, **kw)
+    if model == "heisenberg":
+        qsite, sector = [1, -1], 0
+    else:
+        qsite, sector = HUB_QSITE, (L << 16)
+    psi = random_mps(L, qsite, sector, D, seed)
+    arrays = {}
+    arrays.update(cs.chain_to_arrays("H", cs.read_mpo(H)))
+    arrays.update(cs.chain_to_arrays("psi0", cs.read_mps(psi)))
+    en = (C.c_double * sweeps)()
+    ent = (C.c_double * (L - 1))()
+    ret = ref.dmrg_twosite(C.byref(H), sweeps, maxiter, tol, D, C.byref(psi), en, ent)
+    assert ret == 0
+    arrays.update(cs.chain_to_arrays("psi", cs.read_mps(psi)))
+    arrays.update(en_sweeps=np.array(en), entropy=np.array(ent),
+                  params=np.array([L, D, sweeps, maxiter], dtype=np.int64), tol_split=np.array(tol),
+                  seed=np.array(seed), model=np.array(model))
+    np.savez_compressed(os.path.join(OUT, name), **arrays)
+    print(name, "E =", en[sweeps - 1])
+    return H, psi
+
+
+def local_ops_case(name, model, L, D, seed, ibond, **kw):
+    """Reference inputs/outputs of one local-H apply and one left / right environment step."""
+    H = mpo(model, L, **kw)
+    qsite, sector = ([1, -1], 0) if model == "heisenberg" else (HUB_QSITE, L << 16)
+    psi = random_mps(L, qsite, sector, D, seed)
+    h2, le, re, a2, b = (cs.BlockSparseTensor() for _ in range(5))
+    ref.ref_local_hamiltonian_setup(C.byref(H), C.byref(psi), ibond, C.byref(h2), C.byref(le), C.byref(re), C.byref(a2))
+    ref.apply_local_hamiltonian(C.byref(a2), C.byref(h2), C.byref(le), C.byref(re), C.byref(b))
+    lnext, rnext = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+    A = psi.a[ibond]
+    ref.contraction_operator_step_left(C.byref(A), C.byref(A), C.byref(H.a[ibond]), C.byref(le), C.byref(lnext))
+    B = psi.a[ibond + 1]
+    ref.contraction_operator_step_right(C.byref(B), C.byref(B), C.byref(H.a[ibond + 1]), C.byref(re), C.byref(rnext))
+    arrays = {}
+    for p, t in [("h2", h2), ("l", le), ("r", re), ("a", a2), ("b", b), ("lnext", lnext), ("rnext", rnext)]:
+        arrays.update(cs.bst_to_arrays(p, cs.read_bst(t)))
+    arrays.update(cs.bst_to_arrays("A", cs.read_bst(A)))
+    arrays.update(cs.bst_to_arrays("B", cs.read_bst(B)))
+    arrays.update(cs.bst_to_arrays("W", cs.read_bst(H.a[ibond])))
+    arrays.update(cs.bst_to_arrays("W1", cs.read_bst(H.a[ibond + 1])))
+    np.savez_compressed(os.path.join(OUT, name), **arrays)
+    print(name, "entries a/b:", cs.read_bst(a2).num_elements_blocks())
+
+
+def main():
+    # PCG32x2 + Box-Muller sequences (src/util/rng.c:15-125)
+    seqs = {}
+    for seed in (0, 42, 7, 12345678901):
+        buf = (C.c_double * 2000)()
+        ref.ref_randn_sequence(seed, 2000, buf)
+        seqs[f"randn_{seed}"] = np.array(buf)
+    np.savez_compressed(os.path.join(OUT, "rng_sequences.npz"), **seqs)
+
+    # construct_random_mps outputs (src/state/mps.c:93-175), including Floyd sampling of bond quantum numbers
+    arrays = {}
+    for tag, (L, qs, sec, D, seed) in {
+        "heis_L12_D8_s1": (12, [1, -1], 0, 8, 1),
+        "hub_L8_D24_s3": (8, HUB_QSITE, 8 << 16, 24, 3),
+        "hub_L10_D16_s42": (10, HUB_QSITE, (10 << 16) + 2, 16, 42),
+    }.items():
+        p = random_mps(L, qs, sec, D, seed)
+        arrays.update(cs.chain_to_arrays(tag, cs.read_mps(p)))
+        arrays[f"{tag}_params"] = np.array([L, sec, D, seed], dtype=np.int64)
+        arrays[f"{tag}_qsite"] = np.array(qs, dtype=np.int32)
+    np.savez_compressed(os.path.join(OUT, "random_mps.npz"), **arrays)
+
+    # MPOs built by the reference's assembly code (for operator equality of the builders)
+    arrays = {}
+    arrays.update(cs.chain_to_arrays("heis6", cs.read_mpo(mpo("heisenberg", 6, J=1.0, Delta=0.8, h=0.3))))
+    arrays.update(cs.chain_to_arrays("hub4", cs.read_mpo(mpo("hubbard", 4, t=1.0, u=4.0, mu=0.3))))
+    np.savez_compressed(os.path.join(OUT, "mpo_reference.npz"), **arrays)
+
+    # dmrg_twosite end to end
+    dmrg_case("dmrg_heisenberg_L20_D32.npz", "heisenberg", 20, 32, 6, 5, 1e-10, 42)
+    dmrg_case("dmrg_heisenberg_L10_D16.npz", "heisenberg", 10, 16, 3, 5, 1e-10, 7, Delta=0.5, h=0.1)
+    dmrg_case("dmrg_hubbard_L8_D32.npz", "hubbard", 8, 32, 4, 5, 1e-10, 42)
+    dmrg_case("dmrg_hubbard_L12_D48.npz", "hubbard", 12, 48, 2, 7, 1e-10, 5, u=2.0, mu=0.25)
+
+    # single operations on one bond
+    local_ops_case("local_ops_heisenberg_L12.npz", "heisenberg", 12, 16, 11, 5)
+    local_ops_case("local_ops_hubbard_L8.npz", "hubbard", 8, 32, 13, 3)
+
+
+if __name__ == "__main__":
+    main()

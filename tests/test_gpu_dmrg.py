@@ -1,0 +1,79 @@
+"""dmrg_twosite on the GPU through the C ABI, against the reference's own results."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import chemtensor_gb300 as ctg
+from chemtensor_gb300 import ctstructs as cs, hamiltonians as hm, native
+from conftest import golden
+from helpers import overlap, run_gpu_dmrg, run_oracle_dmrg, same_structure
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["dmrg_heisenberg_L20_D32.npz", "dmrg_heisenberg_L10_D16.npz",
+         "dmrg_hubbard_L8_D32.npz", "dmrg_hubbard_L12_D48.npz"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_dmrg_matches_reference(gpu, oracle_port, case):
+    g = golden(case)
+    L, D, sweeps, maxiter = [int(x) for x in g["params"]]
+    H = cs.chain_from_arrays("H", g)
+    psi0 = cs.chain_from_arrays("psi0", g)
+    ret, en, ent, psi = run_gpu_dmrg(gpu, H, psi0, sweeps, maxiter, float(g["tol_split"]), D)
+    assert ret == 0, native.last_error()
+    # energies within 1e-10 of the reference, bond structure and quantum numbers bit-exact
+    np.testing.assert_allclose(en, g["en_sweeps"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(ent, g["entropy"], rtol=0, atol=1e-8)
+    ref_psi = cs.chain_from_arrays("psi", g)
+    assert same_structure(psi, ref_psi)
+    # same state up to a global sign (gauge-invariant), normalised
+    assert abs(abs(overlap(oracle_port, psi, ref_psi)) - 1) < 1e-9
+    assert abs(overlap(oracle_port, psi, psi) - 1) < 1e-12
+
+
+def test_dmrg_with_package_hamiltonian_matches_oracle(gpu, oracle_port):
+    H = hm.fermi_hubbard_1d(16, 1.0, 4.0, 0.0)
+    c = native.random_mps(16, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(16, 0), 64, 42)
+    psi0 = cs.read_mps(c)
+    cs.free_mps(c)
+    r1, e1, s1, p1 = run_gpu_dmrg(gpu, H, psi0, 2, 5, 1e-10, 64)
+    r2, e2, s2, p2 = run_oracle_dmrg(oracle_port, H, psi0, 2, 5, 1e-10, 64)
+    assert r1 == 0 and r2 == 0
+    np.testing.assert_allclose(e1, e2, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(s1, s2, rtol=0, atol=1e-8)
+    assert same_structure(p1, p2)
+
+
+def test_python_entry_point_mirrors_reference_binding(gpu):
+    H = hm.heisenberg_xxz_1d(10, 1.0, 1.0, 0.0)
+    psi, en, ent = ctg.dmrg(H, num_sweeps=3, maxiter_lanczos=5, tol_split=1e-10, max_vdim=16, qnum_sector=0, rng_seed=7)
+    assert len(en) == 3 and len(ent) == 9
+    assert en[-1] < -4.2
+    with pytest.raises(ValueError):
+        ctg.dmrg(H, num_sweeps=0)
+
+
+def test_invalid_arguments_return_error_code(gpu):
+    H = hm.heisenberg_xxz_1d(6, 1.0, 1.0, 0.0)
+    cH = cs.make_c_mpo(H)
+    p = native.random_mps(5, 2, [1, -1], 0, 8, 1)       # wrong length
+    en, ent = np.zeros(2), np.zeros(5)
+    assert gpu.dmrg_twosite(C.byref(cH), 2, 5, 1e-10, 8, C.byref(p), en.ctypes.data, ent.ctypes.data) == -5
+    assert "nsites" in native.last_error()
+    cs.free_mps(p)
+    p = native.random_mps(6, 2, [1, -1], 0, 8, 1)
+    assert gpu.dmrg_twosite(C.byref(cH), 2, 999, 1e-10, 8, C.byref(p), en.ctypes.data, ent.ctypes.data) == -5
+    cs.free_mps(p)
+    cs.free_mpo(cH)
+
+
+def test_repeated_calls_are_deterministic(gpu):
+    g = golden("dmrg_hubbard_L8_D32.npz")
+    H = cs.chain_from_arrays("H", g)
+    psi0 = cs.chain_from_arrays("psi0", g)
+    a = run_gpu_dmrg(gpu, H, psi0, 2, 5, 1e-10, 32)
+    b = run_gpu_dmrg(gpu, H, psi0, 2, 5, 1e-10, 32)
+    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
