@@ -83,10 +83,43 @@ int ctgpu_get_last_stats(struct ctgpu_stats* out)
 	out->kernel_launches = s.kernel_launches;
 	out->sweeps = s.sweeps;
 	out->max_bond_dim = s.max_bond_dim;
+	out->svd_max_sweeps = s.svd_max_sweeps;
 	return 0;
 }
 
 const char* ctgpu_last_error(void) { return g_last_error.c_str(); }
+
+int ctgpu_set_profiling(int enable, int skip_sweeps)
+{
+	const int old = g_opts.profile;
+	g_opts.profile = enable;
+	g_opts.profile_skip_sweeps = skip_sweeps;
+	return old;
+}
+
+void ctgpu_set_l2_flush_bytes(ct_long bytes) { g_opts.l2_flush_bytes = bytes; }
+
+int ctgpu_get_sweep_times(double* ms, long* launches, int max)
+{
+	const int n = (int)g_stats.sweep_ms.size();
+	for (int i = 0; i < n && i < max; i++)
+	{
+		if (ms) ms[i] = g_stats.sweep_ms[i];
+		if (launches) launches[i] = g_stats.sweep_launches[i];
+	}
+	return n;
+}
+
+int ctgpu_get_kernel_profile(int cls, long* launches, double* ms, double* flops, double* bytes)
+{
+	if (cls < 0 || cls >= ctg::K_NUM_CLASSES) return -1;
+	const ctg::KProf& k = g_stats.prof[cls];
+	if (launches) *launches = k.launches;
+	if (ms) *ms = k.ms;
+	if (flops) *flops = k.flops;
+	if (bytes) *bytes = k.bytes;
+	return 0;
+}
 
 int ctgpu_block_sparse_tensor_dot(const struct block_sparse_tensor* s, int axrange_s, const struct block_sparse_tensor* t,
                                   int axrange_t, int ndim_mult, struct block_sparse_tensor* r)
@@ -159,6 +192,16 @@ int ctgpu_block_sparse_tensor_svd_values(const struct block_sparse_tensor* a, do
 		*ns = sv.ns;
 		return 0;
 	});
+}
+
+double ctgpu_measure_fp64_tflops(void)
+{
+	double r = -1;
+	guarded([&] {
+		r = ctg::measure_fp64_fma_tflops(g_opts.device);
+		return 0;
+	});
+	return r;
 }
 
 void ctgpu_delete_block_sparse_tensor(struct block_sparse_tensor* t)

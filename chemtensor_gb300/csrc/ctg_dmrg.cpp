@@ -306,11 +306,28 @@ int split_mps_svd(Ctx& c, const DTensor& a, i64 d, const std::vector<q32>& qsite
 	DTensor tmp = op_flatten(c, a4, 0, TENSOR_AXIS_OUT);
 	DTensor am = op_flatten(c, tmp, 1, TENSOR_AXIS_IN);
 	SvdResult sv;
-	int ret = op_svd(c, am, sv);    // synchronises
+	int ret = op_svd(c, am, sv, tol);    // synchronises
 	if (ret < 0) return ret;
 	std::vector<double> sigma((size_t)sv.ns);
 	CTG_CUDA(cudaMemcpy(sigma.data(), sv.s->ptr, sigma.size() * sizeof(double), cudaMemcpyDeviceToHost));
 	TruncResult tr = retained_bond_indices(sigma.data(), sv.ns, tol, true, max_vdim);
+	// Directions the SVD left unresolved weigh at most sv.max_tail in total per block. They
+	// cannot influence the truncation if that bound is far below the smallest retained squared
+	// singular value; otherwise (rare) resolve everything and decide again.
+	if (sv.max_tail > 0)
+	{
+		double smin2 = tr.ind.empty() ? 0.0 : sigma[(size_t)tr.ind[0]] * sigma[(size_t)tr.ind[0]];
+		for (i64 i : tr.ind) smin2 = std::min(smin2, sigma[(size_t)i] * sigma[(size_t)i]);
+		if (!(sv.max_tail < 1e-2 * smin2))
+		{
+			sv = SvdResult();
+			ret = op_svd(c, am, sv, 0.0);
+			if (ret < 0) return ret;
+			CTG_CUDA(cudaMemcpy(sigma.data(), sv.s->ptr, sigma.size() * sizeof(double), cudaMemcpyDeviceToHost));
+			tr = retained_bond_indices(sigma.data(), sv.ns, tol, true, max_vdim);
+			c.svd_full_reruns++;
+		}
+	}
 	std::vector<double> sret;
 	if (tr.ind.empty())
 	{
@@ -401,21 +418,31 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 	double* wp = (double*)wv.ptr;
 	double* pp = (double*)partial.ptr;
 	cudaStream_t s = c.stream();
-	launch_lz_normalize_start(a_start.data(), Vp, n, pp, d_sc, s);
+	const double dn = (double)n;
+	{
+		KScope ks(c, K_LANCZOS, 3, 3.0 * dn, 24.0 * dn);
+		launch_lz_normalize_start(a_start.data(), Vp, n, pp, d_sc, s);
+	}
 	for (int j = 0; j < maxiter; j++)
 	{
 		h.apply(c, Vp + (i64)j * n, wp);
-		launch_lz_alpha(wp, Vp + (i64)j * n, n, j, pp, d_sc, s);
+		{
+			KScope ks(c, K_LANCZOS, 2, 2.0 * dn, 16.0 * dn);
+			launch_lz_alpha(wp, Vp + (i64)j * n, n, j, pp, d_sc, s);
+		}
 		if (j < maxiter - 1)
 		{
+			KScope ks(c, K_LANCZOS, 3, 7.0 * dn, 56.0 * dn);
 			launch_lz_orth_beta(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, n, j, pp, d_sc, s);
 			launch_lz_next(wp, Vp + (i64)(j + 1) * n, n, j, d_sc, s);
 		}
 	}
-	launch_lz_tridiag(maxiter, d_sc, s);
 	a_opt = c.empty(a_start.m());
-	launch_lz_ritz(Vp, n, maxiter, d_sc, a_opt.data(), s);
-	c.kernel_launches += 4L * maxiter + 5;
+	{
+		KScope ks(c, K_LANCZOS, 2, 2.0 * maxiter * dn, 8.0 * (maxiter + 1) * dn);
+		launch_lz_tridiag(maxiter, d_sc, s);
+		launch_lz_ritz(Vp, n, maxiter, d_sc, a_opt.data(), s);
+	}
 	if (st)
 	{
 		st->matvecs += maxiter;
@@ -457,6 +484,9 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	Ctx& c = context_for_device(opt.device);
 	c.gemm_flops = 0;
 	c.kernel_launches = 0;
+	c.profile = false;
+	c.prof_reset();
+	c.svd_max_sweeps = 0;
 	DBuf sc_buf(&c, sizeof(LanczosScalars));
 	LanczosScalars* d_sc = (LanczosScalars*)sc_buf.ptr;
 	LanczosScalars h_sc;
@@ -532,9 +562,19 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		return 0;
 	};
 
+	std::unique_ptr<DBuf> flush;
+	if (opt.l2_flush_bytes > 0) flush.reset(new DBuf(&c, (size_t)opt.l2_flush_bytes));
+	cudaEvent_t sw_ev[2];
+	for (auto& e : sw_ev) CTG_CUDA(cudaEventCreate(&e));
 	double en = 0;
 	for (int sw = 0; sw < num_sweeps && ret == 0; sw++)
 	{
+		// each sweep starts from an idle device (and, if requested, a flushed L2)
+		if (flush) CTG_CUDA(cudaMemsetAsync(flush->ptr, sw & 0xff, flush->bytes, c.stream()));
+		c.sync();
+		c.profile = opt.profile && sw >= opt.profile_skip_sweeps;
+		const long launches0 = c.kernel_launches;
+		CTG_CUDA(cudaEventRecord(sw_ev[0], c.stream()));
 		for (int i = 0; i < L - 2 && ret == 0; i++) ret = bond_step(i, true);
 		for (int i = L - 2; i >= 0 && ret == 0; i--)
 		{
@@ -553,10 +593,20 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		DTensor t = head_tensor(c, A[0], 0.0);
 		ret = local_orthonormalize_rq(c, A[0], t);
 		en_sweeps[sw] = en;
+		CTG_CUDA(cudaEventRecord(sw_ev[1], c.stream()));
+		c.sync();
+		float sms = 0;
+		CTG_CUDA(cudaEventElapsedTime(&sms, sw_ev[0], sw_ev[1]));
+		st->sweep_ms.push_back(sms);
+		st->sweep_launches.push_back(c.kernel_launches - launches0);
+		c.profile = false;
 		st->sweeps++;
 	}
 	c.sync();
+	c.profile = false;
+	for (int k = 0; k < K_NUM_CLASSES; k++) st->prof[k] = c.prof[k];
 	for (auto& e : ev) cudaEventDestroy(e);
+	for (auto& e : sw_ev) cudaEventDestroy(e);
 	const double t_sweeps = now_s();
 	st->sweep_s = t_sweeps - t_setup;
 	if (ret < 0) return ret;
@@ -572,6 +622,7 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	st->download_s = now_s() - t_sweeps;
 	st->kernel_launches = c.kernel_launches;
 	st->total_gemm_flops = c.gemm_flops;
+	st->svd_max_sweeps = c.svd_max_sweeps;
 	st->wall_s = now_s() - t_start;
 	return 0;
 }

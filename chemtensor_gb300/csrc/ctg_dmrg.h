@@ -11,6 +11,9 @@ struct DmrgOptions {
 	int precision = GEMM_FP64;   // GemmPrecision of the bulk local-H GEMMs
 	int final_fp64_sweeps = 1;   // trailing sweeps forced to FP64 when precision != FP64
 	int verbose = 0;
+	i64 l2_flush_bytes = 0;      // if > 0, overwrite a buffer of this size before every sweep
+	int profile = 0;             // time every launch by kernel class (CUDA events)
+	int profile_skip_sweeps = 0; // ... starting with this sweep
 };
 
 struct DmrgStats {
@@ -28,6 +31,10 @@ struct DmrgStats {
 	long kernel_launches = 0;
 	int sweeps = 0;
 	i64 max_bond_dim = 0;
+	int svd_max_sweeps = 0;             // largest Jacobi sweep count of any block SVD
+	std::vector<double> sweep_ms;       // device time of every sweep (CUDA events on the stream)
+	std::vector<long> sweep_launches;   // kernels launched by every sweep
+	KProf prof[K_NUM_CLASSES];          // per kernel class, over the profiled sweeps
 };
 
 // Same contract as dmrg_twosite (src/algorithm/dmrg.c:262-399).

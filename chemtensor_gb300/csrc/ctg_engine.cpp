@@ -19,6 +19,7 @@ DBuf::~DBuf()
 Ctx::Ctx(int device) : dev_(device)
 {
 	CTG_CUDA(cudaSetDevice(dev_));
+	CTG_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev_));
 	CTG_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
 	cudaMemPoolProps props = {};
 	props.allocType = cudaMemAllocationTypePinned;
@@ -72,6 +73,70 @@ void Ctx::sync()
 {
 	CTG_CUDA(cudaStreamSynchronize(st_));
 	staging_used_ = 0;
+	prof_resolve();
+}
+
+cudaEvent_t Ctx::get_event()
+{
+	if (event_pool_.empty())
+	{
+		cudaEvent_t e;
+		CTG_CUDA(cudaEventCreate(&e));
+		return e;
+	}
+	cudaEvent_t e = event_pool_.back();
+	event_pool_.pop_back();
+	return e;
+}
+
+void Ctx::prof_begin()
+{
+	if (!profile) return;
+	open_ = get_event();
+	CTG_CUDA(cudaEventRecord(open_, st_));
+}
+
+void Ctx::prof_end(int cls, int launches, double flops, double bytes)
+{
+	if (!profile || !open_) return;
+	cudaEvent_t e1 = get_event();
+	CTG_CUDA(cudaEventRecord(e1, st_));
+	pending_.push_back(Pending{cls, launches, open_, e1, flops, bytes});
+	open_ = nullptr;
+}
+
+void Ctx::prof_resolve()
+{
+	for (const Pending& p : pending_)
+	{
+		float ms = 0;
+		CTG_CUDA(cudaEventElapsedTime(&ms, p.e0, p.e1));
+		KProf& k = prof[p.cls];
+		k.launches += p.launches;
+		k.ms += ms;
+		k.flops += p.flops;
+		k.bytes += p.bytes;
+		event_pool_.push_back(p.e0);
+		event_pool_.push_back(p.e1);
+	}
+	pending_.clear();
+}
+
+void Ctx::prof_reset()
+{
+	for (auto& k : prof) k = KProf();
+}
+
+KScope::KScope(Ctx& ctx, int cls_, int launches_, double flops_, double bytes_)
+	: c(ctx), cls(cls_), launches(launches_), flops(flops_), bytes(bytes_)
+{
+	c.prof_begin();
+}
+
+KScope::~KScope()
+{
+	c.prof_end(cls, launches, flops, bytes);
+	c.kernel_launches += launches;
 }
 
 DBufPtr Ctx::upload(const void* host, size_t bytes)
@@ -241,6 +306,7 @@ DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, in
 			          "dot: B operand out of range");
 			cons.push_back(g);
 			flops += 2.0 * (double)o.m * (double)o.n * (double)k;
+			p.flops_cls[tile_class(o.m, o.n)] += 2.0 * (double)o.m * (double)o.n * (double)k;
 		}
 		o.nc = (int)cons.size() - o.c0;
 		CTG_CHECK(o.m >= 1 && o.n >= 1 && o.c_off + (i64)o.m * o.n <= r.nnz, "dot: output block out of range");
@@ -271,8 +337,8 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 	for (int k = 0; k < NUM_TILE_CLASSES; k++)
 	{
 		if (ntiles[k] == 0) continue;
+		KScope ks(c, K_GEMM, 1, flops_cls[k], 0);
 		launch_gemm_f64(k, ntiles[k], tiles[k], outs, cons, A, B, C, c.stream());
-		c.kernel_launches++;
 	}
 	c.gemm_flops += flops;
 }
@@ -284,9 +350,9 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 void CopyPlan::run(Ctx& c, const double* src, double* dst) const
 {
 	if (nchunks == 0) return;
+	KScope ks(c, kind == 0 ? K_PERMUTE : K_ROWMAP, 1, 0, 16.0 * (double)elements);
 	if (kind == 0) launch_permute(nchunks, chunks, (const PermDesc*)descs, src, dst, c.stream());
 	else launch_rowmap(nchunks, chunks, (const RowDesc*)descs, maps, src, dst, c.stream());
-	c.kernel_launches++;
 }
 
 static CopyPlan finish_perm(Ctx& c, std::shared_ptr<Meta> out, const std::vector<PermDesc>& d, const std::vector<Chunk>& ch)
@@ -300,6 +366,7 @@ static CopyPlan finish_perm(Ctx& c, std::shared_ptr<Meta> out, const std::vector
 	p.descs = at<PermDesc>(p.desc, od);
 	p.chunks = at<Chunk>(p.desc, oc);
 	p.nchunks = (int)ch.size();
+	p.elements = out->nnz;
 	return p;
 }
 
@@ -330,6 +397,7 @@ static CopyPlan finish_rows(Ctx& c, std::shared_ptr<Meta> out, const std::vector
 	p.chunks = at<Chunk>(p.desc, oc);
 	p.maps = at<i64>(p.desc, om);
 	p.nchunks = (int)ch.size();
+	p.elements = out->nnz;
 	return p;
 }
 
@@ -558,9 +626,9 @@ DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange)
 	const size_t od = pk.add(descs), oc = pk.add(chunks), om = pk.add(maps);
 	DBufPtr desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
 	DTensor r = c.empty(m);
+	KScope ks(c, K_SCALE, 1, 0, 16.0 * (double)m.nnz);
 	launch_scale_axis((int)chunks.size(), at<Chunk>(desc, oc), at<ScaleDesc>(desc, od), at<i64>(desc, om), dvec, s.data(),
 	                  r.data(), c.stream());
-	c.kernel_launches++;
 	return r;
 }
 
@@ -593,7 +661,7 @@ DTensor view_trace_unit(const DTensor& t)
 // SVD and RQ of block-sparse matrices
 // ------------------------------------------------------------------------------------
 
-int op_svd(Ctx& c, const DTensor& a, SvdResult& res)
+int op_svd(Ctx& c, const DTensor& a, SvdResult& res, double tol_hint)
 {
 	const Meta& am = a.m();
 	CTG_CHECK(am.ndim == 2, "svd: matrix expected");
@@ -658,20 +726,65 @@ int op_svd(Ctx& c, const DTensor& a, SvdResult& res)
 		d.w_off = woff;
 		d.m = (int)bl.m;
 		d.n = (int)bl.n;
-		woff += std::max(bl.m, bl.n) * bl.k + bl.k * bl.k;
+		woff += svd_scratch_doubles(d.m, d.n);
 		descs.push_back(d);
 	}
 	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(SvdDesc));
 	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
-	DBuf status(&c, sizeof(int));
-	CTG_CUDA(cudaMemsetAsync(status.ptr, 0, sizeof(int), c.stream()));
-	launch_svd_jacobi((int)descs.size(), (const SvdDesc*)desc->ptr, a.data(), res.u.data(), (double*)res.s->ptr,
-	                  res.vh.data(), (double*)scratch.ptr, (int*)status.ptr, c.stream());
-	c.kernel_launches++;
-	int hst = 0;
-	CTG_CUDA(cudaMemcpyAsync(&hst, status.ptr, sizeof(int), cudaMemcpyDeviceToHost, c.stream()));
+	DBuf status(&c, 2 * sizeof(int));
+	CTG_CUDA(cudaMemsetAsync(status.ptr, 0, 2 * sizeof(int), c.stream()));
+	// Every direction is resolved: skipping pairs of small directions (which the truncation could
+	// never retain) creates slowly converging pairs at the skip boundary, so it is not used.
+	(void)tol_hint;
+	const double tiny_rel2 = 0.0;
+	DBuf tail(&c, descs.size() * sizeof(double));
+	CTG_CUDA(cudaMemsetAsync(tail.ptr, 0, descs.size() * sizeof(double), c.stream()));
+	// one cluster per block; spread the SMs over the blocks (at most 8 CTAs per cluster)
+	int cl = 1;
+	while (cl < 8 && (i64)(2 * cl) * (i64)descs.size() <= (i64)c.num_sms()) cl *= 2;
+	if (const char* e = getenv("CTGPU_SVD_CLUSTER")) cl = std::max(1, std::min(8, atoi(e)));
+	{
+		KScope ks(c, K_SVD, 1);
+		launch_svd_jacobi((int)descs.size(), cl, (const SvdDesc*)desc->ptr, a.data(), res.u.data(), (double*)res.s->ptr,
+		                  res.vh.data(), (double*)scratch.ptr, (int*)status.ptr, tiny_rel2, (double*)tail.ptr, c.stream());
+	}
+	int hst[2] = {0, 0};
+	CTG_CUDA(cudaMemcpyAsync(hst, status.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream()));
 	c.sync();
-	return hst == 0 ? 0 : -1;
+	c.svd_max_sweeps = std::max(c.svd_max_sweeps, hst[1]);
+	{
+		std::vector<double> tw(descs.size());
+		CTG_CUDA(cudaMemcpy(tw.data(), tail.ptr, tw.size() * sizeof(double), cudaMemcpyDeviceToHost));
+		res.max_tail = 0;
+		for (double x : tw) res.max_tail = std::max(res.max_tail, x);
+	}
+	if (hst[0] != 0)
+	{
+		int mmax = 0, nmax = 0;
+		for (const SvdDesc& d : descs) { mmax = std::max(mmax, d.m); nmax = std::max(nmax, d.n); }
+		fprintf(stderr, "ctgpu: block SVD did not converge within %d Jacobi sweeps (%zu blocks, largest %d x %d, cluster %d)\n",
+		        SVD_MAX_SWEEPS, descs.size(), mmax, nmax, cl);
+		// opt-in diagnostics: write the input matrix (row-major blocks) for offline analysis
+		if (const char* path = getenv("CTGPU_SVD_DUMP"))
+		{
+			std::vector<double> host((size_t)am.nnz);
+			copy_to_host(c, a, host.data());
+			if (FILE* f = fopen(path, "wb"))
+			{
+				const i64 nb = (i64)descs.size();
+				fwrite(&nb, sizeof(i64), 1, f);
+				for (const SvdDesc& d : descs)
+				{
+					const i64 mn[2] = {d.m, d.n};
+					fwrite(mn, sizeof(i64), 2, f);
+					fwrite(host.data() + d.a_off, sizeof(double), (size_t)d.m * d.n, f);
+				}
+				fclose(f);
+			}
+		}
+		return -1;
+	}
+	return 0;
 }
 
 int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q)
@@ -736,9 +849,9 @@ int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q)
 	}
 	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(RqDesc));
 	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
+	KScope ks(c, K_RQ, 1);
 	launch_rq_householder((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr,
 	                      c.stream());
-	c.kernel_launches++;
 	return 0;
 }
 

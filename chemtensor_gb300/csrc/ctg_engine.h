@@ -17,6 +17,24 @@ namespace ctg {
 
 class Ctx;
 
+// kernel classes for profiling
+enum KClass { K_GEMM = 0, K_PERMUTE, K_ROWMAP, K_SCALE, K_SVD, K_RQ, K_LANCZOS, K_NUM_CLASSES };
+struct KProf {
+	long launches = 0;
+	double ms = 0;               // summed device time of the launches
+	double flops = 0;            // algorithmic FLOPs (GEMM: sum of 2 m n k)
+	double bytes = 0;            // algorithmic HBM bytes (copies: read + write of the entries moved)
+};
+
+// Counts (and, when profiling, times) the launches issued inside its scope.
+struct KScope {
+	Ctx& c;
+	int cls, launches;
+	double flops, bytes;
+	KScope(Ctx& ctx, int cls_, int launches_, double flops_ = 0, double bytes_ = 0);
+	~KScope();
+};
+
 // Stream-ordered device allocation, freed on the owning context's stream.
 struct DBuf {
 	Ctx* ctx = nullptr;
@@ -53,11 +71,27 @@ public:
 	DTensor empty(const Meta& m);
 	DTensor zeros(const Meta& m);
 	// statistics
-	double gemm_flops = 0;       // algorithmic FP64-path GEMM FLOPs issued
+	double gemm_flops = 0;       // algorithmic GEMM FLOPs issued
 	long kernel_launches = 0;
+	int svd_max_sweeps = 0;      // largest Jacobi sweep count of any block SVD
+	int svd_full_reruns = 0;     // SVDs repeated at full resolution for the truncation decision
+	int num_sms() const { return sms_; }
+	// optional per-kernel-class timing with CUDA events on this stream (resolved at sync points)
+	bool profile = false;
+	KProf prof[K_NUM_CLASSES];
+	void prof_begin();
+	void prof_end(int cls, int launches, double flops, double bytes);
+	void prof_resolve();
+	void prof_reset();
 
 private:
+	struct Pending { int cls, launches; cudaEvent_t e0, e1; double flops, bytes; };
+	std::vector<Pending> pending_;
+	std::vector<cudaEvent_t> event_pool_;
+	cudaEvent_t open_ = nullptr;
+	cudaEvent_t get_event();
 	int dev_;
+	int sms_ = 1;
 	cudaStream_t st_ = nullptr;
 	cudaMemPool_t pool_ = nullptr;
 	char* staging_ = nullptr;
@@ -78,6 +112,7 @@ struct DotPlan {
 	const GemmOut* outs = nullptr;
 	const GemmContrib* cons = nullptr;
 	double flops = 0;
+	double flops_cls[NUM_TILE_CLASSES] = {0, 0, 0};
 	void run(Ctx& c, const double* A, const double* B, double* C) const;
 };
 DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult);
@@ -90,6 +125,7 @@ struct CopyPlan {
 	const Chunk* chunks = nullptr;
 	const void* descs = nullptr;
 	const i64* maps = nullptr;
+	i64 elements = 0;            // entries moved
 	void run(Ctx& c, const double* src, double* dst) const;
 };
 CopyPlan make_transpose_plan(Ctx& c, const Meta& t, const int* perm);
@@ -117,8 +153,9 @@ struct SvdResult {
 	DTensor u, vh;
 	DBufPtr s;
 	i64 ns = 0;
+	double max_tail = 0;     // largest per-block weight of directions left unresolved (see tol_hint)
 };
-int op_svd(Ctx& c, const DTensor& a, SvdResult& res);
+int op_svd(Ctx& c, const DTensor& a, SvdResult& res, double tol_hint = 0.0);
 
 // block RQ (block_sparse_tensor_rq, block_sparse_tensor.c:2544-2676). Returns 0 or -1.
 int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q);

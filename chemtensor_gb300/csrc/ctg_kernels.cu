@@ -211,4 +211,49 @@ void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs,
 	CTG_CUDA(cudaGetLastError());
 }
 
+// ------------------------------------------------------------------------------------
+// FP64 FMA throughput probe: the denominator of the plain path's roofline
+// ------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_fp64_fma(double* out, int iters, double a, double b)
+{
+	double x[8];
+#pragma unroll
+	for (int i = 0; i < 8; i++) x[i] = threadIdx.x * 1e-9 + i;
+	for (int it = 0; it < iters; it++)
+	{
+#pragma unroll
+		for (int i = 0; i < 8; i++) x[i] = fma(x[i], a, b);
+	}
+	double s = 0;
+#pragma unroll
+	for (int i = 0; i < 8; i++) s += x[i];
+	if (s == 12345.678) out[0] = s;   // keeps the chains alive
+}
+
+double measure_fp64_fma_tflops(int device)
+{
+	CTG_CUDA(cudaSetDevice(device));
+	int sms = 0;
+	CTG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+	double* out = nullptr;
+	CTG_CUDA(cudaMalloc(&out, sizeof(double)));
+	cudaEvent_t e0, e1;
+	CTG_CUDA(cudaEventCreate(&e0));
+	CTG_CUDA(cudaEventCreate(&e1));
+	const int blocks = sms * 8, threads = 256, iters = 4096;
+	k_fp64_fma<<<blocks, threads>>>(out, 64, 0.999999, 1e-7);
+	CTG_CUDA(cudaEventRecord(e0));
+	for (int r = 0; r < 5; r++) k_fp64_fma<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+	CTG_CUDA(cudaEventRecord(e1));
+	CTG_CUDA(cudaEventSynchronize(e1));
+	float ms = 0;
+	CTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(out);
+	const double flops = 5.0 * blocks * threads * (double)iters * 8 * 2;
+	return flops / (ms * 1e-3) / 1e12;
+}
+
 }  // namespace ctg

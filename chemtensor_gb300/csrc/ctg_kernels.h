@@ -83,14 +83,21 @@ void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs,
                        const double* src, double* dst, cudaStream_t st);
 
 // ---- dense linear algebra per block ---------------------------------------------
-// One-sided Jacobi SVD of a row-major m x n block: u (m x k), s (k), vh (k x n), k = min(m, n),
-// singular values in descending order. Scratch holds max(m,n)*k + k*k doubles per block.
+// SVD of a row-major m x n block: u (m x k), s (k), vh (k x n), k = min(m, n), singular values
+// in descending order; one thread-block cluster of 'cluster' CTAs (1..8) per block.
+// status[0] becomes -1 if a block does not converge within SVD_MAX_SWEEPS FP64 Jacobi sweeps,
+// status[1] receives the largest sweep count. Pairs of directions whose squared singular values
+// are both below tiny_rel2 times the largest squared column norm are not resolved against each
+// other (0 resolves everything); tail[block] (zeroed by the caller) accumulates their total
+// weight, an upper bound for any singular value squared that was left unresolved.
+constexpr int SVD_MAX_SWEEPS = 60;
 struct SvdDesc {
 	i64 a_off, u_off, s_off, v_off, w_off;
 	int m, n;
 };
-void launch_svd_jacobi(int nblocks, const SvdDesc* descs, const double* a, double* u, double* s, double* vh,
-                       double* scratch, int* status, cudaStream_t st);
+i64 svd_scratch_doubles(int m, int n);
+void launch_svd_jacobi(int nblocks, int cluster, const SvdDesc* descs, const double* a, double* u, double* s,
+                       double* vh, double* scratch, int* status, double tiny_rel2, double* tail, cudaStream_t st);
 
 // Householder RQ of a row-major m x n block: A = R Q with Q (k x n) orthonormal rows, R (m x k), k = min(m, n).
 // Scratch holds n*m + n*k + k doubles per block.
@@ -126,5 +133,8 @@ void launch_lz_orth_beta(double* w, const double* vj, const double* vjm1, i64 n,
 void launch_lz_next(const double* w, double* vj1, i64 n, int j, const LanczosScalars* sc, cudaStream_t st);
 void launch_lz_tridiag(int maxiter, LanczosScalars* sc, cudaStream_t st);
 void launch_lz_ritz(const double* V, i64 n, int maxiter, const LanczosScalars* sc, double* out, cudaStream_t st);
+
+// Sustained FP64 FMA rate of the device in TFLOP/s (register-resident FMA chains).
+double measure_fp64_fma_tflops(int device);
 
 }  // namespace ctg

@@ -16,150 +16,6 @@ __device__ __forceinline__ double warp_sum(double v)
 }
 
 // ------------------------------------------------------------------------------------
-// block SVD: one-sided (Hestenes) Jacobi, one CTA per block.
-// Replaces LAPACK dgesvd in dense_tensor_svd_fill (dense_tensor.c:3538-3680); the
-// singular values agree to rounding, the singular vectors up to the usual sign /
-// degenerate-subspace freedom.
-// ------------------------------------------------------------------------------------
-
-constexpr int SVD_THREADS = 256;
-constexpr int SVD_MAX_SWEEPS = 60;
-
-__global__ void __launch_bounds__(SVD_THREADS)
-k_svd_jacobi(const SvdDesc* __restrict__ descs, const double* __restrict__ a, double* __restrict__ u, double* __restrict__ s,
-             double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status)
-{
-	const SvdDesc d = descs[blockIdx.x];
-	const int m = d.m, n = d.n;
-	const bool tall = m >= n;
-	const int M = tall ? m : n, N = tall ? n : m;
-	double* W = scratch + d.w_off;             // M x N, column-major
-	double* V = W + (i64)M * N;                // N x N, column-major
-	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = SVD_THREADS / 32;
-	const double* ab = a + d.a_off;
-	for (i64 e = tid; e < (i64)M * N; e += SVD_THREADS)
-	{
-		const i64 col = e / M, row = e % M;
-		W[e] = tall ? ab[row * n + col] : ab[col * n + row];
-	}
-	for (i64 e = tid; e < (i64)N * N; e += SVD_THREADS) V[e] = (e / N == e % N) ? 1.0 : 0.0;
-	__syncthreads();
-
-	__shared__ int rotated;
-	const double tol = sqrt((double)M) * DBL_EPSILON;
-	const int Np = N + (N & 1);
-	int sweep = 0;
-	for (; sweep < SVD_MAX_SWEEPS && N > 1; sweep++)
-	{
-		if (tid == 0) rotated = 0;
-		__syncthreads();
-		for (int rnd = 0; rnd < Np - 1; rnd++)
-		{
-			for (int pi = warp; pi < Np / 2; pi += nwarps)
-			{
-				// circle-method round-robin pairing
-				int p, q;
-				if (pi == 0) { p = rnd; q = Np - 1; }
-				else { p = (rnd + pi) % (Np - 1); q = (rnd - pi + (Np - 1)) % (Np - 1); }
-				if (p > q) { const int t = p; p = q; q = t; }
-				if (q >= N) continue;
-				double* wp = W + (i64)p * M;
-				double* wq = W + (i64)q * M;
-				double al = 0, be = 0, ga = 0;
-				for (int r = lane; r < M; r += 32)
-				{
-					const double x = wp[r], y = wq[r];
-					al = fma(x, x, al);
-					be = fma(y, y, be);
-					ga = fma(x, y, ga);
-				}
-				al = warp_sum(al);
-				be = warp_sum(be);
-				ga = warp_sum(ga);
-				if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be))
-				{
-					const double zeta = (be - al) / (2.0 * ga);
-					const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-					const double c = 1.0 / sqrt(1.0 + t * t);
-					const double sn = c * t;
-					for (int r = lane; r < M; r += 32)
-					{
-						const double x = wp[r], y = wq[r];
-						wp[r] = c * x - sn * y;
-						wq[r] = sn * x + c * y;
-					}
-					double* vp = V + (i64)p * N;
-					double* vq = V + (i64)q * N;
-					for (int r = lane; r < N; r += 32)
-					{
-						const double x = vp[r], y = vq[r];
-						vp[r] = c * x - sn * y;
-						vq[r] = sn * x + c * y;
-					}
-					if (lane == 0) rotated = 1;
-				}
-			}
-			__syncthreads();
-		}
-		if (!rotated) break;
-		__syncthreads();
-	}
-	if (tid == 0 && sweep >= SVD_MAX_SWEEPS) atomicExch(status, -1);
-
-	// column norms = singular values; rank by descending value (ties by column index)
-	extern __shared__ double sig[];            // N values
-	for (int c = warp; c < N; c += nwarps)
-	{
-		const double* wc = W + (i64)c * M;
-		double acc = 0;
-		for (int r = lane; r < M; r += 32) acc = fma(wc[r], wc[r], acc);
-		acc = warp_sum(acc);
-		if (lane == 0) sig[c] = sqrt(acc);
-	}
-	__syncthreads();
-	const int k = N;
-	for (int c = tid; c < N; c += SVD_THREADS)
-	{
-		int rank = 0;
-		const double sc = sig[c];
-		for (int c2 = 0; c2 < N; c2++)
-			if (sig[c2] > sc || (sig[c2] == sc && c2 < c)) rank++;
-		s[d.s_off + rank] = sc;
-	}
-	__syncthreads();
-	// write u (m x k) and vh (k x n), row-major
-	for (int c = warp; c < N; c += nwarps)
-	{
-		const double sc = sig[c];
-		int rank = 0;
-		for (int c2 = 0; c2 < N; c2++)
-			if (sig[c2] > sc || (sig[c2] == sc && c2 < c)) rank++;
-		const double inv = sc > 0 ? 1.0 / sc : 0.0;
-		const double* wc = W + (i64)c * M;
-		const double* vc = V + (i64)c * N;
-		if (tall)
-		{
-			for (int r = lane; r < m; r += 32) u[d.u_off + (i64)r * k + rank] = wc[r] * inv;
-			for (int r = lane; r < n; r += 32) vh[d.v_off + (i64)rank * n + r] = vc[r];
-		}
-		else
-		{
-			for (int r = lane; r < m; r += 32) u[d.u_off + (i64)r * k + rank] = vc[r];
-			for (int r = lane; r < n; r += 32) vh[d.v_off + (i64)rank * n + r] = wc[r] * inv;
-		}
-	}
-}
-
-void launch_svd_jacobi(int nblocks, const SvdDesc* descs, const double* a, double* u, double* s, double* vh,
-                       double* scratch, int* status, cudaStream_t st)
-{
-	if (nblocks <= 0) return;
-	// dynamic shared memory: singular values of the largest block (at most 4096 columns)
-	k_svd_jacobi<<<nblocks, SVD_THREADS, 4096 * sizeof(double), st>>>(descs, a, u, s, vh, scratch, status);
-	CTG_CUDA(cudaGetLastError());
-}
-
-// ------------------------------------------------------------------------------------
 // block RQ through a Householder QR of the transpose, one CTA per block.
 // Replaces LAPACK dgerqf + dorgrq in dense_tensor_rq_fill (dense_tensor.c:2680-2880):
 // A = R Q with orthonormal rows of Q; R is the transpose of the triangular QR factor.
@@ -448,7 +304,8 @@ __global__ void k_tridiag(int maxiter, LanczosScalars* sc)
 			diag += A[i * k + i] * A[i * k + i];
 			for (int j = i + 1; j < k; j++) off += A[i * k + j] * A[i * k + j];
 		}
-		if (off <= DBL_EPSILON * DBL_EPSILON * 1e-2 * diag || off == 0.0) break;
+		// off-diagonal norm below 1e-15 of the diagonal norm: converged
+		if (off <= 1e-30 * diag || off == 0.0) break;
 		for (int p = 0; p < k - 1; p++)
 			for (int q = p + 1; q < k; q++)
 			{

@@ -32,7 +32,14 @@ EXPORTS = [
     "ctgpu_contraction_operator_step_right",
     "ctgpu_block_sparse_tensor_svd_values",
     "ctgpu_delete_block_sparse_tensor",
+    "ctgpu_set_profiling",
+    "ctgpu_set_l2_flush_bytes",
+    "ctgpu_get_sweep_times",
+    "ctgpu_get_kernel_profile",
+    "ctgpu_measure_fp64_tflops",
 ]
+
+KERNEL_CLASSES = ["block_gemm", "permute", "row_map", "axis_scale", "block_svd", "block_rq", "lanczos_vector"]
 
 
 class Stats(C.Structure):
@@ -41,7 +48,7 @@ class Stats(C.Structure):
         ("setup_s", C.c_double), ("sweep_s", C.c_double), ("lanczos_ms", C.c_double),
         ("split_ms", C.c_double), ("env_ms", C.c_double), ("matvec_flops", C.c_double),
         ("total_gemm_flops", C.c_double), ("matvecs", C.c_long), ("kernel_launches", C.c_long),
-        ("sweeps", C.c_int), ("max_bond_dim", C.c_int64),
+        ("sweeps", C.c_int), ("max_bond_dim", C.c_int64), ("svd_max_sweeps", C.c_int),
     ]
 
 
@@ -67,6 +74,12 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_block_sparse_tensor_svd_values.argtypes = [P, P, P]
     lib.ctgpu_delete_block_sparse_tensor.argtypes = [P]
     lib.ctgpu_delete_block_sparse_tensor.restype = None
+    lib.ctgpu_set_profiling.argtypes = [C.c_int, C.c_int]
+    lib.ctgpu_set_l2_flush_bytes.argtypes = [C.c_int64]
+    lib.ctgpu_set_l2_flush_bytes.restype = None
+    lib.ctgpu_get_sweep_times.argtypes = [P, P, C.c_int]
+    lib.ctgpu_get_kernel_profile.argtypes = [C.c_int, P, P, P, P]
+    lib.ctgpu_measure_fp64_tflops.restype = C.c_double
     return lib
 
 
@@ -88,6 +101,23 @@ def last_stats() -> dict:
     s = Stats()
     lib().ctgpu_get_last_stats(C.byref(s))
     return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+
+def sweep_times():
+    n = lib().ctgpu_get_sweep_times(None, None, 0)
+    ms = np.zeros(max(n, 1))
+    la = np.zeros(max(n, 1), dtype=np.int64)
+    lib().ctgpu_get_sweep_times(ms.ctypes.data, la.ctypes.data, n)
+    return ms[:n], la[:n]
+
+
+def kernel_profile() -> dict:
+    out = {}
+    for i, name in enumerate(KERNEL_CLASSES):
+        la, ms, fl, by = C.c_long(), C.c_double(), C.c_double(), C.c_double()
+        lib().ctgpu_get_kernel_profile(i, C.byref(la), C.byref(ms), C.byref(fl), C.byref(by))
+        out[name] = {"launches": la.value, "ms": ms.value, "flops": fl.value, "bytes": by.value}
+    return out
 
 
 def set_precision(p: int) -> int:

@@ -60,11 +60,35 @@ struct ctgpu_stats
 	long   kernel_launches;   /* kernels launched by the call */
 	int    sweeps;
 	ct_long max_bond_dim;
+	int    svd_max_sweeps;    /* largest Jacobi sweep count of any block SVD */
 };
 int ctgpu_get_last_stats(struct ctgpu_stats* out);
 
 /* Message of the most recent failure in this thread ("" if none). */
 const char* ctgpu_last_error(void);
+
+/* Measurement hooks (no counterpart in the reference, which only times whole calls). */
+
+/* Time every kernel launch of subsequent calls by kernel class with CUDA events, from sweep
+ * skip_sweeps on. Returns the previous setting. */
+int ctgpu_set_profiling(int enable, int skip_sweeps);
+
+/* Overwrite a device buffer of this many bytes before every sweep (0 = off), so that each
+ * sweep starts with a cold L2. */
+void ctgpu_set_l2_flush_bytes(ct_long bytes);
+
+/* Device time (ms, CUDA events on the call's stream) and kernel launches of every sweep of the
+ * most recent call; fills up to max entries and returns the number of sweeps. */
+int ctgpu_get_sweep_times(double* ms, long* launches, int max);
+
+/* Profile of one kernel class over the profiled sweeps of the most recent call:
+ * 0 block GEMM, 1 permute, 2 row map, 3 axis scaling, 4 block SVD, 5 block RQ, 6 Lanczos vectors.
+ * flops = algorithmic FLOPs (GEMM: sum of 2 m n k), bytes = algorithmic bytes moved. */
+int ctgpu_get_kernel_profile(int cls, long* launches, double* ms, double* flops, double* bytes);
+
+/* FP64 FMA throughput of the current device in TFLOP/s, measured with register-resident FMA
+ * chains (the roofline denominator of the FP64 path); -1 on failure. */
+double ctgpu_measure_fp64_tflops(void);
 
 /* ---- inputs ------------------------------------------------------------------------------ */
 

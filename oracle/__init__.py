@@ -56,6 +56,7 @@ def port() -> C.CDLL:
         lib.oracle_delete_block_sparse_tensor.argtypes = [P]
         lib.oracle_delete_block_sparse_tensor.restype = None
         lib.oracle_set_num_threads.argtypes = [C.c_int]
+        lib.oracle_get_sweep_times.argtypes = [P, C.c_int]
         _port = lib
     return _port
 

@@ -17,6 +17,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <omp.h>
+#include <time.h>
 #include "ct_oracle.h"
 
 /* ---- BLAS / LAPACK (OpenBLAS bundled with scipy: LP64, "scipy_" prefix) ---- */
@@ -1207,6 +1208,25 @@ static int minimize_local_energy(const struct block_sparse_tensor* w, const stru
 	return ret;
 }
 
+/* ---- per-sweep wall time of the last call (CLOCK_MONOTONIC, as src/util/timing.c:26-41) ---- */
+
+#define MAX_SWEEP_TIMES 1024
+static double g_sweep_times[MAX_SWEEP_TIMES];
+static int g_num_sweep_times = 0;
+
+static double wall_seconds(void)
+{
+	struct timespec ts;
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+int oracle_get_sweep_times(double* out, int max)
+{
+	for (int i = 0; i < g_num_sweep_times && i < max; i++) out[i] = g_sweep_times[i];
+	return g_num_sweep_times;
+}
+
 /* ---- dmrg_twosite (dmrg.c:262-399) ---- */
 
 int oracle_dmrg_twosite(const struct mpo* ham, int num_sweeps, int maxiter, double tol_split, ct_long max_vdim,
@@ -1231,8 +1251,10 @@ int oracle_dmrg_twosite(const struct mpo* ham, int num_sweeps, int maxiter, doub
 	for (int i = 0; i < L - 1; i++) merge_mpo_pair(&ham->a[i], &ham->a[i + 1], &h2[i]);
 
 	int ret = 0;
+	g_num_sweep_times = 0;
 	for (int n = 0; n < num_sweeps && ret == 0; n++)
 	{
+		const double t_sweep = wall_seconds();
 		double en = 0;
 		for (int i = 0; i < L - 2 && ret == 0; i++)
 		{
@@ -1273,6 +1295,7 @@ int oracle_dmrg_twosite(const struct mpo* ham, int num_sweeps, int maxiter, doub
 		if (local_orthonormalize_rq(&psi->a[0], &t) < 0) ret = -1;
 		oracle_delete_block_sparse_tensor(&t);
 		en_sweeps[n] = en;
+		if (g_num_sweep_times < MAX_SWEEP_TIMES) g_sweep_times[g_num_sweep_times++] = wall_seconds() - t_sweep;
 	}
 
 	for (int i = 0; i < L - 1; i++) oracle_delete_block_sparse_tensor(&h2[i]);

@@ -61,6 +61,9 @@ int oracle_lanczos_dense(ct_long n, const double* h, const double* vstart, int m
 /* release a tensor allocated by any oracle routine (free() on every array) */
 void oracle_delete_block_sparse_tensor(struct block_sparse_tensor* t);
 
+/* wall time in seconds of every sweep of the last oracle_dmrg_twosite call; returns the count */
+int oracle_get_sweep_times(double* out, int max);
+
 /* number of OpenMP threads the oracle runs with (set via OMP_NUM_THREADS or this call) */
 int oracle_set_num_threads(int n);
 

@@ -131,3 +131,39 @@ def test_svd_values_match_oracle(gpu, oracle_port, shape):
     oracle_port.oracle_delete_block_sparse_tensor(C.byref(u))
     oracle_port.oracle_delete_block_sparse_tensor(C.byref(vh))
     cs.free_bst(ca)
+
+
+@pytest.mark.parametrize("rank,noise", [(30, 1e-17), (30, 1e-15), (60, 0.0), (110, 1e-16)])
+def test_svd_values_rank_deficient_blocks(gpu, oracle_port, rank, noise):
+    """Two-site DMRG matrices are numerically rank deficient: exact low rank plus rounding-level
+    noise, several blocks of ~120 columns (the shape of the D=256 Hubbard bonds)."""
+    rng = np.random.default_rng(rank)
+    dims = (480, 500)
+    q0 = np.repeat(np.arange(4, dtype=np.int32), 120)
+    q1 = np.repeat(np.arange(4, dtype=np.int32), 125)
+    a = cs.BlockSparse(dims, (1, -1), [q0, q1])
+    for idx in a.allowed:
+        m, n = a.block_shape(idx)
+        u, _ = np.linalg.qr(rng.standard_normal((m, rank)))
+        v, _ = np.linalg.qr(rng.standard_normal((n, rank)))
+        s = np.logspace(0, -12, rank)
+        a.blocks[idx] = (u * s) @ v.T + noise * rng.standard_normal((m, n))
+    ca = c_bst(a)
+    sig = np.zeros(min(dims))
+    ns = C.c_int64()
+    assert gpu.ctgpu_block_sparse_tensor_svd_values(C.byref(ca), sig.ctypes.data, C.byref(ns)) == 0
+    u, vh = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+    sp, nsr = C.POINTER(C.c_double)(), C.c_int64()
+    assert oracle_port.oracle_block_sparse_tensor_svd(C.byref(ca), C.byref(u), C.byref(sp), C.byref(nsr), C.byref(vh)) == 0
+    ref = np.ctypeslib.as_array(sp, shape=(nsr.value,)).copy()
+    got = sig[:ns.value]
+    # dgesvd (the oracle) resolves singular values to ~eps sigma_max absolute: compare those above
+    # 1e-6 sigma_max relatively (retained values in DMRG lie above ~1e-5 sigma_max, bar 1e-8) and
+    # all of them at the oracle's own absolute accuracy
+    big = ref > 1e-6 * ref.max()
+    np.testing.assert_allclose(got[big], ref[big], rtol=1e-9)
+    # directions at the rounding floor are resolved to ~(m + n) eps sigma_max absolute
+    np.testing.assert_allclose(got, ref, rtol=0, atol=2e-12 * ref.max())
+    oracle_port.oracle_delete_block_sparse_tensor(C.byref(u))
+    oracle_port.oracle_delete_block_sparse_tensor(C.byref(vh))
+    cs.free_bst(ca)
