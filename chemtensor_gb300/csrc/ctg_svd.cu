@@ -22,6 +22,8 @@
 // whole cluster, separated by cluster barriers (release / acquire at cluster scope for the
 // global-memory data, which is read with L2-coherent loads).
 #include <cfloat>
+#include <cstdio>
+#include <mutex>
 
 #include <cooperative_groups.h>
 
@@ -380,6 +382,132 @@ k_svd_cluster(const SvdDesc* __restrict__ descs, const double* __restrict__ a, d
 }
 
 }  // namespace
+
+// ------------------------------------------------------------------------------------
+// SVD of one dense block without any device allocation
+// ------------------------------------------------------------------------------------
+// Some callers cannot allocate device memory while they run: a service whose device memory is
+// fully reserved up front by its own pool, or code whose stream must not be stalled by the
+// implicit device-wide synchronisation of cudaMalloc / cudaFree. For them the block SVD has a
+// variant whose workspace is this fixed array: every GPU that loads the library keeps it
+// (4 MiB) until the process exits, and it bounds the block to NOALLOC_SVD_MAX_DIM rows and
+// columns. All calls share the array, so calls whose work overlaps on the GPU (for example on
+// two streams) race on it and must be serialised by the caller.
+
+constexpr int NOALLOC_SVD_MAX_DIM = 256;
+constexpr i64 NOALLOC_SCRATCH_DOUBLES = (i64)1 << 19;   // 4 MiB
+
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+namespace {
+
+// layout of the fixed array: descriptor, status[2] + tail (as doubles), then the SVD workspace
+constexpr i64 NA_DESC = 0;
+constexpr i64 NA_STATUS = (sizeof(SvdDesc) + 7) / 8;
+constexpr i64 NA_WORK = NA_STATUS + 2;
+
+__global__ void k_noalloc_prepare(double* base, SvdDesc d, double* u, double* s, double* vh)
+{
+	// the array keeps the previous call's contents: reset everything that must start at zero
+	if (blockIdx.x == 0 && threadIdx.x == 0)
+	{
+		*(SvdDesc*)(base + NA_DESC) = d;
+		int* status = (int*)(base + NA_STATUS);
+		status[0] = 0;
+		status[1] = 0;
+		base[NA_STATUS + 1] = 0.0;                  // tail weight
+	}
+	// factor entries beyond the numerical rank are not written by the SVD kernel
+	const i64 k = d.m < d.n ? d.m : d.n;
+	const i64 stride = (i64)gridDim.x * blockDim.x;
+	for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < (i64)d.m * k; e += stride) u[e] = 0.0;
+	for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < k * (i64)d.n; e += stride) vh[e] = 0.0;
+	for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < k; e += stride) s[e] = 0.0;
+}
+
+__global__ void k_noalloc_finish(const double* base, int* info)
+{
+	*info = ((const int*)(base + NA_STATUS))[0];
+}
+
+}  // namespace
+
+}  // namespace ctg
+
+extern "C" int ctgpu_dense_svd_noalloc(const double* d_a, int m, int n, double* d_u, double* d_s, double* d_vh,
+                                       int* d_info, void* stream)
+{
+	using namespace ctg;
+	if (m < 1 || n < 1 || m > NOALLOC_SVD_MAX_DIM || n > NOALLOC_SVD_MAX_DIM)
+	{
+		fprintf(stderr, "ctgpu_dense_svd_noalloc: block of %d x %d is outside 1..%d rows and columns\n", m, n,
+		        NOALLOC_SVD_MAX_DIM);
+		return -5;
+	}
+	if (NA_WORK + svd_scratch_doubles(m, n) > NOALLOC_SCRATCH_DOUBLES) return -5;
+	if (!d_a || !d_u || !d_s || !d_vh || !d_info) return -5;
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -5;
+	// device address of the fixed array, taken once per device with that device current
+	static double* addr[64] = {nullptr};
+	static std::mutex lock;
+	{
+		std::lock_guard<std::mutex> g(lock);
+		if (!addr[dev])
+		{
+			void* p = nullptr;
+			const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+			if (e != cudaSuccess)
+			{
+				fprintf(stderr, "ctgpu_dense_svd_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+				return -5;
+			}
+			addr[dev] = (double*)p;
+		}
+	}
+	double* base = addr[dev];
+	cudaStream_t st = (cudaStream_t)stream;
+	SvdDesc d = {};
+	d.a_off = 0;
+	d.u_off = 0;
+	d.s_off = 0;
+	d.v_off = 0;
+	d.w_off = 0;
+	d.m = m;
+	d.n = n;
+	k_noalloc_prepare<<<64, 256, 0, st>>>(base, d, d_u, d_s, d_vh);
+	const int cl = 8;
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3((unsigned)cl);
+	cfg.blockDim = dim3(SVD_THREADS);
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = st;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = (unsigned)cl;
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	const SvdDesc* descs = (const SvdDesc*)(base + NA_DESC);
+	int* status = (int*)(base + NA_STATUS);
+	double* tail = base + NA_STATUS + 1;
+	cudaError_t e = cudaLaunchKernelEx(&cfg, k_svd_cluster, descs, d_a, d_u, d_s, d_vh, base + NA_WORK, status, 0.0,
+	                                   tail, cl);
+	if (e == cudaSuccess)
+	{
+		k_noalloc_finish<<<1, 1, 0, st>>>(base, d_info);
+		e = cudaGetLastError();
+	}
+	if (e != cudaSuccess)
+	{
+		fprintf(stderr, "ctgpu_dense_svd_noalloc: launch failed: %s\n", cudaGetErrorString(e));
+		return -5;
+	}
+	return 0;
+}
+
+namespace ctg {
 
 i64 svd_scratch_doubles(int m, int n)
 {

@@ -130,6 +130,24 @@ int ctgpu_block_sparse_tensor_svd_values(const struct block_sparse_tensor* a, do
 /* release a tensor returned by one of the calls above (free() on every array) */
 void ctgpu_delete_block_sparse_tensor(struct block_sparse_tensor* t);
 
+/* SVD of one dense row-major m x n FP64 matrix that is already in device memory, for callers
+ * that must not allocate device memory while they run (for example a service whose device memory
+ * is reserved up front by its own pool, or code whose stream must not be stalled by the implicit
+ * device-wide synchronisation of cudaMalloc / cudaFree). It allocates nothing: its workspace is a
+ * fixed 4 MiB array inside the library, held on every GPU that loads the library until the
+ * process exits, which limits m and n to 1..256.
+ * Outputs (device memory, row-major): d_u (m x k), d_s (k), d_vh (k x n), k = min(m, n), singular
+ * values in descending order; *d_info (device) becomes 0, or -1 if the Jacobi iteration did not
+ * converge. The work is queued on 'stream' (a cudaStream_t, or NULL for the legacy default stream)
+ * and the call returns without waiting; it returns 0 once queued, -5 for sizes outside 1..256, a
+ * null pointer or a CUDA error. The first call on a device looks up the array's device address
+ * (once per device, with that device current); make that first call before any stream capture.
+ * All calls share the array, so calls whose work overlaps on the GPU race and must be serialised
+ * by the caller.
+ * No counterpart in the reference, which computes block SVDs with LAPACK on the host. */
+int ctgpu_dense_svd_noalloc(const double* d_a, int m, int n, double* d_u, double* d_s, double* d_vh,
+	int* d_info, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
