@@ -43,7 +43,7 @@ WORKLOAD = {"workload": "fermi_hubbard_1d L=32 t=1 U=4 mu=0 (N,2Sz)=(32,0) D=256
 METRIC = "two-site DMRG sweeps/s (Fermi-Hubbard L=32, D=256)"
 UNIT = "sweeps/s"
 L2_FLUSH_BYTES = 256 << 20
-PRECISIONS = {"fp64": 0, "bf16x3": 1, "tf32": 2}
+PRECISIONS = {"fp64": 0, "bf16x3": 1}
 
 
 def build_inputs():
@@ -252,7 +252,7 @@ def bench_gpu(args, world, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_dev / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp64": "f64", "bf16x3": "bf16x3+f32acc", "tf32": "tf32+f32acc"}[args.precision],
+        "dtype": {"fp64": "f64", "bf16x3": "bf16x3+f32acc, final sweep f64"}[args.precision],
         "data": "synthetic",
         "config": {"workload": w["workload"], "precision": args.precision, "parallelism": f"replicas x{world}",
                    "l2": "256 MiB buffer overwritten before every sweep"},

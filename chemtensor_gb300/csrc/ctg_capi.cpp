@@ -11,7 +11,7 @@ namespace {
 thread_local std::string g_last_error;
 thread_local ctg::DmrgOptions g_opts = [] {
 	ctg::DmrgOptions o;
-	if (const char* p = std::getenv("CTGPU_PRECISION")) o.precision = std::atoi(p);
+	if (const char* p = std::getenv("CTGPU_PRECISION")) o.precision = std::atoi(p) == ctg::GEMM_BF16X3 ? ctg::GEMM_BF16X3 : ctg::GEMM_FP64;
 	if (const char* d = std::getenv("CTGPU_DEVICE")) o.device = std::atoi(d);
 	return o;
 }();
@@ -53,8 +53,9 @@ int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int 
 
 int ctgpu_set_precision(int precision)
 {
+	if (precision != ctg::GEMM_FP64 && precision != ctg::GEMM_BF16X3) return ERR_RUNTIME;
 	const int old = g_opts.precision;
-	if (precision >= ctg::GEMM_FP64 && precision <= ctg::GEMM_TF32) g_opts.precision = precision;
+	g_opts.precision = precision;
 	return old;
 }
 
@@ -127,7 +128,7 @@ int ctgpu_block_sparse_tensor_dot(const struct block_sparse_tensor* s, int axran
 	return guarded([&] {
 		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
 		ctg::DTensor ds = ctg::tensor_from_struct(c, s), dt = ctg::tensor_from_struct(c, t);
-		ctg::DTensor dr = ctg::op_dot(c, ds, axrange_s, dt, axrange_t, ndim_mult);
+		ctg::DTensor dr = ctg::op_dot(c, ds, axrange_s, dt, axrange_t, ndim_mult, g_opts.precision);
 		ctg::tensor_to_struct(c, dr, r);
 		return 0;
 	});
@@ -164,7 +165,7 @@ int ctgpu_contraction_operator_step_left(const struct block_sparse_tensor* a, co
 	return guarded([&] {
 		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
 		ctg::DTensor da = ctg::tensor_from_struct(c, a), dw = ctg::tensor_from_struct(c, w), dl = ctg::tensor_from_struct(c, l);
-		ctg::tensor_to_struct(c, ctg::contraction_step_left(c, da, dw, dl), l_next);
+		ctg::tensor_to_struct(c, ctg::contraction_step_left(c, da, dw, dl, g_opts.precision), l_next);
 		return 0;
 	});
 }
@@ -175,7 +176,7 @@ int ctgpu_contraction_operator_step_right(const struct block_sparse_tensor* a, c
 	return guarded([&] {
 		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
 		ctg::DTensor da = ctg::tensor_from_struct(c, a), dw = ctg::tensor_from_struct(c, w), dr = ctg::tensor_from_struct(c, r);
-		ctg::tensor_to_struct(c, ctg::contraction_step_right(c, da, dw, dr), r_next);
+		ctg::tensor_to_struct(c, ctg::contraction_step_right(c, da, dw, dr, g_opts.precision), r_next);
 		return 0;
 	});
 }

@@ -39,7 +39,6 @@ enum AxRange { AX_LEADING = 0, AX_TRAILING = 1 };
 enum GemmPrecision {
 	GEMM_FP64 = 0,        // plain IEEE double on the FP64 pipe
 	GEMM_BF16X3 = 1,      // split-BF16, 3 products, FP32 accumulation on tcgen05
-	GEMM_TF32 = 2,        // TF32 on tcgen05, FP32 accumulation
 };
 
 }  // namespace ctg

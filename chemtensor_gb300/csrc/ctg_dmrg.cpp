@@ -214,31 +214,31 @@ DTensor merge_mpo_pair(Ctx& c, const DTensor& w0, const DTensor& w1)
 }  // namespace
 
 // contraction_operator_step_left (src/algorithm/chain_ops.c:196-245), with b = a
-DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l)
+DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, int precision)
 {
 	DTensor br = view_reversed(a);
-	DTensor s = op_dot(c, l, AX_TRAILING, br, AX_LEADING, 1);
+	DTensor s = op_dot(c, l, AX_TRAILING, br, AX_LEADING, 1, precision);
 	const int p0[5] = {0, 1, 4, 2, 3};
 	DTensor t = op_transpose(c, s, p0);
-	s = op_dot(c, t, AX_TRAILING, w, AX_LEADING, 2);
+	s = op_dot(c, t, AX_TRAILING, w, AX_LEADING, 2, precision);
 	const int p1[5] = {1, 3, 4, 2, 0};
 	t = op_transpose(c, s, p1);
-	s = op_dot(c, a, AX_LEADING, t, AX_LEADING, 2);
+	s = op_dot(c, a, AX_LEADING, t, AX_LEADING, 2, precision);
 	const int p2[4] = {3, 0, 1, 2};
 	return op_transpose(c, s, p2);
 }
 
 // contraction_operator_step_right (src/algorithm/chain_ops.c:116-165), with b = a
-DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& r)
+DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& r, int precision)
 {
-	DTensor s = op_dot(c, a, AX_TRAILING, r, AX_LEADING, 1);
+	DTensor s = op_dot(c, a, AX_TRAILING, r, AX_LEADING, 1, precision);
 	const int p0[5] = {1, 2, 0, 3, 4};
 	DTensor t = op_transpose(c, s, p0);
-	s = op_dot(c, w, AX_TRAILING, t, AX_LEADING, 2);
+	s = op_dot(c, w, AX_TRAILING, t, AX_LEADING, 2, precision);
 	const int p1[5] = {4, 2, 0, 1, 3};
 	t = op_transpose(c, s, p1);
 	DTensor br = view_reversed(a);
-	s = op_dot(c, t, AX_TRAILING, br, AX_TRAILING, 2);
+	s = op_dot(c, t, AX_TRAILING, br, AX_TRAILING, 2, precision);
 	const int p2[4] = {1, 2, 3, 0};
 	return op_transpose(c, s, p2);
 }
@@ -370,17 +370,17 @@ struct LocalH {
 	DBufPtr s1, tt1, s2, tt2;
 	double flops = 0;
 
-	LocalH(Ctx& c, const Meta& a, const DTensor& w_, const DTensor& l, const DTensor& r_) : w(w_), r(r_)
+	LocalH(Ctx& c, const Meta& a, const DTensor& w_, const DTensor& l, const DTensor& r_, int precision) : w(w_), r(r_)
 	{
-		d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1);
+		d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1, precision);
 		const int p0[5] = {1, 2, 0, 3, 4};
 		t0 = make_transpose_plan(c, *d1.out, p0);
-		d2 = make_dot_plan(c, w.m(), AX_TRAILING, *t0.out, AX_LEADING, 2);
+		d2 = make_dot_plan(c, w.m(), AX_TRAILING, *t0.out, AX_LEADING, 2, precision);
 		const int p1[5] = {2, 0, 1, 3, 4};
 		t1 = make_transpose_plan(c, *d2.out, p1);
 		const int p2[4] = {0, 3, 1, 2};
 		k = op_transpose(c, l, p2);
-		d3 = make_dot_plan(c, k.m(), AX_TRAILING, *t1.out, AX_LEADING, 2);
+		d3 = make_dot_plan(c, k.m(), AX_TRAILING, *t1.out, AX_LEADING, 2, precision);
 		// the cyclic partial trace of the unit outer bonds keeps blocks and entries (view_trace_unit)
 		const Meta& o = *d3.out;
 		std::vector<std::vector<q32>> ql(o.ql.begin() + 1, o.ql.end() - 1);
@@ -407,9 +407,9 @@ struct LocalH {
 // minimize_local_energy (src/algorithm/dmrg.c:86-147) with lanczos_iteration_d and
 // eigensystem_krylov_symmetric (src/util/krylov.c:24-89, :172-251) on the device
 int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTensor& r, const DTensor& a_start, int maxiter,
-                          LanczosScalars* d_sc, DTensor& a_opt, DmrgStats* st)
+                          LanczosScalars* d_sc, DTensor& a_opt, DmrgStats* st, int precision)
 {
-	LocalH h(c, a_start.m(), w, l, r);
+	LocalH h(c, a_start.m(), w, l, r, precision);
 	const i64 n = a_start.m().nnz;
 	DBuf V(&c, (size_t)maxiter * n * sizeof(double));
 	DBuf wv(&c, (size_t)n * sizeof(double));
@@ -456,8 +456,7 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,
                                      int precision)
 {
-	(void)precision;
-	LocalH h(c, a.m(), w, l, r);
+	LocalH h(c, a.m(), w, l, r, precision);
 	DTensor out = c.empty(a.m());
 	h.apply(c, a.data(), out.data());
 	return out;
@@ -533,11 +532,11 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 
 	cudaEvent_t ev[4];
 	for (auto& e : ev) CTG_CUDA(cudaEventCreate(&e));
-	auto bond_step = [&](int i, bool left_to_right) -> int {
+	auto bond_step = [&](int i, bool left_to_right, int prec) -> int {
 		CTG_CUDA(cudaEventRecord(ev[0], c.stream()));
 		DTensor cur = merge_mps_pair(c, A[i], A[i + 1]);
 		DTensor aopt;
-		int r = minimize_local_energy(c, h2[i], lb[i], rb[i + 1], cur, maxiter, d_sc, aopt, st);
+		int r = minimize_local_energy(c, h2[i], lb[i], rb[i + 1], cur, maxiter, d_sc, aopt, st, prec);
 		if (r < 0) return r;
 		CTG_CUDA(cudaEventRecord(ev[1], c.stream()));
 		double ent = 0;
@@ -546,11 +545,13 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		CTG_CUDA(cudaMemcpy(&h_sc, d_sc, sizeof(LanczosScalars), cudaMemcpyDeviceToHost));
 		if (h_sc.status != 0) return h_sc.status;
 		CTG_CUDA(cudaEventRecord(ev[2], c.stream()));
-		if (left_to_right) lb[i + 1] = contraction_step_left(c, A[i], W[i], lb[i]);
+		// environments stay FP64 in every sweep: each one is built from its neighbour, so
+		// rounding errors of a reduced-precision product would accumulate along the chain
+		if (left_to_right) lb[i + 1] = contraction_step_left(c, A[i], W[i], lb[i], GEMM_FP64);
 		else
 		{
 			entropy[i] = ent;
-			rb[i] = contraction_step_right(c, A[i + 1], W[i + 1], rb[i + 1]);
+			rb[i] = contraction_step_right(c, A[i + 1], W[i + 1], rb[i + 1], GEMM_FP64);
 		}
 		CTG_CUDA(cudaEventRecord(ev[3], c.stream()));
 		CTG_CUDA(cudaEventSynchronize(ev[1]));
@@ -574,11 +575,14 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		c.sync();
 		c.profile = opt.profile && sw >= opt.profile_skip_sweeps;
 		const long launches0 = c.kernel_launches;
+		// reduced-precision local eigenproblems first; the trailing final_fp64_sweeps solve every
+		// local eigenproblem in FP64, so the returned state and energies are FP64 results
+		const int prec = sw < num_sweeps - std::max(opt.final_fp64_sweeps, 0) ? opt.precision : (int)GEMM_FP64;
 		CTG_CUDA(cudaEventRecord(sw_ev[0], c.stream()));
-		for (int i = 0; i < L - 2 && ret == 0; i++) ret = bond_step(i, true);
+		for (int i = 0; i < L - 2 && ret == 0; i++) ret = bond_step(i, true, prec);
 		for (int i = L - 2; i >= 0 && ret == 0; i--)
 		{
-			ret = bond_step(i, false);
+			ret = bond_step(i, false, prec);
 			if (ret == 0)
 			{
 				CTG_CUDA(cudaEventSynchronize(ev[3]));

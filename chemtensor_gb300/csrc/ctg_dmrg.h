@@ -49,8 +49,8 @@ struct TruncResult {
 TruncResult retained_bond_indices(const double* sigma, i64 n, double tol, bool relative_thresh, i64 max_vdim);
 
 // environment updates with b = a (src/algorithm/chain_ops.c:196-245, :116-165)
-DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l);
-DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& r);
+DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, int precision = GEMM_FP64);
+DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& r, int precision = GEMM_FP64);
 
 // one application of the local two-site Hamiltonian (src/algorithm/chain_ops.c:353-390)
 DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,

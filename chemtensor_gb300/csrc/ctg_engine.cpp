@@ -74,6 +74,28 @@ void Ctx::sync()
 	CTG_CUDA(cudaStreamSynchronize(st_));
 	staging_used_ = 0;
 	prof_resolve();
+	if (tc_used_)
+	{
+		int flag = 0;
+		CTG_CUDA(cudaMemcpy(&flag, tc_error_, sizeof(int), cudaMemcpyDeviceToHost));
+		tc_used_ = false;
+		if (flag != 0)
+		{
+			CTG_CUDA(cudaMemset(tc_error_, 0, sizeof(int)));
+			throw std::runtime_error("ctgpu: a tensor-core GEMM timed out waiting for its MMAs");
+		}
+	}
+}
+
+int* Ctx::tc_error()
+{
+	if (!tc_error_)
+	{
+		CTG_CUDA(cudaMalloc(&tc_error_, sizeof(int)));
+		CTG_CUDA(cudaMemset(tc_error_, 0, sizeof(int)));
+	}
+	tc_used_ = true;
+	return tc_error_;
 }
 
 cudaEvent_t Ctx::get_event()
@@ -243,7 +265,7 @@ int tile_class(int m, int n)
 // dot (block_sparse_tensor.c:1826-2001; dense_tensor.c:1761-1837)
 // ------------------------------------------------------------------------------------
 
-DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult)
+DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
 {
 	DotPlan p;
 	auto out = std::make_shared<Meta>(dot_result_meta(s, axs, t, axt, nmult));
@@ -310,10 +332,22 @@ DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, in
 		}
 		o.nc = (int)cons.size() - o.c0;
 		CTG_CHECK(o.m >= 1 && o.n >= 1 && o.c_off + (i64)o.m * o.n <= r.nnz, "dot: output block out of range");
+		if (precision == GEMM_BF16X3)
+		{
+			// tensor-core tiles: one tile class
+			for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
+				for (int n0 = 0; n0 < o.n; n0 += tc_tile_cols()) tiles[0].push_back(GemmTile{b, m0, n0});
+			continue;
+		}
 		const int cls = tile_class(o.m, o.n);
 		const int tr = tile_rows(cls), tc = tile_cols(cls);
 		for (int m0 = 0; m0 < o.m; m0 += tr)
 			for (int n0 = 0; n0 < o.n; n0 += tc) tiles[cls].push_back(GemmTile{b, m0, n0});
+	}
+	p.precision = precision;
+	if (precision == GEMM_BF16X3)
+	{
+		for (int k = 1; k < NUM_TILE_CLASSES; k++) p.flops_cls[0] += p.flops_cls[k], p.flops_cls[k] = 0;
 	}
 	Packer pk;
 	const size_t o_outs = pk.add(outs);
@@ -334,6 +368,16 @@ DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, in
 
 void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 {
+	if (precision == GEMM_BF16X3)
+	{
+		if (ntiles[0] > 0)
+		{
+			KScope ks(c, K_GEMM_TC, 1, flops_cls[0], 0);
+			launch_gemm_bf16x3(ntiles[0], tiles[0], outs, cons, A, B, C, c.tc_error(), c.stream());
+		}
+		c.gemm_flops += flops;
+		return;
+	}
 	for (int k = 0; k < NUM_TILE_CLASSES; k++)
 	{
 		if (ntiles[k] == 0) continue;
@@ -559,9 +603,9 @@ CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& 
 // one-shot operations
 // ------------------------------------------------------------------------------------
 
-DTensor op_dot(Ctx& c, const DTensor& s, int axs, const DTensor& t, int axt, int nmult)
+DTensor op_dot(Ctx& c, const DTensor& s, int axs, const DTensor& t, int axt, int nmult, int precision)
 {
-	DotPlan p = make_dot_plan(c, s.m(), axs, t.m(), axt, nmult);
+	DotPlan p = make_dot_plan(c, s.m(), axs, t.m(), axt, nmult, precision);
 	DTensor r;
 	r.meta = p.out;
 	r.buf = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(p.out->nnz, 1) * sizeof(double));

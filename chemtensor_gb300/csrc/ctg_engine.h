@@ -18,7 +18,7 @@ namespace ctg {
 class Ctx;
 
 // kernel classes for profiling
-enum KClass { K_GEMM = 0, K_PERMUTE, K_ROWMAP, K_SCALE, K_SVD, K_RQ, K_LANCZOS, K_NUM_CLASSES };
+enum KClass { K_GEMM = 0, K_PERMUTE, K_ROWMAP, K_SCALE, K_SVD, K_RQ, K_LANCZOS, K_GEMM_TC, K_NUM_CLASSES };
 struct KProf {
 	long launches = 0;
 	double ms = 0;               // summed device time of the launches
@@ -75,6 +75,8 @@ public:
 	long kernel_launches = 0;
 	int svd_max_sweeps = 0;      // largest Jacobi sweep count of any block SVD
 	int svd_full_reruns = 0;     // SVDs repeated at full resolution for the truncation decision
+	// device flag raised by a tensor-core kernel whose bounded wait timed out (checked at sync)
+	int* tc_error();
 	int num_sms() const { return sms_; }
 	// optional per-kernel-class timing with CUDA events on this stream (resolved at sync points)
 	bool profile = false;
@@ -92,6 +94,8 @@ private:
 	cudaEvent_t get_event();
 	int dev_;
 	int sms_ = 1;
+	int* tc_error_ = nullptr;
+	bool tc_used_ = false;
 	cudaStream_t st_ = nullptr;
 	cudaMemPool_t pool_ = nullptr;
 	char* staging_ = nullptr;
@@ -113,9 +117,10 @@ struct DotPlan {
 	const GemmContrib* cons = nullptr;
 	double flops = 0;
 	double flops_cls[NUM_TILE_CLASSES] = {0, 0, 0};
+	int precision = GEMM_FP64;
 	void run(Ctx& c, const double* A, const double* B, double* C) const;
 };
-DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult);
+DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision = GEMM_FP64);
 
 struct CopyPlan {
 	std::shared_ptr<const Meta> out;
@@ -135,7 +140,7 @@ CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& 
 
 // ---- one-shot operations (plan + run) ------------------------------------------------
 
-DTensor op_dot(Ctx& c, const DTensor& s, int axs, const DTensor& t, int axt, int nmult);
+DTensor op_dot(Ctx& c, const DTensor& s, int axs, const DTensor& t, int axt, int nmult, int precision = GEMM_FP64);
 DTensor op_transpose(Ctx& c, const DTensor& t, const int* perm);
 DTensor op_flatten(Ctx& c, const DTensor& t, int ax, int newdir);
 DTensor op_split(Ctx& c, const DTensor& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq);

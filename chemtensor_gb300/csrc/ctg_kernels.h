@@ -39,6 +39,14 @@ int tile_cols(int cls);
 void launch_gemm_f64(int cls, int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
                      const double* A, const double* B, double* C, cudaStream_t st);
 
+// Same work lists on the tcgen05 tensor cores, split-BF16 (hi*hi + hi*lo + lo*hi, FP32
+// accumulation, FP64 in and out); tiles of tc_tile_rows() x tc_tile_cols(). *error becomes 1 if a
+// bounded wait inside the kernel timed out.
+int tc_tile_rows();
+int tc_tile_cols();
+void launch_gemm_bf16x3(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons, const double* A,
+                        const double* B, double* C, int* error, cudaStream_t st);
+
 // ---- data movement -----------------------------------------------------------
 // Generic per-block permutation: dst block (row-major over dims) gathers
 // src[src_off + sum_i idx_i * sstr_i].

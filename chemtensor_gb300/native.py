@@ -39,7 +39,12 @@ EXPORTS = [
     "ctgpu_measure_fp64_tflops",
 ]
 
-KERNEL_CLASSES = ["block_gemm", "permute", "row_map", "axis_scale", "block_svd", "block_rq", "lanczos_vector"]
+KERNEL_CLASSES = ["block_gemm", "permute", "row_map", "axis_scale", "block_svd", "block_rq", "lanczos_vector",
+                  "block_gemm_tc"]
+
+# arithmetic of the bulk block GEMMs (ctgpu_set_precision)
+PRECISION_FP64 = 0
+PRECISION_BF16X3 = 1
 
 
 class Stats(C.Structure):
@@ -121,7 +126,11 @@ def kernel_profile() -> dict:
 
 
 def set_precision(p: int) -> int:
-    return lib().ctgpu_set_precision(int(p))
+    """Select the block-GEMM arithmetic for later calls; returns the previous setting."""
+    old = lib().ctgpu_set_precision(int(p))
+    if old < 0:
+        raise ValueError(f"unknown precision {p}")
+    return old
 
 
 def random_mps(nsites: int, d: int, qsite, qnum_sector: int, max_vdim: int, seed: int) -> cs.MPS:

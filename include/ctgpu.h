@@ -36,8 +36,13 @@ int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int 
 	const double tol_split, const ct_long max_vdim, struct mps* psi, double* en_sweeps, double* entropy);
 
 /* Arithmetic of the bulk block GEMMs for subsequent calls from this thread.
- * 0 = FP64 (plain path), 1 = split-BF16 with FP32 accumulation, 2 = TF32 with FP32 accumulation.
- * The reference has no such setting (it always computes in FP64). Returns the previous value. */
+ * 0 = FP64 (plain path); 1 = split-BF16 on the tcgen05 tensor cores (each FP64 operand split
+ * into a high and a low BF16 part, three products hi*hi + hi*lo + lo*hi, FP32 accumulation,
+ * about 2^-16 relative error per product). With 1, dmrg_twosite runs all sweeps but the last in
+ * split-BF16 and the last sweep entirely in FP64, so returned energies and tensors are FP64
+ * results; the single-operation entry points below use the setting as given.
+ * The reference has no such setting (it always computes in FP64). Returns the previous value,
+ * or -5 for an unknown value (the setting is then unchanged). */
 int ctgpu_set_precision(int precision);
 
 /* CUDA device used by subsequent calls from this thread. Returns the previous device. */
@@ -82,7 +87,8 @@ void ctgpu_set_l2_flush_bytes(ct_long bytes);
 int ctgpu_get_sweep_times(double* ms, long* launches, int max);
 
 /* Profile of one kernel class over the profiled sweeps of the most recent call:
- * 0 block GEMM, 1 permute, 2 row map, 3 axis scaling, 4 block SVD, 5 block RQ, 6 Lanczos vectors.
+ * 0 block GEMM (FP64), 1 permute, 2 row map, 3 axis scaling, 4 block SVD, 5 block RQ,
+ * 6 Lanczos vectors, 7 block GEMM (split-BF16 tensor cores).
  * flops = algorithmic FLOPs (GEMM: sum of 2 m n k), bytes = algorithmic bytes moved. */
 int ctgpu_get_kernel_profile(int cls, long* launches, double* ms, double* flops, double* bytes);
 
