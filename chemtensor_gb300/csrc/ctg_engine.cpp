@@ -31,11 +31,46 @@ Ctx::Ctx(int device) : dev_(device)
 	CTG_CUDA(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &thr));
 	staging_cap_ = (size_t)64 << 20;
 	CTG_CUDA(cudaMallocHost((void**)&staging_, staging_cap_));
+	CTG_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
+	for (int i = 0; i < NUM_AUX; i++)
+	{
+		CTG_CUDA(cudaStreamCreateWithFlags(&aux_[i], cudaStreamNonBlocking));
+		CTG_CUDA(cudaEventCreateWithFlags(&join_ev_[i], cudaEventDisableTiming));
+	}
+}
+
+cudaStream_t Ctx::aux(int i)
+{
+	return aux_[i % NUM_AUX];
+}
+
+void Ctx::fork(int n)
+{
+	n = std::min(n, (int)NUM_AUX);
+	CTG_CUDA(cudaEventRecord(fork_ev_, st_));
+	for (int i = 0; i < n; i++) CTG_CUDA(cudaStreamWaitEvent(aux_[i], fork_ev_, 0));
+}
+
+void Ctx::join(int n)
+{
+	n = std::min(n, (int)NUM_AUX);
+	for (int i = 0; i < n; i++)
+	{
+		CTG_CUDA(cudaEventRecord(join_ev_[i], aux_[i]));
+		CTG_CUDA(cudaStreamWaitEvent(st_, join_ev_[i], 0));
+	}
 }
 
 Ctx::~Ctx()
 {
 	if (st_) cudaStreamSynchronize(st_);
+	for (int i = 0; i < NUM_AUX; i++)
+	{
+		if (aux_[i]) cudaStreamSynchronize(aux_[i]);
+		if (aux_[i]) cudaStreamDestroy(aux_[i]);
+		if (join_ev_[i]) cudaEventDestroy(join_ev_[i]);
+	}
+	if (fork_ev_) cudaEventDestroy(fork_ev_);
 	if (staging_) cudaFreeHost(staging_);
 	if (pool_) cudaMemPoolDestroy(pool_);
 	if (st_) cudaStreamDestroy(st_);
@@ -773,24 +808,86 @@ int op_svd(Ctx& c, const DTensor& a, SvdResult& res, double tol_hint)
 		woff += svd_scratch_doubles(d.m, d.n);
 		descs.push_back(d);
 	}
+	// One cluster per block, sized to the block's share of the Jacobi work (~N^2 (M + N)): the
+	// largest block gets the largest cluster, and every other block the smallest power of two
+	// that finishes it within about the largest block's time. One launch per configuration,
+	// the launches side by side on auxiliary streams.
+	const int maxcl = svd_max_cluster(c.device());
+	std::vector<double> work(descs.size());
+	double wmax = 0;
+	for (size_t b = 0; b < descs.size(); b++)
+	{
+		const double M = std::max(descs[b].m, descs[b].n), N = std::min(descs[b].m, descs[b].n);
+		work[b] = N * N * (M + N);
+		wmax = std::max(wmax, work[b]);
+	}
+	int forced = 0;
+	if (const char* e = getenv("CTGPU_SVD_CLUSTER")) forced = std::max(1, std::min(maxcl, atoi(e)));
+	std::vector<SvdLaunch> cfg(descs.size());
+	for (double slack = 1.5;; slack *= 2)
+	{
+		int total = 0;
+		for (size_t b = 0; b < descs.size(); b++)
+		{
+			int want = 1;
+			while (want < maxcl && work[b] > slack * wmax / maxcl * want) want *= 2;
+			if (forced) want = forced;
+			cfg[b] = svd_launch_for(descs[b].m, descs[b].n, want, maxcl);
+			total += cfg[b].cluster;
+		}
+		if (forced || total <= 2 * c.num_sms() || slack > 1e6) break;
+	}
+	std::vector<int> order(descs.size());
+	for (size_t b = 0; b < order.size(); b++) order[b] = (int)b;
+	std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+		if (cfg[x].global != cfg[y].global) return cfg[x].global > cfg[y].global;
+		return cfg[x].cluster > cfg[y].cluster;
+	});
+	{
+		std::vector<SvdDesc> sorted(descs.size());
+		std::vector<SvdLaunch> scfg(descs.size());
+		for (size_t b = 0; b < order.size(); b++)
+		{
+			sorted[b] = descs[(size_t)order[b]];
+			scfg[b] = cfg[(size_t)order[b]];
+		}
+		descs.swap(sorted);
+		cfg.swap(scfg);
+	}
+	struct Group { SvdLaunch l; int first, count; };
+	std::vector<Group> groups;
+	for (int b = 0; b < (int)descs.size(); b++)
+	{
+		if (!groups.empty() && groups.back().l.cluster == cfg[b].cluster && groups.back().l.global == cfg[b].global)
+		{
+			groups.back().count++;
+			groups.back().l.smem = std::max(groups.back().l.smem, cfg[b].smem);
+		}
+		else groups.push_back(Group{cfg[b], b, 1});
+	}
 	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(SvdDesc));
 	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
 	DBuf status(&c, 2 * sizeof(int));
 	CTG_CUDA(cudaMemsetAsync(status.ptr, 0, 2 * sizeof(int), c.stream()));
-	// Every direction is resolved: skipping pairs of small directions (which the truncation could
-	// never retain) creates slowly converging pairs at the skip boundary, so it is not used.
 	(void)tol_hint;
-	const double tiny_rel2 = 0.0;
 	DBuf tail(&c, descs.size() * sizeof(double));
 	CTG_CUDA(cudaMemsetAsync(tail.ptr, 0, descs.size() * sizeof(double), c.stream()));
-	// one cluster per block; spread the SMs over the blocks (at most 8 CTAs per cluster)
-	int cl = 1;
-	while (cl < 8 && (i64)(2 * cl) * (i64)descs.size() <= (i64)c.num_sms()) cl *= 2;
-	if (const char* e = getenv("CTGPU_SVD_CLUSTER")) cl = std::max(1, std::min(8, atoi(e)));
 	{
-		KScope ks(c, K_SVD, 1);
-		launch_svd_jacobi((int)descs.size(), cl, (const SvdDesc*)desc->ptr, a.data(), res.u.data(), (double*)res.s->ptr,
-		                  res.vh.data(), (double*)scratch.ptr, (int*)status.ptr, tiny_rel2, (double*)tail.ptr, c.stream());
+		KScope ks(c, K_SVD, (int)groups.size());
+		const int ng = (int)std::min<size_t>(groups.size(), Ctx::NUM_AUX);
+		if (groups.size() == 1)
+			launch_svd_group(groups[0].l, groups[0].first, groups[0].count, (const SvdDesc*)desc->ptr, a.data(),
+			                 res.u.data(), (double*)res.s->ptr, res.vh.data(), (double*)scratch.ptr, (int*)status.ptr,
+			                 (double*)tail.ptr, c.stream());
+		else
+		{
+			c.fork(ng);
+			for (size_t g = 0; g < groups.size(); g++)
+				launch_svd_group(groups[g].l, groups[g].first, groups[g].count, (const SvdDesc*)desc->ptr, a.data(),
+				                 res.u.data(), (double*)res.s->ptr, res.vh.data(), (double*)scratch.ptr,
+				                 (int*)status.ptr, (double*)tail.ptr, c.aux((int)g));
+			c.join(ng);
+		}
 	}
 	int hst[2] = {0, 0};
 	CTG_CUDA(cudaMemcpyAsync(hst, status.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream()));
@@ -806,8 +903,8 @@ int op_svd(Ctx& c, const DTensor& a, SvdResult& res, double tol_hint)
 	{
 		int mmax = 0, nmax = 0;
 		for (const SvdDesc& d : descs) { mmax = std::max(mmax, d.m); nmax = std::max(nmax, d.n); }
-		fprintf(stderr, "ctgpu: block SVD did not converge within %d Jacobi sweeps (%zu blocks, largest %d x %d, cluster %d)\n",
-		        SVD_MAX_SWEEPS, descs.size(), mmax, nmax, cl);
+		fprintf(stderr, "ctgpu: block SVD did not converge within %d Jacobi sweeps (%zu blocks, largest %d x %d, %zu launches)\n",
+		        SVD_MAX_SWEEPS, descs.size(), mmax, nmax, groups.size());
 		// opt-in diagnostics: write the input matrix (row-major blocks) for offline analysis
 		if (const char* path = getenv("CTGPU_SVD_DUMP"))
 		{

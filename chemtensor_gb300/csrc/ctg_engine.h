@@ -62,6 +62,12 @@ public:
 	~Ctx();
 	cudaStream_t stream() const { return st_; }
 	int device() const { return dev_; }
+	// auxiliary streams for independent launches: fork(n) makes aux(0..n-1) wait for the work
+	// queued so far on stream(); join(n) makes stream() wait for everything queued on them
+	static constexpr int NUM_AUX = 8;
+	cudaStream_t aux(int i);
+	void fork(int n);
+	void join(int n);
 	void* alloc(size_t bytes);
 	void free(void* p);
 	// copy host bytes to a new device buffer (through pinned staging, asynchronous)
@@ -97,6 +103,9 @@ private:
 	int* tc_error_ = nullptr;
 	bool tc_used_ = false;
 	cudaStream_t st_ = nullptr;
+	cudaStream_t aux_[NUM_AUX] = {};
+	cudaEvent_t fork_ev_ = nullptr;
+	cudaEvent_t join_ev_[NUM_AUX] = {};
 	cudaMemPool_t pool_ = nullptr;
 	char* staging_ = nullptr;
 	size_t staging_cap_ = 0, staging_used_ = 0;

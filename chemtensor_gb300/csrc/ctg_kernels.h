@@ -92,20 +92,32 @@ void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs,
 
 // ---- dense linear algebra per block ---------------------------------------------
 // SVD of a row-major m x n block: u (m x k), s (k), vh (k x n), k = min(m, n), singular values
-// in descending order; one thread-block cluster of 'cluster' CTAs (1..8) per block.
-// status[0] becomes -1 if a block does not converge within SVD_MAX_SWEEPS FP64 Jacobi sweeps,
-// status[1] receives the largest sweep count. Pairs of directions whose squared singular values
-// are both below tiny_rel2 times the largest squared column norm are not resolved against each
-// other (0 resolves everything); tail[block] (zeroed by the caller) accumulates their total
-// weight, an upper bound for any singular value squared that was left unresolved.
+// in descending order; one thread-block cluster per block. Entries of u, s and vh beyond the
+// numerical rank are not written (the caller zeroes them). status[0] becomes -1 if a block does
+// not converge within SVD_MAX_SWEEPS FP64 Jacobi sweeps, status[1] receives the largest sweep
+// count; tail[block] (zeroed by the caller) receives an upper bound for the squared singular
+// values dropped as rank deficient.
 constexpr int SVD_MAX_SWEEPS = 60;
 struct SvdDesc {
 	i64 a_off, u_off, s_off, v_off, w_off;
 	int m, n;
 };
 i64 svd_scratch_doubles(int m, int n);
-void launch_svd_jacobi(int nblocks, int cluster, const SvdDesc* descs, const double* a, double* u, double* s,
-                       double* vh, double* scratch, int* status, double tiny_rel2, double* tail, cudaStream_t st);
+
+// Launch configuration of one block's SVD: cluster size, dynamic shared memory, and whether the
+// Jacobi columns live in global memory (blocks too large for the shared-memory path).
+struct SvdLaunch {
+	int cluster = 1;
+	int smem = 0;
+	int global = 0;
+};
+// largest cluster the device schedules for the SVD kernel (16 where non-portable sizes work, else 8)
+int svd_max_cluster(int device);
+// smallest configuration with at least 'want' CTAs (a power of two) that fits an m x n block
+SvdLaunch svd_launch_for(int m, int n, int want, int max_cluster);
+// SVDs of descs[first .. first + count), all with configuration g, on stream st
+void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* descs, const double* a, double* u,
+                      double* s, double* vh, double* scratch, int* status, double* tail, cudaStream_t st);
 
 // Householder RQ of a row-major m x n block: A = R Q with Q (k x n) orthonormal rows, R (m x k), k = min(m, n).
 // Scratch holds n*m + n*k + k doubles per block.

@@ -3,7 +3,7 @@
 //
 // Replaces LAPACK dgesvd in dense_tensor_svd_fill (dense_tensor.c:3538-3680), which
 // block_sparse_tensor_svd (block_sparse_tensor.c:2686-2848) calls once per
-// quantum-number block. FP64 throughout. Singular values agree with dgesvd to rounding
+// quantum-number block. FP64 results. Singular values agree with dgesvd to rounding
 // (dgesvd resolves them to ~eps sigma_max absolute, this method to ~(m + n) eps sigma_max);
 // singular vectors up to sign / rotation within degenerate subspaces.
 //
@@ -16,14 +16,17 @@
 //      on the pivoted, graded R^T this takes about half the sweeps that Jacobi on B needs
 //      for the graded spectra of two-site DMRG matrices;
 //   3. B = (Q V) Sigma (P T Sigma^-1)^T.
-// On GB300 an SM retires about two FP64 FMAs per clock, so each dense block gets a cluster
-// of up to 8 CTAs: the pivoted QR runs on one CTA, the Jacobi rounds (disjoint column pairs
-// shared out over all warps of the cluster), the formation of Q and the outputs run on the
-// whole cluster, separated by cluster barriers (release / acquire at cluster scope for the
-// global-memory data, which is read with L2-coherent loads).
+// On GB300 an SM retires about two FP64 FMAs per clock and every FP64 warp instruction
+// occupies its SM sub-partition for 64 cycles whatever the number of active lanes, so each
+// dense block gets a cluster of up to 16 CTAs sized to its share of the work: the pivoted QR
+// runs on one CTA, the Jacobi sweeps on the whole cluster with the columns in shared memory
+// (k_svd_tour), the outputs on the whole cluster. Blocks too large for shared memory keep
+// their columns in global memory (k_svd_global: one cluster barrier per round of disjoint
+// pairs, L2-coherent loads).
 #include <cfloat>
 #include <cstdio>
 #include <mutex>
+#include <stdexcept>
 
 #include <cooperative_groups.h>
 
@@ -37,6 +40,8 @@ namespace {
 
 constexpr int SVD_THREADS = 256;
 constexpr int NWARPS = SVD_THREADS / 32;
+constexpr int SVD_STEP_PAIRS = 32;            // most column pairs of one inner step (group size <= 32)
+constexpr int SVD_SMEM_LIMIT = 220 * 1024;    // dynamic shared memory per CTA (227 KB less static use)
 
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -170,14 +175,449 @@ __device__ int qr_pivoted_cta(double* W, int M, int N, double* nrm, double* tau,
 	return r;
 }
 
+// ---- one-sided Jacobi on a thread-block cluster, columns resident in shared memory ----------
+//
+// The r columns of R^T (with their rows of V) are cut into 2 cl groups of bs consecutive columns.
+// Each CTA of the cluster holds two groups (slots 0 and 1) in shared memory. A sweep is a
+// round-robin tournament over the groups (circle method, 2 cl - 1 rounds): in each round a CTA
+// rotates every column of its slot-0 group against every column of its slot-1 group (bs steps of
+// bs disjoint pairs), in round 0 also the pairs inside each group; then it writes both groups into
+// the shared memory of the CTAs that hold them in the next round (distributed shared memory,
+// double-buffered) and the cluster synchronises once. Each column pair meets once per sweep,
+// as in the cyclic one-sided Jacobi method; a round costs one cluster barrier instead of one per
+// pair set, and the column data never leaves the SMs.
+
+__device__ __forceinline__ float rcp_approx(float x)
+{
+	float y;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
+}
+
+// Jacobi rotation for the 2 x 2 Gram matrix [al ga; ga be] of a column pair: c, s with
+// x' = c x - s y, y' = s x + c y making x' and y' orthogonal. The tangent t of the smaller
+// rotation angle, t = sign(be - al) 2 ga / (|be - al| + sqrt((be - al)^2 + 4 ga^2)), is evaluated
+// in FP32 on operands scaled by a power of two (an FP64 division and square root cost over a
+// thousand cycles on GB300's FP64 pipe). The rotation is then built in FP64 from the half-angle
+// tangent tau = t / (1 + sqrt(1 + t^2)) in the Cayley form c = (1 - tau^2) / (1 + tau^2),
+// s = 2 tau / (1 + tau^2): orthogonal to FP64 rounding for any tau. The reciprocal of
+// q = 1 + tau^2 is an FP32 estimate d0 refined by one cubically convergent Newton step,
+// d = d0 (1 + e + e^2) with e = 1 - q d0. The angle is accurate to FP32 only: the rotation
+// leaves a cosine of about 1e-7 of the previous one, which a later sweep removes.
+__device__ __forceinline__ void rotation_params(double al, double be, double ga, double& c, double& s, float& t32)
+{
+	const double dl = be - al;
+	const double mx = fmax(fabs(dl), 2.0 * fabs(ga));
+	int ex = (__double2hiint(mx) >> 20) & 0x7ff;      // biased exponent of mx
+	ex = ex < 1 ? 1 : (ex > 2045 ? 2045 : ex);
+	const double sc = __hiloint2double((2046 - ex) << 20, 0);   // 2^(1023 - ex): mx * sc in [1, 2)
+	const float ds = (float)(dl * sc), gs = (float)(ga * sc);
+	const float h = sqrtf(fmaf(ds, ds, 4.0f * gs * gs));
+	t32 = (2.0f * gs) * copysignf(1.0f, ds) / (fabsf(ds) + h);
+	const float tau32 = t32 / (1.0f + sqrtf(fmaf(t32, t32, 1.0f)));
+	const double tau = (double)tau32;
+	const double q = fma(tau, tau, 1.0);
+	const double d0 = (double)rcp_approx((float)q);
+	const double e = fma(-q, d0, 1.0);
+	const double d = fma(d0, fma(e, e, e), d0);
+	c = fma(-tau, tau, 1.0) * d;
+	s = (2.0 * tau) * d;
+}
+
+// groups held by CTA pi in round rho (circle method over nm + 1 groups; group nm stays with CTA 0)
+__device__ __forceinline__ void round_groups(int rho, int pi, int nm, int& a, int& b)
+{
+	if (pi == 0) { a = rho; b = nm; }
+	else { a = (rho + pi) % nm; b = (rho - pi + nm) % nm; }
+}
+
+// CTA and slot that hold group x in round rho
+__device__ __forceinline__ void group_owner(int x, int rho, int nm, int& pi, int& slot)
+{
+	if (x == nm) { pi = 0; slot = 1; return; }
+	const int dd = ((x - rho) % nm + nm) % nm;
+	const int half = (nm + 1) / 2;
+	if (dd == 0) { pi = 0; slot = 0; }
+	else if (dd <= half - 1) { pi = dd; slot = 0; }
+	else { pi = nm - dd; slot = 1; }
+}
+
+struct Tour {
+	int nblk, nm, bs, bsmax, r, N, ld;
+	double* sm;
+	__device__ double* col(int buf, int slot, int c) const { return sm + (i64)((buf * 2 + slot) * bsmax + c) * ld; }
+	__device__ double* nrm(int buf, int slot) const { return sm + (i64)4 * bsmax * ld + (buf * 2 + slot) * bsmax; }
+	__device__ int cnt(int x) const
+	{
+		const int c = r - x * bs;
+		return c < 0 ? 0 : (c > bs ? bs : c);
+	}
+};
+
+struct StepBuf {
+	double* gam;
+	double* csc;
+	double* css;
+	int* rotk;
+	int* local_rot;
+};
+
+// pair k of an inner step: mode 0 pairs inside each slot (circle method over npad columns),
+// mode 1 pairs slot-0 column k with slot-1 column (k + step) mod bs
+__device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int k, int cA, int cB, int npad, int& sp,
+                                          int& cp, int& sq, int& cq)
+{
+	if (mode == 0)
+	{
+		const int half = npad >> 1;
+		const int sl = k < half ? 0 : 1;
+		int p, q;
+		round_robin_pair(step, k < half ? k : k - half, npad, p, q);
+		sp = sl;
+		sq = sl;
+		cp = p;
+		cq = q;
+		return q < (sl == 0 ? cA : cB);
+	}
+	sp = 0;
+	sq = 1;
+	cp = k;
+	cq = (k + step) % t.bs;
+	return k < cA && cq < cB;
+}
+
+__device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, int cB, int npad, double tol2, const StepBuf& sb)
+{
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int np = mode == 0 ? npad : t.bs;
+	// 1. inner products, one warp per pair
+	for (int k = warp; k < np; k += NWARPS)
+	{
+		int sp, cp, sq, cq;
+		if (!step_pair(t, mode, step, k, cA, cB, npad, sp, cp, sq, cq)) continue;
+		const double* x = t.col(buf, sp, cp);
+		const double* y = t.col(buf, sq, cq);
+		double g = 0;
+		for (int i = lane; i < t.N; i += 32) g = fma(x[i], y[i], g);
+		g = warp_sum(g);
+		if (lane == 0) sb.gam[k] = g;
+	}
+	__syncthreads();
+	// 2. rotations, one lane per pair; rotate while the cosine exceeds tol
+	if (warp == 0 && lane < np)
+	{
+		int sp, cp, sq, cq;
+		int rot = 0;
+		double c = 1.0, s = 0.0;
+		if (step_pair(t, mode, step, lane, cA, cB, npad, sp, cp, sq, cq))
+		{
+			double* np_ = t.nrm(buf, sp) + cp;
+			double* nq_ = t.nrm(buf, sq) + cq;
+			const double al = *np_, be = *nq_, ga = sb.gam[lane];
+			if (ga != 0.0 && ga * ga > tol2 * al * be)
+			{
+				float t32;
+				rotation_params(al, be, ga, c, s, t32);
+				if (s != 0.0)
+				{
+					rot = 1;
+					*np_ = al - (double)t32 * ga;
+					*nq_ = be + (double)t32 * ga;
+					*sb.local_rot = 1;
+				}
+			}
+		}
+		sb.csc[lane] = c;
+		sb.css[lane] = s;
+		sb.rotk[lane] = rot;
+	}
+	__syncthreads();
+	// 3. apply: work items of 32 consecutive entries of one pair's T or V columns
+	const int segT = (t.N + 31) >> 5, nseg = segT + ((t.r + 31) >> 5);
+	for (int it = warp; it < np * nseg; it += NWARPS)
+	{
+		const int k = it / nseg, g = it - k * nseg;
+		if (!sb.rotk[k]) continue;
+		int sp, cp, sq, cq;
+		step_pair(t, mode, step, k, cA, cB, npad, sp, cp, sq, cq);
+		int i;
+		if (g < segT)
+		{
+			i = g * 32 + lane;
+			if (i >= t.N) continue;
+		}
+		else
+		{
+			i = (g - segT) * 32 + lane;
+			if (i >= t.r) continue;
+			i += t.N;
+		}
+		double* x = t.col(buf, sp, cp);
+		double* y = t.col(buf, sq, cq);
+		const double c = sb.csc[k], s = sb.css[k];
+		const double xv = x[i], yv = y[i];
+		x[i] = c * xv - s * yv;
+		y[i] = s * xv + c * yv;
+	}
+	__syncthreads();
+}
+
+struct SvdScratch {
+	double *W, *T, *V, *nrm, *tau, *sig, *misc;
+	int *flags, *perm;
+};
+
+// workspace of one block: W (M x N, B then R and the reflectors), T (N x r), V (r x r), column
+// norms, reflector scalars, singular values, misc [rank, ||B||_F^2, unscale], sweep flags, pivots
+__device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
+{
+	SvdScratch x;
+	x.W = base;
+	x.T = x.W + (i64)M * N;
+	x.V = x.T + (i64)N * N;
+	x.nrm = x.V + (i64)N * N;
+	x.tau = x.nrm + N;
+	x.sig = x.tau + N;
+	x.misc = x.sig + N;
+	x.flags = (int*)(x.misc + 4);
+	x.perm = x.flags + SVD_MAX_SWEEPS;
+	return x;
+}
+
 __global__ void __launch_bounds__(SVD_THREADS)
-k_svd_cluster(const SvdDesc* __restrict__ descs, const double* __restrict__ a, double* __restrict__ u,
+k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
+           double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
+           double* __restrict__ tail, int cl)
+{
+	extern __shared__ __align__(16) double smem[];
+	cg::cluster_group cluster = cg::this_cluster();
+	const int rank = (int)cluster.block_rank();
+	const int blk = first + blockIdx.x / cl;
+	const SvdDesc d = descs[blk];
+	const int m = d.m, n = d.n;
+	const bool tall = m >= n;
+	const int M = tall ? m : n, N = tall ? n : m;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const SvdScratch xs = scratch_layout(scratch + d.w_off, M, N);
+	const double* ab = a + d.a_off;
+
+	for (int e = rank * SVD_THREADS + tid; e < SVD_MAX_SWEEPS; e += cl * SVD_THREADS) xs.flags[e] = 0;
+
+	// ---- 1. pivoted QR on the cluster's first CTA, of B scaled to a Frobenius norm in [1/2, 1) ----
+	if (rank == 0)
+	{
+		__shared__ double red[NWARPS];
+		double part = 0;
+		for (i64 e = tid; e < (i64)M * N; e += SVD_THREADS)
+		{
+			const i64 col = e / M, row = e % M;
+			const double x = tall ? ab[row * n + col] : ab[col * n + row];
+			part = fma(x, x, part);
+		}
+		for (int j = tid; j < N; j += SVD_THREADS) xs.perm[j] = j;
+		const double total = block_sum(part, red);
+		// exact power-of-two scaling: keeps products of squared column norms far from underflow
+		int ex = 0;
+		if (total > 0) frexp(sqrt(total), &ex);
+		const double sc = ldexp(1.0, -ex);
+		for (i64 e = tid; e < (i64)M * N; e += SVD_THREADS)
+		{
+			const i64 col = e / M, row = e % M;
+			xs.W[e] = sc * (tall ? ab[row * n + col] : ab[col * n + row]);
+		}
+		__syncthreads();
+		const int rr = qr_pivoted_cta(xs.W, M, N, xs.nrm, xs.tau, xs.perm, DBL_EPSILON * DBL_EPSILON * total * sc * sc);
+		if (tid == 0)
+		{
+			xs.misc[0] = (double)rr;
+			xs.misc[1] = total;
+			xs.misc[2] = ldexp(1.0, ex);
+		}
+	}
+	cluster.sync();
+	const int r = (int)__ldcg(xs.misc);
+
+	// ---- 2. one-sided Jacobi on R^T (N x r), block-pair tournament over the cluster ----
+	Tour t;
+	t.nblk = 2 * cl;
+	t.nm = t.nblk - 1;
+	t.r = r;
+	t.N = N;
+	t.ld = 2 * N;
+	t.bsmax = (N + t.nblk - 1) / t.nblk;
+	t.bs = r > 0 ? (r + t.nblk - 1) / t.nblk : 1;
+	t.sm = smem;
+	StepBuf sb;
+	sb.gam = smem + (i64)4 * t.bsmax * t.ld + 4 * t.bsmax;
+	sb.csc = sb.gam + SVD_STEP_PAIRS;
+	sb.css = sb.csc + SVD_STEP_PAIRS;
+	sb.rotk = (int*)(sb.css + SVD_STEP_PAIRS);
+	sb.local_rot = sb.rotk + SVD_STEP_PAIRS;
+
+	int A, B;
+	round_groups(0, rank, t.nm, A, B);
+	// column g of T is row g of R (upper triangle of W); column g of V is e_g
+	for (int slot = 0; slot < 2; slot++)
+	{
+		const int x = slot ? B : A;
+		double* dst = t.col(0, slot, 0);
+		for (i64 e = tid; e < (i64)t.cnt(x) * t.ld; e += SVD_THREADS)
+		{
+			const int c = (int)(e / t.ld), i = (int)(e % t.ld);
+			const int g = x * t.bs + c;
+			double v;
+			if (i < N) v = (i >= g) ? __ldcg(xs.W + (i64)i * M + g) : 0.0;
+			else v = (i - N == g) ? 1.0 : 0.0;
+			dst[e] = v;
+		}
+	}
+	__syncthreads();
+
+	const double tol = (double)N * DBL_EPSILON, tol2 = tol * tol;
+	int buf = 0, sweep = 0;
+	bool converged = r <= 1;
+	for (; sweep < SVD_MAX_SWEEPS && !converged; sweep++)
+	{
+		round_groups(0, rank, t.nm, A, B);
+		// exact squared norms of the columns held here
+		for (int slot = 0; slot < 2; slot++)
+		{
+			const int nc = t.cnt(slot ? B : A);
+			for (int c = warp; c < nc; c += NWARPS)
+			{
+				const double* col = t.col(buf, slot, c);
+				double acc = 0;
+				for (int i = lane; i < N; i += 32) acc = fma(col[i], col[i], acc);
+				acc = warp_sum(acc);
+				if (lane == 0) t.nrm(buf, slot)[c] = acc;
+			}
+		}
+		if (tid == 0) *sb.local_rot = 0;
+		__syncthreads();
+		for (int rho = 0; rho < t.nm; rho++)
+		{
+			round_groups(rho, rank, t.nm, A, B);
+			const int cA = t.cnt(A), cB = t.cnt(B);
+			if (rho == 0)
+			{
+				const int npad = t.bs + (t.bs & 1);
+				for (int st = 0; st < npad - 1; st++) jacobi_step(t, buf, 0, st, cA, cB, npad, tol2, sb);
+			}
+			for (int st = 0; st < t.bs; st++) jacobi_step(t, buf, 1, st, cA, cB, 0, tol2, sb);
+			if (cl > 1)
+			{
+				// jacobi_step ended with a CTA barrier: this round's rotations are complete
+				if (tid == 0 && *sb.local_rot) atomicOr(xs.flags + sweep, 1);
+				const int rho1 = (rho + 1) % t.nm;
+				for (int slot = 0; slot < 2; slot++)
+				{
+					const int x = slot ? B : A, nc = t.cnt(x);
+					int pi2, slot2;
+					group_owner(x, rho1, t.nm, pi2, slot2);
+					const double2* src = (const double2*)t.col(buf, slot, 0);
+					double2* dst = (double2*)cluster.map_shared_rank(t.col(buf ^ 1, slot2, 0), (unsigned)pi2);
+					for (i64 e = tid; e < (i64)nc * t.ld / 2; e += SVD_THREADS) dst[e] = src[e];
+					const double* nsrc = t.nrm(buf, slot);
+					double* ndst = cluster.map_shared_rank(t.nrm(buf ^ 1, slot2), (unsigned)pi2);
+					for (int e = tid; e < nc; e += SVD_THREADS) ndst[e] = nsrc[e];
+				}
+				cluster.sync();
+				buf ^= 1;
+			}
+		}
+		if (cl > 1) converged = __ldcg(xs.flags + sweep) == 0;
+		else
+		{
+			converged = *sb.local_rot == 0;
+			__syncthreads();
+		}
+	}
+	// columns back in global memory (arrangement of round 0), singular values as column norms
+	round_groups(0, rank, t.nm, A, B);
+	for (int slot = 0; slot < 2; slot++)
+	{
+		const int x = slot ? B : A, nc = t.cnt(x);
+		const double* src = t.col(buf, slot, 0);
+		for (i64 e = tid; e < (i64)nc * t.ld; e += SVD_THREADS)
+		{
+			const int c = (int)(e / t.ld), i = (int)(e % t.ld);
+			const int g = x * t.bs + c;
+			if (i < N) xs.T[(i64)g * N + i] = src[e];
+			else if (i - N < r) xs.V[(i64)g * r + (i - N)] = src[e];
+		}
+		for (int c = warp; c < nc; c += NWARPS)
+		{
+			const double* col = t.col(buf, slot, c);
+			double acc = 0;
+			for (int i = lane; i < N; i += 32) acc = fma(col[i], col[i], acc);
+			acc = warp_sum(acc);
+			if (lane == 0) xs.sig[x * t.bs + c] = sqrt(acc);
+		}
+	}
+	if (rank == 0 && tid == 0)
+	{
+		atomicMax(status + 1, sweep);
+		if (!converged) atomicExch(status, -1);
+		// rank-deficient part beyond r: its weight is below eps^2 ||B||_F^2 per column
+		if (r < N) atomicAdd(tail + blk, (double)(N - r) * DBL_EPSILON * DBL_EPSILON * __ldcg(xs.misc + 1));
+	}
+	cluster.sync();
+
+	// ---- 3. outputs: L = Q V (M x r) by the r reflectors applied to [V_c; 0], Rf = P T Sigma^-1 ----
+	const double unscale = __ldcg(xs.misc + 2);
+	const int kk = N;                                     // min(m, n): width of the factor blocks
+	double* ub = smem + (i64)warp * M;
+	for (int c = rank * NWARPS + warp; c < r; c += cl * NWARPS)
+	{
+		for (int i = lane; i < M; i += 32) ub[i] = i < r ? __ldcg(xs.V + (i64)c * r + i) : 0.0;
+		__syncwarp();
+		for (int k = r - 1; k >= 0; k--)
+		{
+			const double tk = __ldcg(xs.tau + k);
+			if (tk == 0.0) continue;
+			const double* wk = xs.W + (i64)k * M;
+			double acc = 0;
+			for (int i = k + lane; i < M; i += 32) acc = fma(i == k ? 1.0 : __ldcg(wk + i), ub[i], acc);
+			acc = warp_sum(acc) * tk;
+			for (int i = k + lane; i < M; i += 32) ub[i] -= acc * (i == k ? 1.0 : __ldcg(wk + i));
+			__syncwarp();
+		}
+		const double sc = __ldcg(xs.sig + c);
+		int cnt = 0;
+		for (int c2 = lane; c2 < r; c2 += 32)
+		{
+			const double v = __ldcg(xs.sig + c2);
+			cnt += (v > sc || (v == sc && c2 < c)) ? 1 : 0;
+		}
+		const int pos = (int)__reduce_add_sync(0xffffffffu, (unsigned)cnt);
+		if (lane == 0) s[d.s_off + pos] = sc * unscale;
+		const double inv = sc > 0 ? 1.0 / sc : 0.0;
+		for (int i = lane; i < M; i += 32)
+		{
+			if (tall) u[d.u_off + (i64)i * kk + pos] = ub[i];       // u: m x k, row i
+			else vh[d.v_off + (i64)pos * n + i] = ub[i];            // vh: k x n, column i
+		}
+		const double* tc = xs.T + (i64)c * N;
+		for (int j = lane; j < N; j += 32)
+		{
+			const double x = __ldcg(tc + j) * inv;
+			const int pj = __ldcg(xs.perm + j);
+			if (tall) vh[d.v_off + (i64)pos * n + pj] = x;         // vh: k x n
+			else u[d.u_off + (i64)pj * kk + pos] = x;               // u: m x k
+		}
+		__syncwarp();
+	}
+}
+
+// ---- global-memory variant for blocks too large for shared memory ----
+__global__ void __launch_bounds__(SVD_THREADS)
+k_svd_global(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
               double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
               double tiny_rel2, double* __restrict__ tail, int cl)
 {
 	cg::cluster_group cluster = cg::this_cluster();
 	const int rank = (int)cluster.block_rank();
-	const SvdDesc d = descs[blockIdx.x / cl];
+	const SvdDesc d = descs[first + blockIdx.x / cl];
 	const int m = d.m, n = d.n;
 	const bool tall = m >= n;
 	const int M = tall ? m : n, N = tall ? n : m;
@@ -320,12 +760,12 @@ k_svd_cluster(const SvdDesc* __restrict__ descs, const double* __restrict__ a, d
 			sig[c] = sqrt(acc);
 			// weight of the directions left unresolved (both partners below the tiny bound)
 			if (tiny_rel2 > 0 && acc <= tiny_rel2 * __longlong_as_double((long long)__ldcg(amax)))
-				atomicAdd(tail + blockIdx.x / cl, acc);
+				atomicAdd(tail + first + blockIdx.x / cl, acc);
 		}
 	}
 	// rank-deficient part beyond r: its weight is below eps^2 ||B||_F^2 per column
 	if (rank == 0 && tid == 0 && r < N)
-		atomicAdd(tail + blockIdx.x / cl, (double)(N - r) * DBL_EPSILON * DBL_EPSILON * __ldcg(misc + 1));
+		atomicAdd(tail + first + blockIdx.x / cl, (double)(N - r) * DBL_EPSILON * DBL_EPSILON * __ldcg(misc + 1));
 
 	// ---- 3. explicit Q (M x r) = H_0 ... H_{r-1} E_r over the cluster ----
 	for (i64 e = gtid; e < (i64)M * r; e += gstride) Q[e] = (e / M == e % M) ? 1.0 : 0.0;
@@ -476,32 +916,21 @@ extern "C" int ctgpu_dense_svd_noalloc(const double* d_a, int m, int n, double* 
 	d.m = m;
 	d.n = n;
 	k_noalloc_prepare<<<64, 256, 0, st>>>(base, d, d_u, d_s, d_vh);
-	const int cl = 8;
-	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim = dim3((unsigned)cl);
-	cfg.blockDim = dim3(SVD_THREADS);
-	cfg.dynamicSmemBytes = 0;
-	cfg.stream = st;
-	cudaLaunchAttribute attr[1];
-	attr[0].id = cudaLaunchAttributeClusterDimension;
-	attr[0].val.clusterDim.x = (unsigned)cl;
-	attr[0].val.clusterDim.y = 1;
-	attr[0].val.clusterDim.z = 1;
-	cfg.attrs = attr;
-	cfg.numAttrs = 1;
 	const SvdDesc* descs = (const SvdDesc*)(base + NA_DESC);
 	int* status = (int*)(base + NA_STATUS);
 	double* tail = base + NA_STATUS + 1;
-	cudaError_t e = cudaLaunchKernelEx(&cfg, k_svd_cluster, descs, d_a, d_u, d_s, d_vh, base + NA_WORK, status, 0.0,
-	                                   tail, cl);
-	if (e == cudaSuccess)
+	try
 	{
+		const int maxcl = svd_max_cluster(dev);
+		launch_svd_group(svd_launch_for(m, n, maxcl, maxcl), 0, 1, descs, d_a, d_u, d_s, d_vh, base + NA_WORK, status,
+		                 tail, st);
 		k_noalloc_finish<<<1, 1, 0, st>>>(base, d_info);
-		e = cudaGetLastError();
+		const cudaError_t e = cudaGetLastError();
+		if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
 	}
-	if (e != cudaSuccess)
+	catch (const std::exception& ex)
 	{
-		fprintf(stderr, "ctgpu_dense_svd_noalloc: launch failed: %s\n", cudaGetErrorString(e));
+		fprintf(stderr, "ctgpu_dense_svd_noalloc: launch failed: %s\n", ex.what());
 		return -5;
 	}
 	return 0;
@@ -512,27 +941,104 @@ namespace ctg {
 i64 svd_scratch_doubles(int m, int n)
 {
 	const i64 M = m >= n ? m : n, N = m >= n ? n : m;
-	// W, Q, T, V, nrm, tau, sig, misc, flags + amax, perm
-	return 2 * M * N + 2 * N * N + 3 * N + 2 + 2 * SVD_MAX_SWEEPS + (N + 1) / 2 + 1;
+	// the larger of the two layouts: global-memory path (W, Q, T, V, nrm, tau, sig, misc, flags +
+	// amax, perm) and shared-memory path (W, T, V, nrm, tau, sig, misc, flags, perm)
+	return 2 * M * N + 2 * N * N + 3 * N + 4 + 2 * SVD_MAX_SWEEPS + (N + 1) / 2 + 1;
 }
 
-void launch_svd_jacobi(int nblocks, int cluster, const SvdDesc* descs, const double* a, double* u, double* s,
-                       double* vh, double* scratch, int* status, double tiny_rel2, double* tail, cudaStream_t st)
+static i64 tour_smem_bytes(int M, int N, int cl)
 {
-	if (nblocks <= 0) return;
+	const i64 nblk = 2 * cl, bsmax = (N + nblk - 1) / nblk;
+	const i64 jac = 4 * bsmax * 2 * N + 4 * bsmax + 3 * SVD_STEP_PAIRS + SVD_STEP_PAIRS / 2 + 8;
+	const i64 out = (i64)NWARPS * M;
+	return 8 * (jac > out ? jac : out);
+}
+
+int svd_max_cluster(int device)
+{
+	static int cache[64] = {0};
+	static std::mutex lock;
+	std::lock_guard<std::mutex> g(lock);
+	if (device < 0 || device >= 64) return 8;
+	if (cache[device]) return cache[device];
+	int best = 8;
+	// 16-CTA clusters are a non-portable size: use them where the device can schedule one
+	if (cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+	    cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeMaxDynamicSharedMemorySize, SVD_SMEM_LIMIT) == cudaSuccess)
+	{
+		cudaLaunchConfig_t cfg = {};
+		cfg.gridDim = dim3(16);
+		cfg.blockDim = dim3(SVD_THREADS);
+		cfg.dynamicSmemBytes = 64 * 1024;
+		cudaLaunchAttribute attr[1];
+		attr[0].id = cudaLaunchAttributeClusterDimension;
+		attr[0].val.clusterDim.x = 16;
+		attr[0].val.clusterDim.y = 1;
+		attr[0].val.clusterDim.z = 1;
+		cfg.attrs = attr;
+		cfg.numAttrs = 1;
+		int nclusters = 0;
+		if (cudaOccupancyMaxActiveClusters(&nclusters, k_svd_tour, &cfg) == cudaSuccess && nclusters >= 1) best = 16;
+	}
+	cudaGetLastError();
+	cache[device] = best;
+	return best;
+}
+
+SvdLaunch svd_launch_for(int m, int n, int want, int max_cluster)
+{
+	const int M = m >= n ? m : n, N = m >= n ? n : m;
+	SvdLaunch l;
+	for (int cl = want < 1 ? 1 : want; cl <= max_cluster; cl *= 2)
+	{
+		const int bsmax = (N + 2 * cl - 1) / (2 * cl);
+		const i64 bytes = tour_smem_bytes(M, N, cl);
+		if (bsmax <= SVD_STEP_PAIRS && bytes <= SVD_SMEM_LIMIT)
+		{
+			l.cluster = cl;
+			l.smem = (int)bytes;
+			l.global = 0;
+			return l;
+		}
+	}
+	// too large for the shared-memory path: columns stay in global memory
+	l.cluster = want < 1 ? 1 : (want > 8 ? 8 : want);
+	l.smem = 0;
+	l.global = 1;
+	return l;
+}
+
+void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* descs, const double* a, double* u,
+                      double* s, double* vh, double* scratch, int* status, double* tail, cudaStream_t st)
+{
+	if (count <= 0) return;
 	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim = dim3((unsigned)(nblocks * cluster));
+	cfg.gridDim = dim3((unsigned)(count * g.cluster));
 	cfg.blockDim = dim3(SVD_THREADS);
-	cfg.dynamicSmemBytes = 0;
+	cfg.dynamicSmemBytes = (size_t)g.smem;
 	cfg.stream = st;
 	cudaLaunchAttribute attr[1];
 	attr[0].id = cudaLaunchAttributeClusterDimension;
-	attr[0].val.clusterDim.x = (unsigned)cluster;
+	attr[0].val.clusterDim.x = (unsigned)g.cluster;
 	attr[0].val.clusterDim.y = 1;
 	attr[0].val.clusterDim.z = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_cluster, descs, a, u, s, vh, scratch, status, tiny_rel2, tail, cluster));
+	if (g.global)
+	{
+		CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_global, descs, first, a, u, s, vh, scratch, status, 0.0, tail, g.cluster));
+		return;
+	}
+	static bool attr_set[64] = {false};
+	int dev = 0;
+	CTG_CUDA(cudaGetDevice(&dev));
+	if (dev >= 0 && dev < 64 && !attr_set[dev])
+	{
+		CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeMaxDynamicSharedMemorySize, SVD_SMEM_LIMIT));
+		CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+		attr_set[dev] = true;
+	}
+	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, tail, g.cluster));
 }
 
 }  // namespace ctg
