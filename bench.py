@@ -260,7 +260,12 @@ def bench_gpu(args, world, rank, local):
         "energy_last_sweep": float(en[-1]),
         "breakdown_ms_per_sweep": {"lanczos": stats["lanczos_ms"] / max(stats["sweeps"], 1),
                                    "svd_split": stats["split_ms"] / max(stats["sweeps"], 1),
-                                   "svd_max_jacobi_sweeps": stats["svd_max_sweeps"]},
+                                   "svd_max_jacobi_sweeps": stats["svd_max_sweeps"],
+                                   "host_planning": 1e3 * stats["host_plan_s"] / max(stats["sweeps"], 1),
+                                   "plan_cache_hit_rate": stats["plan_hits"] / max(stats["plan_hits"] + stats["plan_misses"], 1)},
+        # device time of each kernel class per profiled sweep (CUDA events around every launch;
+        # the difference to ms_per_step is time the device waits for the host)
+        "kernel_ms_per_sweep": {k: v["ms"] / K for k, v in prof.items()},
     }
 
     # 4) CPU baseline on rank 0: the reference algorithm on the host cores, one sweep

@@ -85,6 +85,9 @@ int ctgpu_get_last_stats(struct ctgpu_stats* out)
 	out->sweeps = s.sweeps;
 	out->max_bond_dim = s.max_bond_dim;
 	out->svd_max_sweeps = s.svd_max_sweeps;
+	out->host_plan_s = s.host_plan_s;
+	out->plan_hits = s.plan_hits;
+	out->plan_misses = s.plan_misses;
 	return 0;
 }
 

@@ -486,6 +486,9 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	c.profile = false;
 	c.prof_reset();
 	c.svd_max_sweeps = 0;
+	c.host_plan_s = 0;
+	c.plan_hits = 0;
+	c.plan_misses = 0;
 	DBuf sc_buf(&c, sizeof(LanczosScalars));
 	LanczosScalars* d_sc = (LanczosScalars*)sc_buf.ptr;
 	LanczosScalars h_sc;
@@ -627,6 +630,9 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	st->kernel_launches = c.kernel_launches;
 	st->total_gemm_flops = c.gemm_flops;
 	st->svd_max_sweeps = c.svd_max_sweeps;
+	st->host_plan_s = c.host_plan_s;
+	st->plan_hits = c.plan_hits;
+	st->plan_misses = c.plan_misses;
 	st->wall_s = now_s() - t_start;
 	return 0;
 }

@@ -32,6 +32,8 @@ struct DmrgStats {
 	int sweeps = 0;
 	i64 max_bond_dim = 0;
 	int svd_max_sweeps = 0;             // largest Jacobi sweep count of any block SVD
+	double host_plan_s = 0;             // host time lowering operations into device work lists
+	long plan_hits = 0, plan_misses = 0;
 	std::vector<double> sweep_ms;       // device time of every sweep (CUDA events on the stream)
 	std::vector<long> sweep_launches;   // kernels launched by every sweep
 	KProf prof[K_NUM_CLASSES];          // per kernel class, over the profiled sweeps

@@ -2,6 +2,8 @@
 #include "ctg_engine.h"
 
 #include <algorithm>
+#include <chrono>
+#include <functional>
 #include <cstring>
 
 namespace ctg {
@@ -14,6 +16,72 @@ DBuf::DBuf(Ctx* c, size_t n) : ctx(c), bytes(n) { ptr = c->alloc(n); }
 DBuf::~DBuf()
 {
 	if (ptr && ctx) ctx->free(ptr);
+}
+
+// ---- plan cache ------------------------------------------------------------------------
+// An entry holds the operand structures it was built for (dims, directions, quantum numbers),
+// the operation parameters, and the plan: a lookup is a hash probe plus an exact comparison.
+struct StructSig {
+	int ndim = 0;
+	std::vector<i64> dim;
+	std::vector<int> dir;
+	std::vector<std::vector<q32>> ql;
+	StructSig() = default;
+	explicit StructSig(const Meta& m) : ndim(m.ndim), dim(m.dim), dir(m.dir), ql(m.ql) {}
+	bool matches(const Meta& m) const { return ndim == m.ndim && dim == m.dim && dir == m.dir && ql == m.ql; }
+};
+
+struct PlanEntry {
+	int kind = 0;
+	std::vector<i64> params;
+	StructSig s, t;
+	DotPlan dot;
+	CopyPlan copy;
+};
+
+struct PlanCache {
+	std::unordered_multimap<uint64_t, PlanEntry> map;
+	size_t bytes = 0;
+	static constexpr size_t MAX_ENTRIES = 1 << 14;
+	static constexpr size_t MAX_BYTES = (size_t)1 << 30;
+};
+
+static uint64_t plan_key(int kind, const std::vector<i64>& params, const Meta& s, const Meta* t)
+{
+	uint64_t h = s.structure_hash() * 0x9e3779b97f4a7c15ull + (uint64_t)kind;
+	if (t) h ^= t->structure_hash() + 0x632be59bd9b4e019ull + (h << 7) + (h >> 3);
+	for (i64 v : params) h = (h ^ (uint64_t)v) * 0x100000001b3ull;
+	return h;
+}
+
+static const PlanEntry* plan_find(Ctx& c, uint64_t key, int kind, const std::vector<i64>& params, const Meta& s,
+                                  const Meta* t)
+{
+	PlanCache* pc = c.plans();
+	auto range = pc->map.equal_range(key);
+	for (auto it = range.first; it != range.second; ++it)
+	{
+		const PlanEntry& e = it->second;
+		if (e.kind == kind && e.params == params && e.s.matches(s) && (!t || e.t.matches(*t)))
+		{
+			c.plan_hits++;
+			return &e;
+		}
+	}
+	c.plan_misses++;
+	return nullptr;
+}
+
+static void plan_insert(Ctx& c, uint64_t key, PlanEntry&& e, size_t bytes)
+{
+	PlanCache* pc = c.plans();
+	if (pc->map.size() >= PlanCache::MAX_ENTRIES || pc->bytes + bytes > PlanCache::MAX_BYTES)
+	{
+		pc->map.clear();
+		pc->bytes = 0;
+	}
+	pc->bytes += bytes;
+	pc->map.emplace(key, std::move(e));
 }
 
 Ctx::Ctx(int device) : dev_(device)
@@ -31,12 +99,25 @@ Ctx::Ctx(int device) : dev_(device)
 	CTG_CUDA(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &thr));
 	staging_cap_ = (size_t)64 << 20;
 	CTG_CUDA(cudaMallocHost((void**)&staging_, staging_cap_));
+	plans_ = new PlanCache();
 	CTG_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
 	for (int i = 0; i < NUM_AUX; i++)
 	{
 		CTG_CUDA(cudaStreamCreateWithFlags(&aux_[i], cudaStreamNonBlocking));
 		CTG_CUDA(cudaEventCreateWithFlags(&join_ev_[i], cudaEventDisableTiming));
 	}
+}
+
+static double host_seconds()
+{
+	return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+PlanTimer::PlanTimer(Ctx& ctx) : c(ctx), t0(host_seconds()) {}
+
+PlanTimer::~PlanTimer()
+{
+	c.host_plan_s += host_seconds() - t0;
 }
 
 cudaStream_t Ctx::aux(int i)
@@ -70,6 +151,7 @@ Ctx::~Ctx()
 		if (aux_[i]) cudaStreamDestroy(aux_[i]);
 		if (join_ev_[i]) cudaEventDestroy(join_ev_[i]);
 	}
+	delete plans_;
 	if (fork_ev_) cudaEventDestroy(fork_ev_);
 	if (staging_) cudaFreeHost(staging_);
 	if (pool_) cudaMemPoolDestroy(pool_);
@@ -300,7 +382,7 @@ int tile_class(int m, int n)
 // dot (block_sparse_tensor.c:1826-2001; dense_tensor.c:1761-1837)
 // ------------------------------------------------------------------------------------
 
-DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
+static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
 {
 	DotPlan p;
 	auto out = std::make_shared<Meta>(dot_result_meta(s, axs, t, axt, nmult));
@@ -481,7 +563,7 @@ static CopyPlan finish_rows(Ctx& c, std::shared_ptr<Meta> out, const std::vector
 }
 
 // block_sparse_tensor_transpose (block_sparse_tensor.c:785-870)
-CopyPlan make_transpose_plan(Ctx& c, const Meta& t, const int* perm)
+static CopyPlan build_transpose_plan(Ctx& c, const Meta& t, const int* perm)
 {
 	auto out = std::make_shared<Meta>(transpose_meta(t, perm));
 	const Meta& r = *out;
@@ -516,7 +598,7 @@ CopyPlan make_transpose_plan(Ctx& c, const Meta& t, const int* perm)
 
 // block_sparse_tensor_flatten_axes (block_sparse_tensor.c:950-1112): each source block
 // scatters its rows (j0, j1) into the fused rows of one target block
-CopyPlan make_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
+static CopyPlan build_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
 {
 	auto out = std::make_shared<Meta>(flatten_meta(t, ax, newdir));
 	const Meta& r = *out;
@@ -558,7 +640,7 @@ CopyPlan make_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
 
 // block_sparse_tensor_split_axis (block_sparse_tensor.c:1123-1285): each target block
 // gathers its rows (j0, j1) from the fused rows of one source block
-CopyPlan make_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
+static CopyPlan build_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
 {
 	auto out = std::make_shared<Meta>(split_meta(t, ax, nd, ndir, nq));
 	const Meta& r = *out;
@@ -598,7 +680,7 @@ CopyPlan make_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const i
 }
 
 // block_sparse_tensor_slice (block_sparse_tensor.c:1446-1553)
-CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& ind)
+static CopyPlan build_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& ind)
 {
 	auto out = std::make_shared<Meta>(slice_meta(t, ax, ind));
 	const Meta& r = *out;
@@ -632,6 +714,73 @@ CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& 
 	}
 	check_rows(descs, maps, t.nnz, r.nnz);
 	return finish_rows(c, out, descs, chunks, maps);
+}
+
+
+// ---- cached entry points ----------------------------------------------------------------
+
+DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
+{
+	PlanTimer plan_timer(c);
+	const std::vector<i64> params = {axs, axt, nmult, precision};
+	const uint64_t key = plan_key(0, params, s, &t);
+	if (const PlanEntry* e = plan_find(c, key, 0, params, s, &t)) return e->dot;
+	PlanEntry e;
+	e.kind = 0;
+	e.params = params;
+	e.s = StructSig(s);
+	e.t = StructSig(t);
+	e.dot = build_dot_plan(c, s, axs, t, axt, nmult, precision);
+	const size_t bytes = e.dot.desc ? e.dot.desc->bytes : 0;
+	DotPlan p = e.dot;
+	plan_insert(c, key, std::move(e), bytes);
+	return p;
+}
+
+static CopyPlan cached_copy(Ctx& c, int kind, const std::vector<i64>& params, const Meta& t,
+                            const std::function<CopyPlan()>& build)
+{
+	const uint64_t key = plan_key(kind, params, t, nullptr);
+	if (const PlanEntry* e = plan_find(c, key, kind, params, t, nullptr)) return e->copy;
+	PlanEntry e;
+	e.kind = kind;
+	e.params = params;
+	e.s = StructSig(t);
+	e.copy = build();
+	const size_t bytes = e.copy.desc ? e.copy.desc->bytes : 0;
+	CopyPlan p = e.copy;
+	plan_insert(c, key, std::move(e), bytes);
+	return p;
+}
+
+CopyPlan make_transpose_plan(Ctx& c, const Meta& t, const int* perm)
+{
+	PlanTimer plan_timer(c);
+	const std::vector<i64> params(perm, perm + t.ndim);
+	return cached_copy(c, 1, params, t, [&] { return build_transpose_plan(c, t, perm); });
+}
+
+CopyPlan make_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
+{
+	PlanTimer plan_timer(c);
+	return cached_copy(c, 2, {ax, newdir}, t, [&] { return build_flatten_plan(c, t, ax, newdir); });
+}
+
+CopyPlan make_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
+{
+	PlanTimer plan_timer(c);
+	std::vector<i64> params = {ax, nd[0], nd[1], ndir[0], ndir[1], nq ? 1 : 0};
+	if (nq)
+		for (q32 q : *nq) params.push_back(q);
+	return cached_copy(c, 3, params, t, [&] { return build_split_plan(c, t, ax, nd, ndir, nq); });
+}
+
+CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& ind)
+{
+	PlanTimer plan_timer(c);
+	std::vector<i64> params = {ax};
+	params.insert(params.end(), ind.begin(), ind.end());
+	return cached_copy(c, 4, params, t, [&] { return build_slice_plan(c, t, ax, ind); });
 }
 
 // ------------------------------------------------------------------------------------

@@ -81,6 +81,11 @@ public:
 	long kernel_launches = 0;
 	int svd_max_sweeps = 0;      // largest Jacobi sweep count of any block SVD
 	int svd_full_reruns = 0;     // SVDs repeated at full resolution for the truncation decision
+	double host_plan_s = 0;      // host time spent lowering operations into descriptor lists
+	long plan_hits = 0, plan_misses = 0;
+	// cache of lowered operations, keyed by operation and operand structures (DMRG revisits the
+	// same block structures every sweep once the bond dimensions have settled)
+	struct PlanCache* plans() { return plans_; }
 	// device flag raised by a tensor-core kernel whose bounded wait timed out (checked at sync)
 	int* tc_error();
 	int num_sms() const { return sms_; }
@@ -102,6 +107,7 @@ private:
 	int sms_ = 1;
 	int* tc_error_ = nullptr;
 	bool tc_used_ = false;
+	struct PlanCache* plans_ = nullptr;
 	cudaStream_t st_ = nullptr;
 	cudaStream_t aux_[NUM_AUX] = {};
 	cudaEvent_t fork_ev_ = nullptr;
@@ -109,6 +115,14 @@ private:
 	cudaMemPool_t pool_ = nullptr;
 	char* staging_ = nullptr;
 	size_t staging_cap_ = 0, staging_used_ = 0;
+};
+
+// Adds the host time of its scope to Ctx::host_plan_s.
+struct PlanTimer {
+	Ctx& c;
+	double t0;
+	explicit PlanTimer(Ctx& ctx);
+	~PlanTimer();
 };
 
 // Per-thread execution context for a device, created on first use and kept for the

@@ -50,6 +50,32 @@ bool Meta::same_structure(const Meta& o) const
 	return ndim == o.ndim && dim == o.dim && dir == o.dir && ql == o.ql;
 }
 
+static inline uint64_t mix64(uint64_t h, uint64_t v)
+{
+	// splitmix64 finaliser applied to the running state combined with the next word
+	uint64_t z = h ^ (v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2));
+	z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+	z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+	return z ^ (z >> 31);
+}
+
+uint64_t Meta::structure_hash() const
+{
+	if (!hashed_)
+	{
+		uint64_t h = mix64(0, (uint64_t)ndim);
+		for (int i = 0; i < ndim; i++)
+		{
+			h = mix64(h, (uint64_t)dim[(size_t)i]);
+			h = mix64(h, (uint64_t)(int64_t)dir[(size_t)i]);
+			for (q32 q : ql[(size_t)i]) h = mix64(h, (uint64_t)(uint32_t)q);
+		}
+		hash_ = h;
+		hashed_ = true;
+	}
+	return hash_;
+}
+
 Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::vector<q32>>& ql)
 {
 	CTG_CHECK(ndim >= 1 && ndim <= 8, "tensor degree out of range");

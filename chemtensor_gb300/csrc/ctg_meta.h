@@ -45,6 +45,12 @@ struct Meta {
 	int find(const i64* idx) const;
 	int find_q(int ax, q32 q) const;          // block index of a quantum number on an axis, or -1
 	bool same_structure(const Meta& o) const;
+	// hash of (ndim, dim, dir, ql): equal structures hash equally (computed once, on first use)
+	uint64_t structure_hash() const;
+
+private:
+	mutable uint64_t hash_ = 0;
+	mutable bool hashed_ = false;
 };
 
 // Build the block structure from logical dims, directions and quantum numbers.

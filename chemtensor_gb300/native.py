@@ -54,6 +54,7 @@ class Stats(C.Structure):
         ("split_ms", C.c_double), ("env_ms", C.c_double), ("matvec_flops", C.c_double),
         ("total_gemm_flops", C.c_double), ("matvecs", C.c_long), ("kernel_launches", C.c_long),
         ("sweeps", C.c_int), ("max_bond_dim", C.c_int64), ("svd_max_sweeps", C.c_int),
+        ("host_plan_s", C.c_double), ("plan_hits", C.c_long), ("plan_misses", C.c_long),
     ]
 
 

@@ -66,6 +66,9 @@ struct ctgpu_stats
 	int    sweeps;
 	ct_long max_bond_dim;
 	int    svd_max_sweeps;    /* largest Jacobi sweep count of any block SVD */
+	double host_plan_s;       /* host time spent lowering operations into device work lists */
+	long   plan_hits;         /* lowered operations reused from the per-thread plan cache */
+	long   plan_misses;       /* lowered operations built afresh */
 };
 int ctgpu_get_last_stats(struct ctgpu_stats* out);
 
