@@ -216,7 +216,7 @@ DTensor merge_mpo_pair(Ctx& c, const DTensor& w0, const DTensor& w1)
 // contraction_operator_step_left (src/algorithm/chain_ops.c:196-245), with b = a
 DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, int precision)
 {
-	DTensor br = view_reversed(a);
+	DTensor br = view_reversed(c, a);
 	DTensor s = op_dot(c, l, AX_TRAILING, br, AX_LEADING, 1, precision);
 	const int p0[5] = {0, 1, 4, 2, 3};
 	DTensor t = op_transpose(c, s, p0);
@@ -237,7 +237,7 @@ DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const
 	s = op_dot(c, w, AX_TRAILING, t, AX_LEADING, 2, precision);
 	const int p1[5] = {4, 2, 0, 1, 3};
 	t = op_transpose(c, s, p1);
-	DTensor br = view_reversed(a);
+	DTensor br = view_reversed(c, a);
 	s = op_dot(c, t, AX_TRAILING, br, AX_TRAILING, 2, precision);
 	const int p2[4] = {1, 2, 3, 0};
 	return op_transpose(c, s, p2);
@@ -306,28 +306,16 @@ int split_mps_svd(Ctx& c, const DTensor& a, i64 d, const std::vector<q32>& qsite
 	DTensor tmp = op_flatten(c, a4, 0, TENSOR_AXIS_OUT);
 	DTensor am = op_flatten(c, tmp, 1, TENSOR_AXIS_IN);
 	SvdResult sv;
-	int ret = op_svd(c, am, sv, tol);    // synchronises
+	SvdPending pend;
+	int ret = op_svd_launch(c, am, sv, pend);
 	if (ret < 0) return ret;
-	std::vector<double> sigma((size_t)sv.ns);
-	CTG_CUDA(cudaMemcpy(sigma.data(), sv.s->ptr, sigma.size() * sizeof(double), cudaMemcpyDeviceToHost));
-	TruncResult tr = retained_bond_indices(sigma.data(), sv.ns, tol, true, max_vdim);
-	// Directions the SVD left unresolved weigh at most sv.max_tail in total per block. They
-	// cannot influence the truncation if that bound is far below the smallest retained squared
-	// singular value; otherwise (rare) resolve everything and decide again.
-	if (sv.max_tail > 0)
-	{
-		double smin2 = tr.ind.empty() ? 0.0 : sigma[(size_t)tr.ind[0]] * sigma[(size_t)tr.ind[0]];
-		for (i64 i : tr.ind) smin2 = std::min(smin2, sigma[(size_t)i] * sigma[(size_t)i]);
-		if (!(sv.max_tail < 1e-2 * smin2))
-		{
-			sv = SvdResult();
-			ret = op_svd(c, am, sv, 0.0);
-			if (ret < 0) return ret;
-			CTG_CUDA(cudaMemcpy(sigma.data(), sv.s->ptr, sigma.size() * sizeof(double), cudaMemcpyDeviceToHost));
-			tr = retained_bond_indices(sigma.data(), sv.ns, tol, true, max_vdim);
-			c.svd_full_reruns++;
-		}
-	}
+	// the one host synchronisation of a bond step: the truncation needs the singular values
+	double* sigma = c.pinned_doubles((size_t)sv.ns);
+	CTG_CUDA(cudaMemcpyAsync(sigma, sv.s->ptr, (size_t)sv.ns * sizeof(double), cudaMemcpyDeviceToHost, c.stream()));
+	c.sync();
+	ret = op_svd_finish(c, pend);
+	if (ret < 0) return ret;
+	TruncResult tr = retained_bond_indices(sigma, sv.ns, tol, true, max_vdim);
 	std::vector<double> sret;
 	if (tr.ind.empty())
 	{
@@ -381,12 +369,17 @@ struct LocalH {
 		const int p2[4] = {0, 3, 1, 2};
 		k = op_transpose(c, l, p2);
 		d3 = make_dot_plan(c, k.m(), AX_TRAILING, *t1.out, AX_LEADING, 2, precision);
-		// the cyclic partial trace of the unit outer bonds keeps blocks and entries (view_trace_unit)
+		// the cyclic partial trace of the unit outer bonds keeps blocks and entries (view_trace_unit):
+		// with outer axes of dimension 1, equal quantum numbers and opposite directions, the inner
+		// axes obey the conservation law of a, so equal inner axes mean an equal block structure
 		const Meta& o = *d3.out;
-		std::vector<std::vector<q32>> ql(o.ql.begin() + 1, o.ql.end() - 1);
-		Meta tr = make_meta(o.ndim - 2, o.dim.data() + 1, o.dir.data() + 1, ql);
-		CTG_CHECK(tr.same_structure(a) && tr.nnz == a.nnz && tr.nblocks == a.nblocks && o.nnz == a.nnz,
-		          "local Hamiltonian output structure differs from the input");
+		bool same = o.ndim == a.ndim + 2 && o.dim[0] == 1 && o.dim[(size_t)o.ndim - 1] == 1 &&
+		            o.dir[0] == -o.dir[(size_t)o.ndim - 1] && o.ql[0] == o.ql[(size_t)o.ndim - 1] && o.nnz == a.nnz &&
+		            o.nblocks == a.nblocks;
+		for (int i = 0; same && i < a.ndim; i++)
+			same = o.dim[(size_t)i + 1] == a.dim[(size_t)i] && o.dir[(size_t)i + 1] == a.dir[(size_t)i] &&
+			       o.ql[(size_t)i + 1] == a.ql[(size_t)i];
+		CTG_CHECK(same, "local Hamiltonian output structure differs from the input");
 		s1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
 		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t0.out->nnz, 1) * sizeof(double));
 		s2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
@@ -406,10 +399,14 @@ struct LocalH {
 
 // minimize_local_energy (src/algorithm/dmrg.c:86-147) with lanczos_iteration_d and
 // eigensystem_krylov_symmetric (src/util/krylov.c:24-89, :172-251) on the device
+thread_local double g_host_detail[4];       // host time: local-H setup, matvecs, vector kernels, teardown
+
 int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTensor& r, const DTensor& a_start, int maxiter,
                           LanczosScalars* d_sc, DTensor& a_opt, DmrgStats* st, int precision)
 {
+	double hz = now_s();
 	LocalH h(c, a_start.m(), w, l, r, precision);
+	g_host_detail[0] += now_s() - hz;
 	const i64 n = a_start.m().nnz;
 	DBuf V(&c, (size_t)maxiter * n * sizeof(double));
 	DBuf wv(&c, (size_t)n * sizeof(double));
@@ -425,7 +422,10 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 	}
 	for (int j = 0; j < maxiter; j++)
 	{
+		hz = now_s();
 		h.apply(c, Vp + (i64)j * n, wp);
+		g_host_detail[1] += now_s() - hz;
+		hz = now_s();
 		{
 			KScope ks(c, K_LANCZOS, 2, 2.0 * dn, 16.0 * dn);
 			launch_lz_alpha(wp, Vp + (i64)j * n, n, j, pp, d_sc, s);
@@ -436,8 +436,9 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 			launch_lz_orth_beta(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, n, j, pp, d_sc, s);
 			launch_lz_next(wp, Vp + (i64)(j + 1) * n, n, j, d_sc, s);
 		}
+		g_host_detail[2] += now_s() - hz;
 	}
-	a_opt = c.empty(a_start.m());
+	a_opt = c.empty(a_start.meta);
 	{
 		KScope ks(c, K_LANCZOS, 2, 2.0 * maxiter * dn, 8.0 * (maxiter + 1) * dn);
 		launch_lz_tridiag(maxiter, d_sc, s);
@@ -457,7 +458,7 @@ DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w,
                                      int precision)
 {
 	LocalH h(c, a.m(), w, l, r, precision);
-	DTensor out = c.empty(a.m());
+	DTensor out = c.empty(a.meta);
 	h.apply(c, a.data(), out.data());
 	return out;
 }
@@ -489,9 +490,11 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	c.host_plan_s = 0;
 	c.plan_hits = 0;
 	c.plan_misses = 0;
+	for (double& x : c.svd_phase_ms) x = 0;
+	for (double& x : c.svd_jacobi_cycles) x = 0;
+	for (double& x : g_host_detail) x = 0;
 	DBuf sc_buf(&c, sizeof(LanczosScalars));
 	LanczosScalars* d_sc = (LanczosScalars*)sc_buf.ptr;
-	LanczosScalars h_sc;
 
 	// upload
 	std::vector<DTensor> W(L), A(L);
@@ -533,21 +536,31 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	const double t_setup = now_s();
 	st->setup_s = t_setup - t_up;
 
-	cudaEvent_t ev[4];
-	for (auto& e : ev) CTG_CUDA(cudaEventCreate(&e));
-	auto bond_step = [&](int i, bool left_to_right, int prec) -> int {
+	// four events per bond step (start, Lanczos done, split done, environment done), read at the
+	// end of each sweep so that timing adds no host synchronisation
+	const int nbond = 2 * (L - 1);
+	std::vector<cudaEvent_t> bev((size_t)4 * nbond);
+	for (auto& e : bev) CTG_CUDA(cudaEventCreate(&e));
+	LanczosScalars* h_sc = c.lanczos_host();
+	double host_t[3] = {0, 0, 0};             // host time enqueueing Lanczos, in the split, enqueueing environments
+	auto bond_step = [&](int i, bool left_to_right, int prec, int slot) -> int {
+		cudaEvent_t* ev = &bev[(size_t)4 * slot];
+		const double h0 = now_s();
 		CTG_CUDA(cudaEventRecord(ev[0], c.stream()));
 		DTensor cur = merge_mps_pair(c, A[i], A[i + 1]);
 		DTensor aopt;
 		int r = minimize_local_energy(c, h2[i], lb[i], rb[i + 1], cur, maxiter, d_sc, aopt, st, prec);
 		if (r < 0) return r;
+		CTG_CUDA(cudaMemcpyAsync(h_sc, d_sc, sizeof(LanczosScalars), cudaMemcpyDeviceToHost, c.stream()));
 		CTG_CUDA(cudaEventRecord(ev[1], c.stream()));
+		const double h1 = now_s();
 		double ent = 0;
+		// synchronises once (for the singular values); the Lanczos scalars have arrived by then
 		r = split_mps_svd(c, aopt, psi->d, qsite, tol_split, max_vdim, !left_to_right, A[i], A[i + 1], &ent);
 		if (r < 0) return r;
-		CTG_CUDA(cudaMemcpy(&h_sc, d_sc, sizeof(LanczosScalars), cudaMemcpyDeviceToHost));
-		if (h_sc.status != 0) return h_sc.status;
+		if (h_sc->status != 0) return h_sc->status;
 		CTG_CUDA(cudaEventRecord(ev[2], c.stream()));
+		const double h2 = now_s();
 		// environments stay FP64 in every sweep: each one is built from its neighbour, so
 		// rounding errors of a reduced-precision product would accumulate along the chain
 		if (left_to_right) lb[i + 1] = contraction_step_left(c, A[i], W[i], lb[i], GEMM_FP64);
@@ -557,12 +570,10 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 			rb[i] = contraction_step_right(c, A[i + 1], W[i + 1], rb[i + 1], GEMM_FP64);
 		}
 		CTG_CUDA(cudaEventRecord(ev[3], c.stream()));
-		CTG_CUDA(cudaEventSynchronize(ev[1]));
-		float ms = 0;
-		CTG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
-		st->lanczos_ms += ms;
-		CTG_CUDA(cudaEventElapsedTime(&ms, ev[1], ev[2]));
-		st->split_ms += ms;
+		const double h3 = now_s();
+		host_t[0] += h1 - h0;
+		host_t[1] += h2 - h1;
+		host_t[2] += h3 - h2;
 		return 0;
 	};
 
@@ -582,20 +593,11 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		// local eigenproblem in FP64, so the returned state and energies are FP64 results
 		const int prec = sw < num_sweeps - std::max(opt.final_fp64_sweeps, 0) ? opt.precision : (int)GEMM_FP64;
 		CTG_CUDA(cudaEventRecord(sw_ev[0], c.stream()));
-		for (int i = 0; i < L - 2 && ret == 0; i++) ret = bond_step(i, true, prec);
-		for (int i = L - 2; i >= 0 && ret == 0; i--)
-		{
-			ret = bond_step(i, false, prec);
-			if (ret == 0)
-			{
-				CTG_CUDA(cudaEventSynchronize(ev[3]));
-				float ms = 0;
-				CTG_CUDA(cudaEventElapsedTime(&ms, ev[2], ev[3]));
-				st->env_ms += ms;
-			}
-		}
+		int slot = 0;
+		for (int i = 0; i < L - 2 && ret == 0; i++) ret = bond_step(i, true, prec, slot++);
+		for (int i = L - 2; i >= 0 && ret == 0; i--) ret = bond_step(i, false, prec, slot++);
 		if (ret < 0) break;
-		en = h_sc.lambda;
+		en = h_sc->lambda;
 		// right-normalise the leftmost tensor (dmrg.c:366-378)
 		DTensor t = head_tensor(c, A[0], 0.0);
 		ret = local_orthonormalize_rq(c, A[0], t);
@@ -606,14 +608,32 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		CTG_CUDA(cudaEventElapsedTime(&sms, sw_ev[0], sw_ev[1]));
 		st->sweep_ms.push_back(sms);
 		st->sweep_launches.push_back(c.kernel_launches - launches0);
+		for (int k = 0; k < slot; k++)
+		{
+			const cudaEvent_t* ev = &bev[(size_t)4 * k];
+			float ms = 0;
+			CTG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+			st->lanczos_ms += ms;
+			CTG_CUDA(cudaEventElapsedTime(&ms, ev[1], ev[2]));
+			st->split_ms += ms;
+			CTG_CUDA(cudaEventElapsedTime(&ms, ev[2], ev[3]));
+			st->env_ms += ms;
+		}
 		c.profile = false;
 		st->sweeps++;
 	}
 	c.sync();
 	c.profile = false;
 	for (int k = 0; k < K_NUM_CLASSES; k++) st->prof[k] = c.prof[k];
-	for (auto& e : ev) cudaEventDestroy(e);
+	for (auto& e : bev) cudaEventDestroy(e);
 	for (auto& e : sw_ev) cudaEventDestroy(e);
+	if (getenv("CTGPU_HOST_TIMES") && st->sweeps > 0)
+	{
+		fprintf(stderr, "ctgpu: host ms per sweep: Lanczos enqueue %.1f, split (incl. wait) %.1f, environment enqueue %.1f\n",
+		        1e3 * host_t[0] / st->sweeps, 1e3 * host_t[1] / st->sweeps, 1e3 * host_t[2] / st->sweeps);
+		fprintf(stderr, "ctgpu: host ms per sweep in Lanczos: local-H setup %.1f, matvec enqueue %.1f, vector kernels %.1f\n",
+		        1e3 * g_host_detail[0] / st->sweeps, 1e3 * g_host_detail[1] / st->sweeps, 1e3 * g_host_detail[2] / st->sweeps);
+	}
 	const double t_sweeps = now_s();
 	st->sweep_s = t_sweeps - t_setup;
 	if (ret < 0) return ret;
@@ -633,6 +653,14 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	st->host_plan_s = c.host_plan_s;
 	st->plan_hits = c.plan_hits;
 	st->plan_misses = c.plan_misses;
+	if (getenv("CTGPU_SVD_PHASES") && st->sweeps > 0)
+		fprintf(stderr, "ctgpu: block SVD, last-finishing block per call, ms per sweep: QR %.2f Jacobi %.2f outputs %.2f launch %.2f\n",
+		        c.svd_phase_ms[0] / st->sweeps, c.svd_phase_ms[1] / st->sweeps, c.svd_phase_ms[2] / st->sweeps,
+		        c.svd_phase_ms[3] / st->sweeps);
+	if (getenv("CTGPU_SVD_PHASES") && st->sweeps > 0)
+		fprintf(stderr, "ctgpu: Jacobi of that block, SM cycles per sweep: inner products %.3g parameters %.3g rotations %.3g exchanges %.3g\n",
+		        c.svd_jacobi_cycles[0] / st->sweeps, c.svd_jacobi_cycles[1] / st->sweeps, c.svd_jacobi_cycles[2] / st->sweeps,
+		        c.svd_jacobi_cycles[3] / st->sweeps);
 	st->wall_s = now_s() - t_start;
 	return 0;
 }

@@ -24,7 +24,7 @@ struct DmrgStats {
 	double sweep_s = 0;          // all sweeps
 	double lanczos_ms = 0;       // device time in the Lanczos eigensolver (CUDA events)
 	double split_ms = 0;         // device+host time in the SVD split
-	double env_ms = 0;           // device time in the environment updates
+	double env_ms = 0;           // device time in the environment updates (both directions)
 	double matvec_flops = 0;     // algorithmic GEMM FLOPs of all local-H applications
 	double total_gemm_flops = 0; // algorithmic GEMM FLOPs of everything
 	long matvecs = 0;

@@ -2,8 +2,10 @@
 #include "ctg_engine.h"
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <functional>
+#include <memory>
 #include <cstring>
 
 namespace ctg {
@@ -100,6 +102,8 @@ Ctx::Ctx(int device) : dev_(device)
 	staging_cap_ = (size_t)64 << 20;
 	CTG_CUDA(cudaMallocHost((void**)&staging_, staging_cap_));
 	plans_ = new PlanCache();
+	CTG_CUDA(cudaMallocHost(&pinned_, 4096));
+	memset(pinned_, 0, 4096);
 	CTG_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
 	for (int i = 0; i < NUM_AUX; i++)
 	{
@@ -118,6 +122,20 @@ PlanTimer::PlanTimer(Ctx& ctx) : c(ctx), t0(host_seconds()) {}
 PlanTimer::~PlanTimer()
 {
 	c.host_plan_s += host_seconds() - t0;
+}
+
+static_assert(256 + sizeof(LanczosScalars) <= 4096, "pinned result slots overlap");
+
+double* Ctx::pinned_doubles(size_t n)
+{
+	if (n > pinned_d_cap_)
+	{
+		if (pinned_d_) CTG_CUDA(cudaFreeHost(pinned_d_));
+		pinned_d_ = nullptr;
+		pinned_d_cap_ = std::max<size_t>(n, 1 << 16);
+		CTG_CUDA(cudaMallocHost((void**)&pinned_d_, pinned_d_cap_ * sizeof(double)));
+	}
+	return pinned_d_;
 }
 
 cudaStream_t Ctx::aux(int i)
@@ -152,6 +170,8 @@ Ctx::~Ctx()
 		if (join_ev_[i]) cudaEventDestroy(join_ev_[i]);
 	}
 	delete plans_;
+	if (pinned_) cudaFreeHost(pinned_);
+	if (pinned_d_) cudaFreeHost(pinned_d_);
 	if (fork_ev_) cudaEventDestroy(fork_ev_);
 	if (staging_) cudaFreeHost(staging_);
 	if (pool_) cudaMemPoolDestroy(pool_);
@@ -303,6 +323,14 @@ DTensor Ctx::empty(const Meta& m)
 	return t;
 }
 
+DTensor Ctx::empty(const std::shared_ptr<const Meta>& m)
+{
+	DTensor t;
+	t.meta = m;
+	t.buf = std::make_shared<DBuf>(this, (size_t)std::max<i64>(m->nnz, 1) * sizeof(double));
+	return t;
+}
+
 DTensor Ctx::zeros(const Meta& m)
 {
 	DTensor t = empty(m);
@@ -399,8 +427,11 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	std::vector<GemmOut> outs(r.nblocks);
 	std::vector<GemmContrib> cons;
 	std::vector<GemmTile> tiles[NUM_TILE_CLASSES];
+	// contracted block indices: all combinations over the first nmult - 1 contracted axes; the
+	// last one is fixed by the conservation law of s
 	i64 ncontract = 1;
-	for (int i = 0; i < nmult; i++) ncontract *= t.nb[shift_t + i];
+	for (int i = 0; i < nmult - 1; i++) ncontract *= t.nb[shift_t + i];
+	const int lc = shift_s + nmult - 1;          // last contracted axis of s
 	std::vector<i64> is(s.ndim), it(t.ndim), ic(nmult);
 	double flops = 0;
 	for (int b = 0; b < r.nblocks; b++)
@@ -412,10 +443,23 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 		o.m = (int)prod(rd, nfs);
 		o.n = (int)prod(rd + nfs, nft);
 		o.c0 = (int)cons.size();
+		long long qfree = 0;
+		for (int i = 0; i < nfs; i++) qfree += (long long)s.dir[off_s + i] * s.qb[off_s + i][ir[i]];
 		for (i64 mm = 0; mm < ncontract; mm++)
 		{
 			i64 rem = mm;
-			for (int i = nmult - 1; i >= 0; i--) { ic[i] = rem % t.nb[shift_t + i]; rem /= t.nb[shift_t + i]; }
+			long long qsum = qfree;
+			for (int i = nmult - 2; i >= 0; i--)
+			{
+				ic[i] = rem % t.nb[shift_t + i];
+				rem /= t.nb[shift_t + i];
+				qsum += (long long)s.dir[shift_s + i] * s.qb[shift_s + i][ic[i]];
+			}
+			const long long qneed = -(long long)s.dir[lc] * qsum;
+			if (qneed < INT32_MIN || qneed > INT32_MAX) continue;
+			const int jl = s.find_q(lc, (q32)qneed);
+			if (jl < 0) continue;
+			ic[nmult - 1] = jl;
 			for (int i = 0; i < nfs; i++) is[off_s + i] = ir[i];
 			for (int i = 0; i < nmult; i++) is[shift_s + i] = ic[i];
 			const int bs = s.find(is.data());
@@ -449,17 +493,100 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 		}
 		o.nc = (int)cons.size() - o.c0;
 		CTG_CHECK(o.m >= 1 && o.n >= 1 && o.c_off + (i64)o.m * o.n <= r.nnz, "dot: output block out of range");
+		// every tile first takes the whole sum over the block's contributions
+		GemmTile whole = {};
+		whole.out = b;
+		whole.c0 = o.c0;
+		whole.k0 = 0;
+		whole.c1 = o.c0 + o.nc - 1;
+		whole.k1 = o.nc > 0 ? cons[(size_t)whole.c1].k : 0;
+		whole.part = -1;
 		if (precision == GEMM_BF16X3)
 		{
 			// tensor-core tiles: one tile class
 			for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
-				for (int n0 = 0; n0 < o.n; n0 += tc_tile_cols()) tiles[0].push_back(GemmTile{b, m0, n0});
+				for (int n0 = 0; n0 < o.n; n0 += tc_tile_cols())
+				{
+					whole.m0 = m0;
+					whole.n0 = n0;
+					tiles[0].push_back(whole);
+				}
 			continue;
 		}
 		const int cls = tile_class(o.m, o.n);
 		const int tr = tile_rows(cls), tc = tile_cols(cls);
 		for (int m0 = 0; m0 < o.m; m0 += tr)
-			for (int n0 = 0; n0 < o.n; n0 += tc) tiles[cls].push_back(GemmTile{b, m0, n0});
+			for (int n0 = 0; n0 < o.n; n0 += tc)
+			{
+				whole.m0 = m0;
+				whole.n0 = n0;
+				tiles[cls].push_back(whole);
+			}
+	}
+	// Split-K: on GB300 one SM retires about two FP64 FMAs per clock, so a block GEMM with fewer
+	// tiles than SMs leaves most of the FP64 pipes idle. Tiles whose work exceeds a fair share of
+	// the whole product are cut into shares of consecutive 16-wide k chunks, one CTA each; their
+	// partial sums are added in a fixed order (deterministic) by k_gemm_reduce.
+	std::vector<GemmSplit> splits;
+	i64 wsz = 0;
+	if (precision != GEMM_BF16X3)
+	{
+		constexpr int KCH = 16;                  // k chunk of the FP64 kernels
+		auto nchunks = [&](const GemmOut& o) {
+			i64 n = 0;
+			for (int cc = o.c0; cc < o.c0 + o.nc; cc++) n += (cons[(size_t)cc].k + KCH - 1) / KCH;
+			return n;
+		};
+		double total = 0;
+		for (int k = 0; k < NUM_TILE_CLASSES; k++)
+			for (const GemmTile& t : tiles[k])
+				total += (double)tile_rows(k) * tile_cols(k) * (double)(nchunks(outs[(size_t)t.out]) * KCH);
+		const double target = std::max(total / (2.0 * c.num_sms()), 65536.0);
+		std::vector<std::pair<int, int>> pos;
+		for (int k = 0; k < NUM_TILE_CLASSES; k++)
+		{
+			std::vector<GemmTile> kept;
+			const int tr = tile_rows(k), tc = tile_cols(k);
+			for (const GemmTile& t : tiles[k])
+			{
+				const GemmOut& o = outs[(size_t)t.out];
+				const i64 n = nchunks(o);
+				const double w = (double)tr * tc * (double)(n * KCH);
+				const int S = (int)std::min<double>((double)n, std::ceil(w / target));
+				if (S <= 1)
+				{
+					kept.push_back(t);
+					continue;
+				}
+				pos.clear();
+				for (int cc = o.c0; cc < o.c0 + o.nc; cc++)
+					for (int kk = 0; kk < cons[(size_t)cc].k; kk += KCH) pos.emplace_back(cc, kk);
+				for (int sp = 0; sp < S; sp++)
+				{
+					const i64 a = sp * n / S, e = (sp + 1) * n / S;
+					GemmTile u = t;
+					u.c0 = pos[(size_t)a].first;
+					u.k0 = pos[(size_t)a].second;
+					u.c1 = pos[(size_t)e - 1].first;
+					u.k1 = std::min(pos[(size_t)e - 1].second + KCH, cons[(size_t)u.c1].k);
+					u.part = wsz + (i64)sp * tr * tc;
+					kept.push_back(u);
+				}
+				GemmSplit g = {};
+				g.out = t.out;
+				g.m0 = t.m0;
+				g.n0 = t.n0;
+				g.rows = std::min(tr, o.m - t.m0);
+				g.cols = std::min(tc, o.n - t.n0);
+				g.nsplit = S;
+				g.ld = tc;
+				g.stride = tr * tc;
+				g.part = wsz;
+				splits.push_back(g);
+				wsz += (i64)S * tr * tc;
+			}
+			tiles[k].swap(kept);
+		}
 	}
 	p.precision = precision;
 	if (precision == GEMM_BF16X3)
@@ -471,9 +598,13 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	const size_t o_cons = pk.add(cons);
 	size_t o_tiles[NUM_TILE_CLASSES];
 	for (int k = 0; k < NUM_TILE_CLASSES; k++) o_tiles[k] = pk.add(tiles[k]);
+	const size_t o_splits = pk.add(splits);
 	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
 	p.outs = at<GemmOut>(p.desc, o_outs);
 	p.cons = at<GemmContrib>(p.desc, o_cons);
+	p.splits = at<GemmSplit>(p.desc, o_splits);
+	p.nsplits = (int)splits.size();
+	if (wsz > 0) p.work = std::make_shared<DBuf>(&c, (size_t)wsz * sizeof(double));
 	for (int k = 0; k < NUM_TILE_CLASSES; k++)
 	{
 		p.ntiles[k] = (int)tiles[k].size();
@@ -495,11 +626,17 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 		c.gemm_flops += flops;
 		return;
 	}
+	double* w = work ? (double*)work->ptr : nullptr;
 	for (int k = 0; k < NUM_TILE_CLASSES; k++)
 	{
 		if (ntiles[k] == 0) continue;
 		KScope ks(c, K_GEMM, 1, flops_cls[k], 0);
-		launch_gemm_f64(k, ntiles[k], tiles[k], outs, cons, A, B, C, c.stream());
+		launch_gemm_f64(k, ntiles[k], tiles[k], outs, cons, A, B, C, w, c.stream());
+	}
+	if (nsplits > 0)
+	{
+		KScope ks(c, K_GEMM, 1, 0, 0);
+		launch_gemm_reduce(nsplits, splits, outs, w, C, c.stream());
 	}
 	c.gemm_flops += flops;
 }
@@ -827,9 +964,8 @@ DTensor op_slice(Ctx& c, const DTensor& t, int ax, const std::vector<i64>& ind)
 }
 
 // block_sparse_tensor_multiply_pointwise_vector (block_sparse_tensor.c:1654-1703)
-DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange)
+static CopyPlan build_scale_plan(Ctx& c, const Meta& m, int axrange)
 {
-	const Meta& m = s.m();
 	const int ax = (axrange == AX_LEADING ? 0 : m.ndim - 1);
 	std::vector<ScaleDesc> descs;
 	std::vector<Chunk> chunks;
@@ -852,18 +988,46 @@ DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange)
 	}
 	Packer pk;
 	const size_t od = pk.add(descs), oc = pk.add(chunks), om = pk.add(maps);
-	DBufPtr desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
-	DTensor r = c.empty(m);
-	KScope ks(c, K_SCALE, 1, 0, 16.0 * (double)m.nnz);
-	launch_scale_axis((int)chunks.size(), at<Chunk>(desc, oc), at<ScaleDesc>(desc, od), at<i64>(desc, om), dvec, s.data(),
-	                  r.data(), c.stream());
+	CopyPlan p;
+	p.kind = 2;
+	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	p.descs = at<ScaleDesc>(p.desc, od);
+	p.chunks = at<Chunk>(p.desc, oc);
+	p.maps = at<i64>(p.desc, om);
+	p.nchunks = (int)chunks.size();
+	p.elements = m.nnz;
+	return p;
+}
+
+DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange)
+{
+	CopyPlan p;
+	{
+		PlanTimer plan_timer(c);
+		p = cached_copy(c, 5, {axrange}, s.m(), [&] { return build_scale_plan(c, s.m(), axrange); });
+	}
+	DTensor r = c.empty(s.meta);
+	if (p.nchunks > 0)
+	{
+		KScope ks(c, K_SCALE, 1, 0, 16.0 * (double)s.m().nnz);
+		launch_scale_axis(p.nchunks, p.chunks, (const ScaleDesc*)p.descs, p.maps, dvec, s.data(), r.data(), c.stream());
+	}
 	return r;
 }
 
-DTensor view_reversed(const DTensor& t)
+DTensor view_reversed(Ctx& c, const DTensor& t)
 {
+	CopyPlan p;
+	{
+		PlanTimer plan_timer(c);
+		p = cached_copy(c, 6, {}, t.m(), [&] {
+			CopyPlan q;
+			q.out = std::make_shared<const Meta>(reversed_meta(t.m()));
+			return q;
+		});
+	}
 	DTensor r;
-	r.meta = std::make_shared<const Meta>(reversed_meta(t.m()));
+	r.meta = p.out;
 	r.buf = t.buf;
 	return r;
 }
@@ -889,9 +1053,11 @@ DTensor view_trace_unit(const DTensor& t)
 // SVD and RQ of block-sparse matrices
 // ------------------------------------------------------------------------------------
 
-int op_svd(Ctx& c, const DTensor& a, SvdResult& res, double tol_hint)
+int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 {
 	const Meta& am = a.m();
+	pend = SvdPending();
+	pend.a = a;
 	CTG_CHECK(am.ndim == 2, "svd: matrix expected");
 	// intermediate axis: column quantum numbers (sorted), min(m, n) copies per block
 	std::vector<q32> qi;
@@ -931,7 +1097,6 @@ int op_svd(Ctx& c, const DTensor& a, SvdResult& res, double tol_hint)
 		CTG_CHECK(b >= 0, "svd: dummy block missing");
 		static const double one = 1.0;
 		CTG_CUDA(cudaMemcpyAsync(res.u.data() + mu.boff[b], &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
-		c.sync();
 		return 0;
 	}
 	std::vector<SvdDesc> descs;
@@ -1018,63 +1183,102 @@ int op_svd(Ctx& c, const DTensor& a, SvdResult& res, double tol_hint)
 	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
 	DBuf status(&c, 2 * sizeof(int));
 	CTG_CUDA(cudaMemsetAsync(status.ptr, 0, 2 * sizeof(int), c.stream()));
-	(void)tol_hint;
 	DBuf tail(&c, descs.size() * sizeof(double));
 	CTG_CUDA(cudaMemsetAsync(tail.ptr, 0, descs.size() * sizeof(double), c.stream()));
+	// opt-in diagnostics: per-block phase stamps (QR, Jacobi, outputs) of the shared-memory path
+	static const bool phases = getenv("CTGPU_SVD_PHASES") != nullptr;
+	std::unique_ptr<DBuf> ts;
+	if (phases)
+	{
+		ts.reset(new DBuf(&c, descs.size() * 8 * sizeof(unsigned long long)));
+		CTG_CUDA(cudaMemsetAsync(ts->ptr, 0, ts->bytes, c.stream()));
+	}
+	unsigned long long* tsp = ts ? (unsigned long long*)ts->ptr : nullptr;
 	{
 		KScope ks(c, K_SVD, (int)groups.size());
 		const int ng = (int)std::min<size_t>(groups.size(), Ctx::NUM_AUX);
 		if (groups.size() == 1)
 			launch_svd_group(groups[0].l, groups[0].first, groups[0].count, (const SvdDesc*)desc->ptr, a.data(),
 			                 res.u.data(), (double*)res.s->ptr, res.vh.data(), (double*)scratch.ptr, (int*)status.ptr,
-			                 (double*)tail.ptr, c.stream());
+			                 (double*)tail.ptr, c.stream(), tsp);
 		else
 		{
 			c.fork(ng);
 			for (size_t g = 0; g < groups.size(); g++)
 				launch_svd_group(groups[g].l, groups[g].first, groups[g].count, (const SvdDesc*)desc->ptr, a.data(),
 				                 res.u.data(), (double*)res.s->ptr, res.vh.data(), (double*)scratch.ptr,
-				                 (int*)status.ptr, (double*)tail.ptr, c.aux((int)g));
+				                 (int*)status.ptr, (double*)tail.ptr, c.aux((int)g), tsp);
 			c.join(ng);
 		}
 	}
-	int hst[2] = {0, 0};
-	CTG_CUDA(cudaMemcpyAsync(hst, status.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream()));
-	c.sync();
-	c.svd_max_sweeps = std::max(c.svd_max_sweeps, hst[1]);
+	if (ts)
 	{
-		std::vector<double> tw(descs.size());
-		CTG_CUDA(cudaMemcpy(tw.data(), tail.ptr, tw.size() * sizeof(double), cudaMemcpyDeviceToHost));
-		res.max_tail = 0;
-		for (double x : tw) res.max_tail = std::max(res.max_tail, x);
-	}
-	if (hst[0] != 0)
-	{
-		int mmax = 0, nmax = 0;
-		for (const SvdDesc& d : descs) { mmax = std::max(mmax, d.m); nmax = std::max(nmax, d.n); }
-		fprintf(stderr, "ctgpu: block SVD did not converge within %d Jacobi sweeps (%zu blocks, largest %d x %d, %zu launches)\n",
-		        SVD_MAX_SWEEPS, descs.size(), mmax, nmax, groups.size());
-		// opt-in diagnostics: write the input matrix (row-major blocks) for offline analysis
-		if (const char* path = getenv("CTGPU_SVD_DUMP"))
+		std::vector<unsigned long long> h(descs.size() * 8);
+		CTG_CUDA(cudaMemcpyAsync(h.data(), ts->ptr, ts->bytes, cudaMemcpyDeviceToHost, c.stream()));
+		c.sync();
+		// the block that finished last sets the launch's duration
+		size_t crit = 0;
+		unsigned long long t0 = ~0ull, t1 = 0;
+		for (size_t b = 0; b < descs.size(); b++)
 		{
-			std::vector<double> host((size_t)am.nnz);
-			copy_to_host(c, a, host.data());
-			if (FILE* f = fopen(path, "wb"))
-			{
-				const i64 nb = (i64)descs.size();
-				fwrite(&nb, sizeof(i64), 1, f);
-				for (const SvdDesc& d : descs)
-				{
-					const i64 mn[2] = {d.m, d.n};
-					fwrite(mn, sizeof(i64), 2, f);
-					fwrite(host.data() + d.a_off, sizeof(double), (size_t)d.m * d.n, f);
-				}
-				fclose(f);
-			}
+			if (!h[8 * b]) continue;
+			t0 = std::min(t0, h[8 * b]);
+			if (h[8 * b + 3] > t1) { t1 = h[8 * b + 3]; crit = b; }
 		}
-		return -1;
+		if (t1 > 0)
+		{
+			c.svd_phase_ms[0] += 1e-6 * (double)(h[8 * crit + 1] - h[8 * crit]);
+			c.svd_phase_ms[1] += 1e-6 * (double)(h[8 * crit + 2] - h[8 * crit + 1]);
+			c.svd_phase_ms[2] += 1e-6 * (double)(h[8 * crit + 3] - h[8 * crit + 2]);
+			c.svd_phase_ms[3] += 1e-6 * (double)(t1 - t0);
+			for (int i = 0; i < 4; i++) c.svd_jacobi_cycles[i] += (double)h[8 * crit + 4 + i];
+		}
 	}
+	// the status reaches pinned host memory once the stream gets there (read by op_svd_finish)
+	CTG_CUDA(cudaMemcpyAsync(c.svd_status_host(), status.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream()));
+	pend.descs = descs;
+	pend.launches = groups.size();
 	return 0;
+}
+
+int op_svd_finish(Ctx& c, const SvdPending& pend)
+{
+	if (pend.descs.empty()) return 0;
+	const int* hst = c.svd_status_host();
+	c.svd_max_sweeps = std::max(c.svd_max_sweeps, hst[1]);
+	if (hst[0] == 0) return 0;
+	int mmax = 0, nmax = 0;
+	for (const SvdDesc& d : pend.descs) { mmax = std::max(mmax, d.m); nmax = std::max(nmax, d.n); }
+	fprintf(stderr, "ctgpu: block SVD did not converge within %d Jacobi sweeps (%zu blocks, largest %d x %d, %zu launches)\n",
+	        SVD_MAX_SWEEPS, pend.descs.size(), mmax, nmax, pend.launches);
+	// opt-in diagnostics: write the input matrix (row-major blocks) for offline analysis
+	if (const char* path = getenv("CTGPU_SVD_DUMP"))
+	{
+		std::vector<double> host((size_t)pend.a.m().nnz);
+		copy_to_host(c, pend.a, host.data());
+		if (FILE* f = fopen(path, "wb"))
+		{
+			const i64 nb = (i64)pend.descs.size();
+			fwrite(&nb, sizeof(i64), 1, f);
+			for (const SvdDesc& d : pend.descs)
+			{
+				const i64 mn[2] = {d.m, d.n};
+				fwrite(mn, sizeof(i64), 2, f);
+				fwrite(host.data() + d.a_off, sizeof(double), (size_t)d.m * d.n, f);
+			}
+			fclose(f);
+		}
+	}
+	return -1;
+}
+
+int op_svd(Ctx& c, const DTensor& a, SvdResult& res)
+{
+	SvdPending pend;
+	const int ret = op_svd_launch(c, a, res, pend);
+	if (ret < 0) return ret;
+	c.sync();
+	return op_svd_finish(c, pend);
 }
 
 int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q)

@@ -75,6 +75,7 @@ public:
 	// block until the stream is idle; recycles the staging arena
 	void sync();
 	DTensor empty(const Meta& m);
+	DTensor empty(const std::shared_ptr<const Meta>& m);   // shares the structure, no copy
 	DTensor zeros(const Meta& m);
 	// statistics
 	double gemm_flops = 0;       // algorithmic GEMM FLOPs issued
@@ -83,12 +84,22 @@ public:
 	int svd_full_reruns = 0;     // SVDs repeated at full resolution for the truncation decision
 	double host_plan_s = 0;      // host time spent lowering operations into descriptor lists
 	long plan_hits = 0, plan_misses = 0;
+	// with CTGPU_SVD_PHASES set: summed QR / Jacobi / output / launch time (ms) of the block that
+	// finished last in each block SVD
+	double svd_phase_ms[4] = {0, 0, 0, 0};
+	double svd_jacobi_cycles[4] = {0, 0, 0, 0};   // inner products, parameters, rotations, exchanges
 	// cache of lowered operations, keyed by operation and operand structures (DMRG revisits the
 	// same block structures every sweep once the bond dimensions have settled)
 	struct PlanCache* plans() { return plans_; }
 	// device flag raised by a tensor-core kernel whose bounded wait timed out (checked at sync)
 	int* tc_error();
 	int num_sms() const { return sms_; }
+	// pinned host memory for small device-to-host results read after a synchronisation
+	int* svd_status_host() { return (int*)pinned_; }
+	LanczosScalars* lanczos_host() { return (LanczosScalars*)((char*)pinned_ + 256); }
+	// n doubles of pinned host memory (contents valid until the next call); only call while no
+	// asynchronous copy into it is pending
+	double* pinned_doubles(size_t n);
 	// optional per-kernel-class timing with CUDA events on this stream (resolved at sync points)
 	bool profile = false;
 	KProf prof[K_NUM_CLASSES];
@@ -114,6 +125,9 @@ private:
 	cudaEvent_t join_ev_[NUM_AUX] = {};
 	cudaMemPool_t pool_ = nullptr;
 	char* staging_ = nullptr;
+	void* pinned_ = nullptr;                 // status words and Lanczos scalars
+	double* pinned_d_ = nullptr;
+	size_t pinned_d_cap_ = 0;
 	size_t staging_cap_ = 0, staging_used_ = 0;
 };
 
@@ -138,6 +152,9 @@ struct DotPlan {
 	const GemmTile* tiles[NUM_TILE_CLASSES] = {nullptr, nullptr, nullptr};
 	const GemmOut* outs = nullptr;
 	const GemmContrib* cons = nullptr;
+	const GemmSplit* splits = nullptr;   // tiles whose sum is split over several CTAs
+	int nsplits = 0;
+	DBufPtr work;                        // their partial sums
 	double flops = 0;
 	double flops_cls[NUM_TILE_CLASSES] = {0, 0, 0};
 	int precision = GEMM_FP64;
@@ -170,20 +187,31 @@ DTensor op_split(Ctx& c, const DTensor& t, int ax, const i64 nd[2], const int nd
 DTensor op_slice(Ctx& c, const DTensor& t, int ax, const std::vector<i64>& ind);
 // multiply along the leading (axrange 0) or trailing (1) axis by a device vector indexed by logical position
 DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange);
-// same entries, all axis directions reversed
-DTensor view_reversed(const DTensor& t);
+// same entries, all axis directions reversed (structure cached per context)
+DTensor view_reversed(Ctx& c, const DTensor& t);
 // cyclic partial trace of one leading with one trailing axis of logical dimension 1 (a relabelling)
 DTensor view_trace_unit(const DTensor& t);
 
 // block SVD (block_sparse_tensor_svd, block_sparse_tensor.c:2686-2848); singular values in a
-// device buffer indexed like the logical intermediate axis. Returns 0 or -1.
+// device buffer indexed like the logical intermediate axis.
 struct SvdResult {
 	DTensor u, vh;
 	DBufPtr s;
 	i64 ns = 0;
-	double max_tail = 0;     // largest per-block weight of directions left unresolved (see tol_hint)
 };
-int op_svd(Ctx& c, const DTensor& a, SvdResult& res, double tol_hint = 0.0);
+// what op_svd_finish needs to check a launched SVD
+struct SvdPending {
+	std::vector<SvdDesc> descs;
+	size_t launches = 0;
+	DTensor a;
+};
+// enqueue the SVD without waiting for it; its status reaches pinned host memory when the stream
+// gets there, so op_svd_finish may run only after a synchronisation of c's stream
+int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend);
+// 0, or -1 if a block did not converge (diagnostics on stderr)
+int op_svd_finish(Ctx& c, const SvdPending& pend);
+// launch, synchronise, finish. Returns 0 or -1.
+int op_svd(Ctx& c, const DTensor& a, SvdResult& res);
 
 // block RQ (block_sparse_tensor_rq, block_sparse_tensor.c:2544-2676). Returns 0 or -1.
 int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q);

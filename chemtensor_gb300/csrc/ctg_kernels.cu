@@ -10,7 +10,7 @@ namespace ctg {
 template <int BM, int BN, int BK, int TM, int TN>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const GemmContrib* __restrict__ cons,
-           const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C)
+           const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C, double* __restrict__ work)
 {
 	constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
 	__shared__ double As[BK][BM + 1];
@@ -25,12 +25,13 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
 #pragma unroll
 		for (int j = 0; j < TN; j++) acc[i][j] = 0.0;
 
-	for (int c = o.c0; c < o.c0 + o.nc; c++)
+	for (int c = tile.c0; c <= tile.c1; c++)
 	{
 		const GemmContrib g = cons[c];
 		const double* a = A + g.a_off;
 		const double* b = B + g.b_off;
-		for (int k0 = 0; k0 < g.k; k0 += BK)
+		const int kb = (c == tile.c0 ? tile.k0 : 0), ke = (c == tile.c1 ? tile.k1 : g.k);
+		for (int k0 = kb; k0 < ke; k0 += BK)
 		{
 			// A tile: BM x BK; the thread-to-element map follows the unit-stride index
 			if (g.sAk == 1)
@@ -39,7 +40,7 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
 				{
 					const int kk = e % BK, i = e / BK;
 					const int gi = tile.m0 + i, gk = k0 + kk;
-					As[kk][i] = (gi < o.m && gk < g.k) ? a[(i64)gi * g.sAm + gk] : 0.0;
+					As[kk][i] = (gi < o.m && gk < ke) ? a[(i64)gi * g.sAm + gk] : 0.0;
 				}
 			}
 			else
@@ -48,7 +49,7 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
 				{
 					const int i = e % BM, kk = e / BM;
 					const int gi = tile.m0 + i, gk = k0 + kk;
-					As[kk][i] = (gi < o.m && gk < g.k) ? a[(i64)gi * g.sAm + (i64)gk * g.sAk] : 0.0;
+					As[kk][i] = (gi < o.m && gk < ke) ? a[(i64)gi * g.sAm + (i64)gk * g.sAk] : 0.0;
 				}
 			}
 			// B tile: BK x BN
@@ -58,7 +59,7 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
 				{
 					const int j = e % BN, kk = e / BN;
 					const int gj = tile.n0 + j, gk = k0 + kk;
-					Bs[kk][j] = (gj < o.n && gk < g.k) ? b[(i64)gk * g.sBk + gj] : 0.0;
+					Bs[kk][j] = (gj < o.n && gk < ke) ? b[(i64)gk * g.sBk + gj] : 0.0;
 				}
 			}
 			else
@@ -67,11 +68,11 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
 				{
 					const int kk = e % BK, j = e / BK;
 					const int gj = tile.n0 + j, gk = k0 + kk;
-					Bs[kk][j] = (gj < o.n && gk < g.k) ? b[(i64)gk * g.sBk + (i64)gj * g.sBn] : 0.0;
+					Bs[kk][j] = (gj < o.n && gk < ke) ? b[(i64)gk * g.sBk + (i64)gj * g.sBn] : 0.0;
 				}
 			}
 			__syncthreads();
-			const int kmax = min(BK, g.k - k0);
+			const int kmax = min(BK, ke - k0);
 			for (int kk = 0; kk < kmax; kk++)
 			{
 				double av[TM], bv[TN];
@@ -86,6 +87,16 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
 			}
 			__syncthreads();
 		}
+	}
+	if (tile.part >= 0)
+	{
+		// partial sum of a split tile (full BM x BN, leading dimension BN)
+		double* w = work + tile.part;
+#pragma unroll
+		for (int i = 0; i < TM; i++)
+#pragma unroll
+			for (int j = 0; j < TN; j++) w[(ty + i * NTY) * BN + tx + j * NTX] = acc[i][j];
+		return;
 	}
 	double* cblk = C + o.c_off;
 #pragma unroll
@@ -102,18 +113,44 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
 	}
 }
 
+// sums the partial tiles of each split tile in order of the split index
+__global__ void __launch_bounds__(256)
+k_gemm_reduce(const GemmSplit* __restrict__ splits, const GemmOut* __restrict__ outs, const double* __restrict__ work,
+              double* __restrict__ C)
+{
+	const GemmSplit sp = splits[blockIdx.x];
+	const GemmOut o = outs[sp.out];
+	double* cblk = C + o.c_off;
+	for (int e = threadIdx.x; e < sp.rows * sp.cols; e += blockDim.x)
+	{
+		const int i = e / sp.cols, j = e - i * sp.cols;
+		const double* w = work + sp.part + (i64)i * sp.ld + j;
+		double acc = 0.0;
+		for (int p = 0; p < sp.nsplit; p++) acc += w[(i64)p * sp.stride];
+		cblk[(i64)(sp.m0 + i) * o.n + sp.n0 + j] = acc;
+	}
+}
+
+void launch_gemm_reduce(int nsplit, const GemmSplit* splits, const GemmOut* outs, const double* work, double* C,
+                        cudaStream_t st)
+{
+	if (nsplit <= 0) return;
+	k_gemm_reduce<<<nsplit, 256, 0, st>>>(splits, outs, work, C);
+	CTG_CUDA(cudaGetLastError());
+}
+
 int tile_rows(int cls) { return cls == TILE_L ? 64 : (cls == TILE_M ? 32 : 16); }
 int tile_cols(int cls) { return cls == TILE_L ? 64 : (cls == TILE_M ? 32 : 16); }
 
 void launch_gemm_f64(int cls, int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
-                     const double* A, const double* B, double* C, cudaStream_t st)
+                     const double* A, const double* B, double* C, double* work, cudaStream_t st)
 {
 	if (ntiles <= 0) return;
 	switch (cls)
 	{
-	case TILE_L: k_gemm_f64<64, 64, 16, 4, 4><<<ntiles, 256, 0, st>>>(tiles, outs, cons, A, B, C); break;
-	case TILE_M: k_gemm_f64<32, 32, 16, 4, 4><<<ntiles, 64, 0, st>>>(tiles, outs, cons, A, B, C); break;
-	default:     k_gemm_f64<16, 16, 16, 2, 2><<<ntiles, 64, 0, st>>>(tiles, outs, cons, A, B, C); break;
+	case TILE_L: k_gemm_f64<64, 64, 16, 4, 4><<<ntiles, 256, 0, st>>>(tiles, outs, cons, A, B, C, work); break;
+	case TILE_M: k_gemm_f64<32, 32, 16, 4, 4><<<ntiles, 64, 0, st>>>(tiles, outs, cons, A, B, C, work); break;
+	default:     k_gemm_f64<16, 16, 16, 2, 2><<<ntiles, 64, 0, st>>>(tiles, outs, cons, A, B, C, work); break;
 	}
 	CTG_CUDA(cudaGetLastError());
 }

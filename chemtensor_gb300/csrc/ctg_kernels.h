@@ -26,9 +26,23 @@ struct GemmContrib {
 	int sAm, sAk, sBk, sBn;
 };
 
+// One CTA's share of an output tile: the terms from (contribution c0, k = k0) up to (contribution c1,
+// k = k1 exclusive) of the tile's sum over its contributions and their inner index k, in order.
+// part < 0: the share is the whole sum and goes to C; otherwise the CTA writes its partial sum to
+// work[part + i * tile_cols + j] and a GemmSplit entry adds the partial sums in order.
 struct GemmTile {
 	int out;           // output block
 	int m0, n0;        // tile origin inside the output block
+	int c0, k0;
+	int c1, k1;        // c1 < c0: no terms (the tile is written as zeros)
+	i64 part;
+};
+
+// A tile whose sum is split over nsplit CTAs: C = sum over p < nsplit of the partial tile at
+// work[part + p * stride] (rows x cols used, leading dimension ld), added in order of p.
+struct GemmSplit {
+	int out, m0, n0, rows, cols, nsplit, ld, stride;
+	i64 part;
 };
 
 // tile classes (rows x cols of C per CTA)
@@ -37,7 +51,9 @@ int tile_rows(int cls);
 int tile_cols(int cls);
 
 void launch_gemm_f64(int cls, int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
-                     const double* A, const double* B, double* C, cudaStream_t st);
+                     const double* A, const double* B, double* C, double* work, cudaStream_t st);
+void launch_gemm_reduce(int nsplit, const GemmSplit* splits, const GemmOut* outs, const double* work, double* C,
+                        cudaStream_t st);
 
 // Same work lists on the tcgen05 tensor cores, split-BF16 (hi*hi + hi*lo + lo*hi, FP32
 // accumulation, FP64 in and out); tiles of tc_tile_rows() x tc_tile_cols(). *error becomes 1 if a
@@ -115,9 +131,14 @@ struct SvdLaunch {
 int svd_max_cluster(int device);
 // smallest configuration with at least 'want' CTAs (a power of two) that fits an m x n block
 SvdLaunch svd_launch_for(int m, int n, int want, int max_cluster);
-// SVDs of descs[first .. first + count), all with configuration g, on stream st
+// SVDs of descs[first .. first + count), all with configuration g, on stream st. With phase_ts
+// non-null (shared-memory path only), the first CTA of each block's cluster writes four
+// %globaltimer stamps (start, QR done, Jacobi done, outputs done) to phase_ts[8 block ..] and
+// its SM clock cycles spent in the Jacobi inner products, rotation parameters, rotations and
+// cluster exchanges to phase_ts[8 block + 4 ..].
 void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* descs, const double* a, double* u,
-                      double* s, double* vh, double* scratch, int* status, double* tail, cudaStream_t st);
+                      double* s, double* vh, double* scratch, int* status, double* tail, cudaStream_t st,
+                      unsigned long long* phase_ts = nullptr);
 
 // Householder RQ of a row-major m x n block: A = R Q with Q (k x n) orthonormal rows, R (m x k), k = min(m, n).
 // Scratch holds n*m + n*k + k doubles per block.

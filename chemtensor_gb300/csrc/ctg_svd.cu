@@ -71,26 +71,30 @@ __device__ __forceinline__ void round_robin_pair(int rnd, int pi, int np, int& p
 
 // Householder QR with column pivoting of W (M x N, column-major) inside one CTA, stopped at
 // the numerical rank; returns r. W keeps R in its upper triangle and the Householder vectors
-// below it; tau and perm receive the scalars and the column permutation.
-__device__ int qr_pivoted_cta(double* W, int M, int N, double* nrm, double* tau, int* perm, double rank_thresh2)
+// below it; tau and perm receive the scalars and the column permutation. The squared norms of
+// the trailing column parts are downdated after every step (nrm[j] -= R_kj^2) and recomputed
+// when cancellation has eaten more than sqrt(eps) of the last exactly computed value (ref), the
+// safeguard of LAPACK's xLAQP2.
+__device__ int qr_pivoted_cta(double* W, int M, int N, double* nrm, double* ref, double* tau, int* perm,
+                              double rank_thresh2)
 {
 	__shared__ double red[NWARPS];
 	__shared__ double sh_beta, sh_tau, sh_scale;
 	__shared__ int sh_piv, sh_stop;
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const double tol3z = sqrt(DBL_EPSILON);
+	for (int j = warp; j < N; j += NWARPS)
+	{
+		const double* wj = W + (i64)j * M;
+		double acc = 0;
+		for (int i = lane; i < M; i += 32) acc = fma(wj[i], wj[i], acc);
+		acc = warp_sum(acc);
+		if (lane == 0) nrm[j] = ref[j] = acc;
+	}
+	__syncthreads();
 	int r = 0;
 	for (int k = 0; k < N; k++)
 	{
-		// squared norms of the trailing parts of the remaining columns
-		for (int j = k + warp; j < N; j += NWARPS)
-		{
-			const double* wj = W + (i64)j * M;
-			double acc = 0;
-			for (int i = k + lane; i < M; i += 32) acc = fma(wj[i], wj[i], acc);
-			acc = warp_sum(acc);
-			if (lane == 0) nrm[j] = acc;
-		}
-		__syncthreads();
 		if (warp == 0)
 		{
 			double best = -1;
@@ -128,6 +132,12 @@ __device__ int qr_pivoted_cta(double* W, int M, int N, double* nrm, double* tau,
 				const int t = perm[k];
 				perm[k] = perm[p];
 				perm[p] = t;
+				double x = nrm[k];
+				nrm[k] = nrm[p];
+				nrm[p] = x;
+				x = ref[k];
+				ref[k] = ref[p];
+				ref[p] = x;
 			}
 		}
 		__syncthreads();
@@ -158,15 +168,31 @@ __device__ int qr_pivoted_cta(double* W, int M, int N, double* nrm, double* tau,
 		__syncthreads();
 		if (tid == 0) { wk[k] = sh_beta; tau[k] = tk; }
 		__syncthreads();
-		if (tk != 0.0)
+		for (int j = k + 1 + warp; j < N; j += NWARPS)
 		{
-			for (int j = k + 1 + warp; j < N; j += NWARPS)
+			double* wj = W + (i64)j * M;
+			if (tk != 0.0)
 			{
-				double* wj = W + (i64)j * M;
 				double acc = 0;
 				for (int i = k + lane; i < M; i += 32) acc = fma(i == k ? 1.0 : wk[i], wj[i], acc);
 				acc = warp_sum(acc) * tk;
 				for (int i = k + lane; i < M; i += 32) wj[i] -= acc * (i == k ? 1.0 : wk[i]);
+			}
+			// downdate the trailing norm by R_kj^2 (lane 0 holds row k of this column)
+			int recompute = 0;
+			if (lane == 0)
+			{
+				const double rkj = wj[k];
+				const double v = fmax(fma(-rkj, rkj, nrm[j]), 0.0);
+				nrm[j] = v;
+				recompute = v <= tol3z * ref[j];
+			}
+			if (__shfl_sync(0xffffffffu, recompute, 0))
+			{
+				double acc = 0;
+				for (int i = k + 1 + lane; i < M; i += 32) acc = fma(wj[i], wj[i], acc);
+				acc = warp_sum(acc);
+				if (lane == 0) nrm[j] = ref[j] = acc;
 			}
 		}
 		__syncthreads();
@@ -187,6 +213,13 @@ __device__ int qr_pivoted_cta(double* W, int M, int N, double* nrm, double* tau,
 // as in the cyclic one-sided Jacobi method; a round costs one cluster barrier instead of one per
 // pair set, and the column data never leaves the SMs.
 
+__device__ __forceinline__ unsigned long long globaltimer()
+{
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
 __device__ __forceinline__ float rcp_approx(float x)
 {
 	float y;
@@ -194,34 +227,98 @@ __device__ __forceinline__ float rcp_approx(float x)
 	return y;
 }
 
-// Jacobi rotation for the 2 x 2 Gram matrix [al ga; ga be] of a column pair: c, s with
-// x' = c x - s y, y' = s x + c y making x' and y' orthogonal. The tangent t of the smaller
-// rotation angle, t = sign(be - al) 2 ga / (|be - al| + sqrt((be - al)^2 + 4 ga^2)), is evaluated
-// in FP32 on operands scaled by a power of two (an FP64 division and square root cost over a
-// thousand cycles on GB300's FP64 pipe). The rotation is then built in FP64 from the half-angle
-// tangent tau = t / (1 + sqrt(1 + t^2)) in the Cayley form c = (1 - tau^2) / (1 + tau^2),
-// s = 2 tau / (1 + tau^2): orthogonal to FP64 rounding for any tau. The reciprocal of
-// q = 1 + tau^2 is an FP32 estimate d0 refined by one cubically convergent Newton step,
-// d = d0 (1 + e + e^2) with e = 1 - q d0. The angle is accurate to FP32 only: the rotation
-// leaves a cosine of about 1e-7 of the previous one, which a later sweep removes.
-__device__ __forceinline__ void rotation_params(double al, double be, double ga, double& c, double& s, float& t32)
+// FP32 mantissa in [1, 2) (truncated to 23 bits) and unbiased exponent of a finite normal double,
+// by integer operations: on GB300 a double -> float conversion costs as much as an FP64 FMA
+__device__ __forceinline__ float mant_exp(double x, int& e)
 {
+	const int hi = __double2hiint(x), lo = __double2loint(x);
+	e = ((hi >> 20) & 0x7ff) - 1023;
+	return __int_as_float(0x3f800000 | ((hi & 0x000fffff) << 3) | (int)((unsigned)lo >> 29));
+}
+
+// the double m * 2^e for a normal float m (exact), by integer operations
+__device__ __forceinline__ double make_double(float m, int e)
+{
+	const int fb = __float_as_int(m);
+	if ((fb & 0x7fffffff) == 0) return 0.0;
+	const int fe = ((fb >> 23) & 0xff) - 127 + e;
+	const int hi = (fb & (int)0x80000000) | ((fe + 1023) << 20) | ((fb & 0x007fffff) >> 3);
+	return __hiloint2double(hi, (fb & 0x7) << 29);
+}
+
+// 2^k as a float for -126 <= k <= 127
+__device__ __forceinline__ float pow2f(int k)
+{
+	return __int_as_float((k + 127) << 23);
+}
+
+// Jacobi rotation for the 2 x 2 Gram matrix [al ga; ga be] of a column pair (al, be > 0).
+// Returns false if the pair counts as orthogonal (cos^2 = ga^2 / (al be) <= tol2). Otherwise the
+// rotation angle theta (tan theta the smaller root of t^2 + 2 zeta t - 1 = 0, zeta = (be - al) /
+// (2 ga)) is found in FP32 on mantissas and integer exponents, and the rotation is returned as
+// tau = tan(theta / 2) and sn = sin theta = 2 tau / (1 + tau^2) in FP64, for the three-shear form
+// x1 = x - tau y, y' = y + sn x1, x' = x1 - tau y' (Paeth), which is a rotation up to FP64
+// rounding for any tau; t = tan theta (FP32 accuracy) updates the squared norms. Only the
+// difference be - al, the FP64 reciprocal of 1 + tau^2 (FP32 estimate, one cubically convergent
+// Newton step d0 (1 + e + e^2), e = 1 - q d0) and the products use the FP64 pipe: an FP64 division
+// or square root costs over a thousand cycles on GB300. The angle is accurate to FP32 only: the
+// rotation leaves a cosine of about 1e-7 of the previous one, which a later sweep removes.
+__device__ __forceinline__ bool rotation_params(double al, double be, double ga, float tol2, double& tau, double& sn,
+                                                double& t)
+{
+	if (ga == 0.0) return false;
+	int ea, eb, eg;
+	const float ma = mant_exp(al, ea), mb = mant_exp(be, eb), mg = mant_exp(ga, eg);
+	const int k2 = 2 * eg - ea - eb;
+	if (k2 < -120) return false;
+	if (k2 <= 0 && (mg * mg) / (ma * mb) * pow2f(k2) <= tol2) return false;
 	const double dl = be - al;
-	const double mx = fmax(fabs(dl), 2.0 * fabs(ga));
-	int ex = (__double2hiint(mx) >> 20) & 0x7ff;      // biased exponent of mx
-	ex = ex < 1 ? 1 : (ex > 2045 ? 2045 : ex);
-	const double sc = __hiloint2double((2046 - ex) << 20, 0);   // 2^(1023 - ex): mx * sc in [1, 2)
-	const float ds = (float)(dl * sc), gs = (float)(ga * sc);
-	const float h = sqrtf(fmaf(ds, ds, 4.0f * gs * gs));
-	t32 = (2.0f * gs) * copysignf(1.0f, ds) / (fabsf(ds) + h);
-	const float tau32 = t32 / (1.0f + sqrtf(fmaf(t32, t32, 1.0f)));
-	const double tau = (double)tau32;
+	const bool neg = (dl < 0.0) != (ga < 0.0);
+	float tm, taum;
+	int te = 0;
+	if (dl == 0.0)
+	{
+		tm = 1.0f;
+		taum = 0.41421356f;
+	}
+	else
+	{
+		int ed;
+		const float md = mant_exp(dl, ed);
+		const int k = ed - eg - 1;                 // |zeta| = (md / mg) 2^k
+		if (k >= 40)
+		{
+			// tan theta ~ 1 / (2 |zeta|), tan(theta / 2) ~ tan theta / 2
+			tm = 0.5f * mg / md;
+			te = -k;
+			taum = 0.5f * tm;
+		}
+		else if (k <= -40)
+		{
+			tm = 1.0f;
+			taum = 0.41421356f;
+		}
+		else
+		{
+			const float z = (md / mg) * pow2f(k);
+			tm = 1.0f / (z + sqrtf(fmaf(z, z, 1.0f)));
+			taum = tm / (1.0f + sqrtf(fmaf(tm, tm, 1.0f)));
+		}
+	}
+	if (neg)
+	{
+		tm = -tm;
+		taum = -taum;
+	}
+	tau = make_double(taum, te);
+	t = make_double(tm, te);
 	const double q = fma(tau, tau, 1.0);
-	const double d0 = (double)rcp_approx((float)q);
+	int eq;
+	const double d0 = make_double(rcp_approx(mant_exp(q, eq)), -eq);
 	const double e = fma(-q, d0, 1.0);
-	const double d = fma(d0, fma(e, e, e), d0);
-	c = fma(-tau, tau, 1.0) * d;
-	s = (2.0 * tau) * d;
+	const double w = fma(d0, fma(e, e, e), d0);
+	sn = make_double(taum + taum, te) * w;
+	return sn != 0.0;
 }
 
 // groups held by CTA pi in round rho (circle method over nm + 1 groups; group nm stays with CTA 0)
@@ -286,9 +383,11 @@ __device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int
 	return k < cA && cq < cB;
 }
 
-__device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, int cB, int npad, double tol2, const StepBuf& sb)
+__device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, int cB, int npad, float tol2, const StepBuf& sb,
+                            long long* cyc)
 {
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const long long c0 = cyc ? clock64() : 0;
 	const int np = mode == 0 ? npad : t.bs;
 	// 1. inner products, one warp per pair
 	for (int k = warp; k < np; k += NWARPS)
@@ -303,63 +402,64 @@ __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, 
 		if (lane == 0) sb.gam[k] = g;
 	}
 	__syncthreads();
+	const long long c1 = cyc ? clock64() : 0;
 	// 2. rotations, one lane per pair; rotate while the cosine exceeds tol
 	if (warp == 0 && lane < np)
 	{
 		int sp, cp, sq, cq;
 		int rot = 0;
-		double c = 1.0, s = 0.0;
+		double tau = 0.0, sn = 0.0;
 		if (step_pair(t, mode, step, lane, cA, cB, npad, sp, cp, sq, cq))
 		{
 			double* np_ = t.nrm(buf, sp) + cp;
 			double* nq_ = t.nrm(buf, sq) + cq;
 			const double al = *np_, be = *nq_, ga = sb.gam[lane];
-			if (ga != 0.0 && ga * ga > tol2 * al * be)
+			double tn;
+			if (rotation_params(al, be, ga, tol2, tau, sn, tn))
 			{
-				float t32;
-				rotation_params(al, be, ga, c, s, t32);
-				if (s != 0.0)
-				{
-					rot = 1;
-					*np_ = al - (double)t32 * ga;
-					*nq_ = be + (double)t32 * ga;
-					*sb.local_rot = 1;
-				}
+				rot = 1;
+				*np_ = fma(-tn, ga, al);
+				*nq_ = fma(tn, ga, be);
+				*sb.local_rot = 1;
 			}
 		}
-		sb.csc[lane] = c;
-		sb.css[lane] = s;
-		sb.rotk[lane] = rot;
+		sb.csc[lane] = tau;
+		sb.css[lane] = sn;
+		// compact list of the rotating pairs, so that the work items below are spread evenly
+		const unsigned mask = __ballot_sync(np >= 32 ? 0xffffffffu : ((1u << np) - 1u), rot);
+		if (rot) sb.rotk[__popc(mask & ((1u << lane) - 1u))] = lane;
+		if (lane == 0) sb.rotk[SVD_STEP_PAIRS] = __popc(mask);
 	}
 	__syncthreads();
-	// 3. apply: work items of 32 consecutive entries of one pair's T or V columns
-	const int segT = (t.N + 31) >> 5, nseg = segT + ((t.r + 31) >> 5);
-	for (int it = warp; it < np * nseg; it += NWARPS)
+	const long long c2 = cyc ? clock64() : 0;
+	// 3. apply: work items of 32 consecutive entries of one rotating pair's column record
+	// (T entries 0 .. N-1 followed by V entries N .. N+r-1)
+	const int len = t.N + t.r, nseg = (len + 31) >> 5;
+	const int nrot = sb.rotk[SVD_STEP_PAIRS];
+	for (int it = warp; it < nrot * nseg; it += NWARPS)
 	{
-		const int k = it / nseg, g = it - k * nseg;
-		if (!sb.rotk[k]) continue;
+		const int j = it / nseg, g = it - j * nseg;
+		const int i = g * 32 + lane;
+		if (i >= len) continue;
+		const int k = sb.rotk[j];
 		int sp, cp, sq, cq;
 		step_pair(t, mode, step, k, cA, cB, npad, sp, cp, sq, cq);
-		int i;
-		if (g < segT)
-		{
-			i = g * 32 + lane;
-			if (i >= t.N) continue;
-		}
-		else
-		{
-			i = (g - segT) * 32 + lane;
-			if (i >= t.r) continue;
-			i += t.N;
-		}
 		double* x = t.col(buf, sp, cp);
 		double* y = t.col(buf, sq, cq);
-		const double c = sb.csc[k], s = sb.css[k];
-		const double xv = x[i], yv = y[i];
-		x[i] = c * xv - s * yv;
-		y[i] = s * xv + c * yv;
+		const double tau = sb.csc[k], sn = sb.css[k];
+		const double x1 = fma(-tau, y[i], x[i]);
+		const double y1 = fma(sn, x1, y[i]);
+		x[i] = fma(-tau, y1, x1);
+		y[i] = y1;
 	}
 	__syncthreads();
+	if (cyc)
+	{
+		const long long c3 = clock64();
+		cyc[0] += c1 - c0;
+		cyc[1] += c2 - c1;
+		cyc[2] += c3 - c2;
+	}
 }
 
 struct SvdScratch {
@@ -387,7 +487,7 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 __global__ void __launch_bounds__(SVD_THREADS)
 k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
            double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
-           double* __restrict__ tail, int cl)
+           double* __restrict__ tail, int cl, int smem_bytes, unsigned long long* __restrict__ phase_ts)
 {
 	extern __shared__ __align__(16) double smem[];
 	cg::cluster_group cluster = cg::this_cluster();
@@ -402,6 +502,8 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	const double* ab = a + d.a_off;
 
 	for (int e = rank * SVD_THREADS + tid; e < SVD_MAX_SWEEPS; e += cl * SVD_THREADS) xs.flags[e] = 0;
+	const bool stamp = phase_ts && rank == 0 && tid == 0;
+	if (stamp) phase_ts[8 * blk] = globaltimer();
 
 	// ---- 1. pivoted QR on the cluster's first CTA, of B scaled to a Frobenius norm in [1/2, 1) ----
 	if (rank == 0)
@@ -420,13 +522,18 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 		int ex = 0;
 		if (total > 0) frexp(sqrt(total), &ex);
 		const double sc = ldexp(1.0, -ex);
+		// the factorisation runs in shared memory when the block fits, then W goes to global memory
+		const bool in_smem = (i64)M * N * 8 <= (i64)smem_bytes;
+		double* Wq = in_smem ? smem : xs.W;
 		for (i64 e = tid; e < (i64)M * N; e += SVD_THREADS)
 		{
 			const i64 col = e / M, row = e % M;
-			xs.W[e] = sc * (tall ? ab[row * n + col] : ab[col * n + row]);
+			Wq[e] = sc * (tall ? ab[row * n + col] : ab[col * n + row]);
 		}
 		__syncthreads();
-		const int rr = qr_pivoted_cta(xs.W, M, N, xs.nrm, xs.tau, xs.perm, DBL_EPSILON * DBL_EPSILON * total * sc * sc);
+		const int rr = qr_pivoted_cta(Wq, M, N, xs.nrm, xs.sig, xs.tau, xs.perm, DBL_EPSILON * DBL_EPSILON * total * sc * sc);
+		if (in_smem)
+			for (i64 e = tid; e < (i64)M * N; e += SVD_THREADS) xs.W[e] = Wq[e];
 		if (tid == 0)
 		{
 			xs.misc[0] = (double)rr;
@@ -436,6 +543,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	}
 	cluster.sync();
 	const int r = (int)__ldcg(xs.misc);
+	if (stamp) phase_ts[8 * blk + 1] = globaltimer();
 
 	// ---- 2. one-sided Jacobi on R^T (N x r), block-pair tournament over the cluster ----
 	Tour t;
@@ -452,7 +560,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	sb.csc = sb.gam + SVD_STEP_PAIRS;
 	sb.css = sb.csc + SVD_STEP_PAIRS;
 	sb.rotk = (int*)(sb.css + SVD_STEP_PAIRS);
-	sb.local_rot = sb.rotk + SVD_STEP_PAIRS;
+	sb.local_rot = sb.rotk + SVD_STEP_PAIRS + 1;
 
 	int A, B;
 	round_groups(0, rank, t.nm, A, B);
@@ -473,7 +581,11 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	}
 	__syncthreads();
 
-	const double tol = (double)N * DBL_EPSILON, tol2 = tol * tol;
+	const float tol2 = (float)((double)N * DBL_EPSILON * (double)N * DBL_EPSILON);
+	long long cyc_acc[4] = {0, 0, 0, 0};               // dots, rotation parameters, rotations, exchanges
+	// counted on the second CTA: the first one holds the last column group, often short or empty
+	const bool count = phase_ts && tid == 0 && rank == (cl > 1 ? 1 : 0);
+	long long* cyc = count ? cyc_acc : nullptr;
 	int buf = 0, sweep = 0;
 	bool converged = r <= 1;
 	for (; sweep < SVD_MAX_SWEEPS && !converged; sweep++)
@@ -501,11 +613,12 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			if (rho == 0)
 			{
 				const int npad = t.bs + (t.bs & 1);
-				for (int st = 0; st < npad - 1; st++) jacobi_step(t, buf, 0, st, cA, cB, npad, tol2, sb);
+				for (int st = 0; st < npad - 1; st++) jacobi_step(t, buf, 0, st, cA, cB, npad, tol2, sb, cyc);
 			}
-			for (int st = 0; st < t.bs; st++) jacobi_step(t, buf, 1, st, cA, cB, 0, tol2, sb);
+			for (int st = 0; st < t.bs; st++) jacobi_step(t, buf, 1, st, cA, cB, 0, tol2, sb, cyc);
 			if (cl > 1)
 			{
+				const long long cx = cyc ? clock64() : 0;
 				// jacobi_step ended with a CTA barrier: this round's rotations are complete
 				if (tid == 0 && *sb.local_rot) atomicOr(xs.flags + sweep, 1);
 				const int rho1 = (rho + 1) % t.nm;
@@ -523,6 +636,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 				}
 				cluster.sync();
 				buf ^= 1;
+				if (cyc) cyc[3] += clock64() - cx;
 			}
 		}
 		if (cl > 1) converged = __ldcg(xs.flags + sweep) == 0;
@@ -562,6 +676,9 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 		if (r < N) atomicAdd(tail + blk, (double)(N - r) * DBL_EPSILON * DBL_EPSILON * __ldcg(xs.misc + 1));
 	}
 	cluster.sync();
+	if (stamp) phase_ts[8 * blk + 2] = globaltimer();
+	if (count)
+		for (int i = 0; i < 4; i++) phase_ts[8 * blk + 4 + i] = (unsigned long long)cyc_acc[i];
 
 	// ---- 3. outputs: L = Q V (M x r) by the r reflectors applied to [V_c; 0], Rf = P T Sigma^-1 ----
 	const double unscale = __ldcg(xs.misc + 2);
@@ -606,6 +723,11 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			else u[d.u_off + (i64)pj * kk + pos] = x;               // u: m x k
 		}
 		__syncwarp();
+	}
+	if (phase_ts)
+	{
+		cluster.sync();
+		if (stamp) phase_ts[8 * blk + 3] = globaltimer();
 	}
 }
 
@@ -658,7 +780,7 @@ k_svd_global(const SvdDesc* __restrict__ descs, int first, const double* __restr
 		for (int j = tid; j < N; j += SVD_THREADS) perm[j] = j;
 		const double total = block_sum(part, red);
 		__syncthreads();
-		const int r = qr_pivoted_cta(W, M, N, nrm, tau, perm, DBL_EPSILON * DBL_EPSILON * total);
+		const int r = qr_pivoted_cta(W, M, N, nrm, sig, tau, perm, DBL_EPSILON * DBL_EPSILON * total);
 		if (tid == 0)
 		{
 			misc[0] = (double)r;
@@ -949,9 +1071,12 @@ i64 svd_scratch_doubles(int m, int n)
 static i64 tour_smem_bytes(int M, int N, int cl)
 {
 	const i64 nblk = 2 * cl, bsmax = (N + nblk - 1) / nblk;
-	const i64 jac = 4 * bsmax * 2 * N + 4 * bsmax + 3 * SVD_STEP_PAIRS + SVD_STEP_PAIRS / 2 + 8;
+	const i64 jac = 4 * bsmax * 2 * N + 4 * bsmax + 3 * SVD_STEP_PAIRS + SVD_STEP_PAIRS / 2 + 16;
 	const i64 out = (i64)NWARPS * M;
-	return 8 * (jac > out ? jac : out);
+	i64 need = jac > out ? jac : out;
+	// pivoted QR staged in shared memory when the whole block fits
+	if ((i64)M * N * 8 <= SVD_SMEM_LIMIT && (i64)M * N > need) need = (i64)M * N;
+	return 8 * need;
 }
 
 int svd_max_cluster(int device)
@@ -1009,7 +1134,8 @@ SvdLaunch svd_launch_for(int m, int n, int want, int max_cluster)
 }
 
 void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* descs, const double* a, double* u,
-                      double* s, double* vh, double* scratch, int* status, double* tail, cudaStream_t st)
+                      double* s, double* vh, double* scratch, int* status, double* tail, cudaStream_t st,
+                      unsigned long long* phase_ts)
 {
 	if (count <= 0) return;
 	cudaLaunchConfig_t cfg = {};
@@ -1038,7 +1164,8 @@ void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* d
 		CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
 		attr_set[dev] = true;
 	}
-	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, tail, g.cluster));
+	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, tail, g.cluster, g.smem,
+	                             phase_ts));
 }
 
 }  // namespace ctg

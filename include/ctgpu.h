@@ -58,7 +58,7 @@ struct ctgpu_stats
 	double sweep_s;           /* all sweeps */
 	double lanczos_ms;        /* device time in the Lanczos eigensolver */
 	double split_ms;          /* time in the SVD split, including the truncation decision */
-	double env_ms;            /* device time in the environment updates (right-to-left pass) */
+	double env_ms;            /* device time in the environment updates */
 	double matvec_flops;      /* algorithmic GEMM FLOPs of all local-Hamiltonian applications */
 	double total_gemm_flops;  /* algorithmic GEMM FLOPs of the whole call */
 	long   matvecs;           /* local-Hamiltonian applications */
