@@ -15,6 +15,8 @@
 
 namespace ctg {
 
+extern double g_plan_stage[12];
+
 namespace {
 
 double now_s()
@@ -482,12 +484,26 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	const std::vector<q32> qsite(psi->qsite, psi->qsite + psi->d);
 
 	Ctx& c = context_for_device(opt.device);
+	{
+		// working set of a sweep: a few hundred times the largest two-site tensor at max_vdim
+		// (MPS, environments, Lanczos basis, local-Hamiltonian intermediates, SVD workspace);
+		// reserved up front so that the memory pool does not grow during the sweeps
+		size_t free_b = 0, total_b = 0;
+		CTG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+		const double two_site = 8.0 * (double)max_vdim * (double)max_vdim * (double)psi->d * (double)psi->d;
+		const double want = std::min(0.25 * (double)free_b, std::max(256.0 * 1048576.0, 400.0 * two_site));
+		c.reserve((size_t)want);
+	}
 	c.gemm_flops = 0;
 	c.kernel_launches = 0;
 	c.profile = false;
 	c.prof_reset();
 	c.svd_max_sweeps = 0;
 	c.host_plan_s = 0;
+	c.host_alloc_s = 0;
+	c.host_upload_s = 0;
+	c.host_plan_cpu_s = 0;
+	for (double& x : g_plan_stage) x = 0;
 	c.plan_hits = 0;
 	c.plan_misses = 0;
 	for (double& x : c.svd_phase_ms) x = 0;
@@ -631,6 +647,12 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	{
 		fprintf(stderr, "ctgpu: host ms per sweep: Lanczos enqueue %.1f, split (incl. wait) %.1f, environment enqueue %.1f\n",
 		        1e3 * host_t[0] / st->sweeps, 1e3 * host_t[1] / st->sweeps, 1e3 * host_t[2] / st->sweeps);
+		fprintf(stderr, "ctgpu: host ms per sweep: planning %.1f (thread CPU %.1f; device allocation %.1f, descriptor upload %.1f)\n",
+		        1e3 * c.host_plan_s / st->sweeps, 1e3 * c.host_plan_cpu_s / st->sweeps, 1e3 * c.host_alloc_s / st->sweeps,
+		        1e3 * c.host_upload_s / st->sweeps);
+		fprintf(stderr, "ctgpu: plan stages ms per sweep:");
+		for (int k = 0; k < 12; k++) fprintf(stderr, " %.1f", 1e3 * g_plan_stage[k] / st->sweeps);
+		fprintf(stderr, "\n");
 		fprintf(stderr, "ctgpu: host ms per sweep in Lanczos: local-H setup %.1f, matvec enqueue %.1f, vector kernels %.1f\n",
 		        1e3 * g_host_detail[0] / st->sweeps, 1e3 * g_host_detail[1] / st->sweeps, 1e3 * g_host_detail[2] / st->sweeps);
 	}

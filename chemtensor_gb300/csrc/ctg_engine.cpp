@@ -7,6 +7,7 @@
 #include <functional>
 #include <memory>
 #include <cstring>
+#include <ctime>
 
 namespace ctg {
 
@@ -117,11 +118,24 @@ static double host_seconds()
 	return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-PlanTimer::PlanTimer(Ctx& ctx) : c(ctx), t0(host_seconds()) {}
+// host time of plan-building stages (diagnostics): 0 dot meta, 1 dot enumeration, 2 split-K,
+// 3 dot packing, 4 transpose meta, 5 transpose loop, 6 flatten meta, 7 flatten loop, 8 split meta,
+// 9 split loop, 10 slice, 11 other
+double g_plan_stage[12];
+
+static double thread_cpu_seconds()
+{
+	timespec ts;
+	clock_gettime(CLOCK_THREAD_CPUTIME_ID, &ts);
+	return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+PlanTimer::PlanTimer(Ctx& ctx) : c(ctx), t0(host_seconds()), cpu0(thread_cpu_seconds()) {}
 
 PlanTimer::~PlanTimer()
 {
 	c.host_plan_s += host_seconds() - t0;
+	c.host_plan_cpu_s += thread_cpu_seconds() - cpu0;
 }
 
 static_assert(256 + sizeof(LanczosScalars) <= 4096, "pinned result slots overlap");
@@ -195,15 +209,26 @@ Ctx& context_for_device(int device)
 
 void* Ctx::alloc(size_t bytes)
 {
+	const double t0 = host_seconds();
 	void* p = nullptr;
 	if (bytes == 0) bytes = 16;
 	CTG_CUDA(cudaMallocFromPoolAsync(&p, (bytes + 255) & ~(size_t)255, pool_, st_));
+	host_alloc_s += host_seconds() - t0;
 	return p;
 }
 
 void Ctx::free(void* p)
 {
 	cudaFreeAsync(p, st_);
+}
+
+void Ctx::reserve(size_t bytes)
+{
+	if (bytes <= reserved_) return;
+	void* p = alloc(bytes);
+	free(p);
+	sync();
+	reserved_ = bytes;
 }
 
 void Ctx::sync()
@@ -300,6 +325,7 @@ KScope::~KScope()
 
 DBufPtr Ctx::upload(const void* host, size_t bytes)
 {
+	struct T { Ctx* c; double t0; ~T() { c->host_upload_s += host_seconds() - t0; } } timer{this, host_seconds()};
 	auto b = std::make_shared<DBuf>(this, bytes);
 	size_t done = 0;
 	while (done < bytes)
@@ -413,8 +439,11 @@ int tile_class(int m, int n)
 static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
 {
 	DotPlan p;
+	double ts0 = host_seconds();
 	auto out = std::make_shared<Meta>(dot_result_meta(s, axs, t, axt, nmult));
 	p.out = out;
+	g_plan_stage[0] += host_seconds() - ts0;
+	ts0 = host_seconds();
 	const Meta& r = *out;
 	const int shift_s = (axs == AX_LEADING ? 0 : s.ndim - nmult);
 	const int shift_t = (axt == AX_LEADING ? 0 : t.ndim - nmult);
@@ -527,6 +556,8 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	// tiles than SMs leaves most of the FP64 pipes idle. Tiles whose work exceeds a fair share of
 	// the whole product are cut into shares of consecutive 16-wide k chunks, one CTA each; their
 	// partial sums are added in a fixed order (deterministic) by k_gemm_reduce.
+	g_plan_stage[1] += host_seconds() - ts0;
+	ts0 = host_seconds();
 	std::vector<GemmSplit> splits;
 	i64 wsz = 0;
 	if (precision != GEMM_BF16X3)
@@ -588,6 +619,8 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 			tiles[k].swap(kept);
 		}
 	}
+	g_plan_stage[2] += host_seconds() - ts0;
+	ts0 = host_seconds();
 	p.precision = precision;
 	if (precision == GEMM_BF16X3)
 	{
@@ -611,6 +644,7 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 		p.tiles[k] = at<GemmTile>(p.desc, o_tiles[k]);
 	}
 	p.flops = flops;
+	g_plan_stage[3] += host_seconds() - ts0;
 	return p;
 }
 
@@ -702,7 +736,10 @@ static CopyPlan finish_rows(Ctx& c, std::shared_ptr<Meta> out, const std::vector
 // block_sparse_tensor_transpose (block_sparse_tensor.c:785-870)
 static CopyPlan build_transpose_plan(Ctx& c, const Meta& t, const int* perm)
 {
+	double ts0 = host_seconds();
 	auto out = std::make_shared<Meta>(transpose_meta(t, perm));
+	g_plan_stage[4] += host_seconds() - ts0;
+	ts0 = host_seconds();
 	const Meta& r = *out;
 	CTG_CHECK(t.ndim <= 6, "transpose: at most 6 axes");
 	std::vector<PermDesc> descs;
@@ -730,6 +767,7 @@ static CopyPlan build_transpose_plan(Ctx& c, const Meta& t, const int* perm)
 		add_chunks(chunks, (int)descs.size(), d.n);
 		descs.push_back(d);
 	}
+	g_plan_stage[5] += host_seconds() - ts0;
 	return finish_perm(c, out, descs, chunks);
 }
 
@@ -737,7 +775,10 @@ static CopyPlan build_transpose_plan(Ctx& c, const Meta& t, const int* perm)
 // scatters its rows (j0, j1) into the fused rows of one target block
 static CopyPlan build_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
 {
+	double ts0 = host_seconds();
 	auto out = std::make_shared<Meta>(flatten_meta(t, ax, newdir));
+	g_plan_stage[6] += host_seconds() - ts0;
+	ts0 = host_seconds();
 	const Meta& r = *out;
 	const i64 d1 = t.dim[ax + 1];
 	std::vector<RowDesc> descs;
@@ -772,6 +813,7 @@ static CopyPlan build_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
 		descs.push_back(d);
 	}
 	check_rows(descs, maps, t.nnz, r.nnz);
+	g_plan_stage[7] += host_seconds() - ts0;
 	return finish_rows(c, out, descs, chunks, maps);
 }
 
@@ -779,7 +821,10 @@ static CopyPlan build_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
 // gathers its rows (j0, j1) from the fused rows of one source block
 static CopyPlan build_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
 {
+	double ts0 = host_seconds();
 	auto out = std::make_shared<Meta>(split_meta(t, ax, nd, ndir, nq));
+	g_plan_stage[8] += host_seconds() - ts0;
+	ts0 = host_seconds();
 	const Meta& r = *out;
 	std::vector<RowDesc> descs;
 	std::vector<Chunk> chunks;
@@ -813,6 +858,7 @@ static CopyPlan build_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2],
 		descs.push_back(d);
 	}
 	check_rows(descs, maps, t.nnz, r.nnz);
+	g_plan_stage[9] += host_seconds() - ts0;
 	return finish_rows(c, out, descs, chunks, maps);
 }
 

@@ -70,6 +70,9 @@ public:
 	void join(int n);
 	void* alloc(size_t bytes);
 	void free(void* p);
+	// make the private pool hold at least this many bytes, so that later allocations are served
+	// without growing it (growing maps new physical memory, which costs milliseconds)
+	void reserve(size_t bytes);
 	// copy host bytes to a new device buffer (through pinned staging, asynchronous)
 	DBufPtr upload(const void* host, size_t bytes);
 	// block until the stream is idle; recycles the staging arena
@@ -83,6 +86,8 @@ public:
 	int svd_max_sweeps = 0;      // largest Jacobi sweep count of any block SVD
 	int svd_full_reruns = 0;     // SVDs repeated at full resolution for the truncation decision
 	double host_plan_s = 0;      // host time spent lowering operations into descriptor lists
+	double host_alloc_s = 0, host_upload_s = 0;   // host time in device allocation / descriptor uploads
+	double host_plan_cpu_s = 0;                   // thread CPU time of the planning
 	long plan_hits = 0, plan_misses = 0;
 	// with CTGPU_SVD_PHASES set: summed QR / Jacobi / output / launch time (ms) of the block that
 	// finished last in each block SVD
@@ -129,12 +134,13 @@ private:
 	double* pinned_d_ = nullptr;
 	size_t pinned_d_cap_ = 0;
 	size_t staging_cap_ = 0, staging_used_ = 0;
+	size_t reserved_ = 0;
 };
 
 // Adds the host time of its scope to Ctx::host_plan_s.
 struct PlanTimer {
 	Ctx& c;
-	double t0;
+	double t0, cpu0;
 	explicit PlanTimer(Ctx& ctx);
 	~PlanTimer();
 };

@@ -33,8 +33,8 @@ int Meta::find(const i64* idx) const
 		if (idx[i] < 0 || idx[i] >= nb[i]) return -1;
 	const i64 k = linear(idx);
 	if (!lut.empty()) return lut[(size_t)k];
-	auto it = lut_map.find(k);
-	return it == lut_map.end() ? -1 : it->second;
+	auto it = std::lower_bound(lin.begin(), lin.end(), k);
+	return (it == lin.end() || *it != k) ? -1 : (int)(it - lin.begin());
 }
 
 int Meta::find_q(int ax, q32 q) const
@@ -107,49 +107,85 @@ Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::
 			m.pos[a][j] = m.bd[a][b]++;
 		}
 	}
-	// enumerate allowed blocks in row-major order: for every prefix over the first
-	// ndim-1 axes, at most one quantum number of the last axis makes the sum vanish
+	// enumerate allowed blocks in row-major order: for every prefix over the first ndim-1 axes
+	// (an odometer with incrementally updated partial quantum-number sums), at most one
+	// quantum number of the last axis makes the sum vanish (looked up in a table over its range)
 	const int last = ndim - 1;
+	const std::vector<q32>& qlast = m.qb[last];
+	const long long qlo = qlast.front(), qhi = qlast.back();
+	std::vector<int> qtab;
+	const bool table = qhi - qlo < (1 << 20);
+	if (table)
+	{
+		qtab.assign((size_t)(qhi - qlo + 1), -1);
+		for (size_t j = 0; j < qlast.size(); j++) qtab[(size_t)(qlast[j] - qlo)] = (int)j;
+	}
 	i64 nprefix = 1;
 	for (int a = 0; a < last; a++) nprefix *= m.nb[a];
+	const size_t cap = (size_t)std::min<i64>(nprefix, (i64)1 << 22);
+	m.bidx.resize(cap * ndim);
+	m.bdim.resize(cap * ndim);
+	m.boff.resize(cap);
+	m.lin.resize(cap);
+	i64 off = 0;
 	std::vector<i64> idx(ndim, 0);
+	std::vector<long long> partial(ndim, 0);   // partial[a]: sum over axes < a
+	for (int a = 0; a < last; a++) partial[a + 1] = partial[a] + (long long)dir[a] * m.qb[a][0];
 	for (i64 p = 0; p < nprefix; p++)
 	{
-		i64 r = p;
-		long long qs = 0;
-		for (int a = last - 1; a >= 0; a--) { idx[a] = r % m.nb[a]; r /= m.nb[a]; }
-		for (int a = 0; a < last; a++) qs += (long long)dir[a] * m.qb[a][idx[a]];
-		const long long qneed = -(long long)dir[last] * qs;
-		if (qneed < INT32_MIN || qneed > INT32_MAX) continue;
-		const int j = m.find_q(last, (q32)qneed);
+		if (p > 0)
+		{
+			int a = last - 1;
+			while (++idx[a] == m.nb[a])
+			{
+				idx[a] = 0;
+				a--;
+			}
+			for (int i = a; i < last; i++) partial[i + 1] = partial[i] + (long long)dir[i] * m.qb[i][idx[i]];
+		}
+		const long long qneed = -(long long)dir[last] * partial[last];
+		int j;
+		if (table) j = (qneed < qlo || qneed > qhi) ? -1 : qtab[(size_t)(qneed - qlo)];
+		else j = (qneed < INT32_MIN || qneed > INT32_MAX) ? -1 : m.find_q(last, (q32)qneed);
 		if (j < 0) continue;
 		idx[last] = j;
+		if ((size_t)m.nblocks == m.boff.size())
+		{
+			m.bidx.resize(m.bidx.size() * 2);
+			m.bdim.resize(m.bdim.size() * 2);
+			m.boff.resize(m.boff.size() * 2);
+			m.lin.resize(m.lin.size() * 2);
+		}
+		i64* bi = &m.bidx[(size_t)m.nblocks * ndim];
+		i64* bdm = &m.bdim[(size_t)m.nblocks * ndim];
+		i64 size = 1;
 		for (int a = 0; a < ndim; a++)
 		{
-			m.bidx.push_back(idx[a]);
-			m.bdim.push_back(m.bd[a][idx[a]]);
+			bi[a] = idx[a];
+			bdm[a] = m.bd[a][idx[a]];
+			size *= bdm[a];
 		}
+		m.boff[(size_t)m.nblocks] = off;
+		m.lin[(size_t)m.nblocks] = p * m.nb[last] + j;
+		off += size;
 		m.nblocks++;
 	}
-	m.boff.resize(m.nblocks);
-	i64 off = 0;
-	for (int b = 0; b < m.nblocks; b++) { m.boff[b] = off; off += m.block_size(b); }
+	m.bidx.resize((size_t)m.nblocks * ndim);
+	m.bdim.resize((size_t)m.nblocks * ndim);
+	m.boff.resize((size_t)m.nblocks);
+	m.lin.resize((size_t)m.nblocks);
 	m.nnz = off;
 	i64 total = 1;
-	bool small = true;
+	bool dense = true;
 	for (int a = 0; a < ndim; a++)
 	{
 		total *= m.nb[a];
-		if (total > (i64)1 << 24) { small = false; break; }
+		if (total > 4 * (i64)m.nblocks + 4096) { dense = false; break; }
 	}
-	if (small)
+	if (dense)
 	{
 		m.lut.assign((size_t)total, -1);
-		for (int b = 0; b < m.nblocks; b++) m.lut[(size_t)m.linear(m.index(b))] = b;
-	}
-	else
-	{
-		for (int b = 0; b < m.nblocks; b++) m.lut_map[m.linear(m.index(b))] = b;
+		for (int b = 0; b < m.nblocks; b++) m.lut[(size_t)m.lin[(size_t)b]] = b;
 	}
 	return m;
 }

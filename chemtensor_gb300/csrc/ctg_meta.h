@@ -34,9 +34,11 @@ struct Meta {
 	std::vector<i64> boff;                    // entry offset of each block
 	i64 nnz = 0;
 
-	// block multi-index -> block number (or -1)
-	std::vector<int> lut;                     // dense table over prod(nb) when small enough
-	std::unordered_map<i64, int> lut_map;     // otherwise
+	// block multi-index -> block number (or -1): blocks are enumerated in row-major order, so
+	// their linear indices are increasing; a dense table is kept only where it is not much
+	// larger than the block list
+	std::vector<i64> lin;                     // linear index of every block, increasing
+	std::vector<int> lut;                     // dense table over prod(nb), or empty
 
 	const i64* index(int b) const { return &bidx[(size_t)b * ndim]; }
 	const i64* dims(int b) const { return &bdim[(size_t)b * ndim]; }
