@@ -44,6 +44,8 @@ METRIC = "two-site DMRG sweeps/s (Fermi-Hubbard L=32, D=256)"
 UNIT = "sweeps/s"
 L2_FLUSH_BYTES = 256 << 20
 PRECISIONS = {"fp64": 0, "bf16x3": 1}
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_svd_tour launch (ncu, see profiles/)
+SVD_TRAFFIC_PER_LAUNCH = 179200 + 256
 
 
 def build_inputs():
@@ -207,7 +209,9 @@ def bench_gpu(args, world, rank, local):
         cs.free_mps(cP)
         return wall, en, out
 
-    # 1) device-resident timing: W warm-up sweeps then K timed sweeps in one call
+    # 1) device-resident timing: W warm-up sweeps then K timed sweeps in one call (first call of the
+    # process: the work lists of each sweep are built as its block structures appear)
+    lib.ctgpu_clear_plan_cache()
     lib.ctgpu_set_l2_flush_bytes(L2_FLUSH_BYTES)
     lib.ctgpu_set_profiling(0, 0)
     barrier(world)
@@ -225,29 +229,48 @@ def bench_gpu(args, world, rank, local):
     lib.ctgpu_set_profiling(0, 0)
     prof = native.kernel_profile()
     stats = native.last_stats()
-    g = prof["block_gemm"]
     fp64_peak = float(lib.ctgpu_measure_fp64_tflops())
-    achieved = (g["flops"] / (g["ms"] * 1e-3)) / 1e12 if g["ms"] > 0 else 0.0
     total_prof_ms = sum(v["ms"] for v in prof.values())
+    nsw = max(stats["sweeps"], 1)
+    # dominant kernel class: the block SVD, bound by the FP64 pipe (no tensor-core or HBM bound applies:
+    # its columns live in shared memory and L2)
+    sv = prof["block_svd"]
+    svd_flops_per_sweep = stats["svd_flops"] / nsw
+    svd_ms_per_sweep = sv["ms"] / K if K > 0 else 0.0
+    svd_launches_per_sweep = sv["launches"] / K if K > 0 else 0.0
+    achieved = (svd_flops_per_sweep / (svd_ms_per_sweep * 1e-3)) / 1e12 if svd_ms_per_sweep > 0 else 0.0
+    g = prof["block_gemm"]
+    g_achieved = (g["flops"] / (g["ms"] * 1e-3)) / 1e12 if g["ms"] > 0 else 0.0
     roofline = {
-        "bound": "fp64", "kernel": "k_gemm_f64 (grouped block GEMM, all local-H and environment contractions)",
+        "bound": "fp64", "kernel": "k_svd_tour (block SVD: pivoted QR + cluster Jacobi, one launch per cluster size)",
         "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None,
-        "peak_source": "FP64 FMA probe measured live in this run (no FP64 entry in MEASURED_PEAKS.json)",
-        "traffic": None, "launches": g["launches"], "flops_per_launch": g["flops"] / max(g["launches"], 1),
-        "avg_launch_us": 1e3 * g["ms"] / max(g["launches"], 1),
+        "peak_source": "FP64 FMA probe measured live in this run (MEASURED_PEAKS.json has HBM and bf16 peaks only)",
+        "flops_definition": "Jacobi inner products and rotations as executed (counted on the device), "
+                            "QR and output factors at full rank (host estimate)",
+        "flops_per_launch": svd_flops_per_sweep / max(svd_launches_per_sweep, 1e-9),
+        "avg_launch_us": 1e3 * svd_ms_per_sweep / max(svd_launches_per_sweep, 1e-9),
+        "traffic": SVD_TRAFFIC_PER_LAUNCH,
+        "traffic_source": "dram read+write of one k_svd_tour launch (16-CTA cluster, largest block of a bond) "
+                          "from profiles/k_svd_tour_hubbard_L32_D256.md",
         "kernel_share": {k: (v["ms"] / total_prof_ms if total_prof_ms > 0 else 0) for k, v in prof.items()},
+        "block_gemm": {"bound": "fp64", "achieved": g_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                       "frac": g_achieved / fp64_peak if fp64_peak > 0 else None, "launches": g["launches"],
+                       "flops_per_launch": g["flops"] / max(g["launches"], 1),
+                       "avg_launch_us": 1e3 * g["ms"] / max(g["launches"], 1)},
     }
 
-    # 3) end to end through the C ABI with host buffers (upload, setup, K sweeps, download)
+    # 3) end to end through the C ABI with host buffers (upload, setup, K sweeps, download), starting
+    # from an empty plan cache like a first call
     lib.ctgpu_set_l2_flush_bytes(0)
+    lib.ctgpu_clear_plan_cache()
     barrier(world)
     wall, en_e2e, out = call(K)
     wall = dist_max(wall, world)
     e2e = {"value": world * K / wall, "unit": UNIT,
            "h2d_bytes_per_step": (chain_bytes(H) + chain_bytes(psi0)) / K,
            "d2h_bytes_per_step": chain_bytes(out) / K,
-           "note": "whole dmrg_twosite call from host structs: upload, right-normalisation, environments, "
-                   "K sweeps, download; per step = per sweep"}
+           "note": "whole dmrg_twosite call from host structs with an empty plan cache: upload, "
+                   "right-normalisation, environments, K sweeps from the start state, download; per step = per sweep"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -280,6 +303,62 @@ def bench_gpu(args, world, rank, local):
     cs.free_mpo(cH)
 
 
+def bench_local_h(args, world, rank, local):
+    """Local-Hamiltonian microbenchmark: D = 1024 over 41 Gaussian sectors, Dw = 26, resident
+    operands, work lists built once, 1000 back-to-back applications per precision."""
+    from chemtensor_gb300 import ctstructs as cs, native, workloads as wl
+    lib = native.lib()
+    lib.ctgpu_set_device(local)
+    a, h2, l, r = wl.local_h_microbench(D=1024, nsec=41, sigma=6.0, Dw=26, seed=1)
+    ca, ch, cl, cr = (cs.BlockSparseTensor() for _ in range(4))
+    for t, c in ((a, ca), (h2, ch), (l, cl), (r, cr)):
+        cs.write_bst(t, c)
+    out = {}
+    results = {}
+    for name, prec in (("fp64", 0), ("bf16x3", 1)):
+        native.set_precision(prec)
+        ms, fl = C.c_double(), C.c_double()
+        ret = lib.ctgpu_time_local_hamiltonian(C.byref(ca), C.byref(ch), C.byref(cl), C.byref(cr), args.matvecs,
+                                               C.byref(ms), C.byref(fl))
+        if ret != 0:
+            raise RuntimeError(native.last_error())
+        b = cs.BlockSparseTensor()
+        if lib.ctgpu_apply_local_hamiltonian(C.byref(ca), C.byref(ch), C.byref(cl), C.byref(cr), C.byref(b)) != 0:
+            raise RuntimeError(native.last_error())
+        results[name] = cs.read_bst(b)
+        cs.free_bst(b)
+        per = ms.value / args.matvecs
+        out[name] = {"ms_per_matvec": per, "tflops": fl.value / (per * 1e-3) / 1e12, "flops_per_matvec": fl.value}
+    native.set_precision(0)
+    num = sum(float(np.sum((results["bf16x3"].blocks[k] - v) ** 2)) for k, v in results["fp64"].blocks.items())
+    den = sum(float(np.sum(v ** 2)) for v in results["fp64"].blocks.values())
+    fp64_peak = float(lib.ctgpu_measure_fp64_tflops())
+    line = {
+        "metric": "local-H TFLOP/s (synthetic D=1024, 41 Gaussian sectors, Dw=26)", "value": out["bf16x3"]["tflops"],
+        "unit": "TFLOP/s", "n_gpus": 1, "steps": args.matvecs, "warmup": 3,
+        "ms_per_step": out["bf16x3"]["ms_per_matvec"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x3+f32acc", "data": "synthetic (seeded N(0,1) blocks)",
+        "config": {"workload": "local_h_microbench D=1024 nsec=41 sigma=6 Dw=26 d=4 seed=1", "l2": "operands resident"},
+        "fp64": out["fp64"], "bf16x3": out["bf16x3"],
+        "bf16x3_rel_error_vs_fp64": (num / den) ** 0.5 if den > 0 else None,
+        "roofline": {"bound": "tensor", "achieved": out["bf16x3"]["tflops"], "peak": None, "unit": "TFLOP/s",
+                     "note": "algorithmic FLOPs (2 m n k of the FP64 product); the split-BF16 form issues 3x that "
+                             "on the tensor cores", "fp64_peak_live": fp64_peak,
+                     "fp64_frac": out["fp64"]["tflops"] / fp64_peak if fp64_peak > 0 else None},
+    }
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        line["roofline"]["peak"] = peaks["bf16_tflops"]
+        line["roofline"]["frac"] = 3 * out["bf16x3"]["tflops"] / peaks["bf16_tflops"]
+        line["roofline"]["peak_source"] = "MEASURED_PEAKS.json bf16_tflops (burst); frac counts the 3 products"
+    except Exception:
+        pass
+    for c in (ca, ch, cl, cr):
+        cs.free_bst(c)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def sweeps_only(args, local):
     """One dmrg_twosite call of warmup + steps sweeps on the workload (profiler target)."""
     from chemtensor_gb300 import ctstructs as cs, native
@@ -309,12 +388,17 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=sorted(PRECISIONS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="full", choices=["full", "sweeps"],
-                    help="sweeps: only one device call of warmup+steps sweeps (for profiler captures), no JSON line")
+    ap.add_argument("--matvecs", type=int, default=1000, help="local-H applications timed in --mode localh")
+    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh"],
+                    help="sweeps: only one device call of warmup+steps sweeps (for profiler captures), no JSON line; "
+                         "localh: local-Hamiltonian microbenchmark (synthetic D=1024), its own JSON line")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.mode == "sweeps":
         sweeps_only(args, local)
+        return
+    if args.mode == "localh":
+        bench_local_h(args, world, rank, local)
         return
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

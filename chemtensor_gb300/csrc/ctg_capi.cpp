@@ -59,6 +59,14 @@ int ctgpu_set_precision(int precision)
 	return old;
 }
 
+int ctgpu_clear_plan_cache(void)
+{
+	return guarded([&] {
+		ctg::context_for_device(g_opts.device).clear_plans();
+		return 0;
+	});
+}
+
 int ctgpu_set_device(int device)
 {
 	const int old = g_opts.device;
@@ -88,6 +96,7 @@ int ctgpu_get_last_stats(struct ctgpu_stats* out)
 	out->host_plan_s = s.host_plan_s;
 	out->plan_hits = s.plan_hits;
 	out->plan_misses = s.plan_misses;
+	out->svd_flops = s.svd_flops;
 	return 0;
 }
 
@@ -158,6 +167,20 @@ int ctgpu_apply_local_hamiltonian(const struct block_sparse_tensor* a, const str
 		ctg::DTensor dl = ctg::tensor_from_struct(c, l), dr = ctg::tensor_from_struct(c, r);
 		ctg::DTensor out = ctg::apply_local_hamiltonian_once(c, da, dw, dl, dr, g_opts.precision);
 		ctg::tensor_to_struct(c, out, b);
+		return 0;
+	});
+}
+
+int ctgpu_time_local_hamiltonian(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
+                                 const struct block_sparse_tensor* l, const struct block_sparse_tensor* r, int nmatvec,
+                                 double* ms, double* flops)
+{
+	return guarded([&] {
+		CTG_CHECK(nmatvec >= 1 && ms && flops, "invalid arguments");
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor da = ctg::tensor_from_struct(c, a), dw = ctg::tensor_from_struct(c, w);
+		ctg::DTensor dl = ctg::tensor_from_struct(c, l), dr = ctg::tensor_from_struct(c, r);
+		*ms = ctg::time_local_hamiltonian(c, da, dw, dl, dr, g_opts.precision, nmatvec, flops);
 		return 0;
 	});
 }

@@ -465,6 +465,26 @@ DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w,
 	return out;
 }
 
+double time_local_hamiltonian(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,
+                              int precision, int nmatvec, double* flops)
+{
+	LocalH h(c, a.m(), w, l, r, precision);
+	DTensor out = c.empty(a.meta);
+	for (int i = 0; i < 3; i++) h.apply(c, a.data(), out.data());
+	cudaEvent_t e[2];
+	for (auto& x : e) CTG_CUDA(cudaEventCreate(&x));
+	c.sync();
+	CTG_CUDA(cudaEventRecord(e[0], c.stream()));
+	for (int i = 0; i < nmatvec; i++) h.apply(c, a.data(), out.data());
+	CTG_CUDA(cudaEventRecord(e[1], c.stream()));
+	c.sync();
+	float ms = 0;
+	CTG_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
+	for (auto& x : e) cudaEventDestroy(x);
+	if (flops) *flops = h.flops;
+	return ms;
+}
+
 // ------------------------------------------------------------------------------------
 // dmrg_twosite
 // ------------------------------------------------------------------------------------
@@ -499,6 +519,7 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	c.profile = false;
 	c.prof_reset();
 	c.svd_max_sweeps = 0;
+	c.svd_flops = 0;
 	c.host_plan_s = 0;
 	c.host_alloc_s = 0;
 	c.host_upload_s = 0;
@@ -674,6 +695,7 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	st->svd_max_sweeps = c.svd_max_sweeps;
 	st->host_plan_s = c.host_plan_s;
 	st->plan_hits = c.plan_hits;
+	st->svd_flops = c.svd_flops;
 	st->plan_misses = c.plan_misses;
 	if (getenv("CTGPU_SVD_PHASES") && st->sweeps > 0)
 		fprintf(stderr, "ctgpu: block SVD, last-finishing block per call, ms per sweep: QR %.2f Jacobi %.2f outputs %.2f launch %.2f\n",

@@ -34,6 +34,7 @@ struct DmrgStats {
 	int svd_max_sweeps = 0;             // largest Jacobi sweep count of any block SVD
 	double host_plan_s = 0;             // host time lowering operations into device work lists
 	long plan_hits = 0, plan_misses = 0;
+	double svd_flops = 0;               // FP64 flops of the block SVDs
 	std::vector<double> sweep_ms;       // device time of every sweep (CUDA events on the stream)
 	std::vector<long> sweep_launches;   // kernels launched by every sweep
 	KProf prof[K_NUM_CLASSES];          // per kernel class, over the profiled sweeps
@@ -57,6 +58,11 @@ DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const
 // one application of the local two-site Hamiltonian (src/algorithm/chain_ops.c:353-390)
 DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,
                                      int precision);
+
+// device time (ms, CUDA events) of nmatvec back-to-back applications of the local Hamiltonian
+// after three untimed ones; *flops receives the algorithmic GEMM FLOPs of one application
+double time_local_hamiltonian(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,
+                              int precision, int nmatvec, double* flops);
 
 // host <-> device conversions of reference structs
 Meta meta_from_struct(const struct block_sparse_tensor* t);

@@ -75,6 +75,12 @@ static const PlanEntry* plan_find(Ctx& c, uint64_t key, int kind, const std::vec
 	return nullptr;
 }
 
+void Ctx::clear_plans()
+{
+	plans_->map.clear();
+	plans_->bytes = 0;
+}
+
 static void plan_insert(Ctx& c, uint64_t key, PlanEntry&& e, size_t bytes)
 {
 	PlanCache* pc = c.plans();
@@ -138,7 +144,7 @@ PlanTimer::~PlanTimer()
 	c.host_plan_cpu_s += thread_cpu_seconds() - cpu0;
 }
 
-static_assert(256 + sizeof(LanczosScalars) <= 4096, "pinned result slots overlap");
+static_assert(256 + sizeof(LanczosScalars) <= 2048, "pinned result slots overlap");
 
 double* Ctx::pinned_doubles(size_t n)
 {
@@ -1229,7 +1235,7 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
 	DBuf status(&c, 2 * sizeof(int));
 	CTG_CUDA(cudaMemsetAsync(status.ptr, 0, 2 * sizeof(int), c.stream()));
-	DBuf tail(&c, descs.size() * sizeof(double));
+	DBuf tail(&c, descs.size() * sizeof(double));     // [0]: executed Jacobi FP64 flops
 	CTG_CUDA(cudaMemsetAsync(tail.ptr, 0, descs.size() * sizeof(double), c.stream()));
 	// opt-in diagnostics: per-block phase stamps (QR, Jacobi, outputs) of the shared-memory path
 	static const bool phases = getenv("CTGPU_SVD_PHASES") != nullptr;
@@ -1280,8 +1286,18 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 			for (int i = 0; i < 4; i++) c.svd_jacobi_cycles[i] += (double)h[8 * crit + 4 + i];
 		}
 	}
-	// the status reaches pinned host memory once the stream gets there (read by op_svd_finish)
+	// the status and the flop count reach pinned host memory once the stream gets there (read by
+	// op_svd_finish)
 	CTG_CUDA(cudaMemcpyAsync(c.svd_status_host(), status.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream()));
+	CTG_CUDA(cudaMemcpyAsync(c.svd_flops_host(), tail.ptr, sizeof(double), cudaMemcpyDeviceToHost, c.stream()));
+	// Householder QR (2 M N^2 - 2 N^3 / 3) and the reflectors applied to V (~4 M N^2 - 2 N^3) at
+	// full rank, counted on the host
+	pend.other_flops = 0;
+	for (const SvdDesc& d : descs)
+	{
+		const double M = std::max(d.m, d.n), N = std::min(d.m, d.n);
+		pend.other_flops += 2.0 * M * N * N - 2.0 * N * N * N / 3.0 + 4.0 * M * N * N - 2.0 * N * N * N;
+	}
 	pend.descs = descs;
 	pend.launches = groups.size();
 	return 0;
@@ -1290,6 +1306,7 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 int op_svd_finish(Ctx& c, const SvdPending& pend)
 {
 	if (pend.descs.empty()) return 0;
+	c.svd_flops += *c.svd_flops_host() + pend.other_flops;
 	const int* hst = c.svd_status_host();
 	c.svd_max_sweeps = std::max(c.svd_max_sweeps, hst[1]);
 	if (hst[0] == 0) return 0;

@@ -84,6 +84,7 @@ public:
 	double gemm_flops = 0;       // algorithmic GEMM FLOPs issued
 	long kernel_launches = 0;
 	int svd_max_sweeps = 0;      // largest Jacobi sweep count of any block SVD
+	double svd_flops = 0;        // FP64 flops of the block SVDs (Jacobi executed, QR and outputs estimated)
 	int svd_full_reruns = 0;     // SVDs repeated at full resolution for the truncation decision
 	double host_plan_s = 0;      // host time spent lowering operations into descriptor lists
 	double host_alloc_s = 0, host_upload_s = 0;   // host time in device allocation / descriptor uploads
@@ -96,12 +97,14 @@ public:
 	// cache of lowered operations, keyed by operation and operand structures (DMRG revisits the
 	// same block structures every sweep once the bond dimensions have settled)
 	struct PlanCache* plans() { return plans_; }
+	void clear_plans();
 	// device flag raised by a tensor-core kernel whose bounded wait timed out (checked at sync)
 	int* tc_error();
 	int num_sms() const { return sms_; }
 	// pinned host memory for small device-to-host results read after a synchronisation
 	int* svd_status_host() { return (int*)pinned_; }
 	LanczosScalars* lanczos_host() { return (LanczosScalars*)((char*)pinned_ + 256); }
+	double* svd_flops_host() { return (double*)((char*)pinned_ + 2048); }
 	// n doubles of pinned host memory (contents valid until the next call); only call while no
 	// asynchronous copy into it is pending
 	double* pinned_doubles(size_t n);
@@ -210,6 +213,7 @@ struct SvdPending {
 	std::vector<SvdDesc> descs;
 	size_t launches = 0;
 	DTensor a;
+	double other_flops = 0;      // QR and output flops (host estimate at full rank)
 };
 // enqueue the SVD without waiting for it; its status reaches pinned host memory when the stream
 // gets there, so op_svd_finish may run only after a synchronisation of c's stream

@@ -111,8 +111,8 @@ void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs,
 // in descending order; one thread-block cluster per block. Entries of u, s and vh beyond the
 // numerical rank are not written (the caller zeroes them). status[0] becomes -1 if a block does
 // not converge within SVD_MAX_SWEEPS FP64 Jacobi sweeps, status[1] receives the largest sweep
-// count; tail[block] (zeroed by the caller) receives an upper bound for the squared singular
-// values dropped as rank deficient.
+// count; flops[0] (zeroed by the caller) accumulates the FP64 flops executed by the Jacobi inner
+// products and rotations of the shared-memory path.
 constexpr int SVD_MAX_SWEEPS = 60;
 struct SvdDesc {
 	i64 a_off, u_off, s_off, v_off, w_off;
@@ -137,7 +137,7 @@ SvdLaunch svd_launch_for(int m, int n, int want, int max_cluster);
 // its SM clock cycles spent in the Jacobi inner products, rotation parameters, rotations and
 // cluster exchanges to phase_ts[8 block + 4 ..].
 void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* descs, const double* a, double* u,
-                      double* s, double* vh, double* scratch, int* status, double* tail, cudaStream_t st,
+                      double* s, double* vh, double* scratch, int* status, double* flops, cudaStream_t st,
                       unsigned long long* phase_ts = nullptr);
 
 // Householder RQ of a row-major m x n block: A = R Q with Q (k x n) orthonormal rows, R (m x k), k = min(m, n).

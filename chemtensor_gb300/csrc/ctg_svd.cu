@@ -384,7 +384,7 @@ __device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int
 }
 
 __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, int cB, int npad, float tol2, const StepBuf& sb,
-                            long long* cyc)
+                            long long* cyc, double& flops)
 {
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const long long c0 = cyc ? clock64() : 0;
@@ -409,7 +409,8 @@ __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, 
 		int sp, cp, sq, cq;
 		int rot = 0;
 		double tau = 0.0, sn = 0.0;
-		if (step_pair(t, mode, step, lane, cA, cB, npad, sp, cp, sq, cq))
+		const bool valid = step_pair(t, mode, step, lane, cA, cB, npad, sp, cp, sq, cq);
+		if (valid)
 		{
 			double* np_ = t.nrm(buf, sp) + cp;
 			double* nq_ = t.nrm(buf, sq) + cq;
@@ -426,9 +427,17 @@ __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, 
 		sb.csc[lane] = tau;
 		sb.css[lane] = sn;
 		// compact list of the rotating pairs, so that the work items below are spread evenly
-		const unsigned mask = __ballot_sync(np >= 32 ? 0xffffffffu : ((1u << np) - 1u), rot);
+		const unsigned amask = np >= 32 ? 0xffffffffu : ((1u << np) - 1u);
+		const unsigned mask = __ballot_sync(amask, rot);
+		const unsigned vmask = __ballot_sync(amask, valid);
 		if (rot) sb.rotk[__popc(mask & ((1u << lane) - 1u))] = lane;
-		if (lane == 0) sb.rotk[SVD_STEP_PAIRS] = __popc(mask);
+		if (lane == 0)
+		{
+			sb.rotk[SVD_STEP_PAIRS] = __popc(mask);
+			// executed FP64 flops: an inner product per examined pair, three FMAs per entry of
+			// the two column records per rotation
+			flops += 2.0 * t.N * __popc(vmask) + 6.0 * (t.N + t.r) * __popc(mask);
+		}
 	}
 	__syncthreads();
 	const long long c2 = cyc ? clock64() : 0;
@@ -487,7 +496,7 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 __global__ void __launch_bounds__(SVD_THREADS)
 k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
            double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
-           double* __restrict__ tail, int cl, int smem_bytes, unsigned long long* __restrict__ phase_ts)
+           double* __restrict__ flops, int cl, int smem_bytes, unsigned long long* __restrict__ phase_ts)
 {
 	extern __shared__ __align__(16) double smem[];
 	cg::cluster_group cluster = cg::this_cluster();
@@ -583,6 +592,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 
 	const float tol2 = (float)((double)N * DBL_EPSILON * (double)N * DBL_EPSILON);
 	long long cyc_acc[4] = {0, 0, 0, 0};               // dots, rotation parameters, rotations, exchanges
+	double jflops = 0;                                 // counted by thread 0 (lane 0 of warp 0)
 	// counted on the second CTA: the first one holds the last column group, often short or empty
 	const bool count = phase_ts && tid == 0 && rank == (cl > 1 ? 1 : 0);
 	long long* cyc = count ? cyc_acc : nullptr;
@@ -613,9 +623,9 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			if (rho == 0)
 			{
 				const int npad = t.bs + (t.bs & 1);
-				for (int st = 0; st < npad - 1; st++) jacobi_step(t, buf, 0, st, cA, cB, npad, tol2, sb, cyc);
+				for (int st = 0; st < npad - 1; st++) jacobi_step(t, buf, 0, st, cA, cB, npad, tol2, sb, cyc, jflops);
 			}
-			for (int st = 0; st < t.bs; st++) jacobi_step(t, buf, 1, st, cA, cB, 0, tol2, sb, cyc);
+			for (int st = 0; st < t.bs; st++) jacobi_step(t, buf, 1, st, cA, cB, 0, tol2, sb, cyc, jflops);
 			if (cl > 1)
 			{
 				const long long cx = cyc ? clock64() : 0;
@@ -668,12 +678,11 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			if (lane == 0) xs.sig[x * t.bs + c] = sqrt(acc);
 		}
 	}
+	if (tid == 0 && jflops > 0) atomicAdd(flops, jflops);
 	if (rank == 0 && tid == 0)
 	{
 		atomicMax(status + 1, sweep);
 		if (!converged) atomicExch(status, -1);
-		// rank-deficient part beyond r: its weight is below eps^2 ||B||_F^2 per column
-		if (r < N) atomicAdd(tail + blk, (double)(N - r) * DBL_EPSILON * DBL_EPSILON * __ldcg(xs.misc + 1));
 	}
 	cluster.sync();
 	if (stamp) phase_ts[8 * blk + 2] = globaltimer();
@@ -885,9 +894,6 @@ k_svd_global(const SvdDesc* __restrict__ descs, int first, const double* __restr
 				atomicAdd(tail + first + blockIdx.x / cl, acc);
 		}
 	}
-	// rank-deficient part beyond r: its weight is below eps^2 ||B||_F^2 per column
-	if (rank == 0 && tid == 0 && r < N)
-		atomicAdd(tail + first + blockIdx.x / cl, (double)(N - r) * DBL_EPSILON * DBL_EPSILON * __ldcg(misc + 1));
 
 	// ---- 3. explicit Q (M x r) = H_0 ... H_{r-1} E_r over the cluster ----
 	for (i64 e = gtid; e < (i64)M * r; e += gstride) Q[e] = (e / M == e % M) ? 1.0 : 0.0;
@@ -963,7 +969,7 @@ static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLE
 
 namespace {
 
-// layout of the fixed array: descriptor, status[2] + tail (as doubles), then the SVD workspace
+// layout of the fixed array: descriptor, status[2] + flop counter (as doubles), then the SVD workspace
 constexpr i64 NA_DESC = 0;
 constexpr i64 NA_STATUS = (sizeof(SvdDesc) + 7) / 8;
 constexpr i64 NA_WORK = NA_STATUS + 2;
@@ -977,7 +983,7 @@ __global__ void k_noalloc_prepare(double* base, SvdDesc d, double* u, double* s,
 		int* status = (int*)(base + NA_STATUS);
 		status[0] = 0;
 		status[1] = 0;
-		base[NA_STATUS + 1] = 0.0;                  // tail weight
+		base[NA_STATUS + 1] = 0.0;                  // flop counter
 	}
 	// factor entries beyond the numerical rank are not written by the SVD kernel
 	const i64 k = d.m < d.n ? d.m : d.n;
@@ -1040,12 +1046,12 @@ extern "C" int ctgpu_dense_svd_noalloc(const double* d_a, int m, int n, double* 
 	k_noalloc_prepare<<<64, 256, 0, st>>>(base, d, d_u, d_s, d_vh);
 	const SvdDesc* descs = (const SvdDesc*)(base + NA_DESC);
 	int* status = (int*)(base + NA_STATUS);
-	double* tail = base + NA_STATUS + 1;
+	double* flops = base + NA_STATUS + 1;
 	try
 	{
 		const int maxcl = svd_max_cluster(dev);
 		launch_svd_group(svd_launch_for(m, n, maxcl, maxcl), 0, 1, descs, d_a, d_u, d_s, d_vh, base + NA_WORK, status,
-		                 tail, st);
+		                 flops, st);
 		k_noalloc_finish<<<1, 1, 0, st>>>(base, d_info);
 		const cudaError_t e = cudaGetLastError();
 		if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
@@ -1134,7 +1140,7 @@ SvdLaunch svd_launch_for(int m, int n, int want, int max_cluster)
 }
 
 void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* descs, const double* a, double* u,
-                      double* s, double* vh, double* scratch, int* status, double* tail, cudaStream_t st,
+                      double* s, double* vh, double* scratch, int* status, double* flops, cudaStream_t st,
                       unsigned long long* phase_ts)
 {
 	if (count <= 0) return;
@@ -1152,7 +1158,7 @@ void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* d
 	cfg.numAttrs = 1;
 	if (g.global)
 	{
-		CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_global, descs, first, a, u, s, vh, scratch, status, 0.0, tail, g.cluster));
+		CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_global, descs, first, a, u, s, vh, scratch, status, 0.0, flops, g.cluster));
 		return;
 	}
 	static bool attr_set[64] = {false};
@@ -1164,7 +1170,7 @@ void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* d
 		CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
 		attr_set[dev] = true;
 	}
-	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, tail, g.cluster, g.smem,
+	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, flops, g.cluster, g.smem,
 	                             phase_ts));
 }
 

@@ -28,6 +28,8 @@ EXPORTS = [
     "ctgpu_block_sparse_tensor_dot",
     "ctgpu_block_sparse_tensor_transpose",
     "ctgpu_apply_local_hamiltonian",
+    "ctgpu_time_local_hamiltonian",
+    "ctgpu_clear_plan_cache",
     "ctgpu_contraction_operator_step_left",
     "ctgpu_contraction_operator_step_right",
     "ctgpu_block_sparse_tensor_svd_values",
@@ -55,6 +57,7 @@ class Stats(C.Structure):
         ("total_gemm_flops", C.c_double), ("matvecs", C.c_long), ("kernel_launches", C.c_long),
         ("sweeps", C.c_int), ("max_bond_dim", C.c_int64), ("svd_max_sweeps", C.c_int),
         ("host_plan_s", C.c_double), ("plan_hits", C.c_long), ("plan_misses", C.c_long),
+        ("svd_flops", C.c_double),
     ]
 
 
@@ -75,6 +78,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_block_sparse_tensor_dot.argtypes = [P, C.c_int, P, C.c_int, C.c_int, P]
     lib.ctgpu_block_sparse_tensor_transpose.argtypes = [P, P, P]
     lib.ctgpu_apply_local_hamiltonian.argtypes = [P] * 5
+    lib.ctgpu_time_local_hamiltonian.argtypes = [P, P, P, P, C.c_int, P, P]
+    lib.ctgpu_clear_plan_cache.argtypes = []
     lib.ctgpu_contraction_operator_step_left.argtypes = [P] * 4
     lib.ctgpu_contraction_operator_step_right.argtypes = [P] * 4
     lib.ctgpu_block_sparse_tensor_svd_values.argtypes = [P, P, P]

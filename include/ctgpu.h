@@ -45,6 +45,10 @@ int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int 
  * or -5 for an unknown value (the setting is then unchanged). */
 int ctgpu_set_precision(int precision);
 
+/* Drop the lowered operations (device work lists) that this thread's context keeps for reuse
+ * across calls; the next calls rebuild them as needed. No counterpart in the reference. */
+int ctgpu_clear_plan_cache(void);
+
 /* CUDA device used by subsequent calls from this thread. Returns the previous device. */
 int ctgpu_set_device(int device);
 
@@ -69,6 +73,8 @@ struct ctgpu_stats
 	double host_plan_s;       /* host time spent lowering operations into device work lists */
 	long   plan_hits;         /* lowered operations reused from the per-thread plan cache */
 	long   plan_misses;       /* lowered operations built afresh */
+	double svd_flops;         /* FP64 flops of the block SVDs: Jacobi inner products and rotations as
+	                             executed, QR and output factors estimated at full rank */
 };
 int ctgpu_get_last_stats(struct ctgpu_stats* out);
 
@@ -124,6 +130,13 @@ int ctgpu_block_sparse_tensor_transpose(const int* perm, const struct block_spar
 /* apply_local_hamiltonian (src/algorithm/chain_ops.c:353-390): b = H_loc(w, l, r) a */
 int ctgpu_apply_local_hamiltonian(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
 	const struct block_sparse_tensor* l, const struct block_sparse_tensor* r, struct block_sparse_tensor* b);
+
+/* Measurement hook (no counterpart in the reference): device time *ms (CUDA events) of nmatvec
+ * back-to-back applications of the local Hamiltonian of apply_local_hamiltonian to a, with the
+ * tensors resident in HBM and the work lists built once, in the arithmetic of ctgpu_set_precision;
+ * *flops receives the algorithmic GEMM FLOPs of one application (sum of 2 m n k). */
+int ctgpu_time_local_hamiltonian(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
+	const struct block_sparse_tensor* l, const struct block_sparse_tensor* r, int nmatvec, double* ms, double* flops);
 
 /* contraction_operator_step_left / _right (src/algorithm/chain_ops.c:196-245 / :116-165), with b = a */
 int ctgpu_contraction_operator_step_left(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
