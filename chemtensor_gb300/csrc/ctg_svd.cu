@@ -31,6 +31,7 @@
 #include <cooperative_groups.h>
 
 #include "ctg_kernels.h"
+#include "ctg_svd_schedule.h"
 
 namespace cg = cooperative_groups;
 
@@ -59,14 +60,6 @@ __device__ double block_sum(double v, double* red)
 	double t = 0;
 	for (int w = 0; w < NWARPS; w++) t += red[w];
 	return t;
-}
-
-__device__ __forceinline__ void round_robin_pair(int rnd, int pi, int np, int& p, int& q)
-{
-	// circle method: index np-1 stays fixed, the others rotate
-	if (pi == 0) { p = rnd; q = np - 1; }
-	else { p = (rnd + pi) % (np - 1); q = (rnd - pi + (np - 1)) % (np - 1); }
-	if (p > q) { const int t = p; p = q; q = t; }
 }
 
 // Householder QR with column pivoting of W (M x N, column-major) inside one CTA, stopped at
@@ -321,24 +314,6 @@ __device__ __forceinline__ bool rotation_params(double al, double be, double ga,
 	return sn != 0.0;
 }
 
-// groups held by CTA pi in round rho (circle method over nm + 1 groups; group nm stays with CTA 0)
-__device__ __forceinline__ void round_groups(int rho, int pi, int nm, int& a, int& b)
-{
-	if (pi == 0) { a = rho; b = nm; }
-	else { a = (rho + pi) % nm; b = (rho - pi + nm) % nm; }
-}
-
-// CTA and slot that hold group x in round rho
-__device__ __forceinline__ void group_owner(int x, int rho, int nm, int& pi, int& slot)
-{
-	if (x == nm) { pi = 0; slot = 1; return; }
-	const int dd = ((x - rho) % nm + nm) % nm;
-	const int half = (nm + 1) / 2;
-	if (dd == 0) { pi = 0; slot = 0; }
-	else if (dd <= half - 1) { pi = dd; slot = 0; }
-	else { pi = nm - dd; slot = 1; }
-}
-
 struct Tour {
 	int nblk, nm, bs, bsmax, r, N, ld;
 	double* sm;
@@ -359,28 +334,10 @@ struct StepBuf {
 	int* local_rot;
 };
 
-// pair k of an inner step: mode 0 pairs inside each slot (circle method over npad columns),
-// mode 1 pairs slot-0 column k with slot-1 column (k + step) mod bs
 __device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int k, int cA, int cB, int npad, int& sp,
                                           int& cp, int& sq, int& cq)
 {
-	if (mode == 0)
-	{
-		const int half = npad >> 1;
-		const int sl = k < half ? 0 : 1;
-		int p, q;
-		round_robin_pair(step, k < half ? k : k - half, npad, p, q);
-		sp = sl;
-		sq = sl;
-		cp = p;
-		cq = q;
-		return q < (sl == 0 ? cA : cB);
-	}
-	sp = 0;
-	sq = 1;
-	cp = k;
-	cq = (k + step) % t.bs;
-	return k < cA && cq < cB;
+	return step_pair_idx(mode, step, k, t.bs, cA, cB, npad, sp, cp, sq, cq);
 }
 
 __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, int cB, int npad, float tol2, const StepBuf& sb,
