@@ -650,6 +650,8 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 		p.tiles[k] = at<GemmTile>(p.desc, o_tiles[k]);
 	}
 	p.flops = flops;
+	p.a_entries = s.nnz;
+	p.b_entries = t.nnz;
 	g_plan_stage[3] += host_seconds() - ts0;
 	return p;
 }
@@ -660,8 +662,19 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 	{
 		if (ntiles[0] > 0)
 		{
+			// both operands split once into BF16 hi / lo arrays with their FP64 layout
+			DBuf ab(&c, (size_t)(a_entries + b_entries) * 2 * sizeof(uint16_t));
+			uint16_t* ahi = (uint16_t*)ab.ptr;
+			uint16_t* alo = ahi + a_entries;
+			uint16_t* bhi = alo + a_entries;
+			uint16_t* blo = bhi + b_entries;
+			{
+				KScope ks(c, K_GEMM_TC, 2, 0, 12.0 * (double)(a_entries + b_entries));
+				launch_split_bf16(A, a_entries, ahi, alo, c.stream());
+				launch_split_bf16(B, b_entries, bhi, blo, c.stream());
+			}
 			KScope ks(c, K_GEMM_TC, 1, flops_cls[0], 0);
-			launch_gemm_bf16x3(ntiles[0], tiles[0], outs, cons, A, B, C, c.tc_error(), c.stream());
+			launch_gemm_bf16x3(ntiles[0], tiles[0], outs, cons, ahi, alo, bhi, blo, C, c.tc_error(), c.stream());
 		}
 		c.gemm_flops += flops;
 		return;

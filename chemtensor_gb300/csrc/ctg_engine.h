@@ -164,6 +164,7 @@ struct DotPlan {
 	const GemmSplit* splits = nullptr;   // tiles whose sum is split over several CTAs
 	int nsplits = 0;
 	DBufPtr work;                        // their partial sums
+	i64 a_entries = 0, b_entries = 0;    // entries of the two operand tensors
 	double flops = 0;
 	double flops_cls[NUM_TILE_CLASSES] = {0, 0, 0};
 	int precision = GEMM_FP64;

@@ -2,16 +2,20 @@
 //
 // Same work lists as the FP64 grouped GEMM (GemmOut / GemmContrib / GemmTile): every output block
 // C = sum_j op(A_j) op(B_j) with arbitrary element strides for the operands. Each FP64 operand
-// value x is split into x_hi = bf16(x) and x_lo = bf16(x - x_hi), and the product is taken as
+// value x is split into x_hi = bf16(x) and x_lo = bf16(x - x_hi) once per product by k_split_bf16
+// (into two BF16 arrays with the operand's layout), and the product is taken as
 // A_hi B_hi + A_hi B_lo + A_lo B_hi (the 3-product split-BF16 form; the dropped A_lo B_lo term and
 // the FP32 accumulation give a relative error of about 2^-16). Output in FP64.
 //
-// Per CTA: one 128 x TC_BN tile of one output block. Four warps load the operand tiles (FP64 ->
-// hi / lo BF16 in registers) into shared memory in the canonical no-swizzle K-major layout of the
-// tensor-core shared-memory descriptors; one thread issues the tcgen05.mma instructions into an
-// FP32 accumulator in tensor memory and commits them to an mbarrier; the epilogue reads the
-// accumulator with tcgen05.ld and writes FP64. Every wait on the mbarrier is bounded: on timeout
-// the CTA records an error flag, stops issuing work, frees its tensor memory and returns.
+// Per CTA: one 128 x TC_BN tile of one output block. Four warps stage the BF16 operand tiles into
+// shared memory in the canonical no-swizzle K-major layout of the tensor-core shared-memory
+// descriptors, double-buffered: while the tensor cores work on one stage the next one is loaded.
+// One thread issues the tcgen05.mma instructions into an FP32 accumulator in tensor memory and
+// commits each stage to that stage's mbarrier; the epilogue reads the accumulator with tcgen05.ld
+// and writes FP64. Every wait on an mbarrier is bounded: on timeout the CTA records an error flag,
+// stops issuing work, frees its tensor memory and returns.
+#include <algorithm>
+
 #include <cuda_bf16.h>
 
 #include "ctg_kernels.h"
@@ -31,7 +35,9 @@ constexpr int TC_LBO = 128;                // bytes between core matrices adjace
 constexpr int TC_SBO = (TC_BK / 8) * 128;  // bytes between core matrices adjacent in M / N
 constexpr int A_TILE_BYTES = TC_BM * TC_BK * 2;
 constexpr int B_TILE_BYTES = TC_BN * TC_BK * 2;
-constexpr int TC_SMEM_BYTES = 2 * A_TILE_BYTES + 2 * B_TILE_BYTES + 64;
+constexpr int STAGE_BYTES = 2 * A_TILE_BYTES + 2 * B_TILE_BYTES;   // hi and lo of A and B
+constexpr int TC_STAGES = 2;
+constexpr int TC_SMEM_BYTES = TC_STAGES * STAGE_BYTES + 64;
 constexpr long long TC_WAIT_LIMIT = 1ll << 26;   // spins before a wait is declared failed
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -114,25 +120,28 @@ __device__ __forceinline__ void fence_async_smem()
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void split_store(unsigned char* hi, unsigned char* lo, uint32_t off, double x)
+__global__ void __launch_bounds__(256)
+k_split_bf16(const double* __restrict__ x, i64 n, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo)
 {
-	const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
-	const __nv_bfloat16 l = __float2bfloat16_rn((float)(x - (double)__bfloat162float(h)));
-	*(__nv_bfloat16*)(hi + off) = h;
-	*(__nv_bfloat16*)(lo + off) = l;
+	for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+	{
+		// FP32 keeps 24 bits of x, more than the 16 that hi + lo carry
+		const float f = (float)x[i];
+		const __nv_bfloat16 h = __float2bfloat16_rn(f);
+		hi[i] = h;
+		lo[i] = __float2bfloat16_rn(f - __bfloat162float(h));
+	}
 }
 
 __global__ void __launch_bounds__(TC_THREADS)
 k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const GemmContrib* __restrict__ cons,
-              const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C, int* __restrict__ error)
+              const unsigned short* __restrict__ Ahi, const unsigned short* __restrict__ Alo,
+              const unsigned short* __restrict__ Bhi, const unsigned short* __restrict__ Blo, double* __restrict__ C,
+              int* __restrict__ error)
 {
 	extern __shared__ __align__(1024) unsigned char smem[];
-	unsigned char* a_hi = smem;
-	unsigned char* a_lo = a_hi + A_TILE_BYTES;
-	unsigned char* b_hi = a_lo + A_TILE_BYTES;
-	unsigned char* b_lo = b_hi + B_TILE_BYTES;
-	uint64_t* mbar = (uint64_t*)(b_lo + B_TILE_BYTES);
-	uint32_t* tmem_slot = (uint32_t*)(mbar + 1);
+	uint64_t* mbar = (uint64_t*)(smem + TC_STAGES * STAGE_BYTES);     // one per stage
+	uint32_t* tmem_slot = (uint32_t*)(mbar + TC_STAGES);
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const GemmTile tile = tiles[blockIdx.x];
 	const GemmOut o = outs[tile.out];
@@ -144,24 +153,35 @@ k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ ou
 		             : "memory");
 		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 	}
-	if (tid == 0) mbar_init(smem_u32(mbar), 1);
+	if (tid == 0)
+		for (int s = 0; s < TC_STAGES; s++) mbar_init(smem_u32(mbar + s), 1);
 	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();
 	const uint32_t tmem = *tmem_slot;
 	const uint32_t idesc = make_idesc();
-	uint32_t phase = 0;
-	bool issued_any = false;
 	bool ok = true;
+	int chunk = 0;                                      // k chunks issued so far
 
 	for (int c = o.c0; c < o.c0 + o.nc && ok; c++)
 	{
 		const GemmContrib g = cons[c];
-		const double* a = A + g.a_off;
-		const double* b = B + g.b_off;
-		for (int k0 = 0; k0 < g.k && ok; k0 += TC_BK)
+		for (int k0 = 0; k0 < g.k && ok; k0 += TC_BK, chunk++)
 		{
+			const int st = chunk % TC_STAGES;
+			unsigned char* a_hi = smem + st * STAGE_BYTES;
+			unsigned char* a_lo = a_hi + A_TILE_BYTES;
+			unsigned char* b_hi = a_lo + A_TILE_BYTES;
+			unsigned char* b_lo = b_hi + B_TILE_BYTES;
+			if (chunk >= TC_STAGES)
+			{
+				// the MMAs that read this stage (chunk - TC_STAGES) must be complete
+				const bool arrived = mbar_wait(smem_u32(mbar + st), (uint32_t)((chunk / TC_STAGES - 1) & 1));
+				ok = __syncthreads_and(arrived ? 1 : 0) != 0;
+				if (!ok) break;
+				tc_fence_after();
+			}
 			// A tile: 128 x 64, element (i, kk) -> (m0 + i, k0 + kk); zero outside the block
 			for (int e = tid; e < TC_BM * TC_BK; e += TC_THREADS)
 			{
@@ -169,8 +189,16 @@ k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ ou
 				if (g.sAk == 1) { kk = e % TC_BK; i = e / TC_BK; }
 				else { i = e % TC_BM; kk = e / TC_BM; }
 				const int gi = tile.m0 + i, gk = k0 + kk;
-				const double x = (gi < o.m && gk < g.k) ? a[(i64)gi * g.sAm + (i64)gk * g.sAk] : 0.0;
-				split_store(a_hi, a_lo, canon_offset(i, kk), x);
+				unsigned short h = 0, l = 0;
+				if (gi < o.m && gk < g.k)
+				{
+					const i64 off = g.a_off + (i64)gi * g.sAm + (i64)gk * g.sAk;
+					h = Ahi[off];
+					l = Alo[off];
+				}
+				const uint32_t so = canon_offset(i, kk);
+				*(unsigned short*)(a_hi + so) = h;
+				*(unsigned short*)(a_lo + so) = l;
 			}
 			// B tile as N x K (K-major): element (j, kk) = op(B)(k0 + kk, n0 + j)
 			for (int e = tid; e < TC_BN * TC_BK; e += TC_THREADS)
@@ -179,8 +207,16 @@ k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ ou
 				if (g.sBk == 1) { kk = e % TC_BK; j = e / TC_BK; }
 				else { j = e % TC_BN; kk = e / TC_BN; }
 				const int gj = tile.n0 + j, gk = k0 + kk;
-				const double x = (gj < o.n && gk < g.k) ? b[(i64)gk * g.sBk + (i64)gj * g.sBn] : 0.0;
-				split_store(b_hi, b_lo, canon_offset(j, kk), x);
+				unsigned short h = 0, l = 0;
+				if (gj < o.n && gk < g.k)
+				{
+					const i64 off = g.b_off + (i64)gk * g.sBk + (i64)gj * g.sBn;
+					h = Bhi[off];
+					l = Blo[off];
+				}
+				const uint32_t so = canon_offset(j, kk);
+				*(unsigned short*)(b_hi + so) = h;
+				*(unsigned short*)(b_lo + so) = l;
 			}
 			fence_async_smem();
 			tc_fence_before();
@@ -194,20 +230,20 @@ k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ ou
 					const uint32_t koff = (uint32_t)s * 2 * TC_LBO;
 					const uint64_t dah = make_desc(smem_u32(a_hi) + koff), dal = make_desc(smem_u32(a_lo) + koff);
 					const uint64_t dbh = make_desc(smem_u32(b_hi) + koff), dbl = make_desc(smem_u32(b_lo) + koff);
-					mma_bf16(tmem, dah, dbh, idesc, issued_any);
+					mma_bf16(tmem, dah, dbh, idesc, chunk > 0 || s > 0);
 					mma_bf16(tmem, dah, dbl, idesc, true);
 					mma_bf16(tmem, dal, dbh, idesc, true);
-					issued_any = true;
 				}
-				mma_commit(smem_u32(mbar));
+				mma_commit(smem_u32(mbar + st));
 			}
-			// every thread waits until the tensor cores have read this stage; the outcome is made
-			// uniform over the CTA so that all threads leave the loop together
-			const bool arrived = mbar_wait(smem_u32(mbar), phase);
-			phase ^= 1;
-			ok = __syncthreads_and(arrived ? 1 : 0) != 0;
-			issued_any = true;
 		}
+	}
+	if (ok && chunk > 0)
+	{
+		// the last commit tracks every MMA issued before it
+		const int last = chunk - 1;
+		const bool arrived = mbar_wait(smem_u32(mbar + last % TC_STAGES), (uint32_t)((last / TC_STAGES) & 1));
+		ok = __syncthreads_and(arrived ? 1 : 0) != 0;
 	}
 	if (!ok && lane == 0) atomicExch(error, 1);
 	tc_fence_after();
@@ -215,7 +251,7 @@ k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ ou
 	// epilogue: each warp owns 32 accumulator rows (tensor-memory lanes 32 w .. 32 w + 31)
 	const int row = tile.m0 + warp * 32 + lane;
 	double* cblk = C + o.c_off;
-	const bool have_acc = ok && o.nc > 0;
+	const bool have_acc = ok && chunk > 0;
 	for (int cc = 0; cc < TC_BN; cc += 16)
 	{
 		uint32_t v[16];
@@ -256,8 +292,17 @@ k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ ou
 int tc_tile_rows() { return TC_BM; }
 int tc_tile_cols() { return TC_BN; }
 
-void launch_gemm_bf16x3(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons, const double* A,
-                        const double* B, double* C, int* error, cudaStream_t st)
+void launch_split_bf16(const double* x, i64 n, void* hi, void* lo, cudaStream_t st)
+{
+	if (n <= 0) return;
+	const i64 blocks = std::min<i64>((n + 255) / 256, 4 * 152);
+	k_split_bf16<<<(int)blocks, 256, 0, st>>>(x, n, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo);
+	CTG_CUDA(cudaGetLastError());
+}
+
+void launch_gemm_bf16x3(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
+                        const void* Ahi, const void* Alo, const void* Bhi, const void* Blo, double* C, int* error,
+                        cudaStream_t st)
 {
 	if (ntiles <= 0) return;
 	static bool attr_set = false;
@@ -266,7 +311,9 @@ void launch_gemm_bf16x3(int ntiles, const GemmTile* tiles, const GemmOut* outs, 
 		CTG_CUDA(cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES));
 		attr_set = true;
 	}
-	k_gemm_bf16x3<<<ntiles, TC_THREADS, TC_SMEM_BYTES, st>>>(tiles, outs, cons, A, B, C, error);
+	k_gemm_bf16x3<<<ntiles, TC_THREADS, TC_SMEM_BYTES, st>>>(tiles, outs, cons, (const unsigned short*)Ahi,
+	                                                           (const unsigned short*)Alo, (const unsigned short*)Bhi,
+	                                                           (const unsigned short*)Blo, C, error);
 	CTG_CUDA(cudaGetLastError());
 }
 

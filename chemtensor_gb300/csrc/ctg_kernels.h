@@ -56,12 +56,16 @@ void launch_gemm_reduce(int nsplit, const GemmSplit* splits, const GemmOut* outs
                         cudaStream_t st);
 
 // Same work lists on the tcgen05 tensor cores, split-BF16 (hi*hi + hi*lo + lo*hi, FP32
-// accumulation, FP64 in and out); tiles of tc_tile_rows() x tc_tile_cols(). *error becomes 1 if a
+// accumulation, FP64 out); tiles of tc_tile_rows() x tc_tile_cols(). The operands come as BF16 hi
+// and lo arrays in the layout of the FP64 operands (launch_split_bf16). *error becomes 1 if a
 // bounded wait inside the kernel timed out.
 int tc_tile_rows();
 int tc_tile_cols();
-void launch_gemm_bf16x3(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons, const double* A,
-                        const double* B, double* C, int* error, cudaStream_t st);
+// hi[i] = bf16(x[i]), lo[i] = bf16(x[i] - hi[i]) for i < n (2-byte elements)
+void launch_split_bf16(const double* x, i64 n, void* hi, void* lo, cudaStream_t st);
+void launch_gemm_bf16x3(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
+                        const void* Ahi, const void* Alo, const void* Bhi, const void* Blo, double* C, int* error,
+                        cudaStream_t st);
 
 // ---- data movement -----------------------------------------------------------
 // Generic per-block permutation: dst block (row-major over dims) gathers

@@ -3,10 +3,11 @@
 Two-site wavefunction a (D x d^2 x D), merged MPO pair h2 (Dw x d^2 x d^2 x Dw), left and right
 environments l (1 x D x Dw x D) and r (D x Dw x D x 1), with the axis directions of
 apply_local_hamiltonian's operands (src/algorithm/chain_ops.c:353-390). The bond of dimension D
-is split over nsec quantum-number sectors whose sizes follow a discretised Gaussian (width sigma
-sectors) centred on the middle sector; d = 4 site states with particle numbers (0, 1, 1, 2);
-the MPO bond carries particle-number changes -1, 0, +1. Allowed blocks hold seeded N(0, 1)
-entries.
+is split over nsec quantum-number sectors q = -(nsec-1)/2 .. (nsec-1)/2 whose sizes follow a
+discretised Gaussian (width sigma sectors) centred on q = 0, rounded by largest remainders to sum
+to D (sectors that round to zero are absent); d = 4 site states with charges (-1, 0, 0, +1); the
+MPO bond of dimension Dw carries charges 0 (Dw - 2 Dw/3 of them), +1 and -1 (Dw/3 each).
+Allowed blocks hold seeded N(0, 1) entries.
 """
 
 from __future__ import annotations
@@ -17,20 +18,14 @@ from . import ctstructs as cs
 
 
 def gaussian_sector_sizes(total: int, nsec: int, sigma: float) -> np.ndarray:
+    """Largest-remainder rounding of total * w / sum(w), w = exp(-k^2 / (2 sigma^2))."""
     k = np.arange(nsec) - (nsec - 1) / 2
     w = np.exp(-0.5 * (k / sigma) ** 2)
-    sizes = np.maximum(1, np.floor(total * w / w.sum()).astype(np.int64))
-    # distribute the remainder to the largest sectors first (deterministic)
-    order = np.argsort(-w, kind="stable")
-    i = 0
-    while sizes.sum() < total:
-        sizes[order[i % nsec]] += 1
-        i += 1
-    while sizes.sum() > total:
-        j = order[i % nsec]
-        if sizes[j] > 1:
-            sizes[j] -= 1
-        i += 1
+    exact = total * w / w.sum()
+    sizes = np.floor(exact).astype(np.int64)
+    rest = total - int(sizes.sum())
+    order = np.argsort(-(exact - sizes), kind="stable")
+    sizes[order[:rest]] += 1
     return sizes
 
 
@@ -43,12 +38,13 @@ def _fill(t: cs.BlockSparse, rng) -> cs.BlockSparse:
 def local_h_microbench(D: int = 1024, nsec: int = 41, sigma: float = 6.0, Dw: int = 26, seed: int = 1):
     rng = np.random.default_rng(seed)
     sizes = gaussian_sector_sizes(D, nsec, sigma)
-    ql = np.repeat(np.arange(nsec, dtype=np.int32), sizes)            # left bond
-    qr = ql + 2                                                      # right bond: two sites later
-    qsite = np.array([0, 1, 1, 2], dtype=np.int32)
+    q = np.arange(nsec, dtype=np.int32) - (nsec - 1) // 2
+    ql = np.repeat(q, sizes)                                         # bond charges (both bonds)
+    qr = ql
+    qsite = np.array([-1, 0, 0, 1], dtype=np.int32)
     qpair = (qsite[:, None] + qsite[None, :]).ravel().astype(np.int32)
     nm = Dw // 3
-    qw = np.concatenate([np.full(nm, -1), np.full(Dw - 2 * nm, 0), np.full(nm, 1)]).astype(np.int32)
+    qw = np.concatenate([np.full(Dw - 2 * nm, 0), np.full(nm, 1), np.full(nm, -1)]).astype(np.int32)
     zero = np.zeros(1, dtype=np.int32)
     a = _fill(cs.BlockSparse((D, 16, D), (1, 1, -1), [ql, qpair, qr]), rng)
     h2 = _fill(cs.BlockSparse((Dw, 16, 16, Dw), (1, 1, -1, -1), [qw, qpair, qpair, qw]), rng)
