@@ -358,6 +358,8 @@ struct LocalH {
 	DTensor k;                       // transpose(l, {0,3,1,2}), computed once per bond
 	DTensor w, r;
 	DBufPtr s1, tt1, s2, tt2;
+	DBufPtr pk_r, pk_w, pk_k, pk_x, pk_t1, pk_t2;   // packed tensor-core operands
+	bool tc = false;
 	double flops = 0;
 
 	LocalH(Ctx& c, const Meta& a, const DTensor& w_, const DTensor& l, const DTensor& r_, int precision) : w(w_), r(r_)
@@ -387,10 +389,38 @@ struct LocalH {
 		s2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
 		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t1.out->nnz, 1) * sizeof(double));
 		flops = d1.flops + d2.flops + d3.flops;
+		if (precision == GEMM_BF16X3)
+		{
+			// operands fixed for the bond (r, w, k) are packed once; x and the intermediates per apply
+			auto rec = [&](i64 n, i64 bytes) { return std::make_shared<DBuf>(&c, (size_t)std::max<i64>(n, 1) * bytes); };
+			pk_r = rec(d1.b_recs, TC_B_REC_BYTES);
+			pk_w = rec(d2.a_recs, TC_A_REC_BYTES);
+			pk_k = rec(d3.a_recs, TC_A_REC_BYTES);
+			pk_x = rec(d1.a_recs, TC_A_REC_BYTES);
+			pk_t1 = rec(d2.b_recs, TC_B_REC_BYTES);
+			pk_t2 = rec(d3.b_recs, TC_B_REC_BYTES);
+			d1.pack_b(c, r.data(), pk_r->ptr);
+			d2.pack_a(c, w.data(), pk_w->ptr);
+			d3.pack_a(c, k.data(), pk_k->ptr);
+			tc = true;
+		}
 	}
 
 	void apply(Ctx& c, const double* x, double* y) const
 	{
+		if (tc)
+		{
+			d1.pack_a(c, x, pk_x->ptr);
+			d1.run_packed(c, pk_x->ptr, pk_r->ptr, (double*)s1->ptr);
+			t0.run(c, (const double*)s1->ptr, (double*)tt1->ptr);
+			d2.pack_b(c, (const double*)tt1->ptr, pk_t1->ptr);
+			d2.run_packed(c, pk_w->ptr, pk_t1->ptr, (double*)s2->ptr);
+			t1.run(c, (const double*)s2->ptr, (double*)tt2->ptr);
+			d3.pack_b(c, (const double*)tt2->ptr, pk_t2->ptr);
+			d3.run_packed(c, pk_k->ptr, pk_t2->ptr, y);
+			c.gemm_flops += flops;
+			return;
+		}
 		d1.run(c, x, r.data(), (double*)s1->ptr);
 		t0.run(c, (const double*)s1->ptr, (double*)tt1->ptr);
 		d2.run(c, w.data(), (const double*)tt1->ptr, (double*)s2->ptr);

@@ -461,6 +461,7 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 
 	std::vector<GemmOut> outs(r.nblocks);
 	std::vector<GemmContrib> cons;
+	std::vector<std::pair<int, int>> con_blocks;   // (s block, t block) of every contribution
 	std::vector<GemmTile> tiles[NUM_TILE_CLASSES];
 	// contracted block indices: all combinations over the first nmult - 1 contracted axes; the
 	// last one is fixed by the conservation law of s
@@ -523,6 +524,7 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 			CTG_CHECK(g.b_off + (k - 1) * g.sBk + (i64)(o.n - 1) * g.sBn < t.boff[bt] + t.block_size(bt),
 			          "dot: B operand out of range");
 			cons.push_back(g);
+			con_blocks.emplace_back(bs, bt);
 			flops += 2.0 * (double)o.m * (double)o.n * (double)k;
 			p.flops_cls[tile_class(o.m, o.n)] += 2.0 * (double)o.m * (double)o.n * (double)k;
 		}
@@ -625,6 +627,47 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 			tiles[k].swap(kept);
 		}
 	}
+	// tensor-core operands: one set of packed tile records per operand block, shared by every
+	// contribution that uses the block
+	std::vector<TcContrib> tcons;
+	std::vector<TcPack> apacks, bpacks;
+	if (precision == GEMM_BF16X3)
+	{
+		std::unordered_map<int, i64> abase, bbase;
+		tcons.resize(cons.size());
+		for (size_t ci = 0; ci < cons.size(); ci++)
+		{
+			const GemmContrib& g = cons[ci];
+			const int bs = con_blocks[ci].first, bt = con_blocks[ci].second;
+			const int kt = (g.k + TC_K - 1) / TC_K;
+			// rows of the A view of block bs and of the B view of block bt
+			const i64* sd = s.dims(bs);
+			const i64* td = t.dims(bt);
+			const int am = (int)prod(sd + (axs == AX_LEADING ? nmult : 0), s.ndim - nmult);
+			const int bn = (int)prod(td + (axt == AX_LEADING ? nmult : 0), t.ndim - nmult);
+			auto ia = abase.find(bs);
+			if (ia == abase.end())
+			{
+				const i64 base = (i64)apacks.size();
+				const int mtiles = (am + TC_A_ROWS - 1) / TC_A_ROWS;
+				for (int mt = 0; mt < mtiles; mt++)
+					for (int j = 0; j < kt; j++)
+						apacks.push_back(TcPack{g.a_off, am, g.k, g.sAm, g.sAk, mt * TC_A_ROWS, j * TC_K, base + mt * kt + j});
+				ia = abase.emplace(bs, base).first;
+			}
+			auto ib = bbase.find(bt);
+			if (ib == bbase.end())
+			{
+				const i64 base = (i64)bpacks.size();
+				const int ntiles_b = (bn + TC_B_ROWS - 1) / TC_B_ROWS;
+				for (int nt = 0; nt < ntiles_b; nt++)
+					for (int j = 0; j < kt; j++)
+						bpacks.push_back(TcPack{g.b_off, bn, g.k, g.sBn, g.sBk, nt * TC_B_ROWS, j * TC_K, base + nt * kt + j});
+				ib = bbase.emplace(bt, base).first;
+			}
+			tcons[ci] = TcContrib{ia->second, ib->second, kt, 0};
+		}
+	}
 	g_plan_stage[2] += host_seconds() - ts0;
 	ts0 = host_seconds();
 	p.precision = precision;
@@ -638,7 +681,13 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	size_t o_tiles[NUM_TILE_CLASSES];
 	for (int k = 0; k < NUM_TILE_CLASSES; k++) o_tiles[k] = pk.add(tiles[k]);
 	const size_t o_splits = pk.add(splits);
+	const size_t o_tcons = pk.add(tcons), o_apacks = pk.add(apacks), o_bpacks = pk.add(bpacks);
 	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	p.tcons = at<TcContrib>(p.desc, o_tcons);
+	p.apacks = at<TcPack>(p.desc, o_apacks);
+	p.bpacks = at<TcPack>(p.desc, o_bpacks);
+	p.a_recs = (i64)apacks.size();
+	p.b_recs = (i64)bpacks.size();
 	p.outs = at<GemmOut>(p.desc, o_outs);
 	p.cons = at<GemmContrib>(p.desc, o_cons);
 	p.splits = at<GemmSplit>(p.desc, o_splits);
@@ -662,19 +711,11 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 	{
 		if (ntiles[0] > 0)
 		{
-			// both operands split once into BF16 hi / lo arrays with their FP64 layout
-			DBuf ab(&c, (size_t)(a_entries + b_entries) * 2 * sizeof(uint16_t));
-			uint16_t* ahi = (uint16_t*)ab.ptr;
-			uint16_t* alo = ahi + a_entries;
-			uint16_t* bhi = alo + a_entries;
-			uint16_t* blo = bhi + b_entries;
-			{
-				KScope ks(c, K_GEMM_TC, 2, 0, 12.0 * (double)(a_entries + b_entries));
-				launch_split_bf16(A, a_entries, ahi, alo, c.stream());
-				launch_split_bf16(B, b_entries, bhi, blo, c.stream());
-			}
-			KScope ks(c, K_GEMM_TC, 1, flops_cls[0], 0);
-			launch_gemm_bf16x3(ntiles[0], tiles[0], outs, cons, ahi, alo, bhi, blo, C, c.tc_error(), c.stream());
+			DBuf apk(&c, (size_t)std::max<i64>(a_recs, 1) * TC_A_REC_BYTES);
+			DBuf bpk(&c, (size_t)std::max<i64>(b_recs, 1) * TC_B_REC_BYTES);
+			pack_a(c, A, apk.ptr);
+			pack_b(c, B, bpk.ptr);
+			run_packed(c, apk.ptr, bpk.ptr, C);
 		}
 		c.gemm_flops += flops;
 		return;
@@ -692,6 +733,27 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 		launch_gemm_reduce(nsplits, splits, outs, w, C, c.stream());
 	}
 	c.gemm_flops += flops;
+}
+
+void DotPlan::pack_a(Ctx& c, const double* A, void* apack) const
+{
+	KScope ks(c, K_GEMM_TC, 1, 0, 8.0 * (double)a_entries + (double)a_recs * TC_A_REC_BYTES);
+	launch_tc_pack((int)a_recs, apacks, 1, A, apack, c.stream());
+}
+
+void DotPlan::pack_b(Ctx& c, const double* B, void* bpack) const
+{
+	KScope ks(c, K_GEMM_TC, 1, 0, 8.0 * (double)b_entries + (double)b_recs * TC_B_REC_BYTES);
+	launch_tc_pack((int)b_recs, bpacks, 0, B, bpack, c.stream());
+}
+
+void DotPlan::run_packed(Ctx& c, const void* apack, const void* bpack, double* C) const
+{
+	if (ntiles[0] > 0)
+	{
+		KScope ks(c, K_GEMM_TC, 1, flops_cls[0], 0);
+		launch_gemm_tc(ntiles[0], tiles[0], outs, tcons, apack, bpack, C, c.tc_error(), c.stream());
+	}
 }
 
 // ------------------------------------------------------------------------------------

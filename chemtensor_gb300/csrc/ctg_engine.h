@@ -165,10 +165,19 @@ struct DotPlan {
 	int nsplits = 0;
 	DBufPtr work;                        // their partial sums
 	i64 a_entries = 0, b_entries = 0;    // entries of the two operand tensors
+	// tensor-core path: packed operand records (see launch_tc_pack) and per-contribution records
+	const TcContrib* tcons = nullptr;
+	const TcPack* apacks = nullptr;
+	const TcPack* bpacks = nullptr;
+	i64 a_recs = 0, b_recs = 0;
 	double flops = 0;
 	double flops_cls[NUM_TILE_CLASSES] = {0, 0, 0};
 	int precision = GEMM_FP64;
 	void run(Ctx& c, const double* A, const double* B, double* C) const;
+	// tensor-core path in parts, so that an operand used by many runs is packed once
+	void pack_a(Ctx& c, const double* A, void* apack) const;      // a_recs * TC_A_REC_BYTES bytes
+	void pack_b(Ctx& c, const double* B, void* bpack) const;      // b_recs * TC_B_REC_BYTES bytes
+	void run_packed(Ctx& c, const void* apack, const void* bpack, double* C) const;
 };
 DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision = GEMM_FP64);
 

@@ -1,19 +1,20 @@
 // ctg_gemm_tc.cu - grouped block GEMM on the 5th-generation tensor cores (tcgen05), split-BF16.
 //
-// Same work lists as the FP64 grouped GEMM (GemmOut / GemmContrib / GemmTile): every output block
-// C = sum_j op(A_j) op(B_j) with arbitrary element strides for the operands. Each FP64 operand
-// value x is split into x_hi = bf16(x) and x_lo = bf16(x - x_hi) once per product by k_split_bf16
-// (into two BF16 arrays with the operand's layout), and the product is taken as
+// Same work lists as the FP64 grouped GEMM (GemmOut / GemmTile) with one TcContrib per
+// contribution: every output block C = sum_j op(A_j) op(B_j). Each FP64 operand value x is split
+// into x_hi = bf16(x) and x_lo = bf16(x - x_hi), and the product is taken as
 // A_hi B_hi + A_hi B_lo + A_lo B_hi (the 3-product split-BF16 form; the dropped A_lo B_lo term and
 // the FP32 accumulation give a relative error of about 2^-16). Output in FP64.
 //
-// Per CTA: one 128 x TC_BN tile of one output block. Four warps stage the BF16 operand tiles into
-// shared memory in the canonical no-swizzle K-major layout of the tensor-core shared-memory
-// descriptors, double-buffered: while the tensor cores work on one stage the next one is loaded.
-// One thread issues the tcgen05.mma instructions into an FP32 accumulator in tensor memory and
-// commits each stage to that stage's mbarrier; the epilogue reads the accumulator with tcgen05.ld
-// and writes FP64. Every wait on an mbarrier is bounded: on timeout the CTA records an error flag,
-// stops issuing work, frees its tensor memory and returns.
+// k_tc_pack writes the operands as records of K-major tiles (hi and lo, canonical no-swizzle
+// core-matrix layout of the tensor-core shared-memory descriptors), so that the GEMM moves a tile
+// into shared memory with one bulk copy. k_gemm_tc: one CTA per 128 x 64 output tile; one thread
+// runs a two-stage pipeline - bulk copies of the A and B records of k chunk t complete on stage
+// t's "full" mbarrier (expect-tx), the tcgen05.mma instructions of chunk t - 1 (3 products x 4
+// k-steps of 16) accumulate in FP32 in tensor memory and are committed to that stage's "done"
+// mbarrier, which frees the stage for chunk t + 1. The epilogue reads the accumulator with
+// tcgen05.ld and writes FP64. Every wait is bounded: on timeout the CTA records an error flag,
+// stops issuing work, waits (bounded) for its copies in flight, frees its tensor memory and returns.
 #include <algorithm>
 
 #include <cuda_bf16.h>
@@ -35,9 +36,11 @@ constexpr int TC_LBO = 128;                // bytes between core matrices adjace
 constexpr int TC_SBO = (TC_BK / 8) * 128;  // bytes between core matrices adjacent in M / N
 constexpr int A_TILE_BYTES = TC_BM * TC_BK * 2;
 constexpr int B_TILE_BYTES = TC_BN * TC_BK * 2;
-constexpr int STAGE_BYTES = 2 * A_TILE_BYTES + 2 * B_TILE_BYTES;   // hi and lo of A and B
+constexpr int STAGE_BYTES = 2 * A_TILE_BYTES + 2 * B_TILE_BYTES;   // one A record + one B record
 constexpr int TC_STAGES = 2;
-constexpr int TC_SMEM_BYTES = TC_STAGES * STAGE_BYTES + 64;
+constexpr int TC_SMEM_BYTES = TC_STAGES * STAGE_BYTES + 128;
+static_assert(2 * A_TILE_BYTES == TC_A_REC_BYTES && 2 * B_TILE_BYTES == TC_B_REC_BYTES, "record layout");
+static_assert(TC_BM == TC_A_ROWS && TC_BN == TC_B_ROWS && TC_BK == TC_K, "tile shape");
 constexpr long long TC_WAIT_LIMIT = 1ll << 26;   // spins before a wait is declared failed
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -112,6 +115,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
 	return false;
 }
 
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// global -> shared bulk copy completing on an mbarrier (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+	             "l"(src), "r"(bytes), "r"(mbar)
+	             : "memory");
+}
+
 __device__ __forceinline__ void fence_async_smem()
 {
 	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -120,28 +136,40 @@ __device__ __forceinline__ void fence_async_smem()
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__global__ void __launch_bounds__(256)
-k_split_bf16(const double* __restrict__ x, i64 n, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo)
+template <int R>
+__global__ void __launch_bounds__(128) k_tc_pack(const TcPack* __restrict__ packs, const double* __restrict__ src,
+                                                 unsigned char* __restrict__ dst)
 {
-	for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+	const TcPack p = packs[blockIdx.x];
+	unsigned char* hi = dst + p.rec * (i64)(2 * R * TC_BK * 2);
+	unsigned char* lo = hi + R * TC_BK * 2;
+	for (int e = threadIdx.x; e < R * TC_BK; e += blockDim.x)
 	{
+		// consecutive threads read consecutive addresses along the unit-stride index
+		int i, kk;
+		if (p.s_k == 1) { kk = e % TC_BK; i = e / TC_BK; }
+		else { i = e % R; kk = e / R; }
+		const int gi = p.row0 + i, gk = p.k0 + kk;
 		// FP32 keeps 24 bits of x, more than the 16 that hi + lo carry
-		const float f = (float)x[i];
+		float f = 0.0f;
+		if (gi < p.rows && gk < p.k) f = (float)src[p.src + (i64)gi * p.s_row + (i64)gk * p.s_k];
 		const __nv_bfloat16 h = __float2bfloat16_rn(f);
-		hi[i] = h;
-		lo[i] = __float2bfloat16_rn(f - __bfloat162float(h));
+		const uint32_t so = canon_offset(i, kk);
+		*(__nv_bfloat16*)(hi + so) = h;
+		*(__nv_bfloat16*)(lo + so) = __float2bfloat16_rn(f - __bfloat162float(h));
 	}
 }
 
 __global__ void __launch_bounds__(TC_THREADS)
-k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const GemmContrib* __restrict__ cons,
-              const unsigned short* __restrict__ Ahi, const unsigned short* __restrict__ Alo,
-              const unsigned short* __restrict__ Bhi, const unsigned short* __restrict__ Blo, double* __restrict__ C,
-              int* __restrict__ error)
+k_gemm_tc(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const TcContrib* __restrict__ tcons,
+          const unsigned char* __restrict__ apack, const unsigned char* __restrict__ bpack, double* __restrict__ C,
+          int* __restrict__ error)
 {
 	extern __shared__ __align__(1024) unsigned char smem[];
-	uint64_t* mbar = (uint64_t*)(smem + TC_STAGES * STAGE_BYTES);     // one per stage
-	uint32_t* tmem_slot = (uint32_t*)(mbar + TC_STAGES);
+	uint64_t* full = (uint64_t*)(smem + TC_STAGES * STAGE_BYTES);     // copies of a stage landed
+	uint64_t* done = full + TC_STAGES;                                 // MMAs of a stage finished
+	uint32_t* tmem_slot = (uint32_t*)(done + TC_STAGES);
+	int* sh_ok = (int*)(tmem_slot + 1);
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const GemmTile tile = tiles[blockIdx.x];
 	const GemmOut o = outs[tile.out];
@@ -154,104 +182,101 @@ k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ ou
 		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 	}
 	if (tid == 0)
-		for (int s = 0; s < TC_STAGES; s++) mbar_init(smem_u32(mbar + s), 1);
+	{
+		for (int s = 0; s < TC_STAGES; s++)
+		{
+			mbar_init(smem_u32(full + s), 1);
+			mbar_init(smem_u32(done + s), 1);
+		}
+		*sh_ok = 1;
+	}
 	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();
 	const uint32_t tmem = *tmem_slot;
-	const uint32_t idesc = make_idesc();
-	bool ok = true;
-	int chunk = 0;                                      // k chunks issued so far
+	int nchunks = 0;
+	for (int c = o.c0; c < o.c0 + o.nc; c++) nchunks += tcons[c].kt;
 
-	for (int c = o.c0; c < o.c0 + o.nc && ok; c++)
+	if (tid == 0 && nchunks > 0)
 	{
-		const GemmContrib g = cons[c];
-		for (int k0 = 0; k0 < g.k && ok; k0 += TC_BK, chunk++)
+		const uint32_t idesc = make_idesc();
+		const int mt = tile.m0 / TC_BM, nt = tile.n0 / TC_BN;
+		int lc = o.c0, lk = 0;           // load cursor: contribution, k tile
+		bool ok = true;
+		int issued = 0;                  // chunks whose copies were issued
+		for (int t = 0; t <= nchunks && ok; t++)
 		{
-			const int st = chunk % TC_STAGES;
-			unsigned char* a_hi = smem + st * STAGE_BYTES;
-			unsigned char* a_lo = a_hi + A_TILE_BYTES;
-			unsigned char* b_hi = a_lo + A_TILE_BYTES;
-			unsigned char* b_lo = b_hi + B_TILE_BYTES;
-			if (chunk >= TC_STAGES)
+			if (t < nchunks)
 			{
-				// the MMAs that read this stage (chunk - TC_STAGES) must be complete
-				const bool arrived = mbar_wait(smem_u32(mbar + st), (uint32_t)((chunk / TC_STAGES - 1) & 1));
-				ok = __syncthreads_and(arrived ? 1 : 0) != 0;
-				if (!ok) break;
+				const int st = t % TC_STAGES;
+				if (t >= TC_STAGES && !mbar_wait(smem_u32(done + st), (uint32_t)(((t - TC_STAGES) / TC_STAGES) & 1)))
+				{
+					ok = false;
+					break;
+				}
+				while (lk >= tcons[lc].kt) { lc++; lk = 0; }
+				const TcContrib g = tcons[lc];
+				const unsigned char* arec = apack + (g.a_rec + (i64)mt * g.kt + lk) * TC_A_REC_BYTES;
+				const unsigned char* brec = bpack + (g.b_rec + (i64)nt * g.kt + lk) * TC_B_REC_BYTES;
+				const uint32_t sbase = smem_u32(smem + st * STAGE_BYTES);
+				mbar_expect_tx(smem_u32(full + st), (uint32_t)STAGE_BYTES);
+				bulk_copy(sbase, arec, (uint32_t)TC_A_REC_BYTES, smem_u32(full + st));
+				bulk_copy(sbase + (uint32_t)TC_A_REC_BYTES, brec, (uint32_t)TC_B_REC_BYTES, smem_u32(full + st));
+				issued = t + 1;
+				lk++;
+			}
+			if (t >= 1)
+			{
+				const int u = t - 1, su = u % TC_STAGES;
+				if (!mbar_wait(smem_u32(full + su), (uint32_t)((u / TC_STAGES) & 1)))
+				{
+					ok = false;
+					break;
+				}
 				tc_fence_after();
-			}
-			// A tile: 128 x 64, element (i, kk) -> (m0 + i, k0 + kk); zero outside the block
-			for (int e = tid; e < TC_BM * TC_BK; e += TC_THREADS)
-			{
-				int i, kk;
-				if (g.sAk == 1) { kk = e % TC_BK; i = e / TC_BK; }
-				else { i = e % TC_BM; kk = e / TC_BM; }
-				const int gi = tile.m0 + i, gk = k0 + kk;
-				unsigned short h = 0, l = 0;
-				if (gi < o.m && gk < g.k)
-				{
-					const i64 off = g.a_off + (i64)gi * g.sAm + (i64)gk * g.sAk;
-					h = Ahi[off];
-					l = Alo[off];
-				}
-				const uint32_t so = canon_offset(i, kk);
-				*(unsigned short*)(a_hi + so) = h;
-				*(unsigned short*)(a_lo + so) = l;
-			}
-			// B tile as N x K (K-major): element (j, kk) = op(B)(k0 + kk, n0 + j)
-			for (int e = tid; e < TC_BN * TC_BK; e += TC_THREADS)
-			{
-				int j, kk;
-				if (g.sBk == 1) { kk = e % TC_BK; j = e / TC_BK; }
-				else { j = e % TC_BN; kk = e / TC_BN; }
-				const int gj = tile.n0 + j, gk = k0 + kk;
-				unsigned short h = 0, l = 0;
-				if (gj < o.n && gk < g.k)
-				{
-					const i64 off = g.b_off + (i64)gk * g.sBk + (i64)gj * g.sBn;
-					h = Bhi[off];
-					l = Blo[off];
-				}
-				const uint32_t so = canon_offset(j, kk);
-				*(unsigned short*)(b_hi + so) = h;
-				*(unsigned short*)(b_lo + so) = l;
-			}
-			fence_async_smem();
-			tc_fence_before();
-			__syncthreads();
-			tc_fence_after();
-			if (tid == 0)
-			{
-				const int ksteps = (min(TC_BK, g.k - k0) + 15) / 16;
-				for (int s = 0; s < ksteps; s++)
+				const uint32_t a_hi = smem_u32(smem + su * STAGE_BYTES);
+				const uint32_t a_lo = a_hi + A_TILE_BYTES;
+				const uint32_t b_hi = a_lo + A_TILE_BYTES;
+				const uint32_t b_lo = b_hi + B_TILE_BYTES;
+				for (int s = 0; s < TC_BK / 16; s++)
 				{
 					const uint32_t koff = (uint32_t)s * 2 * TC_LBO;
-					const uint64_t dah = make_desc(smem_u32(a_hi) + koff), dal = make_desc(smem_u32(a_lo) + koff);
-					const uint64_t dbh = make_desc(smem_u32(b_hi) + koff), dbl = make_desc(smem_u32(b_lo) + koff);
-					mma_bf16(tmem, dah, dbh, idesc, chunk > 0 || s > 0);
+					const uint64_t dah = make_desc(a_hi + koff), dal = make_desc(a_lo + koff);
+					const uint64_t dbh = make_desc(b_hi + koff), dbl = make_desc(b_lo + koff);
+					mma_bf16(tmem, dah, dbh, idesc, u > 0 || s > 0);
 					mma_bf16(tmem, dah, dbl, idesc, true);
 					mma_bf16(tmem, dal, dbh, idesc, true);
 				}
-				mma_commit(smem_u32(mbar + st));
+				mma_commit(smem_u32(done + su));
 			}
 		}
+		if (ok)
+		{
+			// the last commit tracks every MMA issued before it
+			const int last = nchunks - 1;
+			ok = mbar_wait(smem_u32(done + last % TC_STAGES), (uint32_t)((last / TC_STAGES) & 1));
+		}
+		else
+		{
+			// let the copies in flight land before the CTA's shared memory is released
+			for (int u = issued - TC_STAGES; u < issued; u++)
+				if (u >= 0) mbar_wait(smem_u32(full + u % TC_STAGES), (uint32_t)((u / TC_STAGES) & 1));
+		}
+		if (!ok)
+		{
+			*sh_ok = 0;
+			atomicExch(error, 1);
+		}
 	}
-	if (ok && chunk > 0)
-	{
-		// the last commit tracks every MMA issued before it
-		const int last = chunk - 1;
-		const bool arrived = mbar_wait(smem_u32(mbar + last % TC_STAGES), (uint32_t)((last / TC_STAGES) & 1));
-		ok = __syncthreads_and(arrived ? 1 : 0) != 0;
-	}
-	if (!ok && lane == 0) atomicExch(error, 1);
+	tc_fence_before();
+	__syncthreads();
 	tc_fence_after();
+	const bool have_acc = *sh_ok && nchunks > 0;
 
 	// epilogue: each warp owns 32 accumulator rows (tensor-memory lanes 32 w .. 32 w + 31)
 	const int row = tile.m0 + warp * 32 + lane;
 	double* cblk = C + o.c_off;
-	const bool have_acc = ok && chunk > 0;
 	for (int cc = 0; cc < TC_BN; cc += 16)
 	{
 		uint32_t v[16];
@@ -292,28 +317,26 @@ k_gemm_bf16x3(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ ou
 int tc_tile_rows() { return TC_BM; }
 int tc_tile_cols() { return TC_BN; }
 
-void launch_split_bf16(const double* x, i64 n, void* hi, void* lo, cudaStream_t st)
+void launch_tc_pack(int nrec, const TcPack* packs, int a_side, const double* src, void* dst, cudaStream_t st)
 {
-	if (n <= 0) return;
-	const i64 blocks = std::min<i64>((n + 255) / 256, 4 * 152);
-	k_split_bf16<<<(int)blocks, 256, 0, st>>>(x, n, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo);
+	if (nrec <= 0) return;
+	if (a_side) k_tc_pack<TC_A_ROWS><<<nrec, 128, 0, st>>>(packs, src, (unsigned char*)dst);
+	else k_tc_pack<TC_B_ROWS><<<nrec, 128, 0, st>>>(packs, src, (unsigned char*)dst);
 	CTG_CUDA(cudaGetLastError());
 }
 
-void launch_gemm_bf16x3(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
-                        const void* Ahi, const void* Alo, const void* Bhi, const void* Blo, double* C, int* error,
-                        cudaStream_t st)
+void launch_gemm_tc(int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons, const void* apack,
+                    const void* bpack, double* C, int* error, cudaStream_t st)
 {
 	if (ntiles <= 0) return;
 	static bool attr_set = false;
 	if (!attr_set)
 	{
-		CTG_CUDA(cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES));
+		CTG_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES));
 		attr_set = true;
 	}
-	k_gemm_bf16x3<<<ntiles, TC_THREADS, TC_SMEM_BYTES, st>>>(tiles, outs, cons, (const unsigned short*)Ahi,
-	                                                           (const unsigned short*)Alo, (const unsigned short*)Bhi,
-	                                                           (const unsigned short*)Blo, C, error);
+	k_gemm_tc<<<ntiles, TC_THREADS, TC_SMEM_BYTES, st>>>(tiles, outs, tcons, (const unsigned char*)apack,
+	                                                       (const unsigned char*)bpack, C, error);
 	CTG_CUDA(cudaGetLastError());
 }
 

@@ -56,16 +56,34 @@ void launch_gemm_reduce(int nsplit, const GemmSplit* splits, const GemmOut* outs
                         cudaStream_t st);
 
 // Same work lists on the tcgen05 tensor cores, split-BF16 (hi*hi + hi*lo + lo*hi, FP32
-// accumulation, FP64 out); tiles of tc_tile_rows() x tc_tile_cols(). The operands come as BF16 hi
-// and lo arrays in the layout of the FP64 operands (launch_split_bf16). *error becomes 1 if a
-// bounded wait inside the kernel timed out.
+// accumulation, FP64 out); output tiles of tc_tile_rows() x tc_tile_cols().
+//
+// Operands are packed first: every operand block is cut into K-major tiles of 128 (A) or 64 (B)
+// rows by 64 k, and each tile is stored as one record holding the BF16 hi part and the BF16 lo part
+// (hi = bf16(x), lo = bf16(x - hi)) in the canonical no-swizzle core-matrix layout of the tcgen05
+// shared-memory descriptors; zero outside the block. A record moves into shared memory with one
+// bulk copy (cp.async.bulk). *error becomes 1 if a bounded wait inside the GEMM timed out.
 int tc_tile_rows();
 int tc_tile_cols();
-// hi[i] = bf16(x[i]), lo[i] = bf16(x[i] - hi[i]) for i < n (2-byte elements)
-void launch_split_bf16(const double* x, i64 n, void* hi, void* lo, cudaStream_t st);
-void launch_gemm_bf16x3(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
-                        const void* Ahi, const void* Alo, const void* Bhi, const void* Blo, double* C, int* error,
-                        cudaStream_t st);
+constexpr int TC_A_ROWS = 128, TC_B_ROWS = 64, TC_K = 64;
+constexpr i64 TC_A_REC_BYTES = 2LL * TC_A_ROWS * TC_K * 2;   // 32 KiB
+constexpr i64 TC_B_REC_BYTES = 2LL * TC_B_ROWS * TC_K * 2;   // 16 KiB
+struct TcPack {
+	i64 src;           // element offset of (row 0, k 0) of the block in the FP64 operand
+	int rows, k;       // block extent
+	int s_row, s_k;    // element strides of rows and k
+	int row0, k0;      // tile origin
+	i64 rec;           // destination record
+};
+struct TcContrib {
+	i64 a_rec, b_rec;  // first record of the A block (tiles mt * kt + j) and of the B block (nt * kt + j)
+	int kt;            // k tiles
+	int pad;
+};
+// a_side: records of TC_A_ROWS rows (A operand), else TC_B_ROWS (B operand)
+void launch_tc_pack(int nrec, const TcPack* packs, int a_side, const double* src, void* dst, cudaStream_t st);
+void launch_gemm_tc(int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons, const void* apack,
+                    const void* bpack, double* C, int* error, cudaStream_t st);
 
 // ---- data movement -----------------------------------------------------------
 // Generic per-block permutation: dst block (row-major over dims) gathers
