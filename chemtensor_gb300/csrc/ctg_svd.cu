@@ -450,6 +450,200 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 	return x;
 }
 
+// Householder QR with column pivoting of the scaled block over a whole cluster. Column j lives in
+// the shared memory of CTA j % cl; columns are not moved: every step the CTAs exchange their
+// largest remaining trailing norm (distributed shared memory, one cluster barrier), the owner of the
+// pivot column forms the reflector and writes it into every CTA's shared memory (second barrier),
+// and each CTA applies it to its own remaining columns and downdates their norms (recomputed when
+// cancellation has eaten more than sqrt(eps) of the last exact value, as LAPACK's xLAQP2). At the
+// end the columns go to global memory in pivot order (the layout of qr_pivoted_cta: R in the upper
+// triangle, reflector k below the diagonal of column k, perm[k] the source column), followed by the
+// columns beyond the numerical rank in source order. Returns the rank; writes tau, perm, misc.
+__device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, const double* ab, bool tall, int n, int M, int N,
+                                  int cl, const SvdScratch& xs)
+{
+	const int rank = (int)cluster.block_rank();
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int nloc_max = (N + cl - 1) / cl;
+	const int nloc = (N - rank + cl - 1) / cl;           // columns j = rank + cl * jl, jl < nloc
+	double* qcol = smem;                                 // nloc_max x M
+	double* qnrm = qcol + (i64)nloc_max * M;
+	double* qref = qnrm + nloc_max;
+	double* vbuf = qref + nloc_max;                      // reflector of the current step (rows k..M-1)
+	double* cand = vbuf + M;                             // [cl] best squared norm per CTA
+	double* part = cand + 16;                            // [cl] partial Frobenius sums
+	double* scal = part + 16;                            // [0] tau of the current step
+	int* cidx = (int*)(scal + 2);                        // [cl] column of the best norm per CTA
+	int* qdone = cidx + 16;                              // [nloc_max] step that took the column, or -1
+	__shared__ double red[NWARPS];
+	__shared__ double sh_beta, sh_scale;
+
+	// load the own columns (B oriented tall) and their squared sums
+	double psum = 0;
+	for (i64 e = tid; e < (i64)nloc * M; e += SVD_THREADS)
+	{
+		const int jl = (int)(e / M), row = (int)(e % M);
+		const int col = rank + cl * jl;
+		const double x = tall ? ab[(i64)row * n + col] : ab[(i64)col * n + row];
+		qcol[e] = x;
+		psum = fma(x, x, psum);
+	}
+	psum = block_sum(psum, red);
+	if (tid < cl) *cluster.map_shared_rank(part + rank, (unsigned)tid) = psum;
+	cluster.sync();
+	double total = 0;
+	for (int i = 0; i < cl; i++) total += part[i];
+	// exact power-of-two scaling to a Frobenius norm in [1/2, 1)
+	int ex = 0;
+	if (total > 0) frexp(sqrt(total), &ex);
+	const double sc = ldexp(1.0, -ex);
+	for (i64 e = tid; e < (i64)nloc * M; e += SVD_THREADS) qcol[e] *= sc;
+	__syncthreads();
+	for (int jl = warp; jl < nloc; jl += NWARPS)
+	{
+		const double* w = qcol + (i64)jl * M;
+		double acc = 0;
+		for (int i = lane; i < M; i += 32) acc = fma(w[i], w[i], acc);
+		acc = warp_sum(acc);
+		if (lane == 0)
+		{
+			qnrm[jl] = qref[jl] = acc;
+			qdone[jl] = -1;
+		}
+	}
+	const double thresh = DBL_EPSILON * DBL_EPSILON * total * sc * sc;
+	const double tol3z = sqrt(DBL_EPSILON);
+	__syncthreads();
+
+	int r = 0;
+	for (int k = 0; k < N; k++)
+	{
+		// a. this CTA's best remaining column, to every CTA
+		if (warp == 0)
+		{
+			double best = -1;
+			int bi = N;
+			for (int jl = lane; jl < nloc; jl += 32)
+				if (qdone[jl] < 0 && qnrm[jl] > best) { best = qnrm[jl]; bi = rank + cl * jl; }
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1)
+			{
+				const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+				const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+				if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+			}
+			if (lane < cl)
+			{
+				*cluster.map_shared_rank(cand + rank, (unsigned)lane) = best;
+				*cluster.map_shared_rank(cidx + rank, (unsigned)lane) = bi;
+			}
+		}
+		cluster.sync();
+		// b. the pivot (identical in every CTA)
+		double pv = -1;
+		int p = N;
+		for (int i = 0; i < cl; i++)
+			if (cand[i] > pv || (cand[i] == pv && cidx[i] < p)) { pv = cand[i]; p = cidx[i]; }
+		if (pv <= thresh || pv <= 0.0 || p >= N) break;
+		// c. the owner forms the reflector and sends it to every CTA
+		if (p % cl == rank)
+		{
+			double* w = qcol + (i64)(p / cl) * M;
+			double part2 = 0;
+			for (int i = k + 1 + tid; i < M; i += SVD_THREADS) part2 = fma(w[i], w[i], part2);
+			const double xnorm2 = block_sum(part2, red);
+			if (tid == 0)
+			{
+				const double alpha = w[k];
+				double tk;
+				if (xnorm2 == 0.0)
+				{
+					tk = 0.0;
+					sh_beta = alpha;
+					sh_scale = 0.0;
+				}
+				else
+				{
+					const double beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
+					tk = (beta - alpha) / beta;
+					sh_beta = beta;
+					sh_scale = 1.0 / (alpha - beta);
+				}
+				xs.tau[k] = tk;
+				for (int c2 = 0; c2 < cl; c2++) *cluster.map_shared_rank(scal, (unsigned)c2) = tk;
+				qdone[p / cl] = k;
+			}
+			__syncthreads();
+			for (int i = k + 1 + tid; i < M; i += SVD_THREADS) w[i] *= sh_scale;
+			__syncthreads();
+			if (tid == 0) w[k] = sh_beta;
+			// reflector v = (1, w[k+1 ..]) into every CTA's vbuf
+			for (i64 e = tid; e < (i64)(M - k) * cl; e += SVD_THREADS)
+			{
+				const int c2 = (int)(e / (M - k)), i = k + (int)(e % (M - k));
+				*cluster.map_shared_rank(vbuf + i, (unsigned)c2) = (i == k) ? 1.0 : w[i];
+			}
+		}
+		cluster.sync();
+		// d. apply the reflector to the own remaining columns, downdate their norms
+		const double tk = scal[0];
+		for (int jl = warp; jl < nloc; jl += NWARPS)
+		{
+			if (qdone[jl] >= 0) continue;
+			double* w = qcol + (i64)jl * M;
+			if (tk != 0.0)
+			{
+				double acc = 0;
+				for (int i = k + lane; i < M; i += 32) acc = fma(vbuf[i], w[i], acc);
+				acc = warp_sum(acc) * tk;
+				for (int i = k + lane; i < M; i += 32) w[i] -= acc * vbuf[i];
+			}
+			int recompute = 0;
+			if (lane == 0)
+			{
+				const double rkj = w[k];
+				const double v = fmax(fma(-rkj, rkj, qnrm[jl]), 0.0);
+				qnrm[jl] = v;
+				recompute = v <= tol3z * qref[jl];
+			}
+			if (__shfl_sync(0xffffffffu, recompute, 0))
+			{
+				double acc = 0;
+				for (int i = k + 1 + lane; i < M; i += 32) acc = fma(w[i], w[i], acc);
+				acc = warp_sum(acc);
+				if (lane == 0) qnrm[jl] = qref[jl] = acc;
+			}
+		}
+		__syncthreads();
+		r = k + 1;
+	}
+	// columns to global memory in pivot order, the remaining ones after them in source order
+	int* gdone = (int*)xs.T;                             // scratch until the Jacobi writes T
+	for (int jl = tid; jl < nloc; jl += SVD_THREADS) gdone[rank + cl * jl] = qdone[jl];
+	cluster.sync();
+	for (int jl = warp; jl < nloc; jl += NWARPS)
+	{
+		const int j = rank + cl * jl;
+		int pos = qdone[jl];
+		if (pos < 0)
+		{
+			int cnt = 0;
+			for (int j2 = lane; j2 < j; j2 += 32) cnt += __ldcg(gdone + j2) < 0 ? 1 : 0;
+			pos = r + (int)__reduce_add_sync(0xffffffffu, (unsigned)cnt);
+		}
+		const double* w = qcol + (i64)jl * M;
+		for (int i = lane; i < M; i += 32) xs.W[(i64)pos * M + i] = w[i];
+		if (lane == 0) xs.perm[pos] = j;
+	}
+	if (rank == 0 && tid == 0)
+	{
+		xs.misc[0] = (double)r;
+		xs.misc[1] = total;
+		xs.misc[2] = ldexp(1.0, ex);
+	}
+	return r;
+}
+
 __global__ void __launch_bounds__(SVD_THREADS)
 k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
            double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
@@ -471,8 +665,10 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	const bool stamp = phase_ts && rank == 0 && tid == 0;
 	if (stamp) phase_ts[8 * blk] = globaltimer();
 
-	// ---- 1. pivoted QR on the cluster's first CTA, of B scaled to a Frobenius norm in [1/2, 1) ----
-	if (rank == 0)
+	// ---- 1. pivoted QR of B scaled to a Frobenius norm in [1/2, 1): over the cluster, or on the
+	// single CTA of a one-CTA cluster ----
+	if (cl > 1) qr_pivoted_cluster(cluster, smem, ab, tall, n, M, N, cl, xs);
+	else
 	{
 		__shared__ double red[NWARPS];
 		double part = 0;
@@ -1037,6 +1233,10 @@ static i64 tour_smem_bytes(int M, int N, int cl)
 	const i64 jac = 4 * bsmax * 2 * N + 4 * bsmax + 3 * SVD_STEP_PAIRS + SVD_STEP_PAIRS / 2 + 16;
 	const i64 out = (i64)NWARPS * M;
 	i64 need = jac > out ? jac : out;
+	// distributed QR (clusters of more than one CTA): own columns, norms, reflector, exchange slots
+	const i64 nloc = (N + cl - 1) / cl;
+	const i64 qr = nloc * M + 2 * nloc + M + 16 + 16 + 2 + (16 + nloc + 1) / 2 + 8;
+	if (cl > 1 && qr > need) need = qr;
 	// pivoted QR staged in shared memory when the whole block fits
 	if ((i64)M * N * 8 <= SVD_SMEM_LIMIT && (i64)M * N > need) need = (i64)M * N;
 	return 8 * need;
