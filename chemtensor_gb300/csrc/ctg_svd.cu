@@ -239,6 +239,13 @@ __device__ __forceinline__ double make_double(float m, int e)
 	return __hiloint2double(hi, (fb & 0x7) << 29);
 }
 
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+	float y;
+	asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
+}
+
 // 2^k as a float for -126 <= k <= 127
 __device__ __forceinline__ float pow2f(int k)
 {
@@ -264,7 +271,7 @@ __device__ __forceinline__ bool rotation_params(double al, double be, double ga,
 	const float ma = mant_exp(al, ea), mb = mant_exp(be, eb), mg = mant_exp(ga, eg);
 	const int k2 = 2 * eg - ea - eb;
 	if (k2 < -120) return false;
-	if (k2 <= 0 && (mg * mg) / (ma * mb) * pow2f(k2) <= tol2) return false;
+	if (k2 <= 0 && __fdividef(mg * mg, ma * mb) * pow2f(k2) <= tol2) return false;
 	const double dl = be - al;
 	const bool neg = (dl < 0.0) != (ga < 0.0);
 	float tm, taum;
@@ -282,7 +289,7 @@ __device__ __forceinline__ bool rotation_params(double al, double be, double ga,
 		if (k >= 40)
 		{
 			// tan theta ~ 1 / (2 |zeta|), tan(theta / 2) ~ tan theta / 2
-			tm = 0.5f * mg / md;
+			tm = __fdividef(0.5f * mg, md);
 			te = -k;
 			taum = 0.5f * tm;
 		}
@@ -293,9 +300,10 @@ __device__ __forceinline__ bool rotation_params(double al, double be, double ga,
 		}
 		else
 		{
-			const float z = (md / mg) * pow2f(k);
-			tm = 1.0f / (z + sqrtf(fmaf(z, z, 1.0f)));
-			taum = tm / (1.0f + sqrtf(fmaf(tm, tm, 1.0f)));
+			// single-instruction approximations: the angle needs FP32 accuracy only
+			const float z = __fdividef(md, mg) * pow2f(k);
+			tm = __fdividef(1.0f, z + sqrt_approx(fmaf(z, z, 1.0f)));
+			taum = __fdividef(tm, 1.0f + sqrt_approx(fmaf(tm, tm, 1.0f)));
 		}
 	}
 	if (neg)
