@@ -431,7 +431,10 @@ std::vector<i64> fanout(const Meta& t, int ax, q32 q)
 
 int tile_class(int m, int n)
 {
+	// the tile that pads the block least (FP64 FMAs on padding cost as much as useful ones)
 	if (m <= 16 && n <= 16) return TILE_S;
+	if (m <= 16) return TILE_W;
+	if (n <= 16) return TILE_T;
 	if (m <= 32 || n <= 32) return TILE_M;
 	return TILE_L;
 }
@@ -552,6 +555,7 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 		}
 		const int cls = tile_class(o.m, o.n);
 		const int tr = tile_rows(cls), tc = tile_cols(cls);
+		whole.cls = cls;
 		for (int m0 = 0; m0 < o.m; m0 += tr)
 			for (int n0 = 0; n0 < o.n; n0 += tc)
 			{
@@ -675,6 +679,12 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	{
 		for (int k = 1; k < NUM_TILE_CLASSES; k++) p.flops_cls[0] += p.flops_cls[k], p.flops_cls[k] = 0;
 	}
+	// one launch covers every class: all tiles in one list
+	for (int k = 1; k < NUM_TILE_CLASSES; k++)
+	{
+		tiles[0].insert(tiles[0].end(), tiles[k].begin(), tiles[k].end());
+		tiles[k].clear();
+	}
 	Packer pk;
 	const size_t o_outs = pk.add(outs);
 	const size_t o_cons = pk.add(cons);
@@ -721,11 +731,10 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 		return;
 	}
 	double* w = work ? (double*)work->ptr : nullptr;
-	for (int k = 0; k < NUM_TILE_CLASSES; k++)
+	if (ntiles[0] > 0)
 	{
-		if (ntiles[k] == 0) continue;
-		KScope ks(c, K_GEMM, 1, flops_cls[k], 0);
-		launch_gemm_f64(k, ntiles[k], tiles[k], outs, cons, A, B, C, w, c.stream());
+		KScope ks(c, K_GEMM, 1, flops, 0);
+		launch_gemm_f64(ntiles[0], tiles[0], outs, cons, A, B, C, w, c.stream());
 	}
 	if (nsplits > 0)
 	{

@@ -157,8 +157,8 @@ Ctx& context_for_device(int device);
 struct DotPlan {
 	std::shared_ptr<const Meta> out;
 	DBufPtr desc;
-	int ntiles[NUM_TILE_CLASSES] = {0, 0, 0};
-	const GemmTile* tiles[NUM_TILE_CLASSES] = {nullptr, nullptr, nullptr};
+	int ntiles[NUM_TILE_CLASSES] = {};
+	const GemmTile* tiles[NUM_TILE_CLASSES] = {};
 	const GemmOut* outs = nullptr;
 	const GemmContrib* cons = nullptr;
 	const GemmSplit* splits = nullptr;   // tiles whose sum is split over several CTAs
@@ -171,7 +171,7 @@ struct DotPlan {
 	const TcPack* bpacks = nullptr;
 	i64 a_recs = 0, b_recs = 0;
 	double flops = 0;
-	double flops_cls[NUM_TILE_CLASSES] = {0, 0, 0};
+	double flops_cls[NUM_TILE_CLASSES] = {};
 	int precision = GEMM_FP64;
 	void run(Ctx& c, const double* A, const double* B, double* C) const;
 	// tensor-core path in parts, so that an operand used by many runs is packed once

@@ -7,15 +7,19 @@ namespace ctg {
 // grouped FP64 block GEMM (plain path; dense_tensor_dot_update, dense_tensor.c:1761-1837)
 // ------------------------------------------------------------------------------------
 
+constexpr int GEMM_THREADS = 256;     // 16 x 16 thread grid for every tile class
+constexpr int GEMM_SMEM_DOUBLES = 16 * (64 + 1) * 2;
+
 template <int BM, int BN, int BK, int TM, int TN>
-__global__ void __launch_bounds__((BM / TM) * (BN / TN))
-k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const GemmContrib* __restrict__ cons,
-           const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C, double* __restrict__ work)
+__device__ __forceinline__ void gemm_tile_f64(const GemmTile& tile, const GemmOut* __restrict__ outs,
+                                              const GemmContrib* __restrict__ cons, const double* __restrict__ A,
+                                              const double* __restrict__ B, double* __restrict__ C,
+                                              double* __restrict__ work, double* sm)
 {
 	constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
-	__shared__ double As[BK][BM + 1];
-	__shared__ double Bs[BK][BN + 1];
-	const GemmTile tile = tiles[blockIdx.x];
+	static_assert(NT == GEMM_THREADS && BK * (BM + 1 + BN + 1) <= GEMM_SMEM_DOUBLES, "tile class layout");
+	double (*As)[BM + 1] = reinterpret_cast<double (*)[BM + 1]>(sm);
+	double (*Bs)[BN + 1] = reinterpret_cast<double (*)[BN + 1]>(sm + BK * (BM + 1));
 	const GemmOut o = outs[tile.out];
 	const int tid = threadIdx.x;
 	const int tx = tid % NTX, ty = tid / NTX;
@@ -113,6 +117,22 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
 	}
 }
 
+__global__ void __launch_bounds__(GEMM_THREADS)
+k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const GemmContrib* __restrict__ cons,
+           const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C, double* __restrict__ work)
+{
+	__shared__ double sm[GEMM_SMEM_DOUBLES];
+	const GemmTile tile = tiles[blockIdx.x];
+	switch (tile.cls)
+	{
+	case TILE_L: gemm_tile_f64<64, 64, 16, 4, 4>(tile, outs, cons, A, B, C, work, sm); break;
+	case TILE_M: gemm_tile_f64<32, 32, 16, 2, 2>(tile, outs, cons, A, B, C, work, sm); break;
+	case TILE_W: gemm_tile_f64<16, 64, 16, 1, 4>(tile, outs, cons, A, B, C, work, sm); break;
+	case TILE_T: gemm_tile_f64<64, 16, 16, 4, 1>(tile, outs, cons, A, B, C, work, sm); break;
+	default:     gemm_tile_f64<16, 16, 16, 1, 1>(tile, outs, cons, A, B, C, work, sm); break;
+	}
+}
+
 // sums the partial tiles of each split tile in order of the split index
 __global__ void __launch_bounds__(256)
 k_gemm_reduce(const GemmSplit* __restrict__ splits, const GemmOut* __restrict__ outs, const double* __restrict__ work,
@@ -139,19 +159,31 @@ void launch_gemm_reduce(int nsplit, const GemmSplit* splits, const GemmOut* outs
 	CTG_CUDA(cudaGetLastError());
 }
 
-int tile_rows(int cls) { return cls == TILE_L ? 64 : (cls == TILE_M ? 32 : 16); }
-int tile_cols(int cls) { return cls == TILE_L ? 64 : (cls == TILE_M ? 32 : 16); }
-
-void launch_gemm_f64(int cls, int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
-                     const double* A, const double* B, double* C, double* work, cudaStream_t st)
+int tile_rows(int cls)
 {
-	if (ntiles <= 0) return;
 	switch (cls)
 	{
-	case TILE_L: k_gemm_f64<64, 64, 16, 4, 4><<<ntiles, 256, 0, st>>>(tiles, outs, cons, A, B, C, work); break;
-	case TILE_M: k_gemm_f64<32, 32, 16, 4, 4><<<ntiles, 64, 0, st>>>(tiles, outs, cons, A, B, C, work); break;
-	default:     k_gemm_f64<16, 16, 16, 2, 2><<<ntiles, 64, 0, st>>>(tiles, outs, cons, A, B, C, work); break;
+	case TILE_L: case TILE_T: return 64;
+	case TILE_M: return 32;
+	default: return 16;
 	}
+}
+
+int tile_cols(int cls)
+{
+	switch (cls)
+	{
+	case TILE_L: case TILE_W: return 64;
+	case TILE_M: return 32;
+	default: return 16;
+	}
+}
+
+void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons, const double* A,
+                     const double* B, double* C, double* work, cudaStream_t st)
+{
+	if (ntiles <= 0) return;
+	k_gemm_f64<<<ntiles, GEMM_THREADS, 0, st>>>(tiles, outs, cons, A, B, C, work);
 	CTG_CUDA(cudaGetLastError());
 }
 

@@ -35,6 +35,7 @@ struct GemmTile {
 	int m0, n0;        // tile origin inside the output block
 	int c0, k0;
 	int c1, k1;        // c1 < c0: no terms (the tile is written as zeros)
+	int cls;           // tile class (shape), see TILE_*
 	i64 part;
 };
 
@@ -46,12 +47,14 @@ struct GemmSplit {
 };
 
 // tile classes (rows x cols of C per CTA)
-enum { TILE_S = 0, TILE_M = 1, TILE_L = 2, NUM_TILE_CLASSES = 3 };
+// S 16 x 16, M 32 x 32, L 64 x 64, W 16 x 64 (few rows), T 64 x 16 (few columns)
+enum { TILE_S = 0, TILE_M = 1, TILE_L = 2, TILE_W = 3, TILE_T = 4, NUM_TILE_CLASSES = 5 };
 int tile_rows(int cls);
 int tile_cols(int cls);
 
-void launch_gemm_f64(int cls, int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
-                     const double* A, const double* B, double* C, double* work, cudaStream_t st);
+// every tile of every class in one launch (256 threads per CTA, the tile's class picks its shape)
+void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons, const double* A,
+                     const double* B, double* C, double* work, cudaStream_t st);
 void launch_gemm_reduce(int nsplit, const GemmSplit* splits, const GemmOut* outs, const double* work, double* C,
                         cudaStream_t st);
 
