@@ -198,6 +198,24 @@ k_permute(const Chunk* __restrict__ chunks, const PermDesc* __restrict__ descs, 
 	const Chunk ch = chunks[blockIdx.x];
 	const PermDesc d = descs[ch.desc];
 	const i64 end = min(d.n, ch.start + (i64)COPY_CHUNK);
+	if (d.n < ((i64)1 << 31))
+	{
+		// 32-bit index arithmetic (64-bit integer division is several times slower)
+		for (int e = (int)ch.start + threadIdx.x; e < (int)end; e += blockDim.x)
+		{
+			unsigned r = (unsigned)e;
+			i64 so = 0;
+			for (int i = d.ndim - 1; i >= 0; i--)
+			{
+				const unsigned di = (unsigned)d.dims[i];
+				const unsigned q = r / di;
+				so += (i64)(r - q * di) * d.sstr[i];
+				r = q;
+			}
+			dst[d.dst_off + e] = src[d.src_off + so];
+		}
+		return;
+	}
 	for (i64 e = ch.start + threadIdx.x; e < end; e += blockDim.x)
 	{
 		i64 r = e, so = 0;

@@ -275,78 +275,145 @@ void launch_lz_next(const double* w, double* vj1, i64 n, int j, const LanczosSca
 	CTG_CUDA(cudaGetLastError());
 }
 
-// Lowest eigenpair of the k x k symmetric tridiagonal Lanczos matrix by cyclic
-// Jacobi rotations (replaces LAPACK dsteqr, krylov.c:230). One thread; k <= LANCZOS_MAX.
-__global__ void k_tridiag(int maxiter, LanczosScalars* sc)
+// 1 / x for a normal double: FP32 estimate on the mantissa, one cubically convergent Newton step
+// d (1 + e + e^2), e = 1 - m d (error ~e^3, below FP64 rounding), exponent negated exactly. An FP64
+// division costs over a thousand cycles of GB300's FP64 pipe; this is six FP64 instructions.
+__device__ __forceinline__ double rcp64(double x)
 {
-	if (threadIdx.x != 0) return;
-	if (!sc->stopped) sc->numiter = maxiter;
+	const int hi = __double2hiint(x), lo = __double2loint(x);
+	const int ex = ((hi >> 20) & 0x7ff) - 1023;
+	const double m = __hiloint2double((hi & 0x800fffff) | 0x3ff00000, lo);       // sign kept, |m| in [1, 2)
+	float r;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)m));
+	const double d = (double)r;
+	const double e = fma(-m, d, 1.0);
+	const double y = fma(d, fma(e, e, e), d);
+	return y * __hiloint2double((1023 - ex) << 20, 0);
+}
+
+// sqrt(x) for a positive normal double: reciprocal square root of the mantissa (scaled into [1, 4)
+// with an even exponent) from FP32, one cubically convergent correction y (1 + e/2 + 3 e^2 / 8),
+// e = 1 - m y^2, then one Newton step for the square root itself, s + y (m - s^2) / 2.
+__device__ __forceinline__ double sqrt64(double x)
+{
+	const int hi = __double2hiint(x), lo = __double2loint(x);
+	int ex = ((hi >> 20) & 0x7ff) - 1023;
+	double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, lo);             // [1, 2)
+	if (ex & 1)
+	{
+		m *= 2.0;                                                                 // [2, 4)
+		ex -= 1;
+	}
+	float r;
+	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)m));
+	const double y0 = (double)r;
+	const double e = fma(-m * y0, y0, 1.0);
+	const double y = y0 * fma(e, fma(e, 0.375, 0.5), 1.0);
+	double sroot = m * y;
+	sroot = fma(0.5 * y, fma(-sroot, sroot, m), sroot);
+	return sroot * __hiloint2double((1023 + ex / 2) << 20, 0);
+}
+
+// Lowest eigenpair of the k x k symmetric tridiagonal Lanczos matrix by cyclic Jacobi rotations
+// (replaces LAPACK dsteqr, krylov.c:230). One warp; k <= LANCZOS_MAX = 32: the matrix and the
+// rotation product live in shared memory, lane r updates row / column r of every rotation.
+__global__ void __launch_bounds__(32) k_tridiag(int maxiter, LanczosScalars* sc)
+{
+	__shared__ double A[LANCZOS_MAX][LANCZOS_MAX + 1], Z[LANCZOS_MAX][LANCZOS_MAX + 1];
+	const int lane = threadIdx.x;
+	if (lane == 0 && !sc->stopped) sc->numiter = maxiter;
+	__syncwarp();
 	const int k = sc->numiter;
-	if (k < 1) { sc->status = -1; return; }
-	// dense symmetric matrix in local memory, eigenvectors accumulated in Z
-	double A[LANCZOS_MAX * LANCZOS_MAX], Z[LANCZOS_MAX * LANCZOS_MAX];
-	if (k > LANCZOS_MAX) { sc->status = -2; return; }
-	for (int i = 0; i < k; i++)
+	if (k < 1 || k > LANCZOS_MAX)
+	{
+		if (lane == 0) sc->status = k < 1 ? -1 : -2;
+		return;
+	}
+	if (lane < k)
 		for (int j = 0; j < k; j++)
 		{
 			double v = 0;
-			if (i == j) v = sc->alpha[i];
-			else if (j == i + 1) v = sc->beta[i];
-			else if (i == j + 1) v = sc->beta[j];
-			A[i * k + j] = v;
-			Z[i * k + j] = (i == j) ? 1.0 : 0.0;
+			if (lane == j) v = sc->alpha[lane];
+			else if (j == lane + 1) v = sc->beta[lane];
+			else if (lane == j + 1) v = sc->beta[j];
+			A[lane][j] = v;
+			Z[lane][j] = (lane == j) ? 1.0 : 0.0;
 		}
+	__syncwarp();
 	for (int sweep = 0; sweep < 100; sweep++)
 	{
 		double off = 0, diag = 0;
-		for (int i = 0; i < k; i++)
+		if (lane < k)
 		{
-			diag += A[i * k + i] * A[i * k + i];
-			for (int j = i + 1; j < k; j++) off += A[i * k + j] * A[i * k + j];
+			diag = A[lane][lane] * A[lane][lane];
+			for (int j = lane + 1; j < k; j++) off = fma(A[lane][j], A[lane][j], off);
+		}
+		for (int o = 16; o > 0; o >>= 1)
+		{
+			off += __shfl_xor_sync(0xffffffffu, off, o);
+			diag += __shfl_xor_sync(0xffffffffu, diag, o);
 		}
 		// off-diagonal norm below 1e-15 of the diagonal norm: converged
 		if (off <= 1e-30 * diag || off == 0.0) break;
 		for (int p = 0; p < k - 1; p++)
 			for (int q = p + 1; q < k; q++)
 			{
-				const double apq = A[p * k + q];
+				const double apq = A[p][q];
 				if (apq == 0.0) continue;
-				const double app = A[p * k + p], aqq = A[q * k + q];
-				const double theta = (aqq - app) / (2.0 * apq);
-				const double t = copysign(1.0, theta) / (fabs(theta) + sqrt(1.0 + theta * theta));
-				const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
-				for (int r = 0; r < k; r++)
+				const double app = A[p][p], aqq = A[q][q];
+				const double theta = (aqq - app) * rcp64(2.0 * apq);
+				const double t = copysign(1.0, theta) * rcp64(fabs(theta) + sqrt64(fma(theta, theta, 1.0)));
+				const double c = rcp64(sqrt64(fma(t, t, 1.0))), s = t * c;
+				double arp = 0, arq = 0;
+				if (lane < k)
 				{
-					const double arp = A[r * k + p], arq = A[r * k + q];
-					A[r * k + p] = c * arp - s * arq;
-					A[r * k + q] = s * arp + c * arq;
+					arp = A[lane][p];
+					arq = A[lane][q];
 				}
-				for (int r = 0; r < k; r++)
+				__syncwarp();
+				if (lane < k)
 				{
-					const double apr = A[p * k + r], aqr = A[q * k + r];
-					A[p * k + r] = c * apr - s * aqr;
-					A[q * k + r] = s * apr + c * aqr;
+					A[lane][p] = c * arp - s * arq;
+					A[lane][q] = s * arp + c * arq;
 				}
-				A[p * k + q] = 0.0;
-				A[q * k + p] = 0.0;
-				for (int r = 0; r < k; r++)
+				__syncwarp();
+				double apr = 0, aqr = 0;
+				if (lane < k)
 				{
-					const double zrp = Z[r * k + p], zrq = Z[r * k + q];
-					Z[r * k + p] = c * zrp - s * zrq;
-					Z[r * k + q] = s * zrp + c * zrq;
+					apr = A[p][lane];
+					aqr = A[q][lane];
 				}
+				__syncwarp();
+				if (lane < k)
+				{
+					A[p][lane] = c * apr - s * aqr;
+					A[q][lane] = s * apr + c * aqr;
+					const double zrp = Z[lane][p], zrq = Z[lane][q];
+					Z[lane][p] = c * zrp - s * zrq;
+					Z[lane][q] = s * zrp + c * zrq;
+				}
+				__syncwarp();
+				if (lane == 0)
+				{
+					A[p][q] = 0.0;
+					A[q][p] = 0.0;
+				}
+				__syncwarp();
 			}
 	}
-	int imin = 0;
-	for (int i = 1; i < k; i++)
-		if (A[i * k + i] < A[imin * k + imin]) imin = i;
-	sc->lambda = A[imin * k + imin];
-	// deterministic sign: largest-magnitude component positive
-	int imax = 0;
-	for (int i = 1; i < k; i++)
-		if (fabs(Z[i * k + imin]) > fabs(Z[imax * k + imin])) imax = i;
-	const double sgn = Z[imax * k + imin] < 0 ? -1.0 : 1.0;
-	for (int i = 0; i < k; i++) sc->y[i] = sgn * Z[i * k + imin];
+	if (lane == 0)
+	{
+		int imin = 0;
+		for (int i = 1; i < k; i++)
+			if (A[i][i] < A[imin][imin]) imin = i;
+		sc->lambda = A[imin][imin];
+		// deterministic sign: largest-magnitude component positive
+		int imax = 0;
+		for (int i = 1; i < k; i++)
+			if (fabs(Z[i][imin]) > fabs(Z[imax][imin])) imax = i;
+		const double sgn = Z[imax][imin] < 0 ? -1.0 : 1.0;
+		for (int i = 0; i < k; i++) sc->y[i] = sgn * Z[i][imin];
+	}
 }
 
 void launch_lz_tridiag(int maxiter, LanczosScalars* sc, cudaStream_t st)
