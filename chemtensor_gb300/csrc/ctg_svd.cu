@@ -791,7 +791,8 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			{
 				const long long cx = cyc ? clock64() : 0;
 				// jacobi_step ended with a CTA barrier: this round's rotations are complete
-				if (tid == 0 && *sb.local_rot) atomicOr(xs.flags + sweep, 1);
+				// one global flag per sweep, raised after the sweep's last round by any CTA that rotated
+				if (tid == 0 && rho == t.nm - 1 && *sb.local_rot) atomicOr(xs.flags + sweep, 1);
 				const int rho1 = (rho + 1) % t.nm;
 				for (int slot = 0; slot < 2; slot++)
 				{
