@@ -1,5 +1,6 @@
 // ctg_engine.cpp - lowering of block-sparse tensor operations to device work lists.
 #include "ctg_engine.h"
+#include "ctg_plan.h"
 
 #include <algorithm>
 #include <cmath>
@@ -124,10 +125,6 @@ static double host_seconds()
 	return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// host time of plan-building stages (diagnostics): 0 dot meta, 1 dot enumeration, 2 split-K,
-// 3 dot packing, 4 transpose meta, 5 transpose loop, 6 flatten meta, 7 flatten loop, 8 split meta,
-// 9 split loop, 10 slice, 11 other
-double g_plan_stage[12];
 
 static double thread_cpu_seconds()
 {
@@ -408,37 +405,6 @@ const T* at(const DBufPtr& b, size_t off)
 	return (const T*)((const char*)b->ptr + off);
 }
 
-i64 prod(const i64* d, int n)
-{
-	i64 p = 1;
-	for (int i = 0; i < n; i++) p *= d[i];
-	return p;
-}
-
-void add_chunks(std::vector<Chunk>& chunks, int desc, i64 n)
-{
-	for (i64 s = 0; s < n; s += COPY_CHUNK) chunks.push_back(Chunk{desc, 0, s});
-}
-
-// logical indices carrying quantum number q on an axis, in order
-std::vector<i64> fanout(const Meta& t, int ax, q32 q)
-{
-	std::vector<i64> f;
-	for (i64 j = 0; j < t.dim[ax]; j++)
-		if (t.ql[ax][(size_t)j] == q) f.push_back(j);
-	return f;
-}
-
-int tile_class(int m, int n)
-{
-	// the tile that pads the block least (FP64 FMAs on padding cost as much as useful ones)
-	if (m <= 16 && n <= 16) return TILE_S;
-	if (m <= 16) return TILE_W;
-	if (n <= 16) return TILE_T;
-	if (m <= 32 || n <= 32) return TILE_M;
-	return TILE_L;
-}
-
 }  // namespace
 
 // ------------------------------------------------------------------------------------
@@ -447,271 +413,33 @@ int tile_class(int m, int n)
 
 static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
 {
+	DotLowering l = lower_dot(s, axs, t, axt, nmult, precision, c.num_sms());
 	DotPlan p;
-	double ts0 = host_seconds();
-	auto out = std::make_shared<Meta>(dot_result_meta(s, axs, t, axt, nmult));
-	p.out = out;
-	g_plan_stage[0] += host_seconds() - ts0;
-	ts0 = host_seconds();
-	const Meta& r = *out;
-	const int shift_s = (axs == AX_LEADING ? 0 : s.ndim - nmult);
-	const int shift_t = (axt == AX_LEADING ? 0 : t.ndim - nmult);
-	const int off_s = (axs == AX_LEADING ? nmult : 0);
-	const int off_t = (axt == AX_LEADING ? nmult : 0);
-	const int nfs = s.ndim - nmult, nft = t.ndim - nmult;
-	const int nlds = (axs == AX_LEADING ? nmult : s.ndim - nmult);
-	const int nldt = (axt == AX_LEADING ? nmult : t.ndim - nmult);
-
-	std::vector<GemmOut> outs(r.nblocks);
-	std::vector<GemmContrib> cons;
-	std::vector<std::pair<int, int>> con_blocks;   // (s block, t block) of every contribution
-	std::vector<GemmTile> tiles[NUM_TILE_CLASSES];
-	// contracted block indices: all combinations over the first nmult - 1 contracted axes; the
-	// last one is fixed by the conservation law of s
-	i64 ncontract = 1;
-	for (int i = 0; i < nmult - 1; i++) ncontract *= t.nb[shift_t + i];
-	const int lc = shift_s + nmult - 1;          // last contracted axis of s
-	std::vector<i64> is(s.ndim), it(t.ndim), ic(nmult);
-	double flops = 0;
-	for (int b = 0; b < r.nblocks; b++)
-	{
-		const i64* ir = r.index(b);
-		const i64* rd = r.dims(b);
-		GemmOut& o = outs[b];
-		o.c_off = r.boff[b];
-		o.m = (int)prod(rd, nfs);
-		o.n = (int)prod(rd + nfs, nft);
-		o.c0 = (int)cons.size();
-		long long qfree = 0;
-		for (int i = 0; i < nfs; i++) qfree += (long long)s.dir[off_s + i] * s.qb[off_s + i][ir[i]];
-		for (i64 mm = 0; mm < ncontract; mm++)
-		{
-			i64 rem = mm;
-			long long qsum = qfree;
-			for (int i = nmult - 2; i >= 0; i--)
-			{
-				ic[i] = rem % t.nb[shift_t + i];
-				rem /= t.nb[shift_t + i];
-				qsum += (long long)s.dir[shift_s + i] * s.qb[shift_s + i][ic[i]];
-			}
-			const long long qneed = -(long long)s.dir[lc] * qsum;
-			if (qneed < INT32_MIN || qneed > INT32_MAX) continue;
-			const int jl = s.find_q(lc, (q32)qneed);
-			if (jl < 0) continue;
-			ic[nmult - 1] = jl;
-			for (int i = 0; i < nfs; i++) is[off_s + i] = ir[i];
-			for (int i = 0; i < nmult; i++) is[shift_s + i] = ic[i];
-			const int bs = s.find(is.data());
-			if (bs < 0) continue;
-			for (int i = 0; i < nft; i++) it[off_t + i] = ir[nfs + i];
-			for (int i = 0; i < nmult; i++) it[shift_t + i] = ic[i];
-			const int bt = t.find(it.data());
-			CTG_CHECK(bt >= 0, "dot: missing partner block");
-			const i64* sd = s.dims(bs);
-			const i64* td = t.dims(bt);
-			const i64 lds = prod(sd, nlds), tds = prod(sd + nlds, s.ndim - nlds);
-			const i64 ldt = prod(td, nldt), tdt = prod(td + nldt, t.ndim - nldt);
-			GemmContrib g;
-			g.a_off = s.boff[bs];
-			g.b_off = t.boff[bt];
-			const i64 k = (axs == AX_LEADING ? lds : tds);
-			g.k = (int)k;
-			if (axs == AX_LEADING) { g.sAm = 1; g.sAk = (int)tds; }
-			else { g.sAm = (int)tds; g.sAk = 1; }
-			if (axt == AX_LEADING) { g.sBk = (int)tdt; g.sBn = 1; }
-			else { g.sBk = 1; g.sBn = (int)tdt; }
-			CTG_CHECK(k == (axt == AX_LEADING ? ldt : tdt), "dot: inner dimensions differ");
-			// every operand access stays inside its block (checked once per plan, on the host)
-			CTG_CHECK(k >= 1 && g.a_off + (i64)(o.m - 1) * g.sAm + (k - 1) * g.sAk < s.boff[bs] + s.block_size(bs),
-			          "dot: A operand out of range");
-			CTG_CHECK(g.b_off + (k - 1) * g.sBk + (i64)(o.n - 1) * g.sBn < t.boff[bt] + t.block_size(bt),
-			          "dot: B operand out of range");
-			cons.push_back(g);
-			con_blocks.emplace_back(bs, bt);
-			flops += 2.0 * (double)o.m * (double)o.n * (double)k;
-			p.flops_cls[tile_class(o.m, o.n)] += 2.0 * (double)o.m * (double)o.n * (double)k;
-		}
-		o.nc = (int)cons.size() - o.c0;
-		CTG_CHECK(o.m >= 1 && o.n >= 1 && o.c_off + (i64)o.m * o.n <= r.nnz, "dot: output block out of range");
-		// every tile first takes the whole sum over the block's contributions
-		GemmTile whole = {};
-		whole.out = b;
-		whole.c0 = o.c0;
-		whole.k0 = 0;
-		whole.c1 = o.c0 + o.nc - 1;
-		whole.k1 = o.nc > 0 ? cons[(size_t)whole.c1].k : 0;
-		whole.part = -1;
-		if (precision == GEMM_BF16X3)
-		{
-			// tensor-core tiles: one tile class
-			for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
-				for (int n0 = 0; n0 < o.n; n0 += tc_tile_cols())
-				{
-					whole.m0 = m0;
-					whole.n0 = n0;
-					tiles[0].push_back(whole);
-				}
-			continue;
-		}
-		const int cls = tile_class(o.m, o.n);
-		const int tr = tile_rows(cls), tc = tile_cols(cls);
-		whole.cls = cls;
-		for (int m0 = 0; m0 < o.m; m0 += tr)
-			for (int n0 = 0; n0 < o.n; n0 += tc)
-			{
-				whole.m0 = m0;
-				whole.n0 = n0;
-				tiles[cls].push_back(whole);
-			}
-	}
-	// Split-K: on GB300 one SM retires about two FP64 FMAs per clock, so a block GEMM with fewer
-	// tiles than SMs leaves most of the FP64 pipes idle. Tiles whose work exceeds a fair share of
-	// the whole product are cut into shares of consecutive 16-wide k chunks, one CTA each; their
-	// partial sums are added in a fixed order (deterministic) by k_gemm_reduce.
-	g_plan_stage[1] += host_seconds() - ts0;
-	ts0 = host_seconds();
-	std::vector<GemmSplit> splits;
-	i64 wsz = 0;
-	if (precision != GEMM_BF16X3)
-	{
-		constexpr int KCH = 16;                  // k chunk of the FP64 kernels
-		auto nchunks = [&](const GemmOut& o) {
-			i64 n = 0;
-			for (int cc = o.c0; cc < o.c0 + o.nc; cc++) n += (cons[(size_t)cc].k + KCH - 1) / KCH;
-			return n;
-		};
-		double total = 0;
-		for (int k = 0; k < NUM_TILE_CLASSES; k++)
-			for (const GemmTile& t : tiles[k])
-				total += (double)tile_rows(k) * tile_cols(k) * (double)(nchunks(outs[(size_t)t.out]) * KCH);
-		const double target = std::max(total / (2.0 * c.num_sms()), 65536.0);
-		std::vector<std::pair<int, int>> pos;
-		for (int k = 0; k < NUM_TILE_CLASSES; k++)
-		{
-			std::vector<GemmTile> kept;
-			const int tr = tile_rows(k), tc = tile_cols(k);
-			for (const GemmTile& t : tiles[k])
-			{
-				const GemmOut& o = outs[(size_t)t.out];
-				const i64 n = nchunks(o);
-				const double w = (double)tr * tc * (double)(n * KCH);
-				const int S = (int)std::min<double>((double)n, std::ceil(w / target));
-				if (S <= 1)
-				{
-					kept.push_back(t);
-					continue;
-				}
-				pos.clear();
-				for (int cc = o.c0; cc < o.c0 + o.nc; cc++)
-					for (int kk = 0; kk < cons[(size_t)cc].k; kk += KCH) pos.emplace_back(cc, kk);
-				for (int sp = 0; sp < S; sp++)
-				{
-					const i64 a = sp * n / S, e = (sp + 1) * n / S;
-					GemmTile u = t;
-					u.c0 = pos[(size_t)a].first;
-					u.k0 = pos[(size_t)a].second;
-					u.c1 = pos[(size_t)e - 1].first;
-					u.k1 = std::min(pos[(size_t)e - 1].second + KCH, cons[(size_t)u.c1].k);
-					u.part = wsz + (i64)sp * tr * tc;
-					kept.push_back(u);
-				}
-				GemmSplit g = {};
-				g.out = t.out;
-				g.m0 = t.m0;
-				g.n0 = t.n0;
-				g.rows = std::min(tr, o.m - t.m0);
-				g.cols = std::min(tc, o.n - t.n0);
-				g.nsplit = S;
-				g.ld = tc;
-				g.stride = tr * tc;
-				g.part = wsz;
-				splits.push_back(g);
-				wsz += (i64)S * tr * tc;
-			}
-			tiles[k].swap(kept);
-		}
-	}
-	// tensor-core operands: one set of packed tile records per operand block, shared by every
-	// contribution that uses the block
-	std::vector<TcContrib> tcons;
-	std::vector<TcPack> apacks, bpacks;
-	if (precision == GEMM_BF16X3)
-	{
-		std::unordered_map<int, i64> abase, bbase;
-		tcons.resize(cons.size());
-		for (size_t ci = 0; ci < cons.size(); ci++)
-		{
-			const GemmContrib& g = cons[ci];
-			const int bs = con_blocks[ci].first, bt = con_blocks[ci].second;
-			const int kt = (g.k + TC_K - 1) / TC_K;
-			// rows of the A view of block bs and of the B view of block bt
-			const i64* sd = s.dims(bs);
-			const i64* td = t.dims(bt);
-			const int am = (int)prod(sd + (axs == AX_LEADING ? nmult : 0), s.ndim - nmult);
-			const int bn = (int)prod(td + (axt == AX_LEADING ? nmult : 0), t.ndim - nmult);
-			auto ia = abase.find(bs);
-			if (ia == abase.end())
-			{
-				const i64 base = (i64)apacks.size();
-				const int mtiles = (am + TC_A_ROWS - 1) / TC_A_ROWS;
-				for (int mt = 0; mt < mtiles; mt++)
-					for (int j = 0; j < kt; j++)
-						apacks.push_back(TcPack{g.a_off, am, g.k, g.sAm, g.sAk, mt * TC_A_ROWS, j * TC_K, base + mt * kt + j});
-				ia = abase.emplace(bs, base).first;
-			}
-			auto ib = bbase.find(bt);
-			if (ib == bbase.end())
-			{
-				const i64 base = (i64)bpacks.size();
-				const int ntiles_b = (bn + TC_B_ROWS - 1) / TC_B_ROWS;
-				for (int nt = 0; nt < ntiles_b; nt++)
-					for (int j = 0; j < kt; j++)
-						bpacks.push_back(TcPack{g.b_off, bn, g.k, g.sBn, g.sBk, nt * TC_B_ROWS, j * TC_K, base + nt * kt + j});
-				ib = bbase.emplace(bt, base).first;
-			}
-			tcons[ci] = TcContrib{ia->second, ib->second, kt, 0};
-		}
-	}
-	g_plan_stage[2] += host_seconds() - ts0;
-	ts0 = host_seconds();
+	p.out = l.out;
 	p.precision = precision;
-	if (precision == GEMM_BF16X3)
-	{
-		for (int k = 1; k < NUM_TILE_CLASSES; k++) p.flops_cls[0] += p.flops_cls[k], p.flops_cls[k] = 0;
-	}
-	// one launch covers every class: all tiles in one list
-	for (int k = 1; k < NUM_TILE_CLASSES; k++)
-	{
-		tiles[0].insert(tiles[0].end(), tiles[k].begin(), tiles[k].end());
-		tiles[k].clear();
-	}
 	Packer pk;
-	const size_t o_outs = pk.add(outs);
-	const size_t o_cons = pk.add(cons);
-	size_t o_tiles[NUM_TILE_CLASSES];
-	for (int k = 0; k < NUM_TILE_CLASSES; k++) o_tiles[k] = pk.add(tiles[k]);
-	const size_t o_splits = pk.add(splits);
-	const size_t o_tcons = pk.add(tcons), o_apacks = pk.add(apacks), o_bpacks = pk.add(bpacks);
+	const size_t o_outs = pk.add(l.outs);
+	const size_t o_cons = pk.add(l.cons);
+	const size_t o_tiles = pk.add(l.tiles);
+	const size_t o_splits = pk.add(l.splits);
+	const size_t o_tcons = pk.add(l.tcons), o_apacks = pk.add(l.apacks), o_bpacks = pk.add(l.bpacks);
 	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
 	p.tcons = at<TcContrib>(p.desc, o_tcons);
 	p.apacks = at<TcPack>(p.desc, o_apacks);
 	p.bpacks = at<TcPack>(p.desc, o_bpacks);
-	p.a_recs = (i64)apacks.size();
-	p.b_recs = (i64)bpacks.size();
+	p.a_recs = (i64)l.apacks.size();
+	p.b_recs = (i64)l.bpacks.size();
 	p.outs = at<GemmOut>(p.desc, o_outs);
 	p.cons = at<GemmContrib>(p.desc, o_cons);
 	p.splits = at<GemmSplit>(p.desc, o_splits);
-	p.nsplits = (int)splits.size();
-	if (wsz > 0) p.work = std::make_shared<DBuf>(&c, (size_t)wsz * sizeof(double));
-	for (int k = 0; k < NUM_TILE_CLASSES; k++)
-	{
-		p.ntiles[k] = (int)tiles[k].size();
-		p.tiles[k] = at<GemmTile>(p.desc, o_tiles[k]);
-	}
-	p.flops = flops;
-	p.a_entries = s.nnz;
-	p.b_entries = t.nnz;
-	g_plan_stage[3] += host_seconds() - ts0;
+	p.nsplits = (int)l.splits.size();
+	if (l.work_doubles > 0) p.work = std::make_shared<DBuf>(&c, (size_t)l.work_doubles * sizeof(double));
+	p.ntiles[0] = (int)l.tiles.size();
+	p.tiles[0] = at<GemmTile>(p.desc, o_tiles);
+	p.flops = l.flops;
+	for (int k = 0; k < NUM_TILE_CLASSES; k++) p.flops_cls[k] = l.flops_cls[k];
+	p.a_entries = l.a_entries;
+	p.b_entries = l.b_entries;
 	return p;
 }
 
@@ -777,220 +505,58 @@ void CopyPlan::run(Ctx& c, const double* src, double* dst) const
 	else launch_rowmap(nchunks, chunks, (const RowDesc*)descs, maps, src, dst, c.stream());
 }
 
-static CopyPlan finish_perm(Ctx& c, std::shared_ptr<Meta> out, const std::vector<PermDesc>& d, const std::vector<Chunk>& ch)
+static CopyPlan upload_copy(Ctx& c, CopyLowering&& l)
 {
 	CopyPlan p;
-	p.out = out;
-	p.kind = 0;
+	p.out = std::move(l.out);
+	p.kind = l.kind;
 	Packer pk;
-	const size_t od = pk.add(d), oc = pk.add(ch);
+	size_t od = 0;
+	if (l.kind == 0) od = pk.add(l.perm);
+	else if (l.kind == 1) od = pk.add(l.rows);
+	else od = pk.add(l.scale);
+	const size_t oc = pk.add(l.chunks), om = pk.add(l.maps);
 	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
-	p.descs = at<PermDesc>(p.desc, od);
-	p.chunks = at<Chunk>(p.desc, oc);
-	p.nchunks = (int)ch.size();
-	p.elements = out->nnz;
-	return p;
-}
-
-static void check_rows(const std::vector<RowDesc>& descs, const std::vector<i64>& maps, i64 src_nnz, i64 dst_nnz)
-{
-	for (const RowDesc& d : descs)
-	{
-		CTG_CHECK(d.map_off + d.nrow <= (i64)maps.size(), "row map: table out of range");
-		const int mrows = d.scatter ? d.dst_rows : d.src_rows;
-		for (int j = 0; j < d.nrow; j++)
-			CTG_CHECK(maps[(size_t)(d.map_off + j)] >= 0 && maps[(size_t)(d.map_off + j)] < mrows, "row map: entry out of range");
-		CTG_CHECK(d.src_off + d.nlead * d.src_rows * d.ntrail <= src_nnz, "row map: source out of range");
-		CTG_CHECK(d.dst_off + d.nlead * d.dst_rows * d.ntrail <= dst_nnz, "row map: destination out of range");
-		CTG_CHECK(d.scatter ? d.nrow <= d.src_rows : d.nrow <= d.dst_rows, "row map: row count out of range");
-	}
-}
-
-static CopyPlan finish_rows(Ctx& c, std::shared_ptr<Meta> out, const std::vector<RowDesc>& d, const std::vector<Chunk>& ch,
-                            const std::vector<i64>& maps)
-{
-	CopyPlan p;
-	p.out = out;
-	p.kind = 1;
-	Packer pk;
-	const size_t od = pk.add(d), oc = pk.add(ch), om = pk.add(maps);
-	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
-	p.descs = at<RowDesc>(p.desc, od);
+	p.descs = (const char*)p.desc->ptr + od;
 	p.chunks = at<Chunk>(p.desc, oc);
 	p.maps = at<i64>(p.desc, om);
-	p.nchunks = (int)ch.size();
-	p.elements = out->nnz;
+	p.nchunks = (int)l.chunks.size();
+	p.elements = l.elements;
 	return p;
 }
 
-// block_sparse_tensor_transpose (block_sparse_tensor.c:785-870)
-static CopyPlan build_transpose_plan(Ctx& c, const Meta& t, const int* perm)
-{
-	double ts0 = host_seconds();
-	auto out = std::make_shared<Meta>(transpose_meta(t, perm));
-	g_plan_stage[4] += host_seconds() - ts0;
-	ts0 = host_seconds();
-	const Meta& r = *out;
-	CTG_CHECK(t.ndim <= 6, "transpose: at most 6 axes");
-	std::vector<PermDesc> descs;
-	std::vector<Chunk> chunks;
-	std::vector<i64> ir(t.ndim);
-	for (int b = 0; b < t.nblocks; b++)
-	{
-		const i64* it = t.index(b);
-		const i64* td = t.dims(b);
-		for (int i = 0; i < t.ndim; i++) ir[i] = it[perm[i]];
-		const int rb = r.find(ir.data());
-		CTG_CHECK(rb >= 0, "transpose: missing block");
-		i64 st[8];
-		st[t.ndim - 1] = 1;
-		for (int i = t.ndim - 2; i >= 0; i--) st[i] = st[i + 1] * td[i + 1];
-		PermDesc d = {};
-		d.src_off = t.boff[b];
-		d.dst_off = r.boff[rb];
-		d.n = t.block_size(b);
-		d.ndim = t.ndim;
-		for (int i = 0; i < t.ndim; i++) { d.dims[i] = (int)td[perm[i]]; d.sstr[i] = st[perm[i]]; }
-		i64 smax = 0;
-		for (int i = 0; i < t.ndim; i++) smax += (i64)(d.dims[i] - 1) * d.sstr[i];
-		CTG_CHECK(d.src_off + smax < t.nnz && d.dst_off + d.n <= r.nnz, "transpose: descriptor out of range");
-		add_chunks(chunks, (int)descs.size(), d.n);
-		descs.push_back(d);
-	}
-	g_plan_stage[5] += host_seconds() - ts0;
-	return finish_perm(c, out, descs, chunks);
-}
-
-// block_sparse_tensor_flatten_axes (block_sparse_tensor.c:950-1112): each source block
-// scatters its rows (j0, j1) into the fused rows of one target block
-static CopyPlan build_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
-{
-	double ts0 = host_seconds();
-	auto out = std::make_shared<Meta>(flatten_meta(t, ax, newdir));
-	g_plan_stage[6] += host_seconds() - ts0;
-	ts0 = host_seconds();
-	const Meta& r = *out;
-	const i64 d1 = t.dim[ax + 1];
-	std::vector<RowDesc> descs;
-	std::vector<Chunk> chunks;
-	std::vector<i64> maps;
-	std::vector<i64> ir(r.ndim);
-	for (int b = 0; b < t.nblocks; b++)
-	{
-		const i64* it = t.index(b);
-		const i64* td = t.dims(b);
-		const q32 q0 = t.qb[ax][it[ax]], q1 = t.qb[ax + 1][it[ax + 1]];
-		const q32 qf = newdir * (t.dir[ax] * q0 + t.dir[ax + 1] * q1);
-		for (int i = 0; i < ax; i++) ir[i] = it[i];
-		ir[ax] = r.find_q(ax, qf);
-		for (int i = ax + 2; i < t.ndim; i++) ir[i - 1] = it[i];
-		const int rb = r.find(ir.data());
-		CTG_CHECK(rb >= 0, "flatten: missing target block");
-		const auto f0 = fanout(t, ax, q0), f1 = fanout(t, ax + 1, q1);
-		RowDesc d = {};
-		d.src_off = t.boff[b];
-		d.dst_off = r.boff[rb];
-		d.nlead = prod(td, ax);
-		d.ntrail = prod(td + ax + 2, t.ndim - ax - 2);
-		d.nrow = (int)(td[ax] * td[ax + 1]);
-		d.src_rows = d.nrow;
-		d.dst_rows = (int)r.dims(rb)[ax];
-		d.scatter = 1;
-		d.map_off = (i64)maps.size();
-		for (size_t j0 = 0; j0 < f0.size(); j0++)
-			for (size_t j1 = 0; j1 < f1.size(); j1++) maps.push_back(r.pos[ax][(size_t)(f0[j0] * d1 + f1[j1])]);
-		add_chunks(chunks, (int)descs.size(), d.nlead * d.nrow * d.ntrail);
-		descs.push_back(d);
-	}
-	check_rows(descs, maps, t.nnz, r.nnz);
-	g_plan_stage[7] += host_seconds() - ts0;
-	return finish_rows(c, out, descs, chunks, maps);
-}
-
-// block_sparse_tensor_split_axis (block_sparse_tensor.c:1123-1285): each target block
-// gathers its rows (j0, j1) from the fused rows of one source block
-static CopyPlan build_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
-{
-	double ts0 = host_seconds();
-	auto out = std::make_shared<Meta>(split_meta(t, ax, nd, ndir, nq));
-	g_plan_stage[8] += host_seconds() - ts0;
-	ts0 = host_seconds();
-	const Meta& r = *out;
-	std::vector<RowDesc> descs;
-	std::vector<Chunk> chunks;
-	std::vector<i64> maps;
-	std::vector<i64> it(t.ndim);
-	for (int b = 0; b < r.nblocks; b++)
-	{
-		const i64* ir = r.index(b);
-		const i64* rd = r.dims(b);
-		const q32 q0 = r.qb[ax][ir[ax]], q1 = r.qb[ax + 1][ir[ax + 1]];
-		const q32 qf = t.dir[ax] * (r.dir[ax] * q0 + r.dir[ax + 1] * q1);
-		for (int i = 0; i < ax; i++) it[i] = ir[i];
-		it[ax] = t.find_q(ax, qf);
-		for (int i = ax + 1; i < t.ndim; i++) it[i] = ir[i + 1];
-		const int tb = t.find(it.data());
-		CTG_CHECK(tb >= 0, "split: missing source block");
-		const auto f0 = fanout(r, ax, q0), f1 = fanout(r, ax + 1, q1);
-		RowDesc d = {};
-		d.src_off = t.boff[tb];
-		d.dst_off = r.boff[b];
-		d.nlead = prod(rd, ax);
-		d.ntrail = prod(rd + ax + 2, r.ndim - ax - 2);
-		d.nrow = (int)(rd[ax] * rd[ax + 1]);
-		d.dst_rows = d.nrow;
-		d.src_rows = (int)t.dims(tb)[ax];
-		d.scatter = 0;
-		d.map_off = (i64)maps.size();
-		for (size_t j0 = 0; j0 < f0.size(); j0++)
-			for (size_t j1 = 0; j1 < f1.size(); j1++) maps.push_back(t.pos[ax][(size_t)(f0[j0] * nd[1] + f1[j1])]);
-		add_chunks(chunks, (int)descs.size(), d.nlead * d.nrow * d.ntrail);
-		descs.push_back(d);
-	}
-	check_rows(descs, maps, t.nnz, r.nnz);
-	g_plan_stage[9] += host_seconds() - ts0;
-	return finish_rows(c, out, descs, chunks, maps);
-}
-
-// block_sparse_tensor_slice (block_sparse_tensor.c:1446-1553)
-static CopyPlan build_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& ind)
-{
-	auto out = std::make_shared<Meta>(slice_meta(t, ax, ind));
-	const Meta& r = *out;
-	std::vector<RowDesc> descs;
-	std::vector<Chunk> chunks;
-	std::vector<i64> maps;
-	std::vector<i64> it(t.ndim);
-	for (int b = 0; b < r.nblocks; b++)
-	{
-		const i64* ir = r.index(b);
-		const i64* rd = r.dims(b);
-		const q32 qn = r.qb[ax][ir[ax]];
-		for (int i = 0; i < t.ndim; i++) it[i] = ir[i];
-		it[ax] = t.find_q(ax, qn);
-		const int tb = t.find(it.data());
-		CTG_CHECK(tb >= 0, "slice: missing source block");
-		const auto fr = fanout(r, ax, qn);
-		RowDesc d = {};
-		d.src_off = t.boff[tb];
-		d.dst_off = r.boff[b];
-		d.nlead = prod(rd, ax);
-		d.ntrail = prod(rd + ax + 1, r.ndim - ax - 1);
-		d.nrow = (int)rd[ax];
-		d.dst_rows = d.nrow;
-		d.src_rows = (int)t.dims(tb)[ax];
-		d.scatter = 0;
-		d.map_off = (i64)maps.size();
-		for (size_t j = 0; j < fr.size(); j++) maps.push_back(t.pos[ax][(size_t)ind[(size_t)fr[j]]]);
-		add_chunks(chunks, (int)descs.size(), d.nlead * d.nrow * d.ntrail);
-		descs.push_back(d);
-	}
-	check_rows(descs, maps, t.nnz, r.nnz);
-	return finish_rows(c, out, descs, chunks, maps);
-}
-
-
 // ---- cached entry points ----------------------------------------------------------------
+
+// opt-in diagnostics: with CTGPU_PLAN_DUMP=path every plan that misses the cache is appended to
+// that file as (kind, parameters, operand structures), so that the host lowering can be replayed
+// and timed without a device
+static void dump_plan_request(int kind, const std::vector<i64>& params, const Meta& s, const Meta* t)
+{
+	static FILE* f = [] {
+		const char* path = getenv("CTGPU_PLAN_DUMP");
+		return path ? fopen(path, "wb") : nullptr;
+	}();
+	if (!f) return;
+	auto put_sig = [](const Meta& m) {
+		const int32_t nd = m.ndim;
+		fwrite(&nd, sizeof(nd), 1, f);
+		for (int a = 0; a < m.ndim; a++)
+		{
+			const int32_t dir = m.dir[(size_t)a];
+			fwrite(&m.dim[(size_t)a], sizeof(i64), 1, f);
+			fwrite(&dir, sizeof(dir), 1, f);
+			fwrite(m.ql[(size_t)a].data(), sizeof(q32), m.ql[(size_t)a].size(), f);
+		}
+	};
+	const int32_t head[2] = {kind, (int32_t)params.size()};
+	fwrite(head, sizeof(head), 1, f);
+	fwrite(params.data(), sizeof(i64), params.size(), f);
+	put_sig(s);
+	const int32_t has_t = t ? 1 : 0;
+	fwrite(&has_t, sizeof(has_t), 1, f);
+	if (t) put_sig(*t);
+	fflush(f);
+}
 
 DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
 {
@@ -998,6 +564,7 @@ DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, in
 	const std::vector<i64> params = {axs, axt, nmult, precision};
 	const uint64_t key = plan_key(0, params, s, &t);
 	if (const PlanEntry* e = plan_find(c, key, 0, params, s, &t)) return e->dot;
+	dump_plan_request(0, params, s, &t);
 	PlanEntry e;
 	e.kind = 0;
 	e.params = params;
@@ -1015,6 +582,7 @@ static CopyPlan cached_copy(Ctx& c, int kind, const std::vector<i64>& params, co
 {
 	const uint64_t key = plan_key(kind, params, t, nullptr);
 	if (const PlanEntry* e = plan_find(c, key, kind, params, t, nullptr)) return e->copy;
+	dump_plan_request(kind, params, t, nullptr);
 	PlanEntry e;
 	e.kind = kind;
 	e.params = params;
@@ -1030,13 +598,13 @@ CopyPlan make_transpose_plan(Ctx& c, const Meta& t, const int* perm)
 {
 	PlanTimer plan_timer(c);
 	const std::vector<i64> params(perm, perm + t.ndim);
-	return cached_copy(c, 1, params, t, [&] { return build_transpose_plan(c, t, perm); });
+	return cached_copy(c, 1, params, t, [&] { return upload_copy(c, lower_transpose(t, perm)); });
 }
 
 CopyPlan make_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir)
 {
 	PlanTimer plan_timer(c);
-	return cached_copy(c, 2, {ax, newdir}, t, [&] { return build_flatten_plan(c, t, ax, newdir); });
+	return cached_copy(c, 2, {ax, newdir}, t, [&] { return upload_copy(c, lower_flatten(t, ax, newdir)); });
 }
 
 CopyPlan make_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
@@ -1045,7 +613,7 @@ CopyPlan make_split_plan(Ctx& c, const Meta& t, int ax, const i64 nd[2], const i
 	std::vector<i64> params = {ax, nd[0], nd[1], ndir[0], ndir[1], nq ? 1 : 0};
 	if (nq)
 		for (q32 q : *nq) params.push_back(q);
-	return cached_copy(c, 3, params, t, [&] { return build_split_plan(c, t, ax, nd, ndir, nq); });
+	return cached_copy(c, 3, params, t, [&] { return upload_copy(c, lower_split(t, ax, nd, ndir, nq)); });
 }
 
 CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& ind)
@@ -1053,7 +621,7 @@ CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& 
 	PlanTimer plan_timer(c);
 	std::vector<i64> params = {ax};
 	params.insert(params.end(), ind.begin(), ind.end());
-	return cached_copy(c, 4, params, t, [&] { return build_slice_plan(c, t, ax, ind); });
+	return cached_copy(c, 4, params, t, [&] { return upload_copy(c, lower_slice(t, ax, ind)); });
 }
 
 // ------------------------------------------------------------------------------------
@@ -1099,48 +667,12 @@ DTensor op_slice(Ctx& c, const DTensor& t, int ax, const std::vector<i64>& ind)
 	return run_copy(c, make_slice_plan(c, t.m(), ax, ind), t);
 }
 
-// block_sparse_tensor_multiply_pointwise_vector (block_sparse_tensor.c:1654-1703)
-static CopyPlan build_scale_plan(Ctx& c, const Meta& m, int axrange)
-{
-	const int ax = (axrange == AX_LEADING ? 0 : m.ndim - 1);
-	std::vector<ScaleDesc> descs;
-	std::vector<Chunk> chunks;
-	std::vector<i64> maps;
-	for (int b = 0; b < m.nblocks; b++)
-	{
-		const i64* ib = m.index(b);
-		const i64* bd = m.dims(b);
-		const auto f = fanout(m, ax, m.qb[ax][ib[ax]]);
-		ScaleDesc d = {};
-		d.off = m.boff[b];
-		d.nlead = prod(bd, ax);
-		d.nax = (int)bd[ax];
-		d.ntrail = prod(bd + ax + 1, m.ndim - ax - 1);
-		d.map_off = (i64)maps.size();
-		maps.insert(maps.end(), f.begin(), f.end());
-		CTG_CHECK((i64)f.size() == d.nax && d.off + d.nlead * d.nax * d.ntrail <= m.nnz, "scale: descriptor out of range");
-		add_chunks(chunks, (int)descs.size(), d.nlead * d.nax * d.ntrail);
-		descs.push_back(d);
-	}
-	Packer pk;
-	const size_t od = pk.add(descs), oc = pk.add(chunks), om = pk.add(maps);
-	CopyPlan p;
-	p.kind = 2;
-	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
-	p.descs = at<ScaleDesc>(p.desc, od);
-	p.chunks = at<Chunk>(p.desc, oc);
-	p.maps = at<i64>(p.desc, om);
-	p.nchunks = (int)chunks.size();
-	p.elements = m.nnz;
-	return p;
-}
-
 DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange)
 {
 	CopyPlan p;
 	{
 		PlanTimer plan_timer(c);
-		p = cached_copy(c, 5, {axrange}, s.m(), [&] { return build_scale_plan(c, s.m(), axrange); });
+		p = cached_copy(c, 5, {axrange}, s.m(), [&] { return upload_copy(c, lower_scale(s.m(), axrange)); });
 	}
 	DTensor r = c.empty(s.meta);
 	if (p.nchunks > 0)

@@ -107,73 +107,151 @@ Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::
 			m.pos[a][j] = m.bd[a][b]++;
 		}
 	}
-	// enumerate allowed blocks in row-major order: for every prefix over the first ndim-1 axes
-	// (an odometer with incrementally updated partial quantum-number sums), at most one
-	// quantum number of the last axis makes the sum vanish (looked up in a table over its range)
-	const int last = ndim - 1;
-	const std::vector<q32>& qlast = m.qb[last];
-	const long long qlo = qlast.front(), qhi = qlast.back();
-	std::vector<int> qtab;
-	const bool table = qhi - qlo < (1 << 20);
-	if (table)
+	// Enumerate the allowed blocks in row-major order by meeting in the middle: the axes are cut
+	// into a prefix [0, k) and a suffix [k, ndim). Every suffix index tuple is listed once with its
+	// signed quantum-number sum, grouped by sum (row-major order inside a group); then every
+	// prefix tuple, in row-major order, looks up the group whose sum cancels its own and emits
+	// one block per member. Cost ~ prefixes + suffixes + blocks instead of the product of all
+	// but one axis, which matters for pair-encoded quantum numbers (many sectors per bond,
+	// few allowed combinations). The cut minimises prefixes + 2 x suffixes.
+	int k = ndim - 1;
 	{
-		qtab.assign((size_t)(qhi - qlo + 1), -1);
-		for (size_t j = 0; j < qlast.size(); j++) qtab[(size_t)(qlast[j] - qlo)] = (int)j;
-	}
-	i64 nprefix = 1;
-	for (int a = 0; a < last; a++) nprefix *= m.nb[a];
-	const size_t cap = (size_t)std::min<i64>(nprefix, (i64)1 << 22);
-	m.bidx.resize(cap * ndim);
-	m.bdim.resize(cap * ndim);
-	m.boff.resize(cap);
-	m.lin.resize(cap);
-	i64 off = 0;
-	std::vector<i64> idx(ndim, 0);
-	std::vector<long long> partial(ndim, 0);   // partial[a]: sum over axes < a
-	for (int a = 0; a < last; a++) partial[a + 1] = partial[a] + (long long)dir[a] * m.qb[a][0];
-	for (i64 p = 0; p < nprefix; p++)
-	{
-		if (p > 0)
+		double best = 1e300;
+		for (int kk = 0; kk < ndim; kk++)
 		{
-			int a = last - 1;
-			while (++idx[a] == m.nb[a])
+			double pcount = 1, scount = 1;
+			for (int a = 0; a < kk; a++) pcount *= (double)m.nb[a];
+			for (int a = kk; a < ndim; a++) scount *= (double)m.nb[a];
+			const double cost = pcount + 2 * scount;
+			if (cost < best) { best = cost; k = kk; }
+		}
+	}
+	const int ns = ndim - k;
+	i64 nsuf = 1, npre = 1;
+	for (int a = k; a < ndim; a++) nsuf *= m.nb[a];
+	for (int a = 0; a < k; a++) npre *= m.nb[a];
+	CTG_CHECK(nsuf <= ((i64)1 << 26) && npre <= ((i64)1 << 40), "block structure too large to enumerate");
+	// suffix tuples: (sum, suffix linear index), sorted by sum then index
+	std::vector<std::pair<long long, i64>> suf((size_t)nsuf);
+	{
+		i64 sidx[8] = {0};
+		long long part[9] = {0};
+		for (int a = k; a < ndim; a++) part[a - k + 1] = part[a - k] + (long long)dir[a] * m.qb[a][0];
+		for (i64 s = 0; s < nsuf; s++)
+		{
+			if (s > 0)
 			{
-				idx[a] = 0;
-				a--;
+				int a = ns - 1;
+				while (++sidx[a] == m.nb[k + a])
+				{
+					sidx[a] = 0;
+					a--;
+				}
+				for (int i = a; i < ns; i++) part[i + 1] = part[i] + (long long)dir[k + i] * m.qb[k + i][sidx[i]];
 			}
-			for (int i = a; i < last; i++) partial[i + 1] = partial[i] + (long long)dir[i] * m.qb[i][idx[i]];
+			suf[(size_t)s] = {part[ns], s};
 		}
-		const long long qneed = -(long long)dir[last] * partial[last];
-		int j;
-		if (table) j = (qneed < qlo || qneed > qhi) ? -1 : qtab[(size_t)(qneed - qlo)];
-		else j = (qneed < INT32_MIN || qneed > INT32_MAX) ? -1 : m.find_q(last, (q32)qneed);
-		if (j < 0) continue;
-		idx[last] = j;
-		if ((size_t)m.nblocks == m.boff.size())
-		{
-			m.bidx.resize(m.bidx.size() * 2);
-			m.bdim.resize(m.bdim.size() * 2);
-			m.boff.resize(m.boff.size() * 2);
-			m.lin.resize(m.lin.size() * 2);
-		}
-		i64* bi = &m.bidx[(size_t)m.nblocks * ndim];
-		i64* bdm = &m.bdim[(size_t)m.nblocks * ndim];
-		i64 size = 1;
-		for (int a = 0; a < ndim; a++)
-		{
-			bi[a] = idx[a];
-			bdm[a] = m.bd[a][idx[a]];
-			size *= bdm[a];
-		}
-		m.boff[(size_t)m.nblocks] = off;
-		m.lin[(size_t)m.nblocks] = p * m.nb[last] + j;
-		off += size;
-		m.nblocks++;
 	}
-	m.bidx.resize((size_t)m.nblocks * ndim);
-	m.bdim.resize((size_t)m.nblocks * ndim);
-	m.boff.resize((size_t)m.nblocks);
-	m.lin.resize((size_t)m.nblocks);
+	std::sort(suf.begin(), suf.end());
+	std::vector<long long> keys;
+	std::vector<i64> gstart;
+	for (size_t s = 0; s < suf.size(); s++)
+		if (s == 0 || suf[s].first != suf[s - 1].first)
+		{
+			keys.push_back(suf[s].first);
+			gstart.push_back((i64)s);
+		}
+	gstart.push_back((i64)suf.size());
+	// suffix index tuples of the sorted list, decoded once
+	std::vector<int> stup((size_t)nsuf * ns);
+	for (size_t s = 0; s < suf.size(); s++)
+	{
+		i64 r = suf[s].second;
+		for (int a = ns - 1; a >= 0; a--)
+		{
+			stup[s * ns + (size_t)a] = (int)(r % m.nb[k + a]);
+			r /= m.nb[k + a];
+		}
+	}
+	// prefix tuples in row-major order: the group of each (pass 1 counts, pass 2 fills)
+	std::vector<int> grp((size_t)npre, -1);
+	i64 nblk = 0;
+	{
+		i64 pidx[8] = {0};
+		long long part[9] = {0};
+		for (int a = 0; a < k; a++) part[a + 1] = part[a] + (long long)dir[a] * m.qb[a][0];
+		for (i64 p = 0; p < npre; p++)
+		{
+			if (p > 0)
+			{
+				int a = k - 1;
+				while (++pidx[a] == m.nb[a])
+				{
+					pidx[a] = 0;
+					a--;
+				}
+				for (int i = a; i < k; i++) part[i + 1] = part[i] + (long long)dir[i] * m.qb[i][pidx[i]];
+			}
+			const long long need = -part[k];
+			auto it = std::lower_bound(keys.begin(), keys.end(), need);
+			if (it == keys.end() || *it != need) continue;
+			const int g = (int)(it - keys.begin());
+			grp[(size_t)p] = g;
+			nblk += gstart[(size_t)g + 1] - gstart[(size_t)g];
+		}
+	}
+	CTG_CHECK(nblk <= INT32_MAX, "too many blocks");
+	m.nblocks = (int)nblk;
+	m.bidx.resize((size_t)nblk * ndim);
+	m.bdim.resize((size_t)nblk * ndim);
+	m.boff.resize((size_t)nblk);
+	m.lin.resize((size_t)nblk);
+	i64 off = 0;
+	{
+		const i64* bdp[8];
+		for (int a = 0; a < ndim; a++) bdp[a] = m.bd[a].data();
+		i64 pidx[8] = {0};
+		i64 pdim = 1;
+		size_t b = 0;
+		for (i64 p = 0; p < npre; p++)
+		{
+			if (p > 0)
+			{
+				int a = k - 1;
+				while (++pidx[a] == m.nb[a])
+				{
+					pidx[a] = 0;
+					a--;
+				}
+			}
+			const int g = grp[(size_t)p];
+			if (g < 0) continue;
+			pdim = 1;
+			for (int a = 0; a < k; a++) pdim *= bdp[a][pidx[a]];
+			for (i64 s = gstart[(size_t)g]; s < gstart[(size_t)g + 1]; s++)
+			{
+				i64* bi = &m.bidx[b * ndim];
+				i64* bdm = &m.bdim[b * ndim];
+				i64 size = pdim;
+				for (int a = 0; a < k; a++)
+				{
+					bi[a] = pidx[a];
+					bdm[a] = bdp[a][pidx[a]];
+				}
+				const int* st = &stup[(size_t)s * ns];
+				for (int a = 0; a < ns; a++)
+				{
+					bi[k + a] = st[a];
+					bdm[k + a] = bdp[k + a][st[a]];
+					size *= bdm[k + a];
+				}
+				m.boff[b] = off;
+				m.lin[b] = p * nsuf + suf[(size_t)s].second;
+				off += size;
+				b++;
+			}
+		}
+	}
 	m.nnz = off;
 	i64 total = 1;
 	bool dense = true;

@@ -1,6 +1,8 @@
 // Block enumeration of make_meta (ctg_meta.cpp) against a brute-force scan over all block
 // multi-indices: allowed blocks (quantum numbers summing to zero with the axis directions, the
 // rule of block_sparse_tensor.c:78-140), row-major order, offsets, dimensions and find().
+// Small quantum numbers, and pairs packed as (a << 16) + b as the Fermi-Hubbard model encodes
+// particle number and spin (wide value ranges, many sectors, few allowed combinations).
 // Built and run by tests/test_host_logic.py on the host; no GPU involved.
 #include <cstdio>
 #include <random>
@@ -10,17 +12,22 @@ int main()
 {
 	std::mt19937 rng(7);
 	int bad = 0;
-	for (int trial = 0; trial < 3000; trial++)
+	for (int trial = 0; trial < 6000; trial++)
 	{
+		const bool pairs = trial >= 3000;
 		const int nd = 1 + rng() % 6;
 		std::vector<i64> dim(nd);
 		std::vector<int> dir(nd);
 		std::vector<std::vector<q32>> ql(nd);
 		for (int a = 0; a < nd; a++)
 		{
-			dim[a] = 1 + rng() % 9;
+			dim[a] = 1 + rng() % (pairs ? 14 : 9);
 			dir[a] = (rng() & 1) ? 1 : -1;
-			for (int j = 0; j < dim[a]; j++) ql[a].push_back((int)(rng() % 7) - 3);
+			for (int j = 0; j < dim[a]; j++)
+			{
+				if (pairs) ql[a].push_back((int)(rng() % 5) * 65536 + (int)(rng() % 5) - 2);
+				else ql[a].push_back((int)(rng() % 7) - 3);
+			}
 		}
 		Meta m = make_meta(nd, dim.data(), dir.data(), ql);
 		// brute force over all block multi-indices in row-major order
