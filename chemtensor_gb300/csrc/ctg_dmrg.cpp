@@ -732,9 +732,9 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		        c.svd_phase_ms[0] / st->sweeps, c.svd_phase_ms[1] / st->sweeps, c.svd_phase_ms[2] / st->sweeps,
 		        c.svd_phase_ms[3] / st->sweeps);
 	if (getenv("CTGPU_SVD_PHASES") && st->sweeps > 0)
-		fprintf(stderr, "ctgpu: Jacobi of that block, SM cycles per sweep: inner products %.3g parameters %.3g rotations %.3g exchanges %.3g\n",
-		        c.svd_jacobi_cycles[0] / st->sweeps, c.svd_jacobi_cycles[1] / st->sweeps, c.svd_jacobi_cycles[2] / st->sweeps,
-		        c.svd_jacobi_cycles[3] / st->sweeps);
+		fprintf(stderr, "ctgpu: Jacobi of that block, SM cycles per sweep: FP64 steps %.3g exchanges %.3g FP32 sweeps %.3g FP32-to-FP64 %.3g\n",
+		        c.svd_jacobi_cycles[0] / st->sweeps, c.svd_jacobi_cycles[3] / st->sweeps, c.svd_jacobi_cycles[4] / st->sweeps,
+		        c.svd_jacobi_cycles[5] / st->sweeps);
 	st->wall_s = now_s() - t_start;
 	return 0;
 }

@@ -858,7 +858,7 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 	std::unique_ptr<DBuf> ts;
 	if (phases)
 	{
-		ts.reset(new DBuf(&c, descs.size() * 8 * sizeof(unsigned long long)));
+		ts.reset(new DBuf(&c, descs.size() * SVD_PHASE_SLOTS * sizeof(unsigned long long)));
 		CTG_CUDA(cudaMemsetAsync(ts->ptr, 0, ts->bytes, c.stream()));
 	}
 	unsigned long long* tsp = ts ? (unsigned long long*)ts->ptr : nullptr;
@@ -881,7 +881,7 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 	}
 	if (ts)
 	{
-		std::vector<unsigned long long> h(descs.size() * 8);
+		std::vector<unsigned long long> h(descs.size() * SVD_PHASE_SLOTS);
 		CTG_CUDA(cudaMemcpyAsync(h.data(), ts->ptr, ts->bytes, cudaMemcpyDeviceToHost, c.stream()));
 		c.sync();
 		// the block that finished last sets the launch's duration
@@ -889,17 +889,17 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 		unsigned long long t0 = ~0ull, t1 = 0;
 		for (size_t b = 0; b < descs.size(); b++)
 		{
-			if (!h[8 * b]) continue;
-			t0 = std::min(t0, h[8 * b]);
-			if (h[8 * b + 3] > t1) { t1 = h[8 * b + 3]; crit = b; }
+			if (!h[SVD_PHASE_SLOTS * b]) continue;
+			t0 = std::min(t0, h[SVD_PHASE_SLOTS * b]);
+			if (h[SVD_PHASE_SLOTS * b + 3] > t1) { t1 = h[SVD_PHASE_SLOTS * b + 3]; crit = b; }
 		}
 		if (t1 > 0)
 		{
-			c.svd_phase_ms[0] += 1e-6 * (double)(h[8 * crit + 1] - h[8 * crit]);
-			c.svd_phase_ms[1] += 1e-6 * (double)(h[8 * crit + 2] - h[8 * crit + 1]);
-			c.svd_phase_ms[2] += 1e-6 * (double)(h[8 * crit + 3] - h[8 * crit + 2]);
+			c.svd_phase_ms[0] += 1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 1] - h[SVD_PHASE_SLOTS * crit]);
+			c.svd_phase_ms[1] += 1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 2] - h[SVD_PHASE_SLOTS * crit + 1]);
+			c.svd_phase_ms[2] += 1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 3] - h[SVD_PHASE_SLOTS * crit + 2]);
 			c.svd_phase_ms[3] += 1e-6 * (double)(t1 - t0);
-			for (int i = 0; i < 4; i++) c.svd_jacobi_cycles[i] += (double)h[8 * crit + 4 + i];
+			for (int i = 0; i < 6; i++) c.svd_jacobi_cycles[i] += (double)h[SVD_PHASE_SLOTS * crit + 4 + i];
 		}
 	}
 	// the status and the flop count reach pinned host memory once the stream gets there (read by

@@ -93,7 +93,7 @@ public:
 	// with CTGPU_SVD_PHASES set: summed QR / Jacobi / output / launch time (ms) of the block that
 	// finished last in each block SVD
 	double svd_phase_ms[4] = {0, 0, 0, 0};
-	double svd_jacobi_cycles[4] = {0, 0, 0, 0};   // inner products, parameters, rotations, exchanges
+	double svd_jacobi_cycles[6] = {0, 0, 0, 0, 0, 0};   // FP64 steps, -, -, exchanges; FP32 sweeps, hand-over
 	// cache of lowered operations, keyed by operation and operand structures (DMRG revisits the
 	// same block structures every sweep once the bond dimensions have settled)
 	struct PlanCache* plans() { return plans_; }

@@ -43,6 +43,32 @@ constexpr int SVD_THREADS = 256;
 constexpr int NWARPS = SVD_THREADS / 32;
 constexpr int SVD_STEP_PAIRS = 32;            // most column pairs of one inner step (group size <= 32)
 constexpr int SVD_SMEM_LIMIT = 220 * 1024;    // dynamic shared memory per CTA (227 KB less static use)
+constexpr int SVD_F32_SWEEPS = 5;             // most FP32 preconditioning sweeps (more do not save FP64 ones)
+constexpr int SVD_F32_MIN_RANK = 48;          // default: smallest rank preconditioned in FP32
+constexpr int SVD_F32_CLUSTER = 8;            // default: CTAs of the FP32 sweeps
+
+// shared memory (doubles) of the Jacobi tour: two buffers of two column groups (records of 2 N),
+// their norms and the per-step pair data
+__host__ __device__ inline i64 tour_jac_doubles(int N, int cl)
+{
+	const i64 nblk = 2 * cl, bsmax = (N + nblk - 1) / nblk;
+	return 4 * bsmax * 2 * N + 4 * bsmax + 3 * SVD_STEP_PAIRS + SVD_STEP_PAIRS / 2 + 16;
+}
+
+// shared memory (bytes) of the FP32 tour over 2 cf groups of the r columns (records of 2 N floats)
+__host__ __device__ inline i64 f32_tour_bytes(int N, int r, int cf)
+{
+	const i64 bs = (r + 2 * cf - 1) / (2 * cf);
+	return 4 * (4 * bs * 2 * N + 4 * bs + 4);
+}
+
+// ... plus the staging of the FP64 steps after the FP32 sweeps: all of V (r x (r | 1)) or of R
+// (r x (N | 1)), and the CTA's own columns (at most 2 bsmax of length r)
+__host__ __device__ inline i64 precond_doubles(int N, int cl)
+{
+	const i64 nblk = 2 * cl, bsmax = (N + nblk - 1) / nblk;
+	return tour_jac_doubles(N, cl) + (i64)N * (N | 1) + 2 * bsmax * N;
+}
 
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -335,11 +361,7 @@ struct Tour {
 };
 
 struct StepBuf {
-	double* gam;
-	double* csc;
-	double* css;
-	int* rotk;
-	int* local_rot;
+	int* local_rot;              // set when a rotation was applied in the current sweep
 };
 
 __device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int k, int cA, int cB, int npad, int& sp,
@@ -348,101 +370,145 @@ __device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int
 	return step_pair_idx(mode, step, k, t.bs, cA, cB, npad, sp, cp, sq, cq);
 }
 
+// One inner step of the FP64 tour. The pairs of a step are disjoint, so each warp takes whole
+// pairs: the inner product (every lane gets the sum), the rotation parameters (computed by every
+// lane: an FP64 warp instruction costs the same whatever the number of active lanes) and the
+// three-shear rotation of the two records (T entries 0 .. N-1, V entries N .. N+r-1). One CTA
+// barrier per step, and the warps of different pairs run on different SM sub-partitions.
 __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, int cB, int npad, float tol2, const StepBuf& sb,
                             long long* cyc, double& flops)
 {
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const long long c0 = cyc ? clock64() : 0;
 	const int np = mode == 0 ? npad : t.bs;
-	// 1. inner products, one warp per pair
+	const int len = t.N + t.r;
 	for (int k = warp; k < np; k += NWARPS)
 	{
 		int sp, cp, sq, cq;
 		if (!step_pair(t, mode, step, k, cA, cB, npad, sp, cp, sq, cq)) continue;
-		const double* x = t.col(buf, sp, cp);
-		const double* y = t.col(buf, sq, cq);
+		double* x = t.col(buf, sp, cp);
+		double* y = t.col(buf, sq, cq);
 		double g = 0;
 		for (int i = lane; i < t.N; i += 32) g = fma(x[i], y[i], g);
 		g = warp_sum(g);
-		if (lane == 0) sb.gam[k] = g;
-	}
-	__syncthreads();
-	const long long c1 = cyc ? clock64() : 0;
-	// 2. rotations, one lane per pair; rotate while the cosine exceeds tol
-	if (warp == 0 && lane < np)
-	{
-		int sp, cp, sq, cq;
-		int rot = 0;
-		double tau = 0.0, sn = 0.0;
-		const bool valid = step_pair(t, mode, step, lane, cA, cB, npad, sp, cp, sq, cq);
-		if (valid)
+		double* pa = t.nrm(buf, sp) + cp;
+		double* pb = t.nrm(buf, sq) + cq;
+		const double al = *pa, be = *pb;
+		double tau, sn, tn;
+		// executed FP64 flops: an inner product per examined pair, three FMAs per entry of the two
+		// column records per rotation (counted on lane 0 of each warp)
+		if (lane == 0) flops += 2.0 * t.N;
+		if (rotation_params(al, be, g, tol2, tau, sn, tn))
 		{
-			double* np_ = t.nrm(buf, sp) + cp;
-			double* nq_ = t.nrm(buf, sq) + cq;
-			const double al = *np_, be = *nq_, ga = sb.gam[lane];
-			double tn;
-			if (rotation_params(al, be, ga, tol2, tau, sn, tn))
+			for (int i = lane; i < len; i += 32)
 			{
-				rot = 1;
-				*np_ = fma(-tn, ga, al);
-				*nq_ = fma(tn, ga, be);
+				const double x1 = fma(-tau, y[i], x[i]);
+				const double y1 = fma(sn, x1, y[i]);
+				x[i] = fma(-tau, y1, x1);
+				y[i] = y1;
+			}
+			__syncwarp();
+			if (lane == 0)
+			{
+				*pa = fma(-tn, g, al);
+				*pb = fma(tn, g, be);
 				*sb.local_rot = 1;
+				flops += 6.0 * len;
 			}
 		}
-		sb.csc[lane] = tau;
-		sb.css[lane] = sn;
-		// compact list of the rotating pairs, so that the work items below are spread evenly
-		const unsigned amask = np >= 32 ? 0xffffffffu : ((1u << np) - 1u);
-		const unsigned mask = __ballot_sync(amask, rot);
-		const unsigned vmask = __ballot_sync(amask, valid);
-		if (rot) sb.rotk[__popc(mask & ((1u << lane) - 1u))] = lane;
-		if (lane == 0)
+	}
+	__syncthreads();
+	if (cyc) cyc[0] += clock64() - c0;
+}
+
+// ---- FP32 preconditioning ----------------------------------------------------------------
+//
+// An SM retires 128 FP32 FMAs per clock against two FP64 FMAs, and the first Jacobi sweeps rotate
+// almost every pair. So for larger blocks the tour first runs on FP32 copies of R^T and V (same
+// schedule, records of N + r floats) until the cosines fall to about N eps_32. V is then made
+// orthogonal to FP64 rounding by two Newton-Schulz steps V <- V - V (V^T V - I) / 2 (the error
+// squares each step: 1e-5, 1e-10, below eps) and T = R^T V is formed in FP64. The FP64 sweeps
+// that follow start from columns orthogonal to FP32 accuracy and converge quadratically, in
+// about two sweeps plus the one that confirms convergence, where six to nine are needed from
+// R^T itself. The FP64 sweeps alone decide the result: the FP32 phase only chooses the starting
+// basis. (Low-precision Jacobi SVD as preconditioner of a high-precision one-sided Jacobi: W. Gao,
+// Y. Ma, M. Shao, "A mixed precision Jacobi SVD algorithm", arXiv:2209.04626.)
+
+struct Tour32 {
+	int nblk, nm, bs, bsmax, r, N, ld;
+	float* sm;
+	__device__ float* col(int buf, int slot, int c) const { return sm + (i64)((buf * 2 + slot) * bsmax + c) * ld; }
+	__device__ float* nrm(int buf, int slot) const { return sm + (i64)4 * bsmax * ld + (buf * 2 + slot) * bsmax; }
+	__device__ int cnt(int x) const
+	{
+		const int c = r - x * bs;
+		return c < 0 ? 0 : (c > bs ? bs : c);
+	}
+};
+
+__device__ __forceinline__ float warp_sumf(float v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// One inner step of the FP32 tour. The pairs of a step are disjoint, so each warp takes whole
+// pairs: inner product (every lane gets the sum), classical Jacobi rotation (tan theta the
+// smaller root of t^2 + 2 zeta t - 1 = 0, computed by every lane), rotation of the two records.
+// One CTA barrier per step.
+__device__ void jacobi_step32(const Tour32& t, int buf, int mode, int step, int cA, int cB, int npad, float tol2,
+                              int* local_rot)
+{
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int np = mode == 0 ? npad : t.bs;
+	const int len = t.N + t.r;
+	for (int k = warp; k < np; k += NWARPS)
+	{
+		int sp, cp, sq, cq;
+		if (!step_pair_idx(mode, step, k, t.bs, cA, cB, npad, sp, cp, sq, cq)) continue;
+		float* x = t.col(buf, sp, cp);
+		float* y = t.col(buf, sq, cq);
+		float g = 0.0f;
+		for (int i = lane; i < t.N; i += 32) g = fmaf(x[i], y[i], g);
+		g = warp_sumf(g);
+		float* pa = t.nrm(buf, sp) + cp;
+		float* pb = t.nrm(buf, sq) + cq;
+		const float al = *pa, be = *pb;
+		if (g != 0.0f && g * g > tol2 * al * be)
 		{
-			sb.rotk[SVD_STEP_PAIRS] = __popc(mask);
-			// executed FP64 flops: an inner product per examined pair, three FMAs per entry of
-			// the two column records per rotation
-			flops += 2.0 * t.N * __popc(vmask) + 6.0 * (t.N + t.r) * __popc(mask);
+			const float zeta = (be - al) / (2.0f * g);
+			const float az = fabsf(zeta);
+			float tn = az > 1e10f ? 0.5f / az : 1.0f / (az + sqrtf(fmaf(az, az, 1.0f)));
+			tn = copysignf(tn, zeta);
+			const float c = rsqrtf(fmaf(tn, tn, 1.0f));
+			const float sn = c * tn;
+			for (int i = lane; i < len; i += 32)
+			{
+				const float xv = x[i], yv = y[i];
+				x[i] = fmaf(c, xv, -sn * yv);
+				y[i] = fmaf(sn, xv, c * yv);
+			}
+			__syncwarp();
+			if (lane == 0)
+			{
+				*pa = fmaf(-tn, g, al);
+				*pb = fmaf(tn, g, be);
+				*local_rot = 1;
+			}
 		}
 	}
 	__syncthreads();
-	const long long c2 = cyc ? clock64() : 0;
-	// 3. apply: work items of 32 consecutive entries of one rotating pair's column record
-	// (T entries 0 .. N-1 followed by V entries N .. N+r-1)
-	const int len = t.N + t.r, nseg = (len + 31) >> 5;
-	const int nrot = sb.rotk[SVD_STEP_PAIRS];
-	for (int it = warp; it < nrot * nseg; it += NWARPS)
-	{
-		const int j = it / nseg, g = it - j * nseg;
-		const int i = g * 32 + lane;
-		if (i >= len) continue;
-		const int k = sb.rotk[j];
-		int sp, cp, sq, cq;
-		step_pair(t, mode, step, k, cA, cB, npad, sp, cp, sq, cq);
-		double* x = t.col(buf, sp, cp);
-		double* y = t.col(buf, sq, cq);
-		const double tau = sb.csc[k], sn = sb.css[k];
-		const double x1 = fma(-tau, y[i], x[i]);
-		const double y1 = fma(sn, x1, y[i]);
-		x[i] = fma(-tau, y1, x1);
-		y[i] = y1;
-	}
-	__syncthreads();
-	if (cyc)
-	{
-		const long long c3 = clock64();
-		cyc[0] += c1 - c0;
-		cyc[1] += c2 - c1;
-		cyc[2] += c3 - c2;
-	}
 }
 
 struct SvdScratch {
 	double *W, *T, *V, *nrm, *tau, *sig, *misc;
-	int *flags, *perm;
+	int *flags, *perm, *flags32;
 };
 
 // workspace of one block: W (M x N, B then R and the reflectors), T (N x r), V (r x r), column
-// norms, reflector scalars, singular values, misc [rank, ||B||_F^2, unscale], sweep flags, pivots
+// norms, reflector scalars, singular values, misc [rank, ||B||_F^2, unscale], sweep flags, pivots,
+// FP32 sweep flags
 __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 {
 	SvdScratch x;
@@ -455,6 +521,7 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 	x.misc = x.sig + N;
 	x.flags = (int*)(x.misc + 4);
 	x.perm = x.flags + SVD_MAX_SWEEPS;
+	x.flags32 = x.perm + N;
 	return x;
 }
 
@@ -652,10 +719,218 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 	return r;
 }
 
+// FP32 preconditioning of the tour (see above). The FP32 sweeps run on the first cf CTAs of the
+// cluster (a tour over 2 cf groups; the others only keep the cluster barriers in step): their
+// cost is latency and barriers, not arithmetic, and fewer, larger groups need fewer rounds. On
+// return, buffer 0 of the FP64 tour holds this CTA's round-0 column records [T | V] with V
+// orthogonal to FP64 rounding and T = R^T V. Staging for the FP64 steps starts after the FP64
+// tour's own shared memory.
+__device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, double* smem, const SvdScratch& xs, int M,
+                                 int cl, int cf, int rank, double& flops, long long* cyc)
+{
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const long long c0 = cyc ? clock64() : 0;
+	const int N = t.N, r = t.r;
+	Tour32 f;
+	f.nblk = 2 * cf;
+	f.nm = f.nblk - 1;
+	f.bs = (r + f.nblk - 1) / f.nblk;
+	f.bsmax = f.bs;
+	f.r = r;
+	f.N = N;
+	f.ld = t.ld;
+	f.sm = (float*)smem;
+	int* local_rot = (int*)(f.sm + (i64)4 * f.bsmax * f.ld + 4 * f.bsmax);
+	int A, B;
+	if (rank < cf)
+	{
+		round_groups(0, rank, f.nm, A, B);
+		// column g of T is row g of R (upper triangle of W); column g of V is e_g
+		for (int slot = 0; slot < 2; slot++)
+		{
+			const int x = slot ? B : A;
+			float* dst = f.col(0, slot, 0);
+			for (i64 e = tid; e < (i64)f.cnt(x) * f.ld; e += SVD_THREADS)
+			{
+				const int c = (int)(e / f.ld), i = (int)(e % f.ld);
+				const int g = x * f.bs + c;
+				float v;
+				if (i < N) v = (i >= g) ? (float)__ldcg(xs.W + (i64)i * M + g) : 0.0f;
+				else v = (i - N == g) ? 1.0f : 0.0f;
+				dst[e] = v;
+			}
+		}
+		__syncthreads();
+		const float tol2 = (float)N * FLT_EPSILON * (float)N * FLT_EPSILON;
+		int buf = 0;
+		for (int sweep = 0; sweep < SVD_F32_SWEEPS; sweep++)
+		{
+			round_groups(0, rank, f.nm, A, B);
+			for (int slot = 0; slot < 2; slot++)
+			{
+				const int nc = f.cnt(slot ? B : A);
+				for (int c = warp; c < nc; c += NWARPS)
+				{
+					const float* col = f.col(buf, slot, c);
+					float acc = 0.0f;
+					for (int i = lane; i < N; i += 32) acc = fmaf(col[i], col[i], acc);
+					acc = warp_sumf(acc);
+					if (lane == 0) f.nrm(buf, slot)[c] = acc;
+				}
+			}
+			if (tid == 0) *local_rot = 0;
+			__syncthreads();
+			for (int rho = 0; rho < f.nm; rho++)
+			{
+				round_groups(rho, rank, f.nm, A, B);
+				const int cA = f.cnt(A), cB = f.cnt(B);
+				if (rho == 0)
+				{
+					const int npad = f.bs + (f.bs & 1);
+					for (int st = 0; st < npad - 1; st++) jacobi_step32(f, buf, 0, st, cA, cB, npad, tol2, local_rot);
+				}
+				for (int st = 0; st < f.bs; st++) jacobi_step32(f, buf, 1, st, cA, cB, 0, tol2, local_rot);
+				if (cf > 1)
+				{
+					if (tid == 0 && rho == f.nm - 1 && *local_rot) atomicOr(xs.flags32 + sweep, 1);
+					const int rho1 = (rho + 1) % f.nm;
+					for (int slot = 0; slot < 2; slot++)
+					{
+						const int x = slot ? B : A, nc = f.cnt(x);
+						int pi2, slot2;
+						group_owner(x, rho1, f.nm, pi2, slot2);
+						const float2* src = (const float2*)f.col(buf, slot, 0);
+						float2* dst = (float2*)cluster.map_shared_rank(f.col(buf ^ 1, slot2, 0), (unsigned)pi2);
+						for (i64 e = tid; e < (i64)nc * f.ld / 2; e += SVD_THREADS) dst[e] = src[e];
+						const float* nsrc = f.nrm(buf, slot);
+						float* ndst = cluster.map_shared_rank(f.nrm(buf ^ 1, slot2), (unsigned)pi2);
+						for (int e = tid; e < nc; e += SVD_THREADS) ndst[e] = nsrc[e];
+					}
+					cluster.sync();
+					buf ^= 1;
+				}
+			}
+			bool conv;
+			if (cf > 1) conv = __ldcg(xs.flags32 + sweep) == 0;
+			else
+			{
+				conv = *local_rot == 0;
+				__syncthreads();
+			}
+			if (conv) break;
+		}
+		// V (FP32) to global memory, column g at V + g r
+		round_groups(0, rank, f.nm, A, B);
+		for (int slot = 0; slot < 2; slot++)
+		{
+			const int x = slot ? B : A, nc = f.cnt(x);
+			const float* src = f.col(buf, slot, 0);
+			for (i64 e = tid; e < (i64)nc * r; e += SVD_THREADS)
+			{
+				const int c = (int)(e / r), i = (int)(e % r);
+				xs.V[(i64)(x * f.bs + c) * r + i] = (double)src[(i64)c * f.ld + N + i];
+			}
+		}
+	}
+	else if (cf > 1)
+	{
+		// the barriers of the working CTAs' rounds, and their convergence decision
+		for (int sweep = 0; sweep < SVD_F32_SWEEPS; sweep++)
+		{
+			for (int rho = 0; rho < f.nm; rho++) cluster.sync();
+			if (__ldcg(xs.flags32 + sweep) == 0) break;
+		}
+	}
+	const long long c1 = cyc ? clock64() : 0;
+	cluster.sync();
+	// the CTA's own columns of the FP64 tour: slot-0 group, then slot-1 group
+	round_groups(0, rank, t.nm, A, B);
+	const int own0 = t.cnt(A), nown = own0 + t.cnt(B);
+	auto own_col = [&](int j) { return j < own0 ? A * t.bs + j : B * t.bs + (j - own0); };
+	double* stage = smem + tour_jac_doubles(N, cl);
+	// two Newton-Schulz steps, V <- V - V E / 2 with E = V^T V - I; V ping-pongs between the V and
+	// T areas of the scratch (T is written only after the Jacobi sweeps)
+	double* Va = xs.V;
+	double* Vb = xs.T;
+	const int ldv = r | 1;                            // odd stride: lanes over columns hit distinct banks
+	double* vs = stage;                               // all of V, column k at vs + k ldv
+	double* es = vs + (i64)r * ldv;                   // E columns of the own columns, es + j r
+	for (int step = 0; step < 2; step++)
+	{
+		for (i64 e = tid; e < (i64)r * r; e += SVD_THREADS)
+		{
+			const int k = (int)(e / r), i = (int)(e % r);
+			vs[(i64)k * ldv + i] = __ldcg(Va + e);
+		}
+		__syncthreads();
+		for (int e = tid; e < r * nown; e += SVD_THREADS)
+		{
+			const int j = e / r, k = e % r;
+			const int g = own_col(j);
+			const double* vk = vs + (i64)k * ldv;
+			const double* vj = vs + (i64)g * ldv;
+			double acc = 0.0;
+			for (int i = 0; i < r; i++) acc = fma(vk[i], vj[i], acc);
+			es[(i64)j * r + k] = acc - (k == g ? 1.0 : 0.0);
+		}
+		__syncthreads();
+		for (int e = tid; e < r * nown; e += SVD_THREADS)
+		{
+			const int j = e / r, i = e % r;
+			const double* ej = es + (i64)j * r;
+			double acc = 0.0;
+			for (int k = 0; k < r; k++) acc = fma(vs[(i64)k * ldv + i], ej[k], acc);
+			const int g = own_col(j);
+			Vb[(i64)g * r + i] = fma(-0.5, acc, vs[(i64)g * ldv + i]);
+		}
+		if (tid == 0) flops += 4.0 * (double)r * r * nown;
+		cluster.sync();
+		double* tmp = Va;
+		Va = Vb;
+		Vb = tmp;
+	}
+	// T = R^T V for the own columns, straight into buffer 0 of the FP64 tour; R staged with an odd
+	// stride (row k at rs + k ldr, R_ki = W_ik for i >= k)
+	const int ldr = N | 1;
+	double* rs = stage;
+	double* vo = rs + (i64)r * ldr;
+	for (i64 e = tid; e < (i64)r * N; e += SVD_THREADS)
+	{
+		const int i = (int)(e / r), k = (int)(e % r);
+		rs[(i64)k * ldr + i] = (k <= i) ? __ldcg(xs.W + (i64)i * M + k) : 0.0;
+	}
+	for (int e = tid; e < r * nown; e += SVD_THREADS)
+	{
+		const int j = e / r, k = e % r;
+		vo[e] = __ldcg(Va + (i64)own_col(j) * r + k);
+	}
+	__syncthreads();
+	for (int e = tid; e < N * nown; e += SVD_THREADS)
+	{
+		const int j = e / N, i = e % N;
+		const int kmax = i < r - 1 ? i : r - 1;
+		const double* vj = vo + (i64)j * r;
+		double acc = 0.0;
+		for (int k = 0; k <= kmax; k++) acc = fma(rs[(i64)k * ldr + i], vj[k], acc);
+		const int slot = j < own0 ? 0 : 1, c = slot ? j - own0 : j;
+		double* rec = t.col(0, slot, c);
+		rec[i] = acc;
+		rec[N + i] = i < r ? vj[i] : 0.0;
+	}
+	if (tid == 0) flops += 2.0 * ((double)N * r - 0.5 * (double)r * r) * nown;
+	__syncthreads();
+	if (cyc)
+	{
+		cyc[4] += c1 - c0;
+		cyc[5] += clock64() - c1;
+	}
+}
+
 __global__ void __launch_bounds__(SVD_THREADS)
 k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
            double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
-           double* __restrict__ flops, int cl, int smem_bytes, unsigned long long* __restrict__ phase_ts)
+           double* __restrict__ flops, int cl, int smem_bytes, unsigned long long* __restrict__ phase_ts, int f32_min,
+           int f32_cl)
 {
 	extern __shared__ __align__(16) double smem[];
 	cg::cluster_group cluster = cg::this_cluster();
@@ -670,8 +945,9 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	const double* ab = a + d.a_off;
 
 	for (int e = rank * SVD_THREADS + tid; e < SVD_MAX_SWEEPS; e += cl * SVD_THREADS) xs.flags[e] = 0;
+	for (int e = rank * SVD_THREADS + tid; e < SVD_F32_SWEEPS; e += cl * SVD_THREADS) xs.flags32[e] = 0;
 	const bool stamp = phase_ts && rank == 0 && tid == 0;
-	if (stamp) phase_ts[8 * blk] = globaltimer();
+	if (stamp) phase_ts[SVD_PHASE_SLOTS * blk] = globaltimer();
 
 	// ---- 1. pivoted QR of B scaled to a Frobenius norm in [1/2, 1): over the cluster, or on the
 	// single CTA of a one-CTA cluster ----
@@ -713,7 +989,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	}
 	cluster.sync();
 	const int r = (int)__ldcg(xs.misc);
-	if (stamp) phase_ts[8 * blk + 1] = globaltimer();
+	if (stamp) phase_ts[SVD_PHASE_SLOTS * blk + 1] = globaltimer();
 
 	// ---- 2. one-sided Jacobi on R^T (N x r), block-pair tournament over the cluster ----
 	Tour t;
@@ -726,37 +1002,44 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	t.bs = r > 0 ? (r + t.nblk - 1) / t.nblk : 1;
 	t.sm = smem;
 	StepBuf sb;
-	sb.gam = smem + (i64)4 * t.bsmax * t.ld + 4 * t.bsmax;
-	sb.csc = sb.gam + SVD_STEP_PAIRS;
-	sb.css = sb.csc + SVD_STEP_PAIRS;
-	sb.rotk = (int*)(sb.css + SVD_STEP_PAIRS);
-	sb.local_rot = sb.rotk + SVD_STEP_PAIRS + 1;
+	sb.local_rot = (int*)(smem + (i64)4 * t.bsmax * t.ld + 4 * t.bsmax);
 
 	int A, B;
-	round_groups(0, rank, t.nm, A, B);
-	// column g of T is row g of R (upper triangle of W); column g of V is e_g
-	for (int slot = 0; slot < 2; slot++)
-	{
-		const int x = slot ? B : A;
-		double* dst = t.col(0, slot, 0);
-		for (i64 e = tid; e < (i64)t.cnt(x) * t.ld; e += SVD_THREADS)
-		{
-			const int c = (int)(e / t.ld), i = (int)(e % t.ld);
-			const int g = x * t.bs + c;
-			double v;
-			if (i < N) v = (i >= g) ? __ldcg(xs.W + (i64)i * M + g) : 0.0;
-			else v = (i - N == g) ? 1.0 : 0.0;
-			dst[e] = v;
-		}
-	}
-	__syncthreads();
-
-	const float tol2 = (float)((double)N * DBL_EPSILON * (double)N * DBL_EPSILON);
-	long long cyc_acc[4] = {0, 0, 0, 0};               // dots, rotation parameters, rotations, exchanges
 	double jflops = 0;                                 // counted by thread 0 (lane 0 of warp 0)
+	long long cyc_acc[6] = {0, 0, 0, 0, 0, 0};         // dots, rotation parameters, rotations, exchanges, FP32, hand-over
 	// counted on the second CTA: the first one holds the last column group, often short or empty
 	const bool count = phase_ts && tid == 0 && rank == (cl > 1 ? 1 : 0);
 	long long* cyc = count ? cyc_acc : nullptr;
+	const bool mixed = f32_min > 0 && r >= f32_min && 8 * precond_doubles(N, cl) <= (i64)smem_bytes;
+	if (mixed)
+	{
+		// FP32 sub-cluster: the requested size, or larger until its column groups fit
+		int cf = f32_cl < cl ? f32_cl : cl;
+		while (cf < cl && f32_tour_bytes(N, r, cf) > (i64)smem_bytes) cf *= 2;
+		precondition_f32(cluster, t, smem, xs, M, cl, cf, rank, jflops, cyc);
+	}
+	else
+	{
+		round_groups(0, rank, t.nm, A, B);
+		// column g of T is row g of R (upper triangle of W); column g of V is e_g
+		for (int slot = 0; slot < 2; slot++)
+		{
+			const int x = slot ? B : A;
+			double* dst = t.col(0, slot, 0);
+			for (i64 e = tid; e < (i64)t.cnt(x) * t.ld; e += SVD_THREADS)
+			{
+				const int c = (int)(e / t.ld), i = (int)(e % t.ld);
+				const int g = x * t.bs + c;
+				double v;
+				if (i < N) v = (i >= g) ? __ldcg(xs.W + (i64)i * M + g) : 0.0;
+				else v = (i - N == g) ? 1.0 : 0.0;
+				dst[e] = v;
+			}
+		}
+		__syncthreads();
+	}
+
+	const float tol2 = (float)((double)N * DBL_EPSILON * (double)N * DBL_EPSILON);
 	int buf = 0, sweep = 0;
 	bool converged = r <= 1;
 	for (; sweep < SVD_MAX_SWEEPS && !converged; sweep++)
@@ -840,16 +1123,16 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			if (lane == 0) xs.sig[x * t.bs + c] = sqrt(acc);
 		}
 	}
-	if (tid == 0 && jflops > 0) atomicAdd(flops, jflops);
+	if (lane == 0 && jflops > 0) atomicAdd(flops, jflops);
 	if (rank == 0 && tid == 0)
 	{
 		atomicMax(status + 1, sweep);
 		if (!converged) atomicExch(status, -1);
 	}
 	cluster.sync();
-	if (stamp) phase_ts[8 * blk + 2] = globaltimer();
+	if (stamp) phase_ts[SVD_PHASE_SLOTS * blk + 2] = globaltimer();
 	if (count)
-		for (int i = 0; i < 4; i++) phase_ts[8 * blk + 4 + i] = (unsigned long long)cyc_acc[i];
+		for (int i = 0; i < 6; i++) phase_ts[SVD_PHASE_SLOTS * blk + 4 + i] = (unsigned long long)cyc_acc[i];
 
 	// ---- 3. outputs: L = Q V (M x r) by the r reflectors applied to [V_c; 0], Rf = P T Sigma^-1 ----
 	const double unscale = __ldcg(xs.misc + 2);
@@ -898,7 +1181,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	if (phase_ts)
 	{
 		cluster.sync();
-		if (stamp) phase_ts[8 * blk + 3] = globaltimer();
+		if (stamp) phase_ts[SVD_PHASE_SLOTS * blk + 3] = globaltimer();
 	}
 }
 
@@ -1236,12 +1519,38 @@ i64 svd_scratch_doubles(int m, int n)
 	return 2 * M * N + 2 * N * N + 3 * N + 4 + 2 * SVD_MAX_SWEEPS + (N + 1) / 2 + 1;
 }
 
+// smallest rank preconditioned in FP32 (CTGPU_SVD_F32_MIN overrides; 0 disables)
+static int svd_f32_min()
+{
+	static const int v = [] {
+		const char* e = getenv("CTGPU_SVD_F32_MIN");
+		return e ? atoi(e) : SVD_F32_MIN_RANK;
+	}();
+	return v;
+}
+
+// CTAs of the FP32 sweeps (CTGPU_SVD_F32_CLUSTER overrides; a power of two)
+static int svd_f32_cluster()
+{
+	static const int v = [] {
+		const char* e = getenv("CTGPU_SVD_F32_CLUSTER");
+		int c = e ? atoi(e) : SVD_F32_CLUSTER;
+		int p = 1;
+		while (p < c && p < 16) p *= 2;
+		return p;
+	}();
+	return v;
+}
+
 static i64 tour_smem_bytes(int M, int N, int cl)
 {
-	const i64 nblk = 2 * cl, bsmax = (N + nblk - 1) / nblk;
-	const i64 jac = 4 * bsmax * 2 * N + 4 * bsmax + 3 * SVD_STEP_PAIRS + SVD_STEP_PAIRS / 2 + 16;
+	const i64 jac = tour_jac_doubles(N, cl);
 	const i64 out = (i64)NWARPS * M;
 	i64 need = jac > out ? jac : out;
+	// FP32 preconditioning, where the rank may reach the threshold and the staging fits
+	const int f32 = svd_f32_min();
+	if (f32 > 0 && N >= f32 && 8 * precond_doubles(N, cl) <= SVD_SMEM_LIMIT && precond_doubles(N, cl) > need)
+		need = precond_doubles(N, cl);
 	// distributed QR (clusters of more than one CTA): own columns, norms, reflector, exchange slots
 	const i64 nloc = (N + cl - 1) / cl;
 	const i64 qr = nloc * M + 2 * nloc + M + 16 + 16 + 2 + (16 + nloc + 1) / 2 + 8;
@@ -1337,7 +1646,7 @@ void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* d
 		attr_set[dev] = true;
 	}
 	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, flops, g.cluster, g.smem,
-	                             phase_ts));
+	                             phase_ts, svd_f32_min(), svd_f32_cluster()));
 }
 
 }  // namespace ctg
