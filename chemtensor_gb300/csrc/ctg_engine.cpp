@@ -434,6 +434,12 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	p.splits = at<GemmSplit>(p.desc, o_splits);
 	p.nsplits = (int)l.splits.size();
 	if (l.work_doubles > 0) p.work = std::make_shared<DBuf>(&c, (size_t)l.work_doubles * sizeof(double));
+	if (!l.splits.empty())
+	{
+		// completion counters of the split tiles: zero now, and reset by the kernel after each use
+		p.counters = std::make_shared<DBuf>(&c, l.splits.size() * sizeof(int));
+		CTG_CUDA(cudaMemsetAsync(p.counters->ptr, 0, l.splits.size() * sizeof(int), c.stream()));
+	}
 	p.ntiles[0] = (int)l.tiles.size();
 	p.tiles[0] = at<GemmTile>(p.desc, o_tiles);
 	p.flops = l.flops;
@@ -459,15 +465,11 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 		return;
 	}
 	double* w = work ? (double*)work->ptr : nullptr;
+	int* cnt = counters ? (int*)counters->ptr : nullptr;
 	if (ntiles[0] > 0)
 	{
 		KScope ks(c, K_GEMM, 1, flops, 0);
-		launch_gemm_f64(ntiles[0], tiles[0], outs, cons, A, B, C, w, c.stream());
-	}
-	if (nsplits > 0)
-	{
-		KScope ks(c, K_GEMM, 1, 0, 0);
-		launch_gemm_reduce(nsplits, splits, outs, w, C, c.stream());
+		launch_gemm_f64(ntiles[0], tiles[0], outs, cons, splits, cnt, A, B, C, w, c.stream());
 	}
 	c.gemm_flops += flops;
 }

@@ -164,6 +164,7 @@ struct DotPlan {
 	const GemmSplit* splits = nullptr;   // tiles whose sum is split over several CTAs
 	int nsplits = 0;
 	DBufPtr work;                        // their partial sums
+	DBufPtr counters;                    // their completion counters (one int per split tile)
 	i64 a_entries = 0, b_entries = 0;    // entries of the two operand tensors
 	// tensor-core path: packed operand records (see launch_tc_pack) and per-contribution records
 	const TcContrib* tcons = nullptr;

@@ -8,11 +8,13 @@ namespace ctg {
 // ------------------------------------------------------------------------------------
 
 constexpr int GEMM_THREADS = 256;     // 16 x 16 thread grid for every tile class
-constexpr int GEMM_SMEM_DOUBLES = 16 * (64 + 1) * 2;
+constexpr int GEMM_SMEM_DOUBLES = 16 * (128 + 1 + 8 + 1);
+constexpr int GEMM_DIRECT_K = 4;      // contributions up to this k skip the shared-memory staging
 
 template <int BM, int BN, int BK, int TM, int TN>
 __device__ __forceinline__ void gemm_tile_f64(const GemmTile& tile, const GemmOut* __restrict__ outs,
-                                              const GemmContrib* __restrict__ cons, const double* __restrict__ A,
+                                              const GemmContrib* __restrict__ cons, const GemmSplit* __restrict__ splits,
+                                              int* __restrict__ counters, const double* __restrict__ A,
                                               const double* __restrict__ B, double* __restrict__ C,
                                               double* __restrict__ work, double* sm)
 {
@@ -35,6 +37,34 @@ __device__ __forceinline__ void gemm_tile_f64(const GemmTile& tile, const GemmOu
 		const double* a = A + g.a_off;
 		const double* b = B + g.b_off;
 		const int kb = (c == tile.c0 ? tile.k0 : 0), ke = (c == tile.c1 ? tile.k1 : g.k);
+		if (ke - kb <= GEMM_DIRECT_K)
+		{
+			// short contraction (most contributions of a block-sparse DMRG contraction have k <= 2):
+			// operands straight from global memory through L1, no staging and no barrier. Same
+			// accumulation order as the staged path.
+#pragma unroll 1
+			for (int kk = kb; kk < ke; kk++)
+			{
+				double av[TM], bv[TN];
+#pragma unroll
+				for (int i = 0; i < TM; i++)
+				{
+					const int gi = tile.m0 + ty + i * NTY;
+					av[i] = gi < o.m ? a[(i64)gi * g.sAm + (i64)kk * g.sAk] : 0.0;
+				}
+#pragma unroll
+				for (int j = 0; j < TN; j++)
+				{
+					const int gj = tile.n0 + tx + j * NTX;
+					bv[j] = gj < o.n ? b[(i64)kk * g.sBk + (i64)gj * g.sBn] : 0.0;
+				}
+#pragma unroll
+				for (int i = 0; i < TM; i++)
+#pragma unroll
+					for (int j = 0; j < TN; j++) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+			}
+			continue;
+		}
 		for (int k0 = kb; k0 < ke; k0 += BK)
 		{
 			// A tile: BM x BK; the thread-to-element map follows the unit-stride index
@@ -92,14 +122,33 @@ __device__ __forceinline__ void gemm_tile_f64(const GemmTile& tile, const GemmOu
 			__syncthreads();
 		}
 	}
-	if (tile.part >= 0)
+	if (tile.split >= 0)
 	{
-		// partial sum of a split tile (full BM x BN, leading dimension BN)
-		double* w = work + tile.part;
+		// partial sum of a split tile (full BM x BN, leading dimension BN); the CTA that completes
+		// the split last adds the partial sums in share order (deterministic) and writes C
+		const GemmSplit sp = splits[tile.split];
+		double* w = work + sp.part + (i64)tile.sp * sp.stride;
 #pragma unroll
 		for (int i = 0; i < TM; i++)
 #pragma unroll
 			for (int j = 0; j < TN; j++) w[(ty + i * NTY) * BN + tx + j * NTX] = acc[i][j];
+		__threadfence();
+		__syncthreads();
+		__shared__ int last;
+		if (tid == 0) last = atomicAdd(counters + tile.split, 1) == sp.nsplit - 1;
+		__syncthreads();
+		if (!last) return;
+		__threadfence();
+		double* cblk = C + o.c_off;
+		for (int e = tid; e < sp.rows * sp.cols; e += NT)
+		{
+			const int i = e / sp.cols, j = e - i * sp.cols;
+			const double* pw = work + sp.part + (i64)i * sp.ld + j;
+			double sum = 0.0;
+			for (int q = 0; q < sp.nsplit; q++) sum += __ldcg(pw + (i64)q * sp.stride);
+			cblk[(i64)(sp.m0 + i) * o.n + sp.n0 + j] = sum;
+		}
+		if (tid == 0) counters[tile.split] = 0;
 		return;
 	}
 	double* cblk = C + o.c_off;
@@ -117,73 +166,45 @@ __device__ __forceinline__ void gemm_tile_f64(const GemmTile& tile, const GemmOu
 	}
 }
 
-__global__ void __launch_bounds__(GEMM_THREADS)
+__global__ void __launch_bounds__(GEMM_THREADS, 3)
 k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const GemmContrib* __restrict__ cons,
-           const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C, double* __restrict__ work)
+           const GemmSplit* __restrict__ splits, int* __restrict__ counters, const double* __restrict__ A,
+           const double* __restrict__ B, double* __restrict__ C, double* __restrict__ work)
 {
 	__shared__ double sm[GEMM_SMEM_DOUBLES];
 	const GemmTile tile = tiles[blockIdx.x];
 	switch (tile.cls)
 	{
-	case TILE_L: gemm_tile_f64<64, 64, 16, 4, 4>(tile, outs, cons, A, B, C, work, sm); break;
-	case TILE_M: gemm_tile_f64<32, 32, 16, 2, 2>(tile, outs, cons, A, B, C, work, sm); break;
-	case TILE_W: gemm_tile_f64<16, 64, 16, 1, 4>(tile, outs, cons, A, B, C, work, sm); break;
-	case TILE_T: gemm_tile_f64<64, 16, 16, 4, 1>(tile, outs, cons, A, B, C, work, sm); break;
-	default:     gemm_tile_f64<16, 16, 16, 1, 1>(tile, outs, cons, A, B, C, work, sm); break;
+	case TILE_L: gemm_tile_f64<64, 64, 16, 4, 4>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_M: gemm_tile_f64<32, 32, 16, 2, 2>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_W: gemm_tile_f64<16, 64, 16, 1, 4>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_T: gemm_tile_f64<64, 16, 16, 4, 1>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_R8: gemm_tile_f64<8, 32, 16, 1, 1>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_R4: gemm_tile_f64<4, 64, 16, 1, 1>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_C8: gemm_tile_f64<32, 8, 16, 1, 1>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_C4: gemm_tile_f64<64, 4, 16, 1, 1>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_W8: gemm_tile_f64<8, 128, 16, 1, 4>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	case TILE_T8: gemm_tile_f64<128, 8, 16, 4, 1>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
+	default:     gemm_tile_f64<16, 16, 16, 1, 1>(tile, outs, cons, splits, counters, A, B, C, work, sm); break;
 	}
-}
-
-// sums the partial tiles of each split tile in order of the split index
-__global__ void __launch_bounds__(256)
-k_gemm_reduce(const GemmSplit* __restrict__ splits, const GemmOut* __restrict__ outs, const double* __restrict__ work,
-              double* __restrict__ C)
-{
-	const GemmSplit sp = splits[blockIdx.x];
-	const GemmOut o = outs[sp.out];
-	double* cblk = C + o.c_off;
-	for (int e = threadIdx.x; e < sp.rows * sp.cols; e += blockDim.x)
-	{
-		const int i = e / sp.cols, j = e - i * sp.cols;
-		const double* w = work + sp.part + (i64)i * sp.ld + j;
-		double acc = 0.0;
-		for (int p = 0; p < sp.nsplit; p++) acc += w[(i64)p * sp.stride];
-		cblk[(i64)(sp.m0 + i) * o.n + sp.n0 + j] = acc;
-	}
-}
-
-void launch_gemm_reduce(int nsplit, const GemmSplit* splits, const GemmOut* outs, const double* work, double* C,
-                        cudaStream_t st)
-{
-	if (nsplit <= 0) return;
-	k_gemm_reduce<<<nsplit, 256, 0, st>>>(splits, outs, work, C);
-	CTG_CUDA(cudaGetLastError());
 }
 
 int tile_rows(int cls)
 {
-	switch (cls)
-	{
-	case TILE_L: case TILE_T: return 64;
-	case TILE_M: return 32;
-	default: return 16;
-	}
+	return TILE_ROWS[cls];
 }
 
 int tile_cols(int cls)
 {
-	switch (cls)
-	{
-	case TILE_L: case TILE_W: return 64;
-	case TILE_M: return 32;
-	default: return 16;
-	}
+	return TILE_COLS[cls];
 }
 
-void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons, const double* A,
-                     const double* B, double* C, double* work, cudaStream_t st)
+void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
+                     const GemmSplit* splits, int* counters, const double* A, const double* B, double* C, double* work,
+                     cudaStream_t st)
 {
 	if (ntiles <= 0) return;
-	k_gemm_f64<<<ntiles, GEMM_THREADS, 0, st>>>(tiles, outs, cons, A, B, C, work);
+	k_gemm_f64<<<ntiles, GEMM_THREADS, 0, st>>>(tiles, outs, cons, splits, counters, A, B, C, work);
 	CTG_CUDA(cudaGetLastError());
 }
 

@@ -28,15 +28,16 @@ struct GemmContrib {
 
 // One CTA's share of an output tile: the terms from (contribution c0, k = k0) up to (contribution c1,
 // k = k1 exclusive) of the tile's sum over its contributions and their inner index k, in order.
-// part < 0: the share is the whole sum and goes to C; otherwise the CTA writes its partial sum to
-// work[part + i * tile_cols + j] and a GemmSplit entry adds the partial sums in order.
+// split < 0: the share is the whole sum and goes to C; otherwise the CTA is share sp of GemmSplit
+// entry `split`: it writes its partial sum to work[part + sp * stride + i * ld + j], and the CTA
+// that finishes its split last adds the partial sums in order of sp and writes C.
 struct GemmTile {
 	int out;           // output block
 	int m0, n0;        // tile origin inside the output block
 	int c0, k0;
 	int c1, k1;        // c1 < c0: no terms (the tile is written as zeros)
 	int cls;           // tile class (shape), see TILE_*
-	i64 part;
+	int split, sp;
 };
 
 // A tile whose sum is split over nsplit CTAs: C = sum over p < nsplit of the partial tile at
@@ -46,17 +47,24 @@ struct GemmSplit {
 	i64 part;
 };
 
-// tile classes (rows x cols of C per CTA)
-// S 16 x 16, M 32 x 32, L 64 x 64, W 16 x 64 (few rows), T 64 x 16 (few columns)
-enum { TILE_S = 0, TILE_M = 1, TILE_L = 2, TILE_W = 3, TILE_T = 4, NUM_TILE_CLASSES = 5 };
+// tile classes (rows x cols of C per CTA of 256 threads): 256 outputs, one per thread (S 16 x 16,
+// R8 8 x 32, R4 4 x 64, C8 32 x 8, C4 64 x 4); 1024 outputs, four per thread (M 32 x 32, W 16 x 64,
+// T 64 x 16, W8 8 x 128, T8 128 x 8); L 64 x 64, sixteen per thread. Block-sparse DMRG outputs are
+// mostly small and skinny, and FP64 FMAs spent on tile padding cost as much as useful ones.
+enum {
+	TILE_S = 0, TILE_M, TILE_L, TILE_W, TILE_T, TILE_R8, TILE_R4, TILE_C8, TILE_C4, TILE_W8, TILE_T8,
+	NUM_TILE_CLASSES
+};
+constexpr int TILE_ROWS[NUM_TILE_CLASSES] = {16, 32, 64, 16, 64, 8, 4, 32, 64, 8, 128};
+constexpr int TILE_COLS[NUM_TILE_CLASSES] = {16, 32, 64, 64, 16, 32, 64, 8, 4, 128, 8};
 int tile_rows(int cls);
 int tile_cols(int cls);
 
-// every tile of every class in one launch (256 threads per CTA, the tile's class picks its shape)
-void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons, const double* A,
-                     const double* B, double* C, double* work, cudaStream_t st);
-void launch_gemm_reduce(int nsplit, const GemmSplit* splits, const GemmOut* outs, const double* work, double* C,
-                        cudaStream_t st);
+// every tile of every class in one launch (256 threads per CTA, the tile's class picks its shape);
+// split tiles use `counters` (one per GemmSplit, zero before the launch and again after it)
+void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
+                     const GemmSplit* splits, int* counters, const double* A, const double* B, double* C, double* work,
+                     cudaStream_t st);
 
 // Same work lists on the tcgen05 tensor cores, split-BF16 (hi*hi + hi*lo + lo*hi, FP32
 // accumulation, FP64 out); output tiles of tc_tile_rows() x tc_tile_cols().

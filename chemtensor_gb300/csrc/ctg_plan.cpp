@@ -45,14 +45,25 @@ struct AxisFan {
 	i64 count(i64 b) const { return start[(size_t)b + 1] - start[(size_t)b]; }
 };
 
-int tile_class(int m, int n)
+int tile_class(int m, int n, bool allow_large)
 {
-	// the tile that pads the block least (FP64 FMAs on padding cost as much as useful ones)
-	if (m <= 16 && n <= 16) return TILE_S;
-	if (m <= 16) return TILE_W;
-	if (n <= 16) return TILE_T;
-	if (m <= 32 || n <= 32) return TILE_M;
-	return TILE_L;
+	// the tile shape with the fewest padded outputs, counting 128 outputs of fixed cost per tile;
+	// 64 x 64 tiles only in products large enough to fill every SM with them (one such tile holds
+	// 65536 FMAs per 16-wide k chunk, a long serial share when the whole product is small)
+	int best = TILE_S;
+	i64 best_cost = INT64_MAX;
+	for (int c = 0; c < NUM_TILE_CLASSES; c++)
+	{
+		if (c == TILE_L && !allow_large) continue;
+		const i64 tr = TILE_ROWS[c], tc = TILE_COLS[c];
+		const i64 cost = ((m + tr - 1) / tr) * ((n + tc - 1) / tc) * (tr * tc + 128);
+		if (cost < best_cost)
+		{
+			best_cost = cost;
+			best = c;
+		}
+	}
+	return best;
 }
 
 void check_rows(const std::vector<RowDesc>& descs, const std::vector<i64>& maps, i64 src_nnz, i64 dst_nnz)
@@ -148,7 +159,27 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 		hi = lo;
 		while (hi < v.size() && v[hi].f == f) hi++;
 	};
+	// operand geometry per block, once: rows of the leading and trailing axis groups, entries
+	auto geometry = [](const Meta& m, int nld, std::vector<i64>& lead, std::vector<i64>& trail) {
+		lead.resize((size_t)m.nblocks);
+		trail.resize((size_t)m.nblocks);
+		for (int b = 0; b < m.nblocks; b++)
+		{
+			const i64* d = m.dims(b);
+			lead[(size_t)b] = prod(d, nld);
+			trail[(size_t)b] = prod(d + nld, m.ndim - nld);
+		}
+	};
+	std::vector<i64> s_lead, s_trail, t_lead, t_trail;
+	geometry(s, nlds, s_lead, s_trail);
+	geometry(t, nldt, t_lead, t_trail);
+	constexpr int KCH = 16;                      // k chunk of the FP64 kernels
+	std::vector<i64> nchunk((size_t)r.nblocks, 0), ksum((size_t)r.nblocks, 0);
+	cons.reserve(ks.size() + (size_t)r.nblocks);
+	for (int k = 0; k < NUM_TILE_CLASSES; k++) tiles[k].reserve((size_t)r.nblocks);
 	double flops = 0;
+	i64 fs_prev = -1;
+	size_t s0 = 0, s1 = 0, tcur = 0;
 	for (int b = 0; b < r.nblocks; b++)
 	{
 		const i64* ir = r.index(b);
@@ -161,18 +192,27 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 		i64 fs = 0, ft = 0;
 		for (int i = 0; i < nfs; i++) fs = fs * r.nb[i] + ir[i];
 		for (int i = 0; i < nft; i++) ft = ft * r.nb[nfs + i] + ir[nfs + i];
-		size_t s0, s1, t0, t1;
-		run_of(ks, fs, s0, s1);
-		run_of(kt, ft, t0, t1);
+		// output blocks come in row-major order: the s run changes only with fs, and within one fs
+		// the t free indices increase, so the t runs are found by a forward scan
+		if (fs != fs_prev)
+		{
+			run_of(ks, fs, s0, s1);
+			fs_prev = fs;
+			tcur = 0;
+		}
+		while (tcur < kt.size() && kt[tcur].f < ft) tcur++;
+		const size_t t0 = tcur;
+		size_t t1 = t0;
+		while (t1 < kt.size() && kt[t1].f == ft) t1++;
 		CTG_CHECK(s1 - s0 == t1 - t0, "dot: operand block runs differ");
+		const double mn2 = 2.0 * (double)o.m * (double)o.n;
+		i64 nch = 0;
 		for (size_t x = s0, y = t0; x < s1; x++, y++)
 		{
 			CTG_CHECK(ks[x].c == kt[y].c, "dot: missing partner block");
 			const int bs = ks[x].b, bt = kt[y].b;
-			const i64* sd = s.dims(bs);
-			const i64* td = t.dims(bt);
-			const i64 lds = prod(sd, nlds), tds = prod(sd + nlds, s.ndim - nlds);
-			const i64 ldt = prod(td, nldt), tdt = prod(td + nldt, t.ndim - nldt);
+			const i64 lds = s_lead[(size_t)bs], tds = s_trail[(size_t)bs];
+			const i64 ldt = t_lead[(size_t)bt], tdt = t_trail[(size_t)bt];
 			GemmContrib g;
 			g.a_off = s.boff[bs];
 			g.b_off = t.boff[bt];
@@ -184,28 +224,37 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			else { g.sBk = 1; g.sBn = (int)tdt; }
 			CTG_CHECK(k == (axt == AX_LEADING ? ldt : tdt), "dot: inner dimensions differ");
 			// every operand access stays inside its block (checked once per plan, on the host)
-			CTG_CHECK(k >= 1 && g.a_off + (i64)(o.m - 1) * g.sAm + (k - 1) * g.sAk < s.boff[bs] + s.block_size(bs),
+			CTG_CHECK(k >= 1 && g.a_off + (i64)(o.m - 1) * g.sAm + (k - 1) * g.sAk < s.boff[bs] + lds * tds,
 			          "dot: A operand out of range");
-			CTG_CHECK(g.b_off + (k - 1) * g.sBk + (i64)(o.n - 1) * g.sBn < t.boff[bt] + t.block_size(bt),
+			CTG_CHECK(g.b_off + (k - 1) * g.sBk + (i64)(o.n - 1) * g.sBn < t.boff[bt] + ldt * tdt,
 			          "dot: B operand out of range");
 			cons.push_back(g);
-			con_blocks.emplace_back(bs, bt);
-			flops += 2.0 * (double)o.m * (double)o.n * (double)k;
-			p.flops_cls[tile_class(o.m, o.n)] += 2.0 * (double)o.m * (double)o.n * (double)k;
+			if (precision == GEMM_BF16X3) con_blocks.emplace_back(bs, bt);
+			flops += mn2 * (double)k;
+			ksum[(size_t)b] += k;
+			nch += (k + KCH - 1) / KCH;
 		}
+		nchunk[(size_t)b] = nch;
 		o.nc = (int)cons.size() - o.c0;
 		CTG_CHECK(o.m >= 1 && o.n >= 1 && o.c_off + (i64)o.m * o.n <= r.nnz, "dot: output block out of range");
-		// every tile first takes the whole sum over the block's contributions
+	}
+	// tiles: every tile first takes the whole sum over its output block's contributions
+	const bool allow_large = flops / 2 > (double)num_sms * 8 * 65536;
+	for (int b = 0; b < r.nblocks; b++)
+	{
+		const GemmOut& o = outs[(size_t)b];
 		GemmTile whole = {};
 		whole.out = b;
 		whole.c0 = o.c0;
 		whole.k0 = 0;
 		whole.c1 = o.c0 + o.nc - 1;
 		whole.k1 = o.nc > 0 ? cons[(size_t)whole.c1].k : 0;
-		whole.part = -1;
+		whole.split = -1;
+		whole.sp = 0;
 		if (precision == GEMM_BF16X3)
 		{
 			// tensor-core tiles: one tile class
+			p.flops_cls[0] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
 			for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
 				for (int n0 = 0; n0 < o.n; n0 += tc_tile_cols())
 				{
@@ -215,7 +264,8 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 				}
 			continue;
 		}
-		const int cls = tile_class(o.m, o.n);
+		const int cls = tile_class(o.m, o.n, allow_large);
+		p.flops_cls[cls] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
 		const int tr = tile_rows(cls), tc = tile_cols(cls);
 		whole.cls = cls;
 		for (int m0 = 0; m0 < o.m; m0 += tr)
@@ -229,24 +279,18 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 	// Split-K: on GB300 one SM retires about two FP64 FMAs per clock, so a block GEMM with fewer
 	// tiles than SMs leaves most of the FP64 pipes idle. Tiles whose work exceeds a fair share of
 	// the whole product are cut into shares of consecutive 16-wide k chunks, one CTA each; their
-	// partial sums are added in a fixed order (deterministic) by k_gemm_reduce.
+	// partial sums are added in a fixed order (deterministic) by the CTA that completes the split last.
 	g_plan_stage[1] += host_seconds() - ts0;
 	ts0 = host_seconds();
 	std::vector<GemmSplit> splits;
 	i64 wsz = 0;
 	if (precision != GEMM_BF16X3)
 	{
-		constexpr int KCH = 16;                  // k chunk of the FP64 kernels
-		auto nchunks = [&](const GemmOut& o) {
-			i64 n = 0;
-			for (int cc = o.c0; cc < o.c0 + o.nc; cc++) n += (cons[(size_t)cc].k + KCH - 1) / KCH;
-			return n;
-		};
 		double total = 0;
 		for (int k = 0; k < NUM_TILE_CLASSES; k++)
 			for (const GemmTile& t : tiles[k])
-				total += (double)tile_rows(k) * tile_cols(k) * (double)(nchunks(outs[(size_t)t.out]) * KCH);
-		const double target = std::max(total / (2.0 * num_sms), 65536.0);
+				total += (double)tile_rows(k) * tile_cols(k) * (double)(nchunk[(size_t)t.out] * KCH);
+		const double target = std::max(total / (2.0 * num_sms), 16384.0);
 		std::vector<std::pair<int, int>> pos;
 		for (int k = 0; k < NUM_TILE_CLASSES; k++)
 		{
@@ -255,7 +299,7 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			for (const GemmTile& t : tiles[k])
 			{
 				const GemmOut& o = outs[(size_t)t.out];
-				const i64 n = nchunks(o);
+				const i64 n = nchunk[(size_t)t.out];
 				const double w = (double)tr * tc * (double)(n * KCH);
 				const int S = (int)std::min<double>((double)n, std::ceil(w / target));
 				if (S <= 1)
@@ -274,7 +318,8 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 					u.k0 = pos[(size_t)a].second;
 					u.c1 = pos[(size_t)e - 1].first;
 					u.k1 = std::min(pos[(size_t)e - 1].second + KCH, cons[(size_t)u.c1].k);
-					u.part = wsz + (i64)sp * tr * tc;
+					u.split = (int)splits.size();
+					u.sp = sp;
 					kept.push_back(u);
 				}
 				GemmSplit g = {};

@@ -30,6 +30,7 @@
 
 #include <cooperative_groups.h>
 
+#include "ctg_fp64.cuh"
 #include "ctg_kernels.h"
 #include "ctg_svd_schedule.h"
 
@@ -526,14 +527,20 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 }
 
 // Householder QR with column pivoting of the scaled block over a whole cluster. Column j lives in
-// the shared memory of CTA j % cl; columns are not moved: every step the CTAs exchange their
-// largest remaining trailing norm (distributed shared memory, one cluster barrier), the owner of the
-// pivot column forms the reflector and writes it into every CTA's shared memory (second barrier),
-// and each CTA applies it to its own remaining columns and downdates their norms (recomputed when
-// cancellation has eaten more than sqrt(eps) of the last exact value, as LAPACK's xLAQP2). At the
-// end the columns go to global memory in pivot order (the layout of qr_pivoted_cta: R in the upper
-// triangle, reflector k below the diagonal of column k, perm[k] the source column), followed by the
-// columns beyond the numerical rank in source order. Returns the rank; writes tau, perm, misc.
+// the shared memory of CTA j % cl; columns are not moved. Every step each CTA forms, in its own
+// shared memory, the reflector of its best remaining column (speculatively: only the pivot's is
+// used) and sends that column's squared norm, index and reflector scalars to every CTA; after one
+// cluster barrier all CTAs agree on the pivot (largest norm, then smallest index), copy its
+// reflector from the owner's shared memory (distributed shared memory, double-buffered by step
+// parity) and apply it to their own remaining columns, downdating the norms (recomputed when
+// cancellation has eaten more than sqrt(eps) of the last exact value, as in qr_pivoted_cta).
+// Its shared memory (doubles):
+__host__ __device__ inline i64 qr_cluster_doubles(int M, int N, int cl)
+{
+	const i64 nloc = (N + cl - 1) / cl;
+	return nloc * M + 2 * nloc + 3 * (i64)M + 16 + 3 * 2 * 16 + (2 * 16 + nloc + 1) / 2 + 8;
+}
+
 __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, const double* ab, bool tall, int n, int M, int N,
                                   int cl, const SvdScratch& xs)
 {
@@ -544,14 +551,17 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 	double* qcol = smem;                                 // nloc_max x M
 	double* qnrm = qcol + (i64)nloc_max * M;
 	double* qref = qnrm + nloc_max;
-	double* vbuf = qref + nloc_max;                      // reflector of the current step (rows k..M-1)
-	double* cand = vbuf + M;                             // [cl] best squared norm per CTA
-	double* part = cand + 16;                            // [cl] partial Frobenius sums
-	double* scal = part + 16;                            // [0] tau of the current step
-	int* cidx = (int*)(scal + 2);                        // [cl] column of the best norm per CTA
-	int* qdone = cidx + 16;                              // [nloc_max] step that took the column, or -1
+	double* vbuf = qref + nloc_max;                      // pivot reflector of the current step (rows k..M-1)
+	double* cbuf = vbuf + M;                             // [2][M] own candidate reflector, by step parity
+	double* part = cbuf + 2 * (i64)M;                    // [cl] partial Frobenius sums
+	double* hnrm = part + 16;                            // [2][16] candidate squared norm per CTA
+	double* htau = hnrm + 32;                            // [2][16] candidate tau per CTA
+	double* hbeta = htau + 32;                           // [2][16] candidate beta per CTA
+	int* hidx = (int*)(hbeta + 32);                      // [2][16] candidate column per CTA
+	int* qdone = hidx + 32;                              // [nloc_max] step that took the column, or -1
 	__shared__ double red[NWARPS];
-	__shared__ double sh_beta, sh_scale;
+	__shared__ double sh_tau, sh_beta, sh_scale, sh_best;
+	__shared__ int sh_jl;
 
 	// load the own columns (B oriented tall) and their squared sums
 	double psum = 0;
@@ -593,75 +603,100 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 	int r = 0;
 	for (int k = 0; k < N; k++)
 	{
-		// a. this CTA's best remaining column, to every CTA
+		const int par = k & 1;
+		// a. this CTA's best remaining column
 		if (warp == 0)
 		{
 			double best = -1;
-			int bi = N;
+			int bi = N, bj = -1;
 			for (int jl = lane; jl < nloc; jl += 32)
-				if (qdone[jl] < 0 && qnrm[jl] > best) { best = qnrm[jl]; bi = rank + cl * jl; }
+				if (qdone[jl] < 0 && qnrm[jl] > best) { best = qnrm[jl]; bi = rank + cl * jl; bj = jl; }
 #pragma unroll
 			for (int o = 16; o > 0; o >>= 1)
 			{
 				const double ob = __shfl_xor_sync(0xffffffffu, best, o);
 				const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-				if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+				const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+				if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; bj = oj; }
 			}
-			if (lane < cl)
+			if (lane == 0)
 			{
-				*cluster.map_shared_rank(cand + rank, (unsigned)lane) = best;
-				*cluster.map_shared_rank(cidx + rank, (unsigned)lane) = bi;
+				sh_best = best;
+				sh_jl = bj;
 			}
 		}
-		cluster.sync();
-		// b. the pivot (identical in every CTA)
-		double pv = -1;
-		int p = N;
-		for (int i = 0; i < cl; i++)
-			if (cand[i] > pv || (cand[i] == pv && cidx[i] < p)) { pv = cand[i]; p = cidx[i]; }
-		if (pv <= thresh || pv <= 0.0 || p >= N) break;
-		// c. the owner forms the reflector and sends it to every CTA
-		if (p % cl == rank)
+		__syncthreads();
+		// b. its reflector, formed speculatively in this CTA's own shared memory
+		const int bj = sh_jl;
+		const double best = sh_best;
+		double* cb = cbuf + (i64)par * M;
+		if (bj >= 0 && best > thresh)
 		{
-			double* w = qcol + (i64)(p / cl) * M;
+			const double* w = qcol + (i64)bj * M;
 			double part2 = 0;
 			for (int i = k + 1 + tid; i < M; i += SVD_THREADS) part2 = fma(w[i], w[i], part2);
 			const double xnorm2 = block_sum(part2, red);
 			if (tid == 0)
 			{
 				const double alpha = w[k];
-				double tk;
 				if (xnorm2 == 0.0)
 				{
-					tk = 0.0;
+					sh_tau = 0.0;
 					sh_beta = alpha;
 					sh_scale = 0.0;
 				}
 				else
 				{
-					const double beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
-					tk = (beta - alpha) / beta;
+					// |beta| >= the remaining norm, above the rank threshold: normal doubles
+					const double beta = -copysign(sqrt64(fma(alpha, alpha, xnorm2)), alpha);
+					sh_tau = (beta - alpha) * rcp64(beta);
 					sh_beta = beta;
-					sh_scale = 1.0 / (alpha - beta);
+					sh_scale = rcp64(alpha - beta);
 				}
-				xs.tau[k] = tk;
-				for (int c2 = 0; c2 < cl; c2++) *cluster.map_shared_rank(scal, (unsigned)c2) = tk;
-				qdone[p / cl] = k;
 			}
 			__syncthreads();
-			for (int i = k + 1 + tid; i < M; i += SVD_THREADS) w[i] *= sh_scale;
-			__syncthreads();
-			if (tid == 0) w[k] = sh_beta;
-			// reflector v = (1, w[k+1 ..]) into every CTA's vbuf
-			for (i64 e = tid; e < (i64)(M - k) * cl; e += SVD_THREADS)
-			{
-				const int c2 = (int)(e / (M - k)), i = k + (int)(e % (M - k));
-				*cluster.map_shared_rank(vbuf + i, (unsigned)c2) = (i == k) ? 1.0 : w[i];
-			}
+			const double scl = sh_scale;
+			for (int i = k + tid; i < M; i += SVD_THREADS) cb[i] = (i == k) ? 1.0 : w[i] * scl;
+		}
+		// c. its candidate to every CTA, one cluster barrier, the pivot
+		if (tid < cl)
+		{
+			const bool has = bj >= 0 && best > thresh;
+			*cluster.map_shared_rank(hnrm + par * 16 + rank, (unsigned)tid) = has ? best : -1.0;
+			*cluster.map_shared_rank(hidx + par * 16 + rank, (unsigned)tid) = has ? rank + cl * bj : N;
+			*cluster.map_shared_rank(htau + par * 16 + rank, (unsigned)tid) = has ? sh_tau : 0.0;
+			*cluster.map_shared_rank(hbeta + par * 16 + rank, (unsigned)tid) = has ? sh_beta : 0.0;
 		}
 		cluster.sync();
-		// d. apply the reflector to the own remaining columns, downdate their norms
-		const double tk = scal[0];
+		double pv = -1;
+		int p = N, owner = 0;
+		for (int i = 0; i < cl; i++)
+		{
+			const double c = hnrm[par * 16 + i];
+			const int ci = hidx[par * 16 + i];
+			if (c > pv || (c == pv && ci < p)) { pv = c; p = ci; owner = i; }
+		}
+		if (pv <= thresh || pv <= 0.0 || p >= N) break;
+		const double tk = htau[par * 16 + owner];
+		// d. the pivot's reflector from its owner; the owner stores R_kk and the reflector in place
+		{
+			const double* src = owner == rank ? cb : cluster.map_shared_rank(cbuf + (i64)par * M, (unsigned)owner);
+			for (int i = k + tid; i < M; i += SVD_THREADS) vbuf[i] = src[i];
+		}
+		if (owner == rank)
+		{
+			const int jl = p / cl;
+			double* w = qcol + (i64)jl * M;
+			for (int i = k + 1 + tid; i < M; i += SVD_THREADS) w[i] = cb[i];
+			if (tid == 0)
+			{
+				w[k] = hbeta[par * 16 + owner];
+				xs.tau[k] = tk;
+				qdone[jl] = k;
+			}
+		}
+		__syncthreads();
+		// e. apply the reflector to the own remaining columns, downdate their norms
 		for (int jl = warp; jl < nloc; jl += NWARPS)
 		{
 			if (qdone[jl] >= 0) continue;
@@ -1551,9 +1586,8 @@ static i64 tour_smem_bytes(int M, int N, int cl)
 	const int f32 = svd_f32_min();
 	if (f32 > 0 && N >= f32 && 8 * precond_doubles(N, cl) <= SVD_SMEM_LIMIT && precond_doubles(N, cl) > need)
 		need = precond_doubles(N, cl);
-	// distributed QR (clusters of more than one CTA): own columns, norms, reflector, exchange slots
-	const i64 nloc = (N + cl - 1) / cl;
-	const i64 qr = nloc * M + 2 * nloc + M + 16 + 16 + 2 + (16 + nloc + 1) / 2 + 8;
+	// distributed QR (clusters of more than one CTA): own columns, norms, reflectors, exchange slots
+	const i64 qr = qr_cluster_doubles(M, N, cl);
 	if (cl > 1 && qr > need) need = qr;
 	// pivoted QR staged in shared memory when the whole block fits
 	if ((i64)M * N * 8 <= SVD_SMEM_LIMIT && (i64)M * N > need) need = (i64)M * N;
