@@ -559,6 +559,7 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	c.plan_misses = 0;
 	for (double& x : c.svd_phase_ms) x = 0;
 	for (double& x : c.svd_jacobi_cycles) x = 0;
+	for (double& x : c.svd_qr_cycles) x = 0;
 	for (double& x : g_host_detail) x = 0;
 	DBuf sc_buf(&c, sizeof(LanczosScalars));
 	LanczosScalars* d_sc = (LanczosScalars*)sc_buf.ptr;
@@ -732,9 +733,13 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		        c.svd_phase_ms[0] / st->sweeps, c.svd_phase_ms[1] / st->sweeps, c.svd_phase_ms[2] / st->sweeps,
 		        c.svd_phase_ms[3] / st->sweeps);
 	if (getenv("CTGPU_SVD_PHASES") && st->sweeps > 0)
-		fprintf(stderr, "ctgpu: Jacobi of that block, SM cycles per sweep: FP64 steps %.3g exchanges %.3g FP32 sweeps %.3g FP32-to-FP64 %.3g\n",
+		fprintf(stderr, "ctgpu: Jacobi of that block, SM cycles per sweep: FP64 steps %.3g exchanges %.3g FP32 sweeps %.3g FP32-to-FP64 %.3g; Jacobi sweeps per sweep: FP64 %.0f FP32 %.0f\n",
 		        c.svd_jacobi_cycles[0] / st->sweeps, c.svd_jacobi_cycles[3] / st->sweeps, c.svd_jacobi_cycles[4] / st->sweeps,
-		        c.svd_jacobi_cycles[5] / st->sweeps);
+		        c.svd_jacobi_cycles[5] / st->sweeps, c.svd_jacobi_cycles[1] / st->sweeps, c.svd_jacobi_cycles[2] / st->sweeps);
+	if (getenv("CTGPU_SVD_PHASES") && st->sweeps > 0)
+		fprintf(stderr, "ctgpu: distributed QR of that block, SM cycles per sweep: candidates %.3g reflectors %.3g exchange %.3g fetch %.3g updates %.3g\n",
+		        c.svd_qr_cycles[0] / st->sweeps, c.svd_qr_cycles[1] / st->sweeps, c.svd_qr_cycles[2] / st->sweeps,
+		        c.svd_qr_cycles[3] / st->sweeps, c.svd_qr_cycles[4] / st->sweeps);
 	st->wall_s = now_s() - t_start;
 	return 0;
 }

@@ -808,7 +808,8 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 	int forced = 0;
 	if (const char* e = getenv("CTGPU_SVD_CLUSTER")) forced = std::max(1, std::min(maxcl, atoi(e)));
 	std::vector<SvdLaunch> cfg(descs.size());
-	for (double slack = 1.5;; slack *= 2)
+	static const double slack0 = getenv("CTGPU_SVD_SLACK") ? atof(getenv("CTGPU_SVD_SLACK")) : 0.75;
+	for (double slack = slack0;; slack *= 2)
 	{
 		int total = 0;
 		for (size_t b = 0; b < descs.size(); b++)
@@ -902,6 +903,16 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 			c.svd_phase_ms[2] += 1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 3] - h[SVD_PHASE_SLOTS * crit + 2]);
 			c.svd_phase_ms[3] += 1e-6 * (double)(t1 - t0);
 			for (int i = 0; i < 6; i++) c.svd_jacobi_cycles[i] += (double)h[SVD_PHASE_SLOTS * crit + 4 + i];
+			for (int i = 0; i < 5; i++) c.svd_qr_cycles[i] += (double)h[SVD_PHASE_SLOTS * crit + 10 + i];
+			// CTGPU_SVD_PHASES=2: one line per call for the block that finished last
+			static const bool each = atoi(getenv("CTGPU_SVD_PHASES")) >= 2;
+			if (each)
+				fprintf(stderr, "ctgpu: svd call: %zu blocks, critical %d x %d (cluster %d): QR %.3f Jacobi %.3f outputs %.3f ms, FP32 sweeps %llu, FP64 sweeps %llu\n",
+				        descs.size(), descs[crit].m, descs[crit].n, cfg[crit].cluster,
+				        1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 1] - h[SVD_PHASE_SLOTS * crit]),
+				        1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 2] - h[SVD_PHASE_SLOTS * crit + 1]),
+				        1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 3] - h[SVD_PHASE_SLOTS * crit + 2]),
+				        h[SVD_PHASE_SLOTS * crit + 6], h[SVD_PHASE_SLOTS * crit + 5]);
 		}
 	}
 	// the status and the flop count reach pinned host memory once the stream gets there (read by

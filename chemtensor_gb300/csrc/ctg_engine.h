@@ -93,7 +93,8 @@ public:
 	// with CTGPU_SVD_PHASES set: summed QR / Jacobi / output / launch time (ms) of the block that
 	// finished last in each block SVD
 	double svd_phase_ms[4] = {0, 0, 0, 0};
-	double svd_jacobi_cycles[6] = {0, 0, 0, 0, 0, 0};   // FP64 steps, -, -, exchanges; FP32 sweeps, hand-over
+	double svd_qr_cycles[5] = {0, 0, 0, 0, 0};     // distributed QR: candidates, reflectors, exchange, fetch, updates
+	double svd_jacobi_cycles[6] = {0, 0, 0, 0, 0, 0};   // FP64 step cycles, FP64 sweeps, FP32 sweeps, exchange / FP32 / hand-over cycles
 	// cache of lowered operations, keyed by operation and operand structures (DMRG revisits the
 	// same block structures every sweep once the bond dimensions have settled)
 	struct PlanCache* plans() { return plans_; }

@@ -48,4 +48,28 @@ __device__ __forceinline__ double sqrt64(double x)
 	return sroot * __hiloint2double((1023 + ex / 2) << 20, 0);
 }
 
+
+// sqrt(x) and 1 / sqrt(x) together for a positive normal double (the reciprocal comes with the
+// square root: one Newton sequence for both, accurate to about one unit in the last place)
+__device__ __forceinline__ void sqrt_rsqrt64(double x, double& sq, double& rsq)
+{
+	const int hi = __double2hiint(x), lo = __double2loint(x);
+	int ex = ((hi >> 20) & 0x7ff) - 1023;
+	double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, lo);             // [1, 2)
+	if (ex & 1)
+	{
+		m *= 2.0;                                                                 // [2, 4)
+		ex -= 1;
+	}
+	float r;
+	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)m));
+	const double y0 = (double)r;
+	const double e = fma(-m * y0, y0, 1.0);
+	const double y = y0 * fma(e, fma(e, 0.375, 0.5), 1.0);
+	double sroot = m * y;
+	sroot = fma(0.5 * y, fma(-sroot, sroot, m), sroot);
+	sq = sroot * __hiloint2double((1023 + ex / 2) << 20, 0);
+	rsq = y * __hiloint2double((1023 - ex / 2) << 20, 0);
+}
+
 }  // namespace ctg

@@ -148,10 +148,12 @@ void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs,
 // products and rotations of the shared-memory path.
 constexpr int SVD_MAX_SWEEPS = 60;
 // per-block diagnostics of the SVD kernel (CTGPU_SVD_PHASES): [0] start, [1] after the QR, [2] after
-// the Jacobi sweeps, [3] end (global timer, ns); SM cycles of the critical CTA in [4] FP64 steps
-// (inner products, rotation parameters, rotations), [5] unused, [6] unused, [7] exchanges, [8] FP32
-// sweeps, [9] FP32 to FP64 hand-over (Newton-Schulz steps and T = R^T V)
-constexpr int SVD_PHASE_SLOTS = 10;
+// the Jacobi sweeps, [3] end (global timer, ns); on the critical CTA: [4] SM cycles of the FP64
+// steps (inner products, rotation parameters, rotations), [5] FP64 sweeps, [6] FP32 sweeps, SM
+// cycles of [7] exchanges, [8] FP32 sweeps, [9] FP32 to FP64 hand-over (Newton-Schulz steps and
+// T = R^T V); SM cycles of the distributed QR's steps in [10] pivot candidates, [11] candidate
+// reflectors, [12] candidate exchange and cluster barrier, [13] pivot reflector fetch, [14] updates
+constexpr int SVD_PHASE_SLOTS = 15;
 struct SvdDesc {
 	i64 a_off, u_off, s_off, v_off, w_off;
 	int m, n;

@@ -45,7 +45,7 @@ constexpr int NWARPS = SVD_THREADS / 32;
 constexpr int SVD_STEP_PAIRS = 32;            // most column pairs of one inner step (group size <= 32)
 constexpr int SVD_SMEM_LIMIT = 220 * 1024;    // dynamic shared memory per CTA (227 KB less static use)
 constexpr int SVD_F32_SWEEPS = 5;             // most FP32 preconditioning sweeps (more do not save FP64 ones)
-constexpr int SVD_F32_MIN_RANK = 48;          // default: smallest rank preconditioned in FP32
+constexpr int SVD_F32_MIN_RANK = 32;          // default: smallest rank preconditioned in FP32
 constexpr int SVD_F32_CLUSTER = 8;            // default: CTAs of the FP32 sweeps
 
 // shared memory (doubles) of the Jacobi tour: two buffers of two column groups (records of 2 N),
@@ -280,7 +280,8 @@ __device__ __forceinline__ float pow2f(int k)
 }
 
 // Jacobi rotation for the 2 x 2 Gram matrix [al ga; ga be] of a column pair (al, be > 0).
-// Returns false if the pair counts as orthogonal (cos^2 = ga^2 / (al be) <= tol2). Otherwise the
+// Returns false if the pair counts as orthogonal (cos^2 = ga^2 / (al be) <= tol2); c2 receives
+// the FP32 estimate of cos^2 (1 when it is not small). Otherwise the
 // rotation angle theta (tan theta the smaller root of t^2 + 2 zeta t - 1 = 0, zeta = (be - al) /
 // (2 ga)) is found in FP32 on mantissas and integer exponents, and the rotation is returned as
 // tau = tan(theta / 2) and sn = sin theta = 2 tau / (1 + tau^2) in FP64, for the three-shear form
@@ -291,14 +292,20 @@ __device__ __forceinline__ float pow2f(int k)
 // or square root costs over a thousand cycles on GB300. The angle is accurate to FP32 only: the
 // rotation leaves a cosine of about 1e-7 of the previous one, which a later sweep removes.
 __device__ __forceinline__ bool rotation_params(double al, double be, double ga, float tol2, double& tau, double& sn,
-                                                double& t)
+                                                double& t, float& c2)
 {
+	c2 = 0.0f;
 	if (ga == 0.0) return false;
 	int ea, eb, eg;
 	const float ma = mant_exp(al, ea), mb = mant_exp(be, eb), mg = mant_exp(ga, eg);
 	const int k2 = 2 * eg - ea - eb;
 	if (k2 < -120) return false;
-	if (k2 <= 0 && __fdividef(mg * mg, ma * mb) * pow2f(k2) <= tol2) return false;
+	if (k2 <= 0)
+	{
+		c2 = __fdividef(mg * mg, ma * mb) * pow2f(k2);
+		if (c2 <= tol2) return false;
+	}
+	else c2 = 1.0f;
 	const double dl = be - al;
 	const bool neg = (dl < 0.0) != (ga < 0.0);
 	float tm, taum;
@@ -363,6 +370,7 @@ struct Tour {
 
 struct StepBuf {
 	int* local_rot;              // set when a rotation was applied in the current sweep
+	int* max_c2;                 // largest cos^2 of the sweep's pairs (bits of a non-negative float)
 };
 
 __device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int k, int cA, int cB, int npad, int& sp,
@@ -396,10 +404,16 @@ __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, 
 		double* pb = t.nrm(buf, sq) + cq;
 		const double al = *pa, be = *pb;
 		double tau, sn, tn;
+		float c2;
+		const bool rot = rotation_params(al, be, g, tol2, tau, sn, tn, c2);
 		// executed FP64 flops: an inner product per examined pair, three FMAs per entry of the two
 		// column records per rotation (counted on lane 0 of each warp)
-		if (lane == 0) flops += 2.0 * t.N;
-		if (rotation_params(al, be, g, tol2, tau, sn, tn))
+		if (lane == 0)
+		{
+			flops += 2.0 * t.N;
+			atomicMax(sb.max_c2, __float_as_int(c2));
+		}
+		if (rot)
 		{
 			for (int i = lane; i < len; i += 32)
 			{
@@ -504,12 +518,12 @@ __device__ void jacobi_step32(const Tour32& t, int buf, int mode, int step, int 
 
 struct SvdScratch {
 	double *W, *T, *V, *nrm, *tau, *sig, *misc;
-	int *flags, *perm, *flags32;
+	int *flags, *perm, *flags32, *cmax;
 };
 
 // workspace of one block: W (M x N, B then R and the reflectors), T (N x r), V (r x r), column
 // norms, reflector scalars, singular values, misc [rank, ||B||_F^2, unscale], sweep flags, pivots,
-// FP32 sweep flags
+// FP32 sweep flags, largest cos^2 per sweep
 __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 {
 	SvdScratch x;
@@ -523,26 +537,28 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 	x.flags = (int*)(x.misc + 4);
 	x.perm = x.flags + SVD_MAX_SWEEPS;
 	x.flags32 = x.perm + N;
+	x.cmax = x.flags32 + SVD_F32_SWEEPS;
 	return x;
 }
 
 // Householder QR with column pivoting of the scaled block over a whole cluster. Column j lives in
-// the shared memory of CTA j % cl; columns are not moved. Every step each CTA forms, in its own
-// shared memory, the reflector of its best remaining column (speculatively: only the pivot's is
-// used) and sends that column's squared norm, index and reflector scalars to every CTA; after one
-// cluster barrier all CTAs agree on the pivot (largest norm, then smallest index), copy its
-// reflector from the owner's shared memory (distributed shared memory, double-buffered by step
-// parity) and apply it to their own remaining columns, downdating the norms (recomputed when
-// cancellation has eaten more than sqrt(eps) of the last exact value, as in qr_pivoted_cta).
+// the shared memory of CTA j % cl; columns are not moved. Every step the first warp of each CTA
+// picks the CTA's best remaining column and forms its reflector (speculatively: only the pivot's
+// is used); the CTA writes that reflector and the column's squared norm, index and reflector
+// scalars into every CTA's shared memory (distributed shared memory, double-buffered by step
+// parity). After one cluster barrier every CTA holds all candidates, agrees on the pivot (largest
+// norm, then smallest index) and applies its reflector to its own remaining columns, downdating
+// the norms (recomputed when cancellation has eaten more than sqrt(eps) of the last exact value,
+// as in qr_pivoted_cta).
 // Its shared memory (doubles):
 __host__ __device__ inline i64 qr_cluster_doubles(int M, int N, int cl)
 {
 	const i64 nloc = (N + cl - 1) / cl;
-	return nloc * M + 2 * nloc + 3 * (i64)M + 16 + 3 * 2 * 16 + (2 * 16 + nloc + 1) / 2 + 8;
+	return nloc * M + 2 * nloc + 2 * (i64)cl * M + M + 16 + 3 * 2 * 16 + (2 * 16 + nloc + 1) / 2 + 8;
 }
 
 __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, const double* ab, bool tall, int n, int M, int N,
-                                  int cl, const SvdScratch& xs)
+                                  int cl, const SvdScratch& xs, long long* qc)
 {
 	const int rank = (int)cluster.block_rank();
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -551,16 +567,16 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 	double* qcol = smem;                                 // nloc_max x M
 	double* qnrm = qcol + (i64)nloc_max * M;
 	double* qref = qnrm + nloc_max;
-	double* vbuf = qref + nloc_max;                      // pivot reflector of the current step (rows k..M-1)
-	double* cbuf = vbuf + M;                             // [2][M] own candidate reflector, by step parity
-	double* part = cbuf + 2 * (i64)M;                    // [cl] partial Frobenius sums
+	double* cand = qref + nloc_max;                      // [2][cl][M] candidate reflectors of all CTAs
+	double* cbuf = cand + 2 * (i64)cl * M;               // [M] own candidate reflector
+	double* part = cbuf + M;                             // [cl] partial Frobenius sums
 	double* hnrm = part + 16;                            // [2][16] candidate squared norm per CTA
 	double* htau = hnrm + 32;                            // [2][16] candidate tau per CTA
 	double* hbeta = htau + 32;                           // [2][16] candidate beta per CTA
 	int* hidx = (int*)(hbeta + 32);                      // [2][16] candidate column per CTA
 	int* qdone = hidx + 32;                              // [nloc_max] step that took the column, or -1
 	__shared__ double red[NWARPS];
-	__shared__ double sh_tau, sh_beta, sh_scale, sh_best;
+	__shared__ double sh_tau, sh_beta, sh_best;
 	__shared__ int sh_jl;
 
 	// load the own columns (B oriented tall) and their squared sums
@@ -604,7 +620,8 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 	for (int k = 0; k < N; k++)
 	{
 		const int par = k & 1;
-		// a. this CTA's best remaining column
+		long long q0 = qc ? clock64() : 0;
+		// a. warp 0: this CTA's best remaining column and its reflector (speculative)
 		if (warp == 0)
 		{
 			double best = -1;
@@ -619,87 +636,115 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 				const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
 				if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; bj = oj; }
 			}
+			double tk = 0.0, beta = 0.0;
+			if (bj >= 0 && best > thresh)
+			{
+				const double* w = qcol + (i64)bj * M;
+				double x2 = 0;
+				for (int i = k + 1 + lane; i < M; i += 32) x2 = fma(w[i], w[i], x2);
+				x2 = warp_sum(x2);
+				const double alpha = w[k];
+				double scl = 0.0;
+				if (x2 == 0.0) beta = alpha;
+				else
+				{
+					// |beta| = sqrt(alpha^2 + x2) >= the remaining norm, above the rank threshold:
+					// normal doubles. tau = (beta - alpha) / beta = (|beta| + |alpha|) / |beta|,
+					// scale = 1 / (alpha - beta) = sign(alpha) / (|alpha| + |beta|).
+					double sq, rsq;
+					sqrt_rsqrt64(fma(alpha, alpha, x2), sq, rsq);
+					beta = -copysign(sq, alpha);
+					const double sum = sq + fabs(alpha);
+					tk = sum * rsq;
+					scl = copysign(rcp64(sum), alpha);
+				}
+				for (int i = k + lane; i < M; i += 32) cbuf[i] = (i == k) ? 1.0 : w[i] * scl;
+			}
+			else best = -1.0;
 			if (lane == 0)
 			{
 				sh_best = best;
 				sh_jl = bj;
+				sh_tau = tk;
+				sh_beta = beta;
 			}
 		}
 		__syncthreads();
-		// b. its reflector, formed speculatively in this CTA's own shared memory
-		const int bj = sh_jl;
-		const double best = sh_best;
-		double* cb = cbuf + (i64)par * M;
-		if (bj >= 0 && best > thresh)
+		if (qc)
 		{
-			const double* w = qcol + (i64)bj * M;
-			double part2 = 0;
-			for (int i = k + 1 + tid; i < M; i += SVD_THREADS) part2 = fma(w[i], w[i], part2);
-			const double xnorm2 = block_sum(part2, red);
-			if (tid == 0)
-			{
-				const double alpha = w[k];
-				if (xnorm2 == 0.0)
-				{
-					sh_tau = 0.0;
-					sh_beta = alpha;
-					sh_scale = 0.0;
-				}
-				else
-				{
-					// |beta| >= the remaining norm, above the rank threshold: normal doubles
-					const double beta = -copysign(sqrt64(fma(alpha, alpha, xnorm2)), alpha);
-					sh_tau = (beta - alpha) * rcp64(beta);
-					sh_beta = beta;
-					sh_scale = rcp64(alpha - beta);
-				}
-			}
-			__syncthreads();
-			const double scl = sh_scale;
-			for (int i = k + tid; i < M; i += SVD_THREADS) cb[i] = (i == k) ? 1.0 : w[i] * scl;
+			const long long q1 = clock64();
+			qc[0] += q1 - q0;
+			q0 = q1;
 		}
-		// c. its candidate to every CTA, one cluster barrier, the pivot
+		// b. the candidate into every CTA's shared memory
+		const double best = sh_best;
+		if (best > 0.0)
+		{
+			const int len = M - k;
+			for (int e = tid; e < len * cl; e += SVD_THREADS)
+			{
+				const int dst = e / len, i = k + (e - dst * len);
+				*cluster.map_shared_rank(cand + ((i64)par * cl + rank) * M + i, (unsigned)dst) = cbuf[i];
+			}
+		}
 		if (tid < cl)
 		{
-			const bool has = bj >= 0 && best > thresh;
-			*cluster.map_shared_rank(hnrm + par * 16 + rank, (unsigned)tid) = has ? best : -1.0;
-			*cluster.map_shared_rank(hidx + par * 16 + rank, (unsigned)tid) = has ? rank + cl * bj : N;
-			*cluster.map_shared_rank(htau + par * 16 + rank, (unsigned)tid) = has ? sh_tau : 0.0;
-			*cluster.map_shared_rank(hbeta + par * 16 + rank, (unsigned)tid) = has ? sh_beta : 0.0;
+			*cluster.map_shared_rank(hnrm + par * 16 + rank, (unsigned)tid) = best;
+			*cluster.map_shared_rank(hidx + par * 16 + rank, (unsigned)tid) = best > 0.0 ? rank + cl * sh_jl : N;
+			*cluster.map_shared_rank(htau + par * 16 + rank, (unsigned)tid) = sh_tau;
+			*cluster.map_shared_rank(hbeta + par * 16 + rank, (unsigned)tid) = sh_beta;
+		}
+		if (qc)
+		{
+			const long long q1 = clock64();
+			qc[1] += q1 - q0;
+			q0 = q1;
 		}
 		cluster.sync();
-		double pv = -1;
-		int p = N, owner = 0;
-		for (int i = 0; i < cl; i++)
+		if (qc)
 		{
-			const double c = hnrm[par * 16 + i];
-			const int ci = hidx[par * 16 + i];
-			if (c > pv || (c == pv && ci < p)) { pv = c; p = ci; owner = i; }
+			const long long q1 = clock64();
+			qc[2] += q1 - q0;
+			q0 = q1;
+		}
+		// c. the pivot: every warp reduces the candidates itself (no barrier)
+		double pv = lane < cl ? hnrm[par * 16 + lane] : -1.0;
+		int p = lane < cl ? hidx[par * 16 + lane] : N;
+		int owner = lane;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1)
+		{
+			const double ov = __shfl_xor_sync(0xffffffffu, pv, o);
+			const int op = __shfl_xor_sync(0xffffffffu, p, o);
+			const int ow = __shfl_xor_sync(0xffffffffu, owner, o);
+			if (ov > pv || (ov == pv && op < p)) { pv = ov; p = op; owner = ow; }
 		}
 		if (pv <= thresh || pv <= 0.0 || p >= N) break;
 		const double tk = htau[par * 16 + owner];
-		// d. the pivot's reflector from its owner; the owner stores R_kk and the reflector in place
+		const double* vbuf = cand + ((i64)par * cl + owner) * M;
+		// the owner stores R_kk and the reflector in place (the updates below skip that column)
+		const int pjl = owner == rank ? p / cl : -1;
+		if (pjl >= 0)
 		{
-			const double* src = owner == rank ? cb : cluster.map_shared_rank(cbuf + (i64)par * M, (unsigned)owner);
-			for (int i = k + tid; i < M; i += SVD_THREADS) vbuf[i] = src[i];
-		}
-		if (owner == rank)
-		{
-			const int jl = p / cl;
-			double* w = qcol + (i64)jl * M;
-			for (int i = k + 1 + tid; i < M; i += SVD_THREADS) w[i] = cb[i];
+			double* w = qcol + (i64)pjl * M;
+			for (int i = k + 1 + tid; i < M; i += SVD_THREADS) w[i] = cbuf[i];
 			if (tid == 0)
 			{
 				w[k] = hbeta[par * 16 + owner];
 				xs.tau[k] = tk;
-				qdone[jl] = k;
+				qdone[pjl] = k;
 			}
 		}
-		__syncthreads();
-		// e. apply the reflector to the own remaining columns, downdate their norms
+		if (qc)
+		{
+			const long long q1 = clock64();
+			qc[3] += q1 - q0;
+			q0 = q1;
+		}
+		// d. apply the reflector to the own remaining columns, downdate their norms
 		for (int jl = warp; jl < nloc; jl += NWARPS)
 		{
-			if (qdone[jl] >= 0) continue;
+			if (jl == pjl || qdone[jl] >= 0) continue;
 			double* w = qcol + (i64)jl * M;
 			if (tk != 0.0)
 			{
@@ -725,6 +770,7 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 			}
 		}
 		__syncthreads();
+		if (qc) qc[4] += clock64() - q0;
 		r = k + 1;
 	}
 	// columns to global memory in pivot order, the remaining ones after them in source order
@@ -797,7 +843,7 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 		}
 		__syncthreads();
 		const float tol2 = (float)N * FLT_EPSILON * (float)N * FLT_EPSILON;
-		int buf = 0;
+		int buf = 0, done32 = SVD_F32_SWEEPS;
 		for (int sweep = 0; sweep < SVD_F32_SWEEPS; sweep++)
 		{
 			round_groups(0, rank, f.nm, A, B);
@@ -852,8 +898,13 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 				conv = *local_rot == 0;
 				__syncthreads();
 			}
-			if (conv) break;
+			if (conv)
+			{
+				done32 = sweep + 1;
+				break;
+			}
 		}
+		if (cyc) cyc[2] += done32;
 		// V (FP32) to global memory, column g at V + g r
 		round_groups(0, rank, f.nm, A, B);
 		for (int slot = 0; slot < 2; slot++)
@@ -981,12 +1032,14 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 
 	for (int e = rank * SVD_THREADS + tid; e < SVD_MAX_SWEEPS; e += cl * SVD_THREADS) xs.flags[e] = 0;
 	for (int e = rank * SVD_THREADS + tid; e < SVD_F32_SWEEPS; e += cl * SVD_THREADS) xs.flags32[e] = 0;
+	for (int e = rank * SVD_THREADS + tid; e < SVD_MAX_SWEEPS; e += cl * SVD_THREADS) xs.cmax[e] = 0;
 	const bool stamp = phase_ts && rank == 0 && tid == 0;
 	if (stamp) phase_ts[SVD_PHASE_SLOTS * blk] = globaltimer();
 
 	// ---- 1. pivoted QR of B scaled to a Frobenius norm in [1/2, 1): over the cluster, or on the
 	// single CTA of a one-CTA cluster ----
-	if (cl > 1) qr_pivoted_cluster(cluster, smem, ab, tall, n, M, N, cl, xs);
+	long long qcyc[5] = {0, 0, 0, 0, 0};
+	if (cl > 1) qr_pivoted_cluster(cluster, smem, ab, tall, n, M, N, cl, xs, phase_ts && tid == 0 && rank == 1 ? qcyc : nullptr);
 	else
 	{
 		__shared__ double red[NWARPS];
@@ -1038,6 +1091,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	t.sm = smem;
 	StepBuf sb;
 	sb.local_rot = (int*)(smem + (i64)4 * t.bsmax * t.ld + 4 * t.bsmax);
+	sb.max_c2 = sb.local_rot + 1;
 
 	int A, B;
 	double jflops = 0;                                 // counted by thread 0 (lane 0 of warp 0)
@@ -1093,7 +1147,11 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 				if (lane == 0) t.nrm(buf, slot)[c] = acc;
 			}
 		}
-		if (tid == 0) *sb.local_rot = 0;
+		if (tid == 0)
+		{
+			*sb.local_rot = 0;
+			*sb.max_c2 = 0;
+		}
 		__syncthreads();
 		for (int rho = 0; rho < t.nm; rho++)
 		{
@@ -1110,7 +1168,11 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 				const long long cx = cyc ? clock64() : 0;
 				// jacobi_step ended with a CTA barrier: this round's rotations are complete
 				// one global flag per sweep, raised after the sweep's last round by any CTA that rotated
-				if (tid == 0 && rho == t.nm - 1 && *sb.local_rot) atomicOr(xs.flags + sweep, 1);
+				if (tid == 0 && rho == t.nm - 1)
+				{
+					if (*sb.local_rot) atomicOr(xs.flags + sweep, 1);
+					atomicMax(xs.cmax + sweep, *sb.max_c2);
+				}
 				const int rho1 = (rho + 1) % t.nm;
 				for (int slot = 0; slot < 2; slot++)
 				{
@@ -1129,10 +1191,15 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 				if (cyc) cyc[3] += clock64() - cx;
 			}
 		}
-		if (cl > 1) converged = __ldcg(xs.flags + sweep) == 0;
+		// Converged when the sweep rotated nothing, or when every pair of the sweep had cos^2 <=
+		// eps / 4: a rotation by an angle of about cos_pq changes the cosine of a pair (p, r) by about
+		// cos_pq cos_qr (whatever the column norms), so after such a sweep every cosine is below
+		// 2 N (eps / 4) <= N eps / 2, within the tolerance, and the confirming sweep is skipped.
+		const int skip_bits = __float_as_int(0.25f * (float)DBL_EPSILON);
+		if (cl > 1) converged = __ldcg(xs.flags + sweep) == 0 || __ldcg(xs.cmax + sweep) <= skip_bits;
 		else
 		{
-			converged = *sb.local_rot == 0;
+			converged = *sb.local_rot == 0 || *sb.max_c2 <= skip_bits;
 			__syncthreads();
 		}
 	}
@@ -1167,7 +1234,11 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	cluster.sync();
 	if (stamp) phase_ts[SVD_PHASE_SLOTS * blk + 2] = globaltimer();
 	if (count)
+	{
+		cyc_acc[1] = sweep;
 		for (int i = 0; i < 6; i++) phase_ts[SVD_PHASE_SLOTS * blk + 4 + i] = (unsigned long long)cyc_acc[i];
+		for (int i = 0; i < 5; i++) phase_ts[SVD_PHASE_SLOTS * blk + 10 + i] = (unsigned long long)qcyc[i];
+	}
 
 	// ---- 3. outputs: L = Q V (M x r) by the r reflectors applied to [V_c; 0], Rf = P T Sigma^-1 ----
 	const double unscale = __ldcg(xs.misc + 2);
