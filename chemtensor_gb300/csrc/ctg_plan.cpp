@@ -1,5 +1,6 @@
 // ctg_plan.cpp - lowering of block-sparse operations into descriptor lists (host only).
 #include "ctg_plan.h"
+#include "ctg_pool.h"
 
 #include <algorithm>
 #include <chrono>
@@ -50,13 +51,15 @@ int tile_class(int m, int n, bool allow_large)
 	// the tile shape with the fewest padded outputs, counting 128 outputs of fixed cost per tile;
 	// 64 x 64 tiles only in products large enough to fill every SM with them (one such tile holds
 	// 65536 FMAs per 16-wide k chunk, a long serial share when the whole product is small)
+	// tile sides are powers of two: ceilings by shifts
+	static const int lr[NUM_TILE_CLASSES] = {4, 5, 6, 4, 6, 3, 2, 5, 6, 3, 7};
+	static const int lc[NUM_TILE_CLASSES] = {4, 5, 6, 6, 4, 5, 6, 3, 2, 7, 3};
 	int best = TILE_S;
 	i64 best_cost = INT64_MAX;
 	for (int c = 0; c < NUM_TILE_CLASSES; c++)
 	{
 		if (c == TILE_L && !allow_large) continue;
-		const i64 tr = TILE_ROWS[c], tc = TILE_COLS[c];
-		const i64 cost = ((m + tr - 1) / tr) * ((n + tc - 1) / tc) * (tr * tc + 128);
+		const i64 cost = (i64)(((m - 1) >> lr[c]) + 1) * (((n - 1) >> lc[c]) + 1) * ((1 << (lr[c] + lc[c])) + 128);
 		if (cost < best_cost)
 		{
 			best_cost = cost;
@@ -150,7 +153,23 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			v[(size_t)b] = Key{f, cc, b};
 		}
 		auto less = [](const Key& x, const Key& y) { return x.f < y.f || (x.f == y.f && x.c < y.c); };
-		if (!std::is_sorted(v.begin(), v.end(), less)) std::sort(v.begin(), v.end(), less);
+		if (!std::is_sorted(v.begin(), v.end(), less))
+		{
+			// The blocks are in row-major order over all axes, so within one free index the
+			// contracted indices already increase: a stable sort by the free index alone gives the
+			// (free, contracted) order. LSD radix sort on the free index, 8 bits per pass.
+			i64 fmax = 0;
+			for (const Key& x : v) fmax = std::max(fmax, x.f);
+			std::vector<Key> tmp(v.size());
+			for (int shift = 0; shift < 64 && (fmax >> shift) > 0; shift += 8)
+			{
+				size_t cnt[257] = {0};
+				for (const Key& x : v) cnt[((x.f >> shift) & 255) + 1]++;
+				for (int d = 0; d < 256; d++) cnt[d + 1] += cnt[d];
+				for (const Key& x : v) tmp[cnt[(x.f >> shift) & 255]++] = x;
+				v.swap(tmp);
+			}
+		}
 		return v;
 	};
 	const std::vector<Key> ks = keyed(s, shift_s, off_s, nfs), kt = keyed(t, shift_t, off_t, nft);
@@ -175,106 +194,171 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 	geometry(t, nldt, t_lead, t_trail);
 	constexpr int KCH = 16;                      // k chunk of the FP64 kernels
 	std::vector<i64> nchunk((size_t)r.nblocks, 0), ksum((size_t)r.nblocks, 0);
-	cons.reserve(ks.size() + (size_t)r.nblocks);
-	for (int k = 0; k < NUM_TILE_CLASSES; k++) tiles[k].reserve((size_t)r.nblocks);
+	// The output blocks are cut into ranges lowered side by side on the host threads (each range
+	// into its own lists, joined in range order afterwards, so the plan does not depend on the
+	// number of threads); small products stay on the calling thread.
+	const int nrange = r.nblocks >= 4096 ? std::min(4 * host_threads(), std::max(1, r.nblocks / 1024)) : 1;
+	struct Range {
+		std::vector<GemmContrib> cons;
+		std::vector<std::pair<int, int>> con_blocks;
+		std::vector<GemmTile> tiles[NUM_TILE_CLASSES];
+		double flops = 0, flops_cls[NUM_TILE_CLASSES] = {};
+	};
+	std::vector<Range> rng((size_t)nrange);
+	auto range_of = [&](int q, int& b0, int& b1) {
+		b0 = (int)((i64)r.nblocks * q / nrange);
+		b1 = (int)((i64)r.nblocks * (q + 1) / nrange);
+	};
+	parallel_for(nrange, [&](int q) {
+		int b0, b1;
+		range_of(q, b0, b1);
+		Range& R = rng[(size_t)q];
+		R.cons.reserve((size_t)(b1 - b0) * 2);
+		i64 fs_prev = -1;
+		size_t s0 = 0, s1 = 0, tcur = 0;
+		for (int b = b0; b < b1; b++)
+		{
+			const i64* ir = r.index(b);
+			const i64* rd = r.dims(b);
+			GemmOut& o = outs[b];
+			o.c_off = r.boff[b];
+			o.m = (int)prod(rd, nfs);
+			o.n = (int)prod(rd + nfs, nft);
+			o.c0 = (int)R.cons.size();             // range-local until the join
+			i64 fs = 0, ft = 0;
+			for (int i = 0; i < nfs; i++) fs = fs * r.nb[i] + ir[i];
+			for (int i = 0; i < nft; i++) ft = ft * r.nb[nfs + i] + ir[nfs + i];
+			// output blocks come in row-major order: the s run changes only with fs, and within one
+			// fs the t free indices increase, so the t runs are found by a forward scan
+			if (fs != fs_prev)
+			{
+				run_of(ks, fs, s0, s1);
+				fs_prev = fs;
+				tcur = 0;
+			}
+			while (tcur < kt.size() && kt[tcur].f < ft) tcur++;
+			const size_t t0 = tcur;
+			size_t t1 = t0;
+			while (t1 < kt.size() && kt[t1].f == ft) t1++;
+			CTG_CHECK(s1 - s0 == t1 - t0, "dot: operand block runs differ");
+			const double mn2 = 2.0 * (double)o.m * (double)o.n;
+			i64 nch = 0;
+			for (size_t x = s0, y = t0; x < s1; x++, y++)
+			{
+				CTG_CHECK(ks[x].c == kt[y].c, "dot: missing partner block");
+				const int bs = ks[x].b, bt = kt[y].b;
+				const i64 lds = s_lead[(size_t)bs], tds = s_trail[(size_t)bs];
+				const i64 ldt = t_lead[(size_t)bt], tdt = t_trail[(size_t)bt];
+				GemmContrib g = {};
+				g.a_off = s.boff[bs];
+				g.b_off = t.boff[bt];
+				const i64 k = (axs == AX_LEADING ? lds : tds);
+				g.k = (int)k;
+				if (axs == AX_LEADING) { g.sAm = 1; g.sAk = (int)tds; }
+				else { g.sAm = (int)tds; g.sAk = 1; }
+				if (axt == AX_LEADING) { g.sBk = (int)tdt; g.sBn = 1; }
+				else { g.sBk = 1; g.sBn = (int)tdt; }
+				CTG_CHECK(k == (axt == AX_LEADING ? ldt : tdt), "dot: inner dimensions differ");
+				// every operand access stays inside its block (checked once per plan, on the host)
+				CTG_CHECK(k >= 1 && g.a_off + (i64)(o.m - 1) * g.sAm + (k - 1) * g.sAk < s.boff[bs] + lds * tds,
+				          "dot: A operand out of range");
+				CTG_CHECK(g.b_off + (k - 1) * g.sBk + (i64)(o.n - 1) * g.sBn < t.boff[bt] + ldt * tdt,
+				          "dot: B operand out of range");
+				R.cons.push_back(g);
+				if (precision == GEMM_BF16X3) R.con_blocks.emplace_back(bs, bt);
+				R.flops += mn2 * (double)k;
+				ksum[(size_t)b] += k;
+				nch += (k + KCH - 1) / KCH;
+			}
+			nchunk[(size_t)b] = nch;
+			o.nc = (int)R.cons.size() - o.c0;
+			CTG_CHECK(o.m >= 1 && o.n >= 1 && o.c_off + (i64)o.m * o.n <= r.nnz, "dot: output block out of range");
+		}
+	});
+	// join the contribution lists; the output blocks' contribution ranges become global
 	double flops = 0;
-	i64 fs_prev = -1;
-	size_t s0 = 0, s1 = 0, tcur = 0;
-	for (int b = 0; b < r.nblocks; b++)
 	{
-		const i64* ir = r.index(b);
-		const i64* rd = r.dims(b);
-		GemmOut& o = outs[b];
-		o.c_off = r.boff[b];
-		o.m = (int)prod(rd, nfs);
-		o.n = (int)prod(rd + nfs, nft);
-		o.c0 = (int)cons.size();
-		i64 fs = 0, ft = 0;
-		for (int i = 0; i < nfs; i++) fs = fs * r.nb[i] + ir[i];
-		for (int i = 0; i < nft; i++) ft = ft * r.nb[nfs + i] + ir[nfs + i];
-		// output blocks come in row-major order: the s run changes only with fs, and within one fs
-		// the t free indices increase, so the t runs are found by a forward scan
-		if (fs != fs_prev)
+		size_t ncons = 0;
+		for (const Range& R : rng) ncons += R.cons.size();
+		if (nrange == 1)
 		{
-			run_of(ks, fs, s0, s1);
-			fs_prev = fs;
-			tcur = 0;
+			cons.swap(rng[0].cons);
+			con_blocks.swap(rng[0].con_blocks);
+			flops = rng[0].flops;
 		}
-		while (tcur < kt.size() && kt[tcur].f < ft) tcur++;
-		const size_t t0 = tcur;
-		size_t t1 = t0;
-		while (t1 < kt.size() && kt[t1].f == ft) t1++;
-		CTG_CHECK(s1 - s0 == t1 - t0, "dot: operand block runs differ");
-		const double mn2 = 2.0 * (double)o.m * (double)o.n;
-		i64 nch = 0;
-		for (size_t x = s0, y = t0; x < s1; x++, y++)
+		else cons.reserve(ncons);
+		for (int q = 0; q < nrange && nrange > 1; q++)
 		{
-			CTG_CHECK(ks[x].c == kt[y].c, "dot: missing partner block");
-			const int bs = ks[x].b, bt = kt[y].b;
-			const i64 lds = s_lead[(size_t)bs], tds = s_trail[(size_t)bs];
-			const i64 ldt = t_lead[(size_t)bt], tdt = t_trail[(size_t)bt];
-			GemmContrib g;
-			g.a_off = s.boff[bs];
-			g.b_off = t.boff[bt];
-			const i64 k = (axs == AX_LEADING ? lds : tds);
-			g.k = (int)k;
-			if (axs == AX_LEADING) { g.sAm = 1; g.sAk = (int)tds; }
-			else { g.sAm = (int)tds; g.sAk = 1; }
-			if (axt == AX_LEADING) { g.sBk = (int)tdt; g.sBn = 1; }
-			else { g.sBk = 1; g.sBn = (int)tdt; }
-			CTG_CHECK(k == (axt == AX_LEADING ? ldt : tdt), "dot: inner dimensions differ");
-			// every operand access stays inside its block (checked once per plan, on the host)
-			CTG_CHECK(k >= 1 && g.a_off + (i64)(o.m - 1) * g.sAm + (k - 1) * g.sAk < s.boff[bs] + lds * tds,
-			          "dot: A operand out of range");
-			CTG_CHECK(g.b_off + (k - 1) * g.sBk + (i64)(o.n - 1) * g.sBn < t.boff[bt] + ldt * tdt,
-			          "dot: B operand out of range");
-			cons.push_back(g);
-			if (precision == GEMM_BF16X3) con_blocks.emplace_back(bs, bt);
-			flops += mn2 * (double)k;
-			ksum[(size_t)b] += k;
-			nch += (k + KCH - 1) / KCH;
+			Range& R = rng[(size_t)q];
+			int b0, b1;
+			range_of(q, b0, b1);
+			const int base = (int)cons.size();
+			for (int b = b0; b < b1; b++) outs[(size_t)b].c0 += base;
+			cons.insert(cons.end(), R.cons.begin(), R.cons.end());
+			con_blocks.insert(con_blocks.end(), R.con_blocks.begin(), R.con_blocks.end());
+			flops += R.flops;
+			std::vector<GemmContrib>().swap(R.cons);
 		}
-		nchunk[(size_t)b] = nch;
-		o.nc = (int)cons.size() - o.c0;
-		CTG_CHECK(o.m >= 1 && o.n >= 1 && o.c_off + (i64)o.m * o.n <= r.nnz, "dot: output block out of range");
 	}
 	// tiles: every tile first takes the whole sum over its output block's contributions
 	const bool allow_large = flops / 2 > (double)num_sms * 8 * 65536;
-	for (int b = 0; b < r.nblocks; b++)
-	{
-		const GemmOut& o = outs[(size_t)b];
-		GemmTile whole = {};
-		whole.out = b;
-		whole.c0 = o.c0;
-		whole.k0 = 0;
-		whole.c1 = o.c0 + o.nc - 1;
-		whole.k1 = o.nc > 0 ? cons[(size_t)whole.c1].k : 0;
-		whole.split = -1;
-		whole.sp = 0;
-		if (precision == GEMM_BF16X3)
+	parallel_for(nrange, [&](int q) {
+		int b0, b1;
+		range_of(q, b0, b1);
+		Range& R = rng[(size_t)q];
+		for (int b = b0; b < b1; b++)
 		{
-			// tensor-core tiles: one tile class
-			p.flops_cls[0] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
-			for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
-				for (int n0 = 0; n0 < o.n; n0 += tc_tile_cols())
+			const GemmOut& o = outs[(size_t)b];
+			GemmTile whole = {};
+			whole.out = b;
+			whole.c0 = o.c0;
+			whole.k0 = 0;
+			whole.c1 = o.c0 + o.nc - 1;
+			whole.k1 = o.nc > 0 ? cons[(size_t)whole.c1].k : 0;
+			whole.split = -1;
+			whole.sp = 0;
+			if (precision == GEMM_BF16X3)
+			{
+				// tensor-core tiles: one tile class
+				R.flops_cls[0] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
+				for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
+					for (int n0 = 0; n0 < o.n; n0 += tc_tile_cols())
+					{
+						whole.m0 = m0;
+						whole.n0 = n0;
+						R.tiles[0].push_back(whole);
+					}
+				continue;
+			}
+			const int cls = tile_class(o.m, o.n, allow_large);
+			R.flops_cls[cls] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
+			const int tr = tile_rows(cls), tc = tile_cols(cls);
+			whole.cls = cls;
+			for (int m0 = 0; m0 < o.m; m0 += tr)
+				for (int n0 = 0; n0 < o.n; n0 += tc)
 				{
 					whole.m0 = m0;
 					whole.n0 = n0;
-					tiles[0].push_back(whole);
+					R.tiles[cls].push_back(whole);
 				}
+		}
+	});
+	for (int k = 0; k < NUM_TILE_CLASSES; k++)
+	{
+		if (nrange == 1)
+		{
+			tiles[k].swap(rng[0].tiles[k]);
+			p.flops_cls[k] += rng[0].flops_cls[k];
 			continue;
 		}
-		const int cls = tile_class(o.m, o.n, allow_large);
-		p.flops_cls[cls] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
-		const int tr = tile_rows(cls), tc = tile_cols(cls);
-		whole.cls = cls;
-		for (int m0 = 0; m0 < o.m; m0 += tr)
-			for (int n0 = 0; n0 < o.n; n0 += tc)
-			{
-				whole.m0 = m0;
-				whole.n0 = n0;
-				tiles[cls].push_back(whole);
-			}
+		size_t nt = 0;
+		for (const Range& R : rng) nt += R.tiles[k].size();
+		tiles[k].reserve(nt);
+		for (const Range& R : rng)
+		{
+			tiles[k].insert(tiles[k].end(), R.tiles[k].begin(), R.tiles[k].end());
+			p.flops_cls[k] += R.flops_cls[k];
+		}
 	}
 	// Split-K: on GB300 one SM retires about two FP64 FMAs per clock, so a block GEMM with fewer
 	// tiles than SMs leaves most of the FP64 pipes idle. Tiles whose work exceeds a fair share of
