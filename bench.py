@@ -45,7 +45,7 @@ UNIT = "sweeps/s"
 L2_FLUSH_BYTES = 256 << 20
 PRECISIONS = {"fp64": 0, "bf16x3": 1}
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_svd_tour launch (ncu, see profiles/)
-SVD_TRAFFIC_PER_LAUNCH = 179200 + 256
+SVD_TRAFFIC_PER_LAUNCH = 379136
 
 
 def build_inputs():
@@ -246,13 +246,14 @@ def bench_gpu(args, world, rank, local):
         "bound": "fp64", "kernel": "k_svd_tour (block SVD: pivoted QR + cluster Jacobi, one launch per cluster size)",
         "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None,
         "peak_source": "FP64 FMA probe measured live in this run (MEASURED_PEAKS.json has HBM and bf16 peaks only)",
-        "flops_definition": "Jacobi inner products and rotations as executed (counted on the device), "
-                            "QR and output factors at full rank (host estimate)",
+        "flops_definition": "FP64 Jacobi inner products and rotations as executed and the FP32-to-FP64 "
+                            "hand-over (counted on the device), QR and output factors at full rank (host "
+                            "estimate); the FP32 preconditioning sweeps are not counted",
         "flops_per_launch": svd_flops_per_sweep / max(svd_launches_per_sweep, 1e-9),
         "avg_launch_us": 1e3 * svd_ms_per_sweep / max(svd_launches_per_sweep, 1e-9),
         "traffic": SVD_TRAFFIC_PER_LAUNCH,
-        "traffic_source": "dram read+write of one k_svd_tour launch (16-CTA cluster, largest block of a bond) "
-                          "from profiles/k_svd_tour_hubbard_L32_D256.md",
+        "traffic_source": "dram read+write of one k_svd_tour launch (one bond's 16-CTA-cluster group, 6 "
+                          "blocks) from profiles/k_svd_tour_hubbard_L32_D256.md",
         "kernel_share": {k: (v["ms"] / total_prof_ms if total_prof_ms > 0 else 0) for k, v in prof.items()},
         "block_gemm": {"bound": "fp64", "achieved": g_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                        "frac": g_achieved / fp64_peak if fp64_peak > 0 else None, "launches": g["launches"],
