@@ -442,15 +442,15 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 	const i64 n = a_start.m().nnz;
 	DBuf V(&c, (size_t)maxiter * n * sizeof(double));
 	DBuf wv(&c, (size_t)n * sizeof(double));
-	DBuf partial(&c, RED_BLOCKS * sizeof(double));
+	DBuf partial(&c, 2 * RED_BLOCKS * sizeof(double));
 	double* Vp = (double*)V.ptr;
 	double* wp = (double*)wv.ptr;
 	double* pp = (double*)partial.ptr;
 	cudaStream_t s = c.stream();
 	const double dn = (double)n;
 	{
-		KScope ks(c, K_LANCZOS, 3, 3.0 * dn, 24.0 * dn);
-		launch_lz_normalize_start(a_start.data(), Vp, n, pp, d_sc, s);
+		KScope ks(c, K_LANCZOS, 1, 3.0 * dn, 24.0 * dn);
+		launch_lz_start(a_start.data(), Vp, n, pp, d_sc, s);
 	}
 	for (int j = 0; j < maxiter; j++)
 	{
@@ -459,14 +459,10 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 		g_host_detail[1] += now_s() - hz;
 		hz = now_s();
 		{
-			KScope ks(c, K_LANCZOS, 2, 2.0 * dn, 16.0 * dn);
-			launch_lz_alpha(wp, Vp + (i64)j * n, n, j, pp, d_sc, s);
-		}
-		if (j < maxiter - 1)
-		{
-			KScope ks(c, K_LANCZOS, 3, 7.0 * dn, 56.0 * dn);
-			launch_lz_orth_beta(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, n, j, pp, d_sc, s);
-			launch_lz_next(wp, Vp + (i64)(j + 1) * n, n, j, d_sc, s);
+			const bool last = j == maxiter - 1;
+			KScope ks(c, K_LANCZOS, 1, last ? 2.0 * dn : 9.0 * dn, last ? 16.0 * dn : 72.0 * dn);
+			launch_lz_step(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, last ? wp : Vp + (i64)(j + 1) * n, n, j,
+			               last ? 1 : 0, pp, d_sc, s);
 		}
 		g_host_detail[2] += now_s() - hz;
 	}

@@ -207,11 +207,12 @@ struct LanczosScalars {
 
 constexpr int RED_BLOCKS = 608;     // 4 x 152 SMs: fixed grid for deterministic reductions
 
-void launch_lz_normalize_start(const double* v0, double* v, i64 n, double* partial, LanczosScalars* sc, cudaStream_t st);
-void launch_lz_alpha(const double* w, const double* vj, i64 n, int j, double* partial, LanczosScalars* sc, cudaStream_t st);
-void launch_lz_orth_beta(double* w, const double* vj, const double* vjm1, i64 n, int j, double* partial,
-                         LanczosScalars* sc, cudaStream_t st);
-void launch_lz_next(const double* w, double* vj1, i64 n, int j, const LanczosScalars* sc, cudaStream_t st);
+// one cooperative launch each (partial: 2 RED_BLOCKS doubles): a whole Lanczos step
+// (alpha; unless last: orthogonalisation, beta and the early exit, next vector), and the start
+// vector's normalisation
+void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, int j, int last,
+                    double* partial, LanczosScalars* sc, cudaStream_t st);
+void launch_lz_start(const double* v0, double* v, i64 n, double* partial, LanczosScalars* sc, cudaStream_t st);
 void launch_lz_tridiag(int maxiter, LanczosScalars* sc, cudaStream_t st);
 void launch_lz_ritz(const double* V, i64 n, int maxiter, const LanczosScalars* sc, double* out, cudaStream_t st);
 

@@ -3,8 +3,12 @@
 // operations with deterministic warp-shuffle reductions.
 #include <cfloat>
 
+#include <cooperative_groups.h>
+
 #include "ctg_fp64.cuh"
 #include "ctg_kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace ctg {
 
@@ -173,107 +177,100 @@ __device__ double final_sum(const double* partial)
 	return t;
 }
 
-__global__ void k_partial_dot(const double* __restrict__ x, const double* __restrict__ y, i64 n, double* partial,
-                              const LanczosScalars* sc)
+// One whole Lanczos step in one cooperative launch: alpha_j = <w, v_j>, then unless it is the last step
+// w -= alpha_j v_j + beta_{j-1} v_{j-1}, beta_j = ||w|| with the early-exit test, v_{j+1} = w / beta_j.
+// Every block forms the scalar reductions itself from the fixed-order partial sums, so no block
+// waits for another except at the two grid barriers. `partial` holds 2 RED_BLOCKS doubles.
+__global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
+k_lz_step(double* __restrict__ w, const double* __restrict__ vj, const double* __restrict__ vjm1,
+          double* __restrict__ vj1, i64 n, int j, int last, double* __restrict__ partial, LanczosScalars* sc)
 {
-	if (sc != nullptr && sc->stopped) return;
+	cg::grid_group grid = cg::this_grid();
+	if (sc->stopped) return;               // read before the first barrier: the same in every block
+	const i64 stride = (i64)RED_BLOCKS * RED_THREADS;
 	double v = 0;
-	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += (i64)RED_BLOCKS * RED_THREADS) v = fma(x[i], y[i], v);
+	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride) v = fma(w[i], vj[i], v);
 	block_partial(v, partial);
-}
-
-__global__ void k_start_final(const double* partial, LanczosScalars* sc)
-{
-	const double t = final_sum(partial);
-	if (threadIdx.x == 0)
-	{
-		sc->nrm0 = sqrt(t);
-		sc->stopped = 0;
-		sc->numiter = 0;
-		sc->status = 0;
-	}
-}
-
-__global__ void k_scale_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, const LanczosScalars* sc)
-{
-	const double inv = 1.0 / sc->nrm0;
-	for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) v[i] = inv * v0[i];
-}
-
-void launch_lz_normalize_start(const double* v0, double* v, i64 n, double* partial, LanczosScalars* sc, cudaStream_t st)
-{
-	k_partial_dot<<<RED_BLOCKS, RED_THREADS, 0, st>>>(v0, v0, n, partial, nullptr);
-	k_start_final<<<1, RED_THREADS, 0, st>>>(partial, sc);
-	k_scale_start<<<RED_BLOCKS, 256, 0, st>>>(v0, v, n, sc);
-	CTG_CUDA(cudaGetLastError());
-}
-
-__global__ void k_alpha_final(const double* partial, LanczosScalars* sc, int j)
-{
-	if (sc->stopped) return;
-	const double t = final_sum(partial);
-	if (threadIdx.x == 0) sc->alpha[j] = t;
-}
-
-void launch_lz_alpha(const double* w, const double* vj, i64 n, int j, double* partial, LanczosScalars* sc, cudaStream_t st)
-{
-	k_partial_dot<<<RED_BLOCKS, RED_THREADS, 0, st>>>(w, vj, n, partial, sc);
-	k_alpha_final<<<1, RED_THREADS, 0, st>>>(partial, sc, j);
-	CTG_CUDA(cudaGetLastError());
-}
-
-__global__ void k_orth_partial(double* __restrict__ w, const double* __restrict__ vj, const double* __restrict__ vjm1, i64 n,
-                               int j, double* partial, const LanczosScalars* sc)
-{
-	if (sc->stopped) return;
-	const double al = sc->alpha[j];
+	grid.sync();
+	const double al = final_sum(partial);
+	if (blockIdx.x == 0 && threadIdx.x == 0) sc->alpha[j] = al;
+	if (last) return;
 	const double be = j > 0 ? sc->beta[j - 1] : 0.0;
-	double v = 0;
-	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += (i64)RED_BLOCKS * RED_THREADS)
+	v = 0;
+	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride)
 	{
 		// w = w' - alpha_j v_j - beta_{j-1} v_{j-1}, evaluated as in krylov.c:44-53
 		const double x = (j > 0) ? w[i] - (al * vj[i] + be * vjm1[i]) : w[i] - al * vj[i];
 		w[i] = x;
 		v = fma(x, x, v);
 	}
-	block_partial(v, partial);
-}
-
-__global__ void k_beta_final(const double* partial, LanczosScalars* sc, int j, i64 n)
-{
-	if (sc->stopped) return;
-	const double t = final_sum(partial);
-	if (threadIdx.x == 0)
+	block_partial(v, partial + RED_BLOCKS);
+	grid.sync();
+	const double b = sqrt(final_sum(partial + RED_BLOCKS));
+	const bool stop = b < 100.0 * (double)n * DBL_EPSILON;
+	if (blockIdx.x == 0 && threadIdx.x == 0)
 	{
-		const double b = sqrt(t);
 		sc->beta[j] = b;
-		if (b < 100.0 * (double)n * DBL_EPSILON)
+		if (stop)
 		{
 			sc->stopped = 1;
 			sc->numiter = j + 1;
 		}
 	}
+	if (stop) return;
+	const double inv = 1.0 / b;
+	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride) vj1[i] = inv * w[i];
 }
 
-void launch_lz_orth_beta(double* w, const double* vj, const double* vjm1, i64 n, int j, double* partial,
-                         LanczosScalars* sc, cudaStream_t st)
+// Normalisation of the start vector in one cooperative launch.
+__global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
+k_lz_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, double* __restrict__ partial, LanczosScalars* sc)
 {
-	k_orth_partial<<<RED_BLOCKS, RED_THREADS, 0, st>>>(w, vj, vjm1, n, j, partial, sc);
-	k_beta_final<<<1, RED_THREADS, 0, st>>>(partial, sc, j, n);
-	CTG_CUDA(cudaGetLastError());
+	cg::grid_group grid = cg::this_grid();
+	const i64 stride = (i64)RED_BLOCKS * RED_THREADS;
+	double x = 0;
+	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride) x = fma(v0[i], v0[i], x);
+	block_partial(x, partial);
+	grid.sync();
+	const double nrm = sqrt(final_sum(partial));
+	if (blockIdx.x == 0 && threadIdx.x == 0)
+	{
+		sc->nrm0 = nrm;
+		sc->stopped = 0;
+		sc->numiter = 0;
+		sc->status = 0;
+	}
+	const double inv = 1.0 / nrm;
+	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride) v[i] = inv * v0[i];
 }
 
-__global__ void k_next(const double* __restrict__ w, double* __restrict__ vj1, i64 n, int j, const LanczosScalars* sc)
+static void check_coop(const void* fn)
 {
-	if (sc->stopped) return;
-	const double inv = 1.0 / sc->beta[j];
-	for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) vj1[i] = inv * w[i];
+	static int ok[2] = {0, 0};
+	const int which = fn == (const void*)k_lz_step ? 0 : 1;
+	if (ok[which]) return;
+	int dev = 0, sms = 0, per_sm = 0, coop = 0;
+	CTG_CUDA(cudaGetDevice(&dev));
+	CTG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	CTG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+	CTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, RED_THREADS, 0));
+	CTG_CHECK(coop && per_sm * sms >= RED_BLOCKS, "Lanczos: the cooperative vector kernels do not fit on this device");
+	ok[which] = 1;
 }
 
-void launch_lz_next(const double* w, double* vj1, i64 n, int j, const LanczosScalars* sc, cudaStream_t st)
+void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, int j, int last,
+                    double* partial, LanczosScalars* sc, cudaStream_t st)
 {
-	k_next<<<RED_BLOCKS, 256, 0, st>>>(w, vj1, n, j, sc);
-	CTG_CUDA(cudaGetLastError());
+	check_coop((const void*)k_lz_step);
+	void* args[] = {&w, (void*)&vj, (void*)&vjm1, &vj1, &n, &j, &last, &partial, &sc};
+	CTG_CUDA(cudaLaunchCooperativeKernel((const void*)k_lz_step, dim3(RED_BLOCKS), dim3(RED_THREADS), args, 0, st));
+}
+
+void launch_lz_start(const double* v0, double* v, i64 n, double* partial, LanczosScalars* sc, cudaStream_t st)
+{
+	check_coop((const void*)k_lz_start);
+	void* args[] = {(void*)&v0, &v, &n, &partial, &sc};
+	CTG_CUDA(cudaLaunchCooperativeKernel((const void*)k_lz_start, dim3(RED_BLOCKS), dim3(RED_THREADS), args, 0, st));
 }
 
 // Lowest eigenpair of the k x k symmetric tridiagonal Lanczos matrix by cyclic Jacobi rotations
@@ -282,6 +279,8 @@ void launch_lz_next(const double* w, double* vj1, i64 n, int j, const LanczosSca
 __global__ void __launch_bounds__(32) k_tridiag(int maxiter, LanczosScalars* sc)
 {
 	__shared__ double A[LANCZOS_MAX][LANCZOS_MAX + 1], Z[LANCZOS_MAX][LANCZOS_MAX + 1];
+	__shared__ double rc[LANCZOS_MAX / 2 + 1], rs[LANCZOS_MAX / 2 + 1];
+	__shared__ int rp[LANCZOS_MAX / 2 + 1], rq[LANCZOS_MAX / 2 + 1];
 	const int lane = threadIdx.x;
 	if (lane == 0 && !sc->stopped) sc->numiter = maxiter;
 	__syncwarp();
@@ -302,6 +301,13 @@ __global__ void __launch_bounds__(32) k_tridiag(int maxiter, LanczosScalars* sc)
 			Z[lane][j] = (lane == j) ? 1.0 : 0.0;
 		}
 	__syncwarp();
+	// Parallel cyclic Jacobi: each step rotates a set of disjoint pairs (round-robin over k rounded
+	// up to even), one lane per pair forming its rotation; A <- J^T A J as all column rotations
+	// (lane r updates row r) then all row rotations (lane c updates column c). The angle comes from
+	// FP32, the rotation itself is orthogonal to FP64 rounding: t from FP32, c = 1 / sqrt(1 + t^2) and
+	// s = t c in FP64. The rotated a_pq (about 1e-7 of its old value) is kept, not set to zero: the
+	// transformation stays an orthogonal similarity, and the next sweep removes the residual.
+	const int np = k + (k & 1), half = np / 2;
 	for (int sweep = 0; sweep < 100; sweep++)
 	{
 		double off = 0, diag = 0;
@@ -317,51 +323,69 @@ __global__ void __launch_bounds__(32) k_tridiag(int maxiter, LanczosScalars* sc)
 		}
 		// off-diagonal norm below 1e-15 of the diagonal norm: converged
 		if (off <= 1e-30 * diag || off == 0.0) break;
-		for (int p = 0; p < k - 1; p++)
-			for (int q = p + 1; q < k; q++)
+		for (int step = 0; step < np - 1; step++)
+		{
+			if (lane < half)
 			{
-				const double apq = A[p][q];
-				if (apq == 0.0) continue;
-				const double app = A[p][p], aqq = A[q][q];
-				const double theta = (aqq - app) * rcp64(2.0 * apq);
-				const double t = copysign(1.0, theta) * rcp64(fabs(theta) + sqrt64(fma(theta, theta, 1.0)));
-				const double c = rcp64(sqrt64(fma(t, t, 1.0))), s = t * c;
-				double arp = 0, arq = 0;
-				if (lane < k)
+				int p, q;
+				if (lane == 0) { p = step; q = np - 1; }
+				else { p = (step + lane) % (np - 1); q = (step - lane + (np - 1)) % (np - 1); }
+				if (p > q) { const int x = p; p = q; q = x; }
+				double c = 1.0, sn = 0.0;
+				if (q < k)
 				{
-					arp = A[lane][p];
-					arq = A[lane][q];
+					const double apq = A[p][q];
+					if (apq != 0.0)
+					{
+						const double app = A[p][p], aqq = A[q][q];
+						const double theta = (aqq - app) * rcp64(2.0 * apq);
+						double t;
+						if (fabs(theta) > 1e15) t = 0.5 * rcp64(theta);
+						else
+						{
+							const float th = (float)theta;
+							const float tf = copysignf(1.0f, th) / (fabsf(th) + sqrtf(fmaf(th, th, 1.0f)));
+							t = (double)tf;
+						}
+						double sq, rsq;
+						sqrt_rsqrt64(fma(t, t, 1.0), sq, rsq);
+						c = rsq;
+						sn = t * rsq;
+					}
 				}
-				__syncwarp();
-				if (lane < k)
-				{
-					A[lane][p] = c * arp - s * arq;
-					A[lane][q] = s * arp + c * arq;
-				}
-				__syncwarp();
-				double apr = 0, aqr = 0;
-				if (lane < k)
-				{
-					apr = A[p][lane];
-					aqr = A[q][lane];
-				}
-				__syncwarp();
-				if (lane < k)
-				{
-					A[p][lane] = c * apr - s * aqr;
-					A[q][lane] = s * apr + c * aqr;
-					const double zrp = Z[lane][p], zrq = Z[lane][q];
-					Z[lane][p] = c * zrp - s * zrq;
-					Z[lane][q] = s * zrp + c * zrq;
-				}
-				__syncwarp();
-				if (lane == 0)
-				{
-					A[p][q] = 0.0;
-					A[q][p] = 0.0;
-				}
-				__syncwarp();
+				else q = -1;
+				rp[lane] = p;
+				rq[lane] = q;
+				rc[lane] = c;
+				rs[lane] = sn;
 			}
+			__syncwarp();
+			if (lane < k)
+				for (int i = 0; i < half; i++)
+				{
+					const int p = rp[i], q = rq[i];
+					if (q < 0) continue;
+					const double c = rc[i], sn = rs[i];
+					const double arp = A[lane][p], arq = A[lane][q];
+					A[lane][p] = c * arp - sn * arq;
+					A[lane][q] = sn * arp + c * arq;
+					const double zrp = Z[lane][p], zrq = Z[lane][q];
+					Z[lane][p] = c * zrp - sn * zrq;
+					Z[lane][q] = sn * zrp + c * zrq;
+				}
+			__syncwarp();
+			if (lane < k)
+				for (int i = 0; i < half; i++)
+				{
+					const int p = rp[i], q = rq[i];
+					if (q < 0) continue;
+					const double c = rc[i], sn = rs[i];
+					const double apc = A[p][lane], aqc = A[q][lane];
+					A[p][lane] = c * apc - sn * aqc;
+					A[q][lane] = sn * apc + c * aqc;
+				}
+			__syncwarp();
+		}
 	}
 	if (lane == 0)
 	{
