@@ -360,19 +360,31 @@ struct LocalH {
 	DBufPtr s1, tt1, s2, tt2;
 	DBufPtr pk_r, pk_w, pk_k, pk_x, pk_t1, pk_t2;   // packed tensor-core operands
 	bool tc = false;
+	bool fused = false;          // transposes written by the GEMM epilogues (FP64)
 	double flops = 0;
 
 	LocalH(Ctx& c, const Meta& a, const DTensor& w_, const DTensor& l, const DTensor& r_, int precision) : w(w_), r(r_)
 	{
-		d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1, precision);
 		const int p0[5] = {1, 2, 0, 3, 4};
-		t0 = make_transpose_plan(c, *d1.out, p0);
-		d2 = make_dot_plan(c, w.m(), AX_TRAILING, *t0.out, AX_LEADING, 2, precision);
 		const int p1[5] = {2, 0, 1, 3, 4};
-		t1 = make_transpose_plan(c, *d2.out, p1);
 		const int p2[4] = {0, 3, 1, 2};
+		// FP64: the two transposes are written by the GEMM epilogues (results land in the transposed
+		// layouts); the tensor-core path keeps them as separate passes
+		fused = precision == GEMM_FP64;
+		if (fused)
+		{
+			d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1, precision, p0);
+			d2 = make_dot_plan(c, w.m(), AX_TRAILING, *d1.out, AX_LEADING, 2, precision, p1);
+		}
+		else
+		{
+			d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1, precision);
+			t0 = make_transpose_plan(c, *d1.out, p0);
+			d2 = make_dot_plan(c, w.m(), AX_TRAILING, *t0.out, AX_LEADING, 2, precision);
+			t1 = make_transpose_plan(c, *d2.out, p1);
+		}
 		k = op_transpose(c, l, p2);
-		d3 = make_dot_plan(c, k.m(), AX_TRAILING, *t1.out, AX_LEADING, 2, precision);
+		d3 = make_dot_plan(c, k.m(), AX_TRAILING, fused ? *d2.out : *t1.out, AX_LEADING, 2, precision);
 		// the cyclic partial trace of the unit outer bonds keeps blocks and entries (view_trace_unit):
 		// with outer axes of dimension 1, equal quantum numbers and opposite directions, the inner
 		// axes obey the conservation law of a, so equal inner axes mean an equal block structure
@@ -384,10 +396,18 @@ struct LocalH {
 			same = o.dim[(size_t)i + 1] == a.dim[(size_t)i] && o.dir[(size_t)i + 1] == a.dir[(size_t)i] &&
 			       o.ql[(size_t)i + 1] == a.ql[(size_t)i];
 		CTG_CHECK(same, "local Hamiltonian output structure differs from the input");
-		s1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
-		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t0.out->nnz, 1) * sizeof(double));
-		s2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
-		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t1.out->nnz, 1) * sizeof(double));
+		if (fused)
+		{
+			tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
+			tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
+		}
+		else
+		{
+			s1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
+			tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t0.out->nnz, 1) * sizeof(double));
+			s2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
+			tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t1.out->nnz, 1) * sizeof(double));
+		}
 		flops = d1.flops + d2.flops + d3.flops;
 		if (precision == GEMM_BF16X3)
 		{
@@ -419,6 +439,13 @@ struct LocalH {
 			d3.pack_b(c, (const double*)tt2->ptr, pk_t2->ptr);
 			d3.run_packed(c, pk_k->ptr, pk_t2->ptr, y);
 			c.gemm_flops += flops;
+			return;
+		}
+		if (fused)
+		{
+			d1.run(c, x, r.data(), (double*)tt1->ptr);
+			d2.run(c, w.data(), (const double*)tt1->ptr, (double*)tt2->ptr);
+			d3.run(c, k.data(), (const double*)tt2->ptr, y);
 			return;
 		}
 		d1.run(c, x, r.data(), (double*)s1->ptr);

@@ -411,9 +411,10 @@ const T* at(const DBufPtr& b, size_t off)
 // dot (block_sparse_tensor.c:1826-2001; dense_tensor.c:1761-1837)
 // ------------------------------------------------------------------------------------
 
-static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
+static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
+                              const int* out_perm)
 {
-	DotLowering l = lower_dot(s, axs, t, axt, nmult, precision, c.num_sms());
+	DotLowering l = lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm);
 	DotPlan p;
 	p.out = l.out;
 	p.precision = precision;
@@ -560,10 +561,13 @@ static void dump_plan_request(int kind, const std::vector<i64>& params, const Me
 	fflush(f);
 }
 
-DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision)
+DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
+                      const int* out_perm)
 {
 	PlanTimer plan_timer(c);
-	const std::vector<i64> params = {axs, axt, nmult, precision};
+	std::vector<i64> params = {axs, axt, nmult, precision};
+	if (out_perm)
+		for (int i = 0; i < s.ndim + t.ndim - 2 * nmult; i++) params.push_back(out_perm[i]);
 	const uint64_t key = plan_key(0, params, s, &t);
 	if (const PlanEntry* e = plan_find(c, key, 0, params, s, &t)) return e->dot;
 	dump_plan_request(0, params, s, &t);
@@ -572,7 +576,7 @@ DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, in
 	e.params = params;
 	e.s = StructSig(s);
 	e.t = StructSig(t);
-	e.dot = build_dot_plan(c, s, axs, t, axt, nmult, precision);
+	e.dot = build_dot_plan(c, s, axs, t, axt, nmult, precision, out_perm);
 	const size_t bytes = e.dot.desc ? e.dot.desc->bytes : 0;
 	DotPlan p = e.dot;
 	plan_insert(c, key, std::move(e), bytes);

@@ -181,7 +181,10 @@ struct DotPlan {
 	void pack_b(Ctx& c, const double* B, void* bpack) const;      // b_recs * TC_B_REC_BYTES bytes
 	void run_packed(Ctx& c, const void* apack, const void* bpack, double* C) const;
 };
-DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision = GEMM_FP64);
+// out_perm (FP64 only): the result is written straight in the layout of its transpose by out_perm
+// (see lower_dot), and the plan's `out` is that transposed structure
+DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision = GEMM_FP64,
+                      const int* out_perm = nullptr);
 
 struct CopyPlan {
 	std::shared_ptr<const Meta> out;

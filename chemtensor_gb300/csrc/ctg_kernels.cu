@@ -139,19 +139,17 @@ __device__ __forceinline__ void gemm_tile_f64(const GemmTile& tile, const GemmOu
 		__syncthreads();
 		if (!last) return;
 		__threadfence();
-		double* cblk = C + o.c_off;
 		for (int e = tid; e < sp.rows * sp.cols; e += NT)
 		{
 			const int i = e / sp.cols, j = e - i * sp.cols;
 			const double* pw = work + sp.part + (i64)i * sp.ld + j;
 			double sum = 0.0;
 			for (int q = 0; q < sp.nsplit; q++) sum += __ldcg(pw + (i64)q * sp.stride);
-			cblk[(i64)(sp.m0 + i) * o.n + sp.n0 + j] = sum;
+			C[gemm_out_index(o, sp.m0 + i, sp.n0 + j)] = sum;
 		}
 		if (tid == 0) counters[tile.split] = 0;
 		return;
 	}
-	double* cblk = C + o.c_off;
 #pragma unroll
 	for (int i = 0; i < TM; i++)
 	{
@@ -161,7 +159,7 @@ __device__ __forceinline__ void gemm_tile_f64(const GemmTile& tile, const GemmOu
 		for (int j = 0; j < TN; j++)
 		{
 			const int gj = tile.n0 + tx + j * NTX;
-			if (gj < o.n) cblk[(i64)gi * o.n + gj] = acc[i][j];
+			if (gj < o.n) C[gemm_out_index(o, gi, gj)] = acc[i][j];
 		}
 	}
 }

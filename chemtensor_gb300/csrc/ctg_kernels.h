@@ -18,7 +18,18 @@ struct GemmOut {
 	i64 c_off;
 	int m, n;
 	int c0, nc;        // contribution range in the contribution array
+	// where element (i, j) of the block goes: c_off + (i / r1) sr0 + (i % r1) sr1 + (j / c1) sc0 +
+	// (j % c1); the plain row-major block is r1 = m, sr1 = n, c1 = n (sr0, sc0 unused). Other values
+	// write the block straight into the layout of a transposed result (two runs of row axes and two
+	// of column axes rearranged, the last column run innermost), so that no transpose pass is needed.
+	int r1, c1;
+	i64 sr0, sr1, sc0;
 };
+
+__host__ __device__ inline i64 gemm_out_index(const GemmOut& o, int i, int j)
+{
+	return o.c_off + (i64)(i / o.r1) * o.sr0 + (i64)(i % o.r1) * o.sr1 + (i64)(j / o.c1) * o.sc0 + (j % o.c1);
+}
 
 struct GemmContrib {
 	i64 a_off, b_off;

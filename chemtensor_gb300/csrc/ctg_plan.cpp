@@ -114,7 +114,8 @@ CopyLowering rows_lowering(std::shared_ptr<Meta> out, std::vector<RowDesc>&& d, 
 // dot (block_sparse_tensor.c:1826-2001; dense_tensor.c:1761-1837)
 // ------------------------------------------------------------------------------------
 
-DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision, int num_sms)
+DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision, int num_sms,
+                      const int* out_perm)
 {
 	DotLowering p;
 	double ts0 = host_seconds();
@@ -224,6 +225,11 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			o.c_off = r.boff[b];
 			o.m = (int)prod(rd, nfs);
 			o.n = (int)prod(rd + nfs, nft);
+			o.r1 = o.m;
+			o.sr0 = 0;
+			o.sr1 = o.n;
+			o.c1 = o.n;
+			o.sc0 = 0;
 			o.c0 = (int)R.cons.size();             // range-local until the join
 			i64 fs = 0, ft = 0;
 			for (int i = 0; i < nfs; i++) fs = fs * r.nb[i] + ir[i];
@@ -359,6 +365,70 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			tiles[k].insert(tiles[k].end(), R.tiles[k].begin(), R.tiles[k].end());
 			p.flops_cls[k] += R.flops_cls[k];
 		}
+	}
+	// Result written in a transposed layout (see GemmOut). The row axes are cut into two runs
+	// [0, x) and [x, nfs), the column axes into [nfs, nfs + y) and [nfs + y, nd); the permutation
+	// must arrange these runs (each kept in order) with the last column run innermost. Then every
+	// entry's position is i_hi sr0 + i_lo sr1 + j_hi sc0 + j_lo.
+	if (out_perm)
+	{
+		const int nd = r.ndim;
+		int cut_x = -1, cut_y = -1;
+		int order[4] = {0, 0, 0, 0}, ngroups = 0;       // groups in new order: 0 R_hi, 1 R_lo, 2 C_hi, 3 C_lo
+		for (int x = 0; x <= nfs && cut_x < 0; x++)
+			for (int y = 0; y <= nft && cut_x < 0; y++)
+			{
+				const int lo[4] = {0, x, nfs, nfs + y}, hi[4] = {x, nfs, nfs + y, nd};
+				int pos = 0, ng = 0, ord[4];
+				bool ok = true;
+				while (pos < nd && ok)
+				{
+					int g = -1;
+					for (int q = 0; q < 4; q++)
+						if (hi[q] > lo[q] && out_perm[pos] == lo[q]) g = q;
+					if (g < 0) { ok = false; break; }
+					for (int e = lo[g]; e < hi[g] && ok; e++, pos++) ok = pos < nd && out_perm[pos] == e;
+					ord[ng++] = g;
+				}
+				// the last column run, if any, must be innermost
+				if (ok && hi[3] > lo[3] && ord[ng - 1] != 3) ok = false;
+				if (ok)
+				{
+					cut_x = x;
+					cut_y = y;
+					ngroups = ng;
+					for (int q = 0; q < ng; q++) order[q] = ord[q];
+				}
+			}
+		CTG_CHECK(cut_x >= 0, "dot: unsupported output permutation");
+		auto outp = std::make_shared<Meta>(transpose_meta(r, out_perm));
+		std::vector<i64> ip((size_t)nd);
+		for (int b = 0; b < r.nblocks; b++)
+		{
+			const i64* ib = r.index(b);
+			const i64* d = r.dims(b);
+			for (int i = 0; i < nd; i++) ip[(size_t)i] = ib[out_perm[i]];
+			const int bp = outp->find(ip.data());
+			CTG_CHECK(bp >= 0, "dot: missing block of the transposed result");
+			const i64 size[4] = {prod(d, cut_x), prod(d + cut_x, nfs - cut_x), prod(d + nfs, cut_y),
+			                     prod(d + nfs + cut_y, nft - cut_y)};
+			i64 stride[4] = {0, 0, 0, 0}, st = 1;
+			for (int q = ngroups - 1; q >= 0; q--)
+			{
+				stride[order[q]] = st;
+				st *= size[order[q]];
+			}
+			GemmOut& o = outs[(size_t)b];
+			o.c_off = outp->boff[bp];
+			o.r1 = (int)size[1];
+			o.sr0 = stride[0];
+			o.sr1 = stride[1];
+			o.c1 = (int)size[3];
+			o.sc0 = stride[2];
+			CTG_CHECK(size[3] == 1 || stride[3] == 1, "dot: output layout");
+			CTG_CHECK(o.c_off + (i64)o.m * o.n <= outp->nnz, "dot: transposed output block out of range");
+		}
+		p.out = outp;
 	}
 	// Split-K: on GB300 one SM retires about two FP64 FMAs per clock, so a block GEMM with fewer
 	// tiles than SMs leaves most of the FP64 pipes idle. Tiles whose work exceeds a fair share of

@@ -28,7 +28,11 @@ struct DotLowering {
 	double flops_cls[NUM_TILE_CLASSES] = {};
 	i64 a_entries = 0, b_entries = 0;
 };
-DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision, int num_sms);
+// out_perm (optional, r.ndim entries): write the result in the layout of its transpose by out_perm,
+// which must arrange two runs of row axes and two runs of column axes (each run kept in order) with
+// the last column run innermost
+DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision, int num_sms,
+                      const int* out_perm = nullptr);
 
 // data movement: kind 0 block permutation (PermDesc), 1 row map (RowDesc + maps), 2 axis scaling
 // (ScaleDesc + maps)
