@@ -368,6 +368,34 @@ def bench_local_h(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def bench_serve(args, world, rank, local):
+    """Serving mix: a seeded Poisson stream of Heisenberg / Hubbard ground-state solves (L 8..48,
+    D 16..256, 2 sweeps each), replayed once by one solver thread (serial plain-FP64 solves, the
+    baseline) and once by --workers solver threads sharing the GPU."""
+    from chemtensor_gb300 import native, serving
+    lib = native.lib()
+    lib.ctgpu_set_device(local)
+    reqs = serving.generate_requests(args.requests, args.rate, seed=2024)
+    # warm-up: the first solves pay for context creation and kernel loading
+    serving.SolverPool(workers=1, device=local, sweeps=1).run(serving.generate_requests(3, 0.0, seed=7))
+    serial = serving.summarize(serving.SolverPool(workers=1, device=local).run(reqs))
+    pool = serving.SolverPool(workers=args.workers, device=local)
+    conc = serving.summarize(pool.run(reqs))
+    energies = {r.rid: r.energy for r in pool.results}
+    line = {
+        "metric": "DMRG serving throughput (Heisenberg/Hubbard mix, L 8-48, D 16-256, 2 sweeps)",
+        "value": conc["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.requests, "warmup": 3,
+        "ms_per_step": 1e3 / conc["solves_per_s"] if conc["solves_per_s"] else None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded request stream)",
+        "config": {"workload": f"{args.requests} requests, Poisson rate {args.rate}/s, seed 2024", "workers": args.workers},
+        "concurrent": conc, "serial": serial,
+        "speedup_vs_serial": (conc["solves_per_s"] / serial["solves_per_s"]) if serial["solves_per_s"] else None,
+        "energy_checksum": float(sum(energies.values())),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def sweeps_only(args, local):
     """One dmrg_twosite call of warmup + steps sweeps on the workload (profiler target)."""
     from chemtensor_gb300 import ctstructs as cs, native
@@ -398,9 +426,13 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=sorted(PRECISIONS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--matvecs", type=int, default=1000, help="local-H applications timed in --mode localh")
-    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh"],
+    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh", "serve"],
                     help="sweeps: only one device call of warmup+steps sweeps (for profiler captures), no JSON line; "
-                         "localh: local-Hamiltonian microbenchmark (synthetic D=1024), its own JSON line")
+                         "localh: local-Hamiltonian microbenchmark (synthetic D=1024), its own JSON line; "
+                         "serve: request stream of small and medium solves, serial vs concurrent solver threads")
+    ap.add_argument("--requests", type=int, default=128, help="requests of the --mode serve stream")
+    ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate (1/s) of --mode serve")
+    ap.add_argument("--workers", type=int, default=4, help="solver threads of --mode serve")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.mode == "sweeps":
@@ -408,6 +440,9 @@ def main():
         return
     if args.mode == "localh":
         bench_local_h(args, world, rank, local)
+        return
+    if args.mode == "serve":
+        bench_serve(args, world, rank, local)
         return
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

@@ -15,7 +15,7 @@
 
 namespace ctg {
 
-extern double g_plan_stage[12];
+extern thread_local double g_plan_stage[12];
 
 namespace {
 

@@ -7,6 +7,7 @@
 #include <chrono>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <cstring>
 #include <ctime>
 
@@ -540,6 +541,8 @@ static void dump_plan_request(int kind, const std::vector<i64>& params, const Me
 		return path ? fopen(path, "wb") : nullptr;
 	}();
 	if (!f) return;
+	static std::mutex mu;
+	std::lock_guard<std::mutex> lock(mu);
 	auto put_sig = [](const Meta& m) {
 		const int32_t nd = m.ndim;
 		fwrite(&nd, sizeof(nd), 1, f);

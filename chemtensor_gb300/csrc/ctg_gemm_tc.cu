@@ -19,6 +19,8 @@
 
 #include <cuda_bf16.h>
 
+#include <mutex>
+
 #include "ctg_kernels.h"
 
 namespace ctg {
@@ -329,12 +331,10 @@ void launch_gemm_tc(int ntiles, const GemmTile* tiles, const GemmOut* outs, cons
                     const void* bpack, double* C, int* error, cudaStream_t st)
 {
 	if (ntiles <= 0) return;
-	static bool attr_set = false;
-	if (!attr_set)
-	{
+	static std::once_flag attr_once;
+	std::call_once(attr_once, [] {
 		CTG_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES));
-		attr_set = true;
-	}
+	});
 	k_gemm_tc<<<ntiles, TC_THREADS, TC_SMEM_BYTES, st>>>(tiles, outs, tcons, (const unsigned char*)apack,
 	                                                       (const unsigned char*)bpack, C, error);
 	CTG_CUDA(cudaGetLastError());

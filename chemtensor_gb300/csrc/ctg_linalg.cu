@@ -1,6 +1,7 @@
 // ctg_linalg.cu - FP64 dense linear algebra on the device: per-block SVD
 // (one-sided Jacobi), per-block RQ (Householder) and the Lanczos vector
 // operations with deterministic warp-shuffle reductions.
+#include <atomic>
 #include <cfloat>
 
 #include <cooperative_groups.h>
@@ -246,16 +247,16 @@ k_lz_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, double*
 
 static void check_coop(const void* fn)
 {
-	static int ok[2] = {0, 0};
+	static std::atomic<int> ok[2] = {{0}, {0}};
 	const int which = fn == (const void*)k_lz_step ? 0 : 1;
-	if (ok[which]) return;
+	if (ok[which].load()) return;
 	int dev = 0, sms = 0, per_sm = 0, coop = 0;
 	CTG_CUDA(cudaGetDevice(&dev));
 	CTG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 	CTG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
 	CTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, RED_THREADS, 0));
 	CTG_CHECK(coop && per_sm * sms >= RED_BLOCKS, "Lanczos: the cooperative vector kernels do not fit on this device");
-	ok[which] = 1;
+	ok[which].store(1);
 }
 
 void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, int j, int last,

@@ -9,7 +9,7 @@
 
 namespace ctg {
 
-double g_plan_stage[12];
+thread_local double g_plan_stage[12];
 
 namespace {
 

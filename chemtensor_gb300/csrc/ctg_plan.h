@@ -55,6 +55,6 @@ CopyLowering lower_scale(const Meta& m, int axrange);
 // host time of the lowering stages (diagnostics): 0 dot meta, 1 dot enumeration, 2 split-K,
 // 3 dot tile lists, 4 transpose meta, 5 transpose loop, 6 flatten meta, 7 flatten loop,
 // 8 split meta, 9 split loop, 10 slice, 11 other
-extern double g_plan_stage[12];
+extern thread_local double g_plan_stage[12];
 
 }  // namespace ctg

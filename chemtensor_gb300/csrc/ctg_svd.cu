@@ -1741,15 +1741,14 @@ void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* d
 		CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_global, descs, first, a, u, s, vh, scratch, status, 0.0, flops, g.cluster));
 		return;
 	}
-	static bool attr_set[64] = {false};
+	static std::once_flag attr_once[64];
 	int dev = 0;
 	CTG_CUDA(cudaGetDevice(&dev));
-	if (dev >= 0 && dev < 64 && !attr_set[dev])
-	{
-		CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeMaxDynamicSharedMemorySize, SVD_SMEM_LIMIT));
-		CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-		attr_set[dev] = true;
-	}
+	if (dev >= 0 && dev < 64)
+		std::call_once(attr_once[dev], [] {
+			CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeMaxDynamicSharedMemorySize, SVD_SMEM_LIMIT));
+			CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+		});
 	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, flops, g.cluster, g.smem,
 	                             phase_ts, svd_f32_min(), svd_f32_cluster()));
 }

@@ -1,0 +1,167 @@
+"""A small DMRG solve service on one GPU: seeded request streams and a pool of solver threads.
+
+Each request is a ground-state search (two-site DMRG through the C-ABI ``dmrg_twosite``) for a 1D
+Heisenberg XXZ or Fermi-Hubbard chain. Worker threads take requests in arrival order; every thread
+owns its own execution context in libctgpu.so (stream, memory pool, plan cache), so solves of
+different threads run side by side on the GPU while each thread's solve stays sequential. The
+library's per-call state (device, precision, last error, statistics) is thread-local.
+
+Request mix (the serving configuration of the two-site DMRG scope): Heisenberg with anisotropy
+Delta ~ U[0.5, 1.5] or Hubbard with U ~ U[1, 8] (t = 1, half filling), length L ~ U{8..48}, bond
+dimension D in {16, 32, 64, 128, 256}, Poisson arrivals; every parameter drawn from one seeded
+generator.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import ctstructs as cs
+from . import hamiltonians as hm
+from . import native
+
+BOND_DIMS = (16, 32, 64, 128, 256)
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds after the start of the stream
+    model: str              # "heisenberg" or "hubbard"
+    nsites: int
+    max_vdim: int
+    param: float            # Delta (Heisenberg) or U (Hubbard)
+    seed: int
+
+
+@dataclass
+class Result:
+    rid: int
+    arrival: float
+    start: float = 0.0
+    end: float = 0.0
+    energy: float = float("nan")
+    ret: int = 0
+    worker: int = -1
+    error: str = ""
+
+    @property
+    def latency(self) -> float:
+        return self.end - self.arrival
+
+
+def generate_requests(n: int, rate: float, seed: int) -> list[Request]:
+    """n requests with exponential inter-arrival times of mean 1 / rate (seconds)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += float(rng.exponential(1.0 / rate)) if rate > 0 else 0.0
+        hub = bool(rng.random() < 0.5)
+        nsites = int(rng.integers(8, 49))
+        d = int(rng.choice(BOND_DIMS))
+        param = float(rng.uniform(1.0, 8.0)) if hub else float(rng.uniform(0.5, 1.5))
+        out.append(Request(i, t, "hubbard" if hub else "heisenberg", nsites, d, param, int(rng.integers(1, 2**31))))
+    return out
+
+
+def build_problem(req: Request):
+    """MPO and seeded random start state of a request (host side)."""
+    # half filling / smallest total spin: 2 Sz = L mod 2
+    sz2 = req.nsites % 2
+    if req.model == "hubbard":
+        H = hm.fermi_hubbard_1d(req.nsites, 1.0, req.param, 0.0)
+        c = native.random_mps(req.nsites, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(req.nsites, sz2),
+                              req.max_vdim, req.seed)
+    else:
+        H = hm.heisenberg_xxz_1d(req.nsites, 1.0, req.param, 0.0)
+        c = native.random_mps(req.nsites, 2, [1, -1], sz2, req.max_vdim, req.seed)
+    psi = cs.read_mps(c)
+    cs.free_mps(c)
+    return H, psi
+
+
+@dataclass
+class SolverPool:
+    """Replays a request stream against `workers` solver threads on one GPU."""
+    workers: int = 4
+    device: int = 0
+    sweeps: int = 2
+    maxiter: int = 5
+    tol: float = 1e-10
+    precision: int = native.PRECISION_FP64
+    results: list = field(default_factory=list)
+
+    def _solve(self, req: Request, res: Result, lib):
+        H, psi = build_problem(req)
+        cH, cP = cs.make_c_mpo(H), cs.make_c_mps(psi)
+        en = np.zeros(self.sweeps)
+        ent = np.zeros(max(H.nsites - 1, 1))
+        try:
+            res.ret = lib.dmrg_twosite(C.byref(cH), self.sweeps, self.maxiter, self.tol, req.max_vdim, C.byref(cP),
+                                       en.ctypes.data, ent.ctypes.data)
+            res.energy = float(en[-1])
+            if res.ret != 0:
+                res.error = native.last_error()
+        finally:
+            cs.free_mps(cP)
+            cs.free_mpo(cH)
+
+    def run(self, requests: list[Request]) -> list[Result]:
+        lib = native.lib()
+        q: queue.Queue = queue.Queue()
+        for r in sorted(requests, key=lambda r: r.arrival):
+            q.put(r)
+        results = {r.rid: Result(r.rid, r.arrival) for r in requests}
+        t0 = time.perf_counter()
+        errors = []
+
+        def worker(wid: int):
+            lib.ctgpu_set_device(self.device)
+            lib.ctgpu_set_precision(self.precision)
+            while True:
+                try:
+                    req = q.get_nowait()
+                except queue.Empty:
+                    return
+                wait = req.arrival - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(wait)
+                res = results[req.rid]
+                res.worker = wid
+                res.start = time.perf_counter() - t0
+                try:
+                    self._solve(req, res, lib)
+                except Exception as e:  # recorded, the stream goes on
+                    res.ret = -99
+                    res.error = str(e)
+                    errors.append(e)
+                res.end = time.perf_counter() - t0
+
+        threads = [threading.Thread(target=worker, args=(i,), daemon=True) for i in range(self.workers)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        self.results = [results[r.rid] for r in requests]
+        return self.results
+
+
+def summarize(results: list[Result]) -> dict:
+    lat = np.array([r.latency for r in results if r.ret == 0])
+    span = max(r.end for r in results) - min(r.arrival for r in results) if results else 0.0
+    ok = int(np.sum([r.ret == 0 for r in results]))
+    return {
+        "requests": len(results), "solved": ok, "failed": len(results) - ok,
+        "solves_per_s": ok / span if span > 0 else None,
+        "p50_ms": float(np.percentile(lat, 50) * 1e3) if lat.size else None,
+        "p99_ms": float(np.percentile(lat, 99) * 1e3) if lat.size else None,
+        "mean_ms": float(lat.mean() * 1e3) if lat.size else None,
+        "makespan_s": span,
+    }
