@@ -51,6 +51,15 @@ int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int 
 	});
 }
 
+int dmrg_singlesite(const struct mpo* hamiltonian, const int num_sweeps, const int maxiter_lanczos, struct mps* psi,
+                    double* en_sweeps)
+{
+	return guarded([&] {
+		CTG_CHECK(hamiltonian && psi && en_sweeps, "null argument");
+		return ctg::dmrg_singlesite_gpu(hamiltonian, num_sweeps, maxiter_lanczos, psi, en_sweeps, g_opts, &g_stats);
+	});
+}
+
 int ctgpu_set_precision(int precision)
 {
 	if (precision != ctg::GEMM_FP64 && precision != ctg::GEMM_BF16X3) return ERR_RUNTIME;
@@ -217,6 +226,40 @@ int ctgpu_block_sparse_tensor_svd_values(const struct block_sparse_tensor* a, do
 		if (ret < 0) return ret;
 		CTG_CUDA(cudaMemcpy(sigma, sv.s->ptr, (size_t)sv.ns * sizeof(double), cudaMemcpyDeviceToHost));
 		*ns = sv.ns;
+		return 0;
+	});
+}
+
+int ctgpu_block_sparse_tensor_qr(const struct block_sparse_tensor* a, int mode, struct block_sparse_tensor* q,
+                                 struct block_sparse_tensor* r)
+{
+	return guarded([&] {
+		CTG_CHECK(a && q && r, "null argument");
+		CTG_CHECK(mode == 0, "block_sparse_tensor_qr: only QR_REDUCED is supported");
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor da = ctg::tensor_from_struct(c, a);
+		ctg::DTensor dq, dr;
+		const int ret = ctg::op_qr(c, da, dq, dr);
+		if (ret < 0) return ret;
+		ctg::tensor_to_struct(c, dq, q);
+		ctg::tensor_to_struct(c, dr, r);
+		return 0;
+	});
+}
+
+int ctgpu_block_sparse_tensor_rq(const struct block_sparse_tensor* a, int mode, struct block_sparse_tensor* r,
+                                 struct block_sparse_tensor* q)
+{
+	return guarded([&] {
+		CTG_CHECK(a && q && r, "null argument");
+		CTG_CHECK(mode == 0, "block_sparse_tensor_rq: only QR_REDUCED is supported");
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		ctg::DTensor da = ctg::tensor_from_struct(c, a);
+		ctg::DTensor dr, dq;
+		const int ret = ctg::op_rq(c, da, dr, dq);
+		if (ret < 0) return ret;
+		ctg::tensor_to_struct(c, dr, r);
+		ctg::tensor_to_struct(c, dq, q);
 		return 0;
 	});
 }

@@ -282,6 +282,23 @@ int local_orthonormalize_rq(Ctx& c, DTensor& a, DTensor& a_prev)
 	return ret;
 }
 
+// mps_local_orthonormalize_qr (src/state/mps.c:513-553)
+int local_orthonormalize_qr(Ctx& c, DTensor& a, DTensor& a_next)
+{
+	const Meta& am = a.m();
+	CTG_CHECK(am.ndim == 3 && am.dir[0] == TENSOR_AXIS_OUT && am.dir[1] == TENSOR_AXIS_OUT,
+	          "mps_local_orthonormalize_qr: unexpected tensor layout");
+	const i64 dl[2] = {am.dim[0], am.dim[1]};
+	const std::vector<q32> ql[2] = {am.ql[0], am.ql[1]};
+	const int adl[2] = {TENSOR_AXIS_OUT, TENSOR_AXIS_OUT};
+	DTensor mat = op_flatten(c, a, 0, TENSOR_AXIS_OUT);
+	DTensor q, r;
+	const int ret = op_qr(c, mat, q, r);
+	a = op_split(c, q, 0, dl, adl, ql);
+	a_next = op_dot(c, r, AX_TRAILING, a_next, AX_LEADING, 1);
+	return ret;
+}
+
 DTensor head_tensor(Ctx& c, const DTensor& a0, double value)
 {
 	const i64 dim[3] = {a0.m().dim[0], 1, a0.m().dim[0]};
@@ -763,6 +780,126 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		fprintf(stderr, "ctgpu: distributed QR of that block, SM cycles per sweep: candidates %.3g reflectors %.3g exchange %.3g fetch %.3g updates %.3g\n",
 		        c.svd_qr_cycles[0] / st->sweeps, c.svd_qr_cycles[1] / st->sweeps, c.svd_qr_cycles[2] / st->sweeps,
 		        c.svd_qr_cycles[3] / st->sweeps, c.svd_qr_cycles[4] / st->sweeps);
+	st->wall_s = now_s() - t_start;
+	return 0;
+}
+
+// ------------------------------------------------------------------------------------
+// dmrg_singlesite (src/algorithm/dmrg.c:155-254)
+// ------------------------------------------------------------------------------------
+
+int dmrg_singlesite_gpu(const struct mpo* H, int num_sweeps, int maxiter, struct mps* psi, double* en_sweeps,
+                        const DmrgOptions& opt, DmrgStats* stats)
+{
+	const double t_start = now_s();
+	DmrgStats local;
+	DmrgStats* st = stats ? stats : &local;
+	*st = DmrgStats();
+	const int L = H->nsites;
+	CTG_CHECK(L >= 1 && psi->nsites == L, "dmrg_singlesite: need nsites >= 1 and matching MPO / MPS lengths");
+	CTG_CHECK(psi->d == H->d, "dmrg_singlesite: physical dimensions of MPO and MPS differ");
+	CTG_CHECK(maxiter >= 1 && maxiter <= LANCZOS_MAX, "dmrg_singlesite: maxiter_lanczos out of the supported range");
+	CTG_CHECK(num_sweeps >= 0, "dmrg_singlesite: negative number of sweeps");
+
+	Ctx& c = context_for_device(opt.device);
+	c.gemm_flops = 0;
+	c.kernel_launches = 0;
+	c.profile = false;
+	DBuf sc_buf(&c, sizeof(LanczosScalars));
+	LanczosScalars* d_sc = (LanczosScalars*)sc_buf.ptr;
+	LanczosScalars* h_sc = c.lanczos_host();
+
+	std::vector<DTensor> W(L), A(L);
+	for (int i = 0; i < L; i++) W[i] = tensor_from_struct(c, &H->a[i]);
+	for (int i = 0; i < L; i++) A[i] = tensor_from_struct(c, &psi->a[i]);
+	c.sync();
+	const double t_up = now_s();
+	st->upload_s = t_up - t_start;
+
+	int ret = 0;
+	// right-normalise (mps_orthonormalize_qr, src/state/mps.c:609-757)
+	for (int i = L - 1; i > 0 && ret == 0; i--) ret = local_orthonormalize_rq(c, A[i], A[i - 1]);
+	{
+		DTensor head = head_tensor(c, A[0], 1.0);
+		if (ret == 0) ret = local_orthonormalize_rq(c, A[0], head);
+		std::vector<double> hv((size_t)std::max<i64>(head.m().nnz, 1), 0.0);
+		if (head.m().nnz > 0) copy_to_host(c, head, hv.data());
+		double nrm = head.m().nblocks > 0 ? hv[0] : 0.0;
+		if (nrm < 0)
+		{
+			std::vector<double> vec((size_t)A[0].m().dim[0], -1.0);
+			DBufPtr mv = c.upload(vec.data(), vec.size() * sizeof(double));
+			A[0] = op_scale_axis(c, A[0], (const double*)mv->ptr, AX_LEADING);
+			nrm = -nrm;
+		}
+		if (nrm == 0) printf("Warning: in 'dmrg_singlesite': initial MPS has norm zero (possibly due to mismatching quantum numbers)\n");
+	}
+	if (ret < 0) return ret;
+
+	// environments (dmrg.c:175-182)
+	std::vector<DTensor> lb(L), rb(L);
+	rb[L - 1] = dummy_block(c, A[L - 1].m().ql[2], W[L - 1].m().ql[3], A[L - 1].m().ql[2], true);
+	for (int i = L - 1; i > 0; i--) rb[i - 1] = contraction_step_right(c, A[i], W[i], rb[i]);
+	lb[0] = dummy_block(c, A[0].m().ql[0], W[0].m().ql[0], A[0].m().ql[0], false);
+	for (int i = 1; i < L; i++) lb[i] = lb[0];
+	c.sync();
+	const double t_setup = now_s();
+	st->setup_s = t_setup - t_up;
+
+	// local optimisation of site i; the Lanczos status is checked per site as in the reference
+	auto site_step = [&](int i) -> int {
+		DTensor aopt;
+		int r = minimize_local_energy(c, W[i], lb[i], rb[i], A[i], maxiter, d_sc, aopt, st, GEMM_FP64);
+		if (r < 0) return r;
+		CTG_CUDA(cudaMemcpyAsync(h_sc, d_sc, sizeof(LanczosScalars), cudaMemcpyDeviceToHost, c.stream()));
+		c.sync();
+		if (h_sc->status != 0) return h_sc->status;
+		A[i] = aopt;
+		return 0;
+	};
+	for (int sw = 0; sw < num_sweeps && ret == 0; sw++)
+	{
+		double en = 0;
+		// sweep from left to right
+		for (int i = 0; i < L - 1 && ret == 0; i++)
+		{
+			ret = site_step(i);
+			if (ret < 0) break;
+			en = h_sc->lambda;
+			ret = local_orthonormalize_qr(c, A[i], A[i + 1]);
+			lb[i + 1] = contraction_step_left(c, A[i], W[i], lb[i]);
+		}
+		// sweep from right to left
+		for (int i = L - 1; i > 0 && ret == 0; i--)
+		{
+			ret = site_step(i);
+			if (ret < 0) break;
+			en = h_sc->lambda;
+			ret = local_orthonormalize_rq(c, A[i], A[i - 1]);
+			rb[i - 1] = contraction_step_right(c, A[i], W[i], rb[i]);
+		}
+		if (ret < 0) break;
+		// right-normalise the leftmost tensor so that psi is normalised (dmrg.c:230-243)
+		DTensor t = head_tensor(c, A[0], 0.0);
+		ret = local_orthonormalize_rq(c, A[0], t);
+		en_sweeps[sw] = en;
+		c.sync();
+		st->sweeps++;
+	}
+	c.sync();
+	const double t_sweeps = now_s();
+	st->sweep_s = t_sweeps - t_setup;
+	if (ret < 0) return ret;
+	for (int i = 0; i < L; i++)
+	{
+		free_struct(&psi->a[i]);
+		tensor_to_struct(c, A[i], &psi->a[i]);
+		st->max_bond_dim = std::max(st->max_bond_dim, A[i].m().dim[2]);
+	}
+	c.sync();
+	st->download_s = now_s() - t_sweeps;
+	st->kernel_launches = c.kernel_launches;
+	st->total_gemm_flops = c.gemm_flops;
 	st->wall_s = now_s() - t_start;
 	return 0;
 }

@@ -44,6 +44,10 @@ struct DmrgStats {
 int dmrg_twosite_gpu(const struct mpo* hamiltonian, int num_sweeps, int maxiter_lanczos, double tol_split, i64 max_vdim,
                      struct mps* psi, double* en_sweeps, double* entropy, const DmrgOptions& opt, DmrgStats* stats);
 
+// Same contract as dmrg_singlesite (src/algorithm/dmrg.c:155-254): bond dimensions fixed by psi.
+int dmrg_singlesite_gpu(const struct mpo* hamiltonian, int num_sweeps, int maxiter_lanczos, struct mps* psi,
+                        double* en_sweeps, const DmrgOptions& opt, DmrgStats* stats);
+
 // truncation rule of retained_bond_indices (src/algorithm/truncation.c:110-223)
 struct TruncResult {
 	std::vector<i64> ind;

@@ -1037,7 +1037,78 @@ int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q)
 		d.w_off = woff;
 		d.m = (int)bl.m;
 		d.n = (int)bl.n;
+		d.qr = 0;
 		woff += bl.n * bl.m + bl.n * bl.k + bl.k;
+		descs.push_back(d);
+	}
+	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(RqDesc));
+	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
+	KScope ks(c, K_RQ, 1);
+	launch_rq_householder((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr,
+	                      c.stream());
+	return 0;
+}
+
+int op_qr(Ctx& c, const DTensor& a, DTensor& q, DTensor& r)
+{
+	const Meta& am = a.m();
+	CTG_CHECK(am.ndim == 2, "qr: matrix expected");
+	std::vector<q32> qi;
+	struct Blk { int ab; i64 m, n, k; };
+	std::vector<Blk> blks;
+	// column blocks outer: the intermediate quantum numbers come out sorted
+	for (i64 j = 0; j < am.nb[1]; j++)
+		for (i64 i = 0; i < am.nb[0]; i++)
+		{
+			const i64 idx[2] = {i, j};
+			const int b = am.find(idx);
+			if (b < 0) continue;
+			const i64 m = am.dims(b)[0], n = am.dims(b)[1], k = std::min(m, n);
+			for (i64 l = 0; l < k; l++) qi.push_back(am.qb[1][j]);
+			blks.push_back(Blk{b, m, n, k});
+		}
+	bool dummy = false;
+	if (qi.empty())
+	{
+		dummy = true;
+		qi.push_back(-am.dir[0] * am.dir[1] * am.qb[0][0]);
+	}
+	const i64 ni = (i64)qi.size();
+	const i64 dq[2] = {am.dim[0], ni};
+	Meta mq = make_meta(2, dq, am.dir.data(), {am.ql[0], qi});
+	const i64 dr[2] = {ni, am.dim[1]};
+	const int dirr[2] = {-am.dir[1], am.dir[1]};
+	Meta mr = make_meta(2, dr, dirr, {qi, am.ql[1]});
+	q = c.zeros(mq);
+	r = c.zeros(mr);
+	if (dummy)
+	{
+		const i64 idx[2] = {0, (i64)mq.find_q(1, qi[0])};
+		const int b = mq.find(idx);
+		CTG_CHECK(b >= 0, "qr: dummy block missing");
+		static const double one = 1.0;
+		CTG_CUDA(cudaMemcpyAsync(q.data() + mq.boff[b], &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
+		c.sync();
+		return 0;
+	}
+	std::vector<RqDesc> descs;
+	i64 woff = 0;
+	for (const Blk& bl : blks)
+	{
+		const i64* ia = am.index(bl.ab);
+		const i64 kb = mq.find_q(1, am.qb[1][ia[1]]);
+		const i64 iq[2] = {ia[0], kb}, ir[2] = {kb, ia[1]};
+		const int bq = mq.find(iq), br = mr.find(ir);
+		CTG_CHECK(br >= 0 && bq >= 0, "qr: factor blocks missing");
+		RqDesc d = {};
+		d.a_off = am.boff[bl.ab];
+		d.r_off = mr.boff[br];
+		d.q_off = mq.boff[bq];
+		d.w_off = woff;
+		d.m = (int)bl.m;
+		d.n = (int)bl.n;
+		d.qr = 1;
+		woff += bl.m * bl.n + bl.m * bl.k + bl.k;
 		descs.push_back(d);
 	}
 	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(RqDesc));

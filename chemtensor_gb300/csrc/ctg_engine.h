@@ -240,6 +240,8 @@ int op_svd(Ctx& c, const DTensor& a, SvdResult& res);
 
 // block RQ (block_sparse_tensor_rq, block_sparse_tensor.c:2544-2676). Returns 0 or -1.
 int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q);
+// block QR (block_sparse_tensor_qr, block_sparse_tensor.c:2402-2540). Returns 0 or -1.
+int op_qr(Ctx& c, const DTensor& a, DTensor& q, DTensor& r);
 
 // host <-> device entry copies (asynchronous on the context stream; host memory must stay valid)
 void copy_to_device(Ctx& c, DTensor& t, const double* host);

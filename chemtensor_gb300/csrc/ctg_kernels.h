@@ -194,8 +194,9 @@ void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* d
 // Householder RQ of a row-major m x n block: A = R Q with Q (k x n) orthonormal rows, R (m x k), k = min(m, n).
 // Scratch holds n*m + n*k + k doubles per block.
 struct RqDesc {
-	i64 a_off, r_off, q_off, w_off;
+	i64 a_off, r_off, q_off, w_off;   // w_off: scratch of m n + max(m, n) min(m, n) + min(m, n) doubles
 	int m, n;
+	int qr;                           // 1: A = Q R (dgeqrf convention), 0: A = R Q (dgerqf convention)
 };
 void launch_rq_householder(int nblocks, const RqDesc* descs, const double* a, double* r, double* q, double* scratch,
                            cudaStream_t st);

@@ -22,9 +22,13 @@ __device__ __forceinline__ double warp_sum(double v)
 }
 
 // ------------------------------------------------------------------------------------
-// block RQ through a Householder QR of the transpose, one CTA per block.
-// Replaces LAPACK dgerqf + dorgrq in dense_tensor_rq_fill (dense_tensor.c:2680-2880):
-// A = R Q with orthonormal rows of Q; R is the transpose of the triangular QR factor.
+// block QR / RQ by Householder reflections, one CTA per block.
+// QR (desc.qr = 1) follows LAPACK dgeqrf + dorgqr in dense_tensor_qr_fill (dense_tensor.c:2253-2651):
+// A = Q R, R upper triangular with diagonal entries -sign(alpha) * |x| of the reflectors.
+// RQ (desc.qr = 0) follows dgerqf + dorgrq in dense_tensor_rq_fill (dense_tensor.c:2680-2880):
+// dgerqf eliminates the rows of A from the last one upwards, each towards its trailing column; that
+// is the QR above applied to W = J A^T J (J reverses an index), with A = (J R_W^T J) (J Q_W^T J).
+// Both run the same column-Householder loop on a column-major work matrix W (p x s).
 // ------------------------------------------------------------------------------------
 
 constexpr int RQ_THREADS = 256;
@@ -49,20 +53,25 @@ k_rq_householder(const RqDesc* __restrict__ descs, const double* __restrict__ a,
 	__shared__ double sh_beta, sh_tau, sh_scale;
 	const RqDesc d = descs[blockIdx.x];
 	const int m = d.m, n = d.n;
+	const bool qr = d.qr != 0;
 	const int k = min(m, n);
+	const int p = qr ? m : n, s = qr ? n : m;   // W is p x s, column-major
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = RQ_THREADS / 32;
-	// B = A^T (n x m) column-major equals A row-major: column c of B is row c of A
-	double* B = scratch + d.w_off;             // n x m
-	double* Q = B + (i64)n * m;                // n x k
-	double* tau = Q + (i64)n * k;              // k
+	double* B = scratch + d.w_off;             // W, p x s
+	double* Q = B + (i64)p * s;                // Q_W, p x k
+	double* tau = Q + (i64)p * k;              // k
 	const double* ab = a + d.a_off;
-	for (i64 e = tid; e < (i64)n * m; e += RQ_THREADS) B[e] = ab[e];
+	for (i64 e = tid; e < (i64)p * s; e += RQ_THREADS)
+	{
+		const i64 i = e % p, j = e / p;
+		B[e] = qr ? ab[i * n + j] : ab[(m - 1 - j) * n + (n - 1 - i)];
+	}
 	__syncthreads();
 	for (int c = 0; c < k; c++)
 	{
-		double* bc = B + (i64)c * n;
+		double* bc = B + (i64)c * p;
 		double part = 0;
-		for (int i = c + 1 + tid; i < n; i += RQ_THREADS) part = fma(bc[i], bc[i], part);
+		for (int i = c + 1 + tid; i < p; i += RQ_THREADS) part = fma(bc[i], bc[i], part);
 		const double xnorm2 = block_sum(part, red);
 		if (tid == 0)
 		{
@@ -83,55 +92,72 @@ k_rq_householder(const RqDesc* __restrict__ descs, const double* __restrict__ a,
 		}
 		__syncthreads();
 		const double tc = sh_tau;
-		for (int i = c + 1 + tid; i < n; i += RQ_THREADS) bc[i] *= sh_scale;
+		for (int i = c + 1 + tid; i < p; i += RQ_THREADS) bc[i] *= sh_scale;
 		__syncthreads();
 		if (tid == 0) { bc[c] = sh_beta; tau[c] = tc; }
 		__syncthreads();
 		// apply H = I - tau v v^T (v = (1, bc[c+1:])) to the remaining columns
 		if (tc != 0.0)
 		{
-			for (int c2 = c + 1 + warp; c2 < m; c2 += nwarps)
+			for (int c2 = c + 1 + warp; c2 < s; c2 += nwarps)
 			{
-				double* b2 = B + (i64)c2 * n;
+				double* b2 = B + (i64)c2 * p;
 				double acc = 0;
-				for (int i = c + lane; i < n; i += 32) acc = fma(i == c ? 1.0 : bc[i], b2[i], acc);
+				for (int i = c + lane; i < p; i += 32) acc = fma(i == c ? 1.0 : bc[i], b2[i], acc);
 				acc = warp_sum(acc) * tc;
-				for (int i = c + lane; i < n; i += 32) b2[i] -= acc * (i == c ? 1.0 : bc[i]);
+				for (int i = c + lane; i < p; i += 32) b2[i] -= acc * (i == c ? 1.0 : bc[i]);
 			}
 		}
 		__syncthreads();
 	}
-	// Q1 = H_0 ... H_{k-1} E (n x k), accumulated backwards, column-major
-	for (i64 e = tid; e < (i64)n * k; e += RQ_THREADS) Q[e] = (e / n == e % n) ? 1.0 : 0.0;
+	// Q_W = H_0 ... H_{k-1} E (p x k), accumulated backwards, column-major
+	for (i64 e = tid; e < (i64)p * k; e += RQ_THREADS) Q[e] = (e / p == e % p) ? 1.0 : 0.0;
 	__syncthreads();
 	for (int c = k - 1; c >= 0; c--)
 	{
 		const double tc = tau[c];
-		const double* bc = B + (i64)c * n;
+		const double* bc = B + (i64)c * p;
 		if (tc != 0.0)
 		{
 			for (int j = warp; j < k; j += nwarps)
 			{
-				double* qj = Q + (i64)j * n;
+				double* qj = Q + (i64)j * p;
 				double acc = 0;
-				for (int i = c + lane; i < n; i += 32) acc = fma(i == c ? 1.0 : bc[i], qj[i], acc);
+				for (int i = c + lane; i < p; i += 32) acc = fma(i == c ? 1.0 : bc[i], qj[i], acc);
 				acc = warp_sum(acc) * tc;
-				for (int i = c + lane; i < n; i += 32) qj[i] -= acc * (i == c ? 1.0 : bc[i]);
+				for (int i = c + lane; i < p; i += 32) qj[i] -= acc * (i == c ? 1.0 : bc[i]);
 			}
 		}
 		__syncthreads();
 	}
-	// R = R1^T (m x k): R[i][j] = R1[j][i] = B(col i, row j) for i >= j
-	for (i64 e = tid; e < (i64)m * k; e += RQ_THREADS)
+	if (qr)
 	{
-		const i64 i = e / k, j = e % k;
-		r[d.r_off + e] = (i >= j) ? B[i * n + j] : 0.0;
+		// R (k x n) = upper part of W; Q (m x k) = Q_W
+		for (i64 e = tid; e < (i64)k * n; e += RQ_THREADS)
+		{
+			const i64 i = e / n, j = e % n;
+			r[d.r_off + e] = (i <= j) ? B[i + (i64)p * j] : 0.0;
+		}
+		for (i64 e = tid; e < (i64)m * k; e += RQ_THREADS)
+		{
+			const i64 i = e / k, j = e % k;
+			q[d.q_off + e] = Q[i + (i64)p * j];
+		}
 	}
-	// Q = Q1^T (k x n)
-	for (i64 e = tid; e < (i64)k * n; e += RQ_THREADS)
+	else
 	{
-		const i64 j = e / n, i = e % n;
-		q[d.q_off + e] = Q[j * n + i];
+		// R (m x k): R[i][j] = R_W[k-1-j][m-1-i]; Q (k x n): Q[j][i] = Q_W[n-1-i][k-1-j]
+		for (i64 e = tid; e < (i64)m * k; e += RQ_THREADS)
+		{
+			const i64 i = e / k, j = e % k;
+			const i64 a0 = k - 1 - j, b0 = m - 1 - i;
+			r[d.r_off + e] = (a0 <= b0) ? B[a0 + (i64)p * b0] : 0.0;
+		}
+		for (i64 e = tid; e < (i64)k * n; e += RQ_THREADS)
+		{
+			const i64 j = e / n, i = e % n;
+			q[d.q_off + e] = Q[(n - 1 - i) + (i64)p * (k - 1 - j)];
+		}
 	}
 }
 

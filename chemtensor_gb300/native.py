@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libctgpu.so")
 # exported C symbols (include/ctgpu.h)
 EXPORTS = [
     "dmrg_twosite",
+    "dmrg_singlesite",
     "ctgpu_set_precision",
     "ctgpu_set_device",
     "ctgpu_get_last_stats",
@@ -33,6 +34,8 @@ EXPORTS = [
     "ctgpu_contraction_operator_step_left",
     "ctgpu_contraction_operator_step_right",
     "ctgpu_block_sparse_tensor_svd_values",
+    "ctgpu_block_sparse_tensor_qr",
+    "ctgpu_block_sparse_tensor_rq",
     "ctgpu_delete_block_sparse_tensor",
     "ctgpu_set_profiling",
     "ctgpu_set_l2_flush_bytes",
@@ -68,6 +71,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     P = C.c_void_p
     lib.dmrg_twosite.argtypes = [P, C.c_int, C.c_int, C.c_double, C.c_int64, P, P, P]
     lib.dmrg_twosite.restype = C.c_int
+    lib.dmrg_singlesite.argtypes = [P, C.c_int, C.c_int, P, P]
+    lib.dmrg_singlesite.restype = C.c_int
     lib.ctgpu_set_precision.argtypes = [C.c_int]
     lib.ctgpu_set_device.argtypes = [C.c_int]
     lib.ctgpu_get_last_stats.argtypes = [P]
@@ -83,6 +88,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_contraction_operator_step_left.argtypes = [P] * 4
     lib.ctgpu_contraction_operator_step_right.argtypes = [P] * 4
     lib.ctgpu_block_sparse_tensor_svd_values.argtypes = [P, P, P]
+    lib.ctgpu_block_sparse_tensor_qr.argtypes = [P, C.c_int, P, P]
+    lib.ctgpu_block_sparse_tensor_rq.argtypes = [P, C.c_int, P, P]
     lib.ctgpu_delete_block_sparse_tensor.argtypes = [P]
     lib.ctgpu_delete_block_sparse_tensor.restype = None
     lib.ctgpu_set_profiling.argtypes = [C.c_int, C.c_int]
@@ -156,3 +163,10 @@ def dmrg_twosite(mpo: cs.MPO, psi: cs.MPS, num_sweeps: int, maxiter_lanczos: int
     ret = lib().dmrg_twosite(C.byref(mpo), num_sweeps, maxiter_lanczos, tol_split, max_vdim, C.byref(psi),
                              en.ctypes.data, ent.ctypes.data)
     return ret, en[:num_sweeps], ent[:mpo.nsites - 1]
+
+
+def dmrg_singlesite(mpo: cs.MPO, psi: cs.MPS, num_sweeps: int, maxiter_lanczos: int):
+    """Call the C-ABI dmrg_singlesite; psi is updated in place. Returns (ret, en_sweeps)."""
+    en = np.zeros(max(num_sweeps, 1))
+    ret = lib().dmrg_singlesite(C.byref(mpo), num_sweeps, maxiter_lanczos, C.byref(psi), en.ctypes.data)
+    return ret, en[:num_sweeps]

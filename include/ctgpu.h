@@ -35,6 +35,12 @@ extern "C" {
 int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int maxiter_lanczos,
 	const double tol_split, const ct_long max_vdim, struct mps* psi, double* en_sweeps, double* entropy);
 
+/* Single-site DMRG ground-state search (bond dimensions fixed by the initial psi).
+ * Replaces dmrg_singlesite, src/algorithm/dmrg.c:155-254 (declared in include/algorithm/dmrg.h:10).
+ * Same ownership rules as dmrg_twosite; en_sweeps[num_sweeps] is caller-allocated. Always FP64. */
+int dmrg_singlesite(const struct mpo* hamiltonian, const int num_sweeps, const int maxiter_lanczos,
+	struct mps* psi, double* en_sweeps);
+
 /* Arithmetic of the bulk block GEMMs for subsequent calls from this thread.
  * 0 = FP64 (plain path); 1 = split-BF16 on the tcgen05 tensor cores (each FP64 operand split
  * into a high and a low BF16 part, three products hi*hi + hi*lo + lo*hi, FP32 accumulation,
@@ -148,6 +154,15 @@ int ctgpu_contraction_operator_step_right(const struct block_sparse_tensor* a, c
  * (src/tensor/block_sparse_tensor.c:2686-2848); sigma must hold min(dim0, dim1) entries,
  * *ns receives the count */
 int ctgpu_block_sparse_tensor_svd_values(const struct block_sparse_tensor* a, double* sigma, ct_long* ns);
+
+/* block_sparse_tensor_qr / block_sparse_tensor_rq (src/tensor/block_sparse_tensor.c:2402-2540 /
+ * :2544-2676), mode QR_REDUCED (= 0) only; blocks factored with the conventions of LAPACK
+ * dgeqrf + dorgqr and dgerqf + dorgrq (dense_tensor.c:2253-2651 / :2680-2880). Other modes
+ * return -5. */
+int ctgpu_block_sparse_tensor_qr(const struct block_sparse_tensor* a, int mode, struct block_sparse_tensor* q,
+	struct block_sparse_tensor* r);
+int ctgpu_block_sparse_tensor_rq(const struct block_sparse_tensor* a, int mode, struct block_sparse_tensor* r,
+	struct block_sparse_tensor* q);
 
 /* release a tensor returned by one of the calls above (free() on every array) */
 void ctgpu_delete_block_sparse_tensor(struct block_sparse_tensor* t);

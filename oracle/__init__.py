@@ -42,7 +42,10 @@ def port() -> C.CDLL:
         lib = C.CDLL(PORT)
         P = C.c_void_p
         lib.oracle_dmrg_twosite.argtypes = [P, C.c_int, C.c_int, C.c_double, C.c_int64, P, P, P]
+        lib.oracle_dmrg_singlesite.argtypes = [P, C.c_int, C.c_int, P, P]
         lib.oracle_apply_local_hamiltonian.argtypes = [P] * 5
+        lib.oracle_block_sparse_tensor_qr.argtypes = [P, P, P]
+        lib.oracle_block_sparse_tensor_rq.argtypes = [P, P, P]
         lib.oracle_block_sparse_tensor_dot.argtypes = [P, C.c_int, P, C.c_int, C.c_int, P]
         lib.oracle_block_sparse_tensor_transpose.argtypes = [P, P, P]
         lib.oracle_block_sparse_tensor_svd.argtypes = [P, P, P, P, P]

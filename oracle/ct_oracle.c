@@ -34,6 +34,10 @@ void   scipy_dgerqf_(const int* m, const int* n, double* a, const int* lda, doub
                      const int* lwork, int* info);
 void   scipy_dorgrq_(const int* m, const int* n, const int* k, double* a, const int* lda, const double* tau,
                      double* work, const int* lwork, int* info);
+void   scipy_dgeqrf_(const int* m, const int* n, double* a, const int* lda, double* tau, double* work,
+                     const int* lwork, int* info);
+void   scipy_dorgqr_(const int* m, const int* n, const int* k, double* a, const int* lda, const double* tau,
+                     double* work, const int* lwork, int* info);
 void   scipy_dsteqr_(const char* compz, const int* n, double* d, double* e, double* z, const int* ldz, double* work,
                      int* info, size_t);
 void   scipy_openblas_set_num_threads(int);
@@ -640,6 +644,49 @@ static int dense_rq(const struct dense_tensor* a, struct dense_tensor* r, struct
 	return 0;
 }
 
+/* dense_tensor_qr_fill (dense_tensor.c:2253-2651), QR_REDUCED, real double case */
+static int dense_qr(const struct dense_tensor* a, struct dense_tensor* q, struct dense_tensor* r)
+{
+	const int m = (int)a->dim[0], n = (int)a->dim[1];
+	const int k = m < n ? m : n;
+	const int l = k;
+	double* tau = xmalloc(k * sizeof(double));
+	double* t = xcalloc((size_t)m * n, sizeof(double));
+	const double* ad = a->data;
+	for (int i = 0; i < m; i++)
+		for (int j = 0; j < n; j++) t[i + (size_t)m * j] = ad[(size_t)i * n + j];
+	int info, lwork = -1;
+	double wsz;
+	scipy_dgeqrf_(&m, &n, NULL, &m, NULL, &wsz, &lwork, &info);
+	if (info != 0) { free(t); free(tau); return -1; }
+	lwork = (int)wsz;
+	double* work = xmalloc((size_t)lwork * sizeof(double));
+	scipy_dgeqrf_(&m, &n, t, &m, tau, work, &lwork, &info);
+	free(work);
+	if (info != 0) { free(t); free(tau); return -1; }
+	double* rd = r->data;
+	for (int i = 0; i < l; i++)
+	{
+		const int numzero = i < n ? i : n;
+		for (int j = 0; j < numzero; j++) rd[(size_t)i * n + j] = 0;
+		for (int j = numzero; j < n; j++) rd[(size_t)i * n + j] = t[i + (size_t)m * j];
+	}
+	lwork = -1;
+	scipy_dorgqr_(&m, &l, &k, NULL, &m, NULL, &wsz, &lwork, &info);
+	if (info != 0) { free(t); free(tau); return -2; }
+	lwork = (int)wsz;
+	work = xmalloc((size_t)lwork * sizeof(double));
+	scipy_dorgqr_(&m, &l, &k, t, &m, tau, work, &lwork, &info);
+	free(work);
+	if (info != 0) { free(t); free(tau); return -2; }
+	double* qd = q->data;
+	for (int i = 0; i < m; i++)
+		for (int j = 0; j < l; j++) qd[(size_t)i * l + j] = t[i + (size_t)m * j];
+	free(t);
+	free(tau);
+	return 0;
+}
+
 /* block_sparse_tensor_svd (block_sparse_tensor.c:2686-2848) */
 int oracle_block_sparse_tensor_svd(const struct block_sparse_tensor* a, struct block_sparse_tensor* u, double** s_out,
                                    ct_long* ns, struct block_sparse_tensor* vh)
@@ -751,6 +798,71 @@ static int bst_rq(const struct block_sparse_tensor* a, struct block_sparse_tenso
 			if (dense_rq(ba, br, bq) != 0) failed = 1;
 		}
 	return failed ? -1 : 0;
+}
+
+/* block_sparse_tensor_qr (block_sparse_tensor.c:2402-2540), QR_REDUCED */
+static int bst_qr(const struct block_sparse_tensor* a, struct block_sparse_tensor* q, struct block_sparse_tensor* r)
+{
+	assert(a->ndim == 2);
+	ct_long dim_interm = 0;
+	qnumber* qi = xcalloc(a->dim_logical[0] + 1, sizeof(qnumber));
+	for (ct_long j = 0; j < a->dim_blocks[1]; j++)
+		for (ct_long i = 0; i < a->dim_blocks[0]; i++)
+		{
+			if (a->axis_dir[0] * a->qnums_blocks[0][i] + a->axis_dir[1] * a->qnums_blocks[1][j] != 0) continue;
+			const struct dense_tensor* b = a->blocks[i * a->dim_blocks[1] + j];
+			const ct_long k = b->dim[0] < b->dim[1] ? b->dim[0] : b->dim[1];
+			for (ct_long l = 0; l < k; l++) qi[dim_interm + l] = a->qnums_blocks[1][j];
+			dim_interm += k;
+		}
+	int dummy = 0;
+	if (dim_interm == 0)
+	{
+		dummy = 1;
+		dim_interm = 1;
+		qi[0] = -a->axis_dir[0] * a->axis_dir[1] * a->qnums_blocks[0][0];
+	}
+	const ct_long dim_q[2] = { a->dim_logical[0], dim_interm };
+	const qnumber* qq[2] = { a->qnums_logical[0], qi };
+	bst_alloc(2, dim_q, a->axis_dir, qq, q);
+	const ct_long dim_r[2] = { dim_interm, a->dim_logical[1] };
+	const enum tensor_axis_direction dr[2] = { -a->axis_dir[1], a->axis_dir[1] };
+	const qnumber* qr_[2] = { qi, a->qnums_logical[1] };
+	bst_alloc(2, dim_r, dr, qr_, r);
+	free(qi);
+	if (dummy)
+	{
+		const qnumber q0 = a->qnums_blocks[0][0];
+		const qnumber q1 = -a->axis_dir[0] * a->axis_dir[1] * q0;
+		const ct_long j1 = block_index_of(q, 1, q1);
+		((double*)q->blocks[0 * q->dim_blocks[1] + j1]->data)[0] = 1.0;
+		return 0;
+	}
+	int failed = 0;
+	#pragma omp parallel for schedule(dynamic) collapse(2)
+	for (ct_long i = 0; i < a->dim_blocks[0]; i++)
+		for (ct_long j = 0; j < a->dim_blocks[1]; j++)
+		{
+			const struct dense_tensor* ba = a->blocks[i * a->dim_blocks[1] + j];
+			if (!ba) continue;
+			const ct_long kb = block_index_of(q, 1, a->qnums_blocks[1][j]);
+			struct dense_tensor* bq = q->blocks[i * q->dim_blocks[1] + kb];
+			struct dense_tensor* br = r->blocks[kb * r->dim_blocks[1] + j];
+			if (dense_qr(ba, bq, br) != 0) failed = 1;
+		}
+	return failed ? -1 : 0;
+}
+
+int oracle_block_sparse_tensor_qr(const struct block_sparse_tensor* a, struct block_sparse_tensor* q,
+                                  struct block_sparse_tensor* r)
+{
+	return bst_qr(a, q, r);
+}
+
+int oracle_block_sparse_tensor_rq(const struct block_sparse_tensor* a, struct block_sparse_tensor* r,
+                                  struct block_sparse_tensor* q)
+{
+	return bst_rq(a, r, q);
 }
 
 /* ---- truncation: retained_bond_indices (truncation.c:110-223), von_neumann_entropy (:13-31) ---- */
@@ -925,6 +1037,32 @@ static int local_orthonormalize_rq(struct block_sparse_tensor* a, struct block_s
 	oracle_block_sparse_tensor_dot(a_prev, AXR_TRAILING, &r, AXR_LEADING, 1, &upd);
 	oracle_delete_block_sparse_tensor(a_prev);
 	*a_prev = upd;
+	oracle_delete_block_sparse_tensor(&r);
+	return ret;
+}
+
+/* mps_local_orthonormalize_qr (mps.c:513-553) */
+static int local_orthonormalize_qr(struct block_sparse_tensor* a, struct block_sparse_tensor* a_next)
+{
+	const ct_long dl[2] = { a->dim_logical[0], a->dim_logical[1] };
+	qnumber* ql[2];
+	for (int i = 0; i < 2; i++) {
+		ql[i] = xmalloc(dl[i] * sizeof(qnumber));
+		memcpy(ql[i], a->qnums_logical[i], dl[i] * sizeof(qnumber));
+	}
+	const enum tensor_axis_direction adl[2] = { TENSOR_AXIS_OUT, TENSOR_AXIS_OUT };
+	struct block_sparse_tensor am, q, r, upd;
+	bst_flatten(a, 0, TENSOR_AXIS_OUT, &am);
+	oracle_delete_block_sparse_tensor(a);
+	int ret = bst_qr(&am, &q, &r);
+	oracle_delete_block_sparse_tensor(&am);
+	bst_split(&q, 0, dl, adl, (const qnumber* const*)ql, a);
+	oracle_delete_block_sparse_tensor(&q);
+	free(ql[0]);
+	free(ql[1]);
+	oracle_block_sparse_tensor_dot(&r, AXR_TRAILING, a_next, AXR_LEADING, 1, &upd);
+	oracle_delete_block_sparse_tensor(a_next);
+	*a_next = upd;
 	oracle_delete_block_sparse_tensor(&r);
 	return ret;
 }
@@ -1300,6 +1438,68 @@ int oracle_dmrg_twosite(const struct mpo* ham, int num_sweeps, int maxiter, doub
 
 	for (int i = 0; i < L - 1; i++) oracle_delete_block_sparse_tensor(&h2[i]);
 	free(h2);
+	for (int i = 0; i < L; i++) { oracle_delete_block_sparse_tensor(&rb[i]); oracle_delete_block_sparse_tensor(&lb[i]); }
+	free(rb);
+	free(lb);
+	return ret;
+}
+
+/* ---- dmrg_singlesite (dmrg.c:155-254) ---- */
+
+int oracle_dmrg_singlesite(const struct mpo* ham, int num_sweeps, int maxiter, struct mps* psi, double* en_sweeps)
+{
+	const int L = ham->nsites;
+	assert(L == psi->nsites && L >= 1);
+	scipy_openblas_set_num_threads(1);
+	int err = 0;
+	double nrm = orthonormalize_right(psi, &err);
+	if (err < 0) return err;
+	if (nrm == 0) printf("Warning: in 'dmrg_singlesite': initial MPS has norm zero (possibly due to mismatching quantum numbers)\n");
+
+	struct block_sparse_tensor* lb = xcalloc(L, sizeof(*lb));
+	struct block_sparse_tensor* rb = xcalloc(L, sizeof(*rb));
+	dummy_block(psi->a[L - 1].qnums_logical[2], ham->a[L - 1].qnums_logical[3], psi->a[L - 1].qnums_logical[2], 1, &rb[L - 1]);
+	for (int i = L - 1; i > 0; i--)
+		oracle_contraction_operator_step_right(&psi->a[i], &psi->a[i], &ham->a[i], &rb[i], &rb[i - 1]);
+	dummy_block(psi->a[0].qnums_logical[0], ham->a[0].qnums_logical[0], psi->a[0].qnums_logical[0], 0, &lb[0]);
+	for (int i = 1; i < L; i++) bst_copy(&lb[0], &lb[i]);
+
+	int ret = 0;
+	g_num_sweep_times = 0;
+	for (int n = 0; n < num_sweeps && ret == 0; n++)
+	{
+		const double t_sweep = wall_seconds();
+		double en = 0;
+		for (int i = 0; i < L - 1 && ret == 0; i++)
+		{
+			struct block_sparse_tensor opt;
+			ret = minimize_local_energy(&ham->a[i], &lb[i], &rb[i], &psi->a[i], maxiter, &en, &opt);
+			if (ret < 0) break;
+			oracle_delete_block_sparse_tensor(&psi->a[i]);
+			psi->a[i] = opt;
+			if (local_orthonormalize_qr(&psi->a[i], &psi->a[i + 1]) < 0) ret = -1;
+			oracle_delete_block_sparse_tensor(&lb[i + 1]);
+			oracle_contraction_operator_step_left(&psi->a[i], &psi->a[i], &ham->a[i], &lb[i], &lb[i + 1]);
+		}
+		for (int i = L - 1; i > 0 && ret == 0; i--)
+		{
+			struct block_sparse_tensor opt;
+			ret = minimize_local_energy(&ham->a[i], &lb[i], &rb[i], &psi->a[i], maxiter, &en, &opt);
+			if (ret < 0) break;
+			oracle_delete_block_sparse_tensor(&psi->a[i]);
+			psi->a[i] = opt;
+			if (local_orthonormalize_rq(&psi->a[i], &psi->a[i - 1]) < 0) ret = -1;
+			oracle_delete_block_sparse_tensor(&rb[i - 1]);
+			oracle_contraction_operator_step_right(&psi->a[i], &psi->a[i], &ham->a[i], &rb[i], &rb[i - 1]);
+		}
+		if (ret < 0) break;
+		struct block_sparse_tensor t;
+		make_head(&psi->a[0], &t);
+		if (local_orthonormalize_rq(&psi->a[0], &t) < 0) ret = -1;
+		oracle_delete_block_sparse_tensor(&t);
+		en_sweeps[n] = en;
+		if (g_num_sweep_times < MAX_SWEEP_TIMES) g_sweep_times[g_num_sweep_times++] = wall_seconds() - t_sweep;
+	}
 	for (int i = 0; i < L; i++) { oracle_delete_block_sparse_tensor(&rb[i]); oracle_delete_block_sparse_tensor(&lb[i]); }
 	free(rb);
 	free(lb);

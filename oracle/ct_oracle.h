@@ -1,4 +1,4 @@
-/* ct_oracle.h - CPU restatement of chemtensor's two-site DMRG path.
+/* ct_oracle.h - CPU restatement of chemtensor's DMRG path (two-site and single-site).
  *
  * TEST INFRASTRUCTURE ONLY. This library is the parity checker for the GB300
  * implementation and the timed CPU baseline; nothing in the product links or
@@ -23,6 +23,10 @@ extern "C" {
 int oracle_dmrg_twosite(const struct mpo* hamiltonian, int num_sweeps, int maxiter_lanczos, double tol_split,
 	ct_long max_vdim, struct mps* psi, double* en_sweeps, double* entropy);
 
+/* dmrg_singlesite (src/algorithm/dmrg.c:155-254); same arguments and return codes */
+int oracle_dmrg_singlesite(const struct mpo* hamiltonian, int num_sweeps, int maxiter_lanczos, struct mps* psi,
+	double* en_sweeps);
+
 /* apply_local_hamiltonian (src/algorithm/chain_ops.c:353-390): b = H_loc a, b allocated here */
 void oracle_apply_local_hamiltonian(const struct block_sparse_tensor* a, const struct block_sparse_tensor* w,
 	const struct block_sparse_tensor* l, const struct block_sparse_tensor* r, struct block_sparse_tensor* b);
@@ -38,6 +42,13 @@ void oracle_block_sparse_tensor_transpose(const int* perm, const struct block_sp
  * allocated with aligned_alloc; returns 0 or -1 */
 int oracle_block_sparse_tensor_svd(const struct block_sparse_tensor* a, struct block_sparse_tensor* u,
 	double** s, ct_long* ns, struct block_sparse_tensor* vh);
+
+/* block_sparse_tensor_qr / _rq (src/tensor/block_sparse_tensor.c:2402-2540 / :2544-2676), QR_REDUCED;
+ * factors allocated here; return 0 or -1 */
+int oracle_block_sparse_tensor_qr(const struct block_sparse_tensor* a, struct block_sparse_tensor* q,
+	struct block_sparse_tensor* r);
+int oracle_block_sparse_tensor_rq(const struct block_sparse_tensor* a, struct block_sparse_tensor* r,
+	struct block_sparse_tensor* q);
 
 /* contraction_operator_step_left / _right (src/algorithm/chain_ops.c:196-245 / :116-165) */
 void oracle_contraction_operator_step_left(const struct block_sparse_tensor* a, const struct block_sparse_tensor* b,

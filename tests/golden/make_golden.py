@@ -7,12 +7,15 @@ drives it through ctypes and stores, as .npz:
 * the reference's own inputs: MPOs built by its Hamiltonian assembly code and
   seeded random MPS from construct_random_mps (src/state/mps.c:93);
 * the reference's outputs of dmrg_twosite (src/algorithm/dmrg.c:262): energies
-  per sweep, entanglement entropies and the optimised MPS;
+  per sweep, entanglement entropies and the optimised MPS; and of dmrg_singlesite
+  (src/algorithm/dmrg.c:155): energies per sweep and the optimised MPS;
 * pseudo-random sequences of its PCG32x2 + Box-Muller generator (src/util/rng.c);
 * single-operation pins: apply_local_hamiltonian and the environment updates on
-  one bond (src/algorithm/chain_ops.c).
+  one bond (src/algorithm/chain_ops.c); block_sparse_tensor_qr / _rq on random
+  block-sparse matrices (src/tensor/block_sparse_tensor.c).
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [singlesite|qr]
+(with an argument, only the dmrg_singlesite or the QR / RQ fixtures are written).
 """
 
 import ctypes as C
@@ -29,6 +32,7 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
 ref = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libct_ref.so"))
 ref.dmrg_twosite.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+ref.dmrg_singlesite.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
 ref.ref_heisenberg_mpo.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_void_p]
 ref.ref_hubbard_mpo.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_void_p]
 ref.ref_random_mps.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_void_p]
@@ -37,6 +41,8 @@ ref.ref_local_hamiltonian_setup.argtypes = [C.c_void_p] * 2 + [C.c_int] + [C.c_v
 ref.apply_local_hamiltonian.argtypes = [C.c_void_p] * 5
 ref.contraction_operator_step_left.argtypes = [C.c_void_p] * 5
 ref.contraction_operator_step_right.argtypes = [C.c_void_p] * 5
+ref.block_sparse_tensor_qr.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+ref.block_sparse_tensor_rq.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
 
 HUB_QSITE = [(n << 16) + s for n, s in [(0, 0), (1, -1), (1, 1), (2, 0)]]
 
@@ -78,6 +84,73 @@ def dmrg_case(name, model, L, D, sweeps, maxiter, tol, seed, **kw):
     np.savez_compressed(os.path.join(OUT, name), **arrays)
     print(name, "E =", en[sweeps - 1])
     return H, psi
+
+
+def dmrg1_case(name, model, L, D, sweeps, maxiter, seed, **kw):
+    H = mpo(model, L, **kw)
+    if model == "heisenberg":
+        qsite, sector = [1, -1], 0
+    else:
+        qsite, sector = HUB_QSITE, (L << 16)
+    psi = random_mps(L, qsite, sector, D, seed)
+    arrays = {}
+    arrays.update(cs.chain_to_arrays("H", cs.read_mpo(H)))
+    arrays.update(cs.chain_to_arrays("psi0", cs.read_mps(psi)))
+    en = (C.c_double * sweeps)()
+    ret = ref.dmrg_singlesite(C.byref(H), sweeps, maxiter, C.byref(psi), en)
+    assert ret == 0
+    arrays.update(cs.chain_to_arrays("psi", cs.read_mps(psi)))
+    arrays.update(en_sweeps=np.array(en), params=np.array([L, D, sweeps, maxiter], dtype=np.int64),
+                  seed=np.array(seed), model=np.array(model))
+    np.savez_compressed(os.path.join(OUT, name), **arrays)
+    print(name, "E =", en[sweeps - 1])
+
+
+def singlesite_cases():
+    # dmrg_singlesite end to end (bond dimensions fixed by the start state)
+    dmrg1_case("dmrg1_heisenberg_L12_D16.npz", "heisenberg", 12, 16, 4, 5, 3, Delta=0.7)
+    dmrg1_case("dmrg1_hubbard_L8_D24.npz", "hubbard", 8, 24, 3, 5, 11, u=3.0)
+
+
+def qr_cases():
+    """block_sparse_tensor_qr / _rq (src/tensor/block_sparse_tensor.c:2402-2676), QR_REDUCED, on
+    random block-sparse matrices: tall and wide blocks, a zero column, and a matrix without blocks."""
+    rng = np.random.default_rng(2024)
+    arrays = {}
+    specs = {
+        "m0": ((40, 30), (1, -1), 3),
+        "m1": ((30, 52), (-1, 1), 2),
+        "m2": ((64, 64), (1, 1), 1),
+        "m3": ((17, 9), (1, -1), 4),
+    }
+    for tag, (dims, dirs, qr_) in specs.items():
+        qn = [rng.integers(-qr_, qr_ + 1, size=d).astype(np.int32) for d in dims]
+        t = cs.BlockSparse(dims, dirs, qn)
+        for i, idx in enumerate(t.allowed):
+            b = rng.standard_normal(t.block_shape(idx))
+            if i == 0 and b.shape[1] > 2:
+                b[:, 1] = 0.0
+            t.blocks[idx] = b
+        arrays.update(cs.bst_to_arrays(tag, t))
+    # no allowed blocks: dummy factors
+    t = cs.BlockSparse((5, 6), (1, -1), [np.zeros(5, np.int32), np.ones(6, np.int32)])
+    assert not t.allowed
+    arrays.update(cs.bst_to_arrays("m4", t))
+    for tag in ["m0", "m1", "m2", "m3", "m4"]:
+        a = cs.BlockSparseTensor()
+        cs.write_bst(cs.bst_from_arrays(tag, arrays), a)
+        q, r = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+        assert ref.block_sparse_tensor_qr(C.byref(a), 0, C.byref(q), C.byref(r)) == 0
+        arrays.update(cs.bst_to_arrays(tag + "_qr_q", cs.read_bst(q)))
+        arrays.update(cs.bst_to_arrays(tag + "_qr_r", cs.read_bst(r)))
+        r2, q2 = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+        assert ref.block_sparse_tensor_rq(C.byref(a), 0, C.byref(r2), C.byref(q2)) == 0
+        arrays.update(cs.bst_to_arrays(tag + "_rq_r", cs.read_bst(r2)))
+        arrays.update(cs.bst_to_arrays(tag + "_rq_q", cs.read_bst(q2)))
+        for x in (a, q, r, r2, q2):
+            cs.free_bst(x)
+    np.savez_compressed(os.path.join(OUT, "qr_rq_blocks.npz"), **arrays)
+    print("qr_rq_blocks.npz", len(arrays), "arrays")
 
 
 def local_ops_case(name, model, L, D, seed, ibond, **kw):
@@ -144,4 +217,11 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["singlesite"]:
+        singlesite_cases()
+    elif sys.argv[1:] == ["qr"]:
+        qr_cases()
+    else:
+        main()
+        singlesite_cases()
+        qr_cases()

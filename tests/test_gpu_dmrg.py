@@ -1,4 +1,4 @@
-"""dmrg_twosite on the GPU through the C ABI, against the reference's own results."""
+"""dmrg_twosite and dmrg_singlesite on the GPU through the C ABI, against the reference's own results."""
 
 import ctypes as C
 
@@ -77,3 +77,23 @@ def test_repeated_calls_are_deterministic(gpu):
     a = run_gpu_dmrg(gpu, H, psi0, 2, 5, 1e-10, 32)
     b = run_gpu_dmrg(gpu, H, psi0, 2, 5, 1e-10, 32)
     assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+@pytest.mark.parametrize("case", ["dmrg1_heisenberg_L12_D16.npz", "dmrg1_hubbard_L8_D24.npz"])
+def test_dmrg_singlesite_matches_reference(gpu, oracle_port, case):
+    g = golden(case)
+    L, D, sweeps, maxiter = [int(x) for x in g["params"]]
+    H = cs.chain_from_arrays("H", g)
+    psi0 = cs.chain_from_arrays("psi0", g)
+    cH, cP = cs.make_c_mpo(H), cs.make_c_mps(psi0)
+    en = np.zeros(sweeps)
+    ret = gpu.dmrg_singlesite(C.byref(cH), sweeps, maxiter, C.byref(cP), en.ctypes.data)
+    psi = cs.read_mps(cP)
+    cs.free_mps(cP)
+    cs.free_mpo(cH)
+    assert ret == 0
+    np.testing.assert_allclose(en, g["en_sweeps"], rtol=0, atol=1e-10)
+    ref_psi = cs.chain_from_arrays("psi", g)
+    assert same_structure(psi, ref_psi)
+    assert abs(abs(overlap(oracle_port, psi, ref_psi)) - 1) < 1e-9
+    assert abs(overlap(oracle_port, psi, psi) - 1) < 1e-12

@@ -167,3 +167,25 @@ def test_svd_values_rank_deficient_blocks(gpu, oracle_port, rank, noise):
     oracle_port.oracle_delete_block_sparse_tensor(C.byref(u))
     oracle_port.oracle_delete_block_sparse_tensor(C.byref(vh))
     cs.free_bst(ca)
+
+
+@pytest.mark.parametrize("tag", ["m0", "m1", "m2", "m3", "m4"])
+def test_qr_rq_match_reference(gpu, tag):
+    """Householder QR / RQ kernel against the reference's LAPACK factors (same sign conventions:
+    the factors agree entry by entry, not only up to the gauge of the connecting axis)."""
+    g = golden("qr_rq_blocks.npz")
+    a = c_bst(cs.bst_from_arrays(tag, g))
+    q, r = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+    assert gpu.ctgpu_block_sparse_tensor_qr(C.byref(a), 0, C.byref(q), C.byref(r)) == 0
+    assert_bst_close(cs.read_bst(q), cs.bst_from_arrays(tag + "_qr_q", g), 1e-12)
+    assert_bst_close(cs.read_bst(r), cs.bst_from_arrays(tag + "_qr_r", g), 1e-12)
+    r2, q2 = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+    assert gpu.ctgpu_block_sparse_tensor_rq(C.byref(a), 0, C.byref(r2), C.byref(q2)) == 0
+    assert_bst_close(cs.read_bst(r2), cs.bst_from_arrays(tag + "_rq_r", g), 1e-12)
+    assert_bst_close(cs.read_bst(q2), cs.bst_from_arrays(tag + "_rq_q", g), 1e-12)
+    for x in (q, r, r2, q2):
+        cs.free_bst(x)
+    # QR_COMPLETE is not provided: an error code, not a silent reduced factorisation
+    q3, r3 = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+    assert gpu.ctgpu_block_sparse_tensor_qr(C.byref(a), 1, C.byref(q3), C.byref(r3)) == -5
+    cs.free_bst(a)

@@ -85,3 +85,44 @@ def test_oracle_lanczos_exact_in_full_krylov_space(oracle_port):
     w = np.linalg.eigvalsh(h)
     assert abs(lam.value - w[0]) < 1e-10
     assert np.linalg.norm(h @ u - lam.value * u) < 1e-8
+
+
+QR_TAGS = ["m0", "m1", "m2", "m3", "m4"]
+
+
+@pytest.mark.parametrize("tag", QR_TAGS)
+def test_oracle_qr_rq_match_reference(oracle_port, tag):
+    """block_sparse_tensor_qr / _rq restated (dgeqrf / dgerqf per block) against the reference's factors."""
+    g = golden("qr_rq_blocks.npz")
+    a = c_bst(cs.bst_from_arrays(tag, g))
+    q, r = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+    assert oracle_port.oracle_block_sparse_tensor_qr(C.byref(a), C.byref(q), C.byref(r)) == 0
+    assert_bst_close(cs.read_bst(q), cs.bst_from_arrays(tag + "_qr_q", g), 1e-13)
+    assert_bst_close(cs.read_bst(r), cs.bst_from_arrays(tag + "_qr_r", g), 1e-13)
+    r2, q2 = cs.BlockSparseTensor(), cs.BlockSparseTensor()
+    assert oracle_port.oracle_block_sparse_tensor_rq(C.byref(a), C.byref(r2), C.byref(q2)) == 0
+    assert_bst_close(cs.read_bst(r2), cs.bst_from_arrays(tag + "_rq_r", g), 1e-13)
+    assert_bst_close(cs.read_bst(q2), cs.bst_from_arrays(tag + "_rq_q", g), 1e-13)
+    for x in (q, r, r2, q2):
+        oracle_port.oracle_delete_block_sparse_tensor(C.byref(x))
+    cs.free_bst(a)
+
+
+@pytest.mark.parametrize("case", ["dmrg1_heisenberg_L12_D16.npz", "dmrg1_hubbard_L8_D24.npz"])
+def test_oracle_dmrg_singlesite_matches_reference(oracle_port, case):
+    g = golden(case)
+    L, D, sweeps, maxiter = [int(x) for x in g["params"]]
+    H = cs.chain_from_arrays("H", g)
+    psi0 = cs.chain_from_arrays("psi0", g)
+    cH, cP = cs.make_c_mpo(H), cs.make_c_mps(psi0)
+    en = np.zeros(sweeps)
+    ret = oracle_port.oracle_dmrg_singlesite(C.byref(cH), sweeps, maxiter, C.byref(cP), en.ctypes.data)
+    psi = cs.read_mps(cP)
+    cs.free_mps(cP)
+    cs.free_mpo(cH)
+    assert ret == 0
+    np.testing.assert_allclose(en, g["en_sweeps"], rtol=0, atol=1e-12)
+    ref_psi = cs.chain_from_arrays("psi", g)
+    assert same_structure(psi, ref_psi)
+    assert abs(abs(overlap(oracle_port, psi, ref_psi)) - 1) < 1e-10
+    assert abs(overlap(oracle_port, psi, psi) - 1) < 1e-12
