@@ -396,6 +396,73 @@ def bench_serve(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def bench_molecular(args, world, rank, local):
+    """Molecular workload: spin-orbital Hamiltonian of n spatial orbitals with the synthetic integrals
+    of workloads.molecular_integrals (seed 7), (N, 2Sz) = (n, 0), bond dimension D, seeded random
+    start state (seed 42), 5 Lanczos iterations, tol 1e-10. The same start state is run once in
+    plain FP64 and once in split-BF16 with the final sweep in FP64; both report device time per
+    sweep (CUDA events) and the energies, and the line gives the speed-up and |dE| between them."""
+    from chemtensor_gb300 import ctstructs as cs, hamiltonians as hm, native, workloads as wl
+    lib = native.lib()
+    lib.ctgpu_set_device(local)
+    n, D, S = args.orbitals, args.mol_vdim, args.mol_sweeps
+    tk, vi = wl.molecular_integrals(n, seed=7)
+    t0 = time.perf_counter()
+    H = hm.spin_molecular(tk, vi)
+    t_mpo = time.perf_counter() - t0
+    c = native.random_mps(n, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(n, 0), D, 42)
+    psi0 = cs.read_mps(c)
+    cs.free_mps(c)
+    cH = cs.make_c_mpo(H)
+    runs = {}
+    for name in args.mol_precisions.split(","):
+        # "bf16x3env": split-BF16 also in the environment updates of the reduced-precision sweeps
+        native.set_precision(PRECISIONS[name.replace("env", "")])
+        lib.ctgpu_set_reduced_environments(1 if name.endswith("env") else 0)
+        lib.ctgpu_clear_plan_cache()
+        lib.ctgpu_set_profiling(1 if args.mol_profile else 0, 0)
+        cP = cs.make_c_mps(psi0)
+        en, ent = np.zeros(S), np.zeros(n - 1)
+        t0 = time.perf_counter()
+        with ClockSampler(local) as clk:
+            ret = lib.dmrg_twosite(C.byref(cH), S, 5, 1e-10, D, C.byref(cP), en.ctypes.data, ent.ctypes.data)
+        wall = time.perf_counter() - t0
+        if ret != 0:
+            raise RuntimeError(f"dmrg_twosite failed: {ret} {native.last_error()}")
+        ms, la = native.sweep_times()
+        st = native.last_stats()
+        runs[name] = {"sweep_ms": [float(x) for x in ms], "energies": en.tolist(), "wall_s": wall,
+                      "max_bond_dim": st["max_bond_dim"], "matvec_tflops": st["matvec_flops"] / max(st["lanczos_ms"], 1e-9) / 1e9,
+                      "lanczos_ms_per_sweep": st["lanczos_ms"] / S, "split_ms_per_sweep": st["split_ms"] / S,
+                      "env_ms_per_sweep": st["env_ms"] / S, "host_plan_s": st["host_plan_s"], "clocks": clk.summary()}
+        if args.mol_profile:
+            runs[name]["kernel_ms_per_sweep"] = {k: v["ms"] / S for k, v in native.kernel_profile().items()}
+        cs.free_mps(cP)
+        lib.ctgpu_set_profiling(0, 0)
+    native.set_precision(0)
+    lib.ctgpu_set_reduced_environments(0)
+    cs.free_mpo(cH)
+    line = {"metric": f"two-site DMRG sweep time (spin-orbital molecular Hamiltonian n={n}, D={D})",
+            "unit": "ms/sweep", "higher_is_better": False, "n_gpus": 1, "steps": S, "warmup": 0,
+            "data": "synthetic (seeded integrals and start state)",
+            "config": {"workload": f"spin molecular n={n} (N,2Sz)=({n},0) D={D} maxiter=5 tol=1e-10 "
+                                   f"integrals seed=7 start seed=42", "mpo_bond_dims_max": max(
+                                       t.dim_logical[0] for t in H.tensors), "mpo_build_s": t_mpo},
+            "runs": runs}
+    mixed = [k for k in ("bf16x3env", "bf16x3") if k in runs]
+    if "fp64" in runs and mixed:
+        a, b = runs["fp64"], runs[mixed[0]]
+        line["mixed_run"] = mixed[0]
+        # the split-BF16 run's last sweep is FP64: compare the mean of the bulk sweeps after the first
+        bulk = lambda r, k: float(np.mean(r["sweep_ms"][1:k])) if k > 1 else float(r["sweep_ms"][0])
+        line["value"] = bulk(b, S - 1)
+        line["speedup_bulk_sweeps_bf16x3_vs_fp64"] = bulk(a, S - 1) / bulk(b, S - 1)
+        line["speedup_total_vs_fp64"] = sum(a["sweep_ms"]) / sum(b["sweep_ms"])
+        line["abs_dE_final"] = abs(a["energies"][-1] - b["energies"][-1])
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def sweeps_only(args, local):
     """One dmrg_twosite call of warmup + steps sweeps on the workload (profiler target)."""
     from chemtensor_gb300 import ctstructs as cs, native
@@ -426,10 +493,16 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=sorted(PRECISIONS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--matvecs", type=int, default=1000, help="local-H applications timed in --mode localh")
-    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh", "serve"],
+    ap.add_argument("--orbitals", type=int, default=24, help="spatial orbitals of --mode molecular")
+    ap.add_argument("--mol-vdim", type=int, default=512, help="bond dimension of --mode molecular")
+    ap.add_argument("--mol-sweeps", type=int, default=10, help="sweeps of --mode molecular")
+    ap.add_argument("--mol-precisions", default="fp64,bf16x3", help="runs of --mode molecular")
+    ap.add_argument("--mol-profile", action="store_true", help="time every launch by kernel class in --mode molecular")
+    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh", "serve", "molecular"],
                     help="sweeps: only one device call of warmup+steps sweeps (for profiler captures), no JSON line; "
                          "localh: local-Hamiltonian microbenchmark (synthetic D=1024), its own JSON line; "
-                         "serve: request stream of small and medium solves, serial vs concurrent solver threads")
+                         "serve: request stream of small and medium solves, serial vs concurrent solver threads; "
+                         "molecular: spin-orbital molecular Hamiltonian (n=24, D=512), FP64 vs split-BF16")
     ap.add_argument("--requests", type=int, default=128, help="requests of the --mode serve stream")
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate (1/s) of --mode serve")
     ap.add_argument("--workers", type=int, default=4, help="solver threads of --mode serve")
@@ -443,6 +516,9 @@ def main():
         return
     if args.mode == "serve":
         bench_serve(args, world, rank, local)
+        return
+    if args.mode == "molecular":
+        bench_molecular(args, world, rank, local)
         return
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

@@ -60,6 +60,13 @@ int dmrg_singlesite(const struct mpo* hamiltonian, const int num_sweeps, const i
 	});
 }
 
+int ctgpu_set_reduced_environments(int on)
+{
+	const int prev = g_opts.reduced_env ? 1 : 0;
+	g_opts.reduced_env = on != 0;
+	return prev;
+}
+
 int ctgpu_set_precision(int precision)
 {
 	if (precision != ctg::GEMM_FP64 && precision != ctg::GEMM_BF16X3) return ERR_RUNTIME;
@@ -228,6 +235,11 @@ int ctgpu_block_sparse_tensor_svd_values(const struct block_sparse_tensor* a, do
 		*ns = sv.ns;
 		return 0;
 	});
+}
+
+int ctgpu_construct_spin_molecular_mpo(int nsites, const double* tkin, const double* vint, struct mpo* out)
+{
+	return guarded([&] { return ctg::build_spin_molecular_mpo(nsites, tkin, vint, out); });
 }
 
 int ctgpu_block_sparse_tensor_qr(const struct block_sparse_tensor* a, int mode, struct block_sparse_tensor* q,

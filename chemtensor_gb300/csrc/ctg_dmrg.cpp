@@ -371,37 +371,25 @@ int split_mps_svd(Ctx& c, const DTensor& a, i64 d, const std::vector<q32>& qsite
 
 struct LocalH {
 	DotPlan d1, d2, d3;
-	CopyPlan t0, t1;
 	DTensor k;                       // transpose(l, {0,3,1,2}), computed once per bond
 	DTensor w, r;
-	DBufPtr s1, tt1, s2, tt2;
+	DBufPtr tt1, tt2;                // the two intermediates, in their transposed layouts
 	DBufPtr pk_r, pk_w, pk_k, pk_x, pk_t1, pk_t2;   // packed tensor-core operands
 	bool tc = false;
-	bool fused = false;          // transposes written by the GEMM epilogues (FP64)
 	double flops = 0;
 
 	LocalH(Ctx& c, const Meta& a, const DTensor& w_, const DTensor& l, const DTensor& r_, int precision) : w(w_), r(r_)
 	{
+		// the reference's transposes {1,2,0,3,4} and {2,0,1,3,4} of the first two products are written
+		// by the GEMM epilogues (the results land in the transposed layouts), in FP64 and on the tensor
+		// cores alike; no separate transpose pass
 		const int p0[5] = {1, 2, 0, 3, 4};
 		const int p1[5] = {2, 0, 1, 3, 4};
 		const int p2[4] = {0, 3, 1, 2};
-		// FP64: the two transposes are written by the GEMM epilogues (results land in the transposed
-		// layouts); the tensor-core path keeps them as separate passes
-		fused = precision == GEMM_FP64;
-		if (fused)
-		{
-			d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1, precision, p0);
-			d2 = make_dot_plan(c, w.m(), AX_TRAILING, *d1.out, AX_LEADING, 2, precision, p1);
-		}
-		else
-		{
-			d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1, precision);
-			t0 = make_transpose_plan(c, *d1.out, p0);
-			d2 = make_dot_plan(c, w.m(), AX_TRAILING, *t0.out, AX_LEADING, 2, precision);
-			t1 = make_transpose_plan(c, *d2.out, p1);
-		}
+		d1 = make_dot_plan(c, a, AX_TRAILING, r.m(), AX_LEADING, 1, precision, p0);
+		d2 = make_dot_plan(c, w.m(), AX_TRAILING, *d1.out, AX_LEADING, 2, precision, p1);
 		k = op_transpose(c, l, p2);
-		d3 = make_dot_plan(c, k.m(), AX_TRAILING, fused ? *d2.out : *t1.out, AX_LEADING, 2, precision);
+		d3 = make_dot_plan(c, k.m(), AX_TRAILING, *d2.out, AX_LEADING, 2, precision);
 		// the cyclic partial trace of the unit outer bonds keeps blocks and entries (view_trace_unit):
 		// with outer axes of dimension 1, equal quantum numbers and opposite directions, the inner
 		// axes obey the conservation law of a, so equal inner axes mean an equal block structure
@@ -413,18 +401,8 @@ struct LocalH {
 			same = o.dim[(size_t)i + 1] == a.dim[(size_t)i] && o.dir[(size_t)i + 1] == a.dir[(size_t)i] &&
 			       o.ql[(size_t)i + 1] == a.ql[(size_t)i];
 		CTG_CHECK(same, "local Hamiltonian output structure differs from the input");
-		if (fused)
-		{
-			tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
-			tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
-		}
-		else
-		{
-			s1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
-			tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t0.out->nnz, 1) * sizeof(double));
-			s2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
-			tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(t1.out->nnz, 1) * sizeof(double));
-		}
+		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
+		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
 		flops = d1.flops + d2.flops + d3.flops;
 		if (precision == GEMM_BF16X3)
 		{
@@ -445,31 +423,22 @@ struct LocalH {
 
 	void apply(Ctx& c, const double* x, double* y) const
 	{
+		double* t1 = (double*)tt1->ptr;
+		double* t2 = (double*)tt2->ptr;
 		if (tc)
 		{
 			d1.pack_a(c, x, pk_x->ptr);
-			d1.run_packed(c, pk_x->ptr, pk_r->ptr, (double*)s1->ptr);
-			t0.run(c, (const double*)s1->ptr, (double*)tt1->ptr);
-			d2.pack_b(c, (const double*)tt1->ptr, pk_t1->ptr);
-			d2.run_packed(c, pk_w->ptr, pk_t1->ptr, (double*)s2->ptr);
-			t1.run(c, (const double*)s2->ptr, (double*)tt2->ptr);
-			d3.pack_b(c, (const double*)tt2->ptr, pk_t2->ptr);
+			d1.run_packed(c, pk_x->ptr, pk_r->ptr, t1);
+			d2.pack_b(c, t1, pk_t1->ptr);
+			d2.run_packed(c, pk_w->ptr, pk_t1->ptr, t2);
+			d3.pack_b(c, t2, pk_t2->ptr);
 			d3.run_packed(c, pk_k->ptr, pk_t2->ptr, y);
 			c.gemm_flops += flops;
 			return;
 		}
-		if (fused)
-		{
-			d1.run(c, x, r.data(), (double*)tt1->ptr);
-			d2.run(c, w.data(), (const double*)tt1->ptr, (double*)tt2->ptr);
-			d3.run(c, k.data(), (const double*)tt2->ptr, y);
-			return;
-		}
-		d1.run(c, x, r.data(), (double*)s1->ptr);
-		t0.run(c, (const double*)s1->ptr, (double*)tt1->ptr);
-		d2.run(c, w.data(), (const double*)tt1->ptr, (double*)s2->ptr);
-		t1.run(c, (const double*)s2->ptr, (double*)tt2->ptr);
-		d3.run(c, k.data(), (const double*)tt2->ptr, y);
+		d1.run(c, x, r.data(), t1);
+		d2.run(c, w.data(), t1, t2);
+		d3.run(c, k.data(), t2, y);
 	}
 };
 
@@ -669,13 +638,15 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		if (h_sc->status != 0) return h_sc->status;
 		CTG_CUDA(cudaEventRecord(ev[2], c.stream()));
 		const double h2 = now_s();
-		// environments stay FP64 in every sweep: each one is built from its neighbour, so
-		// rounding errors of a reduced-precision product would accumulate along the chain
-		if (left_to_right) lb[i + 1] = contraction_step_left(c, A[i], W[i], lb[i], GEMM_FP64);
+		// environments stay FP64 unless reduced_env is set: each one is built from its neighbour, so
+		// rounding errors of a reduced-precision product accumulate along the chain (the trailing
+		// FP64 sweeps rebuild them)
+		const int eprec = opt.reduced_env ? prec : (int)GEMM_FP64;
+		if (left_to_right) lb[i + 1] = contraction_step_left(c, A[i], W[i], lb[i], eprec);
 		else
 		{
 			entropy[i] = ent;
-			rb[i] = contraction_step_right(c, A[i + 1], W[i + 1], rb[i + 1], GEMM_FP64);
+			rb[i] = contraction_step_right(c, A[i + 1], W[i + 1], rb[i + 1], eprec);
 		}
 		CTG_CUDA(cudaEventRecord(ev[3], c.stream()));
 		const double h3 = now_s();

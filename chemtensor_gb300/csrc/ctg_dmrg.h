@@ -10,6 +10,7 @@ struct DmrgOptions {
 	int device = 0;
 	int precision = GEMM_FP64;   // GemmPrecision of the bulk local-H GEMMs
 	int final_fp64_sweeps = 1;   // trailing sweeps forced to FP64 when precision != FP64
+	bool reduced_env = false;    // environment updates of the reduced-precision sweeps in that precision too
 	int verbose = 0;
 	i64 l2_flush_bytes = 0;      // if > 0, overwrite a buffer of this size before every sweep
 	int profile = 0;             // time every launch by kernel class (CUDA events)
@@ -67,6 +68,11 @@ DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w,
 // after three untimed ones; *flops receives the algorithmic GEMM FLOPs of one application
 double time_local_hamiltonian(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,
                               int precision, int nmatvec, double* flops);
+
+// spin-orbital molecular Hamiltonian as an MPO (construct_spin_molecular_hamiltonian_mpo_assembly with
+// optimize = false + mpo_from_assembly, src/operator/hamiltonian.c:2768-2979); tkin n x n and vint
+// n x n x n x n row-major; out receives reference-layout tensors
+int build_spin_molecular_mpo(int n, const double* tkin, const double* vint, struct mpo* out);
 
 // host <-> device conversions of reference structs
 Meta meta_from_struct(const struct block_sparse_tensor* t);

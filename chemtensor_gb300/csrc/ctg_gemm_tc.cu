@@ -13,7 +13,8 @@
 // t's "full" mbarrier (expect-tx), the tcgen05.mma instructions of chunk t - 1 (3 products x 4
 // k-steps of 16) accumulate in FP32 in tensor memory and are committed to that stage's "done"
 // mbarrier, which frees the stage for chunk t + 1. The epilogue reads the accumulator with
-// tcgen05.ld and writes FP64. Every wait is bounded: on timeout the CTA records an error flag,
+// tcgen05.ld, stages it in shared memory and writes FP64 rows, coalesced, into the output block's
+// layout (which may be that of a transposed result, see GemmOut). Every wait is bounded: on timeout the CTA records an error flag,
 // stops issuing work, waits (bounded) for its copies in flight, frees its tensor memory and returns.
 #include <algorithm>
 
@@ -43,6 +44,7 @@ constexpr int TC_STAGES = 2;
 constexpr int TC_SMEM_BYTES = TC_STAGES * STAGE_BYTES + 128;
 static_assert(2 * A_TILE_BYTES == TC_A_REC_BYTES && 2 * B_TILE_BYTES == TC_B_REC_BYTES, "record layout");
 static_assert(TC_BM == TC_A_ROWS && TC_BN == TC_B_ROWS && TC_BK == TC_K, "tile shape");
+static_assert(TC_BM * (TC_BN + 1) * 4 <= TC_STAGES * STAGE_BYTES, "epilogue tile fits in the stage buffers");
 constexpr long long TC_WAIT_LIMIT = 1ll << 26;   // spins before a wait is declared failed
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -276,14 +278,16 @@ k_gemm_tc(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, 
 	tc_fence_after();
 	const bool have_acc = *sh_ok && nchunks > 0;
 
-	// epilogue: each warp owns 32 accumulator rows (tensor-memory lanes 32 w .. 32 w + 31)
-	const int row = tile.m0 + warp * 32 + lane;
-	double* cblk = C + o.c_off;
-	for (int cc = 0; cc < TC_BN; cc += 16)
+	// epilogue: each warp reads its 32 accumulator rows (tensor-memory lanes 32 w .. 32 w + 31) into
+	// a padded FP32 tile in the (now idle) stage buffers; then the CTA writes the tile row by row,
+	// consecutive threads on consecutive columns, into the block's output layout (plain row-major,
+	// or the layout of a transposed result: gemm_out_index)
+	float* stile = (float*)smem;                                        // TC_BM x (TC_BN + 1)
+	if (have_acc)
 	{
-		uint32_t v[16];
-		if (have_acc)
+		for (int cc = 0; cc < TC_BN; cc += 16)
 		{
+			uint32_t v[16];
 			const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc;
 			asm volatile(
 				"tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -291,19 +295,17 @@ k_gemm_tc(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, 
 				  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
 				: "r"(taddr));
 			asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+			float* srow = stile + (warp * 32 + lane) * (TC_BN + 1) + cc;
+			for (int t = 0; t < 16; t++) srow[t] = __uint_as_float(v[t]);
 		}
-		else
-		{
-			for (int t = 0; t < 16; t++) v[t] = 0u;
-		}
-		if (row < o.m)
-		{
-			for (int t = 0; t < 16; t++)
-			{
-				const int col = tile.n0 + cc + t;
-				if (col < o.n) cblk[(i64)row * o.n + col] = (double)__uint_as_float(v[t]);
-			}
-		}
+	}
+	__syncthreads();
+	const int rows = min(TC_BM, o.m - tile.m0), cols = min(TC_BN, o.n - tile.n0);
+	for (int e = tid; e < TC_BM * TC_BN; e += TC_THREADS)
+	{
+		const int r = e / TC_BN, cl = e % TC_BN;
+		if (r < rows && cl < cols)
+			C[gemm_out_index(o, tile.m0 + r, tile.n0 + cl)] = have_acc ? (double)stile[r * (TC_BN + 1) + cl] : 0.0;
 	}
 	tc_fence_before();
 	__syncthreads();

@@ -130,3 +130,25 @@ def mpo_to_matrix(ch: cs.Chain) -> np.ndarray:
         s = acc.shape
         acc = acc.reshape(s[0] * s[1], s[2] * s[3], s[4])
     return acc[..., 0]
+
+
+def spin_molecular(tkin: np.ndarray, vint: np.ndarray) -> cs.Chain:
+    """Spin-orbital molecular Hamiltonian (physicists' order of vint) as an MPO, built by the
+    C-ABI ctgpu_construct_spin_molecular_mpo (host code of libctgpu.so); same operator, bond
+    dimensions and bond quantum numbers as the reference's
+    construct_spin_molecular_hamiltonian_mpo_assembly(tkin, vint, optimize=false)
+    (src/operator/hamiltonian.c:2768-2979)."""
+    import ctypes as C
+
+    from . import native
+    tkin = np.ascontiguousarray(tkin, dtype=np.float64)
+    vint = np.ascontiguousarray(vint, dtype=np.float64)
+    n = tkin.shape[0]
+    if tkin.shape != (n, n) or vint.shape != (n, n, n, n):
+        raise ValueError("tkin must be n x n and vint n x n x n x n")
+    m = cs.MPO()
+    if native.lib().ctgpu_construct_spin_molecular_mpo(n, tkin.ctypes.data, vint.ctypes.data, C.byref(m)) != 0:
+        raise RuntimeError(native.last_error())
+    ch = cs.read_mpo(m)
+    cs.free_mpo(m)
+    return ch

@@ -21,6 +21,7 @@ EXPORTS = [
     "dmrg_twosite",
     "dmrg_singlesite",
     "ctgpu_set_precision",
+    "ctgpu_set_reduced_environments",
     "ctgpu_set_device",
     "ctgpu_get_last_stats",
     "ctgpu_last_error",
@@ -35,6 +36,7 @@ EXPORTS = [
     "ctgpu_contraction_operator_step_right",
     "ctgpu_block_sparse_tensor_svd_values",
     "ctgpu_block_sparse_tensor_qr",
+    "ctgpu_construct_spin_molecular_mpo",
     "ctgpu_block_sparse_tensor_rq",
     "ctgpu_delete_block_sparse_tensor",
     "ctgpu_set_profiling",
@@ -74,6 +76,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.dmrg_singlesite.argtypes = [P, C.c_int, C.c_int, P, P]
     lib.dmrg_singlesite.restype = C.c_int
     lib.ctgpu_set_precision.argtypes = [C.c_int]
+    lib.ctgpu_set_reduced_environments.argtypes = [C.c_int]
     lib.ctgpu_set_device.argtypes = [C.c_int]
     lib.ctgpu_get_last_stats.argtypes = [P]
     lib.ctgpu_last_error.restype = C.c_char_p
@@ -89,6 +92,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_contraction_operator_step_right.argtypes = [P] * 4
     lib.ctgpu_block_sparse_tensor_svd_values.argtypes = [P, P, P]
     lib.ctgpu_block_sparse_tensor_qr.argtypes = [P, C.c_int, P, P]
+    lib.ctgpu_construct_spin_molecular_mpo.argtypes = [C.c_int, P, P, P]
     lib.ctgpu_block_sparse_tensor_rq.argtypes = [P, C.c_int, P, P]
     lib.ctgpu_delete_block_sparse_tensor.argtypes = [P]
     lib.ctgpu_delete_block_sparse_tensor.restype = None

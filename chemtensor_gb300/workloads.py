@@ -51,3 +51,21 @@ def local_h_microbench(D: int = 1024, nsec: int = 41, sigma: float = 6.0, Dw: in
     l = _fill(cs.BlockSparse((1, D, Dw, D), (1, -1, -1, 1), [zero, ql, qw, ql]), rng)
     r = _fill(cs.BlockSparse((D, Dw, D, 1), (1, 1, -1, -1), [qr, qw, qr, zero]), rng)
     return a, h2, l, r
+
+
+def molecular_integrals(n: int = 24, seed: int = 7):
+    """Synthetic molecular integrals of the molecular DMRG workload: tkin symmetric with entries
+    N(0, 0.5^2); chemists' ERI (ij|kl) = sum_{r < 2n} L_r[i,j] L_r[k,l] over symmetric factors L_r
+    with entries N(0, 0.1^2) (8-fold symmetry); returned in the physicists' order of the MPO
+    builders, vint[i,j,k,l] = (ik|jl)."""
+    rng = np.random.default_rng(seed)
+
+    def sym(scale):
+        a = rng.normal(0.0, scale, size=(n, n))
+        return np.triu(a) + np.triu(a, 1).T
+
+    tkin = sym(0.5)
+    L = np.stack([sym(0.1) for _ in range(2 * n)])
+    eri = np.einsum("rij,rkl->ijkl", L, L)
+    vint = np.ascontiguousarray(eri.transpose(0, 2, 1, 3))
+    return tkin, vint

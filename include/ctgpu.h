@@ -51,6 +51,12 @@ int dmrg_singlesite(const struct mpo* hamiltonian, const int num_sweeps, const i
  * or -5 for an unknown value (the setting is then unchanged). */
 int ctgpu_set_precision(int precision);
 
+/* With 1, the environment updates of the split-BF16 sweeps (ctgpu_set_precision(1)) also run in
+ * split-BF16; with 0 (default) they stay FP64 in every sweep. The trailing FP64 sweep rebuilds
+ * every environment in FP64 either way. Per thread; returns the previous value. No counterpart in
+ * the reference. */
+int ctgpu_set_reduced_environments(int on);
+
 /* Drop the lowered operations (device work lists) that this thread's context keeps for reuse
  * across calls; the next calls rebuild them as needed. No counterpart in the reference. */
 int ctgpu_clear_plan_cache(void);
@@ -121,6 +127,16 @@ int ctgpu_construct_random_mps(int nsites, ct_long d, const qnumber* qsite, qnum
 
 /* First n standard normal draws of a freshly seeded generator (randn, src/util/rng.c:116-125). */
 void ctgpu_randn_sequence(uint64_t seed, int n, double* out);
+
+/* Spin-orbital molecular Hamiltonian
+ *   H = sum_{ij,s} tkin[i,j] a+_{is} a_{js} + 1/2 sum_{ijkl,s,u} vint[i,j,k,l] a+_{is} a+_{ju} a_{lu} a_{ks}
+ * as an MPO with one site per spatial orbital (local basis |0>, |dn>, |up>, |up dn>).
+ * Replaces construct_spin_molecular_hamiltonian_mpo_assembly with optimize = false followed by
+ * mpo_from_assembly (src/operator/hamiltonian.c:2768-2979, src/operator/mpo.c:59-174): same
+ * operator and the same virtual bond dimensions (2 + 4n + 2M^2 - M, M = 2 min(b, n-b)) and bond
+ * quantum numbers. tkin: n x n, vint: n x n x n x n, row-major. Host-only; the tensors of out are
+ * allocated with aligned_alloc. Returns 0, or -5 for invalid arguments. */
+int ctgpu_construct_spin_molecular_mpo(int nsites, const double* tkin, const double* vint, struct mpo* out);
 
 /* ---- single operations, for parity checks of the device kernels ------------------------ */
 

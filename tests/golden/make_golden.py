@@ -14,8 +14,11 @@ drives it through ctypes and stores, as .npz:
   one bond (src/algorithm/chain_ops.c); block_sparse_tensor_qr / _rq on random
   block-sparse matrices (src/tensor/block_sparse_tensor.c).
 
-Run from the repository root:  python tests/golden/make_golden.py [singlesite|qr]
-(with an argument, only the dmrg_singlesite or the QR / RQ fixtures are written).
+* the spin-orbital molecular Hamiltonian MPO (src/operator/hamiltonian.c:2768) and a
+  dmrg_twosite run on it.
+
+Run from the repository root:  python tests/golden/make_golden.py [singlesite|qr|molecular]
+(with an argument, only that group of fixtures is written).
 """
 
 import ctypes as C
@@ -41,6 +44,7 @@ ref.ref_local_hamiltonian_setup.argtypes = [C.c_void_p] * 2 + [C.c_int] + [C.c_v
 ref.apply_local_hamiltonian.argtypes = [C.c_void_p] * 5
 ref.contraction_operator_step_left.argtypes = [C.c_void_p] * 5
 ref.contraction_operator_step_right.argtypes = [C.c_void_p] * 5
+ref.ref_spin_molecular_mpo.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
 ref.block_sparse_tensor_qr.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
 ref.block_sparse_tensor_rq.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
 
@@ -153,6 +157,53 @@ def qr_cases():
     print("qr_rq_blocks.npz", len(arrays), "arrays")
 
 
+def molecular_cases():
+    """construct_spin_molecular_hamiltonian_mpo_assembly(optimize=false) + mpo_from_assembly
+    (src/operator/hamiltonian.c:2768-2979): the full MPO for n = 4 with general (non-symmetric)
+    coefficients, and for n = 24 with the synthetic integrals of the molecular workload the bond
+    quantum numbers and stored entries per site; plus a small dmrg_twosite run on n = 6."""
+    sys.path.insert(0, ROOT)
+    from chemtensor_gb300 import workloads as wl
+
+    def build(tk, vi):
+        m = cs.MPO()
+        n = tk.shape[0]
+        ref.ref_spin_molecular_mpo(n, np.ascontiguousarray(tk).ctypes.data, np.ascontiguousarray(vi).ctypes.data, 0,
+                                   C.byref(m))
+        return m
+
+    arrays = {}
+    rng = np.random.default_rng(205)
+    tk, vi = rng.standard_normal((4, 4)), rng.standard_normal((4, 4, 4, 4))
+    arrays.update(tkin4=tk, vint4=vi)
+    arrays.update(cs.chain_to_arrays("H4", cs.read_mpo(build(tk, vi))))
+    tk, vi = wl.molecular_integrals(24, 7)
+    ch = cs.read_mpo(build(tk, vi))
+    for i, t in enumerate(ch.tensors):
+        arrays[f"q24_bond{i}"] = np.sort(np.asarray(t.qnums_logical[0], dtype=np.int32))
+        arrays[f"nnz24_site{i}"] = np.array(t.num_elements_blocks())
+    np.savez_compressed(os.path.join(OUT, "spin_molecular_mpo.npz"), **arrays)
+    print("spin_molecular_mpo.npz")
+
+    # dmrg_twosite on a 6-orbital molecular Hamiltonian (the workload's integrals at n = 6)
+    L, D, sweeps, maxiter, tol, seed = 6, 32, 3, 5, 1e-10, 17
+    tk, vi = wl.molecular_integrals(L, 3)
+    H = build(tk, vi)
+    psi = random_mps(L, HUB_QSITE, (L << 16), D, seed)
+    arrays = {"tkin": tk, "vint": vi}
+    arrays.update(cs.chain_to_arrays("H", cs.read_mpo(H)))
+    arrays.update(cs.chain_to_arrays("psi0", cs.read_mps(psi)))
+    en = (C.c_double * sweeps)()
+    ent = (C.c_double * (L - 1))()
+    assert ref.dmrg_twosite(C.byref(H), sweeps, maxiter, tol, D, C.byref(psi), en, ent) == 0
+    arrays.update(cs.chain_to_arrays("psi", cs.read_mps(psi)))
+    arrays.update(en_sweeps=np.array(en), entropy=np.array(ent),
+                  params=np.array([L, D, sweeps, maxiter], dtype=np.int64), tol_split=np.array(tol),
+                  seed=np.array(seed), model=np.array("molecular"))
+    np.savez_compressed(os.path.join(OUT, "dmrg_molecular_n6_D32.npz"), **arrays)
+    print("dmrg_molecular_n6_D32.npz E =", en[sweeps - 1])
+
+
 def local_ops_case(name, model, L, D, seed, ibond, **kw):
     """Reference inputs/outputs of one local-H apply and one left / right environment step."""
     H = mpo(model, L, **kw)
@@ -221,7 +272,10 @@ if __name__ == "__main__":
         singlesite_cases()
     elif sys.argv[1:] == ["qr"]:
         qr_cases()
+    elif sys.argv[1:] == ["molecular"]:
+        molecular_cases()
     else:
         main()
         singlesite_cases()
         qr_cases()
+        molecular_cases()
