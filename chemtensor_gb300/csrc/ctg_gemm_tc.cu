@@ -8,14 +8,20 @@
 //
 // k_tc_pack writes the operands as records of K-major tiles (hi and lo, canonical no-swizzle
 // core-matrix layout of the tensor-core shared-memory descriptors), so that the GEMM moves a tile
-// into shared memory with one bulk copy. k_gemm_tc: one CTA per 128 x 64 output tile; one thread
-// runs a two-stage pipeline - bulk copies of the A and B records of k chunk t complete on stage
-// t's "full" mbarrier (expect-tx), the tcgen05.mma instructions of chunk t - 1 (3 products x 4
-// k-steps of 16) accumulate in FP32 in tensor memory and are committed to that stage's "done"
-// mbarrier, which frees the stage for chunk t + 1. The epilogue reads the accumulator with
-// tcgen05.ld, stages it in shared memory and writes FP64 rows, coalesced, into the output block's
-// layout (which may be that of a transposed result, see GemmOut). Every wait is bounded: on timeout the CTA records an error flag,
-// stops issuing work, waits (bounded) for its copies in flight, frees its tensor memory and returns.
+// into shared memory with one bulk copy.
+//
+// k_gemm_tc is persistent and warp-specialised: one CTA per SM walks the output tiles (128 x 64)
+// with a stride of the grid size. Warp 0 (one lane) streams the A and B records of every k chunk
+// into a ring of shared-memory stages (bulk copies completing on the stage's "full" mbarrier);
+// warp 1 (one lane) issues the tcgen05.mma instructions of each chunk (3 products x 4 k-steps of
+// 16, FP32 accumulation in tensor memory) and commits them to the stage's "empty" mbarrier, which
+// hands the stage back to the copy warp; the accumulator of a tile alternates between two
+// tensor-memory buffers, so that warps 2-5 (one per 32-lane quarter of tensor memory) drain tile i
+// with tcgen05.ld while the MMAs of tile i + 1 run. The epilogue stages the FP32 tile in shared
+// memory and writes FP64 rows, coalesced, into the output block's layout (plain, or that of a
+// transposed result, see GemmOut). Every wait is bounded and also ends when another warp has
+// recorded a failure: the CTA then records the error flag, lets its copies in flight land, frees
+// its tensor memory and returns.
 #include <algorithm>
 
 #include <cuda_bf16.h>
@@ -31,8 +37,10 @@ namespace {
 constexpr int TC_BM = 128;                 // tile rows (MMA M)
 constexpr int TC_BN = 64;                  // tile columns (MMA N)
 constexpr int TC_BK = 64;                  // K elements per shared-memory stage
-constexpr int TC_THREADS = 128;
-constexpr int TC_TMEM_COLS = 64;           // FP32 accumulator columns (= TC_BN), power of two >= 32
+constexpr int TC_THREADS = 192;            // copy warp, MMA warp, 4 epilogue warps
+constexpr int TC_EPI_THREADS = 128;
+constexpr int TC_ACC_BUFS = 2;
+constexpr int TC_TMEM_COLS = TC_ACC_BUFS * TC_BN;   // FP32 accumulator columns, power of two >= 32
 // canonical no-swizzle K-major layout: 8 x 16-byte core matrices; (row, k) ->
 // (row / 8) * SBO + (k / 8) * LBO + (row % 8) * 16 + (k % 8) * 2
 constexpr int TC_LBO = 128;                // bytes between core matrices adjacent in K
@@ -40,11 +48,15 @@ constexpr int TC_SBO = (TC_BK / 8) * 128;  // bytes between core matrices adjace
 constexpr int A_TILE_BYTES = TC_BM * TC_BK * 2;
 constexpr int B_TILE_BYTES = TC_BN * TC_BK * 2;
 constexpr int STAGE_BYTES = 2 * A_TILE_BYTES + 2 * B_TILE_BYTES;   // one A record + one B record
-constexpr int TC_STAGES = 2;
-constexpr int TC_SMEM_BYTES = TC_STAGES * STAGE_BYTES + 128;
+constexpr int TC_STAGES = 4;
+constexpr int TC_EPI_BYTES = TC_BM * (TC_BN + 1) * 4;               // padded FP32 staging tile
+constexpr int TC_OFF_BYTES = 8 * (TC_BM + TC_BN);                     // row / column offsets of a tile
+constexpr int TC_BAR_BYTES = 8 * (2 * TC_STAGES + 2 * TC_ACC_BUFS) + 16;
+constexpr int TC_SMEM_BYTES = TC_STAGES * STAGE_BYTES + TC_EPI_BYTES + TC_OFF_BYTES + TC_BAR_BYTES;
 static_assert(2 * A_TILE_BYTES == TC_A_REC_BYTES && 2 * B_TILE_BYTES == TC_B_REC_BYTES, "record layout");
 static_assert(TC_BM == TC_A_ROWS && TC_BN == TC_B_ROWS && TC_BK == TC_K, "tile shape");
-static_assert(TC_BM * (TC_BN + 1) * 4 <= TC_STAGES * STAGE_BYTES, "epilogue tile fits in the stage buffers");
+static_assert(TC_SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
+static_assert(TC_EPI_BYTES % 16 == 0, "barrier alignment");
 constexpr long long TC_WAIT_LIMIT = 1ll << 26;   // spins before a wait is declared failed
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -100,11 +112,12 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, int count)
 	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
 
-// bounded wait for the given phase parity; returns false on timeout
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+// bounded wait for the given phase parity; returns false on timeout, or when *abort is set
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, const volatile int* abort = nullptr)
 {
 	for (long long it = 0; it < TC_WAIT_LIMIT; it++)
 	{
+		if (abort && *abort) return false;
 		uint32_t done = 0;
 		asm volatile(
 			"{\n\t.reg .pred p;\n\t"
@@ -164,21 +177,57 @@ __global__ void __launch_bounds__(128) k_tc_pack(const TcPack* __restrict__ pack
 	}
 }
 
-__global__ void __launch_bounds__(TC_THREADS)
-k_gemm_tc(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, const TcContrib* __restrict__ tcons,
-          const unsigned char* __restrict__ apack, const unsigned char* __restrict__ bpack, double* __restrict__ C,
-          int* __restrict__ error)
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar)
+{
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+
+// named barrier of the four epilogue warps (id 1; id 0 is __syncthreads)
+__device__ __forceinline__ void epi_sync()
+{
+	asm volatile("bar.sync 1, %0;" ::"r"(TC_EPI_THREADS) : "memory");
+}
+
+// the same barrier, returning the AND of v over the epilogue threads
+__device__ __forceinline__ bool epi_sync_and(bool v)
+{
+	uint32_t r;
+	asm volatile(
+		"{\n\t.reg .pred p, q;\n\t"
+		"setp.ne.u32 p, %1, 0;\n\t"
+		"bar.red.and.pred q, 1, %2, p;\n\t"
+		"selp.u32 %0, 1, 0, q;\n\t}"
+		: "=r"(r)
+		: "r"((uint32_t)v), "r"(TC_EPI_THREADS)
+		: "memory");
+	return r != 0;
+}
+
+__device__ __forceinline__ int tile_chunks(const GemmOut& o, const TcContrib* tcons)
+{
+	int n = 0;
+	for (int c = o.c0; c < o.c0 + o.nc; c++) n += tcons[c].kt;
+	return n;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
+          const TcContrib* __restrict__ tcons, const unsigned char* __restrict__ apack,
+          const unsigned char* __restrict__ bpack, double* __restrict__ C, int* __restrict__ error)
 {
 	extern __shared__ __align__(1024) unsigned char smem[];
-	uint64_t* full = (uint64_t*)(smem + TC_STAGES * STAGE_BYTES);     // copies of a stage landed
-	uint64_t* done = full + TC_STAGES;                                 // MMAs of a stage finished
-	uint32_t* tmem_slot = (uint32_t*)(done + TC_STAGES);
-	int* sh_ok = (int*)(tmem_slot + 1);
+	float* stile = (float*)(smem + TC_STAGES * STAGE_BYTES);                  // epilogue staging
+	i64* rowoff = (i64*)(smem + TC_STAGES * STAGE_BYTES + TC_EPI_BYTES);         // output offsets of
+	i64* coloff = rowoff + TC_BM;                                               // the tile's rows, columns
+	uint64_t* full = (uint64_t*)(coloff + TC_BN);                               // copies landed
+	uint64_t* empty = full + TC_STAGES;                                        // MMAs of a stage done
+	uint64_t* acc_full = empty + TC_STAGES;                                    // accumulator ready
+	uint64_t* acc_empty = acc_full + TC_ACC_BUFS;                              // accumulator drained
+	uint32_t* tmem_slot = (uint32_t*)(acc_empty + TC_ACC_BUFS);
+	volatile int* abort = (volatile int*)(tmem_slot + 1);
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	const GemmTile tile = tiles[blockIdx.x];
-	const GemmOut o = outs[tile.out];
 
-	if (warp == 0)
+	if (warp == 1)
 	{
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
 		             "r"(TC_TMEM_COLS)
@@ -187,129 +236,200 @@ k_gemm_tc(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs, 
 	}
 	if (tid == 0)
 	{
-		for (int s = 0; s < TC_STAGES; s++)
+		for (int st = 0; st < TC_STAGES; st++)
 		{
-			mbar_init(smem_u32(full + s), 1);
-			mbar_init(smem_u32(done + s), 1);
+			mbar_init(smem_u32(full + st), 1);
+			mbar_init(smem_u32(empty + st), 1);
 		}
-		*sh_ok = 1;
+		for (int b = 0; b < TC_ACC_BUFS; b++)
+		{
+			mbar_init(smem_u32(acc_full + b), 1);
+			mbar_init(smem_u32(acc_empty + b), TC_EPI_THREADS / 32);
+		}
+		*abort = 0;
 	}
 	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();
 	const uint32_t tmem = *tmem_slot;
-	int nchunks = 0;
-	for (int c = o.c0; c < o.c0 + o.nc; c++) nchunks += tcons[c].kt;
 
-	if (tid == 0 && nchunks > 0)
+	if (warp == 0)
 	{
-		const uint32_t idesc = make_idesc();
-		const int mt = tile.m0 / TC_BM, nt = tile.n0 / TC_BN;
-		int lc = o.c0, lk = 0;           // load cursor: contribution, k tile
-		bool ok = true;
-		int issued = 0;                  // chunks whose copies were issued
-		for (int t = 0; t <= nchunks && ok; t++)
+		// copy warp: k chunks of every tile of this CTA, in order, into the stage ring
+		if (lane == 0)
 		{
-			if (t < nchunks)
+			long long g = 0;           // chunks issued by this CTA
+			bool ok = true;
+			for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x)
 			{
-				const int st = t % TC_STAGES;
-				if (t >= TC_STAGES && !mbar_wait(smem_u32(done + st), (uint32_t)(((t - TC_STAGES) / TC_STAGES) & 1)))
+				const GemmTile tile = tiles[ti];
+				const GemmOut o = outs[tile.out];
+				const int mt = tile.m0 / TC_BM, nt = tile.n0 / TC_BN;
+				for (int c = o.c0; c < o.c0 + o.nc && ok; c++)
 				{
-					ok = false;
-					break;
+					const TcContrib gc = tcons[c];
+					for (int lk = 0; lk < gc.kt; lk++, g++)
+					{
+						const int st = (int)(g % TC_STAGES);
+						if (g >= TC_STAGES &&
+						    !mbar_wait(smem_u32(empty + st), (uint32_t)(((g / TC_STAGES) - 1) & 1), abort))
+						{
+							ok = false;
+							break;
+						}
+						const unsigned char* arec = apack + (gc.a_rec + (i64)mt * gc.kt + lk) * TC_A_REC_BYTES;
+						const unsigned char* brec = bpack + (gc.b_rec + (i64)nt * gc.kt + lk) * TC_B_REC_BYTES;
+						const uint32_t sbase = smem_u32(smem + st * STAGE_BYTES);
+						mbar_expect_tx(smem_u32(full + st), (uint32_t)STAGE_BYTES);
+						bulk_copy(sbase, arec, (uint32_t)TC_A_REC_BYTES, smem_u32(full + st));
+						bulk_copy(sbase + (uint32_t)TC_A_REC_BYTES, brec, (uint32_t)TC_B_REC_BYTES, smem_u32(full + st));
+					}
 				}
-				while (lk >= tcons[lc].kt) { lc++; lk = 0; }
-				const TcContrib g = tcons[lc];
-				const unsigned char* arec = apack + (g.a_rec + (i64)mt * g.kt + lk) * TC_A_REC_BYTES;
-				const unsigned char* brec = bpack + (g.b_rec + (i64)nt * g.kt + lk) * TC_B_REC_BYTES;
-				const uint32_t sbase = smem_u32(smem + st * STAGE_BYTES);
-				mbar_expect_tx(smem_u32(full + st), (uint32_t)STAGE_BYTES);
-				bulk_copy(sbase, arec, (uint32_t)TC_A_REC_BYTES, smem_u32(full + st));
-				bulk_copy(sbase + (uint32_t)TC_A_REC_BYTES, brec, (uint32_t)TC_B_REC_BYTES, smem_u32(full + st));
-				issued = t + 1;
-				lk++;
 			}
-			if (t >= 1)
+			if (!ok)
 			{
-				const int u = t - 1, su = u % TC_STAGES;
-				if (!mbar_wait(smem_u32(full + su), (uint32_t)((u / TC_STAGES) & 1)))
+				*abort = 1;
+				atomicExch(error, 1);
+			}
+			// the copies of the last chunk of every stage must land before shared memory is released
+			for (long long u = g - TC_STAGES; u < g; u++)
+				if (u >= 0) mbar_wait(smem_u32(full + (int)(u % TC_STAGES)), (uint32_t)((u / TC_STAGES) & 1));
+		}
+	}
+	else if (warp == 1)
+	{
+		// MMA warp
+		if (lane == 0)
+		{
+			const uint32_t idesc = make_idesc();
+			long long g = 0;           // chunks consumed
+			int acc = 0;               // tiles accumulated (tiles with at least one chunk)
+			bool ok = true;
+			for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x)
+			{
+				const GemmTile tile = tiles[ti];
+				const GemmOut o = outs[tile.out];
+				const int nch = tile_chunks(o, tcons);
+				if (nch == 0) continue;
+				const int b = acc % TC_ACC_BUFS;
+				if (acc >= TC_ACC_BUFS &&
+				    !mbar_wait(smem_u32(acc_empty + b), (uint32_t)(((acc / TC_ACC_BUFS) - 1) & 1), abort))
 				{
 					ok = false;
 					break;
 				}
 				tc_fence_after();
-				const uint32_t a_hi = smem_u32(smem + su * STAGE_BYTES);
-				const uint32_t a_lo = a_hi + A_TILE_BYTES;
-				const uint32_t b_hi = a_lo + A_TILE_BYTES;
-				const uint32_t b_lo = b_hi + B_TILE_BYTES;
-				for (int s = 0; s < TC_BK / 16; s++)
+				const uint32_t dacc = tmem + (uint32_t)(b * TC_BN);
+				for (int u = 0; u < nch; u++, g++)
 				{
-					const uint32_t koff = (uint32_t)s * 2 * TC_LBO;
-					const uint64_t dah = make_desc(a_hi + koff), dal = make_desc(a_lo + koff);
-					const uint64_t dbh = make_desc(b_hi + koff), dbl = make_desc(b_lo + koff);
-					mma_bf16(tmem, dah, dbh, idesc, u > 0 || s > 0);
-					mma_bf16(tmem, dah, dbl, idesc, true);
-					mma_bf16(tmem, dal, dbh, idesc, true);
+					const int su = (int)(g % TC_STAGES);
+					if (!mbar_wait(smem_u32(full + su), (uint32_t)((g / TC_STAGES) & 1), abort))
+					{
+						ok = false;
+						break;
+					}
+					tc_fence_after();
+					const uint32_t a_hi = smem_u32(smem + su * STAGE_BYTES);
+					const uint32_t a_lo = a_hi + A_TILE_BYTES;
+					const uint32_t b_hi = a_lo + A_TILE_BYTES;
+					const uint32_t b_lo = b_hi + B_TILE_BYTES;
+					for (int k = 0; k < TC_BK / 16; k++)
+					{
+						const uint32_t koff = (uint32_t)k * 2 * TC_LBO;
+						const uint64_t dah = make_desc(a_hi + koff), dal = make_desc(a_lo + koff);
+						const uint64_t dbh = make_desc(b_hi + koff), dbl = make_desc(b_lo + koff);
+						mma_bf16(dacc, dah, dbh, idesc, u > 0 || k > 0);
+						mma_bf16(dacc, dah, dbl, idesc, true);
+						mma_bf16(dacc, dal, dbh, idesc, true);
+					}
+					mma_commit(smem_u32(empty + su));
 				}
-				mma_commit(smem_u32(done + su));
+				if (!ok) break;
+				mma_commit(smem_u32(acc_full + b));
+				acc++;
+			}
+			if (!ok)
+			{
+				*abort = 1;
+				atomicExch(error, 1);
+			}
+			// no MMA may still run when tensor memory is freed: the commit after the last chunk
+			// consumed tracks every MMA issued before it
+			if (g > 0)
+				mbar_wait(smem_u32(empty + (int)((g - 1) % TC_STAGES)), (uint32_t)(((g - 1) / TC_STAGES) & 1));
+		}
+	}
+	else
+	{
+		// epilogue warps: tensor-memory quarter q holds accumulator rows 32 q .. 32 q + 31
+		const int q = warp & 3;
+		const int et = tid - 64;   // 0 .. 127
+		int acc = 0;
+		for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+		{
+			const GemmTile tile = tiles[ti];
+			const GemmOut o = outs[tile.out];
+			const int nch = tile_chunks(o, tcons);
+			// where the tile's rows and columns go (gemm_out_index split into a row and a column part),
+			// while the tile's MMAs may still run
+			static_assert(TC_EPI_THREADS == TC_BM && TC_BN <= TC_EPI_THREADS, "one row offset per thread");
+			{
+				const int i = tile.m0 + et;
+				rowoff[et] = i < o.m ? o.c_off + (i64)(i / o.r1) * o.sr0 + (i64)(i % o.r1) * o.sr1 : 0;
+				const int j = tile.n0 + et;
+				if (et < TC_BN) coloff[et] = j < o.n ? (i64)(j / o.c1) * o.sc0 + (j % o.c1) : -1;
+			}
+			bool have = false;
+			if (nch > 0)
+			{
+				const int b = acc % TC_ACC_BUFS;
+				// warp-uniform outcome: tcgen05.ld is executed by all lanes of a warp or by none
+				have = __all_sync(0xffffffffu, mbar_wait(smem_u32(acc_full + b), (uint32_t)((acc / TC_ACC_BUFS) & 1), abort));
+				if (have)
+				{
+					tc_fence_after();
+					for (int cc = 0; cc < TC_BN; cc += 16)
+					{
+						uint32_t v[16];
+						const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_BN + cc);
+						asm volatile(
+							"tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+							: "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+							  "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+							  "=r"(v[14]), "=r"(v[15])
+							: "r"(taddr));
+						asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+						float* srow = stile + (q * 32 + lane) * (TC_BN + 1) + cc;
+						for (int t = 0; t < 16; t++) srow[t] = __uint_as_float(v[t]);
+					}
+					tc_fence_before();
+					__syncwarp();
+					if (lane == 0) mbar_arrive(smem_u32(acc_empty + b));
+				}
+				acc++;
+			}
+			// CTA-uniform outcome among the epilogue warps (a failed wait ends all of them together)
+			const bool all_have = epi_sync_and(have || nch == 0);
+			have = have && all_have;
+			const int rows = min(TC_BM, o.m - tile.m0);
+			const int cl = et % TC_BN;
+			const i64 co = coloff[cl];
+			if (co >= 0)
+				for (int r = et / TC_BN; r < rows; r += TC_EPI_THREADS / TC_BN)
+					C[rowoff[r] + co] = have ? (double)stile[r * (TC_BN + 1) + cl] : 0.0;
+			epi_sync();
+			if (!all_have)
+			{
+				*abort = 1;
+				atomicExch(error, 1);
+				break;
 			}
 		}
-		if (ok)
-		{
-			// the last commit tracks every MMA issued before it
-			const int last = nchunks - 1;
-			ok = mbar_wait(smem_u32(done + last % TC_STAGES), (uint32_t)((last / TC_STAGES) & 1));
-		}
-		else
-		{
-			// let the copies in flight land before the CTA's shared memory is released
-			for (int u = issued - TC_STAGES; u < issued; u++)
-				if (u >= 0) mbar_wait(smem_u32(full + u % TC_STAGES), (uint32_t)((u / TC_STAGES) & 1));
-		}
-		if (!ok)
-		{
-			*sh_ok = 0;
-			atomicExch(error, 1);
-		}
 	}
 	tc_fence_before();
 	__syncthreads();
-	tc_fence_after();
-	const bool have_acc = *sh_ok && nchunks > 0;
-
-	// epilogue: each warp reads its 32 accumulator rows (tensor-memory lanes 32 w .. 32 w + 31) into
-	// a padded FP32 tile in the (now idle) stage buffers; then the CTA writes the tile row by row,
-	// consecutive threads on consecutive columns, into the block's output layout (plain row-major,
-	// or the layout of a transposed result: gemm_out_index)
-	float* stile = (float*)smem;                                        // TC_BM x (TC_BN + 1)
-	if (have_acc)
-	{
-		for (int cc = 0; cc < TC_BN; cc += 16)
-		{
-			uint32_t v[16];
-			const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc;
-			asm volatile(
-				"tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-				: "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-				  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-				: "r"(taddr));
-			asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-			float* srow = stile + (warp * 32 + lane) * (TC_BN + 1) + cc;
-			for (int t = 0; t < 16; t++) srow[t] = __uint_as_float(v[t]);
-		}
-	}
-	__syncthreads();
-	const int rows = min(TC_BM, o.m - tile.m0), cols = min(TC_BN, o.n - tile.n0);
-	for (int e = tid; e < TC_BM * TC_BN; e += TC_THREADS)
-	{
-		const int r = e / TC_BN, cl = e % TC_BN;
-		if (r < rows && cl < cols)
-			C[gemm_out_index(o, tile.m0 + r, tile.n0 + cl)] = have_acc ? (double)stile[r * (TC_BN + 1) + cl] : 0.0;
-	}
-	tc_fence_before();
-	__syncthreads();
-	if (warp == 0)
+	if (warp == 1)
 	{
 		tc_fence_after();
 		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
@@ -334,11 +454,17 @@ void launch_gemm_tc(int ntiles, const GemmTile* tiles, const GemmOut* outs, cons
 {
 	if (ntiles <= 0) return;
 	static std::once_flag attr_once;
+	static int num_sms = 0;
 	std::call_once(attr_once, [] {
 		CTG_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES));
+		int dev = 0;
+		CTG_CUDA(cudaGetDevice(&dev));
+		CTG_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
 	});
-	k_gemm_tc<<<ntiles, TC_THREADS, TC_SMEM_BYTES, st>>>(tiles, outs, tcons, (const unsigned char*)apack,
-	                                                       (const unsigned char*)bpack, C, error);
+	// persistent: one CTA per SM (the shared-memory ring admits one), each walking every gridDim-th tile
+	const int grid = std::min(ntiles, std::max(num_sms, 1));
+	k_gemm_tc<<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ntiles, tiles, outs, tcons, (const unsigned char*)apack,
+	                                                     (const unsigned char*)bpack, C, error);
 	CTG_CUDA(cudaGetLastError());
 }
 
