@@ -153,6 +153,9 @@ __device__ __forceinline__ void fence_async_smem()
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// One CTA per record. A thread converts one core-matrix row: 8 consecutive k of one row (reads
+// 8 FP64 values, strided by s_k) into 16 bytes of hi and 16 bytes of lo; consecutive threads take
+// consecutive rows, so that 8 threads fill one 128-byte run of the record.
 template <int R>
 __global__ void __launch_bounds__(128) k_tc_pack(const TcPack* __restrict__ packs, const double* __restrict__ src,
                                                  unsigned char* __restrict__ dst)
@@ -160,20 +163,33 @@ __global__ void __launch_bounds__(128) k_tc_pack(const TcPack* __restrict__ pack
 	const TcPack p = packs[blockIdx.x];
 	unsigned char* hi = dst + p.rec * (i64)(2 * R * TC_BK * 2);
 	unsigned char* lo = hi + R * TC_BK * 2;
-	for (int e = threadIdx.x; e < R * TC_BK; e += blockDim.x)
+	constexpr int UNITS = R * (TC_BK / 8);
+	for (int u = threadIdx.x; u < UNITS; u += blockDim.x)
 	{
-		// consecutive threads read consecutive addresses along the unit-stride index
-		int i, kk;
-		if (p.s_k == 1) { kk = e % TC_BK; i = e / TC_BK; }
-		else { i = e % R; kk = e / R; }
-		const int gi = p.row0 + i, gk = p.k0 + kk;
-		// FP32 keeps 24 bits of x, more than the 16 that hi + lo carry
-		float f = 0.0f;
-		if (gi < p.rows && gk < p.k) f = (float)src[p.src + (i64)gi * p.s_row + (i64)gk * p.s_k];
-		const __nv_bfloat16 h = __float2bfloat16_rn(f);
-		const uint32_t so = canon_offset(i, kk);
-		*(__nv_bfloat16*)(hi + so) = h;
-		*(__nv_bfloat16*)(lo + so) = __float2bfloat16_rn(f - __bfloat162float(h));
+		const int i = u % R, kb = u / R;
+		const int gi = p.row0 + i;
+		const double* rowp = src + p.src + (i64)gi * p.s_row;
+		uint32_t h[4], l[4];
+#pragma unroll
+		for (int t = 0; t < 8; t += 2)
+		{
+			const int gk = p.k0 + kb * 8 + t;
+			// FP32 keeps 24 bits of x, more than the 16 that hi + lo carry
+			float f0 = 0.0f, f1 = 0.0f;
+			if (gi < p.rows)
+			{
+				if (gk < p.k) f0 = (float)rowp[(i64)gk * p.s_k];
+				if (gk + 1 < p.k) f1 = (float)rowp[(i64)(gk + 1) * p.s_k];
+			}
+			const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
+			const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
+			const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
+			h[t / 2] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+			l[t / 2] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+		}
+		const uint32_t so = canon_offset(i, kb * 8);
+		*(uint4*)(hi + so) = make_uint4(h[0], h[1], h[2], h[3]);
+		*(uint4*)(lo + so) = make_uint4(l[0], l[1], l[2], l[3]);
 	}
 }
 
