@@ -1,7 +1,10 @@
 // ctg_capi.cpp - extern "C" boundary (include/ctgpu.h).
 #include <cstring>
 #include <exception>
+#include <cmath>
 #include <string>
+
+#include <cuda_runtime.h>
 
 #include "ctgpu.h"
 #include "ctg_dmrg.h"
@@ -233,6 +236,44 @@ int ctgpu_block_sparse_tensor_svd_values(const struct block_sparse_tensor* a, do
 		if (ret < 0) return ret;
 		CTG_CUDA(cudaMemcpy(sigma, sv.s->ptr, (size_t)sv.ns * sizeof(double), cudaMemcpyDeviceToHost));
 		*ns = sv.ns;
+		return 0;
+	});
+}
+
+int ctgpu_device_memory(int device, size_t* free_bytes, size_t* total_bytes)
+{
+	return guarded([&] {
+		CTG_CHECK(free_bytes && total_bytes, "null argument");
+		int prev = 0;
+		CTG_CUDA(cudaGetDevice(&prev));
+		CTG_CUDA(cudaSetDevice(device));
+		CTG_CUDA(cudaMemGetInfo(free_bytes, total_bytes));
+		CTG_CUDA(cudaSetDevice(prev));
+		return 0;
+	});
+}
+
+int ctgpu_mps_vdot(const struct mps* chi, const struct mps* psi, double* ret)
+{
+	return guarded([&] {
+		CTG_CHECK(ret, "null argument");
+		*ret = ctg::mps_vdot_gpu(chi, psi, g_opts.device);
+		return 0;
+	});
+}
+
+int ctgpu_mps_norm(const struct mps* psi, double* ret)
+{
+	return guarded([&] {
+		CTG_CHECK(psi && ret, "null argument");
+		if (psi->nsites == 0)
+		{
+			*ret = 0;
+			return 0;
+		}
+		const double nrm2 = ctg::mps_vdot_gpu(psi, psi, g_opts.device);
+		CTG_CHECK(nrm2 >= -1e-12, "mps_norm: negative squared norm");
+		*ret = std::sqrt(std::max(nrm2, 0.0));
 		return 0;
 	});
 }

@@ -756,6 +756,55 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 }
 
 // ------------------------------------------------------------------------------------
+// mps_vdot (src/state/mps.c:314-370), real case: <chi|psi> by contraction from the right
+// ------------------------------------------------------------------------------------
+
+double mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device)
+{
+	CTG_CHECK(chi && psi && chi->nsites == psi->nsites && psi->nsites >= 1, "mps_vdot: invalid arguments");
+	const int L = psi->nsites;
+	CTG_CHECK(chi->a[0].dim_logical[0] == 1 && psi->a[0].dim_logical[0] == 1 &&
+	              chi->a[L - 1].dim_logical[2] == 1 && psi->a[L - 1].dim_logical[2] == 1,
+	          "mps_vdot: leading and trailing virtual bonds must have dimension 1");
+	Ctx& c = context_for_device(device);
+	// r: 1 x 1 x 1 x 1 with (OUT, IN, IN, OUT) on (psi, chi, psi, chi) trailing bonds, entry 1,
+	// axes 2 and 3 flattened
+	const std::vector<q32> qp(psi->a[L - 1].qnums_logical[2], psi->a[L - 1].qnums_logical[2] + 1);
+	const std::vector<q32> qc(chi->a[L - 1].qnums_logical[2], chi->a[L - 1].qnums_logical[2] + 1);
+	const i64 dim[4] = {1, 1, 1, 1};
+	const int dir[4] = {TENSOR_AXIS_OUT, TENSOR_AXIS_IN, TENSOR_AXIS_IN, TENSOR_AXIS_OUT};
+	Meta m = make_meta(4, dim, dir, {qp, qc, qp, qc});
+	DTensor r;
+	if (m.nblocks == 1)
+	{
+		const double one = 1.0;
+		r.meta = std::make_shared<const Meta>(std::move(m));
+		r.buf = c.upload(&one, sizeof(double));
+	}
+	else r = c.zeros(m);
+	r = op_flatten(c, r, 2, TENSOR_AXIS_IN);
+	for (int i = L - 1; i >= 0; i--)
+	{
+		// mps_contraction_step_right (src/state/mps.c:279-306)
+		DTensor a = tensor_from_struct(c, &psi->a[i]);
+		DTensor b = tensor_from_struct(c, &chi->a[i]);
+		DTensor s1 = op_dot(c, a, AX_TRAILING, r, AX_LEADING, 1);
+		DTensor bc = view_reversed(c, b);
+		const int perm0[4] = {3, 0, 1, 2};
+		DTensor t = op_transpose(c, s1, perm0);
+		DTensor s2 = op_dot(c, t, AX_TRAILING, bc, AX_TRAILING, 2);
+		const int perm1[3] = {1, 2, 0};
+		r = op_transpose(c, s2, perm1);
+	}
+	DTensor rf = op_flatten(c, r, 0, TENSOR_AXIS_OUT);
+	CTG_CHECK(rf.m().ndim == 2 && rf.m().dim[0] == 1 && rf.m().dim[1] == 1, "mps_vdot: unexpected result shape");
+	double v = 0;
+	if (rf.m().nnz > 0) copy_to_host(c, rf, &v);
+	c.sync();
+	return v;
+}
+
+// ------------------------------------------------------------------------------------
 // dmrg_singlesite (src/algorithm/dmrg.c:155-254)
 // ------------------------------------------------------------------------------------
 

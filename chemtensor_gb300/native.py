@@ -37,6 +37,9 @@ EXPORTS = [
     "ctgpu_block_sparse_tensor_svd_values",
     "ctgpu_block_sparse_tensor_qr",
     "ctgpu_construct_spin_molecular_mpo",
+    "ctgpu_mps_vdot",
+    "ctgpu_device_memory",
+    "ctgpu_mps_norm",
     "ctgpu_block_sparse_tensor_rq",
     "ctgpu_delete_block_sparse_tensor",
     "ctgpu_set_profiling",
@@ -93,6 +96,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_block_sparse_tensor_svd_values.argtypes = [P, P, P]
     lib.ctgpu_block_sparse_tensor_qr.argtypes = [P, C.c_int, P, P]
     lib.ctgpu_construct_spin_molecular_mpo.argtypes = [C.c_int, P, P, P]
+    lib.ctgpu_mps_vdot.argtypes = [P, P, P]
+    lib.ctgpu_device_memory.argtypes = [C.c_int, P, P]
+    lib.ctgpu_mps_norm.argtypes = [P, P]
     lib.ctgpu_block_sparse_tensor_rq.argtypes = [P, C.c_int, P, P]
     lib.ctgpu_delete_block_sparse_tensor.argtypes = [P]
     lib.ctgpu_delete_block_sparse_tensor.restype = None

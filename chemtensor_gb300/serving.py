@@ -6,6 +6,13 @@ owns its own execution context in libctgpu.so (stream, memory pool, plan cache),
 different threads run side by side on the GPU while each thread's solve stays sequential. The
 library's per-call state (device, precision, last error, statistics) is thread-local.
 
+Admission: before a thread starts a solve, the request's HBM footprint is estimated from its length,
+bond dimension, local dimension and MPO bond dimension (an upper bound that ignores block
+sparsity: environments, MPS, merged MPO pairs and the local-problem intermediates), and the solve
+waits until the estimates of the solves in flight plus its own fit the pool's budget (by default
+half of the device memory that is free when the pool starts). A request larger than the whole
+budget runs alone.
+
 Request mix (the serving configuration of the two-site DMRG scope): Heisenberg with anisotropy
 Delta ~ U[0.5, 1.5] or Hubbard with U ~ U[1, 8] (t = 1, half filling), length L ~ U{8..48}, bond
 dimension D in {16, 32, 64, 128, 256}, Poisson arrivals; every parameter drawn from one seeded
@@ -71,6 +78,55 @@ def generate_requests(n: int, rate: float, seed: int) -> list[Request]:
     return out
 
 
+MPO_BOND_DIM = {"heisenberg": 5, "hubbard": 6}
+
+
+def estimate_footprint(req: Request, sweeps_buffers: int = 3) -> int:
+    """Upper bound (bytes) of the device memory of one two-site DMRG solve, without block sparsity:
+    left and right environments L x D x Dw x D, the MPS L x D x d x D, merged MPO pairs
+    (L - 1) x Dw^2 x d^4, and `sweeps_buffers` two-site intermediates D x d^2 x Dw x D."""
+    d = 4 if req.model == "hubbard" else 2
+    dw = MPO_BOND_DIM[req.model]
+    L, D = req.nsites, req.max_vdim
+    env = 2 * L * D * dw * D
+    mps = L * D * d * D
+    h2 = (L - 1) * dw * dw * d ** 4
+    inter = sweeps_buffers * D * d * d * dw * D
+    return 8 * (env + mps + h2 + inter)
+
+
+class Admission:
+    """Byte budget shared by the solver threads: acquire blocks until the request fits."""
+
+    def __init__(self, budget: int):
+        self.budget = int(budget)
+        self.in_use = 0
+        self.peak = 0
+        self.cv = threading.Condition()
+
+    def acquire(self, nbytes: int) -> int:
+        take = min(int(nbytes), self.budget)     # a request larger than the budget runs alone
+        with self.cv:
+            while self.in_use + take > self.budget:
+                self.cv.wait()
+            self.in_use += take
+            self.peak = max(self.peak, self.in_use)
+        return take
+
+    def release(self, take: int) -> None:
+        with self.cv:
+            self.in_use -= take
+            self.cv.notify_all()
+
+
+def device_free_bytes(device: int) -> int:
+    import ctypes as C
+    free, total = C.c_size_t(), C.c_size_t()
+    if native.lib().ctgpu_device_memory(device, C.byref(free), C.byref(total)) != 0:
+        raise RuntimeError(native.last_error())
+    return int(free.value)
+
+
 def build_problem(req: Request):
     """MPO and seeded random start state of a request (host side)."""
     # half filling / smallest total spin: 2 Sz = L mod 2
@@ -96,7 +152,10 @@ class SolverPool:
     maxiter: int = 5
     tol: float = 1e-10
     precision: int = native.PRECISION_FP64
+    hbm_budget: int | None = None       # bytes; None: half of the free device memory at start
+    solve: object = None                # the solve function (request, result, lib); None: DMRG
     results: list = field(default_factory=list)
+    admission_peak: int = 0
 
     def _solve(self, req: Request, res: Result, lib):
         H, psi = build_problem(req)
@@ -114,7 +173,10 @@ class SolverPool:
             cs.free_mpo(cH)
 
     def run(self, requests: list[Request]) -> list[Result]:
-        lib = native.lib()
+        lib = native.lib() if self.solve is None else None
+        solve = self.solve or self._solve
+        budget = self.hbm_budget if self.hbm_budget is not None else device_free_bytes(self.device) // 2
+        adm = Admission(budget)
         q: queue.Queue = queue.Queue()
         for r in sorted(requests, key=lambda r: r.arrival):
             q.put(r)
@@ -123,8 +185,9 @@ class SolverPool:
         errors = []
 
         def worker(wid: int):
-            lib.ctgpu_set_device(self.device)
-            lib.ctgpu_set_precision(self.precision)
+            if lib is not None:
+                lib.ctgpu_set_device(self.device)
+                lib.ctgpu_set_precision(self.precision)
             while True:
                 try:
                     req = q.get_nowait()
@@ -135,13 +198,16 @@ class SolverPool:
                     time.sleep(wait)
                 res = results[req.rid]
                 res.worker = wid
+                take = adm.acquire(estimate_footprint(req))
                 res.start = time.perf_counter() - t0
                 try:
-                    self._solve(req, res, lib)
+                    solve(req, res, lib)
                 except Exception as e:  # recorded, the stream goes on
                     res.ret = -99
                     res.error = str(e)
                     errors.append(e)
+                finally:
+                    adm.release(take)
                 res.end = time.perf_counter() - t0
 
         threads = [threading.Thread(target=worker, args=(i,), daemon=True) for i in range(self.workers)]
@@ -150,6 +216,7 @@ class SolverPool:
         for t in threads:
             t.join()
         self.results = [results[r.rid] for r in requests]
+        self.admission_peak = adm.peak
         return self.results
 
 

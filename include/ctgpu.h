@@ -21,6 +21,8 @@
 #ifndef CTGPU_H
 #define CTGPU_H
 
+#include <stddef.h>
+
 #include "ct_structs.h"
 
 #ifdef __cplusplus
@@ -127,6 +129,17 @@ int ctgpu_construct_random_mps(int nsites, ct_long d, const qnumber* qsite, qnum
 
 /* First n standard normal draws of a freshly seeded generator (randn, src/util/rng.c:116-125). */
 void ctgpu_randn_sequence(uint64_t seed, int n, double* out);
+
+/* Free and total device memory of a CUDA device (cudaMemGetInfo), for admission control of
+ * concurrent solves. Returns 0 or -5. No counterpart in the reference. */
+int ctgpu_device_memory(int device, size_t* free_bytes, size_t* total_bytes);
+
+/* <chi|psi> and ||psi|| of real MPS, contracted on the device (bond tensors uploaded, environment
+ * kept in HBM). Replace mps_vdot (src/state/mps.c:314-370; real double case, result in *ret) and
+ * mps_norm (src/state/mps.c:375-424). Leading and trailing virtual bonds must have dimension 1.
+ * Return 0, or -5 (message via ctgpu_last_error). */
+int ctgpu_mps_vdot(const struct mps* chi, const struct mps* psi, double* ret);
+int ctgpu_mps_norm(const struct mps* psi, double* ret);
 
 /* Spin-orbital molecular Hamiltonian
  *   H = sum_{ij,s} tkin[i,j] a+_{is} a_{js} + 1/2 sum_{ijkl,s,u} vint[i,j,k,l] a+_{is} a+_{ju} a_{lu} a_{ks}

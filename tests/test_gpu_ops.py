@@ -189,3 +189,22 @@ def test_qr_rq_match_reference(gpu, tag):
     q3, r3 = cs.BlockSparseTensor(), cs.BlockSparseTensor()
     assert gpu.ctgpu_block_sparse_tensor_qr(C.byref(a), 1, C.byref(q3), C.byref(r3)) == -5
     cs.free_bst(a)
+
+
+@pytest.mark.parametrize("case", ["dmrg_heisenberg_L20_D32.npz", "dmrg_hubbard_L12_D48.npz"])
+def test_mps_vdot_and_norm_match_oracle(gpu, oracle_port, case):
+    """Device mps_vdot / mps_norm against the oracle's mps_vdot (mps.c:314-370) on the reference's
+    start and optimised states (different bond structures, same sector)."""
+    g = golden(case)
+    a, b = cs.chain_from_arrays("psi0", g), cs.chain_from_arrays("psi", g)
+    ca, cb = cs.make_c_mps(a), cs.make_c_mps(b)
+    for x, y in ((ca, cb), (cb, ca), (ca, ca), (cb, cb)):
+        got = C.c_double()
+        assert gpu.ctgpu_mps_vdot(C.byref(x), C.byref(y), C.byref(got)) == 0
+        ref = oracle_port.oracle_mps_vdot(C.byref(x), C.byref(y))
+        assert abs(got.value - ref) <= 1e-12 * max(1.0, abs(ref))
+    nrm = C.c_double()
+    assert gpu.ctgpu_mps_norm(C.byref(ca), C.byref(nrm)) == 0
+    assert abs(nrm.value - np.sqrt(oracle_port.oracle_mps_vdot(C.byref(ca), C.byref(ca)))) <= 1e-12 * nrm.value
+    cs.free_mps(ca)
+    cs.free_mps(cb)

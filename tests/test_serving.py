@@ -1,6 +1,9 @@
 """Serving configuration: the seeded request stream (host) and concurrent solves (GPU) that must
 give the same energies as the same solves one after another."""
 
+import threading
+import time
+
 import numpy as np
 import pytest
 
@@ -30,3 +33,37 @@ def test_concurrent_solves_match_serial():
         # each solve is deterministic: the same energy whatever runs beside it
         assert a.energy == b.energy
     assert len({r.worker for r in conc}) > 1
+
+
+def test_admission_keeps_solves_in_flight_within_the_budget():
+    """Host logic of admission by estimated HBM footprint: a fake solve records how many bytes were
+    admitted while it ran; the total never exceeds the budget, and a request larger than the whole
+    budget still runs (alone)."""
+    reqs = serving.generate_requests(24, 0.0, seed=5)
+    est = {r.rid: serving.estimate_footprint(r) for r in reqs}
+    budget = sorted(est.values())[len(est) // 2] * 2          # about two median solves at a time
+    lock = threading.Lock()
+    live, seen = {}, []
+
+    def fake_solve(req, res, lib):
+        with lock:
+            live[req.rid] = min(est[req.rid], budget)
+            seen.append(sum(live.values()))
+        time.sleep(0.002)
+        with lock:
+            del live[req.rid]
+        res.ret, res.energy = 0, float(req.rid)
+
+    pool = serving.SolverPool(workers=6, hbm_budget=budget, solve=fake_solve)
+    out = pool.run(reqs)
+    assert all(r.ret == 0 for r in out)
+    assert max(seen) <= budget and pool.admission_peak <= budget
+    assert any(v > budget for v in est.values()) or max(seen) > 0
+
+
+def test_footprint_estimate_grows_with_size():
+    small = serving.Request(0, 0.0, "hubbard", 8, 16, 4.0, 1)
+    big = serving.Request(1, 0.0, "hubbard", 48, 256, 4.0, 1)
+    assert 0 < serving.estimate_footprint(small) < serving.estimate_footprint(big)
+    # the dense bound of a D = 256, L = 48 Hubbard solve stays far below one GPU's HBM
+    assert serving.estimate_footprint(big) < 4 << 30
