@@ -463,6 +463,59 @@ def bench_molecular(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def bench_singlesite(args, world, rank, local):
+    """Single-site DMRG (dmrg_singlesite) on the two-site workload's Hamiltonian (Fermi-Hubbard L=32,
+    U=4) from a seeded start state of bond dimension D=256 (bond dimensions stay fixed): W warm-up
+    sweeps then K timed sweeps in one call, device time per sweep from CUDA events; the C
+    restatement of the reference times one sweep on the host cores beside it."""
+    from chemtensor_gb300 import ctstructs as cs, native
+    lib = native.lib()
+    lib.ctgpu_set_device(local)
+    native.set_precision(0)
+    H, psi0 = build_inputs()
+    K, W = args.steps, args.warmup
+    cH, cP = cs.make_c_mpo(H), cs.make_c_mps(psi0)
+    en = np.zeros(W + K)
+    lib.ctgpu_clear_plan_cache()
+    with ClockSampler(local) as clk:
+        ret = lib.dmrg_singlesite(C.byref(cH), W + K, WORKLOAD["maxiter_lanczos"], C.byref(cP), en.ctypes.data)
+    if ret != 0:
+        raise RuntimeError(f"dmrg_singlesite failed: {ret} {native.last_error()}")
+    ms, la = native.sweep_times()
+    t_dev = float(np.sum(ms[W:W + K])) / 1e3
+    t_dev = dist_max(t_dev, world)
+    # <psi|psi> of the result on the device (ctgpu_mps_vdot)
+    nrm = C.c_double()
+    t0 = time.perf_counter()
+    lib.ctgpu_mps_norm(C.byref(cP), C.byref(nrm))
+    t_norm = time.perf_counter() - t0
+    cs.free_mps(cP)
+    cs.free_mpo(cH)
+    line = {"metric": "single-site DMRG sweeps/s (Fermi-Hubbard L=32, D=256)", "value": world * K / t_dev,
+            "unit": "sweeps/s", "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": 1e3 * t_dev / K,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD["workload"].replace("D=256", "D=256 (fixed)") + " dmrg_singlesite",
+                       "parallelism": f"replicas x{world}"},
+            "clocks": clk.summary(), "gpu_launches": int(np.sum(la[W:W + K])),
+            "energies": en.tolist(), "norm_after": nrm.value, "mps_norm_wall_ms": 1e3 * t_norm}
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle
+        port = oracle.port()
+        cH2, cP2 = cs.make_c_mpo(H), cs.make_c_mps(psi0)
+        e2 = np.zeros(1)
+        used = port.oracle_set_num_threads(os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        port.oracle_dmrg_singlesite(C.byref(cH2), 1, WORKLOAD["maxiter_lanczos"], C.byref(cP2), e2.ctypes.data)
+        dt = time.perf_counter() - t0
+        cs.free_mps(cP2)
+        cs.free_mpo(cH2)
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": used, "kind": "port",
+                                "sample": "first sweep from the same start state (C restatement of the reference)",
+                                "energy_after_sweep": float(e2[0]), "gpu_energy_after_sweep": float(en[0])}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def sweeps_only(args, local):
     """One dmrg_twosite call of warmup + steps sweeps on the workload (profiler target)."""
     from chemtensor_gb300 import ctstructs as cs, native
@@ -498,11 +551,12 @@ def main():
     ap.add_argument("--mol-sweeps", type=int, default=10, help="sweeps of --mode molecular")
     ap.add_argument("--mol-precisions", default="fp64,bf16x3", help="runs of --mode molecular")
     ap.add_argument("--mol-profile", action="store_true", help="time every launch by kernel class in --mode molecular")
-    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh", "serve", "molecular"],
+    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh", "serve", "molecular", "singlesite"],
                     help="sweeps: only one device call of warmup+steps sweeps (for profiler captures), no JSON line; "
                          "localh: local-Hamiltonian microbenchmark (synthetic D=1024), its own JSON line; "
                          "serve: request stream of small and medium solves, serial vs concurrent solver threads; "
-                         "molecular: spin-orbital molecular Hamiltonian (n=24, D=512), FP64 vs split-BF16")
+                         "molecular: spin-orbital molecular Hamiltonian (n=24, D=512), FP64 vs split-BF16; "
+                         "singlesite: dmrg_singlesite on the Hubbard workload (D=256 fixed)")
     ap.add_argument("--requests", type=int, default=128, help="requests of the --mode serve stream")
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate (1/s) of --mode serve")
     ap.add_argument("--workers", type=int, default=4, help="solver threads of --mode serve")
@@ -519,6 +573,9 @@ def main():
         return
     if args.mode == "molecular":
         bench_molecular(args, world, rank, local)
+        return
+    if args.mode == "singlesite":
+        bench_singlesite(args, world, rank, local)
         return
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

@@ -825,10 +825,6 @@ int dmrg_singlesite_gpu(const struct mpo* H, int num_sweeps, int maxiter, struct
 	c.gemm_flops = 0;
 	c.kernel_launches = 0;
 	c.profile = false;
-	DBuf sc_buf(&c, sizeof(LanczosScalars));
-	LanczosScalars* d_sc = (LanczosScalars*)sc_buf.ptr;
-	LanczosScalars* h_sc = c.lanczos_host();
-
 	std::vector<DTensor> W(L), A(L);
 	for (int i = 0; i < L; i++) W[i] = tensor_from_struct(c, &H->a[i]);
 	for (int i = 0; i < L; i++) A[i] = tensor_from_struct(c, &psi->a[i]);
@@ -867,25 +863,35 @@ int dmrg_singlesite_gpu(const struct mpo* H, int num_sweeps, int maxiter, struct
 	st->setup_s = t_setup - t_up;
 
 	// local optimisation of site i; the Lanczos status is checked per site as in the reference
+	// every local problem of a sweep writes its Lanczos scalars to its own slot; the host reads them
+	// once per sweep (no synchronisation per site: nothing on the host waits for a site's result),
+	// and reports the first failing site's status as the reference would have returned it
+	const int nsteps = 2 * std::max(L - 1, 0);
+	DBuf steps_buf(&c, (size_t)std::max(nsteps, 1) * sizeof(LanczosScalars));
+	LanczosScalars* d_steps = (LanczosScalars*)steps_buf.ptr;
+	std::vector<LanczosScalars> h_steps((size_t)std::max(nsteps, 1));
+	int step = 0;
 	auto site_step = [&](int i) -> int {
 		DTensor aopt;
-		int r = minimize_local_energy(c, W[i], lb[i], rb[i], A[i], maxiter, d_sc, aopt, st, GEMM_FP64);
+		int r = minimize_local_energy(c, W[i], lb[i], rb[i], A[i], maxiter, d_steps + step, aopt, st, GEMM_FP64);
+		step++;
 		if (r < 0) return r;
-		CTG_CUDA(cudaMemcpyAsync(h_sc, d_sc, sizeof(LanczosScalars), cudaMemcpyDeviceToHost, c.stream()));
-		c.sync();
-		if (h_sc->status != 0) return h_sc->status;
 		A[i] = aopt;
 		return 0;
 	};
+	cudaEvent_t sw_ev[2];
+	for (auto& e : sw_ev) CTG_CUDA(cudaEventCreate(&e));
 	for (int sw = 0; sw < num_sweeps && ret == 0; sw++)
 	{
-		double en = 0;
+		c.sync();
+		const long launches0 = c.kernel_launches;
+		CTG_CUDA(cudaEventRecord(sw_ev[0], c.stream()));
+		step = 0;
 		// sweep from left to right
 		for (int i = 0; i < L - 1 && ret == 0; i++)
 		{
 			ret = site_step(i);
 			if (ret < 0) break;
-			en = h_sc->lambda;
 			ret = local_orthonormalize_qr(c, A[i], A[i + 1]);
 			lb[i + 1] = contraction_step_left(c, A[i], W[i], lb[i]);
 		}
@@ -894,7 +900,6 @@ int dmrg_singlesite_gpu(const struct mpo* H, int num_sweeps, int maxiter, struct
 		{
 			ret = site_step(i);
 			if (ret < 0) break;
-			en = h_sc->lambda;
 			ret = local_orthonormalize_rq(c, A[i], A[i - 1]);
 			rb[i - 1] = contraction_step_right(c, A[i], W[i], rb[i]);
 		}
@@ -902,10 +907,21 @@ int dmrg_singlesite_gpu(const struct mpo* H, int num_sweeps, int maxiter, struct
 		// right-normalise the leftmost tensor so that psi is normalised (dmrg.c:230-243)
 		DTensor t = head_tensor(c, A[0], 0.0);
 		ret = local_orthonormalize_rq(c, A[0], t);
-		en_sweeps[sw] = en;
+		CTG_CUDA(cudaEventRecord(sw_ev[1], c.stream()));
+		if (step > 0)
+			CTG_CUDA(cudaMemcpyAsync(h_steps.data(), d_steps, (size_t)step * sizeof(LanczosScalars), cudaMemcpyDeviceToHost,
+			                         c.stream()));
 		c.sync();
+		for (int k = 0; k < step; k++)
+			if (h_steps[(size_t)k].status != 0) return h_steps[(size_t)k].status;
+		en_sweeps[sw] = step > 0 ? h_steps[(size_t)step - 1].lambda : 0.0;
+		float sms = 0;
+		CTG_CUDA(cudaEventElapsedTime(&sms, sw_ev[0], sw_ev[1]));
+		st->sweep_ms.push_back(sms);
+		st->sweep_launches.push_back(c.kernel_launches - launches0);
 		st->sweeps++;
 	}
+	for (auto& e : sw_ev) cudaEventDestroy(e);
 	c.sync();
 	const double t_sweeps = now_s();
 	st->sweep_s = t_sweeps - t_setup;
