@@ -39,6 +39,7 @@ enum AxRange { AX_LEADING = 0, AX_TRAILING = 1 };
 enum GemmPrecision {
 	GEMM_FP64 = 0,        // plain IEEE double on the FP64 pipe
 	GEMM_BF16X3 = 1,      // split-BF16, 3 products, FP32 accumulation on tcgen05
+	GEMM_Z64 = 2,         // complex128 entries (plan kind; the arithmetic is complex FP64)
 };
 
 }  // namespace ctg

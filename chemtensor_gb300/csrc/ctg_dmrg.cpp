@@ -49,7 +49,8 @@ T* ct_copy(const T* src, size_t n)
 Meta meta_from_struct(const struct block_sparse_tensor* t)
 {
 	CTG_CHECK(t->ndim >= 1, "tensor of degree 0 at the boundary");
-	CTG_CHECK(t->dtype == CT_DOUBLE_REAL, "only double precision real tensors are supported");
+	CTG_CHECK(t->dtype == CT_DOUBLE_REAL || t->dtype == CT_DOUBLE_COMPLEX,
+	          "only double precision tensors (real or complex) are supported");
 	std::vector<i64> dim(t->dim_logical, t->dim_logical + t->ndim);
 	std::vector<int> dir(t->ndim);
 	std::vector<std::vector<q32>> ql(t->ndim);
@@ -71,30 +72,34 @@ Meta meta_from_struct(const struct block_sparse_tensor* t)
 DTensor tensor_from_struct(Ctx& c, const struct block_sparse_tensor* t)
 {
 	Meta m = meta_from_struct(t);
-	std::vector<double> host((size_t)std::max<i64>(m.nnz, 1));
+	const int w = t->dtype == CT_DOUBLE_COMPLEX ? 2 : 1;
+	std::vector<double> host((size_t)std::max<i64>(m.nnz, 1) * w);
 	for (int b = 0; b < m.nblocks; b++)
 	{
 		const struct dense_tensor* bl = t->blocks[m.linear(m.index(b))];
 		CTG_CHECK(bl != nullptr, "missing dense block in the input tensor");
+		CTG_CHECK(bl->dtype == t->dtype, "dense block of another numeric type");
 		for (int i = 0; i < m.ndim; i++) CTG_CHECK(bl->dim[i] == m.dims(b)[i], "dense block shape mismatch");
-		memcpy(host.data() + m.boff[b], bl->data, (size_t)m.block_size(b) * sizeof(double));
+		memcpy(host.data() + m.boff[b] * w, bl->data, (size_t)m.block_size(b) * w * sizeof(double));
 	}
 	DTensor d;
 	d.meta = std::make_shared<const Meta>(std::move(m));
+	d.cplx = w == 2;
 	d.buf = c.upload(host.data(), host.size() * sizeof(double));
 	return d;
 }
 
 void tensor_to_struct(Ctx& c, const DTensor& t, struct block_sparse_tensor* out)
 {
-	std::vector<double> host((size_t)std::max<i64>(t.m().nnz, 1));
+	std::vector<double> host((size_t)std::max<i64>(t.m().nnz, 1) * t.width());
 	copy_to_host(c, t, host.data());
-	write_struct_host(t.m(), host.data(), out);
+	write_struct_host(t.m(), host.data(), out, t.cplx);
 }
 
-void write_struct_host(const Meta& m, const double* host, struct block_sparse_tensor* out)
+void write_struct_host(const Meta& m, const double* host, struct block_sparse_tensor* out, bool cplx)
 {
-	out->dtype = CT_DOUBLE_REAL;
+	const int w = cplx ? 2 : 1;
+	out->dtype = cplx ? CT_DOUBLE_COMPLEX : CT_DOUBLE_REAL;
 	out->ndim = m.ndim;
 	out->dim_logical = ct_copy(m.dim.data(), (size_t)m.ndim);
 	out->dim_blocks = ct_copy(m.nb.data(), (size_t)m.ndim);
@@ -114,10 +119,10 @@ void write_struct_host(const Meta& m, const double* host, struct block_sparse_te
 	for (int b = 0; b < m.nblocks; b++)
 	{
 		struct dense_tensor* d = (struct dense_tensor*)ct_alloc(sizeof(struct dense_tensor));
-		d->dtype = CT_DOUBLE_REAL;
+		d->dtype = out->dtype;
 		d->ndim = m.ndim;
 		d->dim = ct_copy(m.dims(b), (size_t)m.ndim);
-		d->data = ct_copy(host + m.boff[b], (size_t)m.block_size(b));
+		d->data = ct_copy(host + m.boff[b] * w, (size_t)m.block_size(b) * w);
 		out->blocks[m.linear(m.index(b))] = d;
 	}
 }
@@ -218,7 +223,9 @@ DTensor merge_mpo_pair(Ctx& c, const DTensor& w0, const DTensor& w1)
 // contraction_operator_step_left (src/algorithm/chain_ops.c:196-245), with b = a
 DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, int precision)
 {
+	// the bra: a with reversed axis directions, complex conjugated (chain_ops.c:204-215)
 	DTensor br = view_reversed(c, a);
+	br.conj = a.cplx;
 	DTensor s = op_dot(c, l, AX_TRAILING, br, AX_LEADING, 1, precision);
 	const int p0[5] = {0, 1, 4, 2, 3};
 	DTensor t = op_transpose(c, s, p0);
@@ -240,6 +247,7 @@ DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const
 	const int p1[5] = {4, 2, 0, 1, 3};
 	t = op_transpose(c, s, p1);
 	DTensor br = view_reversed(c, a);
+	br.conj = a.cplx;
 	s = op_dot(c, t, AX_TRAILING, br, AX_TRAILING, 2, precision);
 	const int p2[4] = {1, 2, 3, 0};
 	return op_transpose(c, s, p2);
@@ -248,16 +256,18 @@ DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const
 namespace {
 
 // create_dummy_operator_block_right / _left (src/algorithm/chain_ops.c:14-85)
-DTensor dummy_block(Ctx& c, const std::vector<q32>& qa, const std::vector<q32>& qw, const std::vector<q32>& qb, bool right)
+DTensor dummy_block(Ctx& c, const std::vector<q32>& qa, const std::vector<q32>& qw, const std::vector<q32>& qb, bool right,
+                    bool cplx = false)
 {
 	const i64 dim[6] = {1, 1, 1, 1, 1, 1};
 	const int dir[6] = {TENSOR_AXIS_OUT, TENSOR_AXIS_OUT, TENSOR_AXIS_IN, TENSOR_AXIS_IN, TENSOR_AXIS_IN, TENSOR_AXIS_OUT};
 	Meta m = make_meta(6, dim, dir, {qa, qw, qb, qa, qw, qb});
 	CTG_CHECK(m.nblocks == 1, "dummy operator block: unexpected structure");
-	const double one = 1.0;
+	const double one[2] = {1.0, 0.0};
 	DTensor s;
 	s.meta = std::make_shared<const Meta>(std::move(m));
-	s.buf = c.upload(&one, sizeof(double));
+	s.cplx = cplx;
+	s.buf = c.upload(one, (size_t)s.width() * sizeof(double));
 	if (right)
 	{
 		DTensor t = op_flatten(c, s, 4, TENSOR_AXIS_IN);
@@ -304,10 +314,10 @@ DTensor head_tensor(Ctx& c, const DTensor& a0, double value)
 	const i64 dim[3] = {a0.m().dim[0], 1, a0.m().dim[0]};
 	const int dir[3] = {TENSOR_AXIS_OUT, TENSOR_AXIS_OUT, TENSOR_AXIS_IN};
 	Meta m = make_meta(3, dim, dir, {a0.m().ql[0], std::vector<q32>{0}, a0.m().ql[0]});
-	DTensor h = c.zeros(m);
+	DTensor h = c.zeros(m, a0.cplx);
 	if (value != 0 && m.nblocks > 0)
 	{
-		std::vector<double> v((size_t)m.nnz, 0.0);
+		std::vector<double> v((size_t)m.nnz * h.width(), 0.0);
 		v[0] = value;
 		h.buf = c.upload(v.data(), v.size() * sizeof(double));
 	}
@@ -376,10 +386,17 @@ struct LocalH {
 	DBufPtr tt1, tt2;                // the two intermediates, in their transposed layouts
 	DBufPtr pk_r, pk_w, pk_k, pk_x, pk_t1, pk_t2;   // packed tensor-core operands
 	bool tc = false;
+	bool z = false;                  // complex128 entries
 	double flops = 0;
 
 	LocalH(Ctx& c, const Meta& a, const DTensor& w_, const DTensor& l, const DTensor& r_, int precision) : w(w_), r(r_)
 	{
+		z = w.cplx || l.cplx || r.cplx;
+		if (z)
+		{
+			CTG_CHECK(w.cplx && l.cplx && r.cplx, "local Hamiltonian: real and complex operands");
+			precision = GEMM_Z64;
+		}
 		// the reference's transposes {1,2,0,3,4} and {2,0,1,3,4} of the first two products are written
 		// by the GEMM epilogues (the results land in the transposed layouts), in FP64 and on the tensor
 		// cores alike; no separate transpose pass
@@ -401,9 +418,10 @@ struct LocalH {
 			same = o.dim[(size_t)i + 1] == a.dim[(size_t)i] && o.dir[(size_t)i + 1] == a.dir[(size_t)i] &&
 			       o.ql[(size_t)i + 1] == a.ql[(size_t)i];
 		CTG_CHECK(same, "local Hamiltonian output structure differs from the input");
-		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * sizeof(double));
-		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * sizeof(double));
-		flops = d1.flops + d2.flops + d3.flops;
+		const size_t wz = z ? 2 : 1;
+		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * wz * sizeof(double));
+		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * wz * sizeof(double));
+		flops = (z ? 4.0 : 1.0) * (d1.flops + d2.flops + d3.flops);
 		if (precision == GEMM_BF16X3)
 		{
 			// operands fixed for the bond (r, w, k) are packed once; x and the intermediates per apply
@@ -425,6 +443,13 @@ struct LocalH {
 	{
 		double* t1 = (double*)tt1->ptr;
 		double* t2 = (double*)tt2->ptr;
+		if (z)
+		{
+			d1.run_z(c, x, r.data(), t1, false, false);
+			d2.run_z(c, w.data(), t1, t2, false, false);
+			d3.run_z(c, k.data(), t2, y, false, false);
+			return;
+		}
 		if (tc)
 		{
 			d1.pack_a(c, x, pk_x->ptr);
@@ -452,7 +477,12 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 	double hz = now_s();
 	LocalH h(c, a_start.m(), w, l, r, precision);
 	g_host_detail[0] += now_s() - hz;
-	const i64 n = a_start.m().nnz;
+	CTG_CHECK(a_start.cplx == h.z, "local eigenproblem: start vector and operator of different numeric types");
+	// the vector as doubles (a complex128 vector is its real and imaginary parts: the Lanczos
+	// scalars alpha = Re <v, w> and beta = ||w|| of lanczos_iteration_z are the real ones of
+	// that vector, krylov.c:96-165); the breakdown test counts entries
+	const i64 nent = a_start.m().nnz;
+	const i64 n = nent * a_start.width();
 	DBuf V(&c, (size_t)maxiter * n * sizeof(double));
 	DBuf wv(&c, (size_t)n * sizeof(double));
 	DBuf partial(&c, 2 * RED_BLOCKS * sizeof(double));
@@ -474,12 +504,12 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 		{
 			const bool last = j == maxiter - 1;
 			KScope ks(c, K_LANCZOS, 1, last ? 2.0 * dn : 9.0 * dn, last ? 16.0 * dn : 72.0 * dn);
-			launch_lz_step(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, last ? wp : Vp + (i64)(j + 1) * n, n, j,
-			               last ? 1 : 0, pp, d_sc, s);
+			launch_lz_step(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, last ? wp : Vp + (i64)(j + 1) * n, n, nent,
+			               j, last ? 1 : 0, pp, d_sc, s);
 		}
 		g_host_detail[2] += now_s() - hz;
 	}
-	a_opt = c.empty(a_start.meta);
+	a_opt = c.empty(a_start.meta, a_start.cplx);
 	{
 		KScope ks(c, K_LANCZOS, 2, 2.0 * maxiter * dn, 8.0 * (maxiter + 1) * dn);
 		launch_lz_tridiag(maxiter, d_sc, s);
@@ -587,7 +617,7 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	{
 		DTensor head = head_tensor(c, A[0], 1.0);
 		if (ret == 0) ret = local_orthonormalize_rq(c, A[0], head);
-		std::vector<double> hv((size_t)std::max<i64>(head.m().nnz, 1), 0.0);
+		std::vector<double> hv((size_t)std::max<i64>(head.m().nnz, 1) * head.width(), 0.0);
 		if (head.m().nnz > 0) copy_to_host(c, head, hv.data());
 		double nrm = head.m().nblocks > 0 ? hv[0] : 0.0;
 		if (nrm < 0)
@@ -604,9 +634,9 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 
 	// environments and merged MPO pairs
 	std::vector<DTensor> lb(L), rb(L), h2(L - 1);
-	rb[L - 1] = dummy_block(c, A[L - 1].m().ql[2], W[L - 1].m().ql[3], A[L - 1].m().ql[2], true);
+	rb[L - 1] = dummy_block(c, A[L - 1].m().ql[2], W[L - 1].m().ql[3], A[L - 1].m().ql[2], true, A[L - 1].cplx);
 	for (int i = L - 1; i > 0; i--) rb[i - 1] = contraction_step_right(c, A[i], W[i], rb[i]);
-	lb[0] = dummy_block(c, A[0].m().ql[0], W[0].m().ql[0], A[0].m().ql[0], false);
+	lb[0] = dummy_block(c, A[0].m().ql[0], W[0].m().ql[0], A[0].m().ql[0], false, A[0].cplx);
 	for (int i = 1; i < L; i++) lb[i] = lb[0];
 	for (int i = 0; i < L - 1; i++) h2[i] = merge_mpo_pair(c, W[i], W[i + 1]);
 	c.sync();
@@ -838,7 +868,7 @@ int dmrg_singlesite_gpu(const struct mpo* H, int num_sweeps, int maxiter, struct
 	{
 		DTensor head = head_tensor(c, A[0], 1.0);
 		if (ret == 0) ret = local_orthonormalize_rq(c, A[0], head);
-		std::vector<double> hv((size_t)std::max<i64>(head.m().nnz, 1), 0.0);
+		std::vector<double> hv((size_t)std::max<i64>(head.m().nnz, 1) * head.width(), 0.0);
 		if (head.m().nnz > 0) copy_to_host(c, head, hv.data());
 		double nrm = head.m().nblocks > 0 ? hv[0] : 0.0;
 		if (nrm < 0)
@@ -854,9 +884,9 @@ int dmrg_singlesite_gpu(const struct mpo* H, int num_sweeps, int maxiter, struct
 
 	// environments (dmrg.c:175-182)
 	std::vector<DTensor> lb(L), rb(L);
-	rb[L - 1] = dummy_block(c, A[L - 1].m().ql[2], W[L - 1].m().ql[3], A[L - 1].m().ql[2], true);
+	rb[L - 1] = dummy_block(c, A[L - 1].m().ql[2], W[L - 1].m().ql[3], A[L - 1].m().ql[2], true, A[L - 1].cplx);
 	for (int i = L - 1; i > 0; i--) rb[i - 1] = contraction_step_right(c, A[i], W[i], rb[i]);
-	lb[0] = dummy_block(c, A[0].m().ql[0], W[0].m().ql[0], A[0].m().ql[0], false);
+	lb[0] = dummy_block(c, A[0].m().ql[0], W[0].m().ql[0], A[0].m().ql[0], false, A[0].cplx);
 	for (int i = 1; i < L; i++) lb[i] = lb[0];
 	c.sync();
 	const double t_setup = now_s();

@@ -82,7 +82,7 @@ Meta meta_from_struct(const struct block_sparse_tensor* t);
 DTensor tensor_from_struct(Ctx& c, const struct block_sparse_tensor* t);
 void tensor_to_struct(Ctx& c, const DTensor& t, struct block_sparse_tensor* out);
 // allocate a reference-layout tensor (aligned_alloc) holding host entries in block order
-void write_struct_host(const Meta& m, const double* host, struct block_sparse_tensor* out);
+void write_struct_host(const Meta& m, const double* host, struct block_sparse_tensor* out, bool cplx = false);
 void free_struct(struct block_sparse_tensor* t);
 
 }  // namespace ctg

@@ -345,41 +345,47 @@ DBufPtr Ctx::upload(const void* host, size_t bytes)
 	return b;
 }
 
-DTensor Ctx::empty(const Meta& m)
+DTensor Ctx::empty(const Meta& m, bool cplx)
 {
 	DTensor t;
 	t.meta = std::make_shared<const Meta>(m);
-	t.buf = std::make_shared<DBuf>(this, (size_t)std::max<i64>(m.nnz, 1) * sizeof(double));
+	t.cplx = cplx;
+	t.buf = std::make_shared<DBuf>(this, (size_t)std::max<i64>(m.nnz, 1) * t.width() * sizeof(double));
 	return t;
 }
 
-DTensor Ctx::empty(const std::shared_ptr<const Meta>& m)
+DTensor Ctx::empty(const std::shared_ptr<const Meta>& m, bool cplx)
 {
 	DTensor t;
 	t.meta = m;
-	t.buf = std::make_shared<DBuf>(this, (size_t)std::max<i64>(m->nnz, 1) * sizeof(double));
+	t.cplx = cplx;
+	t.buf = std::make_shared<DBuf>(this, (size_t)std::max<i64>(m->nnz, 1) * t.width() * sizeof(double));
 	return t;
 }
 
-DTensor Ctx::zeros(const Meta& m)
+DTensor Ctx::zeros(const Meta& m, bool cplx)
 {
-	DTensor t = empty(m);
-	CTG_CUDA(cudaMemsetAsync(t.data(), 0, (size_t)std::max<i64>(m.nnz, 1) * sizeof(double), st_));
+	DTensor t = empty(m, cplx);
+	CTG_CUDA(cudaMemsetAsync(t.data(), 0, (size_t)std::max<i64>(m.nnz, 1) * t.width() * sizeof(double), st_));
 	return t;
 }
 
 void copy_to_device(Ctx& c, DTensor& t, const double* host)
 {
 	if (t.m().nnz == 0) return;
-	DBufPtr b = c.upload(host, (size_t)t.m().nnz * sizeof(double));
+	DBufPtr b = c.upload(host, (size_t)t.m().nnz * t.width() * sizeof(double));
 	t.buf = b;
 }
 
 void copy_to_host(Ctx& c, const DTensor& t, double* host)
 {
 	if (t.m().nnz == 0) return;
-	CTG_CUDA(cudaMemcpyAsync(host, t.data(), (size_t)t.m().nnz * sizeof(double), cudaMemcpyDeviceToHost, c.stream()));
+	CTG_CUDA(cudaMemcpyAsync(host, t.data(), (size_t)t.m().nnz * t.width() * sizeof(double), cudaMemcpyDeviceToHost,
+	                         c.stream()));
 	c.sync();
+	// a conjugated view is handed out with its conjugation applied
+	if (t.conj)
+		for (i64 i = 0; i < t.m().nnz; i++) host[2 * i + 1] = -host[2 * i + 1];
 }
 
 // ------------------------------------------------------------------------------------
@@ -415,7 +421,19 @@ const T* at(const DBufPtr& b, size_t off)
 static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
                               const int* out_perm)
 {
-	DotLowering l = lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm);
+	// complex128: the FP64 work lists (outputs, contributions) with tiles of the complex GEMM
+	const bool z = precision == GEMM_Z64;
+	DotLowering l = lower_dot(s, axs, t, axt, nmult, z ? (int)GEMM_FP64 : precision, c.num_sms(), out_perm);
+	std::vector<ZTile> zt;
+	if (z)
+	{
+		for (size_t b = 0; b < l.outs.size(); b++)
+			for (int m0 = 0; m0 < l.outs[b].m; m0 += 32)
+				for (int n0 = 0; n0 < l.outs[b].n; n0 += 32) zt.push_back(ZTile{(int)b, m0, n0, 0});
+		l.tiles.clear();
+		l.splits.clear();
+		l.work_doubles = 0;
+	}
 	DotPlan p;
 	p.out = l.out;
 	p.precision = precision;
@@ -425,7 +443,10 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	const size_t o_tiles = pk.add(l.tiles);
 	const size_t o_splits = pk.add(l.splits);
 	const size_t o_tcons = pk.add(l.tcons), o_apacks = pk.add(l.apacks), o_bpacks = pk.add(l.bpacks);
+	const size_t o_zt = pk.add(zt);
 	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	p.nztiles = (int)zt.size();
+	p.ztiles = at<ZTile>(p.desc, o_zt);
 	p.tcons = at<TcContrib>(p.desc, o_tcons);
 	p.apacks = at<TcPack>(p.desc, o_apacks);
 	p.bpacks = at<TcPack>(p.desc, o_bpacks);
@@ -476,6 +497,14 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 	c.gemm_flops += flops;
 }
 
+void DotPlan::run_z(Ctx& c, const double* A, const double* B, double* C, bool conj_a, bool conj_b) const
+{
+	CTG_CHECK(precision == GEMM_Z64, "complex GEMM on a real plan");
+	KScope ks(c, K_GEMM, 1, 4.0 * flops, 0);
+	launch_gemm_z(nztiles, ztiles, outs, cons, A, B, C, conj_a ? 1 : 0, conj_b ? 1 : 0, c.stream());
+	c.gemm_flops += 4.0 * flops;
+}
+
 void DotPlan::pack_a(Ctx& c, const double* A, void* apack) const
 {
 	KScope ks(c, K_GEMM_TC, 1, 0, 8.0 * (double)a_entries + (double)a_recs * TC_A_REC_BYTES);
@@ -501,12 +530,12 @@ void DotPlan::run_packed(Ctx& c, const void* apack, const void* bpack, double* C
 // data movement plans
 // ------------------------------------------------------------------------------------
 
-void CopyPlan::run(Ctx& c, const double* src, double* dst) const
+void CopyPlan::run(Ctx& c, const double* src, double* dst, bool cplx) const
 {
 	if (nchunks == 0) return;
-	KScope ks(c, kind == 0 ? K_PERMUTE : K_ROWMAP, 1, 0, 16.0 * (double)elements);
-	if (kind == 0) launch_permute(nchunks, chunks, (const PermDesc*)descs, src, dst, c.stream());
-	else launch_rowmap(nchunks, chunks, (const RowDesc*)descs, maps, src, dst, c.stream());
+	KScope ks(c, kind == 0 ? K_PERMUTE : K_ROWMAP, 1, 0, (cplx ? 32.0 : 16.0) * (double)elements);
+	if (kind == 0) launch_permute(nchunks, chunks, (const PermDesc*)descs, src, dst, c.stream(), cplx);
+	else launch_rowmap(nchunks, chunks, (const RowDesc*)descs, maps, src, dst, c.stream(), cplx);
 }
 
 static CopyPlan upload_copy(Ctx& c, CopyLowering&& l)
@@ -639,6 +668,16 @@ CopyPlan make_slice_plan(Ctx& c, const Meta& t, int ax, const std::vector<i64>& 
 
 DTensor op_dot(Ctx& c, const DTensor& s, int axs, const DTensor& t, int axt, int nmult, int precision)
 {
+	if (s.cplx || t.cplx)
+	{
+		CTG_CHECK(s.cplx && t.cplx, "dot: real and complex operands");
+		DotPlan p = make_dot_plan(c, s.m(), axs, t.m(), axt, nmult, GEMM_Z64);
+		DTensor r = c.empty(p.out, true);
+		if (p.out->nnz > 0)
+			CTG_CUDA(cudaMemsetAsync(r.data(), 0, (size_t)p.out->nnz * 2 * sizeof(double), c.stream()));
+		p.run_z(c, s.data(), t.data(), r.data(), s.conj, t.conj);
+		return r;
+	}
 	DotPlan p = make_dot_plan(c, s.m(), axs, t.m(), axt, nmult, precision);
 	DTensor r;
 	r.meta = p.out;
@@ -649,10 +688,12 @@ DTensor op_dot(Ctx& c, const DTensor& s, int axs, const DTensor& t, int axt, int
 
 static DTensor run_copy(Ctx& c, const CopyPlan& p, const DTensor& src)
 {
+	CTG_CHECK(!src.conj, "copy of a conjugated view");
 	DTensor r;
 	r.meta = p.out;
-	r.buf = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(p.out->nnz, 1) * sizeof(double));
-	p.run(c, src.data(), r.data());
+	r.cplx = src.cplx;
+	r.buf = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(p.out->nnz, 1) * r.width() * sizeof(double));
+	p.run(c, src.data(), r.data(), src.cplx);
 	return r;
 }
 
@@ -683,11 +724,13 @@ DTensor op_scale_axis(Ctx& c, const DTensor& s, const double* dvec, int axrange)
 		PlanTimer plan_timer(c);
 		p = cached_copy(c, 5, {axrange}, s.m(), [&] { return upload_copy(c, lower_scale(s.m(), axrange)); });
 	}
-	DTensor r = c.empty(s.meta);
+	CTG_CHECK(!s.conj, "scaling of a conjugated view");
+	DTensor r = c.empty(s.meta, s.cplx);
 	if (p.nchunks > 0)
 	{
-		KScope ks(c, K_SCALE, 1, 0, 16.0 * (double)s.m().nnz);
-		launch_scale_axis(p.nchunks, p.chunks, (const ScaleDesc*)p.descs, p.maps, dvec, s.data(), r.data(), c.stream());
+		KScope ks(c, K_SCALE, 1, 0, 16.0 * s.width() * (double)s.m().nnz);
+		launch_scale_axis(p.nchunks, p.chunks, (const ScaleDesc*)p.descs, p.maps, dvec, s.data(), r.data(), c.stream(),
+		                  s.cplx);
 	}
 	return r;
 }
@@ -706,6 +749,8 @@ DTensor view_reversed(Ctx& c, const DTensor& t)
 	DTensor r;
 	r.meta = p.out;
 	r.buf = t.buf;
+	r.cplx = t.cplx;
+	r.conj = t.conj;
 	return r;
 }
 
@@ -723,6 +768,8 @@ DTensor view_trace_unit(const DTensor& t)
 	DTensor o;
 	o.meta = std::make_shared<const Meta>(std::move(r));
 	o.buf = t.buf;
+	o.cplx = t.cplx;
+	o.conj = t.conj;
 	return o;
 }
 
@@ -762,8 +809,9 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 	const i64 dv[2] = {ni, am.dim[1]};
 	const int dirv[2] = {-am.dir[1], am.dir[1]};
 	Meta mv = make_meta(2, dv, dirv, {qi, am.ql[1]});
-	res.u = c.zeros(mu);
-	res.vh = c.zeros(mv);
+	CTG_CHECK(!a.conj, "svd of a conjugated view");
+	res.u = c.zeros(mu, a.cplx);
+	res.vh = c.zeros(mv, a.cplx);
 	res.ns = ni;
 	res.s = std::make_shared<DBuf>(&c, (size_t)ni * sizeof(double));
 	CTG_CUDA(cudaMemsetAsync(res.s->ptr, 0, (size_t)ni * sizeof(double), c.stream()));
@@ -773,7 +821,42 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 		const int b = mu.find(idx);
 		CTG_CHECK(b >= 0, "svd: dummy block missing");
 		static const double one = 1.0;
-		CTG_CUDA(cudaMemcpyAsync(res.u.data() + mu.boff[b], &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
+		CTG_CUDA(cudaMemcpyAsync(res.u.data() + mu.boff[b] * res.u.width(), &one, sizeof(double), cudaMemcpyHostToDevice,
+		                         c.stream()));
+		return 0;
+	}
+	if (a.cplx)
+	{
+		// complex128: one-sided complex Jacobi per block (offsets in complex elements)
+		std::vector<SvdDesc> zd;
+		i64 zw = 0;
+		for (const Blk& bl : blks)
+		{
+			const i64* ia = am.index(bl.ab);
+			const i64 kb = mu.find_q(1, am.qb[1][ia[1]]);
+			const i64 iu[2] = {ia[0], kb}, iv[2] = {kb, ia[1]};
+			const int bu = mu.find(iu), bv = mv.find(iv);
+			CTG_CHECK(bu >= 0 && bv >= 0, "svd: factor blocks missing");
+			i64 first = 0;
+			while (mu.ql[1][(size_t)first] != am.qb[1][ia[1]]) first++;
+			SvdDesc d = {};
+			d.a_off = am.boff[bl.ab];
+			d.u_off = mu.boff[bu];
+			d.v_off = mv.boff[bv];
+			d.s_off = first;
+			d.w_off = zw;
+			d.m = (int)bl.m;
+			d.n = (int)bl.n;
+			zw += svd_z_scratch(d.m, d.n);
+			zd.push_back(d);
+		}
+		DBufPtr desc = c.upload(zd.data(), zd.size() * sizeof(SvdDesc));
+		DBuf scratch(&c, (size_t)std::max<i64>(zw, 1) * 2 * sizeof(double));
+		pend.zstatus = std::make_shared<DBuf>(&c, zd.size() * sizeof(int));
+		pend.zblocks = (int)zd.size();
+		KScope ks(c, K_SVD, 1);
+		launch_svd_z((int)zd.size(), (const SvdDesc*)desc->ptr, a.data(), res.u.data(), (double*)res.s->ptr,
+		             res.vh.data(), (double*)scratch.ptr, (int*)pend.zstatus->ptr, c.stream());
 		return 0;
 	}
 	std::vector<SvdDesc> descs;
@@ -941,6 +1024,18 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 
 int op_svd_finish(Ctx& c, const SvdPending& pend)
 {
+	if (pend.zblocks > 0)
+	{
+		std::vector<int> st((size_t)pend.zblocks);
+		CTG_CUDA(cudaMemcpy(st.data(), pend.zstatus->ptr, st.size() * sizeof(int), cudaMemcpyDeviceToHost));
+		for (int v : st)
+			if (v != 0)
+			{
+				fprintf(stderr, "ctgpu: complex block SVD did not converge\n");
+				return -1;
+			}
+		return 0;
+	}
 	if (pend.descs.empty()) return 0;
 	c.svd_flops += *c.svd_flops_host() + pend.other_flops;
 	const int* hst = c.svd_status_host();
@@ -1009,15 +1104,16 @@ int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q)
 	Meta mr = make_meta(2, dr, dirr, {am.ql[0], qi});
 	const i64 dq[2] = {ni, am.dim[1]};
 	Meta mq = make_meta(2, dq, am.dir.data(), {qi, am.ql[1]});
-	r = c.zeros(mr);
-	q = c.zeros(mq);
+	CTG_CHECK(!a.conj, "rq of a conjugated view");
+	r = c.zeros(mr, a.cplx);
+	q = c.zeros(mq, a.cplx);
 	if (dummy)
 	{
 		const i64 idx[2] = {(i64)mq.find_q(0, qi[0]), 0};
 		const int b = mq.find(idx);
 		CTG_CHECK(b >= 0, "rq: dummy block missing");
 		static const double one = 1.0;
-		CTG_CUDA(cudaMemcpyAsync(q.data() + mq.boff[b], &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
+		CTG_CUDA(cudaMemcpyAsync(q.data() + mq.boff[b] * q.width(), &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
 		c.sync();
 		return 0;
 	}
@@ -1042,10 +1138,13 @@ int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q)
 		descs.push_back(d);
 	}
 	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(RqDesc));
-	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
+	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * a.width() * sizeof(double));
 	KScope ks(c, K_RQ, 1);
-	launch_rq_householder((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr,
-	                      c.stream());
+	if (a.cplx)
+		launch_qr_z((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr, c.stream());
+	else
+		launch_rq_householder((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr,
+		                      c.stream());
 	return 0;
 }
 
@@ -1079,15 +1178,16 @@ int op_qr(Ctx& c, const DTensor& a, DTensor& q, DTensor& r)
 	const i64 dr[2] = {ni, am.dim[1]};
 	const int dirr[2] = {-am.dir[1], am.dir[1]};
 	Meta mr = make_meta(2, dr, dirr, {qi, am.ql[1]});
-	q = c.zeros(mq);
-	r = c.zeros(mr);
+	CTG_CHECK(!a.conj, "qr of a conjugated view");
+	q = c.zeros(mq, a.cplx);
+	r = c.zeros(mr, a.cplx);
 	if (dummy)
 	{
 		const i64 idx[2] = {0, (i64)mq.find_q(1, qi[0])};
 		const int b = mq.find(idx);
 		CTG_CHECK(b >= 0, "qr: dummy block missing");
 		static const double one = 1.0;
-		CTG_CUDA(cudaMemcpyAsync(q.data() + mq.boff[b], &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
+		CTG_CUDA(cudaMemcpyAsync(q.data() + mq.boff[b] * q.width(), &one, sizeof(double), cudaMemcpyHostToDevice, c.stream()));
 		c.sync();
 		return 0;
 	}
@@ -1112,10 +1212,13 @@ int op_qr(Ctx& c, const DTensor& a, DTensor& q, DTensor& r)
 		descs.push_back(d);
 	}
 	DBufPtr desc = c.upload(descs.data(), descs.size() * sizeof(RqDesc));
-	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * sizeof(double));
+	DBuf scratch(&c, (size_t)std::max<i64>(woff, 1) * a.width() * sizeof(double));
 	KScope ks(c, K_RQ, 1);
-	launch_rq_householder((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr,
-	                      c.stream());
+	if (a.cplx)
+		launch_qr_z((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr, c.stream());
+	else
+		launch_rq_householder((int)descs.size(), (const RqDesc*)desc->ptr, a.data(), r.data(), q.data(), (double*)scratch.ptr,
+		                      c.stream());
 	return 0;
 }
 

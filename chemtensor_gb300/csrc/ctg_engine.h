@@ -50,8 +50,11 @@ using DBufPtr = std::shared_ptr<DBuf>;
 struct DTensor {
 	std::shared_ptr<const Meta> meta;
 	DBufPtr buf;
+	bool cplx = false;      // complex128 entries (interleaved real and imaginary parts)
+	bool conj = false;      // read as complex conjugate (a view; only dots honour it)
 	double* data() const { return buf ? (double*)buf->ptr : nullptr; }
 	const Meta& m() const { return *meta; }
+	int width() const { return cplx ? 2 : 1; }    // doubles per entry
 };
 
 // Execution context: one CUDA stream, a private memory pool and a pinned staging
@@ -77,9 +80,9 @@ public:
 	DBufPtr upload(const void* host, size_t bytes);
 	// block until the stream is idle; recycles the staging arena
 	void sync();
-	DTensor empty(const Meta& m);
-	DTensor empty(const std::shared_ptr<const Meta>& m);   // shares the structure, no copy
-	DTensor zeros(const Meta& m);
+	DTensor empty(const Meta& m, bool cplx = false);
+	DTensor empty(const std::shared_ptr<const Meta>& m, bool cplx = false);   // shares the structure, no copy
+	DTensor zeros(const Meta& m, bool cplx = false);
 	// statistics
 	double gemm_flops = 0;       // algorithmic GEMM FLOPs issued
 	long kernel_launches = 0;
@@ -175,7 +178,12 @@ struct DotPlan {
 	double flops = 0;
 	double flops_cls[NUM_TILE_CLASSES] = {};
 	int precision = GEMM_FP64;
+	// complex128 (precision GEMM_Z64): tiles of the complex GEMM
+	int nztiles = 0;
+	const ZTile* ztiles = nullptr;
 	void run(Ctx& c, const double* A, const double* B, double* C) const;
+	// complex128 entries, operands optionally read conjugated
+	void run_z(Ctx& c, const double* A, const double* B, double* C, bool conj_a, bool conj_b) const;
 	// tensor-core path in parts, so that an operand used by many runs is packed once
 	void pack_a(Ctx& c, const double* A, void* apack) const;      // a_recs * TC_A_REC_BYTES bytes
 	void pack_b(Ctx& c, const double* B, void* bpack) const;      // b_recs * TC_B_REC_BYTES bytes
@@ -195,7 +203,7 @@ struct CopyPlan {
 	const void* descs = nullptr;
 	const i64* maps = nullptr;
 	i64 elements = 0;            // entries moved
-	void run(Ctx& c, const double* src, double* dst) const;
+	void run(Ctx& c, const double* src, double* dst, bool cplx = false) const;
 };
 CopyPlan make_transpose_plan(Ctx& c, const Meta& t, const int* perm);
 CopyPlan make_flatten_plan(Ctx& c, const Meta& t, int ax, int newdir);
@@ -229,6 +237,8 @@ struct SvdPending {
 	size_t launches = 0;
 	DTensor a;
 	double other_flops = 0;      // QR and output flops (host estimate at full rank)
+	DBufPtr zstatus;             // complex128: per-block convergence status
+	int zblocks = 0;
 };
 // enqueue the SVD without waiting for it; its status reaches pinned host memory when the stream
 // gets there, so op_svd_finish may run only after a synchronisation of c's stream

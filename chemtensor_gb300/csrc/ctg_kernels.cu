@@ -210,9 +210,11 @@ void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, con
 // block permutation (dense_tensor_transpose, dense_tensor.c:799-932)
 // ------------------------------------------------------------------------------------
 
+// T = double, or double2 for complex128 entries (same descriptors, element units)
+template <class T>
 __global__ void __launch_bounds__(256)
-k_permute(const Chunk* __restrict__ chunks, const PermDesc* __restrict__ descs, const double* __restrict__ src,
-          double* __restrict__ dst)
+k_permute(const Chunk* __restrict__ chunks, const PermDesc* __restrict__ descs, const T* __restrict__ src,
+          T* __restrict__ dst)
 {
 	const Chunk ch = chunks[blockIdx.x];
 	const PermDesc d = descs[ch.desc];
@@ -248,10 +250,12 @@ k_permute(const Chunk* __restrict__ chunks, const PermDesc* __restrict__ descs, 
 	}
 }
 
-void launch_permute(int nchunks, const Chunk* chunks, const PermDesc* descs, const double* src, double* dst, cudaStream_t st)
+void launch_permute(int nchunks, const Chunk* chunks, const PermDesc* descs, const double* src, double* dst, cudaStream_t st,
+                    bool cplx)
 {
 	if (nchunks <= 0) return;
-	k_permute<<<nchunks, 256, 0, st>>>(chunks, descs, src, dst);
+	if (cplx) k_permute<double2><<<nchunks, 256, 0, st>>>(chunks, descs, (const double2*)src, (double2*)dst);
+	else k_permute<double><<<nchunks, 256, 0, st>>>(chunks, descs, src, dst);
 	CTG_CUDA(cudaGetLastError());
 }
 
@@ -259,9 +263,10 @@ void launch_permute(int nchunks, const Chunk* chunks, const PermDesc* descs, con
 // row maps: flatten / split / slice (block_sparse_tensor.c:950-1553)
 // ------------------------------------------------------------------------------------
 
+template <class T>
 __global__ void __launch_bounds__(256)
 k_rowmap(const Chunk* __restrict__ chunks, const RowDesc* __restrict__ descs, const i64* __restrict__ maps,
-         const double* __restrict__ src, double* __restrict__ dst)
+         const T* __restrict__ src, T* __restrict__ dst)
 {
 	const Chunk ch = chunks[blockIdx.x];
 	const RowDesc d = descs[ch.desc];
@@ -282,10 +287,11 @@ k_rowmap(const Chunk* __restrict__ chunks, const RowDesc* __restrict__ descs, co
 }
 
 void launch_rowmap(int nchunks, const Chunk* chunks, const RowDesc* descs, const i64* maps, const double* src, double* dst,
-                   cudaStream_t st)
+                   cudaStream_t st, bool cplx)
 {
 	if (nchunks <= 0) return;
-	k_rowmap<<<nchunks, 256, 0, st>>>(chunks, descs, maps, src, dst);
+	if (cplx) k_rowmap<double2><<<nchunks, 256, 0, st>>>(chunks, descs, maps, (const double2*)src, (double2*)dst);
+	else k_rowmap<double><<<nchunks, 256, 0, st>>>(chunks, descs, maps, src, dst);
 	CTG_CUDA(cudaGetLastError());
 }
 
@@ -294,9 +300,13 @@ void launch_rowmap(int nchunks, const Chunk* chunks, const RowDesc* descs, const
 // block_sparse_tensor.c:1654-1703)
 // ------------------------------------------------------------------------------------
 
+__device__ __forceinline__ double scale_entry(double x, double f) { return x * f; }
+__device__ __forceinline__ double2 scale_entry(double2 x, double f) { return make_double2(x.x * f, x.y * f); }
+
+template <class T>
 __global__ void __launch_bounds__(256)
 k_scale_axis(const Chunk* __restrict__ chunks, const ScaleDesc* __restrict__ descs, const i64* __restrict__ maps,
-             const double* __restrict__ vec, const double* __restrict__ src, double* __restrict__ dst)
+             const double* __restrict__ vec, const T* __restrict__ src, T* __restrict__ dst)
 {
 	const Chunk ch = chunks[blockIdx.x];
 	const ScaleDesc d = descs[ch.desc];
@@ -305,15 +315,16 @@ k_scale_axis(const Chunk* __restrict__ chunks, const ScaleDesc* __restrict__ des
 	for (i64 e = ch.start + threadIdx.x; e < end; e += blockDim.x)
 	{
 		const i64 p = (e / d.ntrail) % d.nax;
-		dst[d.off + e] = src[d.off + e] * vec[maps[d.map_off + p]];
+		dst[d.off + e] = scale_entry(src[d.off + e], vec[maps[d.map_off + p]]);
 	}
 }
 
 void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs, const i64* maps, const double* vec,
-                       const double* src, double* dst, cudaStream_t st)
+                       const double* src, double* dst, cudaStream_t st, bool cplx)
 {
 	if (nchunks <= 0) return;
-	k_scale_axis<<<nchunks, 256, 0, st>>>(chunks, descs, maps, vec, src, dst);
+	if (cplx) k_scale_axis<double2><<<nchunks, 256, 0, st>>>(chunks, descs, maps, vec, (const double2*)src, (double2*)dst);
+	else k_scale_axis<double><<<nchunks, 256, 0, st>>>(chunks, descs, maps, vec, src, dst);
 	CTG_CUDA(cudaGetLastError());
 }
 

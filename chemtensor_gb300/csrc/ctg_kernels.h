@@ -136,9 +136,11 @@ struct Chunk {
 
 constexpr int COPY_CHUNK = 4096;
 
-void launch_permute(int nchunks, const Chunk* chunks, const PermDesc* descs, const double* src, double* dst, cudaStream_t st);
+// cplx: entries are complex128 (two doubles each); descriptors count entries
+void launch_permute(int nchunks, const Chunk* chunks, const PermDesc* descs, const double* src, double* dst, cudaStream_t st,
+                    bool cplx = false);
 void launch_rowmap(int nchunks, const Chunk* chunks, const RowDesc* descs, const i64* maps, const double* src, double* dst,
-                   cudaStream_t st);
+                   cudaStream_t st, bool cplx = false);
 
 // Multiply entries along one axis of each block by vec[map[position]]:
 // entry (lead, p, trail) of a block of shape (nlead, nax, ntrail) is scaled by vec[map[map_off + p]].
@@ -148,7 +150,7 @@ struct ScaleDesc {
 	i64 map_off;
 };
 void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs, const i64* maps, const double* vec,
-                       const double* src, double* dst, cudaStream_t st);
+                       const double* src, double* dst, cudaStream_t st, bool cplx = false);
 
 // ---- dense linear algebra per block ---------------------------------------------
 // SVD of a row-major m x n block: u (m x k), s (k), vh (k x n), k = min(m, n), singular values
@@ -201,6 +203,24 @@ struct RqDesc {
 void launch_rq_householder(int nblocks, const RqDesc* descs, const double* a, double* r, double* q, double* scratch,
                            cudaStream_t st);
 
+// ---- complex128 (interleaved real / imaginary parts, element offsets and strides) -------
+// Tiles of the complex block GEMM: 32 x 32 of output block `out`, all of its contributions.
+struct ZTile {
+	int out, m0, n0, pad;
+};
+// C = sum op(A) op(B) over the same GemmOut / GemmContrib lists as the FP64 GEMM; conj_a / conj_b
+// conjugate the operand's entries as they are read.
+void launch_gemm_z(int ntiles, const ZTile* tiles, const GemmOut* outs, const GemmContrib* cons, const double* A,
+                   const double* B, double* C, int conj_a, int conj_b, cudaStream_t st);
+// complex SVD of each block (SvdDesc offsets in complex elements, s_off in doubles, w_off in
+// complex elements of scratch); status[b] = 1 if block b did not converge
+i64 svd_z_scratch(int m, int n);
+void launch_svd_z(int nblocks, const SvdDesc* descs, const double* a, double* u, double* s, double* vh, double* work,
+                  int* status, cudaStream_t st);
+// complex QR / RQ of each block (RqDesc offsets in complex elements; scratch of
+// m n + max(m, n) min(m, n) + min(m, n) complex elements per block)
+void launch_qr_z(int nblocks, const RqDesc* descs, const double* a, double* r, double* q, double* scratch, cudaStream_t st);
+
 // ---- Lanczos (krylov.c:24-89) ------------------------------------------------------
 // Device-resident scalars of one Lanczos run.
 constexpr int LANCZOS_MAX = 32;     // largest maxiter_lanczos accepted
@@ -222,7 +242,9 @@ constexpr int RED_BLOCKS = 608;     // 4 x 152 SMs: fixed grid for deterministic
 // one cooperative launch each (partial: 2 RED_BLOCKS doubles): a whole Lanczos step
 // (alpha; unless last: orthogonalisation, beta and the early exit, next vector), and the start
 // vector's normalisation
-void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, int j, int last,
+// n doubles per vector (a complex128 vector counts twice); the breakdown test beta < 100 nthr eps
+// uses nthr, the number of entries (krylov.c:62, :129)
+void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, i64 nthr, int j, int last,
                     double* partial, LanczosScalars* sc, cudaStream_t st);
 void launch_lz_start(const double* v0, double* v, i64 n, double* partial, LanczosScalars* sc, cudaStream_t st);
 void launch_lz_tridiag(int maxiter, LanczosScalars* sc, cudaStream_t st);

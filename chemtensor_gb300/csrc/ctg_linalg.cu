@@ -210,7 +210,7 @@ __device__ double final_sum(const double* partial)
 // waits for another except at the two grid barriers. `partial` holds 2 RED_BLOCKS doubles.
 __global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
 k_lz_step(double* __restrict__ w, const double* __restrict__ vj, const double* __restrict__ vjm1,
-          double* __restrict__ vj1, i64 n, int j, int last, double* __restrict__ partial, LanczosScalars* sc)
+          double* __restrict__ vj1, i64 n, i64 nthr, int j, int last, double* __restrict__ partial, LanczosScalars* sc)
 {
 	cg::grid_group grid = cg::this_grid();
 	if (sc->stopped) return;               // read before the first barrier: the same in every block
@@ -234,7 +234,7 @@ k_lz_step(double* __restrict__ w, const double* __restrict__ vj, const double* _
 	block_partial(v, partial + RED_BLOCKS);
 	grid.sync();
 	const double b = sqrt(final_sum(partial + RED_BLOCKS));
-	const bool stop = b < 100.0 * (double)n * DBL_EPSILON;
+	const bool stop = b < 100.0 * (double)nthr * DBL_EPSILON;
 	if (blockIdx.x == 0 && threadIdx.x == 0)
 	{
 		sc->beta[j] = b;
@@ -285,11 +285,11 @@ static void check_coop(const void* fn)
 	ok[which].store(1);
 }
 
-void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, int j, int last,
+void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, i64 nthr, int j, int last,
                     double* partial, LanczosScalars* sc, cudaStream_t st)
 {
 	check_coop((const void*)k_lz_step);
-	void* args[] = {&w, (void*)&vj, (void*)&vjm1, &vj1, &n, &j, &last, &partial, &sc};
+	void* args[] = {&w, (void*)&vj, (void*)&vjm1, &vj1, &n, &nthr, &j, &last, &partial, &sc};
 	CTG_CUDA(cudaLaunchCooperativeKernel((const void*)k_lz_step, dim3(RED_BLOCKS), dim3(RED_THREADS), args, 0, st));
 }
 

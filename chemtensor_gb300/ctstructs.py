@@ -351,9 +351,12 @@ def free_mpo(c: MPO) -> None:
 # ---------------------------------------------------------------------------
 
 def bst_to_arrays(prefix: str, t: BlockSparse) -> dict:
+    cplx = t.dtype == CT_DOUBLE_COMPLEX
     out = {f"{prefix}_dim": np.array(t.dim_logical, dtype=np.int64),
            f"{prefix}_dir": np.array(t.axis_dir, dtype=np.int32),
-           f"{prefix}_data": t.serialize().astype(np.float64)}
+           f"{prefix}_data": t.serialize().astype(np.complex128 if cplx else np.float64)}
+    if cplx:
+        out[f"{prefix}_dtype"] = np.array(CT_DOUBLE_COMPLEX)
     for i, q in enumerate(t.qnums_logical):
         out[f"{prefix}_q{i}"] = np.asarray(q, dtype=np.int32)
     return out
@@ -363,8 +366,9 @@ def bst_from_arrays(prefix: str, arr) -> BlockSparse:
     dim = [int(x) for x in arr[f"{prefix}_dim"]]
     dirs = [int(x) for x in arr[f"{prefix}_dir"]]
     qn = [np.asarray(arr[f"{prefix}_q{i}"], dtype=np.int32) for i in range(len(dim))]
-    t = BlockSparse(dim, dirs, qn)
-    data = np.asarray(arr[f"{prefix}_data"], dtype=np.float64)
+    cplx = f"{prefix}_dtype" in arr and int(arr[f"{prefix}_dtype"]) == CT_DOUBLE_COMPLEX
+    t = BlockSparse(dim, dirs, qn, dtype=CT_DOUBLE_COMPLEX if cplx else CT_DOUBLE_REAL)
+    data = np.asarray(arr[f"{prefix}_data"], dtype=np.complex128 if cplx else np.float64)
     off = 0
     for idx in t.allowed:
         shp = t.block_shape(idx)

@@ -17,7 +17,10 @@ drives it through ctypes and stores, as .npz:
 * the spin-orbital molecular Hamiltonian MPO (src/operator/hamiltonian.c:2768) and a
   dmrg_twosite run on it.
 
-Run from the repository root:  python tests/golden/make_golden.py [singlesite|qr|molecular]
+* complex128 runs of dmrg_twosite and dmrg_singlesite (complex gauge on the MPO bonds,
+  complex random start states).
+
+Run from the repository root:  python tests/golden/make_golden.py [singlesite|qr|molecular|complex]
 (with an argument, only that group of fixtures is written).
 """
 
@@ -204,6 +207,56 @@ def molecular_cases():
     print("dmrg_molecular_n6_D32.npz E =", en[sweeps - 1])
 
 
+def complex_mpo(model, L, seed, **kw):
+    """The reference's real MPO turned complex by random phases on its virtual bonds
+    (W_i[..., k] *= e^{i t_k}, W_{i+1}[k, ...] *= e^{-i t_k}): the same Hermitian operator,
+    complex128 entries throughout."""
+    ch = cs.read_mpo(mpo(model, L, **kw))
+    rng = np.random.default_rng(seed)
+    ts = []
+    for t in ch.tensors:
+        z = cs.BlockSparse(t.dim_logical, t.axis_dir, t.qnums_logical, dtype=cs.CT_DOUBLE_COMPLEX)
+        for idx, b in t.blocks.items():
+            z.blocks[idx] = b.astype(np.complex128)
+        ts.append(z)
+    for i in range(L - 1):
+        ph = np.exp(1j * rng.uniform(0.0, 2 * np.pi, size=ts[i].dim_logical[3]))
+        for t, ax, sgn in ((ts[i], 3, 1), (ts[i + 1], 0, -1)):
+            for idx in list(t.blocks):
+                sel = np.nonzero(t.qnums_logical[ax] == t.qnums_blocks[ax][idx[ax]])[0]
+                shape = [1, 1, 1, 1]
+                shape[ax] = len(sel)
+                t.blocks[idx] = t.blocks[idx] * (ph[sel] if sgn > 0 else np.conj(ph[sel])).reshape(shape)
+    return cs.Chain(ts, ch.qsite, ch.d)
+
+
+def complex_cases():
+    """dmrg_twosite and dmrg_singlesite in complex128 (CT_DOUBLE_COMPLEX): Fermi-Hubbard chain with
+    a complex gauge on the MPO bonds and complex random start states (construct_random_mps)."""
+    for name, L, D, sweeps, maxiter, seed, single in (("dmrg_complex_hubbard_L6_D32.npz", 6, 32, 3, 5, 29, False),
+                                                      ("dmrg1_complex_hubbard_L6_D24.npz", 6, 24, 3, 5, 31, True)):
+        Hc = complex_mpo("hubbard", L, seed + 100, u=3.0)
+        p = cs.MPS()
+        qa = (C.c_int32 * 4)(*HUB_QSITE)
+        ref.ref_random_mps(cs.CT_DOUBLE_COMPLEX, L, 4, qa, (L << 16), D, seed, C.byref(p))
+        arrays = {}
+        arrays.update(cs.chain_to_arrays("H", Hc))
+        arrays.update(cs.chain_to_arrays("psi0", cs.read_mps(p)))
+        cH = cs.make_c_mpo(Hc)
+        en = (C.c_double * sweeps)()
+        ent = (C.c_double * (L - 1))()
+        if single:
+            assert ref.dmrg_singlesite(C.byref(cH), sweeps, maxiter, C.byref(p), en) == 0
+        else:
+            assert ref.dmrg_twosite(C.byref(cH), sweeps, maxiter, 1e-10, D, C.byref(p), en, ent) == 0
+            arrays.update(entropy=np.array(ent))
+        arrays.update(cs.chain_to_arrays("psi", cs.read_mps(p)))
+        arrays.update(en_sweeps=np.array(en), params=np.array([L, D, sweeps, maxiter], dtype=np.int64),
+                      tol_split=np.array(1e-10), seed=np.array(seed), model=np.array("hubbard complex gauge"))
+        np.savez_compressed(os.path.join(OUT, name), **arrays)
+        print(name, "E =", en[sweeps - 1])
+
+
 def local_ops_case(name, model, L, D, seed, ibond, **kw):
     """Reference inputs/outputs of one local-H apply and one left / right environment step."""
     H = mpo(model, L, **kw)
@@ -274,8 +327,11 @@ if __name__ == "__main__":
         qr_cases()
     elif sys.argv[1:] == ["molecular"]:
         molecular_cases()
+    elif sys.argv[1:] == ["complex"]:
+        complex_cases()
     else:
         main()
         singlesite_cases()
         qr_cases()
         molecular_cases()
+        complex_cases()
