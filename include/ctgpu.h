@@ -34,6 +34,8 @@ extern "C" {
  * hamiltonian: read only. psi: in/out; its site tensors are freed with free() and replaced by
  * tensors allocated with aligned_alloc(16, .), as the reference does. en_sweeps[num_sweeps] and
  * entropy[nsites-1] are caller-allocated; entropy[i] is written on the right-to-left pass. */
+/* Tensors may be CT_DOUBLE_REAL or CT_DOUBLE_COMPLEX (MPO and MPS of the same type), as in the
+ * reference; with complex tensors ctgpu_set_precision(1) is ignored (complex FP64 throughout). */
 int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int maxiter_lanczos,
 	const double tol_split, const ct_long max_vdim, struct mps* psi, double* en_sweeps, double* entropy);
 
