@@ -144,6 +144,10 @@ def barrier(world: int):
 
 def run_oracle_sweeps(H, psi0, sweeps: int, threads: int):
     """The reference algorithm on the host cores: per-sweep wall times and energies."""
+    return run_oracle_sweeps_for(H, psi0, sweeps, threads, WORKLOAD["max_vdim"])
+
+
+def run_oracle_sweeps_for(H, psi0, sweeps: int, threads: int, max_vdim: int):
     import oracle
     from chemtensor_gb300 import ctstructs as cs
     port = oracle.port()
@@ -152,7 +156,7 @@ def run_oracle_sweeps(H, psi0, sweeps: int, threads: int):
     en = np.zeros(sweeps)
     ent = np.zeros(H.nsites - 1)
     w = WORKLOAD
-    ret = port.oracle_dmrg_twosite(C.byref(cH), sweeps, w["maxiter_lanczos"], w["tol_split"], w["max_vdim"],
+    ret = port.oracle_dmrg_twosite(C.byref(cH), sweeps, w["maxiter_lanczos"], w["tol_split"], max_vdim,
                                    C.byref(cP), en.ctypes.data, ent.ctypes.data)
     times = np.zeros(sweeps)
     n = port.oracle_get_sweep_times(times.ctypes.data, sweeps)
@@ -516,6 +520,52 @@ def bench_singlesite(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def bench_complex(args, world, rank, local):
+    """complex128 two-site DMRG: the Fermi-Hubbard MPO (L=16, U=4) with random phases on its virtual
+    bonds (the same operator) and a start state of bond dimension 64 with a random phase on every
+    entry; W warm-up sweeps then K timed sweeps in one call, device time per sweep from CUDA events.
+    The host baseline is the C restatement on the real form of the same problem (it has no complex
+    path), one sweep."""
+    from chemtensor_gb300 import ctstructs as cs, hamiltonians as hm, native, workloads as wl
+    lib = native.lib()
+    lib.ctgpu_set_device(local)
+    native.set_precision(0)
+    L, D = 16, 64
+    Hr = hm.fermi_hubbard_1d(L, 1.0, 4.0, 0.0)
+    c = native.random_mps(L, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(L, 0), D, 42)
+    psir = cs.read_mps(c)
+    cs.free_mps(c)
+    H = wl.complex_gauge(Hr, 5)
+    psi0 = wl.complex_gauge(psir, 6, entry_phases=True)
+    K, W = args.steps, args.warmup
+    cH, cP = cs.make_c_mpo(H), cs.make_c_mps(psi0)
+    en, ent = np.zeros(W + K), np.zeros(L - 1)
+    lib.ctgpu_clear_plan_cache()
+    with ClockSampler(local) as clk:
+        ret = lib.dmrg_twosite(C.byref(cH), W + K, 5, 1e-10, D, C.byref(cP), en.ctypes.data, ent.ctypes.data)
+    if ret != 0:
+        raise RuntimeError(f"dmrg_twosite failed: {ret} {native.last_error()}")
+    ms, la = native.sweep_times()
+    t_dev = dist_max(float(np.sum(ms[W:W + K])) / 1e3, world)
+    cs.free_mps(cP)
+    cs.free_mpo(cH)
+    line = {"metric": "complex128 two-site DMRG sweeps/s (Fermi-Hubbard L=16, D=64, complex gauge)",
+            "value": world * K / t_dev, "unit": "sweeps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * t_dev / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic",
+            "config": {"workload": "fermi_hubbard_1d L=16 t=1 U=4 mu=0 (N,2Sz)=(16,0) D=64 maxiter=5 tol=1e-10, "
+                                   "bond phases seed 5, start state seed 42 with entry phases seed 6",
+                       "parallelism": f"replicas x{world}"},
+            "clocks": clk.summary(), "gpu_launches": int(np.sum(la[W:W + K])), "energies": en.tolist()}
+    if rank == 0 and not args.no_cpu_baseline:
+        times, en_cpu, used = run_oracle_sweeps_for(Hr, psir, 1, os.cpu_count() or 1, D)
+        line["cpu_baseline"] = {"value": 1.0 / float(times[0]), "unit": "sweeps/s", "cores": used, "kind": "port",
+                                "sample": "first sweep of the real form of the problem (the C restatement has no "
+                                          "complex path)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def sweeps_only(args, local):
     """One dmrg_twosite call of warmup + steps sweeps on the workload (profiler target)."""
     from chemtensor_gb300 import ctstructs as cs, native
@@ -551,12 +601,13 @@ def main():
     ap.add_argument("--mol-sweeps", type=int, default=10, help="sweeps of --mode molecular")
     ap.add_argument("--mol-precisions", default="fp64,bf16x3", help="runs of --mode molecular")
     ap.add_argument("--mol-profile", action="store_true", help="time every launch by kernel class in --mode molecular")
-    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh", "serve", "molecular", "singlesite"],
+    ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh", "serve", "molecular", "singlesite", "complex"],
                     help="sweeps: only one device call of warmup+steps sweeps (for profiler captures), no JSON line; "
                          "localh: local-Hamiltonian microbenchmark (synthetic D=1024), its own JSON line; "
                          "serve: request stream of small and medium solves, serial vs concurrent solver threads; "
                          "molecular: spin-orbital molecular Hamiltonian (n=24, D=512), FP64 vs split-BF16; "
-                         "singlesite: dmrg_singlesite on the Hubbard workload (D=256 fixed)")
+                         "singlesite: dmrg_singlesite on the Hubbard workload (D=256 fixed); "
+                         "complex: complex128 two-site DMRG (Hubbard L=16, D=64, complex gauge)")
     ap.add_argument("--requests", type=int, default=128, help="requests of the --mode serve stream")
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate (1/s) of --mode serve")
     ap.add_argument("--workers", type=int, default=4, help="solver threads of --mode serve")
@@ -576,6 +627,9 @@ def main():
         return
     if args.mode == "singlesite":
         bench_singlesite(args, world, rank, local)
+        return
+    if args.mode == "complex":
+        bench_complex(args, world, rank, local)
         return
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

@@ -69,3 +69,30 @@ def molecular_integrals(n: int = 24, seed: int = 7):
     eri = np.einsum("rij,rkl->ijkl", L, L)
     vint = np.ascontiguousarray(eri.transpose(0, 2, 1, 3))
     return tkin, vint
+
+
+def complex_gauge(ch: cs.Chain, seed: int, bond_phases: bool = True, entry_phases: bool = False) -> cs.Chain:
+    """complex128 copy of a chain (MPO or MPS). bond_phases: random phases on the virtual bonds,
+    W_i[..., k] e^{i t_k} and W_{i+1}[k, ...] e^{-i t_k}, which leave the operator (or state)
+    unchanged; entry_phases: a random phase on every entry (a different, genuinely complex state)."""
+    rng = np.random.default_rng(seed)
+    ts = []
+    for t in ch.tensors:
+        z = cs.BlockSparse(t.dim_logical, t.axis_dir, t.qnums_logical, dtype=cs.CT_DOUBLE_COMPLEX)
+        for idx, b in t.blocks.items():
+            z.blocks[idx] = b.astype(np.complex128)
+            if entry_phases:
+                z.blocks[idx] = z.blocks[idx] * np.exp(1j * rng.uniform(0.0, 2 * np.pi, size=b.shape))
+        ts.append(z)
+    if bond_phases:
+        last = ts[0].ndim - 1
+        for i in range(len(ts) - 1):
+            ph = np.exp(1j * rng.uniform(0.0, 2 * np.pi, size=ts[i].dim_logical[last]))
+            for t, ax, conj in ((ts[i], last, False), (ts[i + 1], 0, True)):
+                for idx in list(t.blocks):
+                    sel = np.nonzero(t.qnums_logical[ax] == t.qnums_blocks[ax][idx[ax]])[0]
+                    shape = [1] * t.ndim
+                    shape[ax] = len(sel)
+                    f = np.conj(ph[sel]) if conj else ph[sel]
+                    t.blocks[idx] = t.blocks[idx] * f.reshape(shape)
+    return cs.Chain(ts, ch.qsite, ch.d)
