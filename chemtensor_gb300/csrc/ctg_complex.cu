@@ -7,7 +7,8 @@
 //              conjugating either operand (the conjugated bra of the environment updates,
 //              chain_ops.c:116-245); one CTA per 32 x 32 tile of an output block
 //   k_svd_z    one-sided complex Jacobi SVD of each block (zgesvd in dense_tensor_svd_fill,
-//              dense_tensor.c:3538-3680): one CTA per block, columns in global memory
+//              dense_tensor.c:3538-3680): one CTA per block, columns in global memory, the column
+//              pairs of a sweep in round-robin rounds of disjoint pairs, one warp per pair
 //   k_qr_z     complex Householder QR / RQ of each block (zgeqrf + zungqr, zgerqf + zungrq in
 //              dense_tensor_qr_fill / rq_fill): R has a real diagonal, as LAPACK's
 #include <algorithm>
@@ -126,8 +127,6 @@ __global__ void __launch_bounds__(256)
 k_svd_z(const SvdDesc* __restrict__ descs, const double2* __restrict__ a, double2* __restrict__ u,
         double* __restrict__ s, double2* __restrict__ vh, double2* __restrict__ work, int* __restrict__ status)
 {
-	__shared__ double red[8 * 4];
-	__shared__ double sh_c, sh_sr, sh_si;     // cos, sin * e^{i phi}
 	__shared__ int sh_rot;
 	const SvdDesc d = descs[blockIdx.x];
 	const int m = d.m, n = d.n;
@@ -146,73 +145,66 @@ k_svd_z(const SvdDesc* __restrict__ descs, const double2* __restrict__ a, double
 	for (i64 e = threadIdx.x; e < (i64)K * K; e += blockDim.x)
 		V[e] = make_double2((e % K) == (e / K) ? 1.0 : 0.0, 0.0);
 	__syncthreads();
-	int sweep = 0;
-	bool converged = false;
-	for (; sweep < SVDZ_MAX_SWEEPS && !converged; sweep++)
+	// cyclic sweeps in round-robin order: K - 1 rounds of disjoint column pairs (circle method; a
+	// phantom column when K is odd), one warp per pair, a CTA barrier between rounds
+	const int KP = K + (K & 1);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+	bool converged = K < 2;
+	for (int sweep = 0; sweep < SVDZ_MAX_SWEEPS && !converged; sweep++)
 	{
 		if (threadIdx.x == 0) sh_rot = 0;
 		__syncthreads();
-		for (int p = 0; p < K - 1; p++)
-			for (int q = p + 1; q < K; q++)
+		for (int round = 0; round < KP - 1; round++)
+		{
+			for (int pk = warp; pk < KP / 2; pk += nwarps)
 			{
+				int p0, q0;
+				if (pk == 0) { p0 = KP - 1; q0 = round; }
+				else { p0 = (round + pk) % (KP - 1); q0 = (round - pk + (KP - 1)) % (KP - 1); }
+				const int p = min(p0, q0), q = max(p0, q0);
+				if (q >= K) continue;                 // pair with the phantom column
 				double2* wp = W + (i64)p * R;
 				double2* wq = W + (i64)q * R;
-				double v4[4] = {0, 0, 0, 0};
-				for (int i = threadIdx.x; i < R; i += blockDim.x)
+				double v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+				for (int i = lane; i < R; i += 32)
 				{
 					const double2 x = wp[i], y = wq[i];
-					v4[0] = fma(x.x, x.x, fma(x.y, x.y, v4[0]));
-					v4[1] = fma(y.x, y.x, fma(y.y, y.y, v4[1]));
+					v0 = fma(x.x, x.x, fma(x.y, x.y, v0));
+					v1 = fma(y.x, y.x, fma(y.y, y.y, v1));
 					// conj(x) y
-					v4[2] = fma(x.x, y.x, fma(x.y, y.y, v4[2]));
-					v4[3] = fma(x.x, y.y, -fma(x.y, y.x, -v4[3]));
+					v2 = fma(x.x, y.x, fma(x.y, y.y, v2));
+					v3 = fma(x.x, y.y, -fma(x.y, y.x, -v3));
 				}
-				block_sum4(v4, red);
-				const double al = v4[0], be = v4[1];
-				const double gabs = sqrt(v4[2] * v4[2] + v4[3] * v4[3]);
-				if (threadIdx.x == 0)
+				const double al = warp_sum_z(v0), be = warp_sum_z(v1);
+				const double gr = warp_sum_z(v2), gi = warp_sum_z(v3);
+				const double gabs = sqrt(gr * gr + gi * gi);
+				if (!(gabs > 1e-15 * sqrt(al * be) && gabs > 1e-300)) continue;
+				const double zeta = (be - al) / (2.0 * gabs);
+				const double tt = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+				const double cc = 1.0 / sqrt(1.0 + tt * tt);
+				const double ss = cc * tt;
+				// [x, y] <- [x, y] J, J = [[c, s e^{i phi}], [-s e^{-i phi}, c]], e^{i phi} = gamma / |gamma|
+				const double2 se = make_double2(ss * gr / gabs, ss * gi / gabs);
+				for (int i = lane; i < R; i += 32)
 				{
-					sh_c = 1.0;
-					sh_sr = 0.0;
-					sh_si = 0.0;
-					if (gabs > 1e-15 * sqrt(al * be) && gabs > 1e-300)
-					{
-						const double zeta = (be - al) / (2.0 * gabs);
-						const double tt = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-						const double cc = 1.0 / sqrt(1.0 + tt * tt);
-						const double ss = cc * tt;
-						// e^{i phi} = gamma / |gamma|
-						sh_c = cc;
-						sh_sr = ss * v4[2] / gabs;
-						sh_si = ss * v4[3] / gabs;
-						sh_rot = 1;
-					}
+					const double2 x = wp[i], y = wq[i];
+					const double2 sy = cmul(cconj(se), y), sx = cmul(se, x);
+					wp[i] = make_double2(cc * x.x - sy.x, cc * x.y - sy.y);
+					wq[i] = make_double2(sx.x + cc * y.x, sx.y + cc * y.y);
 				}
-				__syncthreads();
-				const double cc = sh_c;
-				const double2 se = make_double2(sh_sr, sh_si);        // s e^{i phi}
-				if (se.x != 0.0 || se.y != 0.0)
+				double2* vp = V + (i64)p * K;
+				double2* vq = V + (i64)q * K;
+				for (int i = lane; i < K; i += 32)
 				{
-					// [x, y] <- [x, y] J, J = [[c, s e^{i phi}], [-s e^{-i phi}, c]]
-					for (int i = threadIdx.x; i < R; i += blockDim.x)
-					{
-						const double2 x = wp[i], y = wq[i];
-						const double2 sy = cmul(cconj(se), y), sx = cmul(se, x);
-						wp[i] = make_double2(cc * x.x - sy.x, cc * x.y - sy.y);
-						wq[i] = make_double2(sx.x + cc * y.x, sx.y + cc * y.y);
-					}
-					double2* vp = V + (i64)p * K;
-					double2* vq = V + (i64)q * K;
-					for (int i = threadIdx.x; i < K; i += blockDim.x)
-					{
-						const double2 x = vp[i], y = vq[i];
-						const double2 sy = cmul(cconj(se), y), sx = cmul(se, x);
-						vp[i] = make_double2(cc * x.x - sy.x, cc * x.y - sy.y);
-						vq[i] = make_double2(sx.x + cc * y.x, sx.y + cc * y.y);
-					}
+					const double2 x = vp[i], y = vq[i];
+					const double2 sy = cmul(cconj(se), y), sx = cmul(se, x);
+					vp[i] = make_double2(cc * x.x - sy.x, cc * x.y - sy.y);
+					vq[i] = make_double2(sx.x + cc * y.x, sx.y + cc * y.y);
 				}
-				__syncthreads();
+				if (lane == 0) sh_rot = 1;
 			}
+			__syncthreads();
+		}
 		converged = sh_rot == 0;
 		__syncthreads();
 	}
