@@ -189,7 +189,7 @@ struct DotPlan {
 	void pack_b(Ctx& c, const double* B, void* bpack) const;      // b_recs * TC_B_REC_BYTES bytes
 	void run_packed(Ctx& c, const void* apack, const void* bpack, double* C) const;
 };
-// out_perm (FP64 only): the result is written straight in the layout of its transpose by out_perm
+// out_perm (every precision): the result is written straight in the layout of its transpose by out_perm
 // (see lower_dot), and the plan's `out` is that transposed structure
 DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision = GEMM_FP64,
                       const int* out_perm = nullptr);
