@@ -257,7 +257,7 @@ int ctgpu_mps_vdot(const struct mps* chi, const struct mps* psi, double* ret)
 {
 	return guarded([&] {
 		CTG_CHECK(ret, "null argument");
-		*ret = ctg::mps_vdot_gpu(chi, psi, g_opts.device);
+		ctg::mps_vdot_gpu(chi, psi, g_opts.device, ret);
 		return 0;
 	});
 }
@@ -271,7 +271,9 @@ int ctgpu_mps_norm(const struct mps* psi, double* ret)
 			*ret = 0;
 			return 0;
 		}
-		const double nrm2 = ctg::mps_vdot_gpu(psi, psi, g_opts.device);
+		double v[2] = {0.0, 0.0};
+		ctg::mps_vdot_gpu(psi, psi, g_opts.device, v);
+		const double nrm2 = v[0];
 		CTG_CHECK(nrm2 >= -1e-12, "mps_norm: negative squared norm");
 		*ret = std::sqrt(std::max(nrm2, 0.0));
 		return 0;

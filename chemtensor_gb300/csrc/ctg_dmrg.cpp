@@ -786,10 +786,10 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 }
 
 // ------------------------------------------------------------------------------------
-// mps_vdot (src/state/mps.c:314-370), real case: <chi|psi> by contraction from the right
+// mps_vdot (src/state/mps.c:314-370): <chi|psi> by contraction from the right (chi conjugated)
 // ------------------------------------------------------------------------------------
 
-double mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device)
+void mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device, double* ret)
 {
 	CTG_CHECK(chi && psi && chi->nsites == psi->nsites && psi->nsites >= 1, "mps_vdot: invalid arguments");
 	const int L = psi->nsites;
@@ -804,14 +804,17 @@ double mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device)
 	const i64 dim[4] = {1, 1, 1, 1};
 	const int dir[4] = {TENSOR_AXIS_OUT, TENSOR_AXIS_IN, TENSOR_AXIS_IN, TENSOR_AXIS_OUT};
 	Meta m = make_meta(4, dim, dir, {qp, qc, qp, qc});
+	const bool cplx = psi->a[0].dtype == CT_DOUBLE_COMPLEX;
+	CTG_CHECK(chi->a[0].dtype == psi->a[0].dtype, "mps_vdot: MPS of different numeric types");
 	DTensor r;
 	if (m.nblocks == 1)
 	{
-		const double one = 1.0;
+		const double one[2] = {1.0, 0.0};
 		r.meta = std::make_shared<const Meta>(std::move(m));
-		r.buf = c.upload(&one, sizeof(double));
+		r.cplx = cplx;
+		r.buf = c.upload(one, (size_t)r.width() * sizeof(double));
 	}
-	else r = c.zeros(m);
+	else r = c.zeros(m, cplx);
 	r = op_flatten(c, r, 2, TENSOR_AXIS_IN);
 	for (int i = L - 1; i >= 0; i--)
 	{
@@ -820,6 +823,7 @@ double mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device)
 		DTensor b = tensor_from_struct(c, &chi->a[i]);
 		DTensor s1 = op_dot(c, a, AX_TRAILING, r, AX_LEADING, 1);
 		DTensor bc = view_reversed(c, b);
+		bc.conj = b.cplx;                 // <chi| is complex conjugated
 		const int perm0[4] = {3, 0, 1, 2};
 		DTensor t = op_transpose(c, s1, perm0);
 		DTensor s2 = op_dot(c, t, AX_TRAILING, bc, AX_TRAILING, 2);
@@ -828,10 +832,11 @@ double mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device)
 	}
 	DTensor rf = op_flatten(c, r, 0, TENSOR_AXIS_OUT);
 	CTG_CHECK(rf.m().ndim == 2 && rf.m().dim[0] == 1 && rf.m().dim[1] == 1, "mps_vdot: unexpected result shape");
-	double v = 0;
-	if (rf.m().nnz > 0) copy_to_host(c, rf, &v);
+	double v[2] = {0.0, 0.0};
+	if (rf.m().nnz > 0) copy_to_host(c, rf, v);
 	c.sync();
-	return v;
+	ret[0] = v[0];
+	if (cplx) ret[1] = v[1];
 }
 
 // ------------------------------------------------------------------------------------

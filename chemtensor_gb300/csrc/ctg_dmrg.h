@@ -69,8 +69,9 @@ DTensor apply_local_hamiltonian_once(Ctx& c, const DTensor& a, const DTensor& w,
 double time_local_hamiltonian(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& l, const DTensor& r,
                               int precision, int nmatvec, double* flops);
 
-// <chi|psi> of two real MPS on the device (mps_vdot, src/state/mps.c:314-370)
-double mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device);
+// <chi|psi> of two MPS on the device (mps_vdot, src/state/mps.c:314-370); ret receives one double
+// (real MPS) or two (complex: real and imaginary part)
+void mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device, double* ret);
 
 // spin-orbital molecular Hamiltonian as an MPO (construct_spin_molecular_hamiltonian_mpo_assembly with
 // optimize = false + mpo_from_assembly, src/operator/hamiltonian.c:2768-2979); tkin n x n and vint

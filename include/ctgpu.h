@@ -136,10 +136,12 @@ void ctgpu_randn_sequence(uint64_t seed, int n, double* out);
  * concurrent solves. Returns 0 or -5. No counterpart in the reference. */
 int ctgpu_device_memory(int device, size_t* free_bytes, size_t* total_bytes);
 
-/* <chi|psi> and ||psi|| of real MPS, contracted on the device (bond tensors uploaded, environment
- * kept in HBM). Replace mps_vdot (src/state/mps.c:314-370; real double case, result in *ret) and
- * mps_norm (src/state/mps.c:375-424). Leading and trailing virtual bonds must have dimension 1.
- * Return 0, or -5 (message via ctgpu_last_error). */
+/* <chi|psi> (chi complex conjugated) and ||psi||, contracted on the device (site tensors uploaded,
+ * the environment kept in HBM). Replace mps_vdot (src/state/mps.c:314-370) and mps_norm
+ * (src/state/mps.c:375-424). ctgpu_mps_vdot writes one double for CT_DOUBLE_REAL MPS and two (real,
+ * imaginary part) for CT_DOUBLE_COMPLEX ones, as the reference writes one entry of the MPS's numeric
+ * type. Leading and trailing virtual bonds must have dimension 1. Return 0, or -5 (message via
+ * ctgpu_last_error). */
 int ctgpu_mps_vdot(const struct mps* chi, const struct mps* psi, double* ret);
 int ctgpu_mps_norm(const struct mps* psi, double* ret);
 

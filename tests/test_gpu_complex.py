@@ -111,3 +111,19 @@ def test_complex_qr_rq_and_svd(gpu, shape):
     for x in (q, r, r2, q2):
         cs.free_bst(x)
     cs.free_bst(ca)
+
+
+def test_complex_mps_vdot_and_norm(gpu):
+    g = golden("dmrg_complex_hubbard_L6_D32.npz")
+    a, b = cs.chain_from_arrays("psi0", g), cs.chain_from_arrays("psi", g)
+    ca, cb = cs.make_c_mps(a), cs.make_c_mps(b)
+    va, vb = mps_vector(a), mps_vector(b)
+    for x, y, ref in ((ca, cb, np.vdot(va, vb)), (cb, ca, np.vdot(vb, va)), (ca, ca, np.vdot(va, va))):
+        got = (C.c_double * 2)()
+        assert gpu.ctgpu_mps_vdot(C.byref(x), C.byref(y), got) == 0
+        assert abs(complex(got[0], got[1]) - ref) <= 1e-12 * max(1.0, abs(ref))
+    nrm = C.c_double()
+    assert gpu.ctgpu_mps_norm(C.byref(ca), C.byref(nrm)) == 0
+    assert abs(nrm.value - np.linalg.norm(va)) <= 1e-12 * nrm.value
+    cs.free_mps(ca)
+    cs.free_mps(cb)
