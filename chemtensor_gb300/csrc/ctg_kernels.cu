@@ -273,6 +273,24 @@ k_rowmap(const Chunk* __restrict__ chunks, const RowDesc* __restrict__ descs, co
 	const i64 n = d.nlead * d.nrow * d.ntrail;
 	const i64 end = min(n, ch.start + (i64)COPY_CHUNK);
 	const i64* map = maps + d.map_off;
+	if (n < ((i64)1 << 31))
+	{
+		// 32-bit index arithmetic (64-bit integer division is several times slower)
+		const unsigned nt = (unsigned)d.ntrail, nr = (unsigned)d.nrow;
+		for (unsigned e = (unsigned)ch.start + threadIdx.x; e < (unsigned)end; e += blockDim.x)
+		{
+			const unsigned lj = e / nt;
+			const unsigned t = e - lj * nt;
+			const unsigned lead = lj / nr;
+			const unsigned j = lj - lead * nr;
+			const i64 mj = map[j];
+			const i64 srow = d.scatter ? (i64)j : mj;
+			const i64 drow = d.scatter ? mj : (i64)j;
+			dst[d.dst_off + ((i64)lead * d.dst_rows + drow) * d.ntrail + t] =
+				src[d.src_off + ((i64)lead * d.src_rows + srow) * d.ntrail + t];
+		}
+		return;
+	}
 	for (i64 e = ch.start + threadIdx.x; e < end; e += blockDim.x)
 	{
 		const i64 t = e % d.ntrail;
@@ -312,6 +330,17 @@ k_scale_axis(const Chunk* __restrict__ chunks, const ScaleDesc* __restrict__ des
 	const ScaleDesc d = descs[ch.desc];
 	const i64 n = d.nlead * d.nax * d.ntrail;
 	const i64 end = min(n, ch.start + (i64)COPY_CHUNK);
+	if (n < ((i64)1 << 31))
+	{
+		const unsigned nt = (unsigned)d.ntrail, na = (unsigned)d.nax;
+		for (unsigned e = (unsigned)ch.start + threadIdx.x; e < (unsigned)end; e += blockDim.x)
+		{
+			const unsigned q = e / nt;
+			const unsigned p = q - (q / na) * na;
+			dst[d.off + e] = scale_entry(src[d.off + e], vec[maps[d.map_off + p]]);
+		}
+		return;
+	}
 	for (i64 e = ch.start + threadIdx.x; e < end; e += blockDim.x)
 	{
 		const i64 p = (e / d.ntrail) % d.nax;
