@@ -292,11 +292,79 @@ Meta dot_result_meta(const Meta& s, int axs, const Meta& t, int axt, int nmult)
 
 Meta transpose_meta(const Meta& t, const int* perm)
 {
-	std::vector<i64> dim(t.ndim);
-	std::vector<int> dir(t.ndim);
-	std::vector<std::vector<q32>> ql(t.ndim);
-	for (int i = 0; i < t.ndim; i++) { dim[i] = t.dim[perm[i]]; dir[i] = t.dir[perm[i]]; ql[i] = t.ql[perm[i]]; }
-	return make_meta(t.ndim, dim.data(), dir.data(), ql);
+	// The allowed blocks of a transposed tensor are the permuted allowed blocks (the rule is a sum
+	// over axes), so the structure follows from t's without a new enumeration: permute the axis
+	// data and the block multi-indices, then order the blocks row-major under the new axis order.
+	const int nd = t.ndim;
+	Meta m;
+	m.ndim = nd;
+	m.dim.resize(nd);
+	m.dir.resize(nd);
+	m.ql.resize(nd);
+	m.qb.resize(nd);
+	m.bd.resize(nd);
+	m.pos.resize(nd);
+	m.blk.resize(nd);
+	m.nb.resize(nd);
+	for (int a = 0; a < nd; a++)
+	{
+		const int p = perm[a];
+		CTG_CHECK(p >= 0 && p < nd, "transpose: invalid permutation");
+		m.dim[a] = t.dim[p];
+		m.dir[a] = t.dir[p];
+		m.ql[a] = t.ql[p];
+		m.qb[a] = t.qb[p];
+		m.bd[a] = t.bd[p];
+		m.pos[a] = t.pos[p];
+		m.blk[a] = t.blk[p];
+		m.nb[a] = t.nb[p];
+	}
+	const int nb = t.nblocks;
+	std::vector<std::pair<i64, int>> order((size_t)nb);
+	for (int b = 0; b < nb; b++)
+	{
+		const i64* ib = t.index(b);
+		i64 k = 0;
+		for (int a = 0; a < nd; a++) k = k * m.nb[a] + ib[perm[a]];
+		order[(size_t)b] = {k, b};
+	}
+	std::sort(order.begin(), order.end());
+	m.nblocks = nb;
+	m.bidx.resize((size_t)nb * nd);
+	m.bdim.resize((size_t)nb * nd);
+	m.boff.resize((size_t)nb);
+	m.lin.resize((size_t)nb);
+	i64 off = 0;
+	for (int b = 0; b < nb; b++)
+	{
+		const int src = order[(size_t)b].second;
+		const i64* ib = t.index(src);
+		const i64* db = t.dims(src);
+		i64 size = 1;
+		for (int a = 0; a < nd; a++)
+		{
+			m.bidx[(size_t)b * nd + a] = ib[perm[a]];
+			m.bdim[(size_t)b * nd + a] = db[perm[a]];
+			size *= db[perm[a]];
+		}
+		m.boff[(size_t)b] = off;
+		m.lin[(size_t)b] = order[(size_t)b].first;
+		off += size;
+	}
+	m.nnz = off;
+	i64 total = 1;
+	bool dense = true;
+	for (int a = 0; a < nd; a++)
+	{
+		total *= m.nb[a];
+		if (total > 4 * (i64)m.nblocks + 4096) { dense = false; break; }
+	}
+	if (dense)
+	{
+		m.lut.assign((size_t)total, -1);
+		for (int b = 0; b < m.nblocks; b++) m.lut[(size_t)m.lin[(size_t)b]] = b;
+	}
+	return m;
 }
 
 Meta flatten_meta(const Meta& t, int ax, int newdir)

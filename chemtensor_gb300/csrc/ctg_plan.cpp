@@ -499,6 +499,8 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 	if (precision == GEMM_BF16X3)
 	{
 		std::unordered_map<int, i64> abase, bbase;
+		abase.reserve((size_t)s.nblocks);
+		bbase.reserve((size_t)t.nblocks);
 		tcons.resize(cons.size());
 		for (size_t ci = 0; ci < cons.size(); ci++)
 		{
@@ -573,6 +575,8 @@ CopyLowering lower_transpose(const Meta& t, const int* perm)
 	CTG_CHECK(t.ndim <= 6, "transpose: at most 6 axes");
 	std::vector<PermDesc> descs;
 	std::vector<Chunk> chunks;
+	descs.reserve((size_t)t.nblocks);
+	chunks.reserve((size_t)t.nblocks);
 	std::vector<i64> ir(t.ndim);
 	for (int b = 0; b < t.nblocks; b++)
 	{

@@ -3,7 +3,10 @@
 // rule of block_sparse_tensor.c:78-140), row-major order, offsets, dimensions and find().
 // Small quantum numbers, and pairs packed as (a << 16) + b as the Fermi-Hubbard model encodes
 // particle number and spin (wide value ranges, many sectors, few allowed combinations).
+// Also: transpose_meta, which permutes an existing structure instead of enumerating again,
+// against make_meta of the permuted axes (every field).
 // Built and run by tests/test_host_logic.py on the host; no GPU involved.
+#include <algorithm>
 #include <cstdio>
 #include <random>
 #include "ctg_meta.h"
@@ -51,6 +54,35 @@ int main()
 			b++;
 		}
 		if (b != m.nblocks || off != m.nnz) bad++;
+	}
+	for (int trial = 0; trial < 2000; trial++)
+	{
+		const int nd = 2 + (int)(rng() % 5);
+		std::vector<i64> dim(nd);
+		std::vector<int> dir(nd);
+		std::vector<std::vector<q32>> ql(nd);
+		for (int a = 0; a < nd; a++)
+		{
+			dim[a] = 1 + (i64)(rng() % 9);
+			dir[a] = (rng() & 1) ? 1 : -1;
+			ql[a].resize((size_t)dim[a]);
+			for (auto& q : ql[a]) q = (q32)(rng() % 5) - 2;
+		}
+		const Meta t = make_meta(nd, dim.data(), dir.data(), ql);
+		std::vector<int> perm(nd);
+		for (int a = 0; a < nd; a++) perm[a] = a;
+		std::shuffle(perm.begin(), perm.end(), rng);
+		const Meta x = transpose_meta(t, perm.data());
+		std::vector<i64> d2(nd);
+		std::vector<int> r2(nd);
+		std::vector<std::vector<q32>> q2(nd);
+		for (int i = 0; i < nd; i++) { d2[i] = dim[perm[i]]; r2[i] = dir[perm[i]]; q2[i] = ql[perm[i]]; }
+		const Meta y = make_meta(nd, d2.data(), r2.data(), q2);
+		const bool same = x.nblocks == y.nblocks && x.nnz == y.nnz && x.bidx == y.bidx && x.bdim == y.bdim &&
+		                  x.boff == y.boff && x.lin == y.lin && x.lut == y.lut && x.qb == y.qb && x.bd == y.bd &&
+		                  x.pos == y.pos && x.blk == y.blk && x.nb == y.nb && x.dim == y.dim && x.dir == y.dir &&
+		                  x.ql == y.ql;
+		if (!same) bad++;
 	}
 	printf("mismatches: %d\n", bad);
 	return bad != 0;
