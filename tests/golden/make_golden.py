@@ -180,6 +180,11 @@ def molecular_cases():
     tk, vi = rng.standard_normal((4, 4)), rng.standard_normal((4, 4, 4, 4))
     arrays.update(tkin4=tk, vint4=vi)
     arrays.update(cs.chain_to_arrays("H4", cs.read_mpo(build(tk, vi))))
+    # odd and small orbital counts (pair states change sides at an odd bond)
+    for n in (1, 2, 5):
+        tk, vi = rng.standard_normal((n, n)), rng.standard_normal((n, n, n, n))
+        arrays.update({f"tkin{n}": tk, f"vint{n}": vi})
+        arrays.update(cs.chain_to_arrays(f"H{n}", cs.read_mpo(build(tk, vi))))
     tk, vi = wl.molecular_integrals(24, 7)
     ch = cs.read_mpo(build(tk, vi))
     for i, t in enumerate(ch.tensors):

@@ -16,10 +16,11 @@ def _bond_dims(ch):
     return [t.dim_logical[0] for t in ch.tensors] + [ch.tensors[-1].dim_logical[3]]
 
 
-def test_molecular_mpo_is_the_reference_operator():
+@pytest.mark.parametrize("n", [1, 2, 4, 5])
+def test_molecular_mpo_is_the_reference_operator(n):
     g = golden("spin_molecular_mpo.npz")
-    ours = hm.spin_molecular(g["tkin4"], g["vint4"])
-    ref = cs.chain_from_arrays("H4", g)
+    ours = hm.spin_molecular(g[f"tkin{n}"], g[f"vint{n}"])
+    ref = cs.chain_from_arrays(f"H{n}", g)
     assert _bond_dims(ours) == _bond_dims(ref)
     for a, b in zip(ours.tensors, ref.tensors):
         assert a.axis_dir == b.axis_dir
