@@ -120,6 +120,10 @@ def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    local_world = int(os.environ.get("LOCAL_WORLD_SIZE", str(world)))
+    if local_world > 1:
+        # replicas share the host: split its cores among the ranks' lowering threads
+        os.environ.setdefault("CTGPU_HOST_THREADS", str(max(1, (os.cpu_count() or 1) // local_world)))
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo", init_method="env://")
