@@ -76,7 +76,27 @@ uint64_t Meta::structure_hash() const
 	return hash_;
 }
 
+namespace {
+
+// Axes of a new structure that are axes of an existing one (same logical quantum numbers): their
+// sorted unique quantum numbers, multiplicities and index maps are copied instead of recomputed.
+struct AxisSource {
+	const Meta* m[8] = {};
+	int ax[8] = {};
+};
+
+Meta build_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::vector<q32>>& ql, const AxisSource* src);
+
+}  // namespace
+
 Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::vector<q32>>& ql)
+{
+	return build_meta(ndim, dim, dir, ql, nullptr);
+}
+
+namespace {
+
+Meta build_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::vector<q32>>& ql, const AxisSource* src)
 {
 	CTG_CHECK(ndim >= 1 && ndim <= 8, "tensor degree out of range");
 	Meta m;
@@ -92,6 +112,17 @@ Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::
 	for (int a = 0; a < ndim; a++)
 	{
 		CTG_CHECK(dim[a] > 0 && (i64)ql[a].size() == dim[a], "logical quantum numbers do not match the dimension");
+		if (src && src->m[a])
+		{
+			const Meta& o = *src->m[a];
+			const int b = src->ax[a];
+			m.qb[a] = o.qb[b];
+			m.nb[a] = o.nb[b];
+			m.bd[a] = o.bd[b];
+			m.pos[a] = o.pos[b];
+			m.blk[a] = o.blk[b];
+			continue;
+		}
 		std::vector<q32> u(ql[a]);
 		std::sort(u.begin(), u.end());
 		u.erase(std::unique(u.begin(), u.end()), u.end());
@@ -268,6 +299,8 @@ Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::
 	return m;
 }
 
+}  // namespace
+
 Meta dot_result_meta(const Meta& s, int axs, const Meta& t, int axt, int nmult)
 {
 	const int shift_s = (axs == AX_LEADING ? 0 : s.ndim - nmult);
@@ -284,10 +317,26 @@ Meta dot_result_meta(const Meta& s, int axs, const Meta& t, int axt, int nmult)
 	std::vector<i64> dim;
 	std::vector<int> dir;
 	std::vector<std::vector<q32>> ql;
-	for (int i = 0; i < nfs; i++) { dim.push_back(s.dim[off_s + i]); dir.push_back(s.dir[off_s + i]); ql.push_back(s.ql[off_s + i]); }
-	for (int i = 0; i < nft; i++) { dim.push_back(t.dim[off_t + i]); dir.push_back(t.dir[off_t + i]); ql.push_back(t.ql[off_t + i]); }
+	AxisSource src;
+	for (int i = 0; i < nfs; i++)
+	{
+		dim.push_back(s.dim[off_s + i]);
+		dir.push_back(s.dir[off_s + i]);
+		ql.push_back(s.ql[off_s + i]);
+		src.m[i] = &s;
+		src.ax[i] = off_s + i;
+	}
+	for (int i = 0; i < nft; i++)
+	{
+		dim.push_back(t.dim[off_t + i]);
+		dir.push_back(t.dir[off_t + i]);
+		ql.push_back(t.ql[off_t + i]);
+		src.m[nfs + i] = &t;
+		src.ax[nfs + i] = off_t + i;
+	}
 	CTG_CHECK(!dim.empty(), "dot: scalar results are not on the DMRG path");
-	return make_meta((int)dim.size(), dim.data(), dir.data(), ql);
+	CTG_CHECK(dim.size() <= 8, "tensor degree out of range");
+	return build_meta((int)dim.size(), dim.data(), dir.data(), ql, &src);
 }
 
 Meta transpose_meta(const Meta& t, const int* perm)
@@ -373,7 +422,15 @@ Meta flatten_meta(const Meta& t, int ax, int newdir)
 	std::vector<i64> dim;
 	std::vector<int> dir;
 	std::vector<std::vector<q32>> ql;
-	for (int i = 0; i < ax; i++) { dim.push_back(t.dim[i]); dir.push_back(t.dir[i]); ql.push_back(t.ql[i]); }
+	AxisSource src;
+	for (int i = 0; i < ax; i++)
+	{
+		dim.push_back(t.dim[i]);
+		dir.push_back(t.dir[i]);
+		ql.push_back(t.ql[i]);
+		src.m[i] = &t;
+		src.ax[i] = i;
+	}
 	const i64 d0 = t.dim[ax], d1 = t.dim[ax + 1];
 	std::vector<q32> qf((size_t)(d0 * d1));
 	for (i64 j = 0; j < d0; j++)
@@ -382,8 +439,15 @@ Meta flatten_meta(const Meta& t, int ax, int newdir)
 	dim.push_back(d0 * d1);
 	dir.push_back(newdir);
 	ql.push_back(qf);
-	for (int i = ax + 2; i < t.ndim; i++) { dim.push_back(t.dim[i]); dir.push_back(t.dir[i]); ql.push_back(t.ql[i]); }
-	return make_meta((int)dim.size(), dim.data(), dir.data(), ql);
+	for (int i = ax + 2; i < t.ndim; i++)
+	{
+		src.m[dim.size()] = &t;
+		src.ax[dim.size()] = i;
+		dim.push_back(t.dim[i]);
+		dir.push_back(t.dir[i]);
+		ql.push_back(t.ql[i]);
+	}
+	return build_meta((int)dim.size(), dim.data(), dir.data(), ql, &src);
 }
 
 Meta split_meta(const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
@@ -396,10 +460,26 @@ Meta split_meta(const Meta& t, int ax, const i64 nd[2], const int ndir[2], const
 	std::vector<i64> dim;
 	std::vector<int> dir;
 	std::vector<std::vector<q32>> ql;
-	for (int i = 0; i < ax; i++) { dim.push_back(t.dim[i]); dir.push_back(t.dir[i]); ql.push_back(t.ql[i]); }
+	AxisSource src;
+	for (int i = 0; i < ax; i++)
+	{
+		src.m[dim.size()] = &t;
+		src.ax[dim.size()] = i;
+		dim.push_back(t.dim[i]);
+		dir.push_back(t.dir[i]);
+		ql.push_back(t.ql[i]);
+	}
 	for (int h = 0; h < 2; h++) { dim.push_back(nd[h]); dir.push_back(ndir[h]); ql.push_back(nq[h]); }
-	for (int i = ax + 1; i < t.ndim; i++) { dim.push_back(t.dim[i]); dir.push_back(t.dir[i]); ql.push_back(t.ql[i]); }
-	return make_meta((int)dim.size(), dim.data(), dir.data(), ql);
+	for (int i = ax + 1; i < t.ndim; i++)
+	{
+		CTG_CHECK(dim.size() < 8, "tensor degree out of range");
+		src.m[dim.size()] = &t;
+		src.ax[dim.size()] = i;
+		dim.push_back(t.dim[i]);
+		dir.push_back(t.dir[i]);
+		ql.push_back(t.ql[i]);
+	}
+	return build_meta((int)dim.size(), dim.data(), dir.data(), ql, &src);
 }
 
 Meta slice_meta(const Meta& t, int ax, const std::vector<i64>& ind)
@@ -414,7 +494,14 @@ Meta slice_meta(const Meta& t, int ax, const std::vector<i64>& ind)
 		ql[ax][j] = t.ql[ax][(size_t)ind[j]];
 	}
 	dim[ax] = (i64)ind.size();
-	return make_meta(t.ndim, dim.data(), t.dir.data(), ql);
+	AxisSource src;
+	for (int i = 0; i < t.ndim; i++)
+		if (i != ax)
+		{
+			src.m[i] = &t;
+			src.ax[i] = i;
+		}
+	return build_meta(t.ndim, dim.data(), t.dir.data(), ql, &src);
 }
 
 Meta reversed_meta(const Meta& t)

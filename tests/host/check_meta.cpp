@@ -3,8 +3,9 @@
 // rule of block_sparse_tensor.c:78-140), row-major order, offsets, dimensions and find().
 // Small quantum numbers, and pairs packed as (a << 16) + b as the Fermi-Hubbard model encodes
 // particle number and spin (wide value ranges, many sectors, few allowed combinations).
-// Also: transpose_meta, which permutes an existing structure instead of enumerating again,
-// against make_meta of the permuted axes (every field).
+// Also: transpose_meta (permutes an existing structure), and the result structures of dot,
+// flatten and slice (which copy the per-axis data of unchanged axes) against make_meta of the
+// same axes, every field.
 // Built and run by tests/test_host_logic.py on the host; no GPU involved.
 #include <algorithm>
 #include <cstdio>
@@ -83,6 +84,38 @@ int main()
 		                  x.pos == y.pos && x.blk == y.blk && x.nb == y.nb && x.dim == y.dim && x.dir == y.dir &&
 		                  x.ql == y.ql;
 		if (!same) bad++;
+	}
+	auto same_meta = [](const Meta& x, const Meta& y) {
+		return x.nblocks == y.nblocks && x.nnz == y.nnz && x.bidx == y.bidx && x.bdim == y.bdim && x.boff == y.boff &&
+		       x.lin == y.lin && x.lut == y.lut && x.qb == y.qb && x.bd == y.bd && x.pos == y.pos && x.blk == y.blk &&
+		       x.nb == y.nb && x.dim == y.dim && x.dir == y.dir && x.ql == y.ql;
+	};
+	for (int trial = 0; trial < 1000; trial++)
+	{
+		// s (a, b, k) . t (k', c): dot over one axis; flatten of s's (a, b); slice of s's axis b
+		auto rq = [&](i64 d) { std::vector<q32> q((size_t)d); for (auto& x : q) x = (q32)(rng() % 5) - 2; return q; };
+		const i64 da = 1 + rng() % 7, db = 1 + rng() % 7, dk = 1 + rng() % 7, dc = 1 + rng() % 7;
+		const std::vector<q32> qa = rq(da), qbv = rq(db), qk = rq(dk), qc = rq(dc);
+		const int sa = (rng() & 1) ? 1 : -1, sb = (rng() & 1) ? 1 : -1, sk = (rng() & 1) ? 1 : -1, sc = (rng() & 1) ? 1 : -1;
+		const i64 ds[3] = {da, db, dk}, dt[2] = {dk, dc};
+		const int rs[3] = {sa, sb, sk}, rt[2] = {-sk, sc};
+		const Meta ms = make_meta(3, ds, rs, {qa, qbv, qk});
+		const Meta mt = make_meta(2, dt, rt, {qk, qc});
+		const i64 dr[3] = {da, db, dc};
+		const int rr[3] = {sa, sb, sc};
+		if (!same_meta(dot_result_meta(ms, AX_TRAILING, mt, AX_LEADING, 1), make_meta(3, dr, rr, {qa, qbv, qc}))) bad++;
+		std::vector<q32> qf((size_t)(da * db));
+		for (i64 j = 0; j < da; j++)
+			for (i64 k = 0; k < db; k++) qf[(size_t)(j * db + k)] = -1 * (sa * qa[(size_t)j] + sb * qbv[(size_t)k]);
+		const i64 dfl[2] = {da * db, dk};
+		const int rfl[2] = {-1, sk};
+		if (!same_meta(flatten_meta(ms, 0, -1), make_meta(2, dfl, rfl, {qf, qk}))) bad++;
+		std::vector<i64> ind;
+		for (i64 j = 0; j < db; j += 2) ind.push_back(j);
+		std::vector<q32> qsl;
+		for (i64 j : ind) qsl.push_back(qbv[(size_t)j]);
+		const i64 dsl[3] = {da, (i64)ind.size(), dk};
+		if (!same_meta(slice_meta(ms, 1, ind), make_meta(3, dsl, rs, {qa, qsl, qk}))) bad++;
 	}
 	printf("mismatches: %d\n", bad);
 	return bad != 0;
