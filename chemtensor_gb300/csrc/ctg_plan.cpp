@@ -498,9 +498,8 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 	std::vector<TcPack> apacks, bpacks;
 	if (precision == GEMM_BF16X3)
 	{
-		std::unordered_map<int, i64> abase, bbase;
-		abase.reserve((size_t)s.nblocks);
-		bbase.reserve((size_t)t.nblocks);
+		// first record of each operand block's packed tiles (-1: not packed yet)
+		std::vector<i64> abase((size_t)s.nblocks, -1), bbase((size_t)t.nblocks, -1);
 		tcons.resize(cons.size());
 		for (size_t ci = 0; ci < cons.size(); ci++)
 		{
@@ -512,27 +511,25 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			const i64* td = t.dims(bt);
 			const int am = (int)prod(sd + (axs == AX_LEADING ? nmult : 0), s.ndim - nmult);
 			const int bn = (int)prod(td + (axt == AX_LEADING ? nmult : 0), t.ndim - nmult);
-			auto ia = abase.find(bs);
-			if (ia == abase.end())
+			if (abase[(size_t)bs] < 0)
 			{
 				const i64 base = (i64)apacks.size();
 				const int mtiles = (am + TC_A_ROWS - 1) / TC_A_ROWS;
 				for (int mt = 0; mt < mtiles; mt++)
 					for (int j = 0; j < kt; j++)
 						apacks.push_back(TcPack{g.a_off, am, g.k, g.sAm, g.sAk, mt * TC_A_ROWS, j * TC_K, base + mt * kt + j});
-				ia = abase.emplace(bs, base).first;
+				abase[(size_t)bs] = base;
 			}
-			auto ib = bbase.find(bt);
-			if (ib == bbase.end())
+			if (bbase[(size_t)bt] < 0)
 			{
 				const i64 base = (i64)bpacks.size();
 				const int ntiles_b = (bn + TC_B_ROWS - 1) / TC_B_ROWS;
 				for (int nt = 0; nt < ntiles_b; nt++)
 					for (int j = 0; j < kt; j++)
 						bpacks.push_back(TcPack{g.b_off, bn, g.k, g.sBn, g.sBk, nt * TC_B_ROWS, j * TC_K, base + nt * kt + j});
-				ib = bbase.emplace(bt, base).first;
+				bbase[(size_t)bt] = base;
 			}
-			tcons[ci] = TcContrib{ia->second, ib->second, kt, 0};
+			tcons[ci] = TcContrib{abase[(size_t)bs], bbase[(size_t)bt], kt, 0};
 		}
 	}
 	g_plan_stage[2] += host_seconds() - ts0;
