@@ -339,7 +339,7 @@ Meta dot_result_meta(const Meta& s, int axs, const Meta& t, int axt, int nmult)
 	return build_meta((int)dim.size(), dim.data(), dir.data(), ql, &src);
 }
 
-Meta transpose_meta(const Meta& t, const int* perm)
+Meta transpose_meta(const Meta& t, const int* perm, std::vector<int>* dst_of_src)
 {
 	// The allowed blocks of a transposed tensor are the permuted allowed blocks (the rule is a sum
 	// over axes), so the structure follows from t's without a new enumeration: permute the axis
@@ -384,9 +384,11 @@ Meta transpose_meta(const Meta& t, const int* perm)
 	m.boff.resize((size_t)nb);
 	m.lin.resize((size_t)nb);
 	i64 off = 0;
+	if (dst_of_src) dst_of_src->assign((size_t)nb, -1);
 	for (int b = 0; b < nb; b++)
 	{
 		const int src = order[(size_t)b].second;
+		if (dst_of_src) (*dst_of_src)[(size_t)src] = b;
 		const i64* ib = t.index(src);
 		const i64* db = t.dims(src);
 		i64 size = 1;

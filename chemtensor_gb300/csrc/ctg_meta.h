@@ -61,8 +61,9 @@ Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::
 // Structure of the result of block_sparse_tensor_dot (src/tensor/block_sparse_tensor.c:1826-1900).
 Meta dot_result_meta(const Meta& s, int axs, const Meta& t, int axt, int nmult);
 
-// Structure of a transposed tensor (block_sparse_tensor.c:785-870).
-Meta transpose_meta(const Meta& t, const int* perm);
+// Structure of a transposed tensor (block_sparse_tensor.c:785-870); dst_of_src (optional) receives,
+// for every block of t, the index of its permuted block in the result.
+Meta transpose_meta(const Meta& t, const int* perm, std::vector<int>* dst_of_src = nullptr);
 
 // Structure after flattening axes ax and ax+1 (block_sparse_tensor.c:950-1000).
 Meta flatten_meta(const Meta& t, int ax, int newdir);

@@ -565,7 +565,8 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 CopyLowering lower_transpose(const Meta& t, const int* perm)
 {
 	double ts0 = host_seconds();
-	auto out = std::make_shared<Meta>(transpose_meta(t, perm));
+	std::vector<int> dst_of_src;
+	auto out = std::make_shared<Meta>(transpose_meta(t, perm, &dst_of_src));
 	g_plan_stage[4] += host_seconds() - ts0;
 	ts0 = host_seconds();
 	const Meta& r = *out;
@@ -574,14 +575,11 @@ CopyLowering lower_transpose(const Meta& t, const int* perm)
 	std::vector<Chunk> chunks;
 	descs.reserve((size_t)t.nblocks);
 	chunks.reserve((size_t)t.nblocks);
-	std::vector<i64> ir(t.ndim);
 	for (int b = 0; b < t.nblocks; b++)
 	{
-		const i64* it = t.index(b);
 		const i64* td = t.dims(b);
-		for (int i = 0; i < t.ndim; i++) ir[i] = it[perm[i]];
-		const int rb = r.find(ir.data());
-		CTG_CHECK(rb >= 0, "transpose: missing block");
+		const int rb = dst_of_src[(size_t)b];
+		CTG_CHECK(rb >= 0 && rb < r.nblocks, "transpose: missing block");
 		i64 st[8];
 		st[t.ndim - 1] = 1;
 		for (int i = t.ndim - 2; i >= 0; i--) st[i] = st[i + 1] * td[i + 1];
