@@ -240,7 +240,8 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			{
 				run_of(ks, fs, s0, s1);
 				fs_prev = fs;
-				tcur = 0;
+				tcur = (size_t)(std::lower_bound(kt.begin(), kt.end(), ft, [](const Key& x, i64 y) { return x.f < y; }) -
+				                kt.begin());
 			}
 			while (tcur < kt.size() && kt[tcur].f < ft) tcur++;
 			const size_t t0 = tcur;
