@@ -29,6 +29,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -48,12 +49,24 @@ PRECISIONS = {"fp64": 0, "bf16x3": 1}
 SVD_TRAFFIC_PER_LAUNCH = 379136
 
 
-def build_inputs():
-    from chemtensor_gb300 import ctstructs as cs, hamiltonians as hm, native
+def build_inputs(host_only: bool = False):
+    """The workload's MPO and seeded start state. host_only: the start state comes from the oracle's
+    generator (bit-identical to the package's, which lives in the GPU library), so that the CPU arm
+    loads no GPU library at all."""
+    from chemtensor_gb300 import ctstructs as cs, hamiltonians as hm
     w = WORKLOAD
     H = hm.fermi_hubbard_1d(w["nsites"], w["t"], w["u"], w["mu"])
     sector = hm.encode_quantum_number_pair(w["nsites"], 0)
-    c = native.random_mps(w["nsites"], 4, hm.HUBBARD_QSITE, sector, w["max_vdim"], w["rng_seed"])
+    if host_only:
+        import oracle
+        q = np.ascontiguousarray(hm.HUBBARD_QSITE, dtype=np.int32)
+        c = cs.MPS()
+        if oracle.port().oracle_construct_random_mps(w["nsites"], 4, q.ctypes.data, sector, w["max_vdim"],
+                                                     w["rng_seed"], C.byref(c)) != 0:
+            raise RuntimeError("oracle_construct_random_mps failed")
+    else:
+        from chemtensor_gb300 import native
+        c = native.random_mps(w["nsites"], 4, hm.HUBBARD_QSITE, sector, w["max_vdim"], w["rng_seed"])
     psi0 = cs.read_mps(c)
     cs.free_mps(c)
     return H, psi0
@@ -76,7 +89,8 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+        out_dir = os.environ.get("CTGPU_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, f"ctgpu_clocks_{os.getpid()}_dev{device}.csv")
 
     def __enter__(self):
         try:
@@ -174,7 +188,7 @@ def run_oracle_sweeps_for(H, psi0, sweeps: int, threads: int, max_vdim: int):
 def bench_reference(args, world, rank):
     if rank != 0:
         return
-    H, psi0 = build_inputs()
+    H, psi0 = build_inputs(host_only=True)
     threads = os.cpu_count() or 1
     times, en, used = run_oracle_sweeps(H, psi0, args.warmup + args.steps, threads)
     t = float(np.sum(times[args.warmup:]))
@@ -282,6 +296,34 @@ def bench_gpu(args, world, rank, local):
            "note": "whole dmrg_twosite call from host structs with an empty plan cache: upload, "
                    "right-normalisation, environments, K sweeps from the start state, download; per step = per sweep"}
 
+    # 4) the same workload in mixed precision: split-BF16 local-H GEMMs on the tensor cores in every
+    # sweep but the last, which is FP64 (so the returned state and energies are FP64 results); same
+    # timing discipline as (1)
+    native.set_precision(PRECISIONS["bf16x3"])
+    lib.ctgpu_clear_plan_cache()
+    lib.ctgpu_set_l2_flush_bytes(L2_FLUSH_BYTES)
+    barrier(world)
+    _, en_mx, _ = call(W + K)
+    ms_mx, _ = native.sweep_times()
+    st_mx = native.last_stats()
+    native.set_precision(PRECISIONS["fp64"])
+    lib.ctgpu_set_l2_flush_bytes(0)
+    bulk = ms_mx[W:W + K - 1] if K > 1 else ms_mx[W:W + K]
+    t_bulk = dist_max(float(np.sum(bulk)) / 1e3, world)
+    t_all = dist_max(float(np.sum(ms_mx[W:W + K])) / 1e3, world)
+    mixed = {"precision": "bf16x3 (split-BF16, 3 products, FP32 accumulate) in sweeps 0..W+K-2, FP64 in the last",
+             "sweeps_per_s_reduced": world * len(bulk) / t_bulk if t_bulk > 0 else None,
+             "sweeps_per_s_incl_final_fp64": world * K / t_all if t_all > 0 else None,
+             "speedup_reduced_vs_fp64": (world * len(bulk) / t_bulk) / value if t_bulk > 0 else None,
+             "energy_last_sweep": float(en_mx[-1]),
+             "abs_dE_vs_fp64_arm": abs(float(en_mx[-1]) - float(en[-1])),
+             "max_abs_dE_over_sweeps": float(np.max(np.abs(en_mx - en))),
+             "lanczos_ms_per_sweep": st_mx["lanczos_ms"] / max(st_mx["sweeps"], 1),
+             "split_ms_per_sweep": st_mx["split_ms"] / max(st_mx["sweeps"], 1)}
+
+    # 5) local-Hamiltonian microbenchmark (synthetic D = 1024, 41 Gaussian sectors, Dw = 26)
+    local_h = local_h_measure(lib, args.matvecs)
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_dev / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -291,6 +333,7 @@ def bench_gpu(args, world, rank, local):
                    "l2": "256 MiB buffer overwritten before every sweep"},
         "clocks": clk.summary(), "gpu_launches": launches, "roofline": roofline, "e2e": e2e,
         "energy_last_sweep": float(en[-1]),
+        "mixed_precision": mixed, "local_h": local_h,
         "breakdown_ms_per_sweep": {"lanczos": stats["lanczos_ms"] / max(stats["sweeps"], 1),
                                    "svd_split": stats["split_ms"] / max(stats["sweeps"], 1),
                                    "svd_max_jacobi_sweeps": stats["svd_max_sweeps"],
@@ -320,35 +363,69 @@ def bench_gpu(args, world, rank, local):
     cs.free_mpo(cH)
 
 
-def bench_local_h(args, world, rank, local):
-    """Local-Hamiltonian microbenchmark: D = 1024 over 41 Gaussian sectors, Dw = 26, resident
-    operands, work lists built once, 1000 back-to-back applications per precision."""
+LOCAL_H_PRECISIONS = (("fp64", 0, 1), ("bf16x3", 1, 3))    # name, ctgpu_set_precision value, products issued
+
+
+def local_h_measure(lib, matvecs: int) -> dict:
+    """Local-Hamiltonian microbenchmark: synthetic a, h2, l, r (D = 1024 over 41 Gaussian sectors,
+    sigma = 6 sectors, Dw = 26, seeded N(0,1) blocks), operands resident, work lists built once,
+    `matvecs` back-to-back applications per precision timed with CUDA events. Returns per precision
+    ms per application and algorithmic TFLOP/s, the relative Frobenius error of each reduced precision
+    against FP64, and the tensor-core fraction against MEASURED_PEAKS.json."""
     from chemtensor_gb300 import ctstructs as cs, native, workloads as wl
-    lib = native.lib()
-    lib.ctgpu_set_device(local)
     a, h2, l, r = wl.local_h_microbench(D=1024, nsec=41, sigma=6.0, Dw=26, seed=1)
     ca, ch, cl, cr = (cs.BlockSparseTensor() for _ in range(4))
     for t, c in ((a, ca), (h2, ch), (l, cl), (r, cr)):
         cs.write_bst(t, c)
-    out = {}
-    results = {}
-    for name, prec in (("fp64", 0), ("bf16x3", 1)):
-        native.set_precision(prec)
-        ms, fl = C.c_double(), C.c_double()
-        ret = lib.ctgpu_time_local_hamiltonian(C.byref(ca), C.byref(ch), C.byref(cl), C.byref(cr), args.matvecs,
-                                               C.byref(ms), C.byref(fl))
-        if ret != 0:
-            raise RuntimeError(native.last_error())
-        b = cs.BlockSparseTensor()
-        if lib.ctgpu_apply_local_hamiltonian(C.byref(ca), C.byref(ch), C.byref(cl), C.byref(cr), C.byref(b)) != 0:
-            raise RuntimeError(native.last_error())
-        results[name] = cs.read_bst(b)
-        cs.free_bst(b)
-        per = ms.value / args.matvecs
-        out[name] = {"ms_per_matvec": per, "tflops": fl.value / (per * 1e-3) / 1e12, "flops_per_matvec": fl.value}
-    native.set_precision(0)
-    num = sum(float(np.sum((results["bf16x3"].blocks[k] - v) ** 2)) for k, v in results["fp64"].blocks.items())
+    out, results = {}, {}
+    old_prec = native.set_precision(0)
+    try:
+        for name, prec, _ in LOCAL_H_PRECISIONS:
+            native.set_precision(prec)
+            ms, fl = C.c_double(), C.c_double()
+            n = matvecs if prec != 0 else max(1, matvecs // 5)
+            ret = lib.ctgpu_time_local_hamiltonian(C.byref(ca), C.byref(ch), C.byref(cl), C.byref(cr), n,
+                                                   C.byref(ms), C.byref(fl))
+            if ret != 0:
+                raise RuntimeError(native.last_error())
+            b = cs.BlockSparseTensor()
+            if lib.ctgpu_apply_local_hamiltonian(C.byref(ca), C.byref(ch), C.byref(cl), C.byref(cr), C.byref(b)) != 0:
+                raise RuntimeError(native.last_error())
+            results[name] = cs.read_bst(b)
+            cs.free_bst(b)
+            per = ms.value / n
+            out[name] = {"ms_per_matvec": per, "tflops": fl.value / (per * 1e-3) / 1e12, "flops_per_matvec": fl.value,
+                         "matvecs_timed": n}
+    finally:
+        native.set_precision(old_prec)
+        for c in (ca, ch, cl, cr):
+            cs.free_bst(c)
     den = sum(float(np.sum(v ** 2)) for v in results["fp64"].blocks.values())
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    for name, prec, products in LOCAL_H_PRECISIONS:
+        if prec == 0:
+            continue
+        num = sum(float(np.sum((results[name].blocks[k] - v) ** 2)) for k, v in results["fp64"].blocks.items())
+        out[name]["rel_error_vs_fp64"] = (num / den) ** 0.5 if den > 0 else None
+        out[name]["products_issued"] = products
+        if "bf16_tflops" in peaks:
+            out[name]["tensor_frac_issued"] = products * out[name]["tflops"] / peaks["bf16_tflops"]
+            out[name]["tensor_frac_algorithmic"] = out[name]["tflops"] / peaks["bf16_tflops"]
+    out["workload"] = "local_h_microbench D=1024 nsec=41 sigma=6 Dw=26 d=4 seed=1 (operands resident)"
+    out["peak_source"] = "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in peaks else None
+    return out
+
+
+def bench_local_h(args, world, rank, local):
+    """Local-Hamiltonian microbenchmark as its own JSON line (see local_h_measure)."""
+    from chemtensor_gb300 import native
+    lib = native.lib()
+    lib.ctgpu_set_device(local)
+    out = local_h_measure(lib, args.matvecs)
     fp64_peak = float(lib.ctgpu_measure_fp64_tflops())
     line = {
         "metric": "local-H TFLOP/s (synthetic D=1024, 41 Gaussian sectors, Dw=26)", "value": out["bf16x3"]["tflops"],
@@ -356,22 +433,16 @@ def bench_local_h(args, world, rank, local):
         "ms_per_step": out["bf16x3"]["ms_per_matvec"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16x3+f32acc", "data": "synthetic (seeded N(0,1) blocks)",
         "config": {"workload": "local_h_microbench D=1024 nsec=41 sigma=6 Dw=26 d=4 seed=1", "l2": "operands resident"},
-        "fp64": out["fp64"], "bf16x3": out["bf16x3"],
-        "bf16x3_rel_error_vs_fp64": (num / den) ** 0.5 if den > 0 else None,
+        "local_h": out,
         "roofline": {"bound": "tensor", "achieved": out["bf16x3"]["tflops"], "peak": None, "unit": "TFLOP/s",
                      "note": "algorithmic FLOPs (2 m n k of the FP64 product); the split-BF16 form issues 3x that "
                              "on the tensor cores", "fp64_peak_live": fp64_peak,
                      "fp64_frac": out["fp64"]["tflops"] / fp64_peak if fp64_peak > 0 else None},
     }
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        line["roofline"]["peak"] = peaks["bf16_tflops"]
-        line["roofline"]["frac"] = 3 * out["bf16x3"]["tflops"] / peaks["bf16_tflops"]
+    if "tensor_frac_issued" in out["bf16x3"]:
+        line["roofline"]["peak"] = out["bf16x3"]["tflops"] / out["bf16x3"]["tensor_frac_algorithmic"]
+        line["roofline"]["frac"] = out["bf16x3"]["tensor_frac_issued"]
         line["roofline"]["peak_source"] = "MEASURED_PEAKS.json bf16_tflops (burst); frac counts the 3 products"
-    except Exception:
-        pass
-    for c in (ca, ch, cl, cr):
-        cs.free_bst(c)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -116,7 +116,16 @@ int ctgpu_get_last_stats(struct ctgpu_stats* out)
 	out->plan_hits = s.plan_hits;
 	out->plan_misses = s.plan_misses;
 	out->svd_flops = s.svd_flops;
+	out->near_ties = s.near_ties;
 	return 0;
+}
+
+ct_long ctgpu_get_bond_singular_values(int bond, double* out, ct_long max)
+{
+	if (bond < 0 || (size_t)bond >= g_stats.bond_sigma.size() || g_stats.bond_sigma[(size_t)bond].empty()) return -1;
+	const std::vector<double>& v = g_stats.bond_sigma[(size_t)bond];
+	for (ct_long i = 0; i < (ct_long)v.size() && i < max; i++) out[i] = v[(size_t)i];
+	return (ct_long)v.size();
 }
 
 const char* ctgpu_last_error(void) { return g_last_error.c_str(); }

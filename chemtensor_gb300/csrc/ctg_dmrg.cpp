@@ -169,6 +169,9 @@ TruncResult retained_bond_indices(const double* sigma, i64 n, double tol, bool r
 	double sqsum = 0;
 	for (auto& p : ss) { p.first = p.first * p.first; sqsum += p.first; }
 	if (sqsum == 0) return res;
+	// near-tie at the bond-dimension cut: the last discarded and the first kept value (ascending order)
+	if (max_vdim < n && max_vdim > 0)
+		res.near_tie = ss[(size_t)(n - max_vdim)].first - ss[(size_t)(n - max_vdim - 1)].first <= 1e-12 * sqsum;
 	if (relative_thresh)
 		for (auto& p : ss) p.first /= sqsum;
 	for (size_t i = 1; i < ss.size(); i++) ss[i].first += ss[i - 1].first;
@@ -326,7 +329,7 @@ DTensor head_tensor(Ctx& c, const DTensor& a0, double value)
 
 // mps_split_tensor_svd (src/state/mps.c:1119-1159) -> split_block_sparse_matrix_svd (bond_ops.c:15-138)
 int split_mps_svd(Ctx& c, const DTensor& a, i64 d, const std::vector<q32>& qsite, double tol, i64 max_vdim, bool distr_left,
-                  DTensor& a0, DTensor& a1, double* entropy)
+                  DTensor& a0, DTensor& a1, double* entropy, std::vector<double>* kept = nullptr, long* near_ties = nullptr)
 {
 	const i64 dd[2] = {d, d};
 	const int od[2] = {TENSOR_AXIS_OUT, TENSOR_AXIS_OUT};
@@ -345,6 +348,7 @@ int split_mps_svd(Ctx& c, const DTensor& a, i64 d, const std::vector<q32>& qsite
 	ret = op_svd_finish(c, pend);
 	if (ret < 0) return ret;
 	TruncResult tr = retained_bond_indices(sigma, sv.ns, tol, true, max_vdim);
+	if (tr.near_tie && near_ties) (*near_ties)++;
 	std::vector<double> sret;
 	if (tr.ind.empty())
 	{
@@ -357,6 +361,7 @@ int split_mps_svd(Ctx& c, const DTensor& a, i64 d, const std::vector<q32>& qsite
 		for (i64 i : tr.ind) sret.push_back(sigma[(size_t)i]);
 	}
 	*entropy = tr.entropy;
+	if (kept) *kept = sret;
 	DTensor m0 = op_slice(c, sv.u, 1, tr.ind);
 	DTensor m1 = op_slice(c, sv.vh, 0, tr.ind);
 	DBufPtr dsv = c.upload(sret.data(), sret.size() * sizeof(double));
@@ -643,6 +648,7 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 	const double t_setup = now_s();
 	st->setup_s = t_setup - t_up;
 
+	st->bond_sigma.assign((size_t)(L - 1), std::vector<double>());
 	// four events per bond step (start, Lanczos done, split done, environment done), read at the
 	// end of each sweep so that timing adds no host synchronisation
 	const int nbond = 2 * (L - 1);
@@ -663,7 +669,8 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		const double h1 = now_s();
 		double ent = 0;
 		// synchronises once (for the singular values); the Lanczos scalars have arrived by then
-		r = split_mps_svd(c, aopt, psi->d, qsite, tol_split, max_vdim, !left_to_right, A[i], A[i + 1], &ent);
+		r = split_mps_svd(c, aopt, psi->d, qsite, tol_split, max_vdim, !left_to_right, A[i], A[i + 1], &ent,
+		                  &st->bond_sigma[(size_t)i], &st->near_ties);
 		if (r < 0) return r;
 		if (h_sc->status != 0) return h_sc->status;
 		CTG_CUDA(cudaEventRecord(ev[2], c.stream()));

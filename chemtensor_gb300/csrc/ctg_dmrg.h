@@ -39,6 +39,12 @@ struct DmrgStats {
 	std::vector<double> sweep_ms;       // device time of every sweep (CUDA events on the stream)
 	std::vector<long> sweep_launches;   // kernels launched by every sweep
 	KProf prof[K_NUM_CLASSES];          // per kernel class, over the profiled sweeps
+	// retained singular values of the most recent split at every bond (after the last sweep: those of
+	// its right-to-left pass), in the order the truncation keeps them
+	std::vector<std::vector<double>> bond_sigma;
+	// splits whose bond-dimension cut fell between two singular values closer than 1e-12 of the sum of
+	// squares (the kept set then depends on the order of near-equal values)
+	long near_ties = 0;
 };
 
 // Same contract as dmrg_twosite (src/algorithm/dmrg.c:262-399).
@@ -53,6 +59,8 @@ int dmrg_singlesite_gpu(const struct mpo* hamiltonian, int num_sweeps, int maxit
 struct TruncResult {
 	std::vector<i64> ind;
 	double norm_sigma = 0, entropy = 0, tol_eff = 0;
+	// the cut at max_vdim separates two squared singular values less than 1e-12 of their sum apart
+	bool near_tie = false;
 };
 TruncResult retained_bond_indices(const double* sigma, i64 n, double tol, bool relative_thresh, i64 max_vdim);
 

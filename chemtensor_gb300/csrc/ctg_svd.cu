@@ -1511,7 +1511,11 @@ k_svd_global(const SvdDesc* __restrict__ descs, int first, const double* __restr
 // variant whose workspace is this fixed array: every GPU that loads the library keeps it
 // (4 MiB) until the process exits, and it bounds the block to NOALLOC_SVD_MAX_DIM rows and
 // columns. All calls share the array, so calls whose work overlaps on the GPU (for example on
-// two streams) race on it and must be serialised by the caller.
+// two streams) race on it and must be serialised by the caller. With lazy module loading (the
+// CUDA default), the array's memory and the library's kernels are loaded onto a device by the
+// first call there (or by any first use of the library on that device); a caller that reserves
+// the rest of the device for its own pool makes that first call before reserving, or sets
+// CUDA_MODULE_LOADING=EAGER.
 
 constexpr int NOALLOC_SVD_MAX_DIM = 256;
 constexpr i64 NOALLOC_SCRATCH_DOUBLES = (i64)1 << 19;   // 4 MiB
@@ -1565,6 +1569,16 @@ extern "C" int ctgpu_dense_svd_noalloc(const double* d_a, int m, int n, double* 
 	}
 	if (NA_WORK + svd_scratch_doubles(m, n) > NOALLOC_SCRATCH_DOUBLES) return -5;
 	if (!d_a || !d_u || !d_s || !d_vh || !d_info) return -5;
+	// an error left by the caller's earlier work is not this call's to consume: report and leave it
+	{
+		const cudaError_t pending = cudaPeekAtLastError();
+		if (pending != cudaSuccess)
+		{
+			fprintf(stderr, "ctgpu_dense_svd_noalloc: a CUDA error from earlier work is pending (%s); nothing queued\n",
+			        cudaGetErrorString(pending));
+			return -5;
+		}
+	}
 	int dev = 0;
 	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -5;
 	// device address of the fixed array, taken once per device with that device current
@@ -1594,7 +1608,17 @@ extern "C" int ctgpu_dense_svd_noalloc(const double* d_a, int m, int n, double* 
 	d.w_off = 0;
 	d.m = m;
 	d.n = n;
-	k_noalloc_prepare<<<64, 256, 0, st>>>(base, d, d_u, d_s, d_vh);
+	// every launch reports its own status (cudaLaunchKernel / cudaLaunchKernelEx return it), so this
+	// call never reads or clears the thread's last-error state on behalf of other work
+	{
+		void* args[] = {&base, &d, &d_u, &d_s, &d_vh};
+		const cudaError_t e = cudaLaunchKernel((const void*)k_noalloc_prepare, dim3(64), dim3(256), args, 0, st);
+		if (e != cudaSuccess)
+		{
+			fprintf(stderr, "ctgpu_dense_svd_noalloc: launch failed: %s\n", cudaGetErrorString(e));
+			return -5;
+		}
+	}
 	const SvdDesc* descs = (const SvdDesc*)(base + NA_DESC);
 	int* status = (int*)(base + NA_STATUS);
 	double* flops = base + NA_STATUS + 1;
@@ -1603,8 +1627,9 @@ extern "C" int ctgpu_dense_svd_noalloc(const double* d_a, int m, int n, double* 
 		const int maxcl = svd_max_cluster(dev);
 		launch_svd_group(svd_launch_for(m, n, maxcl, maxcl), 0, 1, descs, d_a, d_u, d_s, d_vh, base + NA_WORK, status,
 		                 flops, st);
-		k_noalloc_finish<<<1, 1, 0, st>>>(base, d_info);
-		const cudaError_t e = cudaGetLastError();
+		const double* cbase = base;
+		void* args[] = {(void*)&cbase, &d_info};
+		const cudaError_t e = cudaLaunchKernel((const void*)k_noalloc_finish, dim3(1), dim3(1), args, 0, st);
 		if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
 	}
 	catch (const std::exception& ex)

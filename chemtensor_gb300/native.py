@@ -47,6 +47,8 @@ EXPORTS = [
     "ctgpu_get_sweep_times",
     "ctgpu_get_kernel_profile",
     "ctgpu_measure_fp64_tflops",
+    "ctgpu_get_bond_singular_values",
+    "ctgpu_dense_svd_noalloc",
 ]
 
 KERNEL_CLASSES = ["block_gemm", "permute", "row_map", "axis_scale", "block_svd", "block_rq", "lanczos_vector",
@@ -65,7 +67,7 @@ class Stats(C.Structure):
         ("total_gemm_flops", C.c_double), ("matvecs", C.c_long), ("kernel_launches", C.c_long),
         ("sweeps", C.c_int), ("max_bond_dim", C.c_int64), ("svd_max_sweeps", C.c_int),
         ("host_plan_s", C.c_double), ("plan_hits", C.c_long), ("plan_misses", C.c_long),
-        ("svd_flops", C.c_double),
+        ("svd_flops", C.c_double), ("near_ties", C.c_long),
     ]
 
 
@@ -108,6 +110,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_get_sweep_times.argtypes = [P, P, C.c_int]
     lib.ctgpu_get_kernel_profile.argtypes = [C.c_int, P, P, P, P]
     lib.ctgpu_measure_fp64_tflops.restype = C.c_double
+    lib.ctgpu_get_bond_singular_values.argtypes = [C.c_int, P, C.c_int64]
+    lib.ctgpu_get_bond_singular_values.restype = C.c_int64
     return lib
 
 
@@ -146,6 +150,16 @@ def kernel_profile() -> dict:
         lib().ctgpu_get_kernel_profile(i, C.byref(la), C.byref(ms), C.byref(fl), C.byref(by))
         out[name] = {"launches": la.value, "ms": ms.value, "flops": fl.value, "bytes": by.value}
     return out
+
+
+def bond_singular_values(bond: int) -> np.ndarray | None:
+    """Retained singular values of the last split at `bond` in this thread's last dmrg_twosite call."""
+    n = lib().ctgpu_get_bond_singular_values(bond, None, 0)
+    if n < 0:
+        return None
+    out = np.zeros(max(n, 1))
+    lib().ctgpu_get_bond_singular_values(bond, out.ctypes.data, n)
+    return out[:n]
 
 
 def set_precision(p: int) -> int:

@@ -91,8 +91,18 @@ struct ctgpu_stats
 	long   plan_misses;       /* lowered operations built afresh */
 	double svd_flops;         /* FP64 flops of the block SVDs: Jacobi inner products and rotations as
 	                             executed, QR and output factors estimated at full rank */
+	long   near_ties;         /* SVD splits whose max_vdim cut fell between two squared singular values
+	                             closer than 1e-12 of their sum: the kept set then depends on how equal
+	                             values are ordered (the reference sorts with the C library's qsort) */
 };
 int ctgpu_get_last_stats(struct ctgpu_stats* out);
+
+/* Retained singular values (in the order the truncation keeps them, as split_block_sparse_matrix_svd
+ * passes them on, src/algorithm/bond_ops.c:15-138) of the most recent split at bond `bond` (sites
+ * bond, bond + 1) in this thread's last dmrg_twosite call; after a completed call these are the
+ * values of the final right-to-left pass. Fills up to max entries of out and returns the count, or
+ * -1 if that bond was not split. No counterpart in the reference. */
+ct_long ctgpu_get_bond_singular_values(int bond, double* out, ct_long max);
 
 /* Message of the most recent failure in this thread ("" if none). */
 const char* ctgpu_last_error(void);
@@ -210,8 +220,13 @@ void ctgpu_delete_block_sparse_tensor(struct block_sparse_tensor* t);
  * values in descending order; *d_info (device) becomes 0, or -1 if the Jacobi iteration did not
  * converge. The work is queued on 'stream' (a cudaStream_t, or NULL for the legacy default stream)
  * and the call returns without waiting; it returns 0 once queued, -5 for sizes outside 1..256, a
- * null pointer or a CUDA error. The first call on a device looks up the array's device address
- * (once per device, with that device current); make that first call before any stream capture.
+ * null pointer, a CUDA error of one of its own launches, or a CUDA error already pending from the
+ * caller's earlier work (which it reports and leaves in place, queueing nothing). The first call on
+ * a device looks up the array's device address (once per device, with that device current); make
+ * that first call before any stream capture. With lazy module loading (the CUDA default) that first
+ * call, or the first use of the library on a device, also loads the library's kernels and the 4 MiB
+ * array onto the device: a caller that reserves the rest of device memory for its own pool makes
+ * the first call before reserving it, or runs with CUDA_MODULE_LOADING=EAGER.
  * All calls share the array, so calls whose work overlaps on the GPU race and must be serialised
  * by the caller.
  * No counterpart in the reference, which computes block SVDs with LAPACK on the host. */

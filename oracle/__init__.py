@@ -22,8 +22,11 @@ def build_port() -> str:
     return PORT
 
 
-def build_ref(refdir: str = "/root/reference") -> str | None:
-    if not os.path.isdir(refdir):
+def build_ref(refdir: str | None = None) -> str | None:
+    """Compile the reference from its own sources into _ref/ (x86 container only). The checkout is
+    named by the argument or the CHEMTENSOR_REFERENCE_DIR environment variable; None if absent."""
+    refdir = refdir or os.environ.get("CHEMTENSOR_REFERENCE_DIR")
+    if not refdir or not os.path.isdir(refdir):
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={refdir}"], check=True)
     return REF
@@ -60,6 +63,9 @@ def port() -> C.CDLL:
         lib.oracle_delete_block_sparse_tensor.restype = None
         lib.oracle_set_num_threads.argtypes = [C.c_int]
         lib.oracle_get_sweep_times.argtypes = [P, C.c_int]
+        lib.oracle_get_bond_sigma.argtypes = [C.c_int, P, C.c_int64]
+        lib.oracle_get_bond_sigma.restype = C.c_int64
+        lib.oracle_construct_random_mps.argtypes = [C.c_int, C.c_int64, P, C.c_int32, C.c_int64, C.c_uint64, P]
         _port = lib
     return _port
 
@@ -75,3 +81,14 @@ def reference() -> C.CDLL | None:
     lib.ref_mps_vdot_real.argtypes = [P, P]
     lib.ref_mps_vdot_real.restype = C.c_double
     return lib
+
+
+def bond_sigma(lib: C.CDLL, bond: int):
+    """Retained singular values of the last split at `bond` in the last oracle_dmrg_twosite call."""
+    import numpy as np
+    n = lib.oracle_get_bond_sigma(bond, None, 0)
+    if n < 0:
+        return None
+    out = np.zeros(max(n, 1))
+    lib.oracle_get_bond_sigma(bond, out.ctypes.data, n)
+    return out[:n]

@@ -917,6 +917,31 @@ ct_long oracle_retained_bond_indices(const double* sigma, ct_long n, double tol,
 	return num;
 }
 
+/* retained singular values of the most recent split at every bond of the last oracle_dmrg_twosite
+ * call (after the final sweep: those of its right-to-left pass) */
+#define MAX_BONDS 4096
+static double* g_bond_sigma[MAX_BONDS];
+static ct_long g_bond_nsigma[MAX_BONDS];
+static double* g_split_sigma = NULL;     /* written by split_matrix_svd */
+static ct_long g_split_nsigma = 0;
+
+ct_long oracle_get_bond_sigma(int bond, double* out, ct_long max)
+{
+	if (bond < 0 || bond >= MAX_BONDS || !g_bond_sigma[bond]) return -1;
+	for (ct_long i = 0; i < g_bond_nsigma[bond] && i < max; i++) out[i] = g_bond_sigma[bond][i];
+	return g_bond_nsigma[bond];
+}
+
+static void record_bond_sigma(int bond)
+{
+	if (bond < 0 || bond >= MAX_BONDS) return;
+	free(g_bond_sigma[bond]);
+	g_bond_sigma[bond] = g_split_sigma;
+	g_bond_nsigma[bond] = g_split_nsigma;
+	g_split_sigma = NULL;
+	g_split_nsigma = 0;
+}
+
 /* ---- split_block_sparse_matrix_svd (bond_ops.c:15-138), renormalize = false ---- */
 
 static int split_matrix_svd(const struct block_sparse_tensor* a, double tol, ct_long max_vdim, int distr_left,
@@ -942,6 +967,10 @@ static int split_matrix_svd(const struct block_sparse_tensor* a, double tol, ct_
 		sret = xmalloc(num * sizeof(double));
 		for (ct_long i = 0; i < num; i++) sret[i] = s[ind[i]];
 	}
+	free(g_split_sigma);
+	g_split_sigma = xmalloc(num * sizeof(double));
+	memcpy(g_split_sigma, sret, num * sizeof(double));
+	g_split_nsigma = num;
 	struct block_sparse_tensor m0, m1;
 	bst_slice(&u, 1, ind, num, &m0);
 	bst_slice(&vh, 0, ind, num, &m1);
@@ -1407,6 +1436,7 @@ int oracle_dmrg_twosite(const struct mpo* ham, int num_sweeps, int maxiter, doub
 			ret = split_mps_tensor_svd(&opt, psi->d, psi->qsite, tol_split, max_vdim, 0, &psi->a[i], &psi->a[i + 1], &ent);
 			oracle_delete_block_sparse_tensor(&opt);
 			if (ret < 0) break;
+			record_bond_sigma(i);
 			oracle_delete_block_sparse_tensor(&lb[i + 1]);
 			oracle_contraction_operator_step_left(&psi->a[i], &psi->a[i], &ham->a[i], &lb[i], &lb[i + 1]);
 		}
@@ -1423,6 +1453,7 @@ int oracle_dmrg_twosite(const struct mpo* ham, int num_sweeps, int maxiter, doub
 			ret = split_mps_tensor_svd(&opt, psi->d, psi->qsite, tol_split, max_vdim, 1, &psi->a[i], &psi->a[i + 1], &ent);
 			oracle_delete_block_sparse_tensor(&opt);
 			if (ret < 0) break;
+			record_bond_sigma(i);
 			entropy[i] = ent;
 			oracle_delete_block_sparse_tensor(&rb[i]);
 			oracle_contraction_operator_step_right(&psi->a[i + 1], &psi->a[i + 1], &ham->a[i + 1], &rb[i + 1], &rb[i]);
@@ -1541,4 +1572,129 @@ int oracle_set_num_threads(int n)
 	if (n > 0) omp_set_num_threads(n);
 	scipy_openblas_set_num_threads(1);
 	return omp_get_max_threads();
+}
+
+/* ---- seeded random MPS: seed_rng_state, rand_interval, rand_choice, randu, randn (rng.c:15-125),
+ *      the PCG32 generators they use (pcg_basic.c:33-54, :115-151), and construct_random_mps
+ *      (mps.c:93-175), real double precision ---- */
+
+struct pcg32 { uint64_t state, inc; };
+
+static uint32_t pcg32_next(struct pcg32* g)
+{
+	const uint64_t old = g->state;
+	g->state = old * 6364136223846793005ULL + g->inc;
+	const uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+	const uint32_t rot = (uint32_t)(old >> 59u);
+	return (xs >> rot) | (xs << ((-rot) & 31));
+}
+
+static void pcg32_seed(struct pcg32* g, uint64_t initstate, uint64_t initseq)
+{
+	g->state = 0;
+	g->inc = (initseq << 1u) | 1u;
+	pcg32_next(g);
+	g->state += initstate;
+	pcg32_next(g);
+}
+
+struct orng { struct pcg32 g[2]; };
+
+static uint64_t orng_u64(struct orng* r)
+{
+	const uint64_t hi = pcg32_next(&r->g[0]);
+	return (hi << 32) | pcg32_next(&r->g[1]);
+}
+
+static void orng_seed(struct orng* r, uint64_t seed)
+{
+	struct pcg32 t;
+	pcg32_seed(&t, seed, 6364136223846793005ULL * seed + 1442695040888963407ULL);
+	uint64_t v[4];
+	for (int i = 0; i < 4; i++) { const uint64_t hi = pcg32_next(&t); v[i] = (hi << 32) | pcg32_next(&t); }
+	const uint64_t mask = ~0ull >> 1;
+	if ((v[2] & mask) == (v[3] & mask)) v[3] = ~v[3];
+	pcg32_seed(&r->g[0], v[0], v[2]);
+	pcg32_seed(&r->g[1], v[1], v[3]);
+}
+
+static uint64_t orng_bounded(struct orng* r, uint64_t bound)
+{
+	const uint64_t threshold = (0 - bound) % bound;
+	for (;;) { const uint64_t x = orng_u64(r); if (x >= threshold) return x % bound; }
+}
+
+static double orng_normal(struct orng* r)
+{
+	double u1 = ldexp((double)orng_u64(r), -64);
+	const double u2 = ldexp((double)orng_u64(r), -64);
+	if (u1 == 0) u1 = 1;
+	return sqrt(-2 * log(u1)) * sin(6.2831853071795864769 * u2);
+}
+
+/* bond quantum numbers of one virtual bond: all outer sums, or a Floyd sample of max_vdim of them */
+static qnumber* random_bond(struct orng* r, const qnumber* prev, ct_long nprev, int sign, const qnumber* qsite, ct_long d,
+                            ct_long max_vdim, ct_long* nout)
+{
+	const ct_long nfull = nprev * d;
+	qnumber* full = xmalloc(nfull * sizeof(qnumber));
+	for (ct_long i = 0; i < nprev; i++)
+		for (ct_long j = 0; j < d; j++) full[i * d + j] = prev[i] + sign * qsite[j];
+	if (nfull <= max_vdim) { *nout = nfull; return full; }
+	uint64_t* idx = xmalloc(max_vdim * sizeof(uint64_t));
+	for (uint64_t i = 0; i < (uint64_t)max_vdim; i++)
+	{
+		const uint64_t j = (uint64_t)nfull - (uint64_t)max_vdim + 1 + i;
+		const uint64_t t = orng_bounded(r, j);
+		int drawn = 0;
+		for (uint64_t k = 0; k < i; k++) if (idx[k] == t) { drawn = 1; break; }
+		idx[i] = drawn ? j - 1 : t;
+	}
+	qnumber* sel = xmalloc(max_vdim * sizeof(qnumber));
+	for (ct_long i = 0; i < max_vdim; i++) sel[i] = full[idx[i]];
+	free(idx);
+	free(full);
+	*nout = max_vdim;
+	return sel;
+}
+
+int oracle_construct_random_mps(int nsites, ct_long d, const qnumber* qsite, qnumber qnum_sector, ct_long max_vdim,
+                                uint64_t rng_seed, struct mps* mps)
+{
+	if (nsites < 1 || d < 1 || max_vdim < 1) return -1;
+	struct orng r;
+	orng_seed(&r, rng_seed);
+	ct_long* nb = xcalloc(nsites + 1, sizeof(ct_long));
+	qnumber** qb = xcalloc(nsites + 1, sizeof(qnumber*));
+	nb[0] = 1; qb[0] = xcalloc(1, sizeof(qnumber));
+	nb[nsites] = 1; qb[nsites] = xmalloc(sizeof(qnumber)); qb[nsites][0] = qnum_sector;
+	for (int l = 1; l < (nsites + 1) / 2; l++) qb[l] = random_bond(&r, qb[l - 1], nb[l - 1], 1, qsite, d, max_vdim, &nb[l]);
+	for (int l = nsites - 1; l >= (nsites + 1) / 2; l--) qb[l] = random_bond(&r, qb[l + 1], nb[l + 1], -1, qsite, d, max_vdim, &nb[l]);
+	mps->nsites = nsites;
+	mps->d = d;
+	mps->qsite = xmalloc(d * sizeof(qnumber));
+	memcpy(mps->qsite, qsite, d * sizeof(qnumber));
+	mps->a = xcalloc(nsites, sizeof(struct block_sparse_tensor));
+	const enum tensor_axis_direction dir[3] = { TENSOR_AXIS_OUT, TENSOR_AXIS_OUT, TENSOR_AXIS_IN };
+	for (int l = 0; l < nsites; l++)
+	{
+		const ct_long dim[3] = { nb[l], d, nb[l + 1] };
+		const qnumber* qn[3] = { qb[l], qsite, qb[l + 1] };
+		bst_alloc(3, dim, dir, qn, &mps->a[l]);
+		/* block_sparse_tensor_fill_random_normal: blocks in index order, entries alpha * randn + 0 */
+		const double alpha = 1.0 / sqrt((double)(dim[0] * dim[1] * dim[2]));
+		const ct_long nblk = iprod(mps->a[l].dim_blocks, 3);
+		for (ct_long k = 0; k < nblk; k++)
+		{
+			struct dense_tensor* b = mps->a[l].blocks[k];
+			if (!b) continue;
+			double* v = b->data;
+			const ct_long ne = iprod(b->dim, b->ndim);
+			for (ct_long j = 0; j < ne; j++) v[j] = alpha * orng_normal(&r) + 0.0;
+		}
+	}
+	for (int l = 0; l <= nsites; l++) free(qb[l]);
+	free(qb);
+	free(nb);
+	return 0;
 }

@@ -75,6 +75,16 @@ void oracle_delete_block_sparse_tensor(struct block_sparse_tensor* t);
 /* wall time in seconds of every sweep of the last oracle_dmrg_twosite call; returns the count */
 int oracle_get_sweep_times(double* out, int max);
 
+/* retained singular values (in the order the truncation keeps them) of the most recent split at
+ * bond `bond` (sites bond, bond+1) during the last oracle_dmrg_twosite call; fills up to max
+ * entries and returns the count, or -1 if that bond was never split */
+ct_long oracle_get_bond_sigma(int bond, double* out, ct_long max);
+
+/* construct_random_mps (src/state/mps.c:93-175) after seed_rng_state(rng_seed) (src/util/rng.c:15-27),
+ * real double precision; returns 0, or -1 on invalid arguments */
+int oracle_construct_random_mps(int nsites, ct_long d, const qnumber* qsite, qnumber qnum_sector, ct_long max_vdim,
+	uint64_t rng_seed, struct mps* mps);
+
 /* number of OpenMP threads the oracle runs with (set via OMP_NUM_THREADS or this call) */
 int oracle_set_num_threads(int n);
 

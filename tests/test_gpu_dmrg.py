@@ -47,6 +47,39 @@ def test_dmrg_with_package_hamiltonian_matches_oracle(gpu, oracle_port):
     assert same_structure(p1, p2)
 
 
+def test_dmrg_hubbard_L32_D256_matches_oracle(gpu, oracle_port):
+    """The headline workload (Fermi-Hubbard L=32, t=1, U=4, (N, 2Sz) = (32, 0), D=256, maxiter 5,
+    tol 1e-10, seeded start state 42), two sweeps, against the oracle on the host cores: energies
+    within 1e-10, every bond's quantum numbers bit-exact, the retained singular values of every bond
+    within 1e-8 relative, |<psi_gpu|psi_oracle>| = 1 within 1e-9."""
+    import oracle
+    L, D, sweeps = 32, 256, 2
+    H = hm.fermi_hubbard_1d(L, 1.0, 4.0, 0.0)
+    c = native.random_mps(L, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(L, 0), D, 42)
+    psi0 = cs.read_mps(c)
+    cs.free_mps(c)
+    r1, e1, s1, p1 = run_gpu_dmrg(gpu, H, psi0, sweeps, 5, 1e-10, D)
+    assert r1 == 0, native.last_error()
+    st = native.last_stats()
+    sig_gpu = [native.bond_singular_values(b) for b in range(L - 1)]
+    oracle_port.oracle_set_num_threads(0)
+    r2, e2, s2, p2 = run_oracle_dmrg(oracle_port, H, psi0, sweeps, 5, 1e-10, D)
+    assert r2 == 0
+    sig_orc = [oracle.bond_sigma(oracle_port, b) for b in range(L - 1)]
+    np.testing.assert_allclose(e1, e2, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(s1, s2, rtol=0, atol=1e-8)
+    assert same_structure(p1, p2)
+    assert max(t.dim_logical[2] for t in p1.tensors) == D
+    # no bond-dimension cut fell between near-equal singular values, so the kept sets do not depend
+    # on how equal values are ordered
+    assert st["near_ties"] == 0
+    for b in range(L - 1):
+        assert sig_gpu[b] is not None and sig_orc[b] is not None, b
+        assert len(sig_gpu[b]) == len(sig_orc[b]), b
+        np.testing.assert_allclose(sig_gpu[b], sig_orc[b], rtol=1e-8, atol=0, err_msg=f"bond {b}")
+    assert abs(abs(overlap(oracle_port, p1, p2)) - 1) < 1e-9
+
+
 def test_python_entry_point_mirrors_reference_binding(gpu):
     H = hm.heisenberg_xxz_1d(10, 1.0, 1.0, 0.0)
     psi, en, ent = ctg.dmrg(H, num_sweeps=3, maxiter_lanczos=5, tol_split=1e-10, max_vdim=16, qnum_sector=0, rng_seed=7)

@@ -34,6 +34,25 @@ def test_random_mps_bitwise(gpu, tag):
         assert np.array_equal(a.serialize(), b.serialize())
 
 
+@pytest.mark.parametrize("tag", ["heis_L12_D8_s1", "hub_L8_D24_s3", "hub_L10_D16_s42"])
+def test_oracle_random_mps_bitwise(oracle_port, tag):
+    """The oracle's own seeded generator (used by the CPU baseline, which loads no GPU library)
+    reproduces the reference's construct_random_mps bit for bit."""
+    import ctypes as C
+    g = golden("random_mps.npz")
+    L, sector, D, seed = [int(x) for x in g[f"{tag}_params"]]
+    ref = cs.chain_from_arrays(tag, g)
+    q = np.ascontiguousarray(ref.qsite, dtype=np.int32)
+    c = cs.MPS()
+    assert oracle_port.oracle_construct_random_mps(L, ref.d, q.ctypes.data, sector, D, seed, C.byref(c)) == 0
+    mine = cs.read_mps(c)
+    cs.free_mps(c)
+    for a, b in zip(mine.tensors, ref.tensors):
+        assert a.dim_logical == b.dim_logical
+        assert all(np.array_equal(x, y) for x, y in zip(a.qnums_logical, b.qnums_logical))
+        assert np.array_equal(a.serialize(), b.serialize())
+
+
 def test_heisenberg_mpo_equals_reference_operator():
     g = golden("mpo_reference.npz")
     a = hm.mpo_to_matrix(cs.chain_from_arrays("heis6", g))

@@ -76,6 +76,39 @@ def test_dense_svd_noalloc_matches_block_svd(gpu):
         np.testing.assert_allclose(vh @ vh.T, np.eye(k), rtol=0, atol=1e-10)
 
 
+@pytest.mark.parametrize("m,n", [(1, 1), (1, 7), (7, 1), (3, 2), (256, 256), (256, 17), (17, 256)])
+def test_dense_svd_noalloc_edge_shapes(gpu, m, n):
+    """The documented limits: single rows and columns, tiny blocks (most CTAs of the cluster own no
+    column) and the 256 x 256 maximum the fixed workspace is sized for."""
+    torch = pytest.importorskip("torch")
+    fn = gpu.ctgpu_dense_svd_noalloc
+    fn.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    rng = np.random.default_rng(m * 1000 + n)
+    a = _graded(rng, m, n) if min(m, n) > 1 else rng.standard_normal((m, n))
+    k = min(m, n)
+    d_a = torch.from_numpy(a).to(dev)
+    d_u = torch.full((m * k,), np.nan, dtype=torch.float64, device=dev)
+    d_s = torch.full((k,), np.nan, dtype=torch.float64, device=dev)
+    d_vh = torch.full((k * n,), np.nan, dtype=torch.float64, device=dev)
+    d_info = torch.full((1,), 7, dtype=torch.int32, device=dev)
+    assert fn(d_a.data_ptr(), m, n, d_u.data_ptr(), d_s.data_ptr(), d_vh.data_ptr(), d_info.data_ptr(),
+              stream.cuda_stream) == 0
+    torch.cuda.synchronize(dev)
+    assert int(d_info.item()) == 0
+    s = d_s.cpu().numpy()
+    u = d_u.cpu().numpy().reshape(m, k)
+    vh = d_vh.cpu().numpy().reshape(k, n)
+    ref = np.linalg.svd(a, compute_uv=False)
+    np.testing.assert_allclose(s, ref, rtol=1e-10, atol=1e-14 * ref.max())
+    assert np.all(np.diff(s) <= 0)
+    np.testing.assert_allclose((u * s) @ vh, a, rtol=0, atol=1e-12 * np.abs(a).max())
+    np.testing.assert_allclose(u.T @ u, np.eye(k), rtol=0, atol=1e-10)
+    np.testing.assert_allclose(vh @ vh.T, np.eye(k), rtol=0, atol=1e-10)
+
+
 def test_dense_svd_noalloc_rejects_oversized_blocks(gpu):
     torch = pytest.importorskip("torch")
     fn = gpu.ctgpu_dense_svd_noalloc
