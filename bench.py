@@ -44,7 +44,7 @@ WORKLOAD = {"workload": "fermi_hubbard_1d L=32 t=1 U=4 mu=0 (N,2Sz)=(32,0) D=256
 METRIC = "two-site DMRG sweeps/s (Fermi-Hubbard L=32, D=256)"
 UNIT = "sweeps/s"
 L2_FLUSH_BYTES = 256 << 20
-PRECISIONS = {"fp64": 0, "bf16x3": 1}
+PRECISIONS = {"fp64": 0, "bf16x3": 1, "tf32": 2, "bf16x6": 3}
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_svd_tour launch (ncu, see profiles/)
 SVD_TRAFFIC_PER_LAUNCH = 379136
 
@@ -327,13 +327,13 @@ def bench_gpu(args, world, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_dev / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp64": "f64", "bf16x3": "bf16x3+f32acc, final sweep f64"}[args.precision],
+        "dtype": "f64" if args.precision == "fp64" else f"{args.precision}+f32acc, final sweep f64",
         "data": "synthetic",
         "config": {"workload": w["workload"], "precision": args.precision, "parallelism": f"replicas x{world}",
                    "l2": "256 MiB buffer overwritten before every sweep"},
         "clocks": clk.summary(), "gpu_launches": launches, "roofline": roofline, "e2e": e2e,
         "energy_last_sweep": float(en[-1]),
-        "mixed_precision": mixed, "local_h": local_h,
+        "mixed_precision": mixed, "local_h": local_h, "tile_tuning": native.tile_tuning(),
         "breakdown_ms_per_sweep": {"lanczos": stats["lanczos_ms"] / max(stats["sweeps"], 1),
                                    "svd_split": stats["split_ms"] / max(stats["sweeps"], 1),
                                    "svd_max_jacobi_sweeps": stats["svd_max_sweeps"],
@@ -363,7 +363,7 @@ def bench_gpu(args, world, rank, local):
     cs.free_mpo(cH)
 
 
-LOCAL_H_PRECISIONS = (("fp64", 0, 1), ("bf16x3", 1, 3))    # name, ctgpu_set_precision value, products issued
+LOCAL_H_PRECISIONS = (("fp64", 0, 1), ("bf16x3", 1, 3), ("tf32", 2, 1), ("bf16x6", 3, 6))   # name, ctgpu_set_precision value, products issued
 
 
 def local_h_measure(lib, matvecs: int) -> dict:
@@ -528,16 +528,20 @@ def bench_molecular(args, world, rank, local):
                                    f"integrals seed=7 start seed=42", "mpo_bond_dims_max": max(
                                        t.dim_logical[0] for t in H.tensors), "mpo_build_s": t_mpo},
             "runs": runs}
-    mixed = [k for k in ("bf16x3env", "bf16x3") if k in runs]
+    mixed = [k for k in runs if k != "fp64"]
     if "fp64" in runs and mixed:
-        a, b = runs["fp64"], runs[mixed[0]]
-        line["mixed_run"] = mixed[0]
-        # the split-BF16 run's last sweep is FP64: compare the mean of the bulk sweeps after the first
+        a = runs["fp64"]
+        # a reduced-precision run's last sweep is FP64: compare the mean of the bulk sweeps after the first
         bulk = lambda r, k: float(np.mean(r["sweep_ms"][1:k])) if k > 1 else float(r["sweep_ms"][0])
-        line["value"] = bulk(b, S - 1)
-        line["speedup_bulk_sweeps_bf16x3_vs_fp64"] = bulk(a, S - 1) / bulk(b, S - 1)
-        line["speedup_total_vs_fp64"] = sum(a["sweep_ms"]) / sum(b["sweep_ms"])
-        line["abs_dE_final"] = abs(a["energies"][-1] - b["energies"][-1])
+        for name in mixed:
+            b = runs[name]
+            b["speedup_bulk_sweeps_vs_fp64"] = bulk(a, S - 1) / bulk(b, S - 1)
+            b["speedup_total_vs_fp64"] = sum(a["sweep_ms"]) / sum(b["sweep_ms"])
+            b["abs_dE_final_vs_fp64"] = abs(a["energies"][-1] - b["energies"][-1])
+        line["mixed_run"] = mixed[0]
+        line["value"] = bulk(runs[mixed[0]], S - 1)
+        line["speedup_total_vs_fp64"] = runs[mixed[0]]["speedup_total_vs_fp64"]
+        line["abs_dE_final"] = runs[mixed[0]]["abs_dE_final_vs_fp64"]
     if rank == 0:
         print(json.dumps(line), flush=True)
 

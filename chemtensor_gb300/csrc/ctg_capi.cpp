@@ -1,4 +1,5 @@
 // ctg_capi.cpp - extern "C" boundary (include/ctgpu.h).
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <cmath>
@@ -14,7 +15,8 @@ namespace {
 thread_local std::string g_last_error;
 thread_local ctg::DmrgOptions g_opts = [] {
 	ctg::DmrgOptions o;
-	if (const char* p = std::getenv("CTGPU_PRECISION")) o.precision = std::atoi(p) == ctg::GEMM_BF16X3 ? ctg::GEMM_BF16X3 : ctg::GEMM_FP64;
+	if (const char* p = std::getenv("CTGPU_PRECISION"))
+		o.precision = ctg::is_tc_precision(std::atoi(p)) ? std::atoi(p) : (int)ctg::GEMM_FP64;
 	if (const char* d = std::getenv("CTGPU_DEVICE")) o.device = std::atoi(d);
 	return o;
 }();
@@ -72,7 +74,7 @@ int ctgpu_set_reduced_environments(int on)
 
 int ctgpu_set_precision(int precision)
 {
-	if (precision != ctg::GEMM_FP64 && precision != ctg::GEMM_BF16X3) return ERR_RUNTIME;
+	if (precision != ctg::GEMM_FP64 && !ctg::is_tc_precision(precision)) return ERR_RUNTIME;
 	const int old = g_opts.precision;
 	g_opts.precision = precision;
 	return old;
@@ -118,6 +120,40 @@ int ctgpu_get_last_stats(struct ctgpu_stats* out)
 	out->svd_flops = s.svd_flops;
 	out->near_ties = s.near_ties;
 	return 0;
+}
+
+int ctgpu_tile_tuning_report(char* buf, int cap)
+{
+	return guarded([&] {
+		std::string text;
+		for (const ctg::TuneEntry& e : ctg::tile_tuning_entries())
+		{
+			char line[640];
+			snprintf(line, sizeof line, "%s %d %.4f %.4f %.4f %s\n", e.key.c_str(), e.bn, e.ms[0], e.ms[1], e.ms[2],
+			         e.from_file ? "file" : "timed");
+			text += line;
+		}
+		if (buf && cap > 0)
+		{
+			const size_t n = std::min(text.size(), (size_t)cap - 1);
+			memcpy(buf, text.data(), n);
+			buf[n] = 0;
+		}
+		return (int)text.size();
+	});
+}
+
+int ctgpu_set_tc_tile_width(int bn)
+{
+	return guarded([&] {
+		ctg::force_tc_tile_width(bn);
+		return 0;
+	});
+}
+
+void ctgpu_set_tc_wait_limit(long long polls)
+{
+	ctg::set_tc_wait_limit(polls);
 }
 
 ct_long ctgpu_get_bond_singular_values(int bond, double* out, ct_long max)

@@ -36,10 +36,17 @@ struct CudaError : std::runtime_error {
 enum AxRange { AX_LEADING = 0, AX_TRAILING = 1 };
 
 // Arithmetic used for the bulk block GEMMs.
+// The values of the first four are those of ctgpu_set_precision.
 enum GemmPrecision {
 	GEMM_FP64 = 0,        // plain IEEE double on the FP64 pipe
 	GEMM_BF16X3 = 1,      // split-BF16, 3 products, FP32 accumulation on tcgen05
-	GEMM_Z64 = 2,         // complex128 entries (plan kind; the arithmetic is complex FP64)
+	GEMM_TF32 = 2,        // TF32, one product, FP32 accumulation on tcgen05
+	GEMM_BF16X6 = 3,      // three-part split-BF16, 6 products, FP32 accumulation on tcgen05
+	GEMM_Z64 = 16,        // complex128 entries (plan kind; the arithmetic is complex FP64)
 };
+
+// tensor-core precisions and their operand format (TcFormat in ctg_kernels.h)
+inline bool is_tc_precision(int p) { return p == GEMM_BF16X3 || p == GEMM_TF32 || p == GEMM_BF16X6; }
+inline int tc_format_of(int p) { return p == GEMM_BF16X6 ? 1 : p == GEMM_TF32 ? 2 : 0; }
 
 }  // namespace ctg

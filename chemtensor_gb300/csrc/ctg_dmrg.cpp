@@ -170,8 +170,14 @@ TruncResult retained_bond_indices(const double* sigma, i64 n, double tol, bool r
 	for (auto& p : ss) { p.first = p.first * p.first; sqsum += p.first; }
 	if (sqsum == 0) return res;
 	// near-tie at the bond-dimension cut: the last discarded and the first kept value (ascending order)
+	// closer than the resolution of the singular values themselves (1e-12 of the largest), so that
+	// rounding alone could swap them
 	if (max_vdim < n && max_vdim > 0)
-		res.near_tie = ss[(size_t)(n - max_vdim)].first - ss[(size_t)(n - max_vdim - 1)].first <= 1e-12 * sqsum;
+	{
+		const double a = sigma[ss[(size_t)(n - max_vdim - 1)].second], b = sigma[ss[(size_t)(n - max_vdim)].second];
+		const double smax = sigma[ss[(size_t)(n - 1)].second];
+		res.near_tie = b - a <= 1e-12 * smax;
+	}
 	if (relative_thresh)
 		for (auto& p : ss) p.first /= sqsum;
 	for (size_t i = 1; i < ss.size(); i++) ss[i].first += ss[i - 1].first;
@@ -424,23 +430,26 @@ struct LocalH {
 			       o.ql[(size_t)i + 1] == a.ql[(size_t)i];
 		CTG_CHECK(same, "local Hamiltonian output structure differs from the input");
 		const size_t wz = z ? 2 : 1;
-		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * wz * sizeof(double));
-		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * wz * sizeof(double));
+		tc = is_tc_precision(precision);
+		// the intermediates of the tensor-core path only feed the next reduced-precision product: FP32
+		// (which keeps all the bits the operand formats use) halves their traffic
+		const size_t ez = tc ? sizeof(float) : sizeof(double);
+		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * wz * ez);
+		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * wz * ez);
 		flops = (z ? 4.0 : 1.0) * (d1.flops + d2.flops + d3.flops);
-		if (precision == GEMM_BF16X3)
+		if (tc)
 		{
 			// operands fixed for the bond (r, w, k) are packed once; x and the intermediates per apply
-			auto rec = [&](i64 n, i64 bytes) { return std::make_shared<DBuf>(&c, (size_t)std::max<i64>(n, 1) * bytes); };
-			pk_r = rec(d1.b_recs, TC_B_REC_BYTES);
-			pk_w = rec(d2.a_recs, TC_A_REC_BYTES);
-			pk_k = rec(d3.a_recs, TC_A_REC_BYTES);
-			pk_x = rec(d1.a_recs, TC_A_REC_BYTES);
-			pk_t1 = rec(d2.b_recs, TC_B_REC_BYTES);
-			pk_t2 = rec(d3.b_recs, TC_B_REC_BYTES);
+			auto rec = [&](i64 bytes) { return std::make_shared<DBuf>(&c, (size_t)std::max<i64>(bytes, 16)); };
+			pk_r = rec(d1.b_rec_bytes());
+			pk_w = rec(d2.a_rec_bytes());
+			pk_k = rec(d3.a_rec_bytes());
+			pk_x = rec(d1.a_rec_bytes());
+			pk_t1 = rec(d2.b_rec_bytes());
+			pk_t2 = rec(d3.b_rec_bytes());
 			d1.pack_b(c, r.data(), pk_r->ptr);
 			d2.pack_a(c, w.data(), pk_w->ptr);
 			d3.pack_a(c, k.data(), pk_k->ptr);
-			tc = true;
 		}
 	}
 
@@ -458,10 +467,10 @@ struct LocalH {
 		if (tc)
 		{
 			d1.pack_a(c, x, pk_x->ptr);
-			d1.run_packed(c, pk_x->ptr, pk_r->ptr, t1);
-			d2.pack_b(c, t1, pk_t1->ptr);
-			d2.run_packed(c, pk_w->ptr, pk_t1->ptr, t2);
-			d3.pack_b(c, t2, pk_t2->ptr);
+			d1.run_packed(c, pk_x->ptr, pk_r->ptr, tt1->ptr, true);
+			d2.pack_b(c, tt1->ptr, pk_t1->ptr, true);
+			d2.run_packed(c, pk_w->ptr, pk_t1->ptr, tt2->ptr, true);
+			d3.pack_b(c, tt2->ptr, pk_t2->ptr, true);
 			d3.run_packed(c, pk_k->ptr, pk_t2->ptr, y);
 			c.gemm_flops += flops;
 			return;

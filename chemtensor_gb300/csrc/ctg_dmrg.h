@@ -42,8 +42,8 @@ struct DmrgStats {
 	// retained singular values of the most recent split at every bond (after the last sweep: those of
 	// its right-to-left pass), in the order the truncation keeps them
 	std::vector<std::vector<double>> bond_sigma;
-	// splits whose bond-dimension cut fell between two singular values closer than 1e-12 of the sum of
-	// squares (the kept set then depends on the order of near-equal values)
+	// splits whose bond-dimension cut fell between two singular values less than 1e-12 of the largest
+	// apart (rounding alone could then change the kept set)
 	long near_ties = 0;
 };
 
@@ -59,7 +59,7 @@ int dmrg_singlesite_gpu(const struct mpo* hamiltonian, int num_sweeps, int maxit
 struct TruncResult {
 	std::vector<i64> ind;
 	double norm_sigma = 0, entropy = 0, tol_eff = 0;
-	// the cut at max_vdim separates two squared singular values less than 1e-12 of their sum apart
+	// the cut at max_vdim separates two singular values less than 1e-12 of the largest apart
 	bool near_tie = false;
 };
 TruncResult retained_bond_indices(const double* sigma, i64 n, double tol, bool relative_thresh, i64 max_vdim);

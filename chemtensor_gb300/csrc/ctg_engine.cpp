@@ -3,6 +3,7 @@
 #include "ctg_plan.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <chrono>
 #include <functional>
@@ -10,6 +11,8 @@
 #include <mutex>
 #include <cstring>
 #include <ctime>
+
+#include <dlfcn.h>
 
 namespace ctg {
 
@@ -418,12 +421,28 @@ const T* at(const DBufPtr& b, size_t off)
 // dot (block_sparse_tensor.c:1826-2001; dense_tensor.c:1761-1837)
 // ------------------------------------------------------------------------------------
 
+static DotPlan upload_dot_plan(Ctx& c, DotLowering&& l, int precision, int bn);
+static int tuned_tile_width(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
+                            const int* out_perm, DotLowering& l64);
+
 static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
                               const int* out_perm)
 {
 	// complex128: the FP64 work lists (outputs, contributions) with tiles of the complex GEMM
 	const bool z = precision == GEMM_Z64;
 	DotLowering l = lower_dot(s, axs, t, axt, nmult, z ? (int)GEMM_FP64 : precision, c.num_sms(), out_perm);
+	if (is_tc_precision(precision))
+	{
+		const int bn = tuned_tile_width(c, s, axs, t, axt, nmult, precision, out_perm, l);
+		if (bn != 64) l = lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm, bn);
+		return upload_dot_plan(c, std::move(l), precision, bn);
+	}
+	return upload_dot_plan(c, std::move(l), precision, 64);
+}
+
+static DotPlan upload_dot_plan(Ctx& c, DotLowering&& l, int precision, int bn)
+{
+	const bool z = precision == GEMM_Z64;
 	std::vector<ZTile> zt;
 	if (z)
 	{
@@ -437,6 +456,8 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	DotPlan p;
 	p.out = l.out;
 	p.precision = precision;
+	p.tc_fmt = tc_format_of(precision);
+	p.tc_bn = bn;
 	Packer pk;
 	const size_t o_outs = pk.add(l.outs);
 	const size_t o_cons = pk.add(l.cons);
@@ -474,12 +495,12 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 
 void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 {
-	if (precision == GEMM_BF16X3)
+	if (is_tc_precision(precision))
 	{
 		if (ntiles[0] > 0)
 		{
-			DBuf apk(&c, (size_t)std::max<i64>(a_recs, 1) * TC_A_REC_BYTES);
-			DBuf bpk(&c, (size_t)std::max<i64>(b_recs, 1) * TC_B_REC_BYTES);
+			DBuf apk(&c, (size_t)std::max<i64>(a_rec_bytes(), 16));
+			DBuf bpk(&c, (size_t)std::max<i64>(b_rec_bytes(), 16));
 			pack_a(c, A, apk.ptr);
 			pack_b(c, B, bpk.ptr);
 			run_packed(c, apk.ptr, bpk.ptr, C);
@@ -505,25 +526,211 @@ void DotPlan::run_z(Ctx& c, const double* A, const double* B, double* C, bool co
 	c.gemm_flops += 4.0 * flops;
 }
 
-void DotPlan::pack_a(Ctx& c, const double* A, void* apack) const
+void DotPlan::pack_a(Ctx& c, const void* A, void* apack, bool src_f32) const
 {
-	KScope ks(c, K_GEMM_TC, 1, 0, 8.0 * (double)a_entries + (double)a_recs * TC_A_REC_BYTES);
-	launch_tc_pack((int)a_recs, apacks, 1, A, apack, c.stream());
+	KScope ks(c, K_GEMM_TC, 1, 0, (src_f32 ? 4.0 : 8.0) * (double)a_entries + (double)a_rec_bytes());
+	launch_tc_pack(tc_fmt, (int)a_recs, apacks, 1, A, src_f32, apack, c.stream());
 }
 
-void DotPlan::pack_b(Ctx& c, const double* B, void* bpack) const
+void DotPlan::pack_b(Ctx& c, const void* B, void* bpack, bool src_f32) const
 {
-	KScope ks(c, K_GEMM_TC, 1, 0, 8.0 * (double)b_entries + (double)b_recs * TC_B_REC_BYTES);
-	launch_tc_pack((int)b_recs, bpacks, 0, B, bpack, c.stream());
+	KScope ks(c, K_GEMM_TC, 1, 0, (src_f32 ? 4.0 : 8.0) * (double)b_entries + (double)b_rec_bytes());
+	launch_tc_pack(tc_fmt, (int)b_recs, bpacks, 0, B, src_f32, bpack, c.stream());
 }
 
-void DotPlan::run_packed(Ctx& c, const void* apack, const void* bpack, double* C) const
+void DotPlan::run_packed(Ctx& c, const void* apack, const void* bpack, void* C, bool out_f32) const
 {
 	if (ntiles[0] > 0)
 	{
 		KScope ks(c, K_GEMM_TC, 1, flops_cls[0], 0);
-		launch_gemm_tc(ntiles[0], tiles[0], outs, tcons, apack, bpack, C, c.tc_error(), c.stream());
+		launch_gemm_tc(tc_fmt, tc_bn, ntiles[0], tiles[0], outs, tcons, apack, bpack, C, out_f32, c.tc_error(), c.stream());
 	}
+}
+
+// ------------------------------------------------------------------------------------
+// tile autotuner of the tensor-core GEMM
+// ------------------------------------------------------------------------------------
+
+namespace {
+
+struct TuneTable {
+	std::mutex mu;
+	bool loaded = false;
+	std::string path;
+	std::vector<TuneEntry> entries;
+	const TuneEntry* find(const std::string& k) const
+	{
+		for (const TuneEntry& e : entries)
+			if (e.key == k) return &e;
+		return nullptr;
+	}
+};
+
+TuneTable& tune_table()
+{
+	static TuneTable t;
+	return t;
+}
+
+std::string library_dir()
+{
+	Dl_info info;
+	if (dladdr((const void*)&tile_tuning_entries, &info) && info.dli_fname)
+	{
+		std::string f = info.dli_fname;
+		const size_t sl = f.rfind('/');
+		if (sl != std::string::npos) return f.substr(0, sl);
+	}
+	return ".";
+}
+
+void tune_load(TuneTable& t)
+{
+	if (t.loaded) return;
+	t.loaded = true;
+	const char* env = getenv("CTGPU_TUNE_FILE");
+	t.path = env ? env : library_dir() + "/tile_tuning.txt";
+	FILE* f = fopen(t.path.c_str(), "r");
+	if (!f) return;
+	char key[512];
+	int bn;
+	double a, b, d;
+	while (fscanf(f, "%511s %d %lf %lf %lf", key, &bn, &a, &b, &d) == 5)
+	{
+		if (bn != 64 && bn != 128 && bn != 256) continue;
+		if (t.find(key)) continue;
+		TuneEntry e;
+		e.key = key;
+		e.bn = bn;
+		e.ms[0] = a;
+		e.ms[1] = b;
+		e.ms[2] = d;
+		e.from_file = true;
+		t.entries.push_back(e);
+	}
+	fclose(f);
+}
+
+// flop-weighted histogram of a product's output blocks by column extent (<= 64, 128, 256, 512,
+// more) and summed contracted extent (<= 64, 256, more), shares rounded to eighths; with the
+// precision and the log4 of the total work
+std::string tune_key(const DotLowering& l, int precision)
+{
+	double hn[5] = {0, 0, 0, 0, 0}, hk[3] = {0, 0, 0}, total = 0;
+	for (const GemmOut& o : l.outs)
+	{
+		i64 ks = 0;
+		for (int cc = o.c0; cc < o.c0 + o.nc; cc++) ks += l.cons[(size_t)cc].k;
+		const double f = 2.0 * (double)o.m * (double)o.n * (double)ks;
+		const int bn = o.n <= 64 ? 0 : o.n <= 128 ? 1 : o.n <= 256 ? 2 : o.n <= 512 ? 3 : 4;
+		const int bk = ks <= 64 ? 0 : ks <= 256 ? 1 : 2;
+		hn[bn] += f;
+		hk[bk] += f;
+		total += f;
+	}
+	char buf[160];
+	auto q = [&](double x) { return total > 0 ? (int)std::lround(8.0 * x / total) : 0; };
+	snprintf(buf, sizeof buf, "p%d_w%d_n%d.%d.%d.%d.%d_k%d.%d.%d", precision,
+	         total > 0 ? (int)std::floor(std::log(total) / std::log(4.0)) : 0, q(hn[0]), q(hn[1]), q(hn[2]), q(hn[3]),
+	         q(hn[4]), q(hk[0]), q(hk[1]), q(hk[2]));
+	return buf;
+}
+
+// device time (ms) of packing the B operand and running the GEMM of a lowered product on zero operands
+double time_tc_variant(Ctx& c, DotLowering&& l, int precision, int bn, const Meta& s, const Meta& t)
+{
+	DotPlan p = upload_dot_plan(c, std::move(l), precision, bn);
+	if (p.ntiles[0] == 0) return 0.0;
+	DBuf A(&c, (size_t)std::max<i64>(s.nnz, 1) * sizeof(double));
+	DBuf B(&c, (size_t)std::max<i64>(t.nnz, 1) * sizeof(double));
+	DBuf C(&c, (size_t)std::max<i64>(p.out->nnz, 1) * sizeof(double));
+	DBuf apk(&c, (size_t)std::max<i64>(p.a_rec_bytes(), 16));
+	DBuf bpk(&c, (size_t)std::max<i64>(p.b_rec_bytes(), 16));
+	CTG_CUDA(cudaMemsetAsync(A.ptr, 0, A.bytes, c.stream()));
+	CTG_CUDA(cudaMemsetAsync(B.ptr, 0, B.bytes, c.stream()));
+	launch_tc_pack(p.tc_fmt, (int)p.a_recs, p.apacks, 1, A.ptr, false, apk.ptr, c.stream());
+	cudaEvent_t e[2];
+	for (auto& x : e) CTG_CUDA(cudaEventCreate(&x));
+	float best = 1e30f;
+	for (int rep = 0; rep < 3; rep++)
+	{
+		CTG_CUDA(cudaEventRecord(e[0], c.stream()));
+		launch_tc_pack(p.tc_fmt, (int)p.b_recs, p.bpacks, 0, B.ptr, false, bpk.ptr, c.stream());
+		launch_gemm_tc(p.tc_fmt, bn, p.ntiles[0], p.tiles[0], p.outs, p.tcons, apk.ptr, bpk.ptr, C.ptr, false, c.tc_error(),
+		               c.stream());
+		CTG_CUDA(cudaEventRecord(e[1], c.stream()));
+		CTG_CUDA(cudaEventSynchronize(e[1]));
+		float ms = 0;
+		CTG_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
+		if (rep > 0) best = std::min(best, ms);     // the first run pays for loading the kernel
+	}
+	for (auto& x : e) cudaEventDestroy(x);
+	c.sync();
+	return best;
+}
+
+}  // namespace
+
+std::atomic<int> g_forced_tc_bn{0};
+
+void force_tc_tile_width(int bn)
+{
+	CTG_CHECK(bn == 0 || bn == 64 || bn == 128 || bn == 256, "tensor-core tile width must be 0, 64, 128 or 256");
+	g_forced_tc_bn.store(bn);
+}
+
+std::vector<TuneEntry> tile_tuning_entries()
+{
+	TuneTable& t = tune_table();
+	std::lock_guard<std::mutex> g(t.mu);
+	tune_load(t);
+	return t.entries;
+}
+
+static int tuned_tile_width(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
+                            const int* out_perm, DotLowering& l64)
+{
+	static const int env_forced = [] {
+		const char* e = getenv("CTGPU_TC_BN");
+		const int v = e ? atoi(e) : 0;
+		return (v == 64 || v == 128 || v == 256) ? v : 0;
+	}();
+	const int forced = g_forced_tc_bn.load();
+	if (forced) return forced;
+	if (env_forced) return env_forced;
+	if (l64.tiles.empty()) return 64;
+	const std::string key = tune_key(l64, precision);
+	TuneTable& tt = tune_table();
+	{
+		std::lock_guard<std::mutex> g(tt.mu);
+		tune_load(tt);
+		if (const TuneEntry* e = tt.find(key)) return e->bn;
+	}
+	// first sight: time the three widths (the context's work so far completes first)
+	c.sync();
+	TuneEntry e;
+	e.key = key;
+	const int widths[3] = {64, 128, 256};
+	double best = 1e300;
+	for (int i = 0; i < 3; i++)
+	{
+		DotLowering l = i == 0 ? l64 : lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm, widths[i]);
+		e.ms[i] = time_tc_variant(c, std::move(l), precision, widths[i], s, t);
+		if (e.ms[i] < best)
+		{
+			best = e.ms[i];
+			e.bn = widths[i];
+		}
+	}
+	std::lock_guard<std::mutex> g(tt.mu);
+	if (const TuneEntry* prev = tt.find(key)) return prev->bn;    // another thread tuned it meanwhile
+	tt.entries.push_back(e);
+	if (FILE* f = fopen(tt.path.c_str(), "a"))
+	{
+		fprintf(f, "%s %d %.6f %.6f %.6f\n", key.c_str(), e.bn, e.ms[0], e.ms[1], e.ms[2]);
+		fclose(f);
+	}
+	return e.bn;
 }
 
 // ------------------------------------------------------------------------------------

@@ -175,6 +175,8 @@ struct DotPlan {
 	const TcPack* apacks = nullptr;
 	const TcPack* bpacks = nullptr;
 	i64 a_recs = 0, b_recs = 0;
+	int tc_fmt = TC_BF16X3;              // operand format (TcFormat)
+	int tc_bn = 64;                      // tile columns, from the tile autotuner
 	double flops = 0;
 	double flops_cls[NUM_TILE_CLASSES] = {};
 	int precision = GEMM_FP64;
@@ -184,15 +186,36 @@ struct DotPlan {
 	void run(Ctx& c, const double* A, const double* B, double* C) const;
 	// complex128 entries, operands optionally read conjugated
 	void run_z(Ctx& c, const double* A, const double* B, double* C, bool conj_a, bool conj_b) const;
-	// tensor-core path in parts, so that an operand used by many runs is packed once
-	void pack_a(Ctx& c, const double* A, void* apack) const;      // a_recs * TC_A_REC_BYTES bytes
-	void pack_b(Ctx& c, const double* B, void* bpack) const;      // b_recs * TC_B_REC_BYTES bytes
-	void run_packed(Ctx& c, const void* apack, const void* bpack, double* C) const;
+	// tensor-core path in parts, so that an operand used by many runs is packed once; src_f32: the
+	// operand holds FP32 entries (the output of another reduced-precision product)
+	i64 a_rec_bytes() const { return a_recs * tc_a_rec_bytes(tc_fmt); }
+	i64 b_rec_bytes() const { return b_recs * tc_b_rec_bytes(tc_fmt); }
+	void pack_a(Ctx& c, const void* A, void* apack, bool src_f32 = false) const;
+	void pack_b(Ctx& c, const void* B, void* bpack, bool src_f32 = false) const;
+	// out_f32: C receives FP32 entries
+	void run_packed(Ctx& c, const void* apack, const void* bpack, void* C, bool out_f32 = false) const;
 };
 // out_perm (every precision): the result is written straight in the layout of its transpose by out_perm
 // (see lower_dot), and the plan's `out` is that transposed structure
 DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision = GEMM_FP64,
                       const int* out_perm = nullptr);
+
+// Tile autotuner of the tensor-core GEMM: the column width (64, 128 or 256) of a product's tiles,
+// keyed by a histogram of its work list (flop shares of the output blocks by column extent and by
+// summed contracted extent, the precision and the total work). On first sight of a key the three
+// widths are timed on the product's own work lists (CUDA events, zero operands) and the fastest is
+// kept, in memory and appended to a text file (CTGPU_TUNE_FILE, default tile_tuning.txt beside the
+// library), which later processes read back. CTGPU_TC_BN=64|128|256 forces a width.
+struct TuneEntry {
+	std::string key;
+	int bn = 64;
+	double ms[3] = {0, 0, 0};            // timed pack + GEMM of widths 64, 128, 256 (0: not timed here)
+	bool from_file = false;
+};
+std::vector<TuneEntry> tile_tuning_entries();
+// use this width for every product planned from now on (0: the autotuner decides); plans already in a
+// context's cache keep theirs
+void force_tc_tile_width(int bn);
 
 struct CopyPlan {
 	std::shared_ptr<const Meta> out;

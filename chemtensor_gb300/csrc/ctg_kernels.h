@@ -77,35 +77,45 @@ void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, con
                      const GemmSplit* splits, int* counters, const double* A, const double* B, double* C, double* work,
                      cudaStream_t st);
 
-// Same work lists on the tcgen05 tensor cores, split-BF16 (hi*hi + hi*lo + lo*hi, FP32
-// accumulation, FP64 out); output tiles of tc_tile_rows() x tc_tile_cols().
+// Same work lists on the tcgen05 tensor cores with FP32 accumulation, output tiles of
+// tc_tile_rows() x BN (BN = 64, 128 or 256, chosen per product). Operand formats (TcFormat):
+//   TC_BF16X3  x = hi + lo (BF16 parts), products hi.hi + hi.lo + lo.hi: about 2^-16 relative
+//   TC_BF16X6  x = hi + mid + lo (BF16 parts of FP32 x), products hh hm mh hl mm lh: about 2^-23
+//   TC_TF32    x rounded to TF32, one product (kind::tf32): about 2^-11
 //
-// Operands are packed first: every operand block is cut into K-major tiles of 128 (A) or 64 (B)
-// rows by 64 k, and each tile is stored as one record holding the BF16 hi part and the BF16 lo part
-// (hi = bf16(x), lo = bf16(x - hi)) in the canonical no-swizzle core-matrix layout of the tcgen05
-// shared-memory descriptors; zero outside the block. A record moves into shared memory with one
-// bulk copy (cp.async.bulk). *error becomes 1 if a bounded wait inside the GEMM timed out.
+// Operands are packed first: every operand block is cut into K-major records of 128 (A) or 64 (B)
+// rows by one 64-byte k chunk (32 BF16 or 16 TF32 elements), each record holding its parts back to
+// back, each part in the canonical no-swizzle core-matrix layout of the tcgen05 shared-memory
+// descriptors; zero outside the block. B blocks get a multiple of BN / 64 row records. A record
+// moves into shared memory with bulk copies (cp.async.bulk). *error becomes 1 if a bounded wait
+// inside the GEMM ran out (set_tc_wait_limit sets the number of polls; 0 restores the default).
+enum TcFormat { TC_BF16X3 = 0, TC_BF16X6 = 1, TC_TF32 = 2 };
 int tc_tile_rows();
-int tc_tile_cols();
-constexpr int TC_A_ROWS = 128, TC_B_ROWS = 64, TC_K = 64;
-constexpr i64 TC_A_REC_BYTES = 2LL * TC_A_ROWS * TC_K * 2;   // 32 KiB
-constexpr i64 TC_B_REC_BYTES = 2LL * TC_B_ROWS * TC_K * 2;   // 16 KiB
+int tc_parts(int fmt);
+int tc_k_chunk(int fmt);            // elements of k per record
+constexpr int TC_A_ROWS = 128, TC_B_ROWS = 64, TC_KB = 64;
+i64 tc_a_rec_bytes(int fmt);
+i64 tc_b_rec_bytes(int fmt);
+void set_tc_wait_limit(long long polls);
 struct TcPack {
-	i64 src;           // element offset of (row 0, k 0) of the block in the FP64 operand
+	i64 src;           // element offset of (row 0, k 0) of the block in the operand
 	int rows, k;       // block extent
 	int s_row, s_k;    // element strides of rows and k
 	int row0, k0;      // tile origin
 	i64 rec;           // destination record
 };
 struct TcContrib {
-	i64 a_rec, b_rec;  // first record of the A block (tiles mt * kt + j) and of the B block (nt * kt + j)
-	int kt;            // k tiles
+	i64 a_rec, b_rec;  // first record of the A block (tiles mt * kt + j) and of the B block (nt64 * kt + j)
+	int kt;            // k chunks
 	int pad;
 };
-// a_side: records of TC_A_ROWS rows (A operand), else TC_B_ROWS (B operand)
-void launch_tc_pack(int nrec, const TcPack* packs, int a_side, const double* src, void* dst, cudaStream_t st);
-void launch_gemm_tc(int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons, const void* apack,
-                    const void* bpack, double* C, int* error, cudaStream_t st);
+// a_side: records of TC_A_ROWS rows (A operand), else TC_B_ROWS (B operand); src_f32: the operand
+// holds FP32 entries (an intermediate written by a reduced-precision product), else FP64
+void launch_tc_pack(int fmt, int nrec, const TcPack* packs, int a_side, const void* src, bool src_f32, void* dst,
+                    cudaStream_t st);
+// out_f32: C receives FP32 entries, else FP64
+void launch_gemm_tc(int fmt, int bn, int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons,
+                    const void* apack, const void* bpack, void* C, bool out_f32, int* error, cudaStream_t st);
 
 // ---- data movement -----------------------------------------------------------
 // Generic per-block permutation: dst block (row-major over dims) gathers

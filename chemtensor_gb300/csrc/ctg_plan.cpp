@@ -115,8 +115,10 @@ CopyLowering rows_lowering(std::shared_ptr<Meta> out, std::vector<RowDesc>&& d, 
 // ------------------------------------------------------------------------------------
 
 DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision, int num_sms,
-                      const int* out_perm)
+                      const int* out_perm, int tc_bn)
 {
+	CTG_CHECK(!is_tc_precision(precision) || tc_bn == 64 || tc_bn == 128 || tc_bn == 256,
+	          "dot: tensor-core tile width must be 64, 128 or 256");
 	DotLowering p;
 	double ts0 = host_seconds();
 	auto out = std::make_shared<Meta>(dot_result_meta(s, axs, t, axt, nmult));
@@ -272,7 +274,7 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 				CTG_CHECK(g.b_off + (k - 1) * g.sBk + (i64)(o.n - 1) * g.sBn < t.boff[bt] + ldt * tdt,
 				          "dot: B operand out of range");
 				R.cons.push_back(g);
-				if (precision == GEMM_BF16X3) R.con_blocks.emplace_back(bs, bt);
+				if (is_tc_precision(precision)) R.con_blocks.emplace_back(bs, bt);
 				R.flops += mn2 * (double)k;
 				ksum[(size_t)b] += k;
 				nch += (k + KCH - 1) / KCH;
@@ -324,12 +326,12 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			whole.k1 = o.nc > 0 ? cons[(size_t)whole.c1].k : 0;
 			whole.split = -1;
 			whole.sp = 0;
-			if (precision == GEMM_BF16X3)
+			if (is_tc_precision(precision))
 			{
-				// tensor-core tiles: one tile class
+				// tensor-core tiles: one tile class, tc_bn columns wide
 				R.flops_cls[0] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
 				for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
-					for (int n0 = 0; n0 < o.n; n0 += tc_tile_cols())
+					for (int n0 = 0; n0 < o.n; n0 += tc_bn)
 					{
 						whole.m0 = m0;
 						whole.n0 = n0;
@@ -439,7 +441,7 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 	ts0 = host_seconds();
 	std::vector<GemmSplit> splits;
 	i64 wsz = 0;
-	if (precision != GEMM_BF16X3)
+	if (!is_tc_precision(precision))
 	{
 		double total = 0;
 		for (int k = 0; k < NUM_TILE_CLASSES; k++)
@@ -497,8 +499,9 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 	// contribution that uses the block
 	std::vector<TcContrib> tcons;
 	std::vector<TcPack> apacks, bpacks;
-	if (precision == GEMM_BF16X3)
+	if (is_tc_precision(precision))
 	{
+		const int KC = tc_k_chunk(tc_format_of(precision));
 		// first record of each operand block's packed tiles (-1: not packed yet)
 		std::vector<i64> abase((size_t)s.nblocks, -1), bbase((size_t)t.nblocks, -1);
 		tcons.resize(cons.size());
@@ -506,7 +509,7 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 		{
 			const GemmContrib& g = cons[ci];
 			const int bs = con_blocks[ci].first, bt = con_blocks[ci].second;
-			const int kt = (g.k + TC_K - 1) / TC_K;
+			const int kt = (g.k + KC - 1) / KC;
 			// rows of the A view of block bs and of the B view of block bt
 			const i64* sd = s.dims(bs);
 			const i64* td = t.dims(bt);
@@ -518,16 +521,17 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 				const int mtiles = (am + TC_A_ROWS - 1) / TC_A_ROWS;
 				for (int mt = 0; mt < mtiles; mt++)
 					for (int j = 0; j < kt; j++)
-						apacks.push_back(TcPack{g.a_off, am, g.k, g.sAm, g.sAk, mt * TC_A_ROWS, j * TC_K, base + mt * kt + j});
+						apacks.push_back(TcPack{g.a_off, am, g.k, g.sAm, g.sAk, mt * TC_A_ROWS, j * KC, base + mt * kt + j});
 				abase[(size_t)bs] = base;
 			}
 			if (bbase[(size_t)bt] < 0)
 			{
 				const i64 base = (i64)bpacks.size();
-				const int ntiles_b = (bn + TC_B_ROWS - 1) / TC_B_ROWS;
+				// whole tile widths: a tile's columns are tc_bn / 64 consecutive row records
+				const int ntiles_b = (bn + tc_bn - 1) / tc_bn * (tc_bn / TC_B_ROWS);
 				for (int nt = 0; nt < ntiles_b; nt++)
 					for (int j = 0; j < kt; j++)
-						bpacks.push_back(TcPack{g.b_off, bn, g.k, g.sBn, g.sBk, nt * TC_B_ROWS, j * TC_K, base + nt * kt + j});
+						bpacks.push_back(TcPack{g.b_off, bn, g.k, g.sBn, g.sBk, nt * TC_B_ROWS, j * KC, base + nt * kt + j});
 				bbase[(size_t)bt] = base;
 			}
 			tcons[ci] = TcContrib{abase[(size_t)bs], bbase[(size_t)bt], kt, 0};
@@ -535,7 +539,7 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 	}
 	g_plan_stage[2] += host_seconds() - ts0;
 	ts0 = host_seconds();
-	if (precision == GEMM_BF16X3)
+	if (is_tc_precision(precision))
 	{
 		for (int k = 1; k < NUM_TILE_CLASSES; k++) p.flops_cls[0] += p.flops_cls[k], p.flops_cls[k] = 0;
 	}

@@ -30,9 +30,9 @@ struct DotLowering {
 };
 // out_perm (optional, r.ndim entries): write the result in the layout of its transpose by out_perm,
 // which must arrange two runs of row axes and two runs of column axes (each run kept in order) with
-// the last column run innermost
+// the last column run innermost. tc_bn: column width of the tensor-core tiles (64, 128 or 256).
 DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision, int num_sms,
-                      const int* out_perm = nullptr);
+                      const int* out_perm = nullptr, int tc_bn = 64);
 
 // data movement: kind 0 block permutation (PermDesc), 1 row map (RowDesc + maps), 2 axis scaling
 // (ScaleDesc + maps)

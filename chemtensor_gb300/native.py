@@ -49,6 +49,9 @@ EXPORTS = [
     "ctgpu_measure_fp64_tflops",
     "ctgpu_get_bond_singular_values",
     "ctgpu_dense_svd_noalloc",
+    "ctgpu_tile_tuning_report",
+    "ctgpu_set_tc_tile_width",
+    "ctgpu_set_tc_wait_limit",
 ]
 
 KERNEL_CLASSES = ["block_gemm", "permute", "row_map", "axis_scale", "block_svd", "block_rq", "lanczos_vector",
@@ -57,6 +60,9 @@ KERNEL_CLASSES = ["block_gemm", "permute", "row_map", "axis_scale", "block_svd",
 # arithmetic of the bulk block GEMMs (ctgpu_set_precision)
 PRECISION_FP64 = 0
 PRECISION_BF16X3 = 1
+PRECISION_TF32 = 2
+PRECISION_BF16X6 = 3
+PRECISION_NAMES = {"fp64": 0, "bf16x3": 1, "tf32": 2, "bf16x6": 3}
 
 
 class Stats(C.Structure):
@@ -112,6 +118,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_measure_fp64_tflops.restype = C.c_double
     lib.ctgpu_get_bond_singular_values.argtypes = [C.c_int, P, C.c_int64]
     lib.ctgpu_get_bond_singular_values.restype = C.c_int64
+    lib.ctgpu_tile_tuning_report.argtypes = [C.c_char_p, C.c_int]
+    lib.ctgpu_set_tc_tile_width.argtypes = [C.c_int]
+    lib.ctgpu_set_tc_wait_limit.argtypes = [C.c_longlong]
+    lib.ctgpu_set_tc_wait_limit.restype = None
     return lib
 
 
@@ -160,6 +170,19 @@ def bond_singular_values(bond: int) -> np.ndarray | None:
     out = np.zeros(max(n, 1))
     lib().ctgpu_get_bond_singular_values(bond, out.ctypes.data, n)
     return out[:n]
+
+
+def tile_tuning() -> list:
+    """The tile autotuner's choices so far: [{key, bn, ms: [64, 128, 256], source}]."""
+    n = lib().ctgpu_tile_tuning_report(None, 0)
+    buf = C.create_string_buffer(max(n, 0) + 1)
+    lib().ctgpu_tile_tuning_report(buf, len(buf))
+    out = []
+    for line in buf.value.decode().splitlines():
+        p = line.split()
+        if len(p) == 6:
+            out.append({"key": p[0], "bn": int(p[1]), "ms": [float(x) for x in p[2:5]], "source": p[5]})
+    return out
 
 
 def set_precision(p: int) -> int:

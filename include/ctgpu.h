@@ -45,14 +45,18 @@ int dmrg_twosite(const struct mpo* hamiltonian, const int num_sweeps, const int 
 int dmrg_singlesite(const struct mpo* hamiltonian, const int num_sweeps, const int maxiter_lanczos,
 	struct mps* psi, double* en_sweeps);
 
-/* Arithmetic of the bulk block GEMMs for subsequent calls from this thread.
- * 0 = FP64 (plain path); 1 = split-BF16 on the tcgen05 tensor cores (each FP64 operand split
- * into a high and a low BF16 part, three products hi*hi + hi*lo + lo*hi, FP32 accumulation,
- * about 2^-16 relative error per product). With 1, dmrg_twosite runs all sweeps but the last in
- * split-BF16 and the last sweep entirely in FP64, so returned energies and tensors are FP64
- * results; the single-operation entry points below use the setting as given.
- * The reference has no such setting (it always computes in FP64). Returns the previous value,
- * or -5 for an unknown value (the setting is then unchanged). */
+/* Arithmetic of the bulk block GEMMs for subsequent calls from this thread, all but 0 on the
+ * tcgen05 tensor cores with FP32 accumulation:
+ *   0 = FP64 (plain path);
+ *   1 = split-BF16: each operand value split into a high and a low BF16 part, three products
+ *       hi*hi + hi*lo + lo*hi, about 2^-16 relative error per product;
+ *   2 = TF32: operands rounded to TF32, one product, about 2^-11;
+ *   3 = three-part split-BF16: hi + mid + lo BF16 parts of the FP32 value, six products (every
+ *       term down to 2^-16 relative), about 2^-23, i.e. FP32-like accuracy.
+ * With 1-3, dmrg_twosite runs all sweeps but the last in that arithmetic and the last sweep
+ * entirely in FP64, so returned energies and tensors are FP64 results; the single-operation entry
+ * points below use the setting as given. The reference has no such setting (it always computes
+ * in FP64). Returns the previous value, or -5 for an unknown value (the setting is then unchanged). */
 int ctgpu_set_precision(int precision);
 
 /* With 1, the environment updates of the split-BF16 sweeps (ctgpu_set_precision(1)) also run in
@@ -91,9 +95,10 @@ struct ctgpu_stats
 	long   plan_misses;       /* lowered operations built afresh */
 	double svd_flops;         /* FP64 flops of the block SVDs: Jacobi inner products and rotations as
 	                             executed, QR and output factors estimated at full rank */
-	long   near_ties;         /* SVD splits whose max_vdim cut fell between two squared singular values
-	                             closer than 1e-12 of their sum: the kept set then depends on how equal
-	                             values are ordered (the reference sorts with the C library's qsort) */
+	long   near_ties;         /* SVD splits whose max_vdim cut fell between two singular values less
+	                             than 1e-12 of the largest apart: rounding alone could then change which
+	                             one is kept, and for exactly equal values the order of the sort decides
+	                             (the reference sorts with the C library's qsort) */
 };
 int ctgpu_get_last_stats(struct ctgpu_stats* out);
 
@@ -130,6 +135,24 @@ int ctgpu_get_kernel_profile(int cls, long* launches, double* ms, double* flops,
 /* FP64 FMA throughput of the current device in TFLOP/s, measured with register-resident FMA
  * chains (the roofline denominator of the FP64 path); -1 on failure. */
 double ctgpu_measure_fp64_tflops(void);
+
+/* Choices of the tensor-core tile autotuner so far in this process, one line per work-list
+ * histogram key: "key tile_columns ms64 ms128 ms256 source" (source "timed" or "file": read
+ * back from the tuning file). Writes at most cap - 1 characters and a terminating zero to buf
+ * and returns the length of the whole text. No counterpart in the reference. */
+int ctgpu_tile_tuning_report(char* buf, int cap);
+
+/* Column width of the tensor-core GEMM tiles for products planned from now on, process-wide:
+ * 64, 128 or 256, or 0 (default) to let the tile autotuner choose per product. Products already
+ * planned (and cached by a thread's context, see ctgpu_clear_plan_cache) keep their width.
+ * Returns 0, or -5 for another value. No counterpart in the reference. */
+int ctgpu_set_tc_tile_width(int bn);
+
+/* Number of polls after which a bounded mbarrier wait inside the tensor-core GEMM gives up
+ * (0 restores the default, 2^26). A wait that runs out makes the kernel record an error flag,
+ * let its copies in flight land, free its tensor memory and return; the call that launched it
+ * then returns -5. For tests of that error path; process-wide. No counterpart in the reference. */
+void ctgpu_set_tc_wait_limit(long long polls);
 
 /* ---- inputs ------------------------------------------------------------------------------ */
 
