@@ -129,8 +129,8 @@ int ctgpu_tile_tuning_report(char* buf, int cap)
 		for (const ctg::TuneEntry& e : ctg::tile_tuning_entries())
 		{
 			char line[640];
-			snprintf(line, sizeof line, "%s %d %.4f %.4f %.4f %s\n", e.key.c_str(), e.bn, e.ms[0], e.ms[1], e.ms[2],
-			         e.from_file ? "file" : "timed");
+			snprintf(line, sizeof line, "%s %d %.4f %.4f %.4f %.4f %s\n", e.key.c_str(), e.bn, e.ms[0], e.ms[1], e.ms[2],
+			         e.ms[3], e.from_file ? "file" : "timed");
 			text += line;
 		}
 		if (buf && cap > 0)
@@ -141,6 +141,34 @@ int ctgpu_tile_tuning_report(char* buf, int cap)
 		}
 		return (int)text.size();
 	});
+}
+
+int ctgpu_tridiag_lowest(const double* alpha, const double* beta, int k, double* lambda, double* y)
+{
+	return guarded([&] {
+		CTG_CHECK(alpha && lambda && y && k >= 1 && k <= ctg::LANCZOS_MAX && (k == 1 || beta), "invalid arguments");
+		ctg::Ctx& c = ctg::context_for_device(g_opts.device);
+		std::vector<double> in(2 * (size_t)k, 0.0);
+		for (int i = 0; i < k; i++) in[(size_t)i] = alpha[i];
+		for (int i = 0; i + 1 < k; i++) in[(size_t)k + i] = beta[i];
+		ctg::DBufPtr d_in = c.upload(in.data(), in.size() * sizeof(double));
+		ctg::DBuf d_out(&c, (2 + (size_t)k) * sizeof(double));
+		ctg::tridiag_lowest_test((const double*)d_in->ptr, (const double*)d_in->ptr + k, k, (double*)d_out.ptr, c.stream());
+		std::vector<double> out(2 + (size_t)k);
+		CTG_CUDA(cudaMemcpyAsync(out.data(), d_out.ptr, out.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream()));
+		c.sync();
+		*lambda = out[0];
+		for (int i = 0; i < k; i++) y[i] = out[2 + (size_t)i];
+		return (int)out[1];
+	});
+}
+
+int ctgpu_inject_failure(int which, int count)
+{
+	if (count < 0 || (which != 1 && which != 2)) return ERR_RUNTIME;
+	if (which == 1) ctg::g_inject_svd_failure = count;
+	else ctg::g_inject_tridiag_failure = count;
+	return 0;
 }
 
 int ctgpu_set_tc_tile_width(int bn)

@@ -396,7 +396,8 @@ struct LocalH {
 	DTensor w, r;
 	DBufPtr tt1, tt2;                // the two intermediates, in their transposed layouts
 	DBufPtr pk_r, pk_w, pk_k, pk_x, pk_t1, pk_t2;   // packed tensor-core operands
-	bool tc = false;
+	bool tc1 = false, tc2 = false, tc3 = false;     // product on the tensor cores (else FP64)
+	bool f1 = false, f2 = false;     // intermediate in FP32 (written and read by tensor-core products only)
 	bool z = false;                  // complex128 entries
 	double flops = 0;
 
@@ -430,25 +431,35 @@ struct LocalH {
 			       o.ql[(size_t)i + 1] == a.ql[(size_t)i];
 		CTG_CHECK(same, "local Hamiltonian output structure differs from the input");
 		const size_t wz = z ? 2 : 1;
-		tc = is_tc_precision(precision);
-		// the intermediates of the tensor-core path only feed the next reduced-precision product: FP32
-		// (which keeps all the bits the operand formats use) halves their traffic
-		const size_t ez = tc ? sizeof(float) : sizeof(double);
-		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * wz * ez);
-		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * wz * ez);
+		// each product runs where its plan says: the autotuner keeps small products on FP64
+		tc1 = is_tc_precision(d1.precision);
+		tc2 = is_tc_precision(d2.precision);
+		tc3 = is_tc_precision(d3.precision);
+		// an intermediate that only feeds a tensor-core product from a tensor-core product is FP32
+		// (which keeps all the bits the operand formats use): half the traffic
+		f1 = tc1 && tc2;
+		f2 = tc2 && tc3;
+		tt1 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d1.out->nnz, 1) * wz * (f1 ? sizeof(float) : sizeof(double)));
+		tt2 = std::make_shared<DBuf>(&c, (size_t)std::max<i64>(d2.out->nnz, 1) * wz * (f2 ? sizeof(float) : sizeof(double)));
 		flops = (z ? 4.0 : 1.0) * (d1.flops + d2.flops + d3.flops);
-		if (tc)
+		// operands fixed for the bond (r, w, k) are packed once; x and the intermediates per apply
+		auto rec = [&](i64 bytes) { return std::make_shared<DBuf>(&c, (size_t)std::max<i64>(bytes, 16)); };
+		if (tc1)
 		{
-			// operands fixed for the bond (r, w, k) are packed once; x and the intermediates per apply
-			auto rec = [&](i64 bytes) { return std::make_shared<DBuf>(&c, (size_t)std::max<i64>(bytes, 16)); };
 			pk_r = rec(d1.b_rec_bytes());
-			pk_w = rec(d2.a_rec_bytes());
-			pk_k = rec(d3.a_rec_bytes());
 			pk_x = rec(d1.a_rec_bytes());
-			pk_t1 = rec(d2.b_rec_bytes());
-			pk_t2 = rec(d3.b_rec_bytes());
 			d1.pack_b(c, r.data(), pk_r->ptr);
+		}
+		if (tc2)
+		{
+			pk_w = rec(d2.a_rec_bytes());
+			pk_t1 = rec(d2.b_rec_bytes());
 			d2.pack_a(c, w.data(), pk_w->ptr);
+		}
+		if (tc3)
+		{
+			pk_k = rec(d3.a_rec_bytes());
+			pk_t2 = rec(d3.b_rec_bytes());
 			d3.pack_a(c, k.data(), pk_k->ptr);
 		}
 	}
@@ -464,20 +475,27 @@ struct LocalH {
 			d3.run_z(c, k.data(), t2, y, false, false);
 			return;
 		}
-		if (tc)
+		if (tc1)
 		{
 			d1.pack_a(c, x, pk_x->ptr);
-			d1.run_packed(c, pk_x->ptr, pk_r->ptr, tt1->ptr, true);
-			d2.pack_b(c, tt1->ptr, pk_t1->ptr, true);
-			d2.run_packed(c, pk_w->ptr, pk_t1->ptr, tt2->ptr, true);
-			d3.pack_b(c, tt2->ptr, pk_t2->ptr, true);
-			d3.run_packed(c, pk_k->ptr, pk_t2->ptr, y);
-			c.gemm_flops += flops;
-			return;
+			d1.run_packed(c, pk_x->ptr, pk_r->ptr, t1, f1);
+			c.gemm_flops += d1.flops;
 		}
-		d1.run(c, x, r.data(), t1);
-		d2.run(c, w.data(), t1, t2);
-		d3.run(c, k.data(), t2, y);
+		else d1.run(c, x, r.data(), t1);
+		if (tc2)
+		{
+			d2.pack_b(c, t1, pk_t1->ptr, f1);
+			d2.run_packed(c, pk_w->ptr, pk_t1->ptr, t2, f2);
+			c.gemm_flops += d2.flops;
+		}
+		else d2.run(c, w.data(), t1, t2);
+		if (tc3)
+		{
+			d3.pack_b(c, t2, pk_t2->ptr, f2);
+			d3.run_packed(c, pk_k->ptr, pk_t2->ptr, y);
+			c.gemm_flops += d3.flops;
+		}
+		else d3.run(c, k.data(), t2, y);
 	}
 };
 
@@ -509,25 +527,26 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 		KScope ks(c, K_LANCZOS, 1, 3.0 * dn, 24.0 * dn);
 		launch_lz_start(a_start.data(), Vp, n, pp, d_sc, s);
 	}
+	a_opt = c.empty(a_start.meta, a_start.cplx);
 	for (int j = 0; j < maxiter; j++)
 	{
 		hz = now_s();
 		h.apply(c, Vp + (i64)j * n, wp);
 		g_host_detail[1] += now_s() - hz;
 		hz = now_s();
+		if (j < maxiter - 1)
 		{
-			const bool last = j == maxiter - 1;
-			KScope ks(c, K_LANCZOS, 1, last ? 2.0 * dn : 9.0 * dn, last ? 16.0 * dn : 72.0 * dn);
-			launch_lz_step(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, last ? wp : Vp + (i64)(j + 1) * n, n, nent,
-			               j, last ? 1 : 0, pp, d_sc, s);
+			KScope ks(c, K_LANCZOS, 1, 9.0 * dn, 72.0 * dn);
+			launch_lz_step(wp, Vp + (i64)j * n, j > 0 ? Vp + (i64)(j - 1) * n : Vp, Vp + (i64)(j + 1) * n, n, nent, j, 0, pp,
+			               d_sc, s);
+		}
+		else
+		{
+			// alpha of the last step, the tridiagonal eigensolve and the Ritz vector in one launch
+			KScope ks(c, K_LANCZOS, 1, 2.0 * (maxiter + 1) * dn, 8.0 * (maxiter + 3) * dn);
+			launch_lz_finish(wp, Vp, n, maxiter, pp, d_sc, a_opt.data(), s);
 		}
 		g_host_detail[2] += now_s() - hz;
-	}
-	a_opt = c.empty(a_start.meta, a_start.cplx);
-	{
-		KScope ks(c, K_LANCZOS, 2, 2.0 * maxiter * dn, 8.0 * (maxiter + 1) * dn);
-		launch_lz_tridiag(maxiter, d_sc, s);
-		launch_lz_ritz(Vp, n, maxiter, d_sc, a_opt.data(), s);
 	}
 	if (st)
 	{
@@ -680,8 +699,15 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		// synchronises once (for the singular values); the Lanczos scalars have arrived by then
 		r = split_mps_svd(c, aopt, psi->d, qsite, tol_split, max_vdim, !left_to_right, A[i], A[i + 1], &ent,
 		                  &st->bond_sigma[(size_t)i], &st->near_ties);
-		if (r < 0) return r;
+		if (g_inject_tridiag_failure > 0)
+		{
+			// host-side fault injection (tests of the error path): this eigensolve reports failure
+			g_inject_tridiag_failure--;
+			h_sc->status = -2;
+		}
+		// the Lanczos status first: the reference returns before it splits (dmrg.c:312-323)
 		if (h_sc->status != 0) return h_sc->status;
+		if (r < 0) return r;
 		CTG_CUDA(cudaEventRecord(ev[2], c.stream()));
 		const double h2 = now_s();
 		// environments stay FP64 unless reduced_env is set: each one is built from its neighbour, so

@@ -433,7 +433,10 @@ static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int
 	DotLowering l = lower_dot(s, axs, t, axt, nmult, z ? (int)GEMM_FP64 : precision, c.num_sms(), out_perm);
 	if (is_tc_precision(precision))
 	{
+		// the autotuner picks the tile width, or FP64 where the product is too small for the tensor
+		// cores to pay for their operand packing (FP64 is then both faster and exact)
 		const int bn = tuned_tile_width(c, s, axs, t, axt, nmult, precision, out_perm, l);
+		if (bn == 0) return upload_dot_plan(c, lower_dot(s, axs, t, axt, nmult, GEMM_FP64, c.num_sms(), out_perm), GEMM_FP64, 64);
 		if (bn != 64) l = lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm, bn);
 		return upload_dot_plan(c, std::move(l), precision, bn);
 	}
@@ -592,12 +595,13 @@ void tune_load(TuneTable& t)
 	t.path = env ? env : library_dir() + "/tile_tuning.txt";
 	FILE* f = fopen(t.path.c_str(), "r");
 	if (!f) return;
-	char key[512];
+	char line[1024], key[512];
 	int bn;
-	double a, b, d;
-	while (fscanf(f, "%511s %d %lf %lf %lf", key, &bn, &a, &b, &d) == 5)
+	double a, b, d, q;
+	while (fgets(line, sizeof line, f))
 	{
-		if (bn != 64 && bn != 128 && bn != 256) continue;
+		if (sscanf(line, "%511s %d %lf %lf %lf %lf", key, &bn, &a, &b, &d, &q) != 6) continue;
+		if (bn != 0 && bn != 64 && bn != 128 && bn != 256) continue;
 		if (t.find(key)) continue;
 		TuneEntry e;
 		e.key = key;
@@ -605,6 +609,7 @@ void tune_load(TuneTable& t)
 		e.ms[0] = a;
 		e.ms[1] = b;
 		e.ms[2] = d;
+		e.ms[3] = q;
 		e.from_file = true;
 		t.entries.push_back(e);
 	}
@@ -636,11 +641,38 @@ std::string tune_key(const DotLowering& l, int precision)
 	return buf;
 }
 
-// device time (ms) of packing the B operand and running the GEMM of a lowered product on zero operands
+// device time (ms) of one product on zero operands: for the tensor cores, packing the B operand (per
+// application one operand is packed afresh) and the GEMM; for FP64 (bn == 0), the FP64 GEMM
 double time_tc_variant(Ctx& c, DotLowering&& l, int precision, int bn, const Meta& s, const Meta& t)
 {
-	DotPlan p = upload_dot_plan(c, std::move(l), precision, bn);
+	DotPlan p = upload_dot_plan(c, std::move(l), bn == 0 ? (int)GEMM_FP64 : precision, bn == 0 ? 64 : bn);
 	if (p.ntiles[0] == 0) return 0.0;
+	if (bn == 0)
+	{
+		DBuf A(&c, (size_t)std::max<i64>(s.nnz, 1) * sizeof(double));
+		DBuf B(&c, (size_t)std::max<i64>(t.nnz, 1) * sizeof(double));
+		DBuf C(&c, (size_t)std::max<i64>(p.out->nnz, 1) * sizeof(double));
+		CTG_CUDA(cudaMemsetAsync(A.ptr, 0, A.bytes, c.stream()));
+		CTG_CUDA(cudaMemsetAsync(B.ptr, 0, B.bytes, c.stream()));
+		cudaEvent_t e[2];
+		for (auto& x : e) CTG_CUDA(cudaEventCreate(&x));
+		float best = 1e30f;
+		for (int rep = 0; rep < 3; rep++)
+		{
+			CTG_CUDA(cudaEventRecord(e[0], c.stream()));
+			launch_gemm_f64(p.ntiles[0], p.tiles[0], p.outs, p.cons, p.splits, p.counters ? (int*)p.counters->ptr : nullptr,
+			                (const double*)A.ptr, (const double*)B.ptr, (double*)C.ptr,
+			                p.work ? (double*)p.work->ptr : nullptr, c.stream());
+			CTG_CUDA(cudaEventRecord(e[1], c.stream()));
+			CTG_CUDA(cudaEventSynchronize(e[1]));
+			float ms = 0;
+			CTG_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
+			if (rep > 0) best = std::min(best, ms);
+		}
+		for (auto& x : e) cudaEventDestroy(x);
+		c.sync();
+		return best;
+	}
 	DBuf A(&c, (size_t)std::max<i64>(s.nnz, 1) * sizeof(double));
 	DBuf B(&c, (size_t)std::max<i64>(t.nnz, 1) * sizeof(double));
 	DBuf C(&c, (size_t)std::max<i64>(p.out->nnz, 1) * sizeof(double));
@@ -706,7 +738,7 @@ static int tuned_tile_width(Ctx& c, const Meta& s, int axs, const Meta& t, int a
 		tune_load(tt);
 		if (const TuneEntry* e = tt.find(key)) return e->bn;
 	}
-	// first sight: time the three widths (the context's work so far completes first)
+	// first sight: time the three widths and the FP64 GEMM (the context's work so far completes first)
 	c.sync();
 	TuneEntry e;
 	e.key = key;
@@ -722,12 +754,14 @@ static int tuned_tile_width(Ctx& c, const Meta& s, int axs, const Meta& t, int a
 			e.bn = widths[i];
 		}
 	}
+	e.ms[3] = time_tc_variant(c, lower_dot(s, axs, t, axt, nmult, GEMM_FP64, c.num_sms(), out_perm), precision, 0, s, t);
+	if (e.ms[3] < best) e.bn = 0;
 	std::lock_guard<std::mutex> g(tt.mu);
 	if (const TuneEntry* prev = tt.find(key)) return prev->bn;    // another thread tuned it meanwhile
 	tt.entries.push_back(e);
 	if (FILE* f = fopen(tt.path.c_str(), "a"))
 	{
-		fprintf(f, "%s %d %.6f %.6f %.6f\n", key.c_str(), e.bn, e.ms[0], e.ms[1], e.ms[2]);
+		fprintf(f, "%s %d %.6f %.6f %.6f %.6f\n", key.c_str(), e.bn, e.ms[0], e.ms[1], e.ms[2], e.ms[3]);
 		fclose(f);
 	}
 	return e.bn;
@@ -1229,8 +1263,18 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 	return 0;
 }
 
+thread_local int g_inject_svd_failure = 0;
+thread_local int g_inject_tridiag_failure = 0;
+
 int op_svd_finish(Ctx& c, const SvdPending& pend)
 {
+	if (g_inject_svd_failure > 0)
+	{
+		// host-side fault injection (tests of the error path): this SVD reports non-convergence
+		g_inject_svd_failure--;
+		fprintf(stderr, "ctgpu: block SVD did not converge (injected failure)\n");
+		return -1;
+	}
 	if (pend.zblocks > 0)
 	{
 		std::vector<int> st((size_t)pend.zblocks);

@@ -200,16 +200,18 @@ struct DotPlan {
 DotPlan make_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision = GEMM_FP64,
                       const int* out_perm = nullptr);
 
-// Tile autotuner of the tensor-core GEMM: the column width (64, 128 or 256) of a product's tiles,
-// keyed by a histogram of its work list (flop shares of the output blocks by column extent and by
-// summed contracted extent, the precision and the total work). On first sight of a key the three
-// widths are timed on the product's own work lists (CUDA events, zero operands) and the fastest is
-// kept, in memory and appended to a text file (CTGPU_TUNE_FILE, default tile_tuning.txt beside the
-// library), which later processes read back. CTGPU_TC_BN=64|128|256 forces a width.
+// Tile autotuner of the reduced-precision GEMMs: the column width (64, 128 or 256) of a product's
+// tensor-core tiles, or FP64 (0) where the product is too small for the tensor cores to pay for the
+// operand packing, keyed by a histogram of its work list (flop shares of the output blocks by column
+// extent and by summed contracted extent, the precision and the total work). On first sight of a key
+// the three widths and the FP64 GEMM are timed on the product's own work lists (CUDA events, zero
+// operands) and the fastest is kept, in memory and appended to a text file (CTGPU_TUNE_FILE, default
+// tile_tuning.txt beside the library), which later processes read back. CTGPU_TC_BN=64|128|256
+// forces a width.
 struct TuneEntry {
 	std::string key;
-	int bn = 64;
-	double ms[3] = {0, 0, 0};            // timed pack + GEMM of widths 64, 128, 256 (0: not timed here)
+	int bn = 64;                         // 64, 128, 256, or 0 for FP64
+	double ms[4] = {0, 0, 0, 0};         // timed widths 64, 128, 256 (B packing + GEMM) and FP64
 	bool from_file = false;
 };
 std::vector<TuneEntry> tile_tuning_entries();
@@ -270,6 +272,10 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend);
 int op_svd_finish(Ctx& c, const SvdPending& pend);
 // launch, synchronise, finish. Returns 0 or -1.
 int op_svd(Ctx& c, const DTensor& a, SvdResult& res);
+// host-side fault injection for tests of the error paths (per thread): the next n block SVDs report
+// non-convergence, the next n Lanczos tridiagonal eigensolves report failure
+extern thread_local int g_inject_svd_failure;
+extern thread_local int g_inject_tridiag_failure;
 
 // block RQ (block_sparse_tensor_rq, block_sparse_tensor.c:2544-2676). Returns 0 or -1.
 int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q);

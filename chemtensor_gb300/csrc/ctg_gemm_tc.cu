@@ -380,8 +380,9 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 				atomicExch(error, 1);
 			}
 			// the copies of the last chunk of every stage must land before shared memory is released
+			// (always with the default limit: a lowered limit only shortens the pipeline's waits)
 			for (long long u = g - NST; u < g; u++)
-				if (u >= 0) mbar_wait(smem_u32(full + (int)(u % NST)), (uint32_t)((u / NST) & 1), wait_limit);
+				if (u >= 0) mbar_wait(smem_u32(full + (int)(u % NST)), (uint32_t)((u / NST) & 1), TC_WAIT_LIMIT_DEFAULT);
 		}
 	}
 	else if (warp == 1)
@@ -446,7 +447,8 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 			}
 			// no MMA may still run when tensor memory is freed: the commit after the last chunk
 			// consumed tracks every MMA issued before it
-			if (g > 0) mbar_wait(smem_u32(empty + (int)((g - 1) % NST)), (uint32_t)(((g - 1) / NST) & 1), wait_limit);
+			if (g > 0)
+				mbar_wait(smem_u32(empty + (int)((g - 1) % NST)), (uint32_t)(((g - 1) / NST) & 1), TC_WAIT_LIMIT_DEFAULT);
 		}
 	}
 	else

@@ -251,14 +251,19 @@ constexpr int RED_BLOCKS = 608;     // 4 x 152 SMs: fixed grid for deterministic
 
 // one cooperative launch each (partial: 2 RED_BLOCKS doubles): a whole Lanczos step
 // (alpha; unless last: orthogonalisation, beta and the early exit, next vector), and the start
-// vector's normalisation
+// vector's normalisation (a start vector of norm zero sets status -1 and stops the iteration)
 // n doubles per vector (a complex128 vector counts twice); the breakdown test beta < 100 nthr eps
 // uses nthr, the number of entries (krylov.c:62, :129)
 void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, i64 nthr, int j, int last,
                     double* partial, LanczosScalars* sc, cudaStream_t st);
 void launch_lz_start(const double* v0, double* v, i64 n, double* partial, LanczosScalars* sc, cudaStream_t st);
-void launch_lz_tridiag(int maxiter, LanczosScalars* sc, cudaStream_t st);
-void launch_lz_ritz(const double* V, i64 n, int maxiter, const LanczosScalars* sc, double* out, cudaStream_t st);
+// the last step (alpha_{maxiter-1}, unless the iteration stopped early), the lowest eigenpair of the
+// tridiagonal Lanczos matrix and the Ritz vector out = V y, in one cooperative launch
+void launch_lz_finish(const double* w, const double* V, i64 n, int maxiter, double* partial, LanczosScalars* sc,
+                      double* out, cudaStream_t st);
+// the tridiagonal eigensolver of launch_lz_finish alone (one warp, k <= LANCZOS_MAX): d_out receives
+// lambda, the status and y[0..k-1]
+void tridiag_lowest_test(const double* d_alpha, const double* d_beta, int k, double* d_out, cudaStream_t st);
 
 // Sustained FP64 FMA rate of the device in TFLOP/s (register-resident FMA chains).
 double measure_fp64_fma_tflops(int device);

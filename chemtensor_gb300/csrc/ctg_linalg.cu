@@ -260,21 +260,29 @@ k_lz_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, double*
 	block_partial(x, partial);
 	grid.sync();
 	const double nrm = sqrt(final_sum(partial));
+	// a start vector of norm zero (or not finite) admits no Lanczos iteration: fewer iterations than
+	// the one eigenvalue asked for, status -1 (krylov.c:218-223); the later kernels see `stopped`
+	const bool bad = !(nrm > 0.0) || !isfinite(nrm);
 	if (blockIdx.x == 0 && threadIdx.x == 0)
 	{
 		sc->nrm0 = nrm;
-		sc->stopped = 0;
+		sc->stopped = bad ? 1 : 0;
 		sc->numiter = 0;
-		sc->status = 0;
+		sc->status = bad ? -1 : 0;
 	}
+	if (bad) return;
 	const double inv = 1.0 / nrm;
 	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride) v[i] = inv * v0[i];
 }
 
+__global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
+k_lz_finish(const double* __restrict__ w, const double* __restrict__ V, i64 n, int maxiter, double* __restrict__ partial,
+            LanczosScalars* sc, double* __restrict__ out);
+
 static void check_coop(const void* fn)
 {
-	static std::atomic<int> ok[2] = {{0}, {0}};
-	const int which = fn == (const void*)k_lz_step ? 0 : 1;
+	static std::atomic<int> ok[3] = {{0}, {0}, {0}};
+	const int which = fn == (const void*)k_lz_step ? 0 : fn == (const void*)k_lz_start ? 1 : 2;
 	if (ok[which].load()) return;
 	int dev = 0, sms = 0, per_sm = 0, coop = 0;
 	CTG_CUDA(cudaGetDevice(&dev));
@@ -300,156 +308,268 @@ void launch_lz_start(const double* v0, double* v, i64 n, double* partial, Lanczo
 	CTG_CUDA(cudaLaunchCooperativeKernel((const void*)k_lz_start, dim3(RED_BLOCKS), dim3(RED_THREADS), args, 0, st));
 }
 
-// Lowest eigenpair of the k x k symmetric tridiagonal Lanczos matrix by cyclic Jacobi rotations
-// (replaces LAPACK dsteqr, krylov.c:230). One warp; k <= LANCZOS_MAX = 32: the matrix and the
-// rotation product live in shared memory, lane r updates row / column r of every rotation.
-__global__ void __launch_bounds__(32) k_tridiag(int maxiter, LanczosScalars* sc)
+// Lowest eigenpair of the k x k symmetric tridiagonal Lanczos matrix T (replaces LAPACK dsteqr,
+// krylov.c:230, for the lowest eigenpair only). One warp, k <= LANCZOS_MAX = 32. The Lanczos matrix
+// is unreduced (every beta above the breakdown threshold), so its eigenvalues are simple and, by
+// interlacing, the lowest one lies strictly below those of every leading submatrix T_j: at
+// x <= lambda_0 the pivots d_1 .. d_{k-1} of the LDL^T factorisation of T - x I are positive and the
+// number of negative pivots (Sturm count) is the number of eigenvalues below x.
+//   1. FP32 multisection: the 32 lanes take Sturm counts at 32 points of the Gershgorin interval and
+//      keep the sub-interval where the count first reaches one (33x narrower per round), to FP32
+//      resolution;
+//   2. FP64 Newton on the last pivot d_k(x) (zero at lambda_0; its derivative follows the same
+//      recurrence), safeguarded by bisection inside the bracket that the Sturm counts maintain;
+//   3. eigenvector from L^T y = e_k (y_k = 1, y_i = -(b_i / d_i) y_{i+1}), normalised, its
+//      largest-magnitude component made positive (deterministic sign).
+// Reciprocals are rcp64 (FP32 seed, cubic correction): an FP64 division costs over a thousand
+// cycles of GB300's FP64 pipe. Status -2 if the result is not finite.
+__device__ __forceinline__ int sturm_count32(const float* a, const float* b2, int k, float x)
 {
-	__shared__ double A[LANCZOS_MAX][LANCZOS_MAX + 1], Z[LANCZOS_MAX][LANCZOS_MAX + 1];
-	__shared__ double rc[LANCZOS_MAX / 2 + 1], rs[LANCZOS_MAX / 2 + 1];
-	__shared__ int rp[LANCZOS_MAX / 2 + 1], rq[LANCZOS_MAX / 2 + 1];
-	const int lane = threadIdx.x;
-	if (lane == 0 && !sc->stopped) sc->numiter = maxiter;
-	__syncwarp();
-	const int k = sc->numiter;
-	if (k < 1 || k > LANCZOS_MAX)
+	int neg = 0;
+	float d = a[0] - x;
+	for (int i = 0;; i++)
 	{
-		if (lane == 0) sc->status = k < 1 ? -1 : -2;
+		if (fabsf(d) < 1e-30f) d = -1e-30f;
+		neg += d < 0.0f ? 1 : 0;
+		if (i + 1 >= k) break;
+		d = (a[i + 1] - x) - __fdividef(b2[i], d);
+	}
+	return neg;
+}
+
+// last pivot d_k(x), its derivative, and the Sturm count, in FP64
+__device__ __forceinline__ void pivots64(const double* a, const double* b2, int k, double x, double& dk, double& ddk, int& neg)
+{
+	double d = a[0] - x, dd = -1.0;
+	neg = d < 0.0 ? 1 : 0;
+	for (int i = 0; i + 1 < k; i++)
+	{
+		if (fabs(d) < 1e-300) d = -1e-300;
+		const double inv = rcp64(d);
+		const double t = b2[i] * inv;
+		dd = fma(t * inv, dd, -1.0);            // d'_{i+1} = -1 + b_i^2 d'_i / d_i^2
+		d = (a[i + 1] - x) - t;
+		neg += d < 0.0 ? 1 : 0;
+	}
+	dk = d;
+	ddk = dd;
+}
+
+// Lowest eigenpair of the k x k tridiagonal (diagonal al[0..k-1], off-diagonal be[0..k-2]); called
+// by all 32 lanes of one warp; lane 0 writes *lambda, y[0..k-1] and *status (0, or -2 if the result
+// is not finite). `sh` is shared scratch of 6 LANCZOS_MAX doubles.
+__device__ void tridiag_lowest(const double* al, const double* be, int k, double* sh, double* lambda, double* y, int* status)
+{
+	const int lane = threadIdx.x & 31;
+	double* A = sh;
+	double* B2 = sh + LANCZOS_MAX;
+	double* Bv = sh + 2 * LANCZOS_MAX;
+	double* Y = sh + 3 * LANCZOS_MAX;
+	float* Af = (float*)(sh + 4 * LANCZOS_MAX);
+	float* B2f = Af + LANCZOS_MAX;
+	if (lane < k)
+	{
+		A[lane] = al[lane];
+		Af[lane] = (float)A[lane];
+		const double b = lane + 1 < k ? be[lane] : 0.0;
+		Bv[lane] = b;
+		B2[lane] = b * b;
+		B2f[lane] = (float)(b * b);
+	}
+	__syncwarp();
+	if (k == 1)
+	{
+		if (lane == 0)
+		{
+			*lambda = A[0];
+			y[0] = 1.0;
+			*status = isfinite(A[0]) ? 0 : -2;
+		}
+		__syncwarp();
 		return;
 	}
-	if (lane < k)
-		for (int j = 0; j < k; j++)
-		{
-			double v = 0;
-			if (lane == j) v = sc->alpha[lane];
-			else if (j == lane + 1) v = sc->beta[lane];
-			else if (lane == j + 1) v = sc->beta[j];
-			A[lane][j] = v;
-			Z[lane][j] = (lane == j) ? 1.0 : 0.0;
-		}
-	__syncwarp();
-	// Parallel cyclic Jacobi: each step rotates a set of disjoint pairs (round-robin over k rounded
-	// up to even), one lane per pair forming its rotation; A <- J^T A J as all column rotations
-	// (lane r updates row r) then all row rotations (lane c updates column c). The angle comes from
-	// FP32, the rotation itself is orthogonal to FP64 rounding: t from FP32, c = 1 / sqrt(1 + t^2) and
-	// s = t c in FP64. The rotated a_pq (about 1e-7 of its old value) is kept, not set to zero: the
-	// transformation stays an orthogonal similarity, and the next sweep removes the residual.
-	const int np = k + (k & 1), half = np / 2;
-	for (int sweep = 0; sweep < 100; sweep++)
+	// Gershgorin interval of all eigenvalues (FP32, widened by a relative margin)
+	float glo = 3.0e38f, ghi = -3.0e38f;
+	for (int i = 0; i < k; i++)
 	{
-		double off = 0, diag = 0;
-		if (lane < k)
-		{
-			diag = A[lane][lane] * A[lane][lane];
-			for (int j = lane + 1; j < k; j++) off = fma(A[lane][j], A[lane][j], off);
-		}
-		for (int o = 16; o > 0; o >>= 1)
-		{
-			off += __shfl_xor_sync(0xffffffffu, off, o);
-			diag += __shfl_xor_sync(0xffffffffu, diag, o);
-		}
-		// off-diagonal norm below 1e-15 of the diagonal norm: converged
-		if (off <= 1e-30 * diag || off == 0.0) break;
-		for (int step = 0; step < np - 1; step++)
-		{
-			if (lane < half)
-			{
-				int p, q;
-				if (lane == 0) { p = step; q = np - 1; }
-				else { p = (step + lane) % (np - 1); q = (step - lane + (np - 1)) % (np - 1); }
-				if (p > q) { const int x = p; p = q; q = x; }
-				double c = 1.0, sn = 0.0;
-				if (q < k)
-				{
-					const double apq = A[p][q];
-					if (apq != 0.0)
-					{
-						const double app = A[p][p], aqq = A[q][q];
-						const double theta = (aqq - app) * rcp64(2.0 * apq);
-						double t;
-						if (fabs(theta) > 1e15) t = 0.5 * rcp64(theta);
-						else
-						{
-							const float th = (float)theta;
-							const float tf = copysignf(1.0f, th) / (fabsf(th) + sqrtf(fmaf(th, th, 1.0f)));
-							t = (double)tf;
-						}
-						double sq, rsq;
-						sqrt_rsqrt64(fma(t, t, 1.0), sq, rsq);
-						c = rsq;
-						sn = t * rsq;
-					}
-				}
-				else q = -1;
-				rp[lane] = p;
-				rq[lane] = q;
-				rc[lane] = c;
-				rs[lane] = sn;
-			}
-			__syncwarp();
-			if (lane < k)
-				for (int i = 0; i < half; i++)
-				{
-					const int p = rp[i], q = rq[i];
-					if (q < 0) continue;
-					const double c = rc[i], sn = rs[i];
-					const double arp = A[lane][p], arq = A[lane][q];
-					A[lane][p] = c * arp - sn * arq;
-					A[lane][q] = sn * arp + c * arq;
-					const double zrp = Z[lane][p], zrq = Z[lane][q];
-					Z[lane][p] = c * zrp - sn * zrq;
-					Z[lane][q] = sn * zrp + c * zrq;
-				}
-			__syncwarp();
-			if (lane < k)
-				for (int i = 0; i < half; i++)
-				{
-					const int p = rp[i], q = rq[i];
-					if (q < 0) continue;
-					const double c = rc[i], sn = rs[i];
-					const double apc = A[p][lane], aqc = A[q][lane];
-					A[p][lane] = c * apc - sn * aqc;
-					A[q][lane] = sn * apc + c * aqc;
-				}
-			__syncwarp();
-		}
+		const float r = (i > 0 ? fabsf((float)Bv[i - 1]) : 0.0f) + fabsf((float)Bv[i]);
+		glo = fminf(glo, Af[i] - r);
+		ghi = fmaxf(ghi, Af[i] + r);
+	}
+	const float span = fmaxf(ghi - glo, 1e-30f);
+	float lo = glo - 1e-3f * span, hi = ghi + 1e-3f * span;
+	// 1. FP32 multisection
+	for (int round = 0; round < 8; round++)
+	{
+		const float w = hi - lo;
+		if (w <= 4e-7f * fmaxf(fabsf(lo), fabsf(hi))) break;
+		const float x = lo + w * (float)(lane + 1) * (1.0f / 33.0f);
+		const unsigned mask = __ballot_sync(0xffffffffu, sturm_count32(Af, B2f, k, x) >= 1);
+		const int f = mask ? __ffs(mask) - 1 : 32;
+		const float xf = lo + w * (float)(f + 1) * (1.0f / 33.0f), xl = lo + w * (float)f * (1.0f / 33.0f);
+		if (f < 32) hi = xf;
+		lo = f > 0 ? xl : lo;
 	}
 	if (lane == 0)
 	{
-		int imin = 0;
-		for (int i = 1; i < k; i++)
-			if (A[i][i] < A[imin][imin]) imin = i;
-		sc->lambda = A[imin][imin];
-		// deterministic sign: largest-magnitude component positive
+		// 2. FP64 Newton inside the Sturm bracket [L, R] (count(L) = 0, count(R) >= 1)
+		const double gspan = (double)span;
+		double L = (double)lo, R = (double)hi;
+		double dk, ddk;
+		int neg;
+		pivots64(A, B2, k, L, dk, ddk, neg);
+		if (neg != 0) L = (double)glo - gspan;
+		pivots64(A, B2, k, R, dk, ddk, neg);
+		if (neg == 0) R = (double)ghi + gspan;
+		double x = 0.5 * (L + R);
+		bool ok = false;
+		for (int it = 0; it < 100; it++)
+		{
+			pivots64(A, B2, k, x, dk, ddk, neg);
+			if (neg >= 1) R = x;
+			else L = x;
+			if (dk == 0.0)
+			{
+				ok = true;
+				break;
+			}
+			double xn = (ddk != 0.0) ? x - dk * rcp64(ddk) : 0.5 * (L + R);
+			if (!(xn > L && xn < R)) xn = 0.5 * (L + R);
+			const double tol = 2.0 * DBL_EPSILON * (fmax(fabs(x), fabs(xn)) + gspan);
+			const bool done = fabs(xn - x) <= tol || R - L <= 2.0 * tol;
+			x = xn;
+			if (done)
+			{
+				ok = true;
+				break;
+			}
+		}
+		// 3. eigenvector: pivots at the eigenvalue, then L^T y = e_k from the bottom up
+		double d = A[0] - x;
+		Y[0] = d;
+		for (int i = 0; i + 1 < k; i++)
+		{
+			if (fabs(d) < 1e-300) d = 1e-300;
+			Y[i] = d;                                   // pivot d_i, replaced by y_i below
+			d = (A[i + 1] - x) - B2[i] * rcp64(d);
+		}
+		double yn = 1.0, nrm2 = 1.0;
+		Y[k - 1] = 1.0;
+		for (int i = k - 2; i >= 0; i--)
+		{
+			yn = -Bv[i] * rcp64(Y[i]) * yn;
+			Y[i] = yn;
+			nrm2 = fma(yn, yn, nrm2);
+		}
+		double sq, rsq;
+		sqrt_rsqrt64(nrm2, sq, rsq);
 		int imax = 0;
 		for (int i = 1; i < k; i++)
-			if (fabs(Z[i][imin]) > fabs(Z[imax][imin])) imax = i;
-		const double sgn = Z[imax][imin] < 0 ? -1.0 : 1.0;
-		for (int i = 0; i < k; i++) sc->y[i] = sgn * Z[i][imin];
+			if (fabs(Y[i]) > fabs(Y[imax])) imax = i;
+		const double sgn = Y[imax] < 0 ? -rsq : rsq;
+		bool fin = ok && isfinite(x);
+		for (int i = 0; i < k; i++)
+		{
+			const double v = sgn * Y[i];
+			fin = fin && isfinite(v);
+			y[i] = v;
+		}
+		*lambda = x;
+		*status = fin ? 0 : -2;
+	}
+	__syncwarp();
+}
+
+// the eigensolve alone (test hook): one warp
+__global__ void __launch_bounds__(32) k_tridiag_test(const double* al, const double* be, int k, double* out)
+{
+	__shared__ double sh[6 * LANCZOS_MAX];
+	__shared__ double y[LANCZOS_MAX];
+	__shared__ double lam;
+	__shared__ int st;
+	tridiag_lowest(al, be, k, sh, &lam, y, &st);
+	if (threadIdx.x == 0)
+	{
+		out[0] = lam;
+		out[1] = (double)st;
+		for (int i = 0; i < k; i++) out[2 + i] = y[i];
 	}
 }
 
-void launch_lz_tridiag(int maxiter, LanczosScalars* sc, cudaStream_t st)
+// The last Lanczos step and the eigenvector in one cooperative launch: unless the iteration stopped
+// early, alpha_{k-1} = <w, v_{k-1}> (fixed-order reduction, one grid barrier); then every block
+// solves the k x k tridiagonal eigenproblem itself (k <= 32: a few microseconds of one warp, no
+// second barrier) and writes its share of the Ritz vector out = V y; block 0 stores lambda, y and the
+// status. With no iteration at all (a start vector of norm zero) the status is -1 and out is zero.
+__global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
+k_lz_finish(const double* __restrict__ w, const double* __restrict__ V, i64 n, int maxiter, double* __restrict__ partial,
+            LanczosScalars* sc, double* __restrict__ out)
 {
-	k_tridiag<<<1, 32, 0, st>>>(maxiter, sc);
-	CTG_CUDA(cudaGetLastError());
-}
-
-__global__ void k_ritz(const double* __restrict__ V, i64 n, const LanczosScalars* sc, double* __restrict__ out)
-{
-	const int k = sc->numiter;
-	for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+	cg::grid_group grid = cg::this_grid();
+	__shared__ double sh[6 * LANCZOS_MAX];
+	__shared__ double al[LANCZOS_MAX], be[LANCZOS_MAX], y[LANCZOS_MAX];
+	__shared__ double lam;
+	__shared__ int st;
+	const bool stopped = sc->stopped != 0;          // read before the barrier: the same in every block
+	const i64 stride = (i64)RED_BLOCKS * RED_THREADS;
+	const int j = maxiter - 1;
+	double alast = 0.0;
+	if (!stopped)
+	{
+		double v = 0;
+		const double* vj = V + (i64)j * n;
+		for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride) v = fma(w[i], vj[i], v);
+		block_partial(v, partial);
+		grid.sync();
+		alast = final_sum(partial);
+	}
+	const int k = stopped ? sc->numiter : maxiter;
+	if (threadIdx.x < LANCZOS_MAX)
+	{
+		const int t = threadIdx.x;
+		al[t] = t < k ? (stopped || t < j ? sc->alpha[t] : alast) : 0.0;
+		be[t] = t + 1 < k ? sc->beta[t] : 0.0;
+	}
+	__syncthreads();
+	if (k < 1 || k > LANCZOS_MAX)
+	{
+		for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride) out[i] = 0.0;
+		if (blockIdx.x == 0 && threadIdx.x == 0)
+		{
+			sc->numiter = k < 0 ? 0 : k;
+			sc->status = k < 1 ? -1 : -2;
+		}
+		return;
+	}
+	if (threadIdx.x < 32) tridiag_lowest(al, be, k, sh, &lam, y, &st);
+	__syncthreads();
+	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride)
 	{
 		double acc = 0;
-		for (int j = 0; j < k; j++) acc = fma(V[(i64)j * n + i], sc->y[j], acc);
+		for (int t = 0; t < k; t++) acc = fma(V[(i64)t * n + i], y[t], acc);
 		out[i] = acc;
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0)
+	{
+		if (!stopped) sc->alpha[j] = alast;
+		sc->numiter = k;
+		sc->lambda = lam;
+		for (int t = 0; t < k; t++) sc->y[t] = y[t];
+		sc->status = st;
 	}
 }
 
-void launch_lz_ritz(const double* V, i64 n, int maxiter, const LanczosScalars* sc, double* out, cudaStream_t st)
+void launch_lz_finish(const double* w, const double* V, i64 n, int maxiter, double* partial, LanczosScalars* sc,
+                      double* out, cudaStream_t st)
 {
-	(void)maxiter;
-	k_ritz<<<RED_BLOCKS, 256, 0, st>>>(V, n, sc, out);
+	check_coop((const void*)k_lz_finish);
+	void* args[] = {(void*)&w, (void*)&V, &n, &maxiter, &partial, &sc, &out};
+	CTG_CUDA(cudaLaunchCooperativeKernel((const void*)k_lz_finish, dim3(RED_BLOCKS), dim3(RED_THREADS), args, 0, st));
+}
+
+void tridiag_lowest_test(const double* d_alpha, const double* d_beta, int k, double* d_out, cudaStream_t st)
+{
+	k_tridiag_test<<<1, 32, 0, st>>>(d_alpha, d_beta, k, d_out);
 	CTG_CUDA(cudaGetLastError());
 }
 

@@ -52,6 +52,8 @@ EXPORTS = [
     "ctgpu_tile_tuning_report",
     "ctgpu_set_tc_tile_width",
     "ctgpu_set_tc_wait_limit",
+    "ctgpu_inject_failure",
+    "ctgpu_tridiag_lowest",
 ]
 
 KERNEL_CLASSES = ["block_gemm", "permute", "row_map", "axis_scale", "block_svd", "block_rq", "lanczos_vector",
@@ -122,6 +124,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_set_tc_tile_width.argtypes = [C.c_int]
     lib.ctgpu_set_tc_wait_limit.argtypes = [C.c_longlong]
     lib.ctgpu_set_tc_wait_limit.restype = None
+    lib.ctgpu_inject_failure.argtypes = [C.c_int, C.c_int]
+    lib.ctgpu_tridiag_lowest.argtypes = [P, P, C.c_int, P, P]
     return lib
 
 
@@ -173,15 +177,15 @@ def bond_singular_values(bond: int) -> np.ndarray | None:
 
 
 def tile_tuning() -> list:
-    """The tile autotuner's choices so far: [{key, bn, ms: [64, 128, 256], source}]."""
+    """The GEMM autotuner's choices so far: [{key, bn (0 = FP64), ms: [64, 128, 256, fp64], source}]."""
     n = lib().ctgpu_tile_tuning_report(None, 0)
     buf = C.create_string_buffer(max(n, 0) + 1)
     lib().ctgpu_tile_tuning_report(buf, len(buf))
     out = []
     for line in buf.value.decode().splitlines():
         p = line.split()
-        if len(p) == 6:
-            out.append({"key": p[0], "bn": int(p[1]), "ms": [float(x) for x in p[2:5]], "source": p[5]})
+        if len(p) == 7:
+            out.append({"key": p[0], "bn": int(p[1]), "ms": [float(x) for x in p[2:6]], "source": p[6]})
     return out
 
 

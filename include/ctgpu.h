@@ -136,11 +136,27 @@ int ctgpu_get_kernel_profile(int cls, long* launches, double* ms, double* flops,
  * chains (the roofline denominator of the FP64 path); -1 on failure. */
 double ctgpu_measure_fp64_tflops(void);
 
-/* Choices of the tensor-core tile autotuner so far in this process, one line per work-list
- * histogram key: "key tile_columns ms64 ms128 ms256 source" (source "timed" or "file": read
- * back from the tuning file). Writes at most cap - 1 characters and a terminating zero to buf
- * and returns the length of the whole text. No counterpart in the reference. */
+/* Choices of the reduced-precision GEMM autotuner so far in this process, one line per work-list
+ * histogram key: "key choice ms64 ms128 ms256 ms_fp64 source", choice = tensor-core tile columns
+ * (64, 128, 256) or 0 for the FP64 GEMM (products too small for the tensor cores to pay off), source
+ * "timed" or "file" (read back from the tuning file). Writes at most cap - 1 characters and a
+ * terminating zero to buf and returns the length of the whole text. No counterpart in the reference. */
 int ctgpu_tile_tuning_report(char* buf, int cap);
+
+/* Lowest eigenpair of the k x k symmetric tridiagonal matrix with diagonal alpha[0..k-1] and
+ * off-diagonal beta[0..k-2] (1 <= k <= 32), by the device solver that every Lanczos run uses (the
+ * reference calls LAPACK dsteqr here, src/util/krylov.c:230): *lambda and y[0..k-1] (unit norm,
+ * largest-magnitude component positive). For parity tests of that solver. Returns 0, -2 if the
+ * solver failed, or -5. */
+int ctgpu_tridiag_lowest(const double* alpha, const double* beta, int k, double* lambda, double* y);
+
+/* Host-side fault injection for tests of the error paths, per thread: which = 1 makes the next
+ * `count` block SVDs report non-convergence (dmrg_twosite then returns -1, as the reference does
+ * when LAPACK's SVD fails, src/tensor/block_sparse_tensor.c:2843-2847); which = 2 makes the next
+ * `count` Lanczos tridiagonal eigensolves report failure (-2, as for a dsteqr failure,
+ * src/util/krylov.c:231-236). Nothing is injected on the GPU. Returns 0, or -5 for other values.
+ * No counterpart in the reference. */
+int ctgpu_inject_failure(int which, int count);
 
 /* Column width of the tensor-core GEMM tiles for products planned from now on, process-wide:
  * 64, 128 or 256, or 0 (default) to let the tile autotuner choose per product. Products already
