@@ -318,9 +318,11 @@ void launch_lz_start(const double* v0, double* v, i64 n, double* partial, Lanczo
 //      keep the sub-interval where the count first reaches one (33x narrower per round), to FP32
 //      resolution;
 //   2. FP64 Newton on the last pivot d_k(x) (zero at lambda_0; its derivative follows the same
-//      recurrence), safeguarded by bisection inside the bracket that the Sturm counts maintain;
-//   3. eigenvector from L^T y = e_k (y_k = 1, y_i = -(b_i / d_i) y_{i+1}), normalised, its
-//      largest-magnitude component made positive (deterministic sign).
+//      recurrence), taken from the left end of the bracket that the Sturm counts maintain, where
+//      d_k is positive, decreasing and convex, with bisection as the fallback;
+//   3. eigenvector by a twisted factorisation (forward and backward pivots, twisted where the
+//      eigenvector is largest; robust when converged Lanczos runs leave it concentrated at one
+//      end), normalised, its largest-magnitude component made positive (deterministic sign).
 // Reciprocals are rcp64 (FP32 seed, cubic correction): an FP64 division costs over a thousand
 // cycles of GB300's FP64 pipe. Status -2 if the result is not finite.
 __device__ __forceinline__ int sturm_count32(const float* a, const float* b2, int k, float x)
@@ -412,52 +414,89 @@ __device__ void tridiag_lowest(const double* al, const double* be, int k, double
 	}
 	if (lane == 0)
 	{
-		// 2. FP64 Newton inside the Sturm bracket [L, R] (count(L) = 0, count(R) >= 1)
+		// 2. FP64 Newton from the left end of the Sturm bracket [L, R] (count(L) = 0, count(R) >= 1):
+		// left of lambda_0 the last pivot d_k(x) is positive, decreasing and convex, so Newton steps
+		// from L approach lambda_0 from below; a step that passes it (or leaves the bracket) only
+		// moves R, or falls back to bisection. The bracket closes with a probe just above L.
 		const double gspan = (double)span;
 		double L = (double)lo, R = (double)hi;
-		double dk, ddk;
+		double dL, ddL, dk, ddk;
 		int neg;
-		pivots64(A, B2, k, L, dk, ddk, neg);
-		if (neg != 0) L = (double)glo - gspan;
+		pivots64(A, B2, k, L, dL, ddL, neg);
+		if (neg != 0)
+		{
+			L = (double)glo - gspan;
+			pivots64(A, B2, k, L, dL, ddL, neg);
+		}
 		pivots64(A, B2, k, R, dk, ddk, neg);
 		if (neg == 0) R = (double)ghi + gspan;
-		double x = 0.5 * (L + R);
 		bool ok = false;
-		for (int it = 0; it < 100; it++)
+		for (int it = 0; it < 200; it++)
 		{
-			pivots64(A, B2, k, x, dk, ddk, neg);
-			if (neg >= 1) R = x;
-			else L = x;
-			if (dk == 0.0)
+			const double tol = 2.0 * DBL_EPSILON * (fmax(fabs(L), fabs(R)) + gspan);
+			if (R - L <= 2.0 * tol)
 			{
 				ok = true;
 				break;
 			}
-			double xn = (ddk != 0.0) ? x - dk * rcp64(ddk) : 0.5 * (L + R);
-			if (!(xn > L && xn < R)) xn = 0.5 * (L + R);
-			const double tol = 2.0 * DBL_EPSILON * (fmax(fabs(x), fabs(xn)) + gspan);
-			const bool done = fabs(xn - x) <= tol || R - L <= 2.0 * tol;
-			x = xn;
-			if (done)
+			const double mid = 0.5 * (L + R);
+			double xn = (ddL < 0.0 && dL > 0.0) ? L - dL * rcp64(ddL) : mid;
+			if (!(xn > L && xn < R)) xn = mid;
+			if (xn - L <= tol) xn = fmin(L + tol, mid);
+			pivots64(A, B2, k, xn, dk, ddk, neg);
+			if (neg == 0)
 			{
-				ok = true;
-				break;
+				L = xn;
+				dL = dk;
+				ddL = ddk;
+			}
+			else R = xn;
+		}
+		const double x = 0.5 * (L + R);
+		// 3. eigenvector by the twisted factorisation at x (robust where the eigenvector is small at
+		// either end): forward pivots d+ (in Y) and backward pivots d- (Dm), twist index r = argmin
+		// |d+_r + d-_r - (a_r - x)|; y_r = 1, y_i = -(b_i / d+_i) y_{i+1} above r, y_i = -(b_{i-1} /
+		// d-_i) y_{i-1} below
+		double Dm[LANCZOS_MAX];
+		{
+			double d = A[k - 1] - x;
+			for (int i = k - 1; i >= 0; i--)
+			{
+				if (i < k - 1) d = (A[i] - x) - B2[i] * rcp64(d);
+				if (fabs(d) < 1e-300) d = 1e-300;
+				Dm[i] = d;
 			}
 		}
-		// 3. eigenvector: pivots at the eigenvalue, then L^T y = e_k from the bottom up
-		double d = A[0] - x;
-		Y[0] = d;
-		for (int i = 0; i + 1 < k; i++)
+		int r = 0;
+		double gbest = 0.0;
 		{
-			if (fabs(d) < 1e-300) d = 1e-300;
-			Y[i] = d;                                   // pivot d_i, replaced by y_i below
-			d = (A[i + 1] - x) - B2[i] * rcp64(d);
+			double d = A[0] - x;
+			for (int i = 0; i < k; i++)
+			{
+				if (i > 0) d = (A[i] - x) - B2[i - 1] * rcp64(d);
+				if (fabs(d) < 1e-300) d = 1e-300;
+				Y[i] = d;
+				const double g = fabs(d + Dm[i] - (A[i] - x));
+				if (i == 0 || g < gbest)
+				{
+					gbest = g;
+					r = i;
+				}
+			}
 		}
-		double yn = 1.0, nrm2 = 1.0;
-		Y[k - 1] = 1.0;
-		for (int i = k - 2; i >= 0; i--)
+		double nrm2 = 1.0;
+		double yn = 1.0;
+		for (int i = r - 1; i >= 0; i--)
 		{
 			yn = -Bv[i] * rcp64(Y[i]) * yn;
+			Y[i] = yn;
+			nrm2 = fma(yn, yn, nrm2);
+		}
+		Y[r] = 1.0;
+		yn = 1.0;
+		for (int i = r + 1; i < k; i++)
+		{
+			yn = -Bv[i - 1] * rcp64(Dm[i]) * yn;
 			Y[i] = yn;
 			nrm2 = fma(yn, yn, nrm2);
 		}

@@ -57,6 +57,16 @@ def test_tridiag_lanczos_like(gpu):
         _check(gpu, a, b)
 
 
+def test_tridiag_eigenvector_concentrated_at_the_top(gpu):
+    """A converging Lanczos run: the lowest Ritz vector lives in the leading components and is
+    negligible at the end of the chain (a small beta decouples it), which a plain bottom-up
+    recurrence cannot resolve."""
+    a = np.array([-12.0, -3.5, 1.2, 2.5, 4.0])
+    for tiny in (1e-4, 1e-7, 1e-10):
+        _check(gpu, a, np.array([0.8, tiny, 0.6, 0.3]))
+        _check(gpu, a[::-1].copy(), np.array([0.3, 0.6, tiny, 0.8]))
+
+
 def test_tridiag_wilkinson(gpu):
     """Wilkinson's W21+ (pairs of nearly equal eigenvalues at the top of the spectrum)."""
     a = np.abs(np.arange(-10, 11)).astype(np.float64)
