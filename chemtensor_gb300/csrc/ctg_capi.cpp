@@ -165,9 +165,10 @@ int ctgpu_tridiag_lowest(const double* alpha, const double* beta, int k, double*
 
 int ctgpu_inject_failure(int which, int count)
 {
-	if (count < 0 || (which != 1 && which != 2)) return ERR_RUNTIME;
+	if (count < 0 || which < 1 || which > 3) return ERR_RUNTIME;
 	if (which == 1) ctg::g_inject_svd_failure = count;
-	else ctg::g_inject_tridiag_failure = count;
+	else if (which == 2) ctg::g_inject_tridiag_failure = count;
+	else ctg::g_inject_zero_start = count;
 	return 0;
 }
 
@@ -322,6 +323,15 @@ int ctgpu_device_memory(int device, size_t* free_bytes, size_t* total_bytes)
 		CTG_CUDA(cudaSetDevice(device));
 		CTG_CUDA(cudaMemGetInfo(free_bytes, total_bytes));
 		CTG_CUDA(cudaSetDevice(prev));
+		return 0;
+	});
+}
+
+int ctgpu_mpo_inner_product(const struct mps* chi, const struct mpo* op, const struct mps* psi, double* ret)
+{
+	return guarded([&] {
+		CTG_CHECK(ret, "null argument");
+		ctg::mpo_inner_product_gpu(chi, op, psi, g_opts.device, ret);
 		return 0;
 	});
 }

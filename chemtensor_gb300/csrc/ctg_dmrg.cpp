@@ -246,8 +246,9 @@ DTensor contraction_step_left(Ctx& c, const DTensor& a, const DTensor& w, const 
 	return op_transpose(c, s, p2);
 }
 
-// contraction_operator_step_right (src/algorithm/chain_ops.c:116-165), with b = a
-DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& r, int precision)
+// contraction_operator_step_right (src/algorithm/chain_ops.c:116-165) with ket a and bra b
+DTensor contraction_step_right_ab(Ctx& c, const DTensor& a, const DTensor& b, const DTensor& w, const DTensor& r,
+                                  int precision)
 {
 	DTensor s = op_dot(c, a, AX_TRAILING, r, AX_LEADING, 1, precision);
 	const int p0[5] = {1, 2, 0, 3, 4};
@@ -255,11 +256,18 @@ DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const
 	s = op_dot(c, w, AX_TRAILING, t, AX_LEADING, 2, precision);
 	const int p1[5] = {4, 2, 0, 1, 3};
 	t = op_transpose(c, s, p1);
-	DTensor br = view_reversed(c, a);
-	br.conj = a.cplx;
+	// the bra: b with reversed axis directions, complex conjugated (chain_ops.c:138-149)
+	DTensor br = view_reversed(c, b);
+	br.conj = b.cplx;
 	s = op_dot(c, t, AX_TRAILING, br, AX_TRAILING, 2, precision);
 	const int p2[4] = {1, 2, 3, 0};
 	return op_transpose(c, s, p2);
+}
+
+// contraction_operator_step_right with b = a
+DTensor contraction_step_right(Ctx& c, const DTensor& a, const DTensor& w, const DTensor& r, int precision)
+{
+	return contraction_step_right_ab(c, a, a, w, r, precision);
 }
 
 namespace {
@@ -523,6 +531,13 @@ int minimize_local_energy(Ctx& c, const DTensor& w, const DTensor& l, const DTen
 	double* pp = (double*)partial.ptr;
 	cudaStream_t s = c.stream();
 	const double dn = (double)n;
+	if (g_inject_zero_start > 0)
+	{
+		// host-side fault injection (tests of the error path): the start vector is zeroed, so that the
+		// device's own check of its norm takes the breakdown exit (status -1)
+		g_inject_zero_start--;
+		CTG_CUDA(cudaMemsetAsync(a_start.data(), 0, (size_t)n * sizeof(double), s));
+	}
 	{
 		KScope ks(c, K_LANCZOS, 1, 3.0 * dn, 24.0 * dn);
 		launch_lz_start(a_start.data(), Vp, n, pp, d_sc, s);
@@ -876,6 +891,45 @@ void mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device, doub
 	CTG_CHECK(rf.m().ndim == 2 && rf.m().dim[0] == 1 && rf.m().dim[1] == 1, "mps_vdot: unexpected result shape");
 	double v[2] = {0.0, 0.0};
 	if (rf.m().nnz > 0) copy_to_host(c, rf, v);
+	c.sync();
+	ret[0] = v[0];
+	if (cplx) ret[1] = v[1];
+}
+
+// ------------------------------------------------------------------------------------
+// mpo_inner_product (src/algorithm/chain_ops.c:274-317): <chi|op|psi> by right environments
+// ------------------------------------------------------------------------------------
+
+void mpo_inner_product_gpu(const struct mps* chi, const struct mpo* op, const struct mps* psi, int device, double* ret)
+{
+	CTG_CHECK(chi && op && psi && op->nsites >= 1 && chi->nsites == op->nsites && psi->nsites == op->nsites,
+	          "mpo_inner_product: invalid arguments");
+	const int L = op->nsites;
+	CTG_CHECK(chi->a[0].dim_logical[0] == 1 && op->a[0].dim_logical[0] == 1 && psi->a[0].dim_logical[0] == 1 &&
+	              chi->a[L - 1].dim_logical[2] == 1 && op->a[L - 1].dim_logical[3] == 1 &&
+	              psi->a[L - 1].dim_logical[2] == 1,
+	          "mpo_inner_product: leading and trailing virtual bonds must have dimension 1");
+	const bool cplx = psi->a[0].dtype == CT_DOUBLE_COMPLEX;
+	CTG_CHECK(chi->a[0].dtype == psi->a[0].dtype && op->a[0].dtype == psi->a[0].dtype,
+	          "mpo_inner_product: MPS and MPO of different numeric types");
+	Ctx& c = context_for_device(device);
+	const std::vector<q32> qa(psi->a[L - 1].qnums_logical[2], psi->a[L - 1].qnums_logical[2] + 1);
+	const std::vector<q32> qw(op->a[L - 1].qnums_logical[3], op->a[L - 1].qnums_logical[3] + 1);
+	const std::vector<q32> qb(chi->a[L - 1].qnums_logical[2], chi->a[L - 1].qnums_logical[2] + 1);
+	DTensor r = dummy_block(c, qa, qw, qb, true, cplx);
+	for (int i = L - 1; i >= 0; i--)
+	{
+		DTensor a = tensor_from_struct(c, &psi->a[i]);
+		DTensor b = tensor_from_struct(c, &chi->a[i]);
+		DTensor w = tensor_from_struct(c, &op->a[i]);
+		r = contraction_step_right_ab(c, a, b, w, r);
+	}
+	// flatten the left virtual bonds: a 1 x 1 tensor remains
+	DTensor t = op_flatten(c, r, 0, TENSOR_AXIS_OUT);
+	t = op_flatten(c, t, 0, TENSOR_AXIS_OUT);
+	CTG_CHECK(t.m().ndim == 2 && t.m().dim[0] == 1 && t.m().dim[1] == 1, "mpo_inner_product: unexpected result shape");
+	double v[2] = {0.0, 0.0};
+	if (t.m().nnz > 0) copy_to_host(c, t, v);
 	c.sync();
 	ret[0] = v[0];
 	if (cplx) ret[1] = v[1];

@@ -81,6 +81,13 @@ double time_local_hamiltonian(Ctx& c, const DTensor& a, const DTensor& w, const 
 // (real MPS) or two (complex: real and imaginary part)
 void mps_vdot_gpu(const struct mps* chi, const struct mps* psi, int device, double* ret);
 
+// <chi|op|psi> on the device (mpo_inner_product, src/algorithm/chain_ops.c:274-317); ret as above
+void mpo_inner_product_gpu(const struct mps* chi, const struct mpo* op, const struct mps* psi, int device, double* ret);
+
+// contraction_operator_step_right (src/algorithm/chain_ops.c:116-165) with ket a and bra b
+DTensor contraction_step_right_ab(Ctx& c, const DTensor& a, const DTensor& b, const DTensor& w, const DTensor& r,
+                                  int precision = GEMM_FP64);
+
 // spin-orbital molecular Hamiltonian as an MPO (construct_spin_molecular_hamiltonian_mpo_assembly with
 // optimize = false + mpo_from_assembly, src/operator/hamiltonian.c:2768-2979); tkin n x n and vint
 // n x n x n x n row-major; out receives reference-layout tensors

@@ -1265,6 +1265,7 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 
 thread_local int g_inject_svd_failure = 0;
 thread_local int g_inject_tridiag_failure = 0;
+thread_local int g_inject_zero_start = 0;
 
 int op_svd_finish(Ctx& c, const SvdPending& pend)
 {

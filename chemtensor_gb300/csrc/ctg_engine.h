@@ -273,9 +273,11 @@ int op_svd_finish(Ctx& c, const SvdPending& pend);
 // launch, synchronise, finish. Returns 0 or -1.
 int op_svd(Ctx& c, const DTensor& a, SvdResult& res);
 // host-side fault injection for tests of the error paths (per thread): the next n block SVDs report
-// non-convergence, the next n Lanczos tridiagonal eigensolves report failure
+// non-convergence, the next n Lanczos tridiagonal eigensolves report failure, the next n local
+// eigenproblems start from a vector the host has zeroed
 extern thread_local int g_inject_svd_failure;
 extern thread_local int g_inject_tridiag_failure;
+extern thread_local int g_inject_zero_start;
 
 // block RQ (block_sparse_tensor_rq, block_sparse_tensor.c:2544-2676). Returns 0 or -1.
 int op_rq(Ctx& c, const DTensor& a, DTensor& r, DTensor& q);

@@ -72,73 +72,4 @@ __device__ __forceinline__ void sqrt_rsqrt64(double x, double& sq, double& rsq)
 	rsq = y * __hiloint2double((1023 - ex / 2) << 20, 0);
 }
 
-// ---- double-float ("df64") arithmetic: a value is the unevaluated sum hi + lo of two floats with
-// |lo| <= ulp(hi) / 2, about 48 significant bits. Built from the error-free transformations of
-// Knuth (two-sum) and Dekker (two-product, here with a hardware FMA); see D. H. Bailey's
-// double-double / double-float libraries for the scheme. GB300 issues FP32 at 64 times the FP64
-// rate, so a df64 operation of about a dozen FP32 instructions is several times cheaper than one
-// FP64 instruction. Stored as float2 (x = hi, y = lo): the same 8 bytes as a double.
-
-__device__ __forceinline__ float2 df_make(float hi, float lo) { return make_float2(hi, lo); }
-
-// exact split of a double into hi + lo (rounding only below the 48th bit)
-__device__ __forceinline__ float2 df_from_double(double x)
-{
-	const float hi = __double2float_rn(x);
-	return make_float2(hi, __double2float_rn(x - (double)hi));
-}
-
-__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
-
-// s + e = a + b exactly
-__device__ __forceinline__ float2 two_sum(float a, float b)
-{
-	const float s = __fadd_rn(a, b);
-	const float bb = __fsub_rn(s, a);
-	const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-	return make_float2(s, e);
-}
-
-// s + e = a + b exactly, for |a| >= |b|
-__device__ __forceinline__ float2 quick_two_sum(float a, float b)
-{
-	const float s = __fadd_rn(a, b);
-	return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
-
-__device__ __forceinline__ float2 df_add(float2 a, float2 b)
-{
-	const float2 s = two_sum(a.x, b.x);
-	const float2 t = two_sum(a.y, b.y);
-	float2 r = quick_two_sum(s.x, __fadd_rn(s.y, t.x));
-	return quick_two_sum(r.x, __fadd_rn(r.y, t.y));
-}
-
-// a * b (both df64)
-__device__ __forceinline__ float2 df_mul(float2 a, float2 b)
-{
-	const float p = __fmul_rn(a.x, b.x);
-	float e = __fmaf_rn(a.x, b.x, -p);
-	e = __fmaf_rn(a.x, b.y, e);
-	e = __fmaf_rn(a.y, b.x, e);
-	return quick_two_sum(p, e);
-}
-
-// a * b for a float a (exactly representable coefficient) and df64 b
-__device__ __forceinline__ float2 df_mul_f(float a, float2 b)
-{
-	const float p = __fmul_rn(a, b.x);
-	float e = __fmaf_rn(a, b.x, -p);
-	e = __fmaf_rn(a, b.y, e);
-	return quick_two_sum(p, e);
-}
-
-// acc + a * b, the product formed exactly in its leading part (inner products)
-__device__ __forceinline__ float2 df_fma(float2 a, float2 b, float2 acc)
-{
-	return df_add(acc, df_mul(a, b));
-}
-
-__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
-
 }  // namespace ctg

@@ -536,10 +536,11 @@ __global__ void __launch_bounds__(32) k_tridiag_test(const double* al, const dou
 }
 
 // The last Lanczos step and the eigenvector in one cooperative launch: unless the iteration stopped
-// early, alpha_{k-1} = <w, v_{k-1}> (fixed-order reduction, one grid barrier); then every block
-// solves the k x k tridiagonal eigenproblem itself (k <= 32: a few microseconds of one warp, no
-// second barrier) and writes its share of the Ritz vector out = V y; block 0 stores lambda, y and the
-// status. With no iteration at all (a start vector of norm zero) the status is -1 and out is zero.
+// early, alpha_{k-1} = <w, v_{k-1}> (fixed-order reduction, one grid barrier); then one warp of
+// block 0 solves the k x k tridiagonal eigenproblem (k <= 32: microseconds of serial FP64 work, which
+// copies in every block would queue on the same SM sub-partitions) and stores lambda, y and the
+// status; after a second grid barrier every block writes its share of the Ritz vector out = V y.
+// With no iteration at all (a start vector of norm zero) the status is -1 and out is zero.
 __global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
 k_lz_finish(const double* __restrict__ w, const double* __restrict__ V, i64 n, int maxiter, double* __restrict__ partial,
             LanczosScalars* sc, double* __restrict__ out)
@@ -580,21 +581,27 @@ k_lz_finish(const double* __restrict__ w, const double* __restrict__ V, i64 n, i
 		}
 		return;
 	}
-	if (threadIdx.x < 32) tridiag_lowest(al, be, k, sh, &lam, y, &st);
+	if (blockIdx.x == 0)
+	{
+		if (threadIdx.x < 32) tridiag_lowest(al, be, k, sh, &lam, y, &st);
+		__syncthreads();
+		if (threadIdx.x == 0)
+		{
+			if (!stopped) sc->alpha[j] = alast;
+			sc->numiter = k;
+			sc->lambda = lam;
+			for (int t = 0; t < k; t++) sc->y[t] = y[t];
+			sc->status = st;
+		}
+	}
+	grid.sync();
+	if (threadIdx.x < LANCZOS_MAX) y[threadIdx.x] = threadIdx.x < k ? __ldcg(sc->y + threadIdx.x) : 0.0;
 	__syncthreads();
 	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride)
 	{
 		double acc = 0;
 		for (int t = 0; t < k; t++) acc = fma(V[(i64)t * n + i], y[t], acc);
 		out[i] = acc;
-	}
-	if (blockIdx.x == 0 && threadIdx.x == 0)
-	{
-		if (!stopped) sc->alpha[j] = alast;
-		sc->numiter = k;
-		sc->lambda = lam;
-		for (int t = 0; t < k; t++) sc->y[t] = y[t];
-		sc->status = st;
 	}
 }
 

@@ -379,34 +379,11 @@ __device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int
 	return step_pair_idx(mode, step, k, t.bs, cA, cB, npad, sp, cp, sq, cq);
 }
 
-// Precision of the finishing tour: its column records hold double-float values (hi + lo of two
-// floats, about 48 bits; ctg_fp64.cuh), so that the inner products and rotations run on the FP32
-// pipe, which GB300 issues at 64 times the FP64 rate. DF_EPS bounds the rounding of one operation.
-constexpr double DF_EPS = 1.0 / (double)(1ll << 46);
-
-__device__ __forceinline__ float2 warp_sum_df(float2 v)
-{
-	// xor butterfly: every lane ends with the bitwise-identical total (df_add is symmetric)
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1)
-		v = df_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)));
-	return v;
-}
-
-// squared norm of the first n entries of a double-float column record, by one warp
-__device__ __forceinline__ double df_norm2(const float2* col, int n, int lane)
-{
-	float2 acc = make_float2(0.0f, 0.0f);
-	for (int i = lane; i < n; i += 32) acc = df_fma(col[i], col[i], acc);
-	return df_to_double(warp_sum_df(acc));
-}
-
-// One inner step of the finishing tour. The pairs of a step are disjoint, so each warp takes whole
-// pairs: the inner product in double-float (every lane gets the sum), the rotation parameters
-// (computed by every lane in FP64 from the sums: a few FP64 instructions per pair) and the
-// three-shear rotation of the two records (T entries 0 .. N-1, V entries N .. N+r-1) in
-// double-float. One CTA barrier per step, and the warps of different pairs run on different SM
-// sub-partitions.
+// One inner step of the FP64 tour. The pairs of a step are disjoint, so each warp takes whole
+// pairs: the inner product (every lane gets the sum), the rotation parameters (computed by every
+// lane: an FP64 warp instruction costs the same whatever the number of active lanes) and the
+// three-shear rotation of the two records (T entries 0 .. N-1, V entries N .. N+r-1). One CTA
+// barrier per step, and the warps of different pairs run on different SM sub-partitions.
 __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, int cB, int npad, float tol2, const StepBuf& sb,
                             long long* cyc, double& flops)
 {
@@ -418,19 +395,19 @@ __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, 
 	{
 		int sp, cp, sq, cq;
 		if (!step_pair(t, mode, step, k, cA, cB, npad, sp, cp, sq, cq)) continue;
-		float2* x = (float2*)t.col(buf, sp, cp);
-		float2* y = (float2*)t.col(buf, sq, cq);
-		float2 g2 = make_float2(0.0f, 0.0f);
-		for (int i = lane; i < t.N; i += 32) g2 = df_fma(x[i], y[i], g2);
-		const double g = df_to_double(warp_sum_df(g2));
+		double* x = t.col(buf, sp, cp);
+		double* y = t.col(buf, sq, cq);
+		double g = 0;
+		for (int i = lane; i < t.N; i += 32) g = fma(x[i], y[i], g);
+		g = warp_sum(g);
 		double* pa = t.nrm(buf, sp) + cp;
 		double* pb = t.nrm(buf, sq) + cq;
 		const double al = *pa, be = *pb;
 		double tau, sn, tn;
 		float c2;
 		const bool rot = rotation_params(al, be, g, tol2, tau, sn, tn, c2);
-		// executed flops (FP64-equivalent, run as double-float): an inner product per examined pair,
-		// three multiply-adds per entry of the two column records per rotation (counted on lane 0)
+		// executed FP64 flops: an inner product per examined pair, three FMAs per entry of the two
+		// column records per rotation (counted on lane 0 of each warp)
 		if (lane == 0)
 		{
 			flops += 2.0 * t.N;
@@ -438,12 +415,11 @@ __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, 
 		}
 		if (rot)
 		{
-			const float2 ta = df_from_double(tau), sa = df_from_double(sn);
 			for (int i = lane; i < len; i += 32)
 			{
-				const float2 x1 = df_add(x[i], df_neg(df_mul(ta, y[i])));
-				const float2 y1 = df_add(y[i], df_mul(sa, x1));
-				x[i] = df_add(x1, df_neg(df_mul(ta, y1)));
+				const double x1 = fma(-tau, y[i], x[i]);
+				const double y1 = fma(sn, x1, y[i]);
+				x[i] = fma(-tau, y1, x1);
 				y[i] = y1;
 			}
 			__syncwarp();
@@ -1023,9 +999,9 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 		double acc = 0.0;
 		for (int k = 0; k <= kmax; k++) acc = fma(rs[(i64)k * ldr + i], vj[k], acc);
 		const int slot = j < own0 ? 0 : 1, c = slot ? j - own0 : j;
-		float2* rec = (float2*)t.col(0, slot, c);
-		rec[i] = df_from_double(acc);
-		rec[N + i] = df_from_double(i < r ? vj[i] : 0.0);
+		double* rec = t.col(0, slot, c);
+		rec[i] = acc;
+		rec[N + i] = i < r ? vj[i] : 0.0;
 	}
 	if (tid == 0) flops += 2.0 * ((double)N * r - 0.5 * (double)r * r) * nown;
 	__syncthreads();
@@ -1138,7 +1114,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 		for (int slot = 0; slot < 2; slot++)
 		{
 			const int x = slot ? B : A;
-			float2* dst = (float2*)t.col(0, slot, 0);
+			double* dst = t.col(0, slot, 0);
 			for (i64 e = tid; e < (i64)t.cnt(x) * t.ld; e += SVD_THREADS)
 			{
 				const int c = (int)(e / t.ld), i = (int)(e % t.ld);
@@ -1146,13 +1122,13 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 				double v;
 				if (i < N) v = (i >= g) ? __ldcg(xs.W + (i64)i * M + g) : 0.0;
 				else v = (i - N == g) ? 1.0 : 0.0;
-				dst[e] = df_from_double(v);
+				dst[e] = v;
 			}
 		}
 		__syncthreads();
 	}
 
-	const float tol2 = (float)((double)N * DF_EPS * (double)N * DF_EPS);
+	const float tol2 = (float)((double)N * DBL_EPSILON * (double)N * DBL_EPSILON);
 	int buf = 0, sweep = 0;
 	bool converged = r <= 1;
 	for (; sweep < SVD_MAX_SWEEPS && !converged; sweep++)
@@ -1164,7 +1140,10 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			const int nc = t.cnt(slot ? B : A);
 			for (int c = warp; c < nc; c += NWARPS)
 			{
-				const double acc = df_norm2((const float2*)t.col(buf, slot, c), N, lane);
+				const double* col = t.col(buf, slot, c);
+				double acc = 0;
+				for (int i = lane; i < N; i += 32) acc = fma(col[i], col[i], acc);
+				acc = warp_sum(acc);
 				if (lane == 0) t.nrm(buf, slot)[c] = acc;
 			}
 		}
@@ -1216,7 +1195,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 		// eps / 4: a rotation by an angle of about cos_pq changes the cosine of a pair (p, r) by about
 		// cos_pq cos_qr (whatever the column norms), so after such a sweep every cosine is below
 		// 2 N (eps / 4) <= N eps / 2, within the tolerance, and the confirming sweep is skipped.
-		const int skip_bits = __float_as_int(0.25f * (float)DF_EPS);
+		const int skip_bits = __float_as_int(0.25f * (float)DBL_EPSILON);
 		if (cl > 1) converged = __ldcg(xs.flags + sweep) == 0 || __ldcg(xs.cmax + sweep) <= skip_bits;
 		else
 		{
@@ -1229,17 +1208,20 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	for (int slot = 0; slot < 2; slot++)
 	{
 		const int x = slot ? B : A, nc = t.cnt(x);
-		const float2* src = (const float2*)t.col(buf, slot, 0);
+		const double* src = t.col(buf, slot, 0);
 		for (i64 e = tid; e < (i64)nc * t.ld; e += SVD_THREADS)
 		{
 			const int c = (int)(e / t.ld), i = (int)(e % t.ld);
 			const int g = x * t.bs + c;
-			if (i < N) xs.T[(i64)g * N + i] = df_to_double(src[e]);
-			else if (i - N < r) xs.V[(i64)g * r + (i - N)] = df_to_double(src[e]);
+			if (i < N) xs.T[(i64)g * N + i] = src[e];
+			else if (i - N < r) xs.V[(i64)g * r + (i - N)] = src[e];
 		}
 		for (int c = warp; c < nc; c += NWARPS)
 		{
-			const double acc = df_norm2((const float2*)t.col(buf, slot, c), N, lane);
+			const double* col = t.col(buf, slot, c);
+			double acc = 0;
+			for (int i = lane; i < N; i += 32) acc = fma(col[i], col[i], acc);
+			acc = warp_sum(acc);
 			if (lane == 0) xs.sig[x * t.bs + c] = sqrt(acc);
 		}
 	}

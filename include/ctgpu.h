@@ -154,8 +154,10 @@ int ctgpu_tridiag_lowest(const double* alpha, const double* beta, int k, double*
  * `count` block SVDs report non-convergence (dmrg_twosite then returns -1, as the reference does
  * when LAPACK's SVD fails, src/tensor/block_sparse_tensor.c:2843-2847); which = 2 makes the next
  * `count` Lanczos tridiagonal eigensolves report failure (-2, as for a dsteqr failure,
- * src/util/krylov.c:231-236). Nothing is injected on the GPU. Returns 0, or -5 for other values.
- * No counterpart in the reference. */
+ * src/util/krylov.c:231-236); which = 3 zeroes the start vector of the next `count` local
+ * eigenproblems with a host-issued memset, so that the device's own norm check takes the breakdown
+ * exit (-1: fewer Lanczos iterations than eigenvalues, src/util/krylov.c:218-223). No kernel is
+ * made to fault. Returns 0, or -5 for other values. No counterpart in the reference. */
 int ctgpu_inject_failure(int which, int count);
 
 /* Column width of the tensor-core GEMM tiles for products planned from now on, process-wide:
@@ -193,6 +195,13 @@ int ctgpu_device_memory(int device, size_t* free_bytes, size_t* total_bytes);
  * ctgpu_last_error). */
 int ctgpu_mps_vdot(const struct mps* chi, const struct mps* psi, double* ret);
 int ctgpu_mps_norm(const struct mps* psi, double* ret);
+
+/* <chi|op|psi> (chi complex conjugated), contracted on the device by right environments with the
+ * environment kept in HBM. Replaces mpo_inner_product (src/algorithm/chain_ops.c:274-317, declared in
+ * include/algorithm/chain_ops.h:26): one double for CT_DOUBLE_REAL tensors, two (real, imaginary
+ * part) for CT_DOUBLE_COMPLEX ones. Leading and trailing virtual bonds must have dimension 1 (the
+ * reference asserts this). Returns 0, or -5 (message via ctgpu_last_error). */
+int ctgpu_mpo_inner_product(const struct mps* chi, const struct mpo* op, const struct mps* psi, double* ret);
 
 /* Spin-orbital molecular Hamiltonian
  *   H = sum_{ij,s} tkin[i,j] a+_{is} a_{js} + 1/2 sum_{ijkl,s,u} vint[i,j,k,l] a+_{is} a+_{ju} a_{lu} a_{ks}
