@@ -450,25 +450,36 @@ def bench_local_h(args, world, rank, local):
 def bench_serve(args, world, rank, local):
     """Serving mix: a seeded Poisson stream of Heisenberg / Hubbard ground-state solves (L 8..48,
     D 16..256, 2 sweeps each), replayed once by one solver thread (serial plain-FP64 solves, the
-    baseline) and once by --workers solver threads sharing the GPU."""
+    baseline) and once by --workers solver threads sharing the GPU in the arithmetic of
+    --serve-precision, with inputs built ahead by a producer thread."""
     from chemtensor_gb300 import native, serving
     lib = native.lib()
     lib.ctgpu_set_device(local)
     reqs = serving.generate_requests(args.requests, args.rate, seed=2024)
-    # warm-up: the first solves pay for context creation and kernel loading
-    serving.SolverPool(workers=1, device=local, sweeps=1).run(serving.generate_requests(3, 0.0, seed=7))
-    serial = serving.summarize(serving.SolverPool(workers=1, device=local).run(reqs))
-    pool = serving.SolverPool(workers=args.workers, device=local)
+    prec = PRECISIONS[args.serve_precision]
+    # warm-up: the first solves pay for context creation, kernel loading and (reduced precision) the
+    # autotuner's first timings
+    for p in sorted({0, prec}):
+        serving.SolverPool(workers=1, device=local, sweeps=1, precision=p).run(serving.generate_requests(6, 0.0, seed=7))
+    serial_pool = serving.SolverPool(workers=1, device=local)
+    serial = serving.summarize(serial_pool.run(reqs))
+    pool = serving.SolverPool(workers=args.workers, device=local, precision=prec, prefetch=2 * args.workers)
     conc = serving.summarize(pool.run(reqs))
     energies = {r.rid: r.energy for r in pool.results}
+    ref = {r.rid: r.energy for r in serial_pool.results}
+    de = [abs(energies[k] - ref[k]) for k in ref if np.isfinite(energies.get(k, np.nan)) and np.isfinite(ref[k])]
     line = {
         "metric": "DMRG serving throughput (Heisenberg/Hubbard mix, L 8-48, D 16-256, 2 sweeps)",
         "value": conc["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": args.requests, "warmup": 3,
         "ms_per_step": 1e3 / conc["solves_per_s"] if conc["solves_per_s"] else None, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded request stream)",
-        "config": {"workload": f"{args.requests} requests, Poisson rate {args.rate}/s, seed 2024", "workers": args.workers},
-        "concurrent": conc, "serial": serial,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == 0 else f"{args.serve_precision}+f32acc (products chosen by the autotuner), final sweep f64",
+        "data": "synthetic (seeded request stream)",
+        "config": {"workload": f"{args.requests} requests, Poisson rate {args.rate}/s, seed 2024", "workers": args.workers,
+                   "precision": args.serve_precision, "prefetch": 2 * args.workers},
+        "concurrent": conc, "serial_fp64": serial,
         "speedup_vs_serial": (conc["solves_per_s"] / serial["solves_per_s"]) if serial["solves_per_s"] else None,
+        "max_abs_dE_vs_serial_fp64": max(de) if de else None,
         "energy_checksum": float(sum(energies.values())),
     }
     if rank == 0:
@@ -494,10 +505,15 @@ def bench_molecular(args, world, rank, local):
     cs.free_mps(c)
     cH = cs.make_c_mpo(H)
     runs = {}
-    for name in args.mol_precisions.split(","):
-        # "bf16x3env": split-BF16 also in the environment updates of the reduced-precision sweeps
-        native.set_precision(PRECISIONS[name.replace("env", "")])
-        lib.ctgpu_set_reduced_environments(1 if name.endswith("env") else 0)
+    for spec in args.mol_precisions.split(","):
+        # "bf16x3env": split-BF16 also in the environment updates of the reduced-precision sweeps;
+        # a suffix ":k" runs the last k sweeps in FP64 (default 1)
+        name, _, fin = spec.partition(":")
+        lib.ctgpu_set_final_fp64_sweeps(int(fin) if fin else 1)
+        if fin:
+            name = spec
+        native.set_precision(PRECISIONS[name.split(":")[0].replace("env", "")])
+        lib.ctgpu_set_reduced_environments(1 if name.split(":")[0].endswith("env") else 0)
         lib.ctgpu_clear_plan_cache()
         lib.ctgpu_set_profiling(1 if args.mol_profile else 0, 0)
         cP = cs.make_c_mps(psi0)
@@ -520,14 +536,25 @@ def bench_molecular(args, world, rank, local):
         lib.ctgpu_set_profiling(0, 0)
     native.set_precision(0)
     lib.ctgpu_set_reduced_environments(0)
+    lib.ctgpu_set_final_fp64_sweeps(1)
     cs.free_mpo(cH)
+    oracle_leg = None
+    if args.mol_oracle_sweeps > 0 and rank == 0:
+        # the reference algorithm (the C restatement, bit-identical to the reference where both build)
+        # from the same start state on all host cores: the FP64 anchor of the |dE| figures
+        times, en_o, used = run_oracle_sweeps_for(H, psi0, args.mol_oracle_sweeps, os.cpu_count() or 1, D)
+        oracle_leg = {"sweeps": args.mol_oracle_sweeps, "energies": en_o.tolist(), "s_per_sweep": times.tolist(),
+                      "cores": used, "kind": "port"}
+        for name, r in runs.items():
+            k = min(len(r["energies"]), args.mol_oracle_sweeps)
+            r["abs_dE_vs_oracle_per_sweep"] = [abs(r["energies"][i] - en_o[i]) for i in range(k)]
     line = {"metric": f"two-site DMRG sweep time (spin-orbital molecular Hamiltonian n={n}, D={D})",
             "unit": "ms/sweep", "higher_is_better": False, "n_gpus": 1, "steps": S, "warmup": 0,
             "data": "synthetic (seeded integrals and start state)",
             "config": {"workload": f"spin molecular n={n} (N,2Sz)=({n},0) D={D} maxiter=5 tol=1e-10 "
                                    f"integrals seed=7 start seed=42", "mpo_bond_dims_max": max(
                                        t.dim_logical[0] for t in H.tensors), "mpo_build_s": t_mpo},
-            "runs": runs}
+            "runs": runs, "oracle": oracle_leg}
     mixed = [k for k in runs if k != "fp64"]
     if "fp64" in runs and mixed:
         a = runs["fp64"]
@@ -680,6 +707,8 @@ def main():
     ap.add_argument("--mol-sweeps", type=int, default=10, help="sweeps of --mode molecular")
     ap.add_argument("--mol-precisions", default="fp64,bf16x3", help="runs of --mode molecular")
     ap.add_argument("--mol-profile", action="store_true", help="time every launch by kernel class in --mode molecular")
+    ap.add_argument("--mol-oracle-sweeps", type=int, default=0,
+                    help="sweeps of the CPU oracle from the same start state in --mode molecular (0: none)")
     ap.add_argument("--mode", default="full", choices=["full", "sweeps", "localh", "serve", "molecular", "singlesite", "complex"],
                     help="sweeps: only one device call of warmup+steps sweeps (for profiler captures), no JSON line; "
                          "localh: local-Hamiltonian microbenchmark (synthetic D=1024), its own JSON line; "
@@ -690,6 +719,8 @@ def main():
     ap.add_argument("--requests", type=int, default=128, help="requests of the --mode serve stream")
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate (1/s) of --mode serve")
     ap.add_argument("--workers", type=int, default=4, help="solver threads of --mode serve")
+    ap.add_argument("--serve-precision", default="fp64", choices=sorted(PRECISIONS),
+                    help="arithmetic of the concurrent solves of --mode serve (the serial baseline is FP64)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.mode == "sweeps":

@@ -65,6 +65,14 @@ int dmrg_singlesite(const struct mpo* hamiltonian, const int num_sweeps, const i
 	});
 }
 
+int ctgpu_set_final_fp64_sweeps(int n)
+{
+	if (n < 1) return ERR_RUNTIME;
+	const int prev = g_opts.final_fp64_sweeps;
+	g_opts.final_fp64_sweeps = n;
+	return prev;
+}
+
 int ctgpu_set_reduced_environments(int on)
 {
 	const int prev = g_opts.reduced_env ? 1 : 0;

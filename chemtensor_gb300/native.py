@@ -55,6 +55,7 @@ EXPORTS = [
     "ctgpu_inject_failure",
     "ctgpu_tridiag_lowest",
     "ctgpu_mpo_inner_product",
+    "ctgpu_set_final_fp64_sweeps",
 ]
 
 KERNEL_CLASSES = ["block_gemm", "permute", "row_map", "axis_scale", "block_svd", "block_rq", "lanczos_vector",
@@ -128,6 +129,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.ctgpu_inject_failure.argtypes = [C.c_int, C.c_int]
     lib.ctgpu_tridiag_lowest.argtypes = [P, P, C.c_int, P, P]
     lib.ctgpu_mpo_inner_product.argtypes = [P, P, P, P]
+    lib.ctgpu_set_final_fp64_sweeps.argtypes = [C.c_int]
     return lib
 
 

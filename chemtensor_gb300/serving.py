@@ -13,6 +13,10 @@ waits until the estimates of the solves in flight plus its own fit the pool's bu
 half of the device memory that is free when the pool starts). A request larger than the whole
 budget runs alone.
 
+Inputs: with `prefetch`, a producer thread builds every request's MPO and seeded start state (as the C
+structs dmrg_twosite takes) ahead of the solvers, in arrival order, so that input building does not
+sit on a solver's critical path.
+
 Request mix (the serving configuration of the two-site DMRG scope): Heisenberg with anisotropy
 Delta ~ U[0.5, 1.5] or Hubbard with U ~ U[1, 8] (t = 1, half filling), length L ~ U{8..48}, bond
 dimension D in {16, 32, 64, 128, 256}, Poisson arrivals; every parameter drawn from one seeded
@@ -128,7 +132,17 @@ def device_free_bytes(device: int) -> int:
 
 
 def build_problem(req: Request):
-    """MPO and seeded random start state of a request (host side)."""
+    """MPO and seeded random start state of a request (host side), as Python chains."""
+    cH, cP = build_problem_c(req)
+    H, psi = cs.read_mpo(cH), cs.read_mps(cP)
+    cs.free_mpo(cH)
+    cs.free_mps(cP)
+    return H, psi
+
+
+def build_problem_c(req: Request):
+    """MPO and seeded random start state of a request as the C structs dmrg_twosite takes: the start
+    state comes straight from the library's generator (no round trip through Python objects)."""
     # half filling / smallest total spin: 2 Sz = L mod 2
     sz2 = req.nsites % 2
     if req.model == "hubbard":
@@ -138,9 +152,7 @@ def build_problem(req: Request):
     else:
         H = hm.heisenberg_xxz_1d(req.nsites, 1.0, req.param, 0.0)
         c = native.random_mps(req.nsites, 2, [1, -1], sz2, req.max_vdim, req.seed)
-    psi = cs.read_mps(c)
-    cs.free_mps(c)
-    return H, psi
+    return cs.make_c_mpo(H), c
 
 
 @dataclass
@@ -157,11 +169,12 @@ class SolverPool:
     results: list = field(default_factory=list)
     admission_peak: int = 0
 
-    def _solve(self, req: Request, res: Result, lib):
-        H, psi = build_problem(req)
-        cH, cP = cs.make_c_mpo(H), cs.make_c_mps(psi)
+    prefetch: int = 0                   # problems built ahead by a producer thread (0: built by the solver)
+
+    def _solve(self, req: Request, res: Result, lib, problem=None):
+        cH, cP = problem if problem is not None else build_problem_c(req)
         en = np.zeros(self.sweeps)
-        ent = np.zeros(max(H.nsites - 1, 1))
+        ent = np.zeros(max(req.nsites - 1, 1))
         try:
             res.ret = lib.dmrg_twosite(C.byref(cH), self.sweeps, self.maxiter, self.tol, req.max_vdim, C.byref(cP),
                                        en.ctypes.data, ent.ctypes.data)
@@ -177,22 +190,39 @@ class SolverPool:
         solve = self.solve or self._solve
         budget = self.hbm_budget if self.hbm_budget is not None else device_free_bytes(self.device) // 2
         adm = Admission(budget)
-        q: queue.Queue = queue.Queue()
-        for r in sorted(requests, key=lambda r: r.arrival):
-            q.put(r)
+        ordered = sorted(requests, key=lambda r: r.arrival)
         results = {r.rid: Result(r.rid, r.arrival) for r in requests}
-        t0 = time.perf_counter()
         errors = []
+        # requests in arrival order; with prefetch, a producer thread builds each request's MPO and start
+        # state ahead of the solvers (bounded queue), so that input building leaves their critical path
+        q: queue.Queue = queue.Queue(maxsize=self.prefetch if (self.prefetch and lib is not None) else 0)
+        producer = None
+        if self.prefetch and lib is not None:
+            def produce():
+                for r in ordered:
+                    try:
+                        q.put((r, build_problem_c(r)))
+                    except Exception as e:   # the solver records it
+                        q.put((r, e))
+                for _ in range(self.workers):
+                    q.put(None)
+            producer = threading.Thread(target=produce, daemon=True)
+        else:
+            for r in ordered:
+                q.put((r, None))
+            for _ in range(self.workers):
+                q.put(None)
+        t0 = time.perf_counter()
 
         def worker(wid: int):
             if lib is not None:
                 lib.ctgpu_set_device(self.device)
                 lib.ctgpu_set_precision(self.precision)
             while True:
-                try:
-                    req = q.get_nowait()
-                except queue.Empty:
+                item = q.get()
+                if item is None:
                     return
+                req, problem = item
                 wait = req.arrival - (time.perf_counter() - t0)
                 if wait > 0:
                     time.sleep(wait)
@@ -201,7 +231,12 @@ class SolverPool:
                 take = adm.acquire(estimate_footprint(req))
                 res.start = time.perf_counter() - t0
                 try:
-                    solve(req, res, lib)
+                    if isinstance(problem, Exception):
+                        raise problem
+                    if problem is not None:
+                        solve(req, res, lib, problem)
+                    else:
+                        solve(req, res, lib)
                 except Exception as e:  # recorded, the stream goes on
                     res.ret = -99
                     res.error = str(e)
@@ -211,6 +246,8 @@ class SolverPool:
                 res.end = time.perf_counter() - t0
 
         threads = [threading.Thread(target=worker, args=(i,), daemon=True) for i in range(self.workers)]
+        if producer is not None:
+            producer.start()
         for t in threads:
             t.start()
         for t in threads:

@@ -59,6 +59,11 @@ int dmrg_singlesite(const struct mpo* hamiltonian, const int num_sweeps, const i
  * in FP64). Returns the previous value, or -5 for an unknown value (the setting is then unchanged). */
 int ctgpu_set_precision(int precision);
 
+/* Number of trailing sweeps of dmrg_twosite that run entirely in FP64 when ctgpu_set_precision
+ * selects a reduced arithmetic (default 1, at least 1). Per thread; returns the previous value, or -5
+ * for n < 1. No counterpart in the reference. */
+int ctgpu_set_final_fp64_sweeps(int n);
+
 /* With 1, the environment updates of the split-BF16 sweeps (ctgpu_set_precision(1)) also run in
  * split-BF16; with 0 (default) they stay FP64 in every sweep. The trailing FP64 sweep rebuilds
  * every environment in FP64 either way. Per thread; returns the previous value. No counterpart in
