@@ -317,9 +317,10 @@ void launch_lz_start(const double* v0, double* v, i64 n, double* partial, Lanczo
 //   1. FP32 multisection: the 32 lanes take Sturm counts at 32 points of the Gershgorin interval and
 //      keep the sub-interval where the count first reaches one (33x narrower per round), to FP32
 //      resolution;
-//   2. FP64 Newton on the last pivot d_k(x) (zero at lambda_0; its derivative follows the same
-//      recurrence), taken from the left end of the bracket that the Sturm counts maintain, where
-//      d_k is positive, decreasing and convex, with bisection as the fallback;
+//   2. FP64 Newton on the characteristic polynomial (p'/p from the same pivot recurrence), taken
+//      from the left end of the bracket that the Sturm counts maintain, where p is positive,
+//      decreasing and convex (no overshoot; about three steps from the FP32 bracket), with
+//      bisection as the fallback;
 //   3. eigenvector by a twisted factorisation (forward and backward pivots, twisted where the
 //      eigenvector is largest; robust when converged Lanczos runs leave it concentrated at one
 //      end), normalised, its largest-magnitude component made positive (deterministic sign).
@@ -339,22 +340,25 @@ __device__ __forceinline__ int sturm_count32(const float* a, const float* b2, in
 	return neg;
 }
 
-// last pivot d_k(x), its derivative, and the Sturm count, in FP64
-__device__ __forceinline__ void pivots64(const double* a, const double* b2, int k, double x, double& dk, double& ddk, int& neg)
+// Sturm count of T - x I and S = p'(x) / p(x) for the characteristic polynomial p = prod_i d_i (the
+// LDL^T pivots): S = sum_i d_i' / d_i, the derivatives following d_{i+1}' = -1 + b_i^2 d_i' / d_i^2
+__device__ __forceinline__ void pivots64(const double* a, const double* b2, int k, double x, int& neg, double& S)
 {
 	double d = a[0] - x, dd = -1.0;
+	if (fabs(d) < 1e-300) d = -1e-300;
 	neg = d < 0.0 ? 1 : 0;
+	double inv = rcp64(d);
+	S = dd * inv;
 	for (int i = 0; i + 1 < k; i++)
 	{
-		if (fabs(d) < 1e-300) d = -1e-300;
-		const double inv = rcp64(d);
 		const double t = b2[i] * inv;
-		dd = fma(t * inv, dd, -1.0);            // d'_{i+1} = -1 + b_i^2 d'_i / d_i^2
+		dd = fma(t * inv, dd, -1.0);
 		d = (a[i + 1] - x) - t;
+		if (fabs(d) < 1e-300) d = -1e-300;
 		neg += d < 0.0 ? 1 : 0;
+		inv = rcp64(d);
+		S = fma(dd, inv, S);
 	}
-	dk = d;
-	ddk = dd;
 }
 
 // Lowest eigenpair of the k x k tridiagonal (diagonal al[0..k-1], off-diagonal be[0..k-2]); called
@@ -414,45 +418,74 @@ __device__ void tridiag_lowest(const double* al, const double* be, int k, double
 	}
 	if (lane == 0)
 	{
-		// 2. FP64 Newton from the left end of the Sturm bracket [L, R] (count(L) = 0, count(R) >= 1):
-		// left of lambda_0 the last pivot d_k(x) is positive, decreasing and convex, so Newton steps
-		// from L approach lambda_0 from below; a step that passes it (or leaves the bracket) only
-		// moves R, or falls back to bisection. The bracket closes with a probe just above L.
+		// 2. FP64 Newton on the characteristic polynomial p from the left end of the Sturm bracket
+		// [L, R] (count(L) = 0, count(R) >= 1): left of its smallest root a real-rooted polynomial is
+		// positive, decreasing and convex, so Newton steps x - p / p' = x - 1 / S approach lambda_0
+		// from below without passing it (quadratically once close). A step that lands at or past the
+		// root can only be rounding, and a step below the tolerance means convergence: either ends
+		// the iteration. Bisection is the fallback (a bracket reset to the Gershgorin bounds).
 		const double gspan = (double)span;
 		double L = (double)lo, R = (double)hi;
-		double dL, ddL, dk, ddk;
+		double SL, S;
 		int neg;
-		pivots64(A, B2, k, L, dL, ddL, neg);
+		pivots64(A, B2, k, L, neg, SL);
 		if (neg != 0)
 		{
 			L = (double)glo - gspan;
-			pivots64(A, B2, k, L, dL, ddL, neg);
+			pivots64(A, B2, k, L, neg, SL);
 		}
-		pivots64(A, B2, k, R, dk, ddk, neg);
+		pivots64(A, B2, k, R, neg, S);
 		if (neg == 0) R = (double)ghi + gspan;
 		bool ok = false;
+		double x = 0.0;
 		for (int it = 0; it < 200; it++)
 		{
 			const double tol = 2.0 * DBL_EPSILON * (fmax(fabs(L), fabs(R)) + gspan);
 			if (R - L <= 2.0 * tol)
 			{
+				x = 0.5 * (L + R);
 				ok = true;
 				break;
 			}
 			const double mid = 0.5 * (L + R);
-			double xn = (ddL < 0.0 && dL > 0.0) ? L - dL * rcp64(ddL) : mid;
-			if (!(xn > L && xn < R)) xn = mid;
-			if (xn - L <= tol) xn = fmin(L + tol, mid);
-			pivots64(A, B2, k, xn, dk, ddk, neg);
+			bool newton = SL < 0.0;
+			const double step = newton ? -rcp64(SL) : 0.0;
+			if (newton && step <= tol)
+			{
+				x = L + step;
+				ok = true;
+				break;
+			}
+			double xn = newton ? L + step : mid;
+			if (!(xn > L && xn < R))
+			{
+				xn = mid;
+				newton = false;
+			}
+			const double dx = xn - L;
+			pivots64(A, B2, k, xn, neg, S);
 			if (neg == 0)
 			{
 				L = xn;
-				dL = dk;
-				ddL = ddk;
+				SL = S;
+				if (newton && dx <= tol)
+				{
+					x = xn;
+					ok = true;
+					break;
+				}
 			}
-			else R = xn;
+			else
+			{
+				R = xn;
+				if (newton)
+				{
+					x = xn;
+					ok = true;
+					break;
+				}
+			}
 		}
-		const double x = 0.5 * (L + R);
 		// 3. eigenvector by the twisted factorisation at x (robust where the eigenvector is small at
 		// either end): forward pivots d+ (in Y) and backward pivots d- (Dm), twist index r = argmin
 		// |d+_r + d-_r - (a_r - x)|; y_r = 1, y_i = -(b_i / d+_i) y_{i+1} above r, y_i = -(b_{i-1} /
