@@ -113,9 +113,12 @@ struct TcContrib {
 // holds FP32 entries (an intermediate written by a reduced-precision product), else FP64
 void launch_tc_pack(int fmt, int nrec, const TcPack* packs, int a_side, const void* src, bool src_f32, void* dst,
                     cudaStream_t st);
-// out_f32: C receives FP32 entries, else FP64
+// out_f32: C receives FP32 entries, else FP64. b_f32 (with cons): the B operand is read from this FP32
+// tensor in its own layout (the contributions' b_off / sBk / sBn) and split into parts inside the
+// kernel, so that an FP32 intermediate needs no packing pass; bpack is then unused.
 void launch_gemm_tc(int fmt, int bn, int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons,
-                    const void* apack, const void* bpack, void* C, bool out_f32, int* error, cudaStream_t st);
+                    const void* apack, const void* bpack, void* C, bool out_f32, int* error, cudaStream_t st,
+                    const GemmContrib* cons = nullptr, const float* b_f32 = nullptr);
 
 // ---- data movement -----------------------------------------------------------
 // Generic per-block permutation: dst block (row-major over dims) gathers
@@ -247,7 +250,9 @@ struct LanczosScalars {
 	int pad;
 };
 
-constexpr int RED_BLOCKS = 608;     // 4 x 152 SMs: fixed grid for deterministic reductions
+// fixed grid of the cooperative Lanczos kernels (deterministic reductions): one block of 512 threads
+// per SM, so that each grid barrier has 152 participants and each block sums 152 partials
+constexpr int RED_BLOCKS = 152;
 
 // one cooperative launch each (partial: 2 RED_BLOCKS doubles): a whole Lanczos step
 // (alpha; unless last: orthogonalisation, beta and the early exit, next vector), and the start

@@ -175,7 +175,7 @@ void launch_rq_householder(int nblocks, const RqDesc* descs, const double* a, do
 // reproducible run to run.
 // ------------------------------------------------------------------------------------
 
-constexpr int RED_THREADS = 256;
+constexpr int RED_THREADS = 512;
 
 __device__ void block_partial(double v, double* partial)
 {
@@ -208,7 +208,7 @@ __device__ double final_sum(const double* partial)
 // w -= alpha_j v_j + beta_{j-1} v_{j-1}, beta_j = ||w|| with the early-exit test, v_{j+1} = w / beta_j.
 // Every block forms the scalar reductions itself from the fixed-order partial sums, so no block
 // waits for another except at the two grid barriers. `partial` holds 2 RED_BLOCKS doubles.
-__global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
+__global__ void __launch_bounds__(RED_THREADS, 1)
 k_lz_step(double* __restrict__ w, const double* __restrict__ vj, const double* __restrict__ vjm1,
           double* __restrict__ vj1, i64 n, i64 nthr, int j, int last, double* __restrict__ partial, LanczosScalars* sc)
 {
@@ -250,7 +250,7 @@ k_lz_step(double* __restrict__ w, const double* __restrict__ vj, const double* _
 }
 
 // Normalisation of the start vector in one cooperative launch.
-__global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
+__global__ void __launch_bounds__(RED_THREADS, 1)
 k_lz_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, double* __restrict__ partial, LanczosScalars* sc)
 {
 	cg::grid_group grid = cg::this_grid();
@@ -275,7 +275,7 @@ k_lz_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, double*
 	for (i64 i = (i64)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += stride) v[i] = inv * v0[i];
 }
 
-__global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
+__global__ void __launch_bounds__(RED_THREADS, 1)
 k_lz_finish(const double* __restrict__ w, const double* __restrict__ V, i64 n, int maxiter, double* __restrict__ partial,
             LanczosScalars* sc, double* __restrict__ out);
 
@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(32) k_tridiag_test(const double* al, const dou
 // copies in every block would queue on the same SM sub-partitions) and stores lambda, y and the
 // status; after a second grid barrier every block writes its share of the Ritz vector out = V y.
 // With no iteration at all (a start vector of norm zero) the status is -1 and out is zero.
-__global__ void __launch_bounds__(RED_THREADS, RED_BLOCKS / 152)
+__global__ void __launch_bounds__(RED_THREADS, 1)
 k_lz_finish(const double* __restrict__ w, const double* __restrict__ V, i64 n, int maxiter, double* __restrict__ partial,
             LanczosScalars* sc, double* __restrict__ out)
 {
