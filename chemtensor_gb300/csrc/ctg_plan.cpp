@@ -328,10 +328,11 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			whole.sp = 0;
 			if (is_tc_precision(precision))
 			{
-				// tensor-core tiles: one tile class, tc_bn columns wide
+				// tensor-core tiles: one tile class, tc_bn columns wide; the row tiles of one column range
+				// are consecutive, so that the CTAs running them side by side share its B operand in L2
 				R.flops_cls[0] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
-				for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
-					for (int n0 = 0; n0 < o.n; n0 += tc_bn)
+				for (int n0 = 0; n0 < o.n; n0 += tc_bn)
+					for (int m0 = 0; m0 < o.m; m0 += tc_tile_rows())
 					{
 						whole.m0 = m0;
 						whole.n0 = n0;
