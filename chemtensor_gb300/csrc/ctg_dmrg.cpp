@@ -458,17 +458,16 @@ struct LocalH {
 			pk_x = rec(d1.a_rec_bytes());
 			d1.pack_b(c, r.data(), pk_r->ptr);
 		}
-		// a B operand that is an FP32 intermediate is split inside the GEMM (no records, no packing)
 		if (tc2)
 		{
 			pk_w = rec(d2.a_rec_bytes());
-			if (!f1) pk_t1 = rec(d2.b_rec_bytes());
+			pk_t1 = rec(d2.b_rec_bytes());
 			d2.pack_a(c, w.data(), pk_w->ptr);
 		}
 		if (tc3)
 		{
 			pk_k = rec(d3.a_rec_bytes());
-			if (!f2) pk_t2 = rec(d3.b_rec_bytes());
+			pk_t2 = rec(d3.b_rec_bytes());
 			d3.pack_a(c, k.data(), pk_k->ptr);
 		}
 	}
@@ -493,23 +492,15 @@ struct LocalH {
 		else d1.run(c, x, r.data(), t1);
 		if (tc2)
 		{
-			if (f1) d2.run_f32b(c, pk_w->ptr, (const float*)(void*)t1, t2, f2);
-			else
-			{
-				d2.pack_b(c, t1, pk_t1->ptr, false);
-				d2.run_packed(c, pk_w->ptr, pk_t1->ptr, t2, f2);
-			}
+			d2.pack_b(c, t1, pk_t1->ptr, f1);
+			d2.run_packed(c, pk_w->ptr, pk_t1->ptr, t2, f2);
 			c.gemm_flops += d2.flops;
 		}
 		else d2.run(c, w.data(), t1, t2);
 		if (tc3)
 		{
-			if (f2) d3.run_f32b(c, pk_k->ptr, (const float*)(void*)t2, y, false);
-			else
-			{
-				d3.pack_b(c, t2, pk_t2->ptr, false);
-				d3.run_packed(c, pk_k->ptr, pk_t2->ptr, y);
-			}
+			d3.pack_b(c, t2, pk_t2->ptr, f2);
+			d3.run_packed(c, pk_k->ptr, pk_t2->ptr, y);
 			c.gemm_flops += d3.flops;
 		}
 		else d3.run(c, k.data(), t2, y);

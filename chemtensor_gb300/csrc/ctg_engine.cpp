@@ -541,16 +541,6 @@ void DotPlan::pack_b(Ctx& c, const void* B, void* bpack, bool src_f32) const
 	launch_tc_pack(tc_fmt, (int)b_recs, bpacks, 0, B, src_f32, bpack, c.stream());
 }
 
-void DotPlan::run_f32b(Ctx& c, const void* apack, const float* B, void* C, bool out_f32) const
-{
-	if (ntiles[0] > 0)
-	{
-		KScope ks(c, K_GEMM_TC, 1, flops_cls[0], 0);
-		launch_gemm_tc(tc_fmt, tc_bn, ntiles[0], tiles[0], outs, tcons, apack, nullptr, C, out_f32, c.tc_error(), c.stream(),
-		               cons, B);
-	}
-}
-
 void DotPlan::run_packed(Ctx& c, const void* apack, const void* bpack, void* C, bool out_f32) const
 {
 	if (ntiles[0] > 0)

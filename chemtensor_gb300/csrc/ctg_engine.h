@@ -194,8 +194,6 @@ struct DotPlan {
 	void pack_b(Ctx& c, const void* B, void* bpack, bool src_f32 = false) const;
 	// out_f32: C receives FP32 entries
 	void run_packed(Ctx& c, const void* apack, const void* bpack, void* C, bool out_f32 = false) const;
-	// packed A, B read as FP32 in its own layout and split inside the GEMM (no B packing pass)
-	void run_f32b(Ctx& c, const void* apack, const float* B, void* C, bool out_f32 = false) const;
 };
 // out_perm (every precision): the result is written straight in the layout of its transpose by out_perm
 // (see lower_dot), and the plan's `out` is that transposed structure

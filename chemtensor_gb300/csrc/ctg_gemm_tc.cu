@@ -42,8 +42,6 @@ namespace {
 
 constexpr int TC_BM = 128;                 // tile rows (MMA M)
 constexpr int TC_THREADS = 192;            // copy warp, MMA warp, 4 epilogue warps
-constexpr int TC_CONV_WARPS = 4;           // with a B operand converted in the kernel (see k_gemm_tc)
-constexpr int TC_THREADS_CONV = TC_THREADS + 32 * TC_CONV_WARPS;
 constexpr int TC_ACC_BUFS = 2;
 // canonical no-swizzle K-major layout of one part: 8-row x 16-byte core matrices;
 // (row, byte b of the 64-byte k chunk) -> (row / 8) * SBO + (b / 16) * LBO + (row % 8) * 16 + b % 16
@@ -224,38 +222,6 @@ __device__ __forceinline__ uint32_t tf32_bits(float f)
 	return r;
 }
 
-// The parts of 16 / ELEM consecutive k values of one row (a 16-byte core-matrix row segment per
-// part): TF32 rounding, or successive BF16 roundings of what the parts before left over (exact in
-// FP32). w[q] is part q's segment.
-template <int FMT>
-__device__ __forceinline__ void split_segment(const float* f, uint4* w)
-{
-	using F = Fmt<FMT>;
-	if constexpr (FMT == TC_TF32)
-	{
-		w[0] = make_uint4(tf32_bits(f[0]), tf32_bits(f[1]), tf32_bits(f[2]), tf32_bits(f[3]));
-	}
-	else
-	{
-		uint32_t v[F::PARTS][4];
-#pragma unroll
-		for (int t = 0; t < 8; t += 2)
-		{
-			float r0 = f[t], r1 = f[t + 1];
-#pragma unroll
-			for (int q = 0; q < F::PARTS; q++)
-			{
-				const uint32_t b0 = bf16_bits(r0), b1 = bf16_bits(r1);
-				v[q][t / 2] = b0 | (b1 << 16);
-				r0 -= bf16_val(b0);
-				r1 -= bf16_val(b1);
-			}
-		}
-#pragma unroll
-		for (int q = 0; q < F::PARTS; q++) w[q] = make_uint4(v[q][0], v[q][1], v[q][2], v[q][3]);
-	}
-}
-
 // One CTA per record. A thread converts one 16-byte core-matrix row segment of every part: 16 / ELEM
 // consecutive k of one row (read from the FP64 or FP32 operand, strided by s_k); consecutive
 // threads take consecutive rows, so that 8 threads fill one 128-byte run of a part.
@@ -283,10 +249,30 @@ __global__ void __launch_bounds__(128) k_tc_pack(const TcPack* __restrict__ pack
 			f[t] = (gi < p.rows && gk < p.k) ? (float)rowp[(i64)gk * p.s_k] : 0.0f;
 		}
 		const uint32_t so = canon_offset(i, seg * 16);
-		uint4 w[F::PARTS];
-		split_segment<FMT>(f, w);
+		if constexpr (FMT == TC_TF32)
+		{
+			*(uint4*)(rec + so) = make_uint4(tf32_bits(f[0]), tf32_bits(f[1]), tf32_bits(f[2]), tf32_bits(f[3]));
+		}
+		else
+		{
+			uint32_t w[F::PARTS][4];
 #pragma unroll
-		for (int q = 0; q < F::PARTS; q++) *(uint4*)(rec + q * PART + so) = w[q];
+			for (int t = 0; t < PER; t += 2)
+			{
+				float r0 = f[t], r1 = f[t + 1];
+#pragma unroll
+				for (int q = 0; q < F::PARTS; q++)
+				{
+					// each part is the BF16 rounding of what the parts before it left over (exact in FP32)
+					const uint32_t b0 = bf16_bits(r0), b1 = bf16_bits(r1);
+					w[q][t / 2] = b0 | (b1 << 16);
+					r0 -= bf16_val(b0);
+					r1 -= bf16_val(b1);
+				}
+			}
+#pragma unroll
+			for (int q = 0; q < F::PARTS; q++) *(uint4*)(rec + q * PART + so) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+		}
 	}
 }
 
@@ -297,16 +283,11 @@ __device__ __forceinline__ int tile_chunks(const GemmOut& o, const TcContrib* tc
 	return n;
 }
 
-// BF32: the B operand is an FP32 tensor in its own layout (bsrc, element (k, j) of a contribution at
-// cons[c].b_off + k sBk + j sBn) rather than packed records; four more warps (6-9) convert each k
-// chunk of the tile's B columns into the stage's parts (coalesced along j), fence the writes for the
-// tensor cores' proxy and arrive on the stage's "full" barrier beside the copy warp's A record.
-template <int FMT, int BN, class OUT, bool BF32>
-__global__ void __launch_bounds__(TC_THREADS_CONV, 1)
+template <int FMT, int BN, class OUT>
+__global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
           const TcContrib* __restrict__ tcons, const unsigned char* __restrict__ apack,
-          const unsigned char* __restrict__ bpack, OUT* __restrict__ C, int* __restrict__ error, long long wait_limit,
-          const GemmContrib* __restrict__ cons, const float* __restrict__ bsrc)
+          const unsigned char* __restrict__ bpack, OUT* __restrict__ C, int* __restrict__ error, long long wait_limit)
 {
 	using F = Fmt<FMT>;
 	using G = Cfg<FMT, BN>;
@@ -333,7 +314,7 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 	{
 		for (int st = 0; st < NST; st++)
 		{
-			mbar_init(smem_u32(full + st), BF32 ? 1 + TC_CONV_WARPS : 1);
+			mbar_init(smem_u32(full + st), 1);
 			mbar_init(smem_u32(empty + st), 1);
 		}
 		for (int b = 0; b < TC_ACC_BUFS; b++)
@@ -375,23 +356,20 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 						const uint32_t sa = smem_u32(smem + st * G::STAGE_BYTES);
 						const uint32_t sb = sa + (uint32_t)G::A_BYTES;
 						const uint32_t bar = smem_u32(full + st);
-						mbar_expect_tx(bar, (uint32_t)(BF32 ? G::A_BYTES : G::STAGE_BYTES));
+						mbar_expect_tx(bar, (uint32_t)G::STAGE_BYTES);
 						// an A record holds its parts back to back, as the stage does
 						bulk_copy(sa, apack + (gc.a_rec + (i64)mt * gc.kt + lk) * G::A_BYTES, (uint32_t)G::A_BYTES, bar);
 						// B: the SUB consecutive 64-row records of the tile's columns, part by part, so that each
-						// part holds BN rows in one canonical layout (or, BF32, the converter warps' work)
-						if constexpr (!BF32)
+						// part holds BN rows in one canonical layout
+#pragma unroll
+						for (int s = 0; s < SUB; s++)
 						{
+							const unsigned char* brec =
+							    bpack + (gc.b_rec + (i64)(nt * SUB + s) * gc.kt + lk) * (i64)(F::PARTS * B_PART_BYTES);
 #pragma unroll
-							for (int s = 0; s < SUB; s++)
-							{
-								const unsigned char* brec =
-								    bpack + (gc.b_rec + (i64)(nt * SUB + s) * gc.kt + lk) * (i64)(F::PARTS * B_PART_BYTES);
-#pragma unroll
-								for (int q = 0; q < F::PARTS; q++)
-									bulk_copy(sb + (uint32_t)(q * BN * TC_KB + s * B_PART_BYTES), brec + q * B_PART_BYTES,
-									          (uint32_t)B_PART_BYTES, bar);
-							}
+							for (int q = 0; q < F::PARTS; q++)
+								bulk_copy(sb + (uint32_t)(q * BN * TC_KB + s * B_PART_BYTES), brec + q * B_PART_BYTES,
+								          (uint32_t)B_PART_BYTES, bar);
 						}
 					}
 				}
@@ -405,66 +383,6 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 			// (always with the default limit: a lowered limit only shortens the pipeline's waits)
 			for (long long u = g - NST; u < g; u++)
 				if (u >= 0) mbar_wait(smem_u32(full + (int)(u % NST)), (uint32_t)((u / NST) & 1), TC_WAIT_LIMIT_DEFAULT);
-		}
-	}
-	else if (BF32 && warp >= 6)
-	{
-		// converter warps: the same k-chunk sequence as the copy warp; each thread turns 16-byte row
-		// segments of the tile's B columns (row = column j of the block, 16 / ELEM consecutive k) into
-		// the stage's parts. Consecutive threads take consecutive j: the FP32 loads are coalesced when
-		// the block's columns are contiguous.
-		constexpr int PER = 16 / F::ELEM;
-		constexpr int KC = TC_KB / F::ELEM;
-		constexpr int UNITS = BN * (TC_KB / 16);
-		const int ct = tid - 192;                       // 0 .. 127
-		long long g = 0;
-		bool ok = true;
-		for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x)
-		{
-			const GemmTile tile = tiles[ti];
-			const GemmOut o = outs[tile.out];
-			for (int c = o.c0; c < o.c0 + o.nc && ok; c++)
-			{
-				const GemmContrib gb = cons[c];
-				const int kt = tcons[c].kt;
-				for (int lk = 0; lk < kt; lk++, g++)
-				{
-					const int st = (int)(g % NST);
-					// warp-uniform: every lane waits for the same phase
-					if (g >= NST &&
-					    !__all_sync(0xffffffffu, mbar_wait(smem_u32(empty + st), (uint32_t)(((g / NST) - 1) & 1), wait_limit, abort)))
-					{
-						ok = false;
-						break;
-					}
-					unsigned char* sbp = smem + st * G::STAGE_BYTES + G::A_BYTES;
-					for (int u = ct; u < UNITS; u += 32 * TC_CONV_WARPS)
-					{
-						const int row = u % BN, seg = u / BN;
-						const int j = tile.n0 + row;
-						const int k0 = lk * KC + seg * PER;
-						float f[PER];
-						const float* colp = bsrc + gb.b_off + (i64)j * gb.sBn;
-#pragma unroll
-						for (int t = 0; t < PER; t++)
-							f[t] = (j < o.n && k0 + t < gb.k) ? __ldg(colp + (i64)(k0 + t) * gb.sBk) : 0.0f;
-						uint4 w[F::PARTS];
-						split_segment<FMT>(f, w);
-						const uint32_t so = canon_offset(row, seg * 16);
-#pragma unroll
-						for (int q = 0; q < F::PARTS; q++) *(uint4*)(sbp + q * BN * TC_KB + so) = w[q];
-					}
-					// the tensor cores read shared memory through the async proxy
-					asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-					__syncwarp();
-					if (lane == 0) mbar_arrive(smem_u32(full + st));
-				}
-			}
-		}
-		if (!ok && lane == 0)
-		{
-			*abort = 1;
-			atomicExch(error, 1);
 		}
 	}
 	else if (warp == 1)
@@ -626,42 +544,31 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 int g_num_sms = 0;
 long long g_wait_limit = TC_WAIT_LIMIT_DEFAULT;
 
-template <int FMT, int BN, class OUT, bool BF32>
+template <int FMT, int BN, class OUT>
 void launch_gemm_t(int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons, const void* apack,
-                   const void* bpack, OUT* C, int* error, const GemmContrib* cons, const float* bsrc, cudaStream_t st)
+                   const void* bpack, OUT* C, int* error, cudaStream_t st)
 {
 	using G = Cfg<FMT, BN>;
 	static std::once_flag attr_once;
 	std::call_once(attr_once, [] {
-		CTG_CUDA(cudaFuncSetAttribute(k_gemm_tc<FMT, BN, OUT, BF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
+		CTG_CUDA(cudaFuncSetAttribute(k_gemm_tc<FMT, BN, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
 	});
 	// persistent: one CTA per SM (the shared-memory ring admits one), each walking every gridDim-th tile
 	const int grid = std::min(ntiles, std::max(g_num_sms, 1));
-	k_gemm_tc<FMT, BN, OUT, BF32><<<grid, BF32 ? TC_THREADS_CONV : TC_THREADS, G::SMEM, st>>>(
-	    ntiles, tiles, outs, tcons, (const unsigned char*)apack, (const unsigned char*)bpack, C, error, g_wait_limit, cons,
-	    bsrc);
+	k_gemm_tc<FMT, BN, OUT><<<grid, TC_THREADS, G::SMEM, st>>>(ntiles, tiles, outs, tcons, (const unsigned char*)apack,
+	                                                          (const unsigned char*)bpack, C, error, g_wait_limit);
 	CTG_CUDA(cudaGetLastError());
 }
 
 template <int FMT, class OUT>
 void launch_gemm_f(int bn, int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons, const void* apack,
-                   const void* bpack, OUT* C, int* error, const GemmContrib* cons, const float* bsrc, cudaStream_t st)
+                   const void* bpack, OUT* C, int* error, cudaStream_t st)
 {
-	const bool f = bsrc != nullptr;
 	switch (bn)
 	{
-	case 64:
-		if (f) launch_gemm_t<FMT, 64, OUT, true>(ntiles, tiles, outs, tcons, apack, bpack, C, error, cons, bsrc, st);
-		else launch_gemm_t<FMT, 64, OUT, false>(ntiles, tiles, outs, tcons, apack, bpack, C, error, cons, bsrc, st);
-		break;
-	case 128:
-		if (f) launch_gemm_t<FMT, 128, OUT, true>(ntiles, tiles, outs, tcons, apack, bpack, C, error, cons, bsrc, st);
-		else launch_gemm_t<FMT, 128, OUT, false>(ntiles, tiles, outs, tcons, apack, bpack, C, error, cons, bsrc, st);
-		break;
-	case 256:
-		if (f) launch_gemm_t<FMT, 256, OUT, true>(ntiles, tiles, outs, tcons, apack, bpack, C, error, cons, bsrc, st);
-		else launch_gemm_t<FMT, 256, OUT, false>(ntiles, tiles, outs, tcons, apack, bpack, C, error, cons, bsrc, st);
-		break;
+	case 64: launch_gemm_t<FMT, 64, OUT>(ntiles, tiles, outs, tcons, apack, bpack, C, error, st); break;
+	case 128: launch_gemm_t<FMT, 128, OUT>(ntiles, tiles, outs, tcons, apack, bpack, C, error, st); break;
+	case 256: launch_gemm_t<FMT, 256, OUT>(ntiles, tiles, outs, tcons, apack, bpack, C, error, st); break;
 	default: CTG_CHECK(false, "tensor-core GEMM: unsupported tile width");
 	}
 }
@@ -717,11 +624,9 @@ void launch_tc_pack(int fmt, int nrec, const TcPack* packs, int a_side, const vo
 }
 
 void launch_gemm_tc(int fmt, int bn, int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons,
-                    const void* apack, const void* bpack, void* C, bool out_f32, int* error, cudaStream_t st,
-                    const GemmContrib* cons, const float* b_f32)
+                    const void* apack, const void* bpack, void* C, bool out_f32, int* error, cudaStream_t st)
 {
 	if (ntiles <= 0) return;
-	CTG_CHECK(!b_f32 || cons, "tensor-core GEMM: an FP32 B operand needs the contribution descriptors");
 	static std::once_flag sms_once;
 	std::call_once(sms_once, [] {
 		int dev = 0;
@@ -731,16 +636,16 @@ void launch_gemm_tc(int fmt, int bn, int ntiles, const GemmTile* tiles, const Ge
 	if (out_f32)
 	{
 		float* c = (float*)C;
-		if (fmt == TC_BF16X3) launch_gemm_f<TC_BF16X3>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, cons, b_f32, st);
-		else if (fmt == TC_BF16X6) launch_gemm_f<TC_BF16X6>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, cons, b_f32, st);
-		else launch_gemm_f<TC_TF32>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, cons, b_f32, st);
+		if (fmt == TC_BF16X3) launch_gemm_f<TC_BF16X3>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, st);
+		else if (fmt == TC_BF16X6) launch_gemm_f<TC_BF16X6>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, st);
+		else launch_gemm_f<TC_TF32>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, st);
 	}
 	else
 	{
 		double* c = (double*)C;
-		if (fmt == TC_BF16X3) launch_gemm_f<TC_BF16X3>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, cons, b_f32, st);
-		else if (fmt == TC_BF16X6) launch_gemm_f<TC_BF16X6>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, cons, b_f32, st);
-		else launch_gemm_f<TC_TF32>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, cons, b_f32, st);
+		if (fmt == TC_BF16X3) launch_gemm_f<TC_BF16X3>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, st);
+		else if (fmt == TC_BF16X6) launch_gemm_f<TC_BF16X6>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, st);
+		else launch_gemm_f<TC_TF32>(bn, ntiles, tiles, outs, tcons, apack, bpack, c, error, st);
 	}
 }
 

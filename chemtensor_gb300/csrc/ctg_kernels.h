@@ -113,12 +113,9 @@ struct TcContrib {
 // holds FP32 entries (an intermediate written by a reduced-precision product), else FP64
 void launch_tc_pack(int fmt, int nrec, const TcPack* packs, int a_side, const void* src, bool src_f32, void* dst,
                     cudaStream_t st);
-// out_f32: C receives FP32 entries, else FP64. b_f32 (with cons): the B operand is read from this FP32
-// tensor in its own layout (the contributions' b_off / sBk / sBn) and split into parts inside the
-// kernel, so that an FP32 intermediate needs no packing pass; bpack is then unused.
+// out_f32: C receives FP32 entries, else FP64
 void launch_gemm_tc(int fmt, int bn, int ntiles, const GemmTile* tiles, const GemmOut* outs, const TcContrib* tcons,
-                    const void* apack, const void* bpack, void* C, bool out_f32, int* error, cudaStream_t st,
-                    const GemmContrib* cons = nullptr, const float* b_f32 = nullptr);
+                    const void* apack, const void* bpack, void* C, bool out_f32, int* error, cudaStream_t st);
 
 // ---- data movement -----------------------------------------------------------
 // Generic per-block permutation: dst block (row-major over dims) gathers
