@@ -35,6 +35,23 @@ def test_concurrent_solves_match_serial():
     assert len({r.worker for r in conc}) > 1
 
 
+@pytest.mark.gpu
+def test_concurrent_mixed_precision_solves_match_serial():
+    """Reduced-precision solves (split-BF16 matvecs where the autotuner puts them on the tensor cores,
+    final sweep FP64) give the same energy alone and in the mix: every kernel is deterministic and
+    the autotuner's picks are process-wide, so solves running side by side take the same paths."""
+    from chemtensor_gb300 import native
+    reqs = [r for r in serving.generate_requests(60, 0.0, seed=13) if r.max_vdim <= 64 and r.nsites <= 24][:6]
+    assert len(reqs) >= 3
+    p = native.PRECISION_BF16X3
+    serial = serving.SolverPool(workers=1, sweeps=2, precision=p).run(reqs)
+    conc = serving.SolverPool(workers=3, sweeps=2, precision=p, prefetch=4).run(reqs)
+    assert all(r.ret == 0 for r in serial + conc), [r.error for r in serial + conc]
+    for a, b in zip(serial, conc):
+        assert a.energy == b.energy
+    assert len({r.worker for r in conc}) > 1
+
+
 def test_admission_keeps_solves_in_flight_within_the_budget():
     """Host logic of admission by estimated HBM footprint: a fake solve records how many bytes were
     admitted while it ran; the total never exceeds the budget, and a request larger than the whole
