@@ -21,9 +21,10 @@
 // stages (bulk copies completing on the stage's "full" mbarrier); warp 1 (one lane) issues the
 // tcgen05.mma instructions of each chunk into FP32 accumulators in tensor memory and commits them
 // to the stage's "empty" mbarrier, which hands the stage back to the copy warp; the accumulator of
-// a tile alternates between two tensor-memory buffers, so that warps 2-5 (one per 32-lane quarter
-// of tensor memory) drain tile i with tcgen05.ld while the MMAs of tile i + 1 run. Each epilogue
-// warp stages its 32 rows x 32 columns in its own shared memory and writes them row by row,
+// a tile alternates between two tensor-memory buffers, so that warps 2-9 (two per 32-lane quarter
+// of tensor memory, each half of the columns) drain tile i with tcgen05.ld while the MMAs of tile
+// i + 1 run. Each epilogue warp stages 32 rows x 32 columns at a time in its own shared memory and
+// writes them row by row,
 // coalesced, into the output block's layout (plain, or that of a transposed result, see GemmOut);
 // warps whose rows lie outside the block skip the drain. Every wait is bounded and also ends when
 // another warp has recorded a failure: the CTA then records the error flag, lets its copies in
@@ -41,7 +42,8 @@ namespace ctg {
 namespace {
 
 constexpr int TC_BM = 128;                 // tile rows (MMA M)
-constexpr int TC_THREADS = 192;            // copy warp, MMA warp, 4 epilogue warps
+constexpr int TC_EPI_WARPS = 8;            // two per 32-lane quarter of tensor memory, each half the columns
+constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;   // copy warp, MMA warp, epilogue warps
 constexpr int TC_ACC_BUFS = 2;
 // canonical no-swizzle K-major layout of one part: 8-row x 16-byte core matrices;
 // (row, byte b of the 64-byte k chunk) -> (row / 8) * SBO + (b / 16) * LBO + (row % 8) * 16 + b % 16
@@ -50,7 +52,7 @@ constexpr int TC_SBO = (TC_KB / 16) * 128; // bytes between core matrices adjace
 constexpr int A_PART_BYTES = TC_A_ROWS * TC_KB;      // 8 KiB
 constexpr int B_PART_BYTES = TC_B_ROWS * TC_KB;      // 4 KiB
 constexpr int TC_EPI_LD = 33;                        // padded FP32 staging row (32 columns)
-constexpr int TC_EPI_BYTES = 4 * 32 * TC_EPI_LD * 4; // one 32 x 32 staging tile per epilogue warp
+constexpr int TC_EPI_BYTES = TC_EPI_WARPS * 32 * TC_EPI_LD * 4; // one 32 x 32 staging tile per epilogue warp
 constexpr int TC_SMEM_MAX = 227 * 1024;
 constexpr int TC_BAR_BYTES = 8 * (2 * 8 + 2 * TC_ACC_BUFS) + 16;
 static_assert(TC_A_ROWS == TC_BM, "tile shape");
@@ -320,7 +322,7 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 		for (int b = 0; b < TC_ACC_BUFS; b++)
 		{
 			mbar_init(smem_u32(acc_full + b), 1);
-			mbar_init(smem_u32(acc_empty + b), 4);      // one arrival per epilogue warp
+			mbar_init(smem_u32(acc_empty + b), TC_EPI_WARPS);      // one arrival per epilogue warp
 		}
 		*abort = 0;
 	}
@@ -454,9 +456,12 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 	else
 	{
 		// epilogue warps: tensor-memory quarter q holds accumulator rows 32 q .. 32 q + 31; lane l of
-		// the warp holds row 32 q + l. Each warp drains, stages and writes its own rows.
+		// the warp holds row 32 q + l (a warp may only read the lane quarter warp % 4). Two warps per
+		// quarter, each draining, staging and writing half of the tile's columns of its rows.
 		const int q = warp & 3;
-		float* sw = stile + q * 32 * TC_EPI_LD;
+		const int half = (warp - 2) / 4;
+		constexpr int HALF = BN / 2;
+		float* sw = stile + (warp - 2) * 32 * TC_EPI_LD;
 		int acc = 0;
 		for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
 		{
@@ -467,6 +472,7 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 			const i64 ro = i < o.m ? o.c_off + (i64)(i / o.r1) * o.sr0 + (i64)(i % o.r1) * o.sr1 : -1;
 			const int rows = min(32, o.m - tile.m0 - q * 32);      // rows of this warp inside the block
 			const int cols = min(BN, o.n - tile.n0);
+			const int c_lo = half * HALF, c_hi = min(cols, c_lo + HALF);
 			bool ok = true;
 			if (nch > 0)
 			{
@@ -477,7 +483,7 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 				if (ok)
 				{
 					tc_fence_after();
-					for (int cc = 0; cc < cols && rows > 0; cc += 32)
+					for (int cc = c_lo; cc < c_hi && rows > 0; cc += 32)
 					{
 						uint32_t v[32];
 						const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + cc);
@@ -496,7 +502,7 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 						__syncwarp();
 						// row by row: lane = column, coalesced within the output block's rows
 						const int j = tile.n0 + cc + lane;
-						const i64 co = (cc + lane < cols) ? (i64)(j / o.c1) * o.sc0 + (j % o.c1) : -1;
+						const i64 co = (cc + lane < c_hi) ? (i64)(j / o.c1) * o.sc0 + (j % o.c1) : -1;
 						for (int r = 0; r < rows; r++)
 						{
 							const i64 rr = __shfl_sync(0xffffffffu, ro, r);
@@ -513,10 +519,10 @@ k_gemm_tc(int ntiles, const GemmTile* __restrict__ tiles, const GemmOut* __restr
 			else
 			{
 				// no contribution: the tile is zero
-				for (int cc = 0; cc < cols && rows > 0; cc += 32)
+				for (int cc = c_lo; cc < c_hi && rows > 0; cc += 32)
 				{
 					const int j = tile.n0 + cc + lane;
-					const i64 co = (cc + lane < cols) ? (i64)(j / o.c1) * o.sc0 + (j % o.c1) : -1;
+					const i64 co = (cc + lane < c_hi) ? (i64)(j / o.c1) * o.sc0 + (j % o.c1) : -1;
 					for (int r = 0; r < rows; r++)
 					{
 						const i64 rr = __shfl_sync(0xffffffffu, ro, r);
