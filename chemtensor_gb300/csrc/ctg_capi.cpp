@@ -5,12 +5,33 @@
 #include <cmath>
 #include <string>
 
+#include <csignal>
+#include <execinfo.h>
+#include <unistd.h>
+
 #include <cuda_runtime.h>
 
 #include "ctgpu.h"
 #include "ctg_dmrg.h"
 
 namespace {
+
+// opt-in diagnostics: with CTGPU_SEGV_TRACE set, a segmentation fault in the calling process prints
+// the native call stack (symbols of the exported functions) to stderr before the default action
+void segv_trace(int sig)
+{
+	void* frames[64];
+	const int n = backtrace(frames, 64);
+	static const char head[] = "ctgpu: native stack at the fault:\n";
+	if (write(2, head, sizeof head - 1) < 0) {}
+	backtrace_symbols_fd(frames, n, 2);
+	signal(sig, SIG_DFL);
+	raise(sig);
+}
+const bool g_segv_trace_installed = [] {
+	if (std::getenv("CTGPU_SEGV_TRACE")) signal(SIGSEGV, segv_trace);
+	return true;
+}();
 
 thread_local std::string g_last_error;
 thread_local ctg::DmrgOptions g_opts = [] {

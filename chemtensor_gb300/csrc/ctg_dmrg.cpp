@@ -353,7 +353,9 @@ int split_mps_svd(Ctx& c, const DTensor& a, i64 d, const std::vector<q32>& qsite
 	DTensor am = op_flatten(c, tmp, 1, TENSOR_AXIS_IN);
 	SvdResult sv;
 	SvdPending pend;
-	int ret = op_svd_launch(c, am, sv, pend);
+	// relative truncation: the discarded squares sum to at most tol ||a||_F^2; a is the normalised
+	// Lanczos solution, so tol / 2 is a safe lower bound of that budget
+	int ret = op_svd_launch(c, am, sv, pend, tol > 0 ? 0.5 * tol : 0.0);
 	if (ret < 0) return ret;
 	// the one host synchronisation of a bond step: the truncation needs the singular values
 	double* sigma = c.pinned_doubles((size_t)sv.ns);

@@ -332,6 +332,7 @@ KScope::~KScope()
 
 DBufPtr Ctx::upload(const void* host, size_t bytes)
 {
+	CTG_CHECK(host != nullptr || bytes == 0, "upload from a null host pointer");
 	struct T { Ctx* c; double t0; ~T() { c->host_upload_s += host_seconds() - t0; } } timer{this, host_seconds()};
 	auto b = std::make_shared<DBuf>(this, bytes);
 	size_t done = 0;
@@ -468,7 +469,9 @@ static DotPlan upload_dot_plan(Ctx& c, DotLowering&& l, int precision, int bn)
 	const size_t o_splits = pk.add(l.splits);
 	const size_t o_tcons = pk.add(l.tcons), o_apacks = pk.add(l.apacks), o_bpacks = pk.add(l.bpacks);
 	const size_t o_zt = pk.add(zt);
-	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	// at least 16 bytes, from the packer's own storage (a product without output blocks packs nothing)
+	if (pk.bytes.size() < 16) pk.bytes.resize(16);
+	p.desc = c.upload(pk.bytes.data(), pk.bytes.size());
 	p.nztiles = (int)zt.size();
 	p.ztiles = at<ZTile>(p.desc, o_zt);
 	p.tcons = at<TcContrib>(p.desc, o_tcons);
@@ -790,7 +793,8 @@ static CopyPlan upload_copy(Ctx& c, CopyLowering&& l)
 	else if (l.kind == 1) od = pk.add(l.rows);
 	else od = pk.add(l.scale);
 	const size_t oc = pk.add(l.chunks), om = pk.add(l.maps);
-	p.desc = c.upload(pk.bytes.data(), std::max<size_t>(pk.bytes.size(), 16));
+	if (pk.bytes.size() < 16) pk.bytes.resize(16);
+	p.desc = c.upload(pk.bytes.data(), pk.bytes.size());
 	p.descs = (const char*)p.desc->ptr + od;
 	p.chunks = at<Chunk>(p.desc, oc);
 	p.maps = at<i64>(p.desc, om);
@@ -1018,7 +1022,7 @@ DTensor view_trace_unit(const DTensor& t)
 // SVD and RQ of block-sparse matrices
 // ------------------------------------------------------------------------------------
 
-int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
+int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend, double discard_weight)
 {
 	const Meta& am = a.m();
 	pend = SvdPending();
@@ -1045,6 +1049,8 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 		qi.push_back(-am.dir[0] * am.dir[1] * am.qb[0][0]);
 	}
 	const i64 ni = (i64)qi.size();
+	// squared singular values below which every value is discarded by the caller
+	const double discard2 = discard_weight > 0 ? discard_weight / (2.0 * (double)ni) : 0.0;
 	const i64 du[2] = {am.dim[0], ni};
 	Meta mu = make_meta(2, du, am.dir.data(), {am.ql[0], qi});
 	const i64 dv[2] = {ni, am.dim[1]};
@@ -1145,8 +1151,11 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 		int total = 0;
 		for (size_t b = 0; b < descs.size(); b++)
 		{
+			// at least two columns per column group (four per CTA): below that the cluster barriers
+			// of the Jacobi rounds cost more than the extra CTAs save
+			const int ncol = std::min(descs[b].m, descs[b].n);
 			int want = 1;
-			while (want < maxcl && work[b] > slack * wmax / maxcl * want) want *= 2;
+			while (want < maxcl && 2 * (2 * want) * 2 <= ncol && work[b] > slack * wmax / maxcl * want) want *= 2;
 			if (forced) want = forced;
 			cfg[b] = svd_launch_for(descs[b].m, descs[b].n, want, maxcl);
 			total += cfg[b].cluster;
@@ -1202,14 +1211,14 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 		if (groups.size() == 1)
 			launch_svd_group(groups[0].l, groups[0].first, groups[0].count, (const SvdDesc*)desc->ptr, a.data(),
 			                 res.u.data(), (double*)res.s->ptr, res.vh.data(), (double*)scratch.ptr, (int*)status.ptr,
-			                 (double*)tail.ptr, c.stream(), tsp);
+			                 (double*)tail.ptr, c.stream(), tsp, discard2);
 		else
 		{
 			c.fork(ng);
 			for (size_t g = 0; g < groups.size(); g++)
 				launch_svd_group(groups[g].l, groups[g].first, groups[g].count, (const SvdDesc*)desc->ptr, a.data(),
 				                 res.u.data(), (double*)res.s->ptr, res.vh.data(), (double*)scratch.ptr,
-				                 (int*)status.ptr, (double*)tail.ptr, c.aux((int)g), tsp);
+				                 (int*)status.ptr, (double*)tail.ptr, c.aux((int)g), tsp, discard2);
 			c.join(ng);
 		}
 	}
@@ -1238,12 +1247,14 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend)
 			// CTGPU_SVD_PHASES=2: one line per call for the block that finished last
 			static const bool each = atoi(getenv("CTGPU_SVD_PHASES")) >= 2;
 			if (each)
-				fprintf(stderr, "ctgpu: svd call: %zu blocks, critical %d x %d (cluster %d): QR %.3f Jacobi %.3f outputs %.3f ms, FP32 sweeps %llu, FP64 sweeps %llu\n",
+				fprintf(stderr, "ctgpu: svd call: %zu blocks, critical %d x %d (cluster %d): QR %.3f Jacobi %.3f outputs %.3f ms, FP32 sweeps %llu, FP64 sweeps %llu, refinement %llu (kcycles: gram %llu analysis %llu update %llu clusters %llu)\n",
 				        descs.size(), descs[crit].m, descs[crit].n, cfg[crit].cluster,
 				        1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 1] - h[SVD_PHASE_SLOTS * crit]),
 				        1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 2] - h[SVD_PHASE_SLOTS * crit + 1]),
 				        1e-6 * (double)(h[SVD_PHASE_SLOTS * crit + 3] - h[SVD_PHASE_SLOTS * crit + 2]),
-				        h[SVD_PHASE_SLOTS * crit + 6], h[SVD_PHASE_SLOTS * crit + 5]);
+				        h[SVD_PHASE_SLOTS * crit + 6], h[SVD_PHASE_SLOTS * crit + 5], h[SVD_PHASE_SLOTS * crit + 15],
+				        h[SVD_PHASE_SLOTS * crit + 16] / 1000, h[SVD_PHASE_SLOTS * crit + 17] / 1000,
+				        h[SVD_PHASE_SLOTS * crit + 18] / 1000, h[SVD_PHASE_SLOTS * crit + 19] / 1000);
 		}
 	}
 	// the status and the flop count reach pinned host memory once the stream gets there (read by

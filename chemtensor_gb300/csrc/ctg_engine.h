@@ -267,7 +267,12 @@ struct SvdPending {
 };
 // enqueue the SVD without waiting for it; its status reaches pinned host memory when the stream
 // gets there, so op_svd_finish may run only after a synchronisation of c's stream
-int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend);
+// discard_weight: the caller discards singular values from the smallest up while their squares sum
+// to at most this (the relative truncation of the two-site split times a lower bound of ||a||_F^2;
+// 0: the full SVD is needed). Every value whose square is below discard_weight / (2 k), k the total
+// number of singular values, is then certainly discarded, and the block SVD may leave the mutual
+// rotations of such columns out.
+int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend, double discard_weight = 0.0);
 // 0, or -1 if a block did not converge (diagnostics on stderr)
 int op_svd_finish(Ctx& c, const SvdPending& pend);
 // launch, synchronise, finish. Returns 0 or -1.

@@ -175,8 +175,12 @@ constexpr int SVD_MAX_SWEEPS = 60;
 // steps (inner products, rotation parameters, rotations), [5] FP64 sweeps, [6] FP32 sweeps, SM
 // cycles of [7] exchanges, [8] FP32 sweeps, [9] FP32 to FP64 hand-over (Newton-Schulz steps and
 // T = R^T V); SM cycles of the distributed QR's steps in [10] pivot candidates, [11] candidate
-// reflectors, [12] candidate exchange and cluster barrier, [13] pivot reflector fetch, [14] updates
-constexpr int SVD_PHASE_SLOTS = 15;
+// reflectors, [12] candidate exchange and cluster barrier, [13] pivot reflector fetch, [14] updates;
+// [15] refinement iterations of the mixed path (plus 100 when it handed over to FP64 sweeps), SM
+// cycles of the refinement's [16] Gram matrices, [17] analysis (cosines, tail, clusters, generator),
+// [18] updates, [19] cluster rotations. With the refinement, [4] holds its SM cycles and [9] those
+// of the Newton-Schulz steps and T = R^T V.
+constexpr int SVD_PHASE_SLOTS = 20;
 struct SvdDesc {
 	i64 a_off, u_off, s_off, v_off, w_off;
 	int m, n;
@@ -199,9 +203,11 @@ SvdLaunch svd_launch_for(int m, int n, int want, int max_cluster);
 // %globaltimer stamps (start, QR done, Jacobi done, outputs done) to phase_ts[8 block ..] and
 // its SM clock cycles spent in the Jacobi inner products, rotation parameters, rotations and
 // cluster exchanges to phase_ts[8 block + 4 ..].
+// discard2: the caller discards every singular value whose square is below it (0: none); the
+// refinement of the mixed path then leaves the mutual rotations of those columns out.
 void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* descs, const double* a, double* u,
                       double* s, double* vh, double* scratch, int* status, double* flops, cudaStream_t st,
-                      unsigned long long* phase_ts = nullptr);
+                      unsigned long long* phase_ts = nullptr, double discard2 = 0.0);
 
 // Householder RQ of a row-major m x n block: A = R Q with Q (k x n) orthonormal rows, R (m x k), k = min(m, n).
 // Scratch holds n*m + n*k + k doubles per block.

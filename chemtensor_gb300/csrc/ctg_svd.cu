@@ -63,12 +63,20 @@ __host__ __device__ inline i64 f32_tour_bytes(int N, int r, int cf)
 	return 4 * (4 * bs * 2 * N + 4 * bs + 4);
 }
 
-// ... plus the staging of the FP64 steps after the FP32 sweeps: all of V (r x (r | 1)) or of R
-// (r x (N | 1)), and the CTA's own columns (at most 2 bsmax of length r)
-__host__ __device__ inline i64 precond_doubles(int N, int cl)
+// scratch (doubles) of one block's SVD before the refinement's arrays: the larger of the
+// shared-memory path's layout (W, T, V, norms, reflector scalars, singular values, misc, flags,
+// pivots) and the global-memory path's (W, Q, T, V, ...), rounded up to a multiple of 2
+__host__ __device__ inline i64 svd_refine_offset(i64 M, i64 N)
 {
-	const i64 nblk = 2 * cl, bsmax = (N + nblk - 1) / nblk;
-	return tour_jac_doubles(N, cl) + (i64)N * (N | 1) + 2 * bsmax * N;
+	const i64 base = 2 * M * N + 2 * N * N + 3 * N + 4 + 2 * SVD_MAX_SWEEPS + (N + 1) / 2 + 1;
+	return (base + 1) & ~(i64)1;
+}
+// the refinement's arrays: G (N x N doubles), X (N x N floats), (hi, lo) float pairs of T (N x N)
+// and V (N x N), per iteration a failure flag, the largest cosine and the number of cluster edges,
+// and the cluster-edge list (4 N pairs)
+__host__ __device__ inline i64 svd_refine_doubles(i64 N)
+{
+	return N * N + (N * N + 1) / 2 + 2 * N * N + 12 + 4 * N;
 }
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -519,11 +527,13 @@ __device__ void jacobi_step32(const Tour32& t, int buf, int mode, int step, int 
 struct SvdScratch {
 	double *W, *T, *V, *nrm, *tau, *sig, *misc;
 	int *flags, *perm, *flags32, *cmax;
+	double* G;                   // refinement of the mixed path: G, X, (hi, lo) copies of T and V
 };
 
 // workspace of one block: W (M x N, B then R and the reflectors), T (N x r), V (r x r), column
 // norms, reflector scalars, singular values, misc [rank, ||B||_F^2, unscale], sweep flags, pivots,
-// FP32 sweep flags, largest cos^2 per sweep
+// FP32 sweep flags, largest cos^2 per sweep; after the larger of this layout and the global-memory
+// path's, the refinement's arrays (svd_refine_offset)
 __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 {
 	SvdScratch x;
@@ -538,6 +548,7 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 	x.perm = x.flags + SVD_MAX_SWEEPS;
 	x.flags32 = x.perm + N;
 	x.cmax = x.flags32 + SVD_F32_SWEEPS;
+	x.G = base + svd_refine_offset(M, N);
 	return x;
 }
 
@@ -803,11 +814,9 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 // FP32 preconditioning of the tour (see above). The FP32 sweeps run on the first cf CTAs of the
 // cluster (a tour over 2 cf groups; the others only keep the cluster barriers in step): their
 // cost is latency and barriers, not arithmetic, and fewer, larger groups need fewer rounds. On
-// return, buffer 0 of the FP64 tour holds this CTA's round-0 column records [T | V] with V
-// orthogonal to FP64 rounding and T = R^T V. Staging for the FP64 steps starts after the FP64
-// tour's own shared memory.
+// return, V (r x r, orthogonal to FP32 accuracy, column g at xs.V + g r) is in global memory.
 __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, double* smem, const SvdScratch& xs, int M,
-                                 int cl, int cf, int rank, double& flops, long long* cyc)
+                                 int cf, int rank, long long* cyc)
 {
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const long long c0 = cyc ? clock64() : 0;
@@ -927,96 +936,725 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 			if (__ldcg(xs.flags32 + sweep) == 0) break;
 		}
 	}
-	const long long c1 = cyc ? clock64() : 0;
 	cluster.sync();
-	// the CTA's own columns of the FP64 tour: slot-0 group, then slot-1 group
-	round_groups(0, rank, t.nm, A, B);
-	const int own0 = t.cnt(A), nown = own0 + t.cnt(B);
-	auto own_col = [&](int j) { return j < own0 ? A * t.bs + j : B * t.bs + (j - own0); };
-	double* stage = smem + tour_jac_doubles(N, cl);
-	// two Newton-Schulz steps, V <- V - V E / 2 with E = V^T V - I; V ping-pongs between the V and
-	// T areas of the scratch (T is written only after the Jacobi sweeps)
-	double* Va = xs.V;
-	double* Vb = xs.T;
-	const int ldv = r | 1;                            // odd stride: lanes over columns hit distinct banks
-	double* vs = stage;                               // all of V, column k at vs + k ldv
-	double* es = vs + (i64)r * ldv;                   // E columns of the own columns, es + j r
+	if (cyc) cyc[4] += clock64() - c0;
+}
+
+// ---- FP64 finish of the mixed path: Newton-Schulz, T = R^T V, simultaneous refinement -------
+//
+// After the FP32 sweeps the columns of R^T V are orthogonal to about N eps_32 (cosines ~1e-5)
+// and V to FP32 accuracy. FP64 Jacobi sweeps from there cost ~6.5 n^3 FP64 FMAs each (a pair
+// rotation after every inner product, one barrier per step) and GB300 retires two FP64 FMAs per
+// clock per SM. This finish does its FP64 work as inner products of whole Gram matrices and applies
+// the corrections, which are small, with products accumulated in double-float on the FP32 pipe:
+//   1. two Newton-Schulz steps V <- V (I - E / 2), E = V^T V - I (E from FP64 inner products);
+//   2. T = R^T V (FP64);
+//   3. G = T^T T (FP64 inner products, each pair once). For columns i, j whose squared norms lie
+//      apart, the first-order generator X_ij = G_ij / (G_jj - G_ii) (antisymmetric) removes the
+//      cosine of the pair to second order; T and V are multiplied by I + X + X^2 / 2, which is
+//      orthogonal to O(X^4). Columns whose squared norms lie within a relative gap gamma of their
+//      neighbours (a cluster, where the first-order angle would not be small) get X = 0 and are
+//      rotated afterwards among themselves by exact one-sided Jacobi rotations (one warp per
+//      cluster). gamma = c_max / (2 delta) keeps every first-order angle below delta = 3e-4 for
+//      the largest cosine c_max. Repeat until every cosine is within the FP64 sweeps' tolerance
+//      (the cosines fall quadratically: ~1e-5, ~1e-10, below eps).
+// The scheme is the iterative refinement of a symmetric eigendecomposition of Ogita and Aishima
+// (Japan J. Indust. Appl. Math. 35, 2018) applied one-sided to the columns of T. A block whose
+// clusters are too wide or too large, or that does not converge in RF_MAX_IT iterations, continues
+// with the FP64 sweeps from the current columns (V stays orthogonal to FP64 rounding throughout).
+
+constexpr int RF_MAX_IT = 6;              // refinement iterations before the FP64 sweeps take over
+constexpr float RF_DELTA = 3e-4f;         // largest first-order angle outside a cluster
+constexpr int RF_CLUSTER_MAX = 16;        // most columns of one cluster
+constexpr int RF_CLUSTER_SWEEPS = 8;      // most Jacobi sweeps inside one cluster
+constexpr int RF_EDGES_PER_COL = 4;       // capacity of the cluster-edge list, per column
+
+// a double as the pair hi + lo of floats (hi: the leading 24 bits, lo: the next 24), by integer
+// operations (a double -> float conversion costs an FP64 instruction on GB300); values below 2^-126
+// (far below any entry that matters here) give zero, lo below 2^-126 is dropped
+__device__ __forceinline__ float dbl_hi(double x, int& e)
+{
+	const int hi = __double2hiint(x), lo = __double2loint(x);
+	e = ((hi >> 20) & 0x7ff) - 1023;
+	if (e < -126) return 0.0f;
+	return __int_as_float((hi & (int)0x80000000) | ((e + 127) << 23) | ((hi & 0x000fffff) << 3) | (int)((unsigned)lo >> 29));
+}
+__device__ __forceinline__ float2 split_hilo(double x)
+{
+	int e;
+	const float h = dbl_hi(x, e);
+	if (h == 0.0f || e < -74) return make_float2(h, 0.0f);
+	const int lo = __double2loint(x);
+	float l = __int2float_rn(lo & 0x1fffffff) * pow2f(e - 52);
+	if (__double2hiint(x) < 0) l = -l;
+	return make_float2(h, l);
+}
+__device__ __forceinline__ float dbl_to_f32(double x)
+{
+	int e;
+	return dbl_hi(x, e);
+}
+
+// |g|^2 / (a b) in FP32 for a, b > 0 (capped at 1), from mantissas and exponents
+__device__ __forceinline__ float cos2_f32(double g, double a, double b)
+{
+	if (g == 0.0) return 0.0f;
+	int eg, ea, eb;
+	const float mg = mant_exp(g, eg), ma = mant_exp(a, ea), mb = mant_exp(b, eb);
+	const int k2 = 2 * eg - ea - eb;
+	if (k2 < -120) return 0.0f;
+	if (k2 > 0) return 1.0f;
+	return fminf(__fdividef(mg * mg, ma * mb) * pow2f(k2), 1.0f);
+}
+
+// n / d in FP32 (d != 0), from mantissas and exponents; |result| < 2^-126 gives 0, large
+// results are capped at 2 (they mark a pair that should have been in a cluster)
+__device__ __forceinline__ float ratio_f32(double n, double d)
+{
+	if (n == 0.0) return 0.0f;
+	int en, ed;
+	const float mn = mant_exp(n, en), md = mant_exp(d, ed);
+	const int k = en - ed;
+	if (k < -125) return 0.0f;
+	float v = k > 0 ? 2.0f : __fdividef(mn, md) * pow2f(k);
+	if ((__double2hiint(n) < 0) != (__double2hiint(d) < 0)) v = -v;
+	return v;
+}
+
+struct Refine {
+	// global
+	double* G;        // r x r Gram matrix (symmetric; column j at G + j r)
+	float* X;         // r x r first-order generator (column j at X + j r)
+	double* Tr;       // T row-major, entry (k, i) at Tr + k r + i (the scratch T area)
+	double* Vr;       // V row-major (the scratch V area)
+	float2* Th;       // T column-major as (hi, lo) pairs, entry (k, i) at Th + i N + k
+	float2* Vh;       // V column-major as (hi, lo) pairs, entry (k, i) at Vh + i r + k
+	int* gfail;       // per iteration: a first-order angle came out too large
+	int* gc2;         // per iteration: largest cos^2 (bits of a non-negative float)
+	int* gne;         // per iteration: cluster edges found
+	int2* gedges;     // the cluster edges of the current iteration
+	// shared
+	float* F;         // own columns of the update, leading floats (column jj at F + jj r)
+	float* Fl;        // ... and the trailing floats: F + Fl is X + X^2 / 2 exactly
+	float* Xo;        // own columns of X
+	double* D;        // diagonal of G
+	float* key;       // D as floats
+	int* cid;         // cluster of each column: its smallest column index
+	int* cnt;         // columns per cluster (at the cluster's smallest index)
+	int* qidx;        // 2 + index of the non-singleton cluster whose smallest index this is, else 0
+	unsigned char* tail;   // 1: among the smallest columns whose squared norms fit the discard budget
+	int2* edges;      // cluster edges (pairs whose first-order angle would exceed delta)
+	int* memb;        // members of the cluster being rotated (RF_CLUSTER_MAX)
+	double* cstage;   // that cluster's columns [T; V] (RF_CLUSTER_MAX records of N + r, stride ldc)
+	int* misc;        // [0] non-singleton clusters, [1] failure, [2] edges, [3] labels changed, [4] rotated
+	float* red;       // [NWARPS] block reduction
+	// own columns
+	int A, B, own0, nown;
+};
+
+// shared memory (doubles) of the mixed path: the FP64 tour's buffers (the records the finish works
+// on, and the fallback sweeps), then the refinement's arrays
+__host__ __device__ inline i64 refine_doubles(int N, int cl)
+{
+	const i64 nblk = 2 * cl, bsmax = (N + nblk - 1) / nblk;
+	const i64 bytes = 8 * (i64)N                              // D
+	                  + 8 * (i64)RF_CLUSTER_MAX * (2 * N + 1) // cstage
+	                  + 3 * 4 * (2 * bsmax * N)               // F, Fl, Xo
+	                  + 4 * 4 * (i64)N                        // key, cid, cnt, qidx
+	                  + 8 * (i64)RF_EDGES_PER_COL * N         // edges
+	                  + 4 * (i64)RF_CLUSTER_MAX               // memb
+	                  + 4 * 8 + 4 * NWARPS                    // misc, red
+	                  + (i64)N + 16;                          // tail
+	return tour_jac_doubles(N, cl) + (bytes + 7) / 8 + 2;
+}
+
+__device__ __forceinline__ double* rf_rec(const Tour& t, const Refine& rf, int jj)
+{
+	return jj < rf.own0 ? t.col(0, 0, jj) : t.col(0, 1, jj - rf.own0);
+}
+__device__ __forceinline__ int rf_col(const Tour& t, const Refine& rf, int jj)
+{
+	return jj < rf.own0 ? rf.A * t.bs + jj : rf.B * t.bs + (jj - rf.own0);
+}
+
+// own columns to the global copies: row-major FP64 and column-major (hi, lo) pairs; T entries
+// only when with_t
+__device__ void rf_write_own(const Tour& t, const Refine& rf, bool with_t)
+{
+	const int tid = threadIdx.x, N = t.N, r = t.r;
+	if (with_t)
+		for (int e = tid; e < rf.nown * N; e += SVD_THREADS)
+		{
+			const int jj = e / N, k = e % N, g = rf_col(t, rf, jj);
+			const double x = rf_rec(t, rf, jj)[k];
+			rf.Tr[(i64)k * r + g] = x;
+			rf.Th[(i64)g * N + k] = split_hilo(x);
+		}
+	for (int e = tid; e < rf.nown * r; e += SVD_THREADS)
+	{
+		const int jj = e / r, k = e % r, g = rf_col(t, rf, jj);
+		const double x = rf_rec(t, rf, jj)[N + k];
+		rf.Vr[(i64)k * r + g] = x;
+		rf.Vh[(i64)g * r + k] = split_hilo(x);
+	}
+}
+
+// S_ij = sum_k A_ki A_kj (minus 1 on the diagonal when sub_identity) for the own columns j and
+// every i <= j, written to S at (i, j) and (j, i): each pair once over the cluster (the CTA
+// holding groups p and 2 cl - 1 - p gets the same share of pairs as every other CTA). A is
+// row-major (A + k r + i, len rows), column j is read from the own record at offset off. A warp
+// takes 32 consecutive i against one own column; two independent FP64 accumulators.
+__device__ double rf_gram(const Tour& t, const Refine& rf, const double* Ar, int len, int off, bool sub_identity,
+                          double* S)
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, r = t.r;
+	const int nchunk = (r + 31) / 32;
+	double fl = 0;
+	for (int task = warp; task < rf.nown * nchunk; task += NWARPS)
+	{
+		const int jj = task % rf.nown, c = task / rf.nown;
+		const int g = rf_col(t, rf, jj);
+		if (32 * c > g) continue;
+		const int i = 32 * c + lane;
+		const bool valid = i < r && i <= g;
+		const double* rec = rf_rec(t, rf, jj) + off;
+		const double* a = Ar + (valid ? i : 0);
+		// eight loads in flight per thread (a warp reads 32 consecutive doubles of a row per load)
+		double acc[4] = {0.0, 0.0, 0.0, 0.0};
+		int k = 0;
+		for (; k + 7 < len; k += 8)
+		{
+			double x[8];
+#pragma unroll
+			for (int u = 0; u < 8; u++) x[u] = __ldcg(a + (i64)(k + u) * r);
+#pragma unroll
+			for (int u = 0; u < 8; u++) acc[u & 3] = fma(x[u], rec[k + u], acc[u & 3]);
+		}
+		for (; k < len; k++) acc[0] = fma(__ldcg(a + (i64)k * r), rec[k], acc[0]);
+		const double v = ((acc[0] + acc[1]) + (acc[2] + acc[3])) - ((sub_identity && i == g) ? 1.0 : 0.0);
+		if (valid)
+		{
+			S[(i64)i * r + g] = v;
+			S[(i64)g * r + i] = v;
+		}
+		if (lane == 0) fl += 2.0 * len * (double)min(32, g + 1 - 32 * c);
+	}
+	return fl;
+}
+
+// own columns += [T; V] (F + Fl) (rows 0..N-1 of T when with_t, then the r rows of V), the sums
+// accumulated in double-float: exact products of the leading floats (fma error term), the
+// trailing-float cross terms in FP32, two-sum accumulation; the FP64 record gets hi + lo of the sum
+__device__ void rf_update(const Tour& t, const Refine& rf, bool with_t)
+{
+	const int tid = threadIdx.x, N = t.N, r = t.r;
+	constexpr int JB = 8;
+	const int row0 = with_t ? 0 : N;
+	const int nrows = N + r - row0;
+	const int nb = (rf.nown + JB - 1) / JB;
+	for (int task = tid; task < nrows * nb; task += SVD_THREADS)
+	{
+		const int kr = row0 + task % nrows, b = task / nrows;
+		const float2* h = kr < N ? rf.Th + kr : rf.Vh + (kr - N);
+		const i64 ld = kr < N ? N : r;
+		float sh[JB], sl[JB];
+#pragma unroll
+		for (int q = 0; q < JB; q++) sh[q] = sl[q] = 0.0f;
+		const int j0 = b * JB;
+		const int nj = min(JB, rf.nown - j0);
+#pragma unroll 4
+		for (int i = 0; i < r; i++)
+		{
+			const float2 v = __ldcg(h + (i64)i * ld);
+#pragma unroll
+			for (int q = 0; q < JB; q++)
+			{
+				if (q >= nj) break;
+				const float f = rf.F[(j0 + q) * r + i], fl = rf.Fl[(j0 + q) * r + i];
+				const float p = v.x * f;
+				float e = fmaf(v.x, f, -p);
+				e = fmaf(v.y, f, e);
+				e = fmaf(v.x, fl, e);
+				const float s = sh[q] + p;
+				const float bp = s - sh[q];
+				const float err = (sh[q] - (s - bp)) + (p - bp);
+				sh[q] = s;
+				sl[q] += err + e;
+			}
+		}
+		for (int q = 0; q < nj; q++)
+		{
+			double* rec = rf_rec(t, rf, j0 + q);
+			rec[kr] = rec[kr] + (make_double(sh[q], 0) + make_double(sl[q], 0));
+		}
+	}
+}
+
+// one-sided Jacobi sweeps inside each non-singleton cluster, one CTA per cluster: the cluster's
+// columns [T; V] are staged in shared memory, each round rotates disjoint pairs (one warp per pair,
+// circle method), one CTA barrier per round; the columns go back to the global row-major copies.
+// Returns the FP64 flops (counted on lane 0 of each warp).
+__device__ double rf_cluster_jacobi(const Tour& t, const Refine& rf, int cl, int rank, float tol2)
+{
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, N = t.N, r = t.r;
+	const int len = N + r, ldc = len | 1;
+	double fl = 0;
+	const int ncl = rf.misc[0];
+	for (int q = rank; q < ncl; q += cl)
+	{
+		if (warp == 0)
+		{
+			// the cluster's smallest column, then its members in increasing order
+			int root = -1;
+			for (int i = lane; i < r; i += 32)
+				if (rf.qidx[i] == 2 + q) root = i;
+			for (int o = 16; o > 0; o >>= 1) root = max(root, __shfl_xor_sync(0xffffffffu, root, o));
+			int c = 0;
+			for (int base = 0; base < r; base += 32)
+			{
+				const int i = base + lane;
+				const bool in = root >= 0 && i < r && rf.cid[i] == root;
+				const unsigned m = __ballot_sync(0xffffffffu, in);
+				const int at = c + __popc(m & ((1u << lane) - 1));
+				if (in && at < RF_CLUSTER_MAX) rf.memb[at] = i;
+				c += __popc(m);
+			}
+			if (lane == 0) rf.misc[5] = min(c, RF_CLUSTER_MAX);
+		}
+		__syncthreads();
+		const int c = rf.misc[5];
+		for (int e = tid; e < c * len; e += SVD_THREADS)
+		{
+			const int m = e / len, k = e % len, col = rf.memb[m];
+			rf.cstage[(i64)m * ldc + k] = k < N ? __ldcg(rf.Tr + (i64)k * r + col) : __ldcg(rf.Vr + (i64)(k - N) * r + col);
+		}
+		__syncthreads();
+		const int cpad = c + (c & 1);
+		for (int sweep = 0; sweep < RF_CLUSTER_SWEEPS; sweep++)
+		{
+			if (tid == 0) rf.misc[4] = 0;
+			__syncthreads();
+			for (int rnd = 0; rnd < cpad - 1; rnd++)
+			{
+				int pa, pb;
+				if (warp < cpad / 2)
+				{
+					round_robin_pair(rnd, warp, cpad, pa, pb);
+					if (pb < c)
+					{
+						double* x = rf.cstage + (i64)pa * ldc;
+						double* y = rf.cstage + (i64)pb * ldc;
+						double al = 0, be = 0, ga = 0;
+						for (int k = lane; k < N; k += 32)
+						{
+							al = fma(x[k], x[k], al);
+							be = fma(y[k], y[k], be);
+							ga = fma(x[k], y[k], ga);
+						}
+						al = warp_sum(al);
+						be = warp_sum(be);
+						ga = warp_sum(ga);
+						double tau, sn, tn;
+						float c2;
+						if (lane == 0) fl += 6.0 * N;
+						if (al > 0.0 && be > 0.0 && rotation_params(al, be, ga, tol2, tau, sn, tn, c2))
+						{
+							for (int k = lane; k < len; k += 32)
+							{
+								const double x1 = fma(-tau, y[k], x[k]);
+								const double y1 = fma(sn, x1, y[k]);
+								x[k] = fma(-tau, y1, x1);
+								y[k] = y1;
+							}
+							if (lane == 0)
+							{
+								rf.misc[4] = 1;
+								fl += 6.0 * len;
+							}
+						}
+					}
+				}
+				__syncthreads();
+			}
+			const bool any = rf.misc[4] != 0;
+			__syncthreads();
+			if (!any) break;
+		}
+		for (int e = tid; e < c * len; e += SVD_THREADS)
+		{
+			const int m = e / len, k = e % len, col = rf.memb[m];
+			const double v = rf.cstage[(i64)m * ldc + k];
+			if (k < N) __stcg(rf.Tr + (i64)k * r + col, v);
+			else __stcg(rf.Vr + (i64)(k - N) * r + col, v);
+		}
+		__syncthreads();
+	}
+	return fl;
+}
+
+// Steps 1-3 above on the cluster. On entry the FP32 phase has left V (r x r, column g at
+// xs.V + g r) in global memory. tail2: the caller discards every singular value whose square is
+// below this (scaled as B here; 0: none), so the mutual rotations of the smallest columns whose
+// squared norms sum to at most tail2 are skipped. On return buffer 0 of the FP64 tour holds this
+// CTA's round-0 records [T | V]; the return value says whether the refinement converged (the same
+// on every CTA of the cluster); if not, the FP64 sweeps continue from those records.
+__device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* smem, const SvdScratch& xs, int M,
+                             int cl, int rank, bool refine, float tail2, double& flops, long long* cyc, int& iters)
+{
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int N = t.N, r = t.r;
+	const long long c0 = cyc ? clock64() : 0;
+	Refine rf;
+	round_groups(0, rank, t.nm, rf.A, rf.B);
+	rf.own0 = t.cnt(rf.A);
+	rf.nown = rf.own0 + t.cnt(rf.B);
+	rf.G = xs.G;
+	rf.X = (float*)(xs.G + (i64)N * N);
+	rf.Th = (float2*)(xs.G + (i64)N * N + ((i64)N * N + 1) / 2);
+	rf.Vh = rf.Th + (i64)N * N;
+	rf.gfail = (int*)(rf.Vh + (i64)N * N);
+	rf.gc2 = rf.gfail + 8;
+	rf.gne = rf.gfail + 16;
+	rf.gedges = (int2*)(rf.gfail + 24);
+	rf.Tr = xs.T;
+	rf.Vr = xs.V;
+	{
+		char* p = (char*)(smem + tour_jac_doubles(N, cl));
+		rf.D = (double*)p;
+		p += 8 * (i64)N;
+		rf.cstage = (double*)p;
+		p += 8 * (i64)RF_CLUSTER_MAX * (2 * N + 1);
+		rf.edges = (int2*)p;
+		p += 8 * (i64)RF_EDGES_PER_COL * N;
+		rf.F = (float*)p;
+		p += 4 * (i64)(2 * t.bsmax) * N;
+		rf.Fl = (float*)p;
+		p += 4 * (i64)(2 * t.bsmax) * N;
+		rf.Xo = (float*)p;
+		p += 4 * (i64)(2 * t.bsmax) * N;
+		rf.key = (float*)p;
+		p += 4 * (i64)N;
+		rf.cid = (int*)p;
+		p += 4 * (i64)N;
+		rf.cnt = (int*)p;
+		p += 4 * (i64)N;
+		rf.qidx = (int*)p;
+		p += 4 * (i64)N;
+		rf.memb = (int*)p;
+		p += 4 * (i64)RF_CLUSTER_MAX;
+		rf.misc = (int*)p;
+		p += 4 * 8;
+		rf.red = (float*)p;
+		p += 4 * NWARPS;
+		rf.tail = (unsigned char*)p;
+	}
+	double fl = 0;
+
+	// ---- 1. Newton-Schulz on V: own columns from the FP32 phase's output ----
+	for (int e = tid; e < rf.nown * N; e += SVD_THREADS)
+	{
+		const int jj = e / N, k = e % N;
+		rf_rec(t, rf, jj)[N + k] = k < r ? __ldcg(xs.V + (i64)rf_col(t, rf, jj) * r + k) : 0.0;
+	}
+	if (rank == 0 && tid < 24) rf.gfail[tid] = 0;        // failure flags, cosines, edge counts
+	cluster.sync();                              // xs.V is read before its row-major overwrite
 	for (int step = 0; step < 2; step++)
 	{
-		for (i64 e = tid; e < (i64)r * r; e += SVD_THREADS)
-		{
-			const int k = (int)(e / r), i = (int)(e % r);
-			vs[(i64)k * ldv + i] = __ldcg(Va + e);
-		}
-		__syncthreads();
-		for (int e = tid; e < r * nown; e += SVD_THREADS)
-		{
-			const int j = e / r, k = e % r;
-			const int g = own_col(j);
-			const double* vk = vs + (i64)k * ldv;
-			const double* vj = vs + (i64)g * ldv;
-			double acc = 0.0;
-			for (int i = 0; i < r; i++) acc = fma(vk[i], vj[i], acc);
-			es[(i64)j * r + k] = acc - (k == g ? 1.0 : 0.0);
-		}
-		__syncthreads();
-		for (int e = tid; e < r * nown; e += SVD_THREADS)
-		{
-			const int j = e / r, i = e % r;
-			const double* ej = es + (i64)j * r;
-			double acc = 0.0;
-			for (int k = 0; k < r; k++) acc = fma(vs[(i64)k * ldv + i], ej[k], acc);
-			const int g = own_col(j);
-			Vb[(i64)g * r + i] = fma(-0.5, acc, vs[(i64)g * ldv + i]);
-		}
-		if (tid == 0) flops += 4.0 * (double)r * r * nown;
+		rf_write_own(t, rf, false);
 		cluster.sync();
-		double* tmp = Va;
-		Va = Vb;
-		Vb = tmp;
+		fl += rf_gram(t, rf, rf.Vr, r, N, true, rf.G);
+		cluster.sync();
+		for (int e = tid; e < rf.nown * r; e += SVD_THREADS)
+		{
+			const int jj = e / r, i = e % r;
+			rf.F[jj * r + i] = -0.5f * dbl_to_f32(__ldcg(rf.G + (i64)rf_col(t, rf, jj) * r + i));
+			rf.Fl[jj * r + i] = 0.0f;
+		}
+		__syncthreads();
+		rf_update(t, rf, false);
+		cluster.sync();                          // every CTA has read the (hi, lo) pairs
 	}
-	// T = R^T V for the own columns, straight into buffer 0 of the FP64 tour; R staged with an odd
-	// stride (row k at rs + k ldr, R_ki = W_ik for i >= k)
-	const int ldr = N | 1;
-	double* rs = stage;
-	double* vo = rs + (i64)r * ldr;
-	for (i64 e = tid; e < (i64)r * N; e += SVD_THREADS)
+
+	// ---- 2. T = R^T V for the own columns (R_ki = W_ik, k <= i), FP64 ----
 	{
-		const int i = (int)(e / r), k = (int)(e % r);
-		rs[(i64)k * ldr + i] = (k <= i) ? __ldcg(xs.W + (i64)i * M + k) : 0.0;
+		constexpr int JB = 4;
+		for (int j0 = 0; j0 < rf.nown; j0 += JB)
+		{
+			const int nj = min(JB, rf.nown - j0);
+			for (int i = tid; i < N; i += SVD_THREADS)
+			{
+				const int kmax = i < r - 1 ? i : r - 1;
+				const double* wi = xs.W + (i64)i * M;
+				double acc[JB] = {0.0, 0.0, 0.0, 0.0};
+				const double* v0 = rf_rec(t, rf, j0) + N;
+				const double* v1 = rf_rec(t, rf, j0 + min(1, nj - 1)) + N;
+				const double* v2 = rf_rec(t, rf, j0 + min(2, nj - 1)) + N;
+				const double* v3 = rf_rec(t, rf, j0 + min(3, nj - 1)) + N;
+#pragma unroll 4
+				for (int k = 0; k <= kmax; k++)
+				{
+					const double w = __ldcg(wi + k);
+					acc[0] = fma(w, v0[k], acc[0]);
+					acc[1] = fma(w, v1[k], acc[1]);
+					acc[2] = fma(w, v2[k], acc[2]);
+					acc[3] = fma(w, v3[k], acc[3]);
+				}
+				for (int q = 0; q < nj; q++) rf_rec(t, rf, j0 + q)[i] = acc[q];
+			}
+		}
+		if (tid == 0) fl += 2.0 * ((double)N * r - 0.5 * (double)r * r) * rf.nown;
+		__syncthreads();
 	}
-	for (int e = tid; e < r * nown; e += SVD_THREADS)
+	const long long c1 = cyc ? clock64() : 0;
+	if (cyc) cyc[5] += c1 - c0;
+	iters = 0;
+	if (!refine)
 	{
-		const int j = e / r, k = e % r;
-		vo[e] = __ldcg(Va + (i64)own_col(j) * r + k);
+		if (lane == 0) flops += fl;
+		return false;
 	}
+
+	// ---- 3. refinement ----
+	const float tol2 = (float)((double)N * DBL_EPSILON * (double)N * DBL_EPSILON);
+	bool converged = false;
+	if (tid == 0) rf.misc[6] = 0;            // largest cluster seen
 	__syncthreads();
-	for (int e = tid; e < N * nown; e += SVD_THREADS)
+	int fail = 0;            // why the FP64 sweeps take over: 1 edge list full, 2 labels unsettled,
+	                         // 3 cluster too large, 4 first-order angle too large, 5 no convergence
+	long long ck = cyc ? clock64() : 0;
+	auto lap = [&](int slot) {
+		if (cyc)
+		{
+			const long long now = clock64();
+			cyc[slot] += now - ck;
+			ck = now;
+		}
+	};
+	for (int it = 0; it < RF_MAX_IT; it++)
 	{
-		const int j = e / N, i = e % N;
-		const int kmax = i < r - 1 ? i : r - 1;
-		const double* vj = vo + (i64)j * r;
-		double acc = 0.0;
-		for (int k = 0; k <= kmax; k++) acc = fma(rs[(i64)k * ldr + i], vj[k], acc);
-		const int slot = j < own0 ? 0 : 1, c = slot ? j - own0 : j;
-		double* rec = t.col(0, slot, c);
-		rec[i] = acc;
-		rec[N + i] = i < r ? vj[i] : 0.0;
+		rf_write_own(t, rf, true);
+		cluster.sync();
+		fl += rf_gram(t, rf, rf.Tr, N, 0, false, rf.G);
+		cluster.sync();
+		lap(6);
+		// diagonal; the discarded tail: the smallest columns whose squared norms sum to at most tail2
+		// (every CTA computes the same sets and values from the same global G)
+		for (int i = tid; i < r; i += SVD_THREADS)
+		{
+			const double d = __ldcg(rf.G + (i64)i * r + i);
+			rf.D[i] = d;
+			rf.key[i] = dbl_to_f32(d);
+		}
+		__syncthreads();
+		for (int i = tid; i < r; i += SVD_THREADS)
+		{
+			// squared norms up to and including column i in increasing order (ties by index)
+			const float ki = rf.key[i];
+			float below = 0.0f;
+			for (int k = 0; k < r; k++)
+			{
+				const float kk = rf.key[k];
+				if (kk < ki || (kk == ki && k <= i)) below += kk;
+			}
+			rf.tail[i] = below <= tail2 ? 1 : 0;
+		}
+		__syncthreads();
+		// the pairs (i, g), i < g, of the own columns g (each pair once over the cluster): largest
+		// cosine over the pairs not both in the tail, and the cluster edges, pairs (not both in the
+		// tail) whose first-order angle |G_ig / (D_g - D_i)| would exceed delta, to global memory
+		{
+			float c2 = 0.0f;
+			for (int e = tid; e < rf.nown * r; e += SVD_THREADS)
+			{
+				const int jj = e / r, i = e % r, g = rf_col(t, rf, jj);
+				if (i >= g || (rf.tail[i] && rf.tail[g])) continue;
+				const double gv = __ldcg(rf.G + (i64)g * r + i);
+				c2 = fmaxf(c2, cos2_f32(gv, rf.D[i], rf.D[g]));
+				if (fabsf(dbl_to_f32(gv)) > RF_DELTA * fabsf(rf.key[g] - rf.key[i]))
+				{
+					const int at = atomicAdd(rf.gne + it, 1);
+					if (at < RF_EDGES_PER_COL * r) rf.gedges[at] = make_int2(i, g);
+				}
+			}
+			for (int o = 16; o > 0; o >>= 1) c2 = fmaxf(c2, __shfl_xor_sync(0xffffffffu, c2, o));
+			if (lane == 0 && c2 > 0.0f) atomicMax(rf.gc2 + it, __float_as_int(c2));
+		}
+		cluster.sync();
+		iters = it + 1;
+		if (__int_as_float(__ldcg(rf.gc2 + it)) <= tol2)
+		{
+			converged = true;
+			break;
+		}
+		// clusters: connected components of the edges, labelled by their smallest column
+		if (tid == 0) rf.misc[1] = 0;
+		for (int i = tid; i < r; i += SVD_THREADS)
+		{
+			rf.cid[i] = i;
+			rf.cnt[i] = 0;
+		}
+		const int nedge_all = __ldcg(rf.gne + it);
+		if (nedge_all > RF_EDGES_PER_COL * r)
+		{
+			fail = 1;
+			break;                                                  // uniform: one global count
+		}
+		for (int e = tid; e < nedge_all; e += SVD_THREADS) rf.edges[e] = __ldcg(rf.gedges + e);
+		__syncthreads();
+		const int nedge = nedge_all;
+		// minimum-label propagation with pointer jumping (labels are column indices of the same
+		// component and only decrease; cid[cid[i]] shortcuts chains, so a component typically
+		// settles in a number of rounds logarithmic in its diameter). After k rounds every label is
+		// at most the smallest column within k edges, so r + 1 rounds always settle: the outcome is
+		// the same on every CTA of the cluster
+		bool settled = nedge == 0;
+		for (int round = 0; round <= r && !settled; round++)
+		{
+			if (tid == 0) rf.misc[3] = 0;
+			__syncthreads();
+			for (int e = tid; e < nedge; e += SVD_THREADS)
+			{
+				const int2 ed = rf.edges[e];
+				const int a = rf.cid[ed.x], b = rf.cid[ed.y];
+				if (a != b)
+				{
+					const int m = min(a, b);
+					atomicMin(rf.cid + ed.x, m);
+					atomicMin(rf.cid + ed.y, m);
+					atomicMin(rf.cid + max(a, b), m);
+					rf.misc[3] = 1;
+				}
+			}
+			__syncthreads();
+			for (int i = tid; i < r; i += SVD_THREADS)
+			{
+				const int c = rf.cid[i], cc = rf.cid[c];
+				if (cc < c)
+				{
+					atomicMin(rf.cid + i, cc);
+					rf.misc[3] = 1;
+				}
+			}
+			__syncthreads();
+			settled = rf.misc[3] == 0;
+			__syncthreads();
+		}
+		if (!settled)
+		{
+			fail = 2;
+			break;
+		}
+		for (int i = tid; i < r; i += SVD_THREADS) atomicAdd(rf.cnt + rf.cid[i], 1);
+		__syncthreads();
+		if (warp == 0)
+		{
+			// index of every non-singleton cluster, in increasing order of its smallest column
+			int carry = 0, largest = 0;
+			bool big = false;
+			for (int base = 0; base < r; base += 32)
+			{
+				const int i = base + lane;
+				const int c = i < r ? rf.cnt[i] : 0;
+				const bool multi = c >= 2 && c <= RF_CLUSTER_MAX;
+				big = big || c > RF_CLUSTER_MAX;
+				largest = max(largest, c);
+				const unsigned m = __ballot_sync(0xffffffffu, multi);
+				if (i < r) rf.qidx[i] = multi ? 2 + carry + __popc(m & ((1u << lane) - 1)) : 0;
+				carry += __popc(m);
+			}
+			big = __any_sync(0xffffffffu, big);
+			for (int o = 16; o > 0; o >>= 1) largest = max(largest, __shfl_xor_sync(0xffffffffu, largest, o));
+			if (lane == 0)
+			{
+				rf.misc[0] = carry;
+				rf.misc[1] = big ? 1 : 0;
+				rf.misc[6] = max(rf.misc[6], largest);
+			}
+		}
+		__syncthreads();
+		if (rf.misc[1])
+		{
+			fail = 3;
+			break;
+		}
+		// first-order generator, own columns (zero inside a cluster and between tail columns)
+		for (int e = tid; e < rf.nown * r; e += SVD_THREADS)
+		{
+			const int jj = e / r, i = e % r, g = rf_col(t, rf, jj);
+			float x = 0.0f;
+			if (i != g && rf.cid[i] != rf.cid[g] && !(rf.tail[i] && rf.tail[g]))
+			{
+				const double den = rf.D[g] - rf.D[i];
+				x = den != 0.0 ? ratio_f32(__ldcg(rf.G + (i64)g * r + i), den) : 2.0f;
+				// should have been an edge (float rounding of the edge test): the FP64 sweeps take over
+				if (fabsf(x) > 4.0f * RF_DELTA) atomicOr(rf.gfail + it, 1);
+			}
+			rf.Xo[jj * r + i] = x;
+			rf.X[(i64)g * r + i] = x;
+		}
+		cluster.sync();
+		lap(7);
+		if (__ldcg(rf.gfail + it))
+		{
+			fail = 4;
+			break;
+		}
+		// F + Fl = X + X^2 / 2 exactly (two-sum) for the own columns ((X^2)_ij = sum_k X_ik X_kj,
+		// X_ik at X + k r + i): the antisymmetric X stays exact in F + Fl
+		for (int e = tid; e < rf.nown * r; e += SVD_THREADS)
+		{
+			const int jj = e / r, i = e % r;
+			const float* xo = rf.Xo + jj * r;
+			float acc = 0.0f;
+			int k = 0;
+			for (; k + 7 < r; k += 8)
+			{
+				float xv[8];
+#pragma unroll
+				for (int u = 0; u < 8; u++) xv[u] = __ldcg(rf.X + (i64)(k + u) * r + i);
+#pragma unroll
+				for (int u = 0; u < 8; u++) acc = fmaf(xv[u], xo[k + u], acc);
+			}
+			for (; k < r; k++) acc = fmaf(__ldcg(rf.X + (i64)k * r + i), xo[k], acc);
+			const float x = xo[i], h = 0.5f * acc;
+			const float sum = x + h, bp = sum - x;
+			rf.F[jj * r + i] = sum;
+			rf.Fl[jj * r + i] = (x - (sum - bp)) + (h - bp);
+		}
+		__syncthreads();
+		rf_update(t, rf, true);
+		cluster.sync();                          // every CTA has read the global copies
+		lap(8);
+		if (rf.misc[0] > 0)
+		{
+			rf_write_own(t, rf, true);
+			cluster.sync();
+			fl += rf_cluster_jacobi(t, rf, cl, rank, tol2);
+			cluster.sync();
+			for (int e = tid; e < rf.nown * (N + r); e += SVD_THREADS)
+			{
+				const int jj = e / (N + r), k = e % (N + r), g = rf_col(t, rf, jj);
+				rf_rec(t, rf, jj)[k] = k < N ? __ldcg(rf.Tr + (i64)k * r + g) : __ldcg(rf.Vr + (i64)(k - N) * r + g);
+			}
+			__syncthreads();
+			lap(9);
+		}
 	}
-	if (tid == 0) flops += 2.0 * ((double)N * r - 0.5 * (double)r * r) * nown;
-	__syncthreads();
-	if (cyc)
-	{
-		cyc[4] += c1 - c0;
-		cyc[5] += clock64() - c1;
-	}
+	if (!converged && fail == 0) fail = 5;
+	iters += 10 * fail + 1000 * min(rf.misc[6], 999);
+	// every CTA has finished reading the global copies before the columns go back (the write-back
+	// after the sweeps reuses the T and V areas)
+	cluster.sync();
+	if (cyc) cyc[0] += clock64() - c1;
+	if (lane == 0) flops += fl;
+	return converged;
 }
 
 __global__ void __launch_bounds__(SVD_THREADS)
 k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
            double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
            double* __restrict__ flops, int cl, int smem_bytes, unsigned long long* __restrict__ phase_ts, int f32_min,
-           int f32_cl)
+           int f32_cl, int refine, double tail2)
 {
 	extern __shared__ __align__(16) double smem[];
 	cg::cluster_group cluster = cg::this_cluster();
@@ -1095,17 +1733,25 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 
 	int A, B;
 	double jflops = 0;                                 // counted by thread 0 (lane 0 of warp 0)
-	long long cyc_acc[6] = {0, 0, 0, 0, 0, 0};         // dots, rotation parameters, rotations, exchanges, FP32, hand-over
+	// FP64 steps (or the refinement), FP64 sweeps, FP32 sweeps, exchanges, FP32 cycles, hand-over cycles;
+	// refinement cycles: Gram matrices, analysis (cosines, tail, clusters, generator), updates, clusters
+	long long cyc_acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 	// counted on the second CTA: the first one holds the last column group, often short or empty
 	const bool count = phase_ts && tid == 0 && rank == (cl > 1 ? 1 : 0);
 	long long* cyc = count ? cyc_acc : nullptr;
-	const bool mixed = f32_min > 0 && r >= f32_min && 8 * precond_doubles(N, cl) <= (i64)smem_bytes;
+	// FP32 sub-cluster: the requested size, or larger until its column groups fit
+	int cf = f32_cl < cl ? f32_cl : cl;
+	while (cf < cl && f32_tour_bytes(N, r, cf) > (i64)smem_bytes) cf *= 2;
+	const bool mixed = f32_min > 0 && r >= f32_min && 8 * refine_doubles(N, cl) <= (i64)smem_bytes &&
+	                   f32_tour_bytes(N, r, cf) <= (i64)smem_bytes;
+	bool refined = false;
+	int rf_iters = 0;
 	if (mixed)
 	{
-		// FP32 sub-cluster: the requested size, or larger until its column groups fit
-		int cf = f32_cl < cl ? f32_cl : cl;
-		while (cf < cl && f32_tour_bytes(N, r, cf) > (i64)smem_bytes) cf *= 2;
-		precondition_f32(cluster, t, smem, xs, M, cl, cf, rank, jflops, cyc);
+		precondition_f32(cluster, t, smem, xs, M, cf, rank, cyc);
+		const double us = __ldcg(xs.misc + 2);
+		refined = finish_mixed(cluster, t, smem, xs, M, cl, rank, refine != 0, (float)(tail2 / (us * us)), jflops, cyc,
+		                       rf_iters);
 	}
 	else
 	{
@@ -1130,7 +1776,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 
 	const float tol2 = (float)((double)N * DBL_EPSILON * (double)N * DBL_EPSILON);
 	int buf = 0, sweep = 0;
-	bool converged = r <= 1;
+	bool converged = r <= 1 || refined;
 	for (; sweep < SVD_MAX_SWEEPS && !converged; sweep++)
 	{
 		round_groups(0, rank, t.nm, A, B);
@@ -1238,6 +1884,8 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 		cyc_acc[1] = sweep;
 		for (int i = 0; i < 6; i++) phase_ts[SVD_PHASE_SLOTS * blk + 4 + i] = (unsigned long long)cyc_acc[i];
 		for (int i = 0; i < 5; i++) phase_ts[SVD_PHASE_SLOTS * blk + 10 + i] = (unsigned long long)qcyc[i];
+		phase_ts[SVD_PHASE_SLOTS * blk + 15] = (unsigned long long)(rf_iters + (mixed && !refined ? 100 : 0));
+		for (int i = 0; i < 4; i++) phase_ts[SVD_PHASE_SLOTS * blk + 16 + i] = (unsigned long long)cyc_acc[6 + i];
 	}
 
 	// ---- 3. outputs: L = Q V (M x r) by the r reflectors applied to [V_c; 0], Rf = P T Sigma^-1 ----
@@ -1646,8 +2294,9 @@ i64 svd_scratch_doubles(int m, int n)
 {
 	const i64 M = m >= n ? m : n, N = m >= n ? n : m;
 	// the larger of the two layouts: global-memory path (W, Q, T, V, nrm, tau, sig, misc, flags +
-	// amax, perm) and shared-memory path (W, T, V, nrm, tau, sig, misc, flags, perm)
-	return 2 * M * N + 2 * N * N + 3 * N + 4 + 2 * SVD_MAX_SWEEPS + (N + 1) / 2 + 1;
+	// amax, perm) and shared-memory path (W, T, V, nrm, tau, sig, misc, flags, perm); then the
+	// refinement's arrays of the mixed path
+	return svd_refine_offset(M, N) + svd_refine_doubles(N);
 }
 
 // smallest rank preconditioned in FP32 (CTGPU_SVD_F32_MIN overrides; 0 disables)
@@ -1673,15 +2322,31 @@ static int svd_f32_cluster()
 	return v;
 }
 
+// FP64 finish of the mixed path by simultaneous refinement before the FP64 sweeps (opt-in,
+// CTGPU_SVD_REFINE=1: experimental; by default the FP64 sweeps start right after T = R^T V)
+static int svd_refine()
+{
+	static const int v = [] {
+		const char* e = getenv("CTGPU_SVD_REFINE");
+		return e ? atoi(e) : 0;
+	}();
+	return v;
+}
+
 static i64 tour_smem_bytes(int M, int N, int cl)
 {
 	const i64 jac = tour_jac_doubles(N, cl);
 	const i64 out = (i64)NWARPS * M;
 	i64 need = jac > out ? jac : out;
-	// FP32 preconditioning, where the rank may reach the threshold and the staging fits
+	// FP32 preconditioning and the refinement, where the rank may reach the threshold and their
+	// arrays fit
 	const int f32 = svd_f32_min();
-	if (f32 > 0 && N >= f32 && 8 * precond_doubles(N, cl) <= SVD_SMEM_LIMIT && precond_doubles(N, cl) > need)
-		need = precond_doubles(N, cl);
+	if (f32 > 0 && N >= f32)
+	{
+		const i64 f32d = (f32_tour_bytes(N, N, std::min(svd_f32_cluster(), cl)) + 7) / 8;
+		const i64 mix = std::max(refine_doubles(N, cl), f32d);
+		if (8 * mix <= SVD_SMEM_LIMIT && mix > need) need = mix;
+	}
 	// distributed QR (clusters of more than one CTA): own columns, norms, reflectors, exchange slots
 	const i64 qr = qr_cluster_doubles(M, N, cl);
 	if (cl > 1 && qr > need) need = qr;
@@ -1746,7 +2411,7 @@ SvdLaunch svd_launch_for(int m, int n, int want, int max_cluster)
 
 void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* descs, const double* a, double* u,
                       double* s, double* vh, double* scratch, int* status, double* flops, cudaStream_t st,
-                      unsigned long long* phase_ts)
+                      unsigned long long* phase_ts, double discard2)
 {
 	if (count <= 0) return;
 	cudaLaunchConfig_t cfg = {};
@@ -1775,7 +2440,7 @@ void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* d
 			CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
 		});
 	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, flops, g.cluster, g.smem,
-	                             phase_ts, svd_f32_min(), svd_f32_cluster()));
+	                             phase_ts, svd_f32_min(), svd_f32_cluster(), svd_refine(), discard2));
 }
 
 }  // namespace ctg

@@ -47,6 +47,23 @@ def test_dmrg_with_package_hamiltonian_matches_oracle(gpu, oracle_port):
     assert same_structure(p1, p2)
 
 
+@pytest.mark.parametrize("L,D,seed", [(10, 8, 268), (14, 8, 71)])
+def test_dmrg_zero_norm_start_state_matches_oracle(gpu, oracle_port, L, D, seed):
+    """A seeded random start state with a site tensor that has no allowed block (mismatching quantum
+    numbers, norm zero): the reference warns and carries on (its right-normalisation leaves
+    isometries), and so must the GPU path. A product with no output block packs no descriptors."""
+    H = hm.fermi_hubbard_1d(L, 1.0, 4.0, 0.0)
+    c = native.random_mps(L, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(L, 0), D, seed)
+    psi0 = cs.read_mps(c)
+    cs.free_mps(c)
+    assert any(len(t.blocks) == 0 for t in psi0.tensors)
+    r1, e1, s1, p1 = run_gpu_dmrg(gpu, H, psi0, 3, 5, 1e-10, D)
+    r2, e2, s2, p2 = run_oracle_dmrg(oracle_port, H, psi0, 3, 5, 1e-10, D)
+    assert r1 == r2 == 0, native.last_error()
+    np.testing.assert_allclose(e1, e2, rtol=0, atol=1e-10)
+    assert same_structure(p1, p2)
+
+
 def test_dmrg_hubbard_L32_D256_matches_oracle(gpu, oracle_port):
     """The headline workload (Fermi-Hubbard L=32, t=1, U=4, (N, 2Sz) = (32, 0), D=256, maxiter 5,
     tol 1e-10, seeded start state 42), two sweeps, against the oracle on the host cores: energies
