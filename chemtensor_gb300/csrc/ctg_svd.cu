@@ -2322,13 +2322,13 @@ static int svd_f32_cluster()
 	return v;
 }
 
-// FP64 finish of the mixed path by simultaneous refinement before the FP64 sweeps (opt-in,
-// CTGPU_SVD_REFINE=1: experimental; by default the FP64 sweeps start right after T = R^T V)
+// FP64 finish of the mixed path by simultaneous refinement, the FP64 sweeps taking over where it
+// does not converge (CTGPU_SVD_REFINE=0: the FP64 sweeps start right after T = R^T V)
 static int svd_refine()
 {
 	static const int v = [] {
 		const char* e = getenv("CTGPU_SVD_REFINE");
-		return e ? atoi(e) : 0;
+		return e ? atoi(e) : 1;
 	}();
 	return v;
 }
