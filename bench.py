@@ -46,7 +46,7 @@ UNIT = "sweeps/s"
 L2_FLUSH_BYTES = 256 << 20
 PRECISIONS = {"fp64": 0, "bf16x3": 1, "tf32": 2, "bf16x6": 3}
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_svd_tour launch (ncu, see profiles/)
-SVD_TRAFFIC_PER_LAUNCH = 379136
+SVD_TRAFFIC_PER_LAUNCH = 481280
 
 
 def build_inputs(host_only: bool = False):
@@ -274,8 +274,8 @@ def bench_gpu(args, world, rank, local):
         "flops_per_launch": svd_flops_per_sweep / max(svd_launches_per_sweep, 1e-9),
         "avg_launch_us": 1e3 * svd_ms_per_sweep / max(svd_launches_per_sweep, 1e-9),
         "traffic": SVD_TRAFFIC_PER_LAUNCH,
-        "traffic_source": "dram read+write of one k_svd_tour launch (one bond's 16-CTA-cluster group, 6 "
-                          "blocks) from profiles/k_svd_tour_hubbard_L32_D256.md",
+        "traffic_source": "dram read+write of one k_svd_tour launch (the 41st of the run: one cluster-size group "
+                          "of a bond, 56 CTAs) from profiles/k_svd_tour_hubbard_L32_D256.md",
         "kernel_share": {k: (v["ms"] / total_prof_ms if total_prof_ms > 0 else 0) for k, v in prof.items()},
         "block_gemm": {"bound": "fp64", "achieved": g_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                        "frac": g_achieved / fp64_peak if fp64_peak > 0 else None, "launches": g["launches"],

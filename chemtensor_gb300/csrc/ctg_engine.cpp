@@ -1155,7 +1155,7 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend, do
 			// of the Jacobi rounds cost more than the extra CTAs save
 			const int ncol = std::min(descs[b].m, descs[b].n);
 			int want = 1;
-			while (want < maxcl && 2 * (2 * want) * 2 <= ncol && work[b] > slack * wmax / maxcl * want) want *= 2;
+			while (want < maxcl && 2 * (2 * (2 * want)) <= ncol && work[b] > slack * wmax / maxcl * want) want *= 2;
 			if (forced) want = forced;
 			cfg[b] = svd_launch_for(descs[b].m, descs[b].n, want, maxcl);
 			total += cfg[b].cluster;

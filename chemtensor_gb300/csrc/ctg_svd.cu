@@ -1572,11 +1572,10 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 			}
 		}
 		__syncthreads();
-		if (rf.misc[1])
-		{
-			fail = 3;
-			break;
-		}
+		// a component larger than RF_CLUSTER_MAX: this iteration's first-order step still converges
+		// every other pair (the large component keeps X = 0 and is not rotated), then the FP64 sweeps
+		// take over from the improved columns
+		if (rf.misc[1]) fail = 3;
 		// first-order generator, own columns (zero inside a cluster and between tail columns)
 		for (int e = tid; e < rf.nown * r; e += SVD_THREADS)
 		{
@@ -1639,6 +1638,7 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 			__syncthreads();
 			lap(9);
 		}
+		if (fail) break;
 	}
 	if (!converged && fail == 0) fail = 5;
 	iters += 10 * fail + 1000 * min(rf.misc[6], 999);
