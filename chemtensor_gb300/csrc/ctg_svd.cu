@@ -47,6 +47,7 @@ constexpr int SVD_SMEM_LIMIT = 220 * 1024;    // dynamic shared memory per CTA (
 constexpr int SVD_F32_SWEEPS = 5;             // most FP32 preconditioning sweeps (more do not save FP64 ones)
 constexpr int SVD_F32_MIN_RANK = 32;          // default: smallest rank preconditioned in FP32
 constexpr int SVD_F32_CLUSTER = 8;            // default: CTAs of the FP32 sweeps
+constexpr int SVD_OUT_RC = 32;                // reflectors staged per round of the output phase
 
 // shared memory (doubles) of the Jacobi tour: two buffers of two column groups (records of 2 N),
 // their norms and the per-step pair data
@@ -1572,10 +1573,13 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 			}
 		}
 		__syncthreads();
-		// a component larger than RF_CLUSTER_MAX: this iteration's first-order step still converges
-		// every other pair (the large component keeps X = 0 and is not rotated), then the FP64 sweeps
-		// take over from the improved columns
-		if (rf.misc[1]) fail = 3;
+		// a component larger than RF_CLUSTER_MAX: the FP64 sweeps take over (applying this iteration's
+		// first-order step to the other pairs first was measured not to save any of their sweeps)
+		if (rf.misc[1])
+		{
+			fail = 3;
+			break;
+		}
 		// first-order generator, own columns (zero inside a cluster and between tail columns)
 		for (int e = tid; e < rf.nown * r; e += SVD_THREADS)
 		{
@@ -1638,7 +1642,6 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 			__syncthreads();
 			lap(9);
 		}
-		if (fail) break;
 	}
 	if (!converged && fail == 0) fail = 5;
 	iters += 10 * fail + 1000 * min(rf.misc[6], 999);
@@ -1891,22 +1894,47 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	// ---- 3. outputs: L = Q V (M x r) by the r reflectors applied to [V_c; 0], Rf = P T Sigma^-1 ----
 	const double unscale = __ldcg(xs.misc + 2);
 	const int kk = N;                                     // min(m, n): width of the factor blocks
+	// one warp per column of V; the reflectors are staged in shared memory SVD_OUT_RC at a time (in
+	// the order they are applied, last first), so the serial chain of each column reads shared
+	// memory instead of L2
 	double* ub = smem + (i64)warp * M;
-	for (int c = rank * NWARPS + warp; c < r; c += cl * NWARPS)
+	// as many reflectors per round as the shared memory holds (at least 4, at most SVD_OUT_RC)
+	const i64 room = ((i64)smem_bytes / 8 - (i64)NWARPS * M - SVD_OUT_RC) / M;
+	const int rc = room < 1 ? 1 : (room > SVD_OUT_RC ? SVD_OUT_RC : (int)room);
+	double* ws = smem + (i64)NWARPS * M;                  // staged reflectors, unit leading entry
+	double* ts = ws + (i64)rc * M;                        // their scalars
+	const int nround = (r + cl * NWARPS - 1) / (cl * NWARPS);
+	for (int round = 0; round < nround; round++)
 	{
-		for (int i = lane; i < M; i += 32) ub[i] = i < r ? __ldcg(xs.V + (i64)c * r + i) : 0.0;
-		__syncwarp();
-		for (int k = r - 1; k >= 0; k--)
+		const int c = rank * NWARPS + warp + round * cl * NWARPS;
+		const bool has = c < r;
+		if (has)
+			for (int i = lane; i < M; i += 32) ub[i] = i < r ? __ldcg(xs.V + (i64)c * r + i) : 0.0;
+		for (int k1 = r - 1; k1 >= 0; k1 -= rc)
 		{
-			const double tk = __ldcg(xs.tau + k);
-			if (tk == 0.0) continue;
-			const double* wk = xs.W + (i64)k * M;
-			double acc = 0;
-			for (int i = k + lane; i < M; i += 32) acc = fma(i == k ? 1.0 : __ldcg(wk + i), ub[i], acc);
-			acc = warp_sum(acc) * tk;
-			for (int i = k + lane; i < M; i += 32) ub[i] -= acc * (i == k ? 1.0 : __ldcg(wk + i));
-			__syncwarp();
+			const int k0 = k1 - rc + 1 > 0 ? k1 - rc + 1 : 0;
+			__syncthreads();
+			for (i64 e = tid; e < (i64)(k1 - k0 + 1) * M; e += SVD_THREADS)
+			{
+				const int k = k0 + (int)(e / M), i = (int)(e % M);
+				ws[e] = i > k ? __ldcg(xs.W + (i64)k * M + i) : (i == k ? 1.0 : 0.0);
+			}
+			for (int e = tid; e <= k1 - k0; e += SVD_THREADS) ts[e] = __ldcg(xs.tau + k0 + e);
+			__syncthreads();
+			if (!has) continue;
+			for (int k = k1; k >= k0; k--)
+			{
+				const double tk = ts[k - k0];
+				if (tk == 0.0) continue;
+				const double* wk = ws + (i64)(k - k0) * M;
+				double acc = 0;
+				for (int i = k + lane; i < M; i += 32) acc = fma(wk[i], ub[i], acc);
+				acc = warp_sum(acc) * tk;
+				for (int i = k + lane; i < M; i += 32) ub[i] -= acc * wk[i];
+				__syncwarp();
+			}
 		}
+		if (!has) continue;
 		const double sc = __ldcg(xs.sig + c);
 		int cnt = 0;
 		for (int c2 = lane; c2 < r; c2 += 32)
@@ -2336,7 +2364,7 @@ static int svd_refine()
 static i64 tour_smem_bytes(int M, int N, int cl)
 {
 	const i64 jac = tour_jac_doubles(N, cl);
-	const i64 out = (i64)NWARPS * M;
+	const i64 out = (i64)(NWARPS + 4) * M + SVD_OUT_RC;     // column buffers, at least 4 staged reflectors
 	i64 need = jac > out ? jac : out;
 	// FP32 preconditioning and the refinement, where the rank may reach the threshold and their
 	// arrays fit
