@@ -636,20 +636,26 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 		// a. warp 0: this CTA's best remaining column and its reflector (speculative)
 		if (warp == 0)
 		{
-			double best = -1;
+			// the squared norms are non-negative doubles, which order like their bit patterns as
+			// signed integers: the argmax compares integers (an FP64 compare costs an FP64 pipe slot)
+			long long bbits = -1;
 			int bi = N, bj = -1;
 			for (int jl = lane; jl < nloc; jl += 32)
-				if (qdone[jl] < 0 && qnrm[jl] > best) { best = qnrm[jl]; bi = rank + cl * jl; bj = jl; }
+			{
+				const long long nb = __double_as_longlong(qnrm[jl]);
+				if (qdone[jl] < 0 && nb > bbits) { bbits = nb; bi = rank + cl * jl; bj = jl; }
+			}
 #pragma unroll
 			for (int o = 16; o > 0; o >>= 1)
 			{
-				const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+				const long long ob = __shfl_xor_sync(0xffffffffu, bbits, o);
 				const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
 				const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
-				if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; bj = oj; }
+				if (ob > bbits || (ob == bbits && oi < bi)) { bbits = ob; bi = oi; bj = oj; }
 			}
+			double best = bbits < 0 ? -1.0 : __longlong_as_double(bbits);
 			double tk = 0.0, beta = 0.0;
-			if (bj >= 0 && best > thresh)
+			if (bj >= 0 && bbits > __double_as_longlong(thresh))
 			{
 				const double* w = qcol + (i64)bj * M;
 				double x2 = 0;
@@ -657,7 +663,7 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 				x2 = warp_sum(x2);
 				const double alpha = w[k];
 				double scl = 0.0;
-				if (x2 == 0.0) beta = alpha;
+				if (__double_as_longlong(x2) == 0) beta = alpha;    // x2 >= +0: its bits are zero only at zero
 				else
 				{
 					// |beta| = sqrt(alpha^2 + x2) >= the remaining norm, above the rank threshold:
@@ -719,19 +725,25 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 			qc[2] += q1 - q0;
 			q0 = q1;
 		}
-		// c. the pivot: every warp reduces the candidates itself (no barrier)
-		double pv = lane < cl ? hnrm[par * 16 + lane] : -1.0;
+		// c. the pivot: every warp reduces the candidates itself (no barrier); a CTA without a
+		// candidate posts -1, every other candidate norm is positive: integer compares of the bits
+		long long pb = -1;
+		if (lane < cl)
+		{
+			const double h = hnrm[par * 16 + lane];
+			pb = h > 0.0 ? __double_as_longlong(h) : -1;
+		}
 		int p = lane < cl ? hidx[par * 16 + lane] : N;
 		int owner = lane;
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1)
 		{
-			const double ov = __shfl_xor_sync(0xffffffffu, pv, o);
+			const long long ob = __shfl_xor_sync(0xffffffffu, pb, o);
 			const int op = __shfl_xor_sync(0xffffffffu, p, o);
 			const int ow = __shfl_xor_sync(0xffffffffu, owner, o);
-			if (ov > pv || (ov == pv && op < p)) { pv = ov; p = op; owner = ow; }
+			if (ob > pb || (ob == pb && op < p)) { pb = ob; p = op; owner = ow; }
 		}
-		if (pv <= thresh || pv <= 0.0 || p >= N) break;
+		if (pb <= __double_as_longlong(thresh) || pb <= 0 || p >= N) break;
 		const double tk = htau[par * 16 + owner];
 		const double* vbuf = cand + ((i64)par * cl + owner) * M;
 		// the owner stores R_kk and the reflector in place (the updates below skip that column)
@@ -758,7 +770,7 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 		{
 			if (jl == pjl || qdone[jl] >= 0) continue;
 			double* w = qcol + (i64)jl * M;
-			if (tk != 0.0)
+			if (__double_as_longlong(tk) != 0)               // tk >= +0
 			{
 				double acc = 0;
 				for (int i = k + lane; i < M; i += 32) acc = fma(vbuf[i], w[i], acc);
