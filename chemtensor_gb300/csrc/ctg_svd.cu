@@ -304,7 +304,10 @@ __device__ __forceinline__ bool rotation_params(double al, double be, double ga,
                                                 double& t, float& c2)
 {
 	c2 = 0.0f;
-	if (ga == 0.0) return false;
+	// zero and sign tests on the bit patterns: an FP64 compare would take an FP64 pipe slot on the
+	// serial chain of every step
+	const long long gbits = __double_as_longlong(ga);
+	if ((gbits & 0x7fffffffffffffffll) == 0) return false;
 	int ea, eb, eg;
 	const float ma = mant_exp(al, ea), mb = mant_exp(be, eb), mg = mant_exp(ga, eg);
 	const int k2 = 2 * eg - ea - eb;
@@ -316,10 +319,11 @@ __device__ __forceinline__ bool rotation_params(double al, double be, double ga,
 	}
 	else c2 = 1.0f;
 	const double dl = be - al;
-	const bool neg = (dl < 0.0) != (ga < 0.0);
+	const long long dbits = __double_as_longlong(dl);
+	const bool neg = (dbits < 0) != (gbits < 0);
 	float tm, taum;
 	int te = 0;
-	if (dl == 0.0)
+	if ((dbits & 0x7fffffffffffffffll) == 0)
 	{
 		tm = 1.0f;
 		taum = 0.41421356f;
@@ -362,7 +366,7 @@ __device__ __forceinline__ bool rotation_params(double al, double be, double ga,
 	const double e = fma(-q, d0, 1.0);
 	const double w = fma(d0, fma(e, e, e), d0);
 	sn = make_double(taum + taum, te) * w;
-	return sn != 0.0;
+	return (__double_as_longlong(sn) & 0x7fffffffffffffffll) != 0;
 }
 
 struct Tour {
@@ -394,7 +398,7 @@ __device__ __forceinline__ bool step_pair(const Tour& t, int mode, int step, int
 // three-shear rotation of the two records (T entries 0 .. N-1, V entries N .. N+r-1). One CTA
 // barrier per step, and the warps of different pairs run on different SM sub-partitions.
 __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, int cB, int npad, float tol2, const StepBuf& sb,
-                            long long* cyc, double& flops)
+                            long long* cyc, long long& flops)
 {
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const long long c0 = cyc ? clock64() : 0;
@@ -419,7 +423,7 @@ __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, 
 		// column records per rotation (counted on lane 0 of each warp)
 		if (lane == 0)
 		{
-			flops += 2.0 * t.N;
+			flops += 2 * t.N;                    // integer: no FP64 slot on the chain
 			atomicMax(sb.max_c2, __float_as_int(c2));
 		}
 		if (rot)
@@ -437,7 +441,7 @@ __device__ void jacobi_step(const Tour& t, int buf, int mode, int step, int cA, 
 				*pa = fma(-tn, g, al);
 				*pb = fma(tn, g, be);
 				*sb.local_rot = 1;
-				flops += 6.0 * len;
+				flops += 6 * len;
 			}
 		}
 	}
@@ -501,9 +505,12 @@ __device__ void jacobi_step32(const Tour32& t, int buf, int mode, int step, int 
 		const float al = *pa, be = *pb;
 		if (g != 0.0f && g * g > tol2 * al * be)
 		{
-			const float zeta = (be - al) / (2.0f * g);
+			// single-instruction approximations: the FP32 angle needs FP32 accuracy only (the FP64
+			// finish removes what is left), and the IEEE division and square root sequences sit on
+			// the serial chain of every step
+			const float zeta = __fdividef(be - al, 2.0f * g);
 			const float az = fabsf(zeta);
-			float tn = az > 1e10f ? 0.5f / az : 1.0f / (az + sqrtf(fmaf(az, az, 1.0f)));
+			float tn = az > 1e10f ? __fdividef(0.5f, az) : __fdividef(1.0f, az + sqrt_approx(fmaf(az, az, 1.0f)));
 			tn = copysignf(tn, zeta);
 			const float c = rsqrtf(fmaf(tn, tn, 1.0f));
 			const float sn = c * tn;
@@ -1747,7 +1754,8 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	sb.max_c2 = sb.local_rot + 1;
 
 	int A, B;
-	double jflops = 0;                                 // counted by thread 0 (lane 0 of warp 0)
+	double jflops = 0;                                 // counted on lane 0 of every warp
+	long long jsteps = 0;                              // the FP64 sweeps' share, as an integer
 	// FP64 steps (or the refinement), FP64 sweeps, FP32 sweeps, exchanges, FP32 cycles, hand-over cycles;
 	// refinement cycles: Gram matrices, analysis (cosines, tail, clusters, generator), updates, clusters
 	long long cyc_acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -1821,9 +1829,9 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			if (rho == 0)
 			{
 				const int npad = t.bs + (t.bs & 1);
-				for (int st = 0; st < npad - 1; st++) jacobi_step(t, buf, 0, st, cA, cB, npad, tol2, sb, cyc, jflops);
+				for (int st = 0; st < npad - 1; st++) jacobi_step(t, buf, 0, st, cA, cB, npad, tol2, sb, cyc, jsteps);
 			}
-			for (int st = 0; st < t.bs; st++) jacobi_step(t, buf, 1, st, cA, cB, 0, tol2, sb, cyc, jflops);
+			for (int st = 0; st < t.bs; st++) jacobi_step(t, buf, 1, st, cA, cB, 0, tol2, sb, cyc, jsteps);
 			if (cl > 1)
 			{
 				const long long cx = cyc ? clock64() : 0;
@@ -1886,6 +1894,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			if (lane == 0) xs.sig[x * t.bs + c] = sqrt(acc);
 		}
 	}
+	jflops += (double)jsteps;
 	if (lane == 0 && jflops > 0) atomicAdd(flops, jflops);
 	if (rank == 0 && tid == 0)
 	{
