@@ -549,6 +549,22 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 	for (int k = 0; k < NUM_TILE_CLASSES; k++) ntiles += tiles[k].size();
 	p.tiles.reserve(ntiles);
 	for (int k = 0; k < NUM_TILE_CLASSES; k++) p.tiles.insert(p.tiles.end(), tiles[k].begin(), tiles[k].end());
+	if (is_tc_precision(precision) && !p.tiles.empty())
+	{
+		// the persistent tensor-core kernel takes tiles in list order, one per CTA at a time: tiles
+		// whose outputs start from the same B block and cover the same column range are put next to
+		// each other, so that the CTAs running them at the same time read those B records from L2
+		// (output blocks of one column sector meet the same B blocks, one per block of A)
+		auto first_b = [&](const GemmTile& t) -> i64 {
+			const GemmOut& o = outs[(size_t)t.out];
+			return o.nc > 0 ? tcons[(size_t)o.c0].b_rec : -1;    // an output without contributions: zero tiles first
+		};
+		std::stable_sort(p.tiles.begin(), p.tiles.end(), [&](const GemmTile& x, const GemmTile& y) {
+			const i64 bx = first_b(x), by = first_b(y);
+			if (bx != by) return bx < by;
+			return x.n0 < y.n0;
+		});
+	}
 	p.outs = std::move(outs);
 	p.cons = std::move(cons);
 	p.splits = std::move(splits);
