@@ -1139,9 +1139,18 @@ __device__ double rf_gram(const Tour& t, const Refine& rf, const double* Ar, int
 		const bool valid = i < r && i <= g;
 		const double* rec = rf_rec(t, rf, jj) + off;
 		const double* a = Ar + (valid ? i : 0);
-		// eight loads in flight per thread (a warp reads 32 consecutive doubles of a row per load)
+		// sixteen loads in flight per thread (a warp reads 32 consecutive doubles of a row per load):
+		// the loop is bound by L2 latency, not by the FP64 pipe
 		double acc[4] = {0.0, 0.0, 0.0, 0.0};
 		int k = 0;
+		for (; k + 15 < len; k += 16)
+		{
+			double x[16];
+#pragma unroll
+			for (int u = 0; u < 16; u++) x[u] = __ldcg(a + (i64)(k + u) * r);
+#pragma unroll
+			for (int u = 0; u < 16; u++) acc[u & 3] = fma(x[u], rec[k + u], acc[u & 3]);
+		}
 		for (; k + 7 < len; k += 8)
 		{
 			double x[8];
@@ -1182,7 +1191,7 @@ __device__ void rf_update(const Tour& t, const Refine& rf, bool with_t)
 		for (int q = 0; q < JB; q++) sh[q] = sl[q] = 0.0f;
 		const int j0 = b * JB;
 		const int nj = min(JB, rf.nown - j0);
-#pragma unroll 4
+#pragma unroll 8
 		for (int i = 0; i < r; i++)
 		{
 			const float2 v = __ldcg(h + (i64)i * ld);
@@ -1410,7 +1419,7 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 				const double* v1 = rf_rec(t, rf, j0 + min(1, nj - 1)) + N;
 				const double* v2 = rf_rec(t, rf, j0 + min(2, nj - 1)) + N;
 				const double* v3 = rf_rec(t, rf, j0 + min(3, nj - 1)) + N;
-#pragma unroll 4
+#pragma unroll 8
 				for (int k = 0; k <= kmax; k++)
 				{
 					const double w = __ldcg(wi + k);
@@ -1623,25 +1632,50 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 		}
 		// F + Fl = X + X^2 / 2 exactly (two-sum) for the own columns ((X^2)_ij = sum_k X_ik X_kj,
 		// X_ik at X + k r + i): the antisymmetric X stays exact in F + Fl
-		for (int e = tid; e < rf.nown * r; e += SVD_THREADS)
+		// one thread per row i and up to XB own columns at a time: each entry X_ik is loaded once
+		// for all of them (eight loads in flight)
 		{
-			const int jj = e / r, i = e % r;
-			const float* xo = rf.Xo + jj * r;
-			float acc = 0.0f;
-			int k = 0;
-			for (; k + 7 < r; k += 8)
+			constexpr int XB = 8;
+			const int nb = (rf.nown + XB - 1) / XB;
+			for (int e = tid; e < nb * r; e += SVD_THREADS)
 			{
-				float xv[8];
+				const int b = e / r, i = e % r, j0 = b * XB, nj = min(XB, rf.nown - j0);
+				float acc[XB];
 #pragma unroll
-				for (int u = 0; u < 8; u++) xv[u] = __ldcg(rf.X + (i64)(k + u) * r + i);
+				for (int q = 0; q < XB; q++) acc[q] = 0.0f;
+				int k = 0;
+				for (; k + 7 < r; k += 8)
+				{
+					float xv[8];
 #pragma unroll
-				for (int u = 0; u < 8; u++) acc = fmaf(xv[u], xo[k + u], acc);
+					for (int u = 0; u < 8; u++) xv[u] = __ldcg(rf.X + (i64)(k + u) * r + i);
+#pragma unroll
+					for (int q = 0; q < XB; q++)
+						if (q < nj)
+						{
+							const float* xo = rf.Xo + (j0 + q) * r + k;
+#pragma unroll
+							for (int u = 0; u < 8; u++) acc[q] = fmaf(xv[u], xo[u], acc[q]);
+						}
+				}
+				for (; k < r; k++)
+				{
+					const float xv = __ldcg(rf.X + (i64)k * r + i);
+#pragma unroll
+					for (int q = 0; q < XB; q++)
+						if (q < nj) acc[q] = fmaf(xv, rf.Xo[(j0 + q) * r + k], acc[q]);
+				}
+#pragma unroll
+				for (int q = 0; q < XB; q++)
+					if (q < nj)
+					{
+						const int jj = j0 + q;
+						const float x = rf.Xo[jj * r + i], h = 0.5f * acc[q];
+						const float sum = x + h, bp = sum - x;
+						rf.F[jj * r + i] = sum;
+						rf.Fl[jj * r + i] = (x - (sum - bp)) + (h - bp);
+					}
 			}
-			for (; k < r; k++) acc = fmaf(__ldcg(rf.X + (i64)k * r + i), xo[k], acc);
-			const float x = xo[i], h = 0.5f * acc;
-			const float sum = x + h, bp = sum - x;
-			rf.F[jj * r + i] = sum;
-			rf.Fl[jj * r + i] = (x - (sum - bp)) + (h - bp);
 		}
 		__syncthreads();
 		rf_update(t, rf, true);
@@ -1672,7 +1706,7 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 	return converged;
 }
 
-__global__ void __launch_bounds__(SVD_THREADS)
+__global__ void __launch_bounds__(SVD_THREADS, 1)
 k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
            double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
            double* __restrict__ flops, int cl, int smem_bytes, unsigned long long* __restrict__ phase_ts, int f32_min,
