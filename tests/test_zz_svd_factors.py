@@ -72,3 +72,42 @@ def test_svd_factors_preconditioned_ranks(gpu, m, n, kind):
     r = int(np.sum(s > 1e-13 * s[0]))
     np.testing.assert_allclose(u[:, :r].T @ u[:, :r], np.eye(r), rtol=0, atol=1e-12)
     np.testing.assert_allclose(vh[:r] @ vh[:r].T, np.eye(r), rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("seed", range(4))
+@pytest.mark.parametrize("m,n,kind", [
+    (112, 112, "clustered"), (128, 120, "graded"), (150, 140, "clustered"), (100, 96, "clustered"),
+    (140, 150, "graded"),
+])
+def test_svd_factors_seeded_spectra(gpu, seed, m, n, kind):
+    """More seeds of the graded and four-fold clustered spectra (the refinement finish, its exact
+    cluster rotations and the FP64 sweeps it hands over to): orthonormal factors, reconstruction
+    and the retained singular values at the same bars."""
+    torch = pytest.importorskip("torch")
+    fn = gpu.ctgpu_dense_svd_noalloc
+    fn.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    rng = np.random.default_rng(seed * 7919 + m * 1000 + n)
+    a = _spectrum(rng, m, n, kind)
+    k = min(m, n)
+    d_a = torch.from_numpy(a).to(dev)
+    d_u = torch.zeros((m * k,), dtype=torch.float64, device=dev)
+    d_s = torch.zeros((k,), dtype=torch.float64, device=dev)
+    d_vh = torch.zeros((k * n,), dtype=torch.float64, device=dev)
+    d_info = torch.full((1,), 7, dtype=torch.int32, device=dev)
+    assert fn(d_a.data_ptr(), m, n, d_u.data_ptr(), d_s.data_ptr(), d_vh.data_ptr(), d_info.data_ptr(),
+              stream.cuda_stream) == 0
+    torch.cuda.synchronize(dev)
+    assert int(d_info.item()) == 0
+    s = d_s.cpu().numpy()
+    u = d_u.cpu().numpy().reshape(m, k)
+    vh = d_vh.cpu().numpy().reshape(k, n)
+    ref = np.linalg.svd(a, compute_uv=False)
+    big = ref > 1e-6 * ref[0]
+    np.testing.assert_allclose(s[big], ref[big], rtol=1e-10)
+    np.testing.assert_allclose((u * s) @ vh, a, rtol=0, atol=1e-12 * np.abs(a).max())
+    r = int(np.sum(s > 1e-13 * s[0]))
+    np.testing.assert_allclose(u[:, :r].T @ u[:, :r], np.eye(r), rtol=0, atol=1e-12)
+    np.testing.assert_allclose(vh[:r] @ vh[:r].T, np.eye(r), rtol=0, atol=1e-12)
