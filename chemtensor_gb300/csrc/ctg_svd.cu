@@ -44,7 +44,9 @@ constexpr int SVD_THREADS = 256;
 constexpr int NWARPS = SVD_THREADS / 32;
 constexpr int SVD_STEP_PAIRS = 32;            // most column pairs of one inner step (group size <= 32)
 constexpr int SVD_SMEM_LIMIT = 220 * 1024;    // dynamic shared memory per CTA (227 KB less static use)
-constexpr int SVD_F32_SWEEPS = 5;             // most FP32 preconditioning sweeps (more do not save FP64 ones)
+constexpr int SVD_F32_SWEEPS = 5;             // default: most FP32 preconditioning sweeps
+constexpr int SVD_F32_SWEEPS_MAX = 8;         // capacity of the FP32 sweep flags
+constexpr float SVD_F32_COS = 0.0f;           // default: FP32 sweeps rotate every pair above N eps_32
 constexpr int SVD_F32_MIN_RANK = 32;          // default: smallest rank preconditioned in FP32
 constexpr int SVD_F32_CLUSTER = 8;            // default: CTAs of the FP32 sweeps
 constexpr int SVD_OUT_RC = 32;                // reflectors staged per round of the output phase
@@ -555,25 +557,26 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 	x.flags = (int*)(x.misc + 4);
 	x.perm = x.flags + SVD_MAX_SWEEPS;
 	x.flags32 = x.perm + N;
-	x.cmax = x.flags32 + SVD_F32_SWEEPS;
+	x.cmax = x.flags32 + SVD_F32_SWEEPS_MAX;
 	x.G = base + svd_refine_offset(M, N);
 	return x;
 }
 
 // Householder QR with column pivoting of the scaled block over a whole cluster. Column j lives in
 // the shared memory of CTA j % cl; columns are not moved. Every step the first warp of each CTA
-// picks the CTA's best remaining column and forms its reflector (speculatively: only the pivot's
-// is used); the CTA writes that reflector and the column's squared norm, index and reflector
-// scalars into every CTA's shared memory (distributed shared memory, double-buffered by step
-// parity). After one cluster barrier every CTA holds all candidates, agrees on the pivot (largest
-// norm, then smallest index) and applies its reflector to its own remaining columns, downdating
+// picks the CTA's best remaining column and forms its reflector in its own shared memory
+// (speculatively: only the pivot's is used); the CTA writes the column's squared norm, index and
+// reflector scalars into every CTA's shared memory (distributed shared memory, double-buffered by
+// step parity). After one cluster barrier every CTA holds all candidates' scalars, agrees on the
+// pivot (largest norm, then smallest index), reads the pivot's reflector from the CTA that formed
+// it, and applies it to its own remaining columns, downdating
 // the norms (recomputed when cancellation has eaten more than sqrt(eps) of the last exact value,
 // as in qr_pivoted_cta).
 // Its shared memory (doubles):
 __host__ __device__ inline i64 qr_cluster_doubles(int M, int N, int cl)
 {
 	const i64 nloc = (N + cl - 1) / cl;
-	return nloc * M + 2 * nloc + 2 * (i64)cl * M + M + 16 + 3 * 2 * 16 + (2 * 16 + nloc + 1) / 2 + 8;
+	return nloc * M + 2 * nloc + 3 * (i64)M + 16 + 3 * 2 * 16 + (2 * 16 + nloc + 1) / 2 + 8;
 }
 
 __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, const double* ab, bool tall, int n, int M, int N,
@@ -586,9 +589,9 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 	double* qcol = smem;                                 // nloc_max x M
 	double* qnrm = qcol + (i64)nloc_max * M;
 	double* qref = qnrm + nloc_max;
-	double* cand = qref + nloc_max;                      // [2][cl][M] candidate reflectors of all CTAs
-	double* cbuf = cand + 2 * (i64)cl * M;               // [M] own candidate reflector
-	double* part = cbuf + M;                             // [cl] partial Frobenius sums
+	double* cand = qref + nloc_max;                      // [2][M] own candidate reflector, by step parity
+	double* vloc = cand + 2 * (i64)M;                    // [M] the pivot's reflector, fetched from its CTA
+	double* part = vloc + M;                             // [cl] partial Frobenius sums
 	double* hnrm = part + 16;                            // [2][16] candidate squared norm per CTA
 	double* htau = hnrm + 32;                            // [2][16] candidate tau per CTA
 	double* hbeta = htau + 32;                           // [2][16] candidate beta per CTA
@@ -639,6 +642,7 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 	for (int k = 0; k < N; k++)
 	{
 		const int par = k & 1;
+		double* cbuf = cand + (i64)par * M;
 		long long q0 = qc ? clock64() : 0;
 		// a. warp 0: this CTA's best remaining column and its reflector (speculative)
 		if (warp == 0)
@@ -701,17 +705,11 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 			qc[0] += q1 - q0;
 			q0 = q1;
 		}
-		// b. the candidate into every CTA's shared memory
+		// b. the candidate's norm, column and scalars into every CTA's shared memory; its reflector
+		// stays here (cand[par]) and only the winner's is read, after the barrier. cand[par] is
+		// written again two steps later, after the next step's barrier, which every CTA reaches
+		// only once it has read this step's pivot.
 		const double best = sh_best;
-		if (best > 0.0)
-		{
-			const int len = M - k;
-			for (int e = tid; e < len * cl; e += SVD_THREADS)
-			{
-				const int dst = e / len, i = k + (e - dst * len);
-				*cluster.map_shared_rank(cand + ((i64)par * cl + rank) * M + i, (unsigned)dst) = cbuf[i];
-			}
-		}
 		if (tid < cl)
 		{
 			*cluster.map_shared_rank(hnrm + par * 16 + rank, (unsigned)tid) = best;
@@ -752,7 +750,14 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 		}
 		if (pb <= __double_as_longlong(thresh) || pb <= 0 || p >= N) break;
 		const double tk = htau[par * 16 + owner];
-		const double* vbuf = cand + ((i64)par * cl + owner) * M;
+		const double* vbuf = cbuf;
+		if (owner != rank)                                   // uniform in the CTA
+		{
+			const double* src = cluster.map_shared_rank(cbuf, (unsigned)owner);
+			for (int i = k + tid; i < M; i += SVD_THREADS) vloc[i] = src[i];
+			vbuf = vloc;
+			__syncthreads();
+		}
 		// the owner stores R_kk and the reflector in place (the updates below skip that column)
 		const int pjl = owner == rank ? p / cl : -1;
 		if (pjl >= 0)
@@ -836,7 +841,7 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 // cost is latency and barriers, not arithmetic, and fewer, larger groups need fewer rounds. On
 // return, V (r x r, orthogonal to FP32 accuracy, column g at xs.V + g r) is in global memory.
 __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, double* smem, const SvdScratch& xs, int M,
-                                 int cf, int rank, long long* cyc)
+                                 int cf, int rank, int nsw, float cos_min, long long* cyc)
 {
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 	const long long c0 = cyc ? clock64() : 0;
@@ -871,9 +876,9 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 			}
 		}
 		__syncthreads();
-		const float tol2 = (float)N * FLT_EPSILON * (float)N * FLT_EPSILON;
-		int buf = 0, done32 = SVD_F32_SWEEPS;
-		for (int sweep = 0; sweep < SVD_F32_SWEEPS; sweep++)
+		const float tol2 = fmaxf((float)N * FLT_EPSILON * (float)N * FLT_EPSILON, cos_min * cos_min);
+		int buf = 0, done32 = nsw;
+		for (int sweep = 0; sweep < nsw; sweep++)
 		{
 			round_groups(0, rank, f.nm, A, B);
 			for (int slot = 0; slot < 2; slot++)
@@ -950,7 +955,7 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 	else if (cf > 1)
 	{
 		// the barriers of the working CTAs' rounds, and their convergence decision
-		for (int sweep = 0; sweep < SVD_F32_SWEEPS; sweep++)
+		for (int sweep = 0; sweep < nsw; sweep++)
 		{
 			for (int rho = 0; rho < f.nm; rho++) cluster.sync();
 			if (__ldcg(xs.flags32 + sweep) == 0) break;
@@ -1710,7 +1715,7 @@ __global__ void __launch_bounds__(SVD_THREADS, 1)
 k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restrict__ a, double* __restrict__ u,
            double* __restrict__ s, double* __restrict__ vh, double* __restrict__ scratch, int* __restrict__ status,
            double* __restrict__ flops, int cl, int smem_bytes, unsigned long long* __restrict__ phase_ts, int f32_min,
-           int f32_cl, int refine, double tail2)
+           int f32_cl, int refine, double tail2, int f32_sweeps, float f32_cos)
 {
 	extern __shared__ __align__(16) double smem[];
 	cg::cluster_group cluster = cg::this_cluster();
@@ -1725,7 +1730,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	const double* ab = a + d.a_off;
 
 	for (int e = rank * SVD_THREADS + tid; e < SVD_MAX_SWEEPS; e += cl * SVD_THREADS) xs.flags[e] = 0;
-	for (int e = rank * SVD_THREADS + tid; e < SVD_F32_SWEEPS; e += cl * SVD_THREADS) xs.flags32[e] = 0;
+	for (int e = rank * SVD_THREADS + tid; e < SVD_F32_SWEEPS_MAX; e += cl * SVD_THREADS) xs.flags32[e] = 0;
 	for (int e = rank * SVD_THREADS + tid; e < SVD_MAX_SWEEPS; e += cl * SVD_THREADS) xs.cmax[e] = 0;
 	const bool stamp = phase_ts && rank == 0 && tid == 0;
 	if (stamp) phase_ts[SVD_PHASE_SLOTS * blk] = globaltimer();
@@ -1805,7 +1810,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	int rf_iters = 0;
 	if (mixed)
 	{
-		precondition_f32(cluster, t, smem, xs, M, cf, rank, cyc);
+		precondition_f32(cluster, t, smem, xs, M, cf, rank, f32_sweeps, f32_cos, cyc);
 		const double us = __ldcg(xs.misc + 2);
 		refined = finish_mixed(cluster, t, smem, xs, M, cl, rank, refine != 0, (float)(tail2 / (us * us)), jflops, cyc,
 		                       rf_iters);
@@ -2405,6 +2410,28 @@ static int svd_f32_cluster()
 	return v;
 }
 
+// most FP32 preconditioning sweeps (CTGPU_SVD_F32_SWEEPS overrides, 1 to SVD_F32_SWEEPS_MAX)
+static int svd_f32_sweeps()
+{
+	static const int v = [] {
+		const char* e = getenv("CTGPU_SVD_F32_SWEEPS");
+		const int k = e ? atoi(e) : SVD_F32_SWEEPS;
+		return k < 1 ? 1 : (k > SVD_F32_SWEEPS_MAX ? SVD_F32_SWEEPS_MAX : k);
+	}();
+	return v;
+}
+
+// cosine below which the FP32 sweeps leave a pair alone, if above N eps_32 (CTGPU_SVD_F32_COS
+// overrides; default SVD_F32_COS)
+static float svd_f32_cos()
+{
+	static const float v = [] {
+		const char* e = getenv("CTGPU_SVD_F32_COS");
+		return e ? (float)atof(e) : SVD_F32_COS;
+	}();
+	return v;
+}
+
 // FP64 finish of the mixed path by simultaneous refinement, the FP64 sweeps taking over where it
 // does not converge (CTGPU_SVD_REFINE=0: the FP64 sweeps start right after T = R^T V)
 static int svd_refine()
@@ -2523,7 +2550,8 @@ void launch_svd_group(const SvdLaunch& g, int first, int count, const SvdDesc* d
 			CTG_CUDA(cudaFuncSetAttribute(k_svd_tour, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
 		});
 	CTG_CUDA(cudaLaunchKernelEx(&cfg, k_svd_tour, descs, first, a, u, s, vh, scratch, status, flops, g.cluster, g.smem,
-	                             phase_ts, svd_f32_min(), svd_f32_cluster(), svd_refine(), discard2));
+	                             phase_ts, svd_f32_min(), svd_f32_cluster(), svd_refine(), discard2, svd_f32_sweeps(),
+	                             svd_f32_cos()));
 }
 
 }  // namespace ctg
