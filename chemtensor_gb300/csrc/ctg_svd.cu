@@ -907,6 +907,7 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 				for (int st = 0; st < f.bs; st++) jacobi_step32(f, buf, 1, st, cA, cB, 0, tol2, local_rot);
 				if (cf > 1)
 				{
+					const long long cx = cyc ? clock64() : 0;
 					if (tid == 0 && rho == f.nm - 1 && *local_rot) atomicOr(xs.flags32 + sweep, 1);
 					const int rho1 = (rho + 1) % f.nm;
 					for (int slot = 0; slot < 2; slot++)
@@ -923,6 +924,7 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 					}
 					cluster.sync();
 					buf ^= 1;
+					if (cyc) cyc[10] += clock64() - cx;
 				}
 			}
 			bool conv;
@@ -1797,7 +1799,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	long long jsteps = 0;                              // the FP64 sweeps' share, as an integer
 	// FP64 steps (or the refinement), FP64 sweeps, FP32 sweeps, exchanges, FP32 cycles, hand-over cycles;
 	// refinement cycles: Gram matrices, analysis (cosines, tail, clusters, generator), updates, clusters
-	long long cyc_acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+	long long cyc_acc[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 	// counted on the second CTA: the first one holds the last column group, often short or empty
 	const bool count = phase_ts && tid == 0 && rank == (cl > 1 ? 1 : 0);
 	long long* cyc = count ? cyc_acc : nullptr;
@@ -1949,6 +1951,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 		for (int i = 0; i < 5; i++) phase_ts[SVD_PHASE_SLOTS * blk + 10 + i] = (unsigned long long)qcyc[i];
 		phase_ts[SVD_PHASE_SLOTS * blk + 15] = (unsigned long long)(rf_iters + (mixed && !refined ? 100 : 0));
 		for (int i = 0; i < 4; i++) phase_ts[SVD_PHASE_SLOTS * blk + 16 + i] = (unsigned long long)cyc_acc[6 + i];
+		phase_ts[SVD_PHASE_SLOTS * blk + 20] = (unsigned long long)cyc_acc[10];
 	}
 
 	// ---- 3. outputs: L = Q V (M x r) by the r reflectors applied to [V_c; 0], Rf = P T Sigma^-1 ----
