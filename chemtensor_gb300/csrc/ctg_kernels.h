@@ -256,6 +256,11 @@ struct LanczosScalars {
 // fixed grid of the cooperative Lanczos kernels (deterministic reductions): one block of 512 threads
 // per SM, so that each grid barrier has 152 participants and each block sums 152 partials
 constexpr int RED_BLOCKS = 152;
+// shared scratch (doubles) of the one-warp tridiagonal eigensolver
+constexpr int TRIDIAG_SCRATCH = 9 * LANCZOS_MAX;
+// vectors of up to this many doubles take the cluster form of the Lanczos kernels (one
+// thread-block cluster, cluster barriers) instead of the cooperative grid form
+constexpr i64 LZ_CLUSTER_MAX_N = (i64)1 << 19;
 
 // one cooperative launch each (partial: 2 RED_BLOCKS doubles): a whole Lanczos step
 // (alpha; unless last: orthogonalisation, beta and the early exit, next vector), and the start

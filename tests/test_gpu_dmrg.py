@@ -47,6 +47,47 @@ def test_dmrg_with_package_hamiltonian_matches_oracle(gpu, oracle_port):
     assert same_structure(p1, p2)
 
 
+_GRID_FORM_SCRIPT = r"""
+import json, sys
+sys.path.insert(0, "tests")
+from chemtensor_gb300 import ctstructs as cs, hamiltonians as hm, native
+from helpers import run_gpu_dmrg
+H = hm.fermi_hubbard_1d(16, 1.0, 4.0, 0.0)
+c = native.random_mps(16, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(16, 0), 64, 42)
+psi0 = cs.read_mps(c)
+cs.free_mps(c)
+ret, en, ent, psi = run_gpu_dmrg(native.lib(), H, psi0, 2, 5, 1e-10, 64)
+print(json.dumps({"ret": ret, "en": list(en), "ent": list(ent)}))
+"""
+
+
+def test_lanczos_grid_and_cluster_forms_match_oracle(gpu, oracle_port):
+    """The Lanczos vector kernels run as one thread-block cluster for vectors that fit and as a
+    cooperative grid otherwise: the same solve with every vector forced onto the grid form (in a
+    child process, CTGPU_LZ_CLUSTER_MAX_N=0) and with the default choice (cluster form at this size)
+    both match the oracle."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, CTGPU_LZ_CLUSTER_MAX_N="0")
+    r = subprocess.run([sys.executable, "-c", _GRID_FORM_SCRIPT], cwd=root, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    grid = json.loads(r.stdout.strip().splitlines()[-1])
+    H = hm.fermi_hubbard_1d(16, 1.0, 4.0, 0.0)
+    c = native.random_mps(16, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(16, 0), 64, 42)
+    psi0 = cs.read_mps(c)
+    cs.free_mps(c)
+    r1, e1, s1, _ = run_gpu_dmrg(gpu, H, psi0, 2, 5, 1e-10, 64)
+    r2, e2, s2, _ = run_oracle_dmrg(oracle_port, H, psi0, 2, 5, 1e-10, 64)
+    assert r1 == 0 and r2 == 0 and grid["ret"] == 0
+    np.testing.assert_allclose(e1, e2, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(grid["en"], e2, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(grid["ent"], s2, rtol=0, atol=1e-8)
+
+
 @pytest.mark.parametrize("L,D,seed", [(10, 8, 268), (14, 8, 71)])
 def test_dmrg_zero_norm_start_state_matches_oracle(gpu, oracle_port, L, D, seed):
     """A seeded random start state with a site tensor that has no allowed block (mismatching quantum

@@ -2,7 +2,9 @@
 
 The reference diagonalises the k x k Lanczos matrix with dsteqr (src/util/krylov.c:230) and keeps
 the lowest eigenpair; the GPU path solves for that pair on one warp (FP32 Sturm multisection, FP64
-Newton on the last LDL^T pivot, eigenvector by back-substitution), fused into the last Lanczos step.
+Newton on the characteristic polynomial, eigenvector of the twisted factorisation from the leading
+and trailing minors, or from the LDL^T pivots where the minors leave their range), fused into the
+last Lanczos step.
 Lowest eigenvalue within 1e-13 of ||T||, eigenvector within 1e-12 (up to the sign convention:
 largest-magnitude component positive).
 """
@@ -72,6 +74,17 @@ def test_tridiag_wilkinson(gpu):
     a = np.abs(np.arange(-10, 11)).astype(np.float64)
     b = np.ones(20)
     _check(gpu, a, b)
+
+
+@pytest.mark.parametrize("scale", [1e7, 1e-7])
+def test_tridiag_pivot_form_beyond_the_minor_range(gpu, scale):
+    """Spreads whose leading minors leave [2^-600, 2^600] at k = 32: the solver takes its pivot form
+    (LDL^T pivots) instead of the minors, with the same accuracy."""
+    for seed in range(3):
+        rng = np.random.default_rng(7000 + seed)
+        a = rng.standard_normal(32) * scale
+        b = np.abs(rng.standard_normal(31)) * scale + 1e-3 * scale
+        _check(gpu, a, b)
 
 
 def test_tridiag_rejects_bad_size(gpu):
