@@ -833,10 +833,11 @@ int dmrg_twosite_gpu(const struct mpo* H, int num_sweeps, int maxiter, double to
 		        c.svd_phase_ms[0] / st->sweeps, c.svd_phase_ms[1] / st->sweeps, c.svd_phase_ms[2] / st->sweeps,
 		        c.svd_phase_ms[3] / st->sweeps);
 	if (getenv("CTGPU_SVD_PHASES") && st->sweeps > 0)
-		fprintf(stderr, "ctgpu: Jacobi of that block, SM cycles per sweep: FP64 steps %.3g exchanges %.3g FP32 sweeps %.3g (exchanges %.3g) FP32-to-FP64 %.3g; Jacobi sweeps per sweep: FP64 %.0f FP32 %.0f\n",
+		fprintf(stderr, "ctgpu: Jacobi of that block, SM cycles per sweep: FP64 steps %.3g exchanges %.3g FP32 sweeps %.3g (exchanges %.3g) FP32-to-FP64 %.3g (T = R^T V %.3g); Jacobi sweeps per sweep: FP64 %.0f FP32 %.0f\n",
 		        c.svd_jacobi_cycles[0] / st->sweeps, c.svd_jacobi_cycles[3] / st->sweeps, c.svd_jacobi_cycles[4] / st->sweeps,
 		        c.svd_jacobi_cycles[6] / st->sweeps,
-		        c.svd_jacobi_cycles[5] / st->sweeps, c.svd_jacobi_cycles[1] / st->sweeps, c.svd_jacobi_cycles[2] / st->sweeps);
+		        c.svd_jacobi_cycles[5] / st->sweeps, c.svd_jacobi_cycles[7] / st->sweeps, c.svd_jacobi_cycles[1] / st->sweeps,
+		        c.svd_jacobi_cycles[2] / st->sweeps);
 	if (getenv("CTGPU_SVD_PHASES") && st->sweeps > 0)
 		fprintf(stderr, "ctgpu: distributed QR of that block, SM cycles per sweep: candidates %.3g reflectors %.3g exchange %.3g fetch %.3g updates %.3g\n",
 		        c.svd_qr_cycles[0] / st->sweeps, c.svd_qr_cycles[1] / st->sweeps, c.svd_qr_cycles[2] / st->sweeps,

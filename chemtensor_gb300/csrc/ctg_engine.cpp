@@ -1244,6 +1244,7 @@ int op_svd_launch(Ctx& c, const DTensor& a, SvdResult& res, SvdPending& pend, do
 			c.svd_phase_ms[3] += 1e-6 * (double)(t1 - t0);
 			for (int i = 0; i < 6; i++) c.svd_jacobi_cycles[i] += (double)h[SVD_PHASE_SLOTS * crit + 4 + i];
 			c.svd_jacobi_cycles[6] += (double)h[SVD_PHASE_SLOTS * crit + 20];
+			c.svd_jacobi_cycles[7] += (double)h[SVD_PHASE_SLOTS * crit + 21];
 			for (int i = 0; i < 5; i++) c.svd_qr_cycles[i] += (double)h[SVD_PHASE_SLOTS * crit + 10 + i];
 			// CTGPU_SVD_PHASES=2: one line per call for the block that finished last
 			static const bool each = atoi(getenv("CTGPU_SVD_PHASES")) >= 2;

@@ -97,7 +97,7 @@ public:
 	// finished last in each block SVD
 	double svd_phase_ms[4] = {0, 0, 0, 0};
 	double svd_qr_cycles[5] = {0, 0, 0, 0, 0};     // distributed QR: candidates, reflectors, exchange, fetch, updates
-	double svd_jacobi_cycles[7] = {0, 0, 0, 0, 0, 0, 0};   // FP64 step cycles, FP64 sweeps, FP32 sweeps, exchange / FP32 / hand-over / FP32 exchange cycles
+	double svd_jacobi_cycles[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // FP64 step cycles, FP64 sweeps, FP32 sweeps, exchange / FP32 / hand-over / FP32 exchange / T = R^T V cycles
 	// cache of lowered operations, keyed by operation and operand structures (DMRG revisits the
 	// same block structures every sweep once the bond dimensions have settled)
 	struct PlanCache* plans() { return plans_; }

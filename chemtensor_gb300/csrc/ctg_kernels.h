@@ -180,7 +180,7 @@ constexpr int SVD_MAX_SWEEPS = 60;
 // cycles of the refinement's [16] Gram matrices, [17] analysis (cosines, tail, clusters, generator),
 // [18] updates, [19] cluster rotations. With the refinement, [4] holds its SM cycles and [9] those
 // of the Newton-Schulz steps and T = R^T V.
-constexpr int SVD_PHASE_SLOTS = 21;
+constexpr int SVD_PHASE_SLOTS = 22;
 struct SvdDesc {
 	i64 a_off, u_off, s_off, v_off, w_off;
 	int m, n;

@@ -85,7 +85,7 @@ struct AxisSource {
 	int ax[8] = {};
 };
 
-Meta build_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::vector<q32>>& ql, const AxisSource* src);
+Meta build_meta(int ndim, const i64* dim, const int* dir, std::vector<std::vector<q32>> ql, const AxisSource* src);
 
 }  // namespace
 
@@ -96,14 +96,14 @@ Meta make_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::
 
 namespace {
 
-Meta build_meta(int ndim, const i64* dim, const int* dir, const std::vector<std::vector<q32>>& ql, const AxisSource* src)
+Meta build_meta(int ndim, const i64* dim, const int* dir, std::vector<std::vector<q32>> ql, const AxisSource* src)
 {
 	CTG_CHECK(ndim >= 1 && ndim <= 8, "tensor degree out of range");
 	Meta m;
 	m.ndim = ndim;
 	m.dim.assign(dim, dim + ndim);
 	m.dir.assign(dir, dir + ndim);
-	m.ql = ql;
+	m.ql = std::move(ql);
 	m.qb.resize(ndim);
 	m.bd.resize(ndim);
 	m.pos.resize(ndim);
@@ -111,7 +111,7 @@ Meta build_meta(int ndim, const i64* dim, const int* dir, const std::vector<std:
 	m.nb.resize(ndim);
 	for (int a = 0; a < ndim; a++)
 	{
-		CTG_CHECK(dim[a] > 0 && (i64)ql[a].size() == dim[a], "logical quantum numbers do not match the dimension");
+		CTG_CHECK(dim[a] > 0 && (i64)m.ql[a].size() == dim[a], "logical quantum numbers do not match the dimension");
 		if (src && src->m[a])
 		{
 			const Meta& o = *src->m[a];
@@ -123,7 +123,7 @@ Meta build_meta(int ndim, const i64* dim, const int* dir, const std::vector<std:
 			m.blk[a] = o.blk[b];
 			continue;
 		}
-		std::vector<q32> u(ql[a]);
+		std::vector<q32> u(m.ql[a]);
 		std::sort(u.begin(), u.end());
 		u.erase(std::unique(u.begin(), u.end()), u.end());
 		m.qb[a] = u;
@@ -133,7 +133,7 @@ Meta build_meta(int ndim, const i64* dim, const int* dir, const std::vector<std:
 		m.blk[a].resize(dim[a]);
 		for (i64 j = 0; j < dim[a]; j++)
 		{
-			const int b = (int)(std::lower_bound(u.begin(), u.end(), ql[a][j]) - u.begin());
+			const int b = (int)(std::lower_bound(u.begin(), u.end(), m.ql[a][j]) - u.begin());
 			m.blk[a][j] = b;
 			m.pos[a][j] = m.bd[a][b]++;
 		}
@@ -336,7 +336,7 @@ Meta dot_result_meta(const Meta& s, int axs, const Meta& t, int axt, int nmult)
 	}
 	CTG_CHECK(!dim.empty(), "dot: scalar results are not on the DMRG path");
 	CTG_CHECK(dim.size() <= 8, "tensor degree out of range");
-	return build_meta((int)dim.size(), dim.data(), dir.data(), ql, &src);
+	return build_meta((int)dim.size(), dim.data(), dir.data(), std::move(ql), &src);
 }
 
 Meta transpose_meta(const Meta& t, const int* perm, std::vector<int>* dst_of_src)
@@ -449,7 +449,7 @@ Meta flatten_meta(const Meta& t, int ax, int newdir)
 		dir.push_back(t.dir[i]);
 		ql.push_back(t.ql[i]);
 	}
-	return build_meta((int)dim.size(), dim.data(), dir.data(), ql, &src);
+	return build_meta((int)dim.size(), dim.data(), dir.data(), std::move(ql), &src);
 }
 
 Meta split_meta(const Meta& t, int ax, const i64 nd[2], const int ndir[2], const std::vector<q32>* nq)
@@ -481,7 +481,7 @@ Meta split_meta(const Meta& t, int ax, const i64 nd[2], const int ndir[2], const
 		dir.push_back(t.dir[i]);
 		ql.push_back(t.ql[i]);
 	}
-	return build_meta((int)dim.size(), dim.data(), dir.data(), ql, &src);
+	return build_meta((int)dim.size(), dim.data(), dir.data(), std::move(ql), &src);
 }
 
 Meta slice_meta(const Meta& t, int ax, const std::vector<i64>& ind)
@@ -503,7 +503,7 @@ Meta slice_meta(const Meta& t, int ax, const std::vector<i64>& ind)
 			src.m[i] = &t;
 			src.ax[i] = i;
 		}
-	return build_meta(t.ndim, dim.data(), t.dir.data(), ql, &src);
+	return build_meta(t.ndim, dim.data(), t.dir.data(), std::move(ql), &src);
 }
 
 Meta reversed_meta(const Meta& t)

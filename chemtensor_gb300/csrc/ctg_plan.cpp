@@ -309,12 +309,26 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 			std::vector<GemmContrib>().swap(R.cons);
 		}
 	}
-	// tiles: every tile first takes the whole sum over its output block's contributions
+	// tiles: every tile first takes the whole sum over its output block's contributions; the FP64
+	// tile class of every output block first, so that each class list is allocated once
 	const bool allow_large = flops / 2 > (double)num_sms * 8 * 65536;
+	std::vector<unsigned char> ocls(is_tc_precision(precision) ? 0 : (size_t)r.nblocks);
 	parallel_for(nrange, [&](int q) {
 		int b0, b1;
 		range_of(q, b0, b1);
 		Range& R = rng[(size_t)q];
+		if (!is_tc_precision(precision))
+		{
+			size_t cnt[NUM_TILE_CLASSES] = {};
+			for (int b = b0; b < b1; b++)
+			{
+				const GemmOut& o = outs[(size_t)b];
+				const int cls = tile_class(o.m, o.n, allow_large);
+				ocls[(size_t)b] = (unsigned char)cls;
+				cnt[cls] += (size_t)((o.m + TILE_ROWS[cls] - 1) / TILE_ROWS[cls]) * ((o.n + TILE_COLS[cls] - 1) / TILE_COLS[cls]);
+			}
+			for (int k = 0; k < NUM_TILE_CLASSES; k++) R.tiles[k].reserve(cnt[k]);
+		}
 		for (int b = b0; b < b1; b++)
 		{
 			const GemmOut& o = outs[(size_t)b];
@@ -340,16 +354,17 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 					}
 				continue;
 			}
-			const int cls = tile_class(o.m, o.n, allow_large);
+			const int cls = ocls[(size_t)b];
 			R.flops_cls[cls] += 2.0 * (double)o.m * (double)o.n * (double)ksum[(size_t)b];
-			const int tr = tile_rows(cls), tc = tile_cols(cls);
+			const int tr = TILE_ROWS[cls], tc = TILE_COLS[cls];
 			whole.cls = cls;
+			std::vector<GemmTile>& tl = R.tiles[cls];
 			for (int m0 = 0; m0 < o.m; m0 += tr)
 				for (int n0 = 0; n0 < o.n; n0 += tc)
 				{
 					whole.m0 = m0;
 					whole.n0 = n0;
-					R.tiles[cls].push_back(whole);
+					tl.push_back(whole);
 				}
 		}
 	});
@@ -405,14 +420,12 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 				}
 			}
 		CTG_CHECK(cut_x >= 0, "dot: unsupported output permutation");
-		auto outp = std::make_shared<Meta>(transpose_meta(r, out_perm));
-		std::vector<i64> ip((size_t)nd);
+		std::vector<int> dst_of_src;
+		auto outp = std::make_shared<Meta>(transpose_meta(r, out_perm, &dst_of_src));
 		for (int b = 0; b < r.nblocks; b++)
 		{
-			const i64* ib = r.index(b);
 			const i64* d = r.dims(b);
-			for (int i = 0; i < nd; i++) ip[(size_t)i] = ib[out_perm[i]];
-			const int bp = outp->find(ip.data());
+			const int bp = dst_of_src[(size_t)b];
 			CTG_CHECK(bp >= 0, "dot: missing block of the transposed result");
 			const i64 size[4] = {prod(d, cut_x), prod(d + cut_x, nfs - cut_x), prod(d + nfs, cut_y),
 			                     prod(d + nfs + cut_y, nft - cut_y)};
@@ -447,13 +460,13 @@ DotLowering lower_dot(const Meta& s, int axs, const Meta& t, int axt, int nmult,
 		double total = 0;
 		for (int k = 0; k < NUM_TILE_CLASSES; k++)
 			for (const GemmTile& t : tiles[k])
-				total += (double)tile_rows(k) * tile_cols(k) * (double)(nchunk[(size_t)t.out] * KCH);
+				total += (double)TILE_ROWS[k] * TILE_COLS[k] * (double)(nchunk[(size_t)t.out] * KCH);
 		const double target = std::max(total / (2.0 * num_sms), 16384.0);
 		std::vector<std::pair<int, int>> pos;
 		for (int k = 0; k < NUM_TILE_CLASSES; k++)
 		{
 			std::vector<GemmTile> kept;
-			const int tr = tile_rows(k), tc = tile_cols(k);
+			const int tr = TILE_ROWS[k], tc = TILE_COLS[k];
 			for (const GemmTile& t : tiles[k])
 			{
 				const GemmOut& o = outs[(size_t)t.out];

@@ -1412,6 +1412,7 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 	}
 
 	// ---- 2. T = R^T V for the own columns (R_ki = W_ik, k <= i), FP64 ----
+	const long long ct = cyc ? clock64() : 0;
 	{
 		constexpr int JB = 4;
 		for (int j0 = 0; j0 < rf.nown; j0 += JB)
@@ -1443,6 +1444,7 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 	}
 	const long long c1 = cyc ? clock64() : 0;
 	if (cyc) cyc[5] += c1 - c0;
+	if (cyc) cyc[11] += c1 - ct;
 	iters = 0;
 	if (!refine)
 	{
@@ -1799,7 +1801,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 	long long jsteps = 0;                              // the FP64 sweeps' share, as an integer
 	// FP64 steps (or the refinement), FP64 sweeps, FP32 sweeps, exchanges, FP32 cycles, hand-over cycles;
 	// refinement cycles: Gram matrices, analysis (cosines, tail, clusters, generator), updates, clusters
-	long long cyc_acc[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+	long long cyc_acc[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 	// counted on the second CTA: the first one holds the last column group, often short or empty
 	const bool count = phase_ts && tid == 0 && rank == (cl > 1 ? 1 : 0);
 	long long* cyc = count ? cyc_acc : nullptr;
@@ -1952,6 +1954,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 		phase_ts[SVD_PHASE_SLOTS * blk + 15] = (unsigned long long)(rf_iters + (mixed && !refined ? 100 : 0));
 		for (int i = 0; i < 4; i++) phase_ts[SVD_PHASE_SLOTS * blk + 16 + i] = (unsigned long long)cyc_acc[6 + i];
 		phase_ts[SVD_PHASE_SLOTS * blk + 20] = (unsigned long long)cyc_acc[10];
+		phase_ts[SVD_PHASE_SLOTS * blk + 21] = (unsigned long long)cyc_acc[11];
 	}
 
 	// ---- 3. outputs: L = Q V (M x r) by the r reflectors applied to [V_c; 0], Rf = P T Sigma^-1 ----
