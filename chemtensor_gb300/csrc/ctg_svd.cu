@@ -1412,31 +1412,26 @@ __device__ bool finish_mixed(cg::cluster_group& cluster, const Tour& t, double* 
 	}
 
 	// ---- 2. T = R^T V for the own columns (R_ki = W_ik, k <= i), FP64 ----
+	// one task per (32 rows of T, own column): a lane forms one entry, its k loop in order over its
+	// row of R (column i of W, read from L2); the tasks go round the warps so that the FP64 work of
+	// the long rows (row i takes i + 1 terms) is spread over every sub-partition
 	const long long ct = cyc ? clock64() : 0;
 	{
-		constexpr int JB = 4;
-		for (int j0 = 0; j0 < rf.nown; j0 += JB)
+		const int ngrp = (N + 31) / 32;
+		for (int task = warp; task < ngrp * rf.nown; task += NWARPS)
 		{
-			const int nj = min(JB, rf.nown - j0);
-			for (int i = tid; i < N; i += SVD_THREADS)
+			const int gi = ngrp - 1 - task / rf.nown, jj = task % rf.nown;
+			const int i = 32 * gi + lane;
+			double* rec = rf_rec(t, rf, jj);
+			const double* v = rec + N;
+			if (i < N)
 			{
 				const int kmax = i < r - 1 ? i : r - 1;
 				const double* wi = xs.W + (i64)i * M;
-				double acc[JB] = {0.0, 0.0, 0.0, 0.0};
-				const double* v0 = rf_rec(t, rf, j0) + N;
-				const double* v1 = rf_rec(t, rf, j0 + min(1, nj - 1)) + N;
-				const double* v2 = rf_rec(t, rf, j0 + min(2, nj - 1)) + N;
-				const double* v3 = rf_rec(t, rf, j0 + min(3, nj - 1)) + N;
+				double acc = 0.0;
 #pragma unroll 8
-				for (int k = 0; k <= kmax; k++)
-				{
-					const double w = __ldcg(wi + k);
-					acc[0] = fma(w, v0[k], acc[0]);
-					acc[1] = fma(w, v1[k], acc[1]);
-					acc[2] = fma(w, v2[k], acc[2]);
-					acc[3] = fma(w, v3[k], acc[3]);
-				}
-				for (int q = 0; q < nj; q++) rf_rec(t, rf, j0 + q)[i] = acc[q];
+				for (int k = 0; k <= kmax; k++) acc = fma(__ldcg(wi + k), v[k], acc);
+				rec[i] = acc;
 			}
 		}
 		if (tid == 0) fl += 2.0 * ((double)N * r - 0.5 * (double)r * r) * rf.nown;
