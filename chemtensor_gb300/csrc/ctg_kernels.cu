@@ -1,5 +1,6 @@
 // ctg_kernels.cu - FP64 grouped block GEMM and the block data-movement kernels.
 #include "ctg_kernels.h"
+#include "ctg_launch.cuh"
 
 namespace ctg {
 
@@ -169,6 +170,8 @@ k_gemm_f64(const GemmTile* __restrict__ tiles, const GemmOut* __restrict__ outs,
            const GemmSplit* __restrict__ splits, int* __restrict__ counters, const double* __restrict__ A,
            const double* __restrict__ B, double* __restrict__ C, double* __restrict__ work)
 {
+	pdl_wait();
+	pdl_trigger();
 	__shared__ double sm[GEMM_SMEM_DOUBLES];
 	const GemmTile tile = tiles[blockIdx.x];
 	switch (tile.cls)
@@ -202,8 +205,8 @@ void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, con
                      cudaStream_t st)
 {
 	if (ntiles <= 0) return;
-	k_gemm_f64<<<ntiles, GEMM_THREADS, 0, st>>>(tiles, outs, cons, splits, counters, A, B, C, work);
-	CTG_CUDA(cudaGetLastError());
+	launch_pdl(launch_config(dim3(ntiles), dim3(GEMM_THREADS), 0, st), k_gemm_f64, tiles, outs, cons, splits, counters, A, B,
+	           C, work);
 }
 
 // ------------------------------------------------------------------------------------
@@ -216,6 +219,8 @@ __global__ void __launch_bounds__(256)
 k_permute(const Chunk* __restrict__ chunks, const PermDesc* __restrict__ descs, const T* __restrict__ src,
           T* __restrict__ dst)
 {
+	pdl_wait();
+	pdl_trigger();
 	const Chunk ch = chunks[blockIdx.x];
 	const PermDesc d = descs[ch.desc];
 	const i64 end = min(d.n, ch.start + (i64)COPY_CHUNK);
@@ -254,8 +259,9 @@ void launch_permute(int nchunks, const Chunk* chunks, const PermDesc* descs, con
                     bool cplx)
 {
 	if (nchunks <= 0) return;
-	if (cplx) k_permute<double2><<<nchunks, 256, 0, st>>>(chunks, descs, (const double2*)src, (double2*)dst);
-	else k_permute<double><<<nchunks, 256, 0, st>>>(chunks, descs, src, dst);
+	const cudaLaunchConfig_t cfg = launch_config(dim3(nchunks), dim3(256), 0, st);
+	if (cplx) launch_pdl(cfg, k_permute<double2>, chunks, descs, (const double2*)src, (double2*)dst);
+	else launch_pdl(cfg, k_permute<double>, chunks, descs, src, dst);
 	CTG_CUDA(cudaGetLastError());
 }
 
@@ -268,6 +274,8 @@ __global__ void __launch_bounds__(256)
 k_rowmap(const Chunk* __restrict__ chunks, const RowDesc* __restrict__ descs, const i64* __restrict__ maps,
          const T* __restrict__ src, T* __restrict__ dst)
 {
+	pdl_wait();
+	pdl_trigger();
 	const Chunk ch = chunks[blockIdx.x];
 	const RowDesc d = descs[ch.desc];
 	const i64 n = d.nlead * d.nrow * d.ntrail;
@@ -308,8 +316,9 @@ void launch_rowmap(int nchunks, const Chunk* chunks, const RowDesc* descs, const
                    cudaStream_t st, bool cplx)
 {
 	if (nchunks <= 0) return;
-	if (cplx) k_rowmap<double2><<<nchunks, 256, 0, st>>>(chunks, descs, maps, (const double2*)src, (double2*)dst);
-	else k_rowmap<double><<<nchunks, 256, 0, st>>>(chunks, descs, maps, src, dst);
+	const cudaLaunchConfig_t cfg = launch_config(dim3(nchunks), dim3(256), 0, st);
+	if (cplx) launch_pdl(cfg, k_rowmap<double2>, chunks, descs, maps, (const double2*)src, (double2*)dst);
+	else launch_pdl(cfg, k_rowmap<double>, chunks, descs, maps, src, dst);
 	CTG_CUDA(cudaGetLastError());
 }
 
@@ -326,6 +335,8 @@ __global__ void __launch_bounds__(256)
 k_scale_axis(const Chunk* __restrict__ chunks, const ScaleDesc* __restrict__ descs, const i64* __restrict__ maps,
              const double* __restrict__ vec, const T* __restrict__ src, T* __restrict__ dst)
 {
+	pdl_wait();
+	pdl_trigger();
 	const Chunk ch = chunks[blockIdx.x];
 	const ScaleDesc d = descs[ch.desc];
 	const i64 n = d.nlead * d.nax * d.ntrail;
@@ -352,8 +363,9 @@ void launch_scale_axis(int nchunks, const Chunk* chunks, const ScaleDesc* descs,
                        const double* src, double* dst, cudaStream_t st, bool cplx)
 {
 	if (nchunks <= 0) return;
-	if (cplx) k_scale_axis<double2><<<nchunks, 256, 0, st>>>(chunks, descs, maps, vec, (const double2*)src, (double2*)dst);
-	else k_scale_axis<double><<<nchunks, 256, 0, st>>>(chunks, descs, maps, vec, src, dst);
+	const cudaLaunchConfig_t cfg = launch_config(dim3(nchunks), dim3(256), 0, st);
+	if (cplx) launch_pdl(cfg, k_scale_axis<double2>, chunks, descs, maps, vec, (const double2*)src, (double2*)dst);
+	else launch_pdl(cfg, k_scale_axis<double>, chunks, descs, maps, vec, src, dst);
 	CTG_CUDA(cudaGetLastError());
 }
 

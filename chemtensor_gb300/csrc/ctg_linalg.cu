@@ -10,6 +10,7 @@
 
 #include "ctg_fp64.cuh"
 #include "ctg_kernels.h"
+#include "ctg_launch.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -323,6 +324,8 @@ __global__ void __launch_bounds__(RED_THREADS, 1)
 k_lzc_step(double* __restrict__ w, const double* __restrict__ vj, const double* __restrict__ vjm1,
            double* __restrict__ vj1, i64 n, i64 nthr, int j, int last, LanczosScalars* sc)
 {
+	pdl_wait();
+	pdl_trigger();
 	__shared__ double part[3], wred[RED_THREADS / 32], bc[3];
 	ClusterReduce red(part, wred, bc);
 	lz_step(red, w, vj, vjm1, vj1, n, nthr, j, last, sc);
@@ -365,6 +368,8 @@ k_lz_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, double*
 __global__ void __launch_bounds__(RED_THREADS, 1)
 k_lzc_start(const double* __restrict__ v0, double* __restrict__ v, i64 n, LanczosScalars* sc)
 {
+	pdl_wait();
+	pdl_trigger();
 	__shared__ double part[3], wred[RED_THREADS / 32], bc[3];
 	ClusterReduce red(part, wred, bc);
 	lz_start(red, v0, v, n, sc);
@@ -451,7 +456,7 @@ static void launch_cluster_form(void (*fn)(Args...), cudaStream_t st, Args... ar
 	at[0].val.clusterDim.z = 1;
 	cfg.attrs = at;
 	cfg.numAttrs = 1;
-	CTG_CUDA(cudaLaunchKernelEx(&cfg, fn, args...));
+	launch_pdl(cfg, fn, args...);
 }
 
 void launch_lz_step(double* w, const double* vj, const double* vjm1, double* vj1, i64 n, i64 nthr, int j, int last,
@@ -989,6 +994,8 @@ __global__ void __launch_bounds__(RED_THREADS, 1)
 k_lzc_finish(const double* __restrict__ w, const double* __restrict__ V, i64 n, int maxiter, LanczosScalars* sc,
              double* __restrict__ out)
 {
+	pdl_wait();
+	pdl_trigger();
 	__shared__ double part[3], wred[RED_THREADS / 32], bc[3];
 	ClusterReduce red(part, wred, bc);
 	lz_finish(red, w, V, n, maxiter, sc, out);
