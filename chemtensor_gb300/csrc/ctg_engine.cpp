@@ -519,7 +519,7 @@ void DotPlan::run(Ctx& c, const double* A, const double* B, double* C) const
 	if (ntiles[0] > 0)
 	{
 		KScope ks(c, K_GEMM, 1, flops, 0);
-		launch_gemm_f64(ntiles[0], tiles[0], outs, cons, splits, cnt, A, B, C, w, c.stream());
+		launch_gemm_f64(ntiles[0], tiles[0], outs, cons, splits, cnt, A, B, C, w, c.stream(), flops);
 	}
 	c.gemm_flops += flops;
 }

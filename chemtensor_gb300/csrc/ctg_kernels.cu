@@ -202,11 +202,15 @@ int tile_cols(int cls)
 
 void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
                      const GemmSplit* splits, int* counters, const double* A, const double* B, double* C, double* work,
-                     cudaStream_t st)
+                     cudaStream_t st, double flops)
 {
 	if (ntiles <= 0) return;
-	launch_pdl(launch_config(dim3(ntiles), dim3(GEMM_THREADS), 0, st), k_gemm_f64, tiles, outs, cons, splits, counters, A, B,
-	           C, work);
+	// programmatic dependent launch for the short products of a sweep (tens of microseconds); a
+	// product of milliseconds gains nothing from it and lost 2 % with it (the next kernel's blocks
+	// scheduled beside its last waves)
+	const cudaLaunchConfig_t cfg = launch_config(dim3(ntiles), dim3(GEMM_THREADS), 0, st);
+	if (flops < 2e8) launch_pdl(cfg, k_gemm_f64, tiles, outs, cons, splits, counters, A, B, C, work);
+	else CTG_CUDA(cudaLaunchKernelEx(&cfg, k_gemm_f64, tiles, outs, cons, splits, counters, A, B, C, work));
 }
 
 // ------------------------------------------------------------------------------------

@@ -75,7 +75,7 @@ int tile_cols(int cls);
 // split tiles use `counters` (one per GemmSplit, zero before the launch and again after it)
 void launch_gemm_f64(int ntiles, const GemmTile* tiles, const GemmOut* outs, const GemmContrib* cons,
                      const GemmSplit* splits, int* counters, const double* A, const double* B, double* C, double* work,
-                     cudaStream_t st);
+                     cudaStream_t st, double flops = 0.0);
 
 // Same work lists on the tcgen05 tensor cores with FP32 accumulation, output tiles of
 // tc_tile_rows() x BN (BN = 64, 128 or 256, chosen per product). Operand formats (TcFormat):

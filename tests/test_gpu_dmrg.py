@@ -88,6 +88,29 @@ def test_lanczos_grid_and_cluster_forms_match_oracle(gpu, oracle_port):
     np.testing.assert_allclose(grid["ent"], s2, rtol=0, atol=1e-8)
 
 
+def test_launch_without_programmatic_dependence_gives_the_same_bits(gpu):
+    """The sweep's kernels are launched with programmatic dependent launch (each waits for its
+    predecessor on the device before touching memory); with it switched off (child process,
+    CTGPU_PDL=0) the same solve gives bit-identical energies and entropies."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, CTGPU_PDL="0")
+    r = subprocess.run([sys.executable, "-c", _GRID_FORM_SCRIPT], cwd=root, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    off = json.loads(r.stdout.strip().splitlines()[-1])
+    H = hm.fermi_hubbard_1d(16, 1.0, 4.0, 0.0)
+    c = native.random_mps(16, 4, hm.HUBBARD_QSITE, hm.encode_quantum_number_pair(16, 0), 64, 42)
+    psi0 = cs.read_mps(c)
+    cs.free_mps(c)
+    ret, en, ent, _ = run_gpu_dmrg(gpu, H, psi0, 2, 5, 1e-10, 64)
+    assert ret == 0 and off["ret"] == 0
+    assert list(en) == off["en"] and list(ent) == off["ent"]
+
+
 @pytest.mark.parametrize("L,D,seed", [(10, 8, 268), (14, 8, 71)])
 def test_dmrg_zero_norm_start_state_matches_oracle(gpu, oracle_port, L, D, seed):
     """A seeded random start state with a site tensor that has no allowed block (mismatching quantum
