@@ -499,8 +499,23 @@ __device__ void jacobi_step32(const Tour32& t, int buf, int mode, int step, int 
 		if (!step_pair_idx(mode, step, k, t.bs, cA, cB, npad, sp, cp, sq, cq)) continue;
 		float* x = t.col(buf, sp, cp);
 		float* y = t.col(buf, sq, cq);
+		// the lane's entries loaded eight at a time before they are added (in the same order): the
+		// loads of a step are then in flight together instead of one pair per iteration
 		float g = 0.0f;
-		for (int i = lane; i < t.N; i += 32) g = fmaf(x[i], y[i], g);
+		for (int i0 = 0; i0 < t.N; i0 += 256)
+		{
+			float xs[8], ys[8];
+#pragma unroll
+			for (int u = 0; u < 8; u++)
+			{
+				const int i = i0 + lane + 32 * u;
+				xs[u] = i < t.N ? x[i] : 0.0f;
+				ys[u] = i < t.N ? y[i] : 0.0f;
+			}
+#pragma unroll
+			for (int u = 0; u < 8; u++)
+				if (i0 + 32 * u < t.N) g = fmaf(xs[u], ys[u], g);     // the same in every lane
+		}
 		g = warp_sumf(g);
 		float* pa = t.nrm(buf, sp) + cp;
 		float* pb = t.nrm(buf, sq) + cq;
@@ -516,11 +531,26 @@ __device__ void jacobi_step32(const Tour32& t, int buf, int mode, int step, int 
 			tn = copysignf(tn, zeta);
 			const float c = rsqrtf(fmaf(tn, tn, 1.0f));
 			const float sn = c * tn;
-			for (int i = lane; i < len; i += 32)
+			for (int i0 = 0; i0 < len; i0 += 128)
 			{
-				const float xv = x[i], yv = y[i];
-				x[i] = fmaf(c, xv, -sn * yv);
-				y[i] = fmaf(sn, xv, c * yv);
+				float xv[4], yv[4];
+#pragma unroll
+				for (int u = 0; u < 4; u++)
+				{
+					const int i = i0 + lane + 32 * u;
+					xv[u] = i < len ? x[i] : 0.0f;
+					yv[u] = i < len ? y[i] : 0.0f;
+				}
+#pragma unroll
+				for (int u = 0; u < 4; u++)
+				{
+					const int i = i0 + lane + 32 * u;
+					if (i < len)
+					{
+						x[i] = fmaf(c, xv[u], -sn * yv[u]);
+						y[i] = fmaf(sn, xv[u], c * yv[u]);
+					}
+				}
 			}
 			__syncwarp();
 			if (lane == 0)
@@ -1986,7 +2016,7 @@ k_svd_tour(const SvdDesc* __restrict__ descs, int first, const double* __restric
 			for (int k = k1; k >= k0; k--)
 			{
 				const double tk = ts[k - k0];
-				if (tk == 0.0) continue;
+				if (__double_as_longlong(tk) == 0) continue;     // tk >= +0: bits zero only at zero
 				const double* wk = ws + (i64)(k - k0) * M;
 				double acc = 0;
 				for (int i = k + lane; i < M; i += 32) acc = fma(wk[i], ub[i], acc);

@@ -7,12 +7,21 @@
 
 namespace ctg {
 
-// Pair pi of round rnd of the circle method over np (even) indices: index np - 1 stays fixed,
-// the others rotate; p < q on return.
+// Pair pi (0 <= pi < np / 2) of round rnd (0 <= rnd < np - 1) of the circle method over np (even)
+// indices: index np - 1 stays fixed, the others rotate; p < q on return. The residues mod np - 1
+// by one conditional subtraction (both sums lie below 2 (np - 1)): an integer division sits on
+// the serial chain of every Jacobi step.
 __host__ __device__ inline void round_robin_pair(int rnd, int pi, int np, int& p, int& q)
 {
-	if (pi == 0) { p = rnd; q = np - 1; }
-	else { p = (rnd + pi) % (np - 1); q = (rnd - pi + (np - 1)) % (np - 1); }
+	const int m = np - 1;
+	if (pi == 0) { p = rnd; q = m; }
+	else
+	{
+		p = rnd + pi;
+		if (p >= m) p -= m;
+		q = rnd - pi + m;
+		if (q >= m) q -= m;
+	}
 	if (p > q) { const int t = p; p = q; q = t; }
 }
 
@@ -57,7 +66,8 @@ __host__ __device__ inline bool step_pair_idx(int mode, int step, int k, int bs,
 	sp = 0;
 	sq = 1;
 	cp = k;
-	cq = (k + step) % bs;
+	cq = k + step;                 // (k + step) mod bs, with k, step < bs
+	if (cq >= bs) cq -= bs;
 	return k < cA && cq < cB;
 }
 
