@@ -59,11 +59,15 @@ __host__ __device__ inline i64 tour_jac_doubles(int N, int cl)
 	return 4 * bsmax * 2 * N + 4 * bsmax + 3 * SVD_STEP_PAIRS + SVD_STEP_PAIRS / 2 + 16;
 }
 
-// shared memory (bytes) of the FP32 tour over 2 cf groups of the r columns (records of 2 N floats)
+// records of the FP32 tour: 2 N floats rounded up to a multiple of four, so that every column
+// starts on a 16-byte boundary (the exchanges between CTAs move float4)
+__host__ __device__ inline int f32_record(int N) { return (2 * N + 3) & ~3; }
+
+// shared memory (bytes) of the FP32 tour over 2 cf groups of the r columns
 __host__ __device__ inline i64 f32_tour_bytes(int N, int r, int cf)
 {
 	const i64 bs = (r + 2 * cf - 1) / (2 * cf);
-	return 4 * (4 * bs * 2 * N + 4 * bs + 4);
+	return 4 * (4 * bs * (i64)f32_record(N) + 4 * bs + 4);
 }
 
 // scratch (doubles) of one block's SVD before the refinement's arrays: the larger of the
@@ -883,7 +887,7 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 	f.bsmax = f.bs;
 	f.r = r;
 	f.N = N;
-	f.ld = t.ld;
+	f.ld = f32_record(N);
 	f.sm = (float*)smem;
 	int* local_rot = (int*)(f.sm + (i64)4 * f.bsmax * f.ld + 4 * f.bsmax);
 	int A, B;
@@ -918,7 +922,19 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 				{
 					const float* col = f.col(buf, slot, c);
 					float acc = 0.0f;
-					for (int i = lane; i < N; i += 32) acc = fmaf(col[i], col[i], acc);
+					for (int i0 = 0; i0 < N; i0 += 256)
+					{
+						float xs[8];
+#pragma unroll
+						for (int u = 0; u < 8; u++)
+						{
+							const int i = i0 + lane + 32 * u;
+							xs[u] = i < N ? col[i] : 0.0f;
+						}
+#pragma unroll
+						for (int u = 0; u < 8; u++)
+							if (i0 + 32 * u < N) acc = fmaf(xs[u], xs[u], acc);
+					}
 					acc = warp_sumf(acc);
 					if (lane == 0) f.nrm(buf, slot)[c] = acc;
 				}
@@ -945,9 +961,9 @@ __device__ void precondition_f32(cg::cluster_group& cluster, const Tour& t, doub
 						const int x = slot ? B : A, nc = f.cnt(x);
 						int pi2, slot2;
 						group_owner(x, rho1, f.nm, pi2, slot2);
-						const float2* src = (const float2*)f.col(buf, slot, 0);
-						float2* dst = (float2*)cluster.map_shared_rank(f.col(buf ^ 1, slot2, 0), (unsigned)pi2);
-						for (i64 e = tid; e < (i64)nc * f.ld / 2; e += SVD_THREADS) dst[e] = src[e];
+						const float4* src = (const float4*)f.col(buf, slot, 0);
+						float4* dst = (float4*)cluster.map_shared_rank(f.col(buf ^ 1, slot2, 0), (unsigned)pi2);
+						for (i64 e = tid; e < (i64)nc * f.ld / 4; e += SVD_THREADS) dst[e] = src[e];
 						const float* nsrc = f.nrm(buf, slot);
 						float* ndst = cluster.map_shared_rank(f.nrm(buf ^ 1, slot2), (unsigned)pi2);
 						for (int e = tid; e < nc; e += SVD_THREADS) ndst[e] = nsrc[e];
