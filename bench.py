@@ -46,7 +46,7 @@ UNIT = "sweeps/s"
 L2_FLUSH_BYTES = 256 << 20
 PRECISIONS = {"fp64": 0, "bf16x3": 1, "tf32": 2, "bf16x6": 3}
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_svd_tour launch (ncu, see profiles/)
-SVD_TRAFFIC_PER_LAUNCH = 488192
+SVD_TRAFFIC_PER_LAUNCH = 496384
 
 
 def build_inputs(host_only: bool = False):
