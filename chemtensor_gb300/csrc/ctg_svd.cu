@@ -596,6 +596,22 @@ __device__ __forceinline__ SvdScratch scratch_layout(double* base, int M, int N)
 	return x;
 }
 
+// Warp-wide argmax of 64-bit keys (a non-negative double's bits, or -1 for no candidate): the
+// largest key, equal keys to the smallest index, by three warp reductions (redux.sync on the key's
+// high and low words, then on the index) instead of a five-round shuffle butterfly on the serial
+// chain of every QR step. Every lane returns the winner's key (-1 if none) and index.
+__device__ __forceinline__ void warp_argmax_key(long long key, int idx, long long& kbest, int& ibest)
+{
+	const unsigned long long u = key < 0 ? 0ull : (unsigned long long)key + 1ull;   // 0: no candidate
+	const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+	const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+	const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+	const bool win = hi == mhi && lo == mlo;
+	ibest = (int)__reduce_min_sync(0xffffffffu, win ? (unsigned)idx : 0xffffffffu);
+	const unsigned long long ub = ((unsigned long long)mhi << 32) | mlo;
+	kbest = ub == 0ull ? -1 : (long long)(ub - 1ull);
+}
+
 // Householder QR with column pivoting of the scaled block over a whole cluster. Column j lives in
 // the shared memory of CTA j % cl; columns are not moved. Every step the first warp of each CTA
 // picks the CTA's best remaining column and forms its reflector in its own shared memory
@@ -684,20 +700,14 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 			// the squared norms are non-negative doubles, which order like their bit patterns as
 			// signed integers: the argmax compares integers (an FP64 compare costs an FP64 pipe slot)
 			long long bbits = -1;
-			int bi = N, bj = -1;
+			int bi = N;
 			for (int jl = lane; jl < nloc; jl += 32)
 			{
 				const long long nb = __double_as_longlong(qnrm[jl]);
-				if (qdone[jl] < 0 && nb > bbits) { bbits = nb; bi = rank + cl * jl; bj = jl; }
+				if (qdone[jl] < 0 && nb > bbits) { bbits = nb; bi = rank + cl * jl; }
 			}
-#pragma unroll
-			for (int o = 16; o > 0; o >>= 1)
-			{
-				const long long ob = __shfl_xor_sync(0xffffffffu, bbits, o);
-				const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-				const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
-				if (ob > bbits || (ob == bbits && oi < bi)) { bbits = ob; bi = oi; bj = oj; }
-			}
+			warp_argmax_key(bbits, bi, bbits, bi);
+			const int bj = bbits >= 0 ? (bi - rank) / cl : -1;
 			double best = bbits < 0 ? -1.0 : __longlong_as_double(bbits);
 			double tk = 0.0, beta = 0.0;
 			if (bj >= 0 && bbits > __double_as_longlong(thresh))
@@ -769,20 +779,13 @@ __device__ int qr_pivoted_cluster(cg::cluster_group& cluster, double* smem, cons
 		long long pb = -1;
 		if (lane < cl)
 		{
-			const double h = hnrm[par * 16 + lane];
-			pb = h > 0.0 ? __double_as_longlong(h) : -1;
+			const long long hb = __double_as_longlong(hnrm[par * 16 + lane]);    // -1.0: no candidate
+			pb = hb > 0 ? hb : -1;
 		}
 		int p = lane < cl ? hidx[par * 16 + lane] : N;
-		int owner = lane;
-#pragma unroll
-		for (int o = 16; o > 0; o >>= 1)
-		{
-			const long long ob = __shfl_xor_sync(0xffffffffu, pb, o);
-			const int op = __shfl_xor_sync(0xffffffffu, p, o);
-			const int ow = __shfl_xor_sync(0xffffffffu, owner, o);
-			if (ob > pb || (ob == pb && op < p)) { pb = ob; p = op; owner = ow; }
-		}
+		warp_argmax_key(pb, p, pb, p);
 		if (pb <= __double_as_longlong(thresh) || pb <= 0 || p >= N) break;
+		const int owner = p % cl;                            // column p lives in CTA p mod cl
 		const double tk = htau[par * 16 + owner];
 		const double* vbuf = cbuf;
 		if (owner != rank)                                   // uniform in the CTA
