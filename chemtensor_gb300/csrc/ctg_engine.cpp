@@ -424,23 +424,25 @@ const T* at(const DBufPtr& b, size_t off)
 
 static DotPlan upload_dot_plan(Ctx& c, DotLowering&& l, int precision, int bn);
 static int tuned_tile_width(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
-                            const int* out_perm, DotLowering& l64);
+                            const int* out_perm, const DotLowering& l64);
 
 static DotPlan build_dot_plan(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
                               const int* out_perm)
 {
 	// complex128: the FP64 work lists (outputs, contributions) with tiles of the complex GEMM
 	const bool z = precision == GEMM_Z64;
-	DotLowering l = lower_dot(s, axs, t, axt, nmult, z ? (int)GEMM_FP64 : precision, c.num_sms(), out_perm);
 	if (is_tc_precision(precision))
 	{
 		// the autotuner picks the tile width, or FP64 where the product is too small for the tensor
-		// cores to pay for their operand packing (FP64 is then both faster and exact)
+		// cores to pay for their operand packing (FP64 is then both faster and exact). Its key comes
+		// from the output blocks and contributions, which the FP64 lowering has too: a product that
+		// stays on FP64 is lowered once, one on the tensor cores twice
+		DotLowering l = lower_dot(s, axs, t, axt, nmult, GEMM_FP64, c.num_sms(), out_perm);
 		const int bn = tuned_tile_width(c, s, axs, t, axt, nmult, precision, out_perm, l);
-		if (bn == 0) return upload_dot_plan(c, lower_dot(s, axs, t, axt, nmult, GEMM_FP64, c.num_sms(), out_perm), GEMM_FP64, 64);
-		if (bn != 64) l = lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm, bn);
-		return upload_dot_plan(c, std::move(l), precision, bn);
+		if (bn == 0) return upload_dot_plan(c, std::move(l), GEMM_FP64, 64);
+		return upload_dot_plan(c, lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm, bn), precision, bn);
 	}
+	DotLowering l = lower_dot(s, axs, t, axt, nmult, z ? (int)GEMM_FP64 : precision, c.num_sms(), out_perm);
 	return upload_dot_plan(c, std::move(l), precision, 64);
 }
 
@@ -723,7 +725,7 @@ std::vector<TuneEntry> tile_tuning_entries()
 }
 
 static int tuned_tile_width(Ctx& c, const Meta& s, int axs, const Meta& t, int axt, int nmult, int precision,
-                            const int* out_perm, DotLowering& l64)
+                            const int* out_perm, const DotLowering& l64)
 {
 	static const int env_forced = [] {
 		const char* e = getenv("CTGPU_TC_BN");
@@ -749,7 +751,7 @@ static int tuned_tile_width(Ctx& c, const Meta& s, int axs, const Meta& t, int a
 	double best = 1e300;
 	for (int i = 0; i < 3; i++)
 	{
-		DotLowering l = i == 0 ? l64 : lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm, widths[i]);
+		DotLowering l = lower_dot(s, axs, t, axt, nmult, precision, c.num_sms(), out_perm, widths[i]);
 		e.ms[i] = time_tc_variant(c, std::move(l), precision, widths[i], s, t);
 		if (e.ms[i] < best)
 		{
